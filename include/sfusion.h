@@ -1,0 +1,279 @@
+/*
+ * sfusion.h — C ABI of the GB300 (sm_103a) dense tracking-and-fusion loop.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers / POD structs and
+ * returns an int status (SF_OK == 0).  Device buffers are raw CUDA device
+ * pointers; images are (data, step in bytes, cols, rows) like the reference's
+ * pitched DeviceArray2D / PtrStepSz.  No torch or C++ types cross this line.
+ *
+ * Reference interfaces replaced (paths inside YuhangMing/semantic_icpSLAM):
+ *   Tracking/Reduction.h    FilterDepth :18, ComputeVMap :22, ComputeNMap :26,
+ *                           PyrDownGauss(float) :29, ResizeMap :40, ICPStep :74
+ *   Mapping/RenderScene.h   ResetMap :3, Raycast :13, CreateRenderingBlocks :20,
+ *                           CheckBlockVisibility :40, FuseMapColor :45,
+ *                           AnalyzeMapSemantics :57
+ *   Tracking/Tracking.cc    Tracker::ComputeSE3 :369-517 (whole ICP loop)
+ *   Core/System.cc          System::GrabImage :131-270 (per-frame order)
+ * Error convention: the reference prints and exit(0)s on a CUDA error
+ * (Utility/SafeCall.h:13-16); here every call returns a status instead.
+ */
+#ifndef SFUSION_H_
+#define SFUSION_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum {
+  SF_OK = 0,
+  SF_ERR_INVALID = 1,   /* bad argument / size / config                   */
+  SF_ERR_CUDA = 2,      /* a CUDA runtime call failed                      */
+  SF_ERR_OVERFLOW = 3,  /* a fixed-capacity list overflowed (counted)      */
+  SF_ERR_TIMEOUT = 4,   /* a bounded device wait gave up                   */
+  SF_ERR_NO_DEVICE = 5, /* no CUDA device                                  */
+  SF_ERR_STATE = 6      /* call not valid in the object's current state    */
+};
+
+/* ----------------------------------------------------------- POD layouts */
+/* Matrix3f: three float3 rows, row-major (Utility/VectorMath.h:360-375). */
+typedef struct { float x, y, z; } sf_float3;
+typedef struct { sf_float3 rowx, rowy, rowz; } sf_mat3;
+/* Intrinsics (Utility/Intrinsics.h:4-18); level l uses fx/2^l etc. */
+typedef struct { float fx, fy, cx, cy; } sf_intrinsics;
+/* Pitched 2-D image view (Utility/DeviceArray.h:31-42 PtrStepSz). */
+typedef struct { void *data; size_t step; int cols, rows; } sf_image;
+
+/* HashEntry, 32 bytes (Mapping/DeviceMap.h:20-60): int3 pos, int ptr
+ * (voxel index = heap block * 512; -1 = free), int offset (1-based excess
+ * link; 0 = end of chain), 12 bytes padding from __align__(16). */
+typedef struct { int x, y, z, ptr, offset, pad_[3]; } sf_hash_entry;
+/* Voxel, 16 bytes (Mapping/DeviceMap.h:63-123). */
+typedef struct {
+  float sdf;
+  uint8_t weight;
+  uint8_t color[3];
+  uint8_t label, count, label_2, count_2;
+  uint8_t color_2[3];
+  uint8_t obj_idx;
+} sf_voxel;
+/* RenderingBlock, 16 bytes (Mapping/DeviceMap.h:11-18). */
+typedef struct { int16_t ulx, uly, lrx, lry; float zmin, zmax; } sf_rendering_block;
+
+/* Runtime replacement of DeviceMap's static constexpr constants
+ * (Mapping/DeviceMap.h:166-189).  Derived constants are computed exactly
+ * as the reference's constexpr expressions are. */
+typedef struct {
+  float voxel_size;          /* VoxelSize (m)                           */
+  float trunc_dist;          /* TruncateDist (m)                        */
+  float depth_min;           /* DepthMin (m)                            */
+  float depth_max;           /* DepthMax (m)                            */
+  uint32_t num_buckets;      /* NumBuckets                              */
+  uint32_t num_excess;       /* NumExcess                               */
+  uint32_t num_sdf_blocks;   /* NumSdfBlocks (heap capacity)            */
+  uint32_t max_rendering_blocks; /* MaxRenderingBlocks                 */
+} sf_map_config;
+
+/* DeviceMap's arrays (Mapping/DeviceMap.h:191-198) as raw device pointers. */
+typedef struct {
+  int *heap_mem;               /* [num_sdf_blocks]                      */
+  int *entry_ptr;              /* [1] next excess slot, starts at 1     */
+  int *heap_counter;           /* [1] top of the free-block stack       */
+  int *bucket_mutex;           /* [num_buckets]                         */
+  sf_voxel *voxel_blocks;      /* [num_sdf_blocks * 512]                */
+  uint32_t *no_visible_blocks; /* [1]                                   */
+  sf_hash_entry *hash_entries; /* [num_buckets + num_excess]            */
+  sf_hash_entry *visible_entries; /* [num_buckets + num_excess]         */
+} sf_device_map;
+
+typedef struct sf_context sf_context; /* stream + per-call scratch       */
+typedef struct sf_map sf_map;         /* voxel-block hash map            */
+typedef struct sf_system sf_system;   /* whole per-frame loop            */
+
+/* ------------------------------------------------------------- context */
+/* A context owns one non-default CUDA stream on the current device and
+ * the scratch every launcher below needs.  Not thread-safe; one per host
+ * thread.  (Reference: default stream + caller-owned DeviceArrays.) */
+int sf_context_create(sf_context **out);
+int sf_context_destroy(sf_context *ctx);
+int sf_context_stream(sf_context *ctx, void **stream_out);
+int sf_context_sync(sf_context *ctx);
+/* Last device-side overflow / error flags recorded by the context. */
+int sf_context_flags(sf_context *ctx, uint32_t *flags_out);
+/* Copies `bytes` between any two host/device pointers (unified addressing)
+ * on the context stream and waits for it. */
+int sf_memcpy(sf_context *ctx, void *dst, const void *src, size_t bytes);
+
+/* ----------------------------------------------------------------- map */
+/* Mapping::Create (Mapping/Mapping.cc:11-51): allocates every map array. */
+int sf_map_create(const sf_map_config *cfg, sf_map **out);
+/* Wraps caller-owned arrays (a reference Mapping's DeviceArrays). */
+int sf_map_wrap(const sf_map_config *cfg, const sf_device_map *arrays, sf_map **out);
+int sf_map_destroy(sf_map *map);
+int sf_map_arrays(const sf_map *map, sf_device_map *out);
+/* Rebuilds the allocated-entry index after the hash table was written
+ * outside this library (e.g. a map loaded from disk). */
+int sf_map_rebuild_index(sf_context *ctx, sf_map *map);
+/* Host copies of the map's counters: heapCounter, entryPtr, visible count,
+ * allocated (ptr >= 0) entry count. */
+int sf_map_counters(sf_context *ctx, const sf_map *map, int out[4]);
+
+/* ResetMap (Mapping/RenderScene.h:3; FuseMap.cu:1251-1304). */
+int sf_ResetMap(sf_context *ctx, sf_map *map);
+
+/* ------------------------------------------------------------- pyramid */
+/* FilterDepth (Tracking/Reduction.h:18; Pyrdown.cu:72-121).
+ * depth: uint16; raw, filtered: float. */
+int sf_FilterDepth(sf_context *ctx, sf_image depth, sf_image raw_depth,
+                   sf_image filtered_depth, float depth_scale, float depth_cutoff);
+/* ComputeVMap (Reduction.h:22; Pyrdown.cu:123-158). vmap: float4. */
+int sf_ComputeVMap(sf_context *ctx, sf_image depth, sf_image vmap, float fx,
+                   float fy, float cx, float cy, float depth_cutoff);
+/* ComputeNMap (Reduction.h:26; Pyrdown.cu:160-192). */
+int sf_ComputeNMap(sf_context *ctx, sf_image vmap, sf_image nmap);
+/* PyrDownGauss, float overload (Reduction.h:29; Pyrdown.cu:201-236). */
+int sf_PyrDownGauss(sf_context *ctx, sf_image src, sf_image dst);
+/* ResizeMap (Reduction.h:40; Pyrdown.cu:318-358). */
+int sf_ResizeMap(sf_context *ctx, sf_image vsrc, sf_image nsrc, sf_image vdst,
+                 sf_image ndst);
+/* Frame::FillImages depth part (Core/Frame.cc:68-92) fused: raw + filtered
+ * depth, Gaussian levels, vertex and normal maps of `levels` levels.
+ * depth_levels/vmaps/nmaps: arrays of `levels` images. */
+int sf_BuildPyramid(sf_context *ctx, sf_image depth_u16, sf_image raw_depth,
+                    const sf_image *depth_levels, const sf_image *vmaps,
+                    const sf_image *nmaps, int levels, sf_intrinsics K0,
+                    float depth_scale, float depth_cutoff);
+
+/* ----------------------------------------------------------------- ICP */
+/* ICPStep (Tracking/Reduction.h:74; Reduction.cu:213-385): one projective
+ * point-to-plane step.  Writes residual[2] = {sum r^2, count},
+ * matrixA[36] (row-major symmetric) and vectorB[6] to HOST memory.
+ * Per-pixel terms FP32; block partials Kahan-compensated FP32; the
+ * cross-block sum FP64. */
+int sf_ICPStep(sf_context *ctx, sf_image next_vmap, sf_image last_vmap,
+               sf_image next_nmap, sf_image last_nmap, sf_mat3 Rcurr,
+               sf_float3 tcurr, sf_mat3 Rlast, sf_mat3 RlastInv,
+               sf_float3 tlast, sf_intrinsics K, float residual[2],
+               double matrixA[36], double vectorB[6]);
+
+/* Tracker::ComputeSE3(icpOnly = true, iter, thresh) (Tracking/Tracking.cc
+ * :369-517) as ONE persistent cooperative launch: every level (coarse to
+ * fine) and iteration, the divergence guard, the FP64 6x6 LDLT solve and
+ * SE(3) update, and the acceptance gate, with no host round trip.
+ * next_* / last_*: `levels` images each (level 0 first), float4.
+ * last_pose: host double[16] (camera->world).  next_pose_out: host
+ * double[16], rolled back to last_pose on failure as the reference does.
+ * stats_out (may be NULL): {accepted, fail (0/1 count-NaN/2 diverged),
+ * iterations, icp_count}; icp_error_out (may be NULL). */
+int sf_ComputeSE3(sf_context *ctx, int levels, const sf_image *next_vmaps,
+                  const sf_image *next_nmaps, const sf_image *last_vmaps,
+                  const sf_image *last_nmaps, sf_intrinsics K0, const int *iters,
+                  const int *min_count, float thresh, const double last_pose[16],
+                  double next_pose_out[16], int stats_out[4], float *icp_error_out);
+
+/* --------------------------------------------------------------- fusion */
+/* CheckBlockVisibility (RenderScene.h:40; FuseMap.cu:991-1037). */
+int sf_CheckBlockVisibility(sf_context *ctx, sf_map *map, sf_mat3 Rview,
+                            sf_mat3 RviewInv, sf_float3 tview, int cols,
+                            int rows, float fx, float fy, float cx, float cy,
+                            float depth_max, float depth_min,
+                            uint32_t *host_data);
+/* FuseMapColor (RenderScene.h:45; FuseMap.cu:1039-1162): allocate blocks
+ * along each raw-depth ray, compact the visible blocks, integrate
+ * TSDF/weight/colour and, when num_detection > 0, fuse labels from `mask`.
+ * depth: float (raw metres), color: uchar3, nmap: float4, mask: uint8. */
+int sf_FuseMapColor(sf_context *ctx, sf_map *map, sf_image depth,
+                    sf_image color, sf_image nmap, sf_image mask,
+                    int num_detection, sf_mat3 Rview, sf_mat3 RviewInv,
+                    sf_float3 tview, float fx, float fy, float cx, float cy,
+                    float depth_max, float depth_min, uint32_t *host_data);
+/* AnalyzeMapSemantics (RenderScene.h:57; FuseMap.cu:1164-1247), without
+ * the racy UnifyNeighbor pass. */
+int sf_AnalyzeMapSemantics(sf_context *ctx, sf_map *map, sf_image depth,
+                           sf_image color, sf_image nmap, sf_image mask,
+                           int num_detection, sf_mat3 Rview, sf_mat3 RviewInv,
+                           sf_float3 tview, float fx, float fy, float cx,
+                           float cy, float depth_max, float depth_min);
+
+/* -------------------------------------------------------------- raycast */
+/* CreateRenderingBlocks (RenderScene.h:20; RenderScene.cu:210-289).
+ * zrange_min/zrange_max: float images (cols/8 x rows/8 in the reference),
+ * rendering_blocks: device array of max_rendering_blocks entries,
+ * no_rendering_blocks: device uint32[1].  *ok_out = reference's bool. */
+int sf_CreateRenderingBlocks(sf_context *ctx, sf_map *map, sf_image zrange_min,
+                             sf_image zrange_max, float depth_max,
+                             float depth_min, sf_rendering_block *rendering_blocks,
+                             uint32_t *no_rendering_blocks, sf_mat3 RviewInv,
+                             sf_float3 tview, uint32_t no_visible_blocks,
+                             float fx, float fy, float cx, float cy, int *ok_out);
+/* Raycast (RenderScene.h:13; RenderScene.cu:291-537). */
+int sf_Raycast(sf_context *ctx, sf_map *map, sf_image vmap, sf_image nmap,
+               sf_image zrange_min, sf_image zrange_max, sf_mat3 Rview,
+               sf_mat3 RviewInv, sf_float3 tview, float invfx, float invfy,
+               float cx, float cy);
+
+/* ------------------------------------------------------- whole frame loop */
+/* System::GrabImage (Core/System.cc:131-270) with Tracker::GrabFrame /
+ * Track / ComputeSE3(icpOnly) (Tracking/Tracking.cc:65-173,246-280,369-517),
+ * Mapping::FuseColor and Mapping::RayTrace (Mapping/Mapping.cc:76-161).
+ * Keyframes, SURF matching, relocalisation by features and the viewer are
+ * not part of this loop. */
+typedef struct {
+  sf_map_config map;
+  int cols, rows;          /* level-0 image size                          */
+  int levels;              /* pyramid levels (<= 4; reference: 3)          */
+  sf_intrinsics K;         /* level-0 intrinsics                           */
+  float depth_scale;       /* raw depth units per metre                   */
+  float depth_cutoff;      /* Frame::mDepthCutoff                          */
+  int iters[4];            /* ICP iterations per level (level 0 first)     */
+  int min_count[4];        /* MIN_ICP_COUNT per level                      */
+  float icp_thresh;        /* THRESH_ICP_SE3                               */
+  int zrange_cols;         /* z-range image (0: ceil(cols / 8))            */
+  int zrange_rows;         /* z-range image (0: ceil(rows / 8))            */
+  int use_graph;           /* 1: one CUDA graph per frame; 0: per launch  */
+} sf_system_config;
+
+typedef struct {
+  int tracked;             /* Track() result for this frame                */
+  int accepted;            /* ComputeSE3 acceptance (1 on the first frame) */
+  int fail;                /* 0 ok, 1 ICP count/NaN failure, 2 diverged    */
+  int iterations;          /* ICP iterations run                           */
+  float icp_error;         /* sqrt(sum r^2) / count of the last iteration  */
+  int icp_count;
+  uint32_t visible;        /* visible blocks                               */
+  int heap_counter;        /* DeviceMap heapCounter                        */
+  int entry_ptr;           /* DeviceMap entryPtr                           */
+  int allocated;           /* entries with ptr >= 0                        */
+  uint32_t flags;          /* SF_FLAG_* overflow / timeout bits            */
+  double pose[16];         /* camera->world pose after this frame          */
+} sf_frame_stats;
+
+int sf_system_create(sf_context *ctx, const sf_system_config *cfg,
+                     const double init_pose[16], sf_system **out);
+int sf_system_destroy(sf_system *sys);
+/* One frame from HOST buffers: depth uint16[rows*cols], rgb uint8[rows*cols*3],
+ * mask uint8[rows*cols] (may be NULL).  Copies in, runs the frame, copies
+ * the stats (pose included) out; returns when the frame is done. */
+int sf_system_grab(sf_system *sys, const uint16_t *depth, const uint8_t *rgb,
+                   const uint8_t *mask, int num_detection, sf_frame_stats *stats);
+/* One frame from DEVICE buffers (already resident); asynchronous on the
+ * context stream.  Read results with sf_system_stats. */
+int sf_system_grab_device(sf_system *sys, const uint16_t *depth, const uint8_t *rgb,
+                          const uint8_t *mask, int num_detection);
+int sf_system_stats(sf_system *sys, sf_frame_stats *stats);
+/* Device views of the model maps (the last frame's raycast prediction,
+ * level l) and of the current frame's measured maps. */
+int sf_system_model_maps(sf_system *sys, int level, sf_image *vmap, sf_image *nmap);
+int sf_system_frame_maps(sf_system *sys, int level, sf_image *vmap, sf_image *nmap,
+                         sf_image *depth);
+int sf_system_get_map(sf_system *sys, sf_map **map);
+/* Device pointers to the pose state: last (tracked) pose, double[16]. */
+int sf_system_pose_device(sf_system *sys, double **last_pose);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SFUSION_H_ */

@@ -1,0 +1,376 @@
+"""ctypes front end of the oracle (test infrastructure only).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module; the product never does.  Arrays are numpy, C-contiguous.
+"""
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+_lock = threading.Lock()
+
+F32P = C.POINTER(C.c_float)
+F64P = C.POINTER(C.c_double)
+U16P = C.POINTER(C.c_uint16)
+U8P = C.POINTER(C.c_uint8)
+I32P = C.POINTER(C.c_int)
+
+ENTRY_DTYPE = np.dtype([("x", "<i4"), ("y", "<i4"), ("z", "<i4"), ("ptr", "<i4"),
+                        ("offset", "<i4"), ("pad", "<i4", 3)])
+VOXEL_DTYPE = np.dtype([("sdf", "<f4"), ("weight", "u1"), ("color", "u1", 3),
+                        ("label", "u1"), ("count", "u1"), ("label_2", "u1"),
+                        ("count_2", "u1"), ("color_2", "u1", 3), ("obj_idx", "u1")])
+RBLOCK_DTYPE = np.dtype([("ulx", "<i2"), ("uly", "<i2"), ("lrx", "<i2"), ("lry", "<i2"),
+                         ("zmin", "<f4"), ("zmax", "<f4")])
+assert ENTRY_DTYPE.itemsize == 32 and VOXEL_DTYPE.itemsize == 16 and RBLOCK_DTYPE.itemsize == 16
+
+
+class Config(C.Structure):
+    _fields_ = [("voxel_size", C.c_float), ("trunc_dist", C.c_float),
+                ("depth_min", C.c_float), ("depth_max", C.c_float),
+                ("num_buckets", C.c_uint32), ("num_excess", C.c_uint32),
+                ("num_sdf_blocks", C.c_uint32), ("max_rendering_blocks", C.c_uint32)]
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            path = _build.build()
+            L = C.CDLL(path)
+            vp = C.c_void_p
+            sig = {
+                "sfo_filter_depth": (None, [U16P, C.c_int, C.c_int, C.c_float, C.c_float, F32P, F32P]),
+                "sfo_pyrdown": (None, [F32P, C.c_int, C.c_int, F32P, C.c_int, C.c_int]),
+                "sfo_vmap": (None, [F32P, C.c_int, C.c_int] + [C.c_float] * 5 + [F32P]),
+                "sfo_nmap": (None, [F32P, C.c_int, C.c_int, F32P]),
+                "sfo_resize": (None, [F32P, F32P, C.c_int, C.c_int, F32P, F32P, C.c_int, C.c_int]),
+                "sfo_icp_sums": (None, [F32P] * 4 + [C.c_int, C.c_int] + [F32P] * 5 + [C.c_float] * 4 + [C.c_int, F64P]),
+                "sfo_icp_rows": (None, [F32P] * 4 + [C.c_int, C.c_int] + [F32P] * 5 + [C.c_float] * 4 + [F32P]),
+                "sfo_create_matrix": (None, [F64P, F64P, F64P]),
+                "sfo_ldlt_solve6": (None, [F64P, F64P, F64P]),
+                "sfo_se3_exp": (None, [F64P, F64P]),
+                "sfo_compute_se3": (C.c_int, [C.c_int, I32P, I32P, vp, vp, vp, vp, F32P, I32P, I32P,
+                                              C.c_float, F64P, F64P, C.c_int, F64P]),
+                "sfo_map_create": (vp, [C.POINTER(Config)]),
+                "sfo_map_destroy": (None, [vp]),
+                "sfo_map_reset": (None, [vp]),
+                "sfo_map_entries": (vp, [vp]),
+                "sfo_map_voxels": (vp, [vp]),
+                "sfo_map_visible": (vp, [vp]),
+                "sfo_map_heap": (vp, [vp]),
+                "sfo_map_counters": (None, [vp, I32P]),
+                "sfo_alloc": (None, [vp, F32P, C.c_int, C.c_int, F32P, F32P] + [C.c_float] * 4),
+                "sfo_visibility": (C.c_uint, [vp, F32P, F32P, F32P, C.c_int, C.c_int] + [C.c_float] * 6),
+                "sfo_integrate": (None, [vp, F32P, U8P, C.c_int, C.c_int, F32P, F32P] + [C.c_float] * 6),
+                "sfo_semantics": (None, [vp, F32P, U8P, F32P, U8P, C.c_int, C.c_int, C.c_int, F32P, F32P] + [C.c_float] * 6),
+                "sfo_fuse": (C.c_uint, [vp, F32P, U8P, F32P, U8P, C.c_int, C.c_int, C.c_int, F32P, F32P, F32P] + [C.c_float] * 4),
+                "sfo_zrange": (C.c_int, [vp, F32P, F32P, C.c_int, C.c_int, C.c_float, C.c_float, F32P, F32P]
+                               + [C.c_float] * 4 + [vp, C.c_int, C.POINTER(C.c_uint)]),
+                "sfo_raycast": (None, [vp, F32P, F32P, C.c_int, C.c_int, F32P, F32P, C.c_int, C.c_int,
+                                       F32P, F32P, F32P] + [C.c_float] * 4),
+                "sfo_system_create": (vp, [C.POINTER(Config), C.c_int, C.c_int, C.c_int, F32P, C.c_float,
+                                           C.c_float, I32P, I32P, C.c_float, F64P]),
+                "sfo_system_destroy": (None, [vp]),
+                "sfo_system_grab": (C.c_int, [vp, U16P, U8P, U8P, C.c_int, F64P, F64P]),
+                "sfo_system_map": (vp, [vp]),
+                "sfo_system_vmap": (vp, [vp, C.c_int]),
+                "sfo_system_nmap": (vp, [vp, C.c_int]),
+            }
+            for name, (res, args) in sig.items():
+                f = getattr(L, name)
+                f.restype = res
+                f.argtypes = args
+            _lib = L
+    return _lib
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def filter_depth(depth_u16, depth_scale, cutoff):
+    d = np.ascontiguousarray(depth_u16, dtype=np.uint16)
+    rows, cols = d.shape
+    raw = np.empty((rows, cols), np.float32)
+    filt = np.empty((rows, cols), np.float32)
+    lib().sfo_filter_depth(_p(d, U16P), cols, rows, depth_scale, cutoff, _p(raw, F32P), _p(filt, F32P))
+    return raw, filt
+
+
+def pyrdown(src):
+    src = _f32(src)
+    sr, sc = src.shape
+    dst = np.empty((sr // 2, sc // 2), np.float32)
+    lib().sfo_pyrdown(_p(src, F32P), sc, sr, _p(dst, F32P), sc // 2, sr // 2)
+    return dst
+
+
+def vmap(depth, fx, fy, cx, cy, cutoff):
+    depth = _f32(depth)
+    rows, cols = depth.shape
+    out = np.empty((rows, cols, 4), np.float32)
+    lib().sfo_vmap(_p(depth, F32P), cols, rows, fx, fy, cx, cy, cutoff, _p(out, F32P))
+    return out
+
+
+def nmap(vm):
+    vm = _f32(vm)
+    rows, cols = vm.shape[:2]
+    out = np.empty((rows, cols, 4), np.float32)
+    lib().sfo_nmap(_p(vm, F32P), cols, rows, _p(out, F32P))
+    return out
+
+
+def resize(vsrc, nsrc):
+    vsrc, nsrc = _f32(vsrc), _f32(nsrc)
+    sr, sc = vsrc.shape[:2]
+    vd = np.empty((sr // 2, sc // 2, 4), np.float32)
+    nd = np.empty((sr // 2, sc // 2, 4), np.float32)
+    lib().sfo_resize(_p(vsrc, F32P), _p(nsrc, F32P), sc, sr, _p(vd, F32P), _p(nd, F32P), sc // 2, sr // 2)
+    return vd, nd
+
+
+def pose_to_gpu(P):
+    """Frame::GpuRotation / GpuInvRotation / GpuTranslation (Frame.cc:626-645)."""
+    P = np.asarray(P, np.float64)
+    R = P[:3, :3].astype(np.float32)
+    Rinv = P[:3, :3].T.astype(np.float32)
+    t = P[:3, 3].astype(np.float32)
+    return np.ascontiguousarray(R), np.ascontiguousarray(Rinv), np.ascontiguousarray(t)
+
+
+def icp_sums(vcurr, vlast, ncurr, nlast, Pcurr, Plast, K, fp64=False):
+    vcurr, vlast, ncurr, nlast = map(_f32, (vcurr, vlast, ncurr, nlast))
+    rows, cols = vcurr.shape[:2]
+    Rc, _, tc = pose_to_gpu(Pcurr)
+    Rl, RlI, tl = pose_to_gpu(Plast)
+    out = np.zeros(29, np.float64)
+    lib().sfo_icp_sums(_p(vcurr, F32P), _p(vlast, F32P), _p(ncurr, F32P), _p(nlast, F32P), cols, rows,
+                       _p(Rc, F32P), _p(tc, F32P), _p(Rl, F32P), _p(RlI, F32P), _p(tl, F32P),
+                       *map(float, K), int(fp64), _p(out, F64P))
+    return out
+
+
+def icp_rows(vcurr, vlast, ncurr, nlast, Pcurr, Plast, K):
+    vcurr, vlast, ncurr, nlast = map(_f32, (vcurr, vlast, ncurr, nlast))
+    rows, cols = vcurr.shape[:2]
+    Rc, _, tc = pose_to_gpu(Pcurr)
+    Rl, RlI, tl = pose_to_gpu(Plast)
+    out = np.zeros((rows * cols, 29), np.float32)
+    lib().sfo_icp_rows(_p(vcurr, F32P), _p(vlast, F32P), _p(ncurr, F32P), _p(nlast, F32P), cols, rows,
+                       _p(Rc, F32P), _p(tc, F32P), _p(Rl, F32P), _p(RlI, F32P), _p(tl, F32P),
+                       *map(float, K), _p(out, F32P))
+    return out
+
+
+def create_matrix(s29):
+    s = np.ascontiguousarray(s29, np.float64)
+    A = np.zeros(36, np.float64)
+    b = np.zeros(6, np.float64)
+    lib().sfo_create_matrix(_p(s, F64P), _p(A, F64P), _p(b, F64P))
+    return A.reshape(6, 6), b
+
+
+def ldlt_solve6(A, b):
+    A = np.ascontiguousarray(A, np.float64).reshape(36)
+    b = np.ascontiguousarray(b, np.float64)
+    x = np.zeros(6, np.float64)
+    lib().sfo_ldlt_solve6(_p(A, F64P), _p(b, F64P), _p(x, F64P))
+    return x
+
+
+def se3_exp(xi):
+    xi = np.ascontiguousarray(xi, np.float64)
+    T = np.zeros(16, np.float64)
+    lib().sfo_se3_exp(_p(xi, F64P), _p(T, F64P))
+    return T.reshape(4, 4)
+
+
+def compute_se3(vnext, nnext, vlast, nlast, K, iters, min_count, thresh, last_pose, next_pose,
+                fp64=False):
+    L = len(vnext)
+    keep = [_f32(a) for a in list(vnext) + list(nnext) + list(vlast) + list(nlast)]
+    ptrs = [a.ctypes.data for a in keep]
+    arr = lambda k: (C.c_void_p * L)(*ptrs[k * L:(k + 1) * L])
+    cols = (C.c_int * L)(*[a.shape[1] for a in keep[:L]])
+    rows = (C.c_int * L)(*[a.shape[0] for a in keep[:L]])
+    Kf = np.asarray(K, np.float32)
+    it = np.asarray(iters, np.int32)
+    mc = np.asarray(min_count, np.int32)
+    lp = np.ascontiguousarray(last_pose, np.float64)
+    npose = np.ascontiguousarray(next_pose, np.float64).copy()
+    stats = np.zeros(4, np.float64)
+    ok = lib().sfo_compute_se3(L, cols, rows, arr(0), arr(1), arr(2), arr(3), _p(Kf, F32P), _p(it, I32P),
+                               _p(mc, I32P), thresh, _p(lp, F64P), _p(npose, F64P), int(fp64), _p(stats, F64P))
+    return bool(ok), npose, stats
+
+
+def _view(ptr, dtype, n):
+    buf = (C.c_char * (n * dtype.itemsize)).from_address(ptr)
+    return np.frombuffer(buf, dtype=dtype, count=n)
+
+
+class Map:
+    """Oracle voxel-block hash map (Mapping::Create, Mapping.cc:11-51)."""
+
+    def __init__(self, voxel_size, trunc_dist, num_buckets, num_excess, num_sdf_blocks,
+                 depth_min=0.1, depth_max=3.0, max_rendering_blocks=260000):
+        self.cfg = Config(voxel_size, trunc_dist, depth_min, depth_max, num_buckets, num_excess,
+                          num_sdf_blocks, max_rendering_blocks)
+        self.h = lib().sfo_map_create(C.byref(self.cfg))
+        self.num_entries = num_buckets + num_excess
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().sfo_map_destroy(self.h)
+            self.h = None
+
+    def reset(self):
+        lib().sfo_map_reset(self.h)
+
+    @property
+    def entries(self):
+        return _view(lib().sfo_map_entries(self.h), ENTRY_DTYPE, self.num_entries)
+
+    @property
+    def voxels(self):
+        return _view(lib().sfo_map_voxels(self.h), VOXEL_DTYPE, self.cfg.num_sdf_blocks * 512)
+
+    @property
+    def visible(self):
+        return _view(lib().sfo_map_visible(self.h), ENTRY_DTYPE, self.num_entries)
+
+    @property
+    def heap(self):
+        return _view(lib().sfo_map_heap(self.h), np.dtype("<i4"), self.cfg.num_sdf_blocks)
+
+    def counters(self):
+        out = np.zeros(4, np.int32)
+        lib().sfo_map_counters(self.h, _p(out, I32P))
+        return out
+
+    def alloc(self, depth, P, K):
+        depth = _f32(depth)
+        rows, cols = depth.shape
+        R, _, t = pose_to_gpu(P)
+        lib().sfo_alloc(self.h, _p(depth, F32P), cols, rows, _p(R, F32P), _p(t, F32P), *map(float, K))
+
+    def visibility(self, P, K, cols, rows, depth_max=None, depth_min=None):
+        R, RI, t = pose_to_gpu(P)
+        dmax = self.cfg.depth_max if depth_max is None else depth_max
+        dmin = self.cfg.depth_min if depth_min is None else depth_min
+        return lib().sfo_visibility(self.h, _p(R, F32P), _p(RI, F32P), _p(t, F32P), cols, rows,
+                                    *map(float, K), dmax, dmin)
+
+    def integrate(self, depth, rgb, P, K):
+        depth = _f32(depth)
+        rgb = np.ascontiguousarray(rgb, np.uint8)
+        rows, cols = depth.shape
+        _, RI, t = pose_to_gpu(P)
+        lib().sfo_integrate(self.h, _p(depth, F32P), _p(rgb, U8P), cols, rows, _p(RI, F32P), _p(t, F32P),
+                            *map(float, K), self.cfg.depth_max, self.cfg.depth_min)
+
+    def semantics(self, depth, rgb, nmap_, mask, num_detection, P, K):
+        depth, nmap_ = _f32(depth), _f32(nmap_)
+        rgb = np.ascontiguousarray(rgb, np.uint8)
+        mask = np.ascontiguousarray(mask, np.uint8)
+        rows, cols = depth.shape
+        _, RI, t = pose_to_gpu(P)
+        lib().sfo_semantics(self.h, _p(depth, F32P), _p(rgb, U8P), _p(nmap_, F32P), _p(mask, U8P),
+                            num_detection, cols, rows, _p(RI, F32P), _p(t, F32P), *map(float, K),
+                            self.cfg.depth_max, self.cfg.depth_min)
+
+    def fuse(self, depth, rgb, nmap_, mask, num_detection, P, K):
+        depth, nmap_ = _f32(depth), _f32(nmap_)
+        rgb = np.ascontiguousarray(rgb, np.uint8)
+        rows, cols = depth.shape
+        mask = np.zeros((rows, cols), np.uint8) if mask is None else np.ascontiguousarray(mask, np.uint8)
+        R, RI, t = pose_to_gpu(P)
+        return lib().sfo_fuse(self.h, _p(depth, F32P), _p(rgb, U8P), _p(nmap_, F32P), _p(mask, U8P),
+                              num_detection, cols, rows, _p(R, F32P), _p(RI, F32P), _p(t, F32P),
+                              *map(float, K))
+
+    def zrange(self, P, K, zc, zr, max_blocks=0):
+        _, RI, t = pose_to_gpu(P)
+        zmin = np.zeros((zr, zc), np.float32)
+        zmax = np.zeros((zr, zc), np.float32)
+        blocks = np.zeros(max(max_blocks, 1), RBLOCK_DTYPE)
+        n = C.c_uint(0)
+        ok = lib().sfo_zrange(self.h, _p(zmin, F32P), _p(zmax, F32P), zc, zr, self.cfg.depth_max,
+                              self.cfg.depth_min, _p(RI, F32P), _p(t, F32P), *map(float, K),
+                              blocks.ctypes.data_as(C.c_void_p), max_blocks, C.byref(n))
+        return bool(ok), zmin, zmax, blocks[:min(n.value, max_blocks)], n.value
+
+    def raycast(self, P, K, cols, rows, zmin, zmax):
+        zmin, zmax = _f32(zmin), _f32(zmax)
+        zr, zc = zmin.shape
+        R, RI, t = pose_to_gpu(P)
+        vm = np.empty((rows, cols, 4), np.float32)
+        nm = np.empty((rows, cols, 4), np.float32)
+        fx, fy, cx, cy = map(float, K)
+        invfx = np.float32(1.0 / np.float64(np.float32(fx)))
+        invfy = np.float32(1.0 / np.float64(np.float32(fy)))
+        lib().sfo_raycast(self.h, _p(vm, F32P), _p(nm, F32P), cols, rows, _p(zmin, F32P), _p(zmax, F32P),
+                          zc, zr, _p(R, F32P), _p(RI, F32P), _p(t, F32P), float(invfx), float(invfy), cx, cy)
+        return vm, nm
+
+
+class System:
+    """Oracle of the whole per-frame loop (System::GrabImage, System.cc:131-270)."""
+
+    def __init__(self, map_kw, cols, rows, K, levels=3, iters=(10, 5, 4), min_count=(2000, 1000, 100),
+                 depth_scale=1000.0, depth_cutoff=3.0, icp_thresh=1e-4, init_pose=None):
+        self.cfg = Config(map_kw["voxel_size"], map_kw["trunc_dist"], map_kw.get("depth_min", 0.1),
+                          map_kw.get("depth_max", 3.0), map_kw["num_buckets"], map_kw["num_excess"],
+                          map_kw["num_sdf_blocks"], map_kw.get("max_rendering_blocks", 260000))
+        Kf = np.asarray(K, np.float32)
+        it = np.asarray(iters, np.int32)
+        mc = np.asarray(min_count, np.int32)
+        ip = np.eye(4) if init_pose is None else np.ascontiguousarray(init_pose, np.float64)
+        ip = np.ascontiguousarray(ip, np.float64)
+        self.cols, self.rows, self.levels = cols, rows, levels
+        self.h = lib().sfo_system_create(C.byref(self.cfg), cols, rows, levels, _p(Kf, F32P), depth_scale,
+                                         depth_cutoff, _p(it, I32P), _p(mc, I32P), icp_thresh, _p(ip, F64P))
+        self.num_entries = self.cfg.num_buckets + self.cfg.num_excess
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().sfo_system_destroy(self.h)
+            self.h = None
+
+    def grab(self, depth_u16, rgb, mask=None, num_detection=0):
+        d = np.ascontiguousarray(depth_u16, np.uint16)
+        rgb = np.ascontiguousarray(rgb, np.uint8)
+        m = np.zeros(d.shape, np.uint8) if mask is None else np.ascontiguousarray(mask, np.uint8)
+        pose = np.zeros(16, np.float64)
+        stats = np.zeros(8, np.float64)
+        ok = lib().sfo_system_grab(self.h, _p(d, U16P), _p(rgb, U8P), _p(m, U8P), num_detection,
+                                   _p(pose, F64P), _p(stats, F64P))
+        return bool(ok), pose.reshape(4, 4), stats
+
+    def entries(self):
+        return _view(lib().sfo_map_entries(lib().sfo_system_map(self.h)), ENTRY_DTYPE, self.num_entries).copy()
+
+    def voxels(self):
+        return _view(lib().sfo_map_voxels(lib().sfo_system_map(self.h)), VOXEL_DTYPE,
+                     self.cfg.num_sdf_blocks * 512).copy()
+
+    def vmap(self, level=0):
+        n = (self.cols >> level) * (self.rows >> level) * 4
+        return _view(lib().sfo_system_vmap(self.h, level), np.dtype("<f4"), n).reshape(
+            self.rows >> level, self.cols >> level, 4).copy()
+
+    def nmap(self, level=0):
+        n = (self.cols >> level) * (self.rows >> level) * 4
+        return _view(lib().sfo_system_nmap(self.h, level), np.dtype("<f4"), n).reshape(
+            self.rows >> level, self.cols >> level, 4).copy()

@@ -1,0 +1,1341 @@
+// ORACLE — test infrastructure only.  Only tests/, __graft_entry__.smoke() and
+// bench.py's CPU-baseline leg may load this library, and only as the checker
+// (or the timed CPU baseline); the product (semantic_icpslam_gb300/) never
+// links, loads or calls it.
+//
+// CPU restatement of the dense per-frame loop of YuhangMing/semantic_icpSLAM
+// (pyramid -> projective point-to-plane ICP -> voxel-hash allocation ->
+// visible-block compaction -> TSDF/weight/colour/label integration ->
+// block-skipping raycast).  Each function cites the reference file:line it
+// restates.  Build: g++ -O2 -ffp-contract=off (no FMA contraction), so every
+// float operation is one IEEE-754 rounding, as the reference's source states
+// it; values the reference promotes to double are computed in double.
+//
+// Parity pin: tests/golden/ holds outputs of the reference's own device code
+// (compiled for the CPU from the reference sources by oracle/ref_shim/) and
+// tests/test_oracle_golden.py checks this restatement against them.
+#include "sfo.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <limits>
+#include <vector>
+
+namespace {
+
+// ------------------------------------------------------------------ helpers
+struct f3 { float x, y, z; };
+struct f4 { float x, y, z, w; };
+struct i3 { int x, y, z; };
+struct m3 { f3 rx, ry, rz; };  // Matrix3f rows (Utility/VectorMath.h:360-375)
+
+const float kNaN = [] { uint32_t u = 0x7fffffffu; float f; memcpy(&f, &u, 4); return f; }();
+
+inline f3 mk3(float x, float y, float z) { return {x, y, z}; }
+inline f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline f3 operator-(f3 a) { return {-a.x, -a.y, -a.z}; }
+inline f3 operator*(f3 a, float b) { return {a.x * b, a.y * b, a.z * b}; }
+inline f3 operator*(float a, f3 b) { return {a * b.x, a * b.y, a * b.z}; }
+inline f3 operator/(f3 a, float b) { return {a.x / b, a.y / b, a.z / b}; }
+// float3 . float3, VectorMath.h:195-197 (left-to-right sum)
+inline float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline f3 cross(f3 a, f3 b) {  // VectorMath.h:312-316
+  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+inline float norm(f3 a) { return std::sqrt(dot(a, a)); }     // :324-326
+inline f3 normalised(f3 a) { return a / norm(a); }           // :340-342
+inline f3 mul(const m3 &m, f3 a) { return {dot(m.rx, a), dot(m.ry, a), dot(m.rz, a)}; }
+inline f3 xyz(f4 v) { return {v.x, v.y, v.z}; }
+
+// CUDA's cvt.rzi (the reference's (int) casts run on the GPU): NaN -> 0,
+// out-of-range saturates.  Used wherever the reference casts float -> int.
+inline int f2i(double v) {
+  if (std::isnan(v)) return 0;
+  if (v >= 2147483647.0) return 2147483647;
+  if (v <= -2147483648.0) return (-2147483647 - 1);
+  return (int)v;
+}
+// make_int3(float3) == floor, VectorMath.h:36-42.
+inline i3 floor3(f3 a) {
+  i3 b{f2i(a.x), f2i(a.y), f2i(a.z)};
+  b.x = (float)b.x > a.x ? b.x - 1 : b.x;
+  b.y = (float)b.y > a.y ? b.y - 1 : b.y;
+  b.z = (float)b.z > a.z ? b.z - 1 : b.z;
+  return b;
+}
+// make_uchar3(float3) (VectorMath.h:16-18): int cast then uchar narrowing.
+inline uint8_t f2u8(float v) { return (uint8_t)(uint32_t)f2i(v); }
+
+m3 m3_from(const float *R) { return {{R[0], R[1], R[2]}, {R[3], R[4], R[5]}, {R[6], R[7], R[8]}}; }
+f3 f3_from(const float *t) { return {t[0], t[1], t[2]}; }
+
+// __constant__ sigSpace / sigRange (Pyrdown.cu:3-4)
+const float kSigSpace = (float)(0.5 / (4 * 4));
+const float kSigRange = (float)(0.5 / (0.5 * 0.5));
+// gaussKernel (Pyrdown.cu:194-200)
+const float kGauss[25] = {1, 4, 6, 4, 1, 4, 16, 24, 16, 4, 6, 24, 36,
+                          24, 6, 4, 16, 24, 16, 4, 1, 4, 6, 4, 1};
+
+}  // namespace
+
+// =================================================================== pyramid
+// FilterDepthKernel, Tracking/Pyrdown.cu:72-108 (+ launcher :110-121 passes
+// depthScaleInv = 1.0 / depthScale as a float).
+extern "C" void sfo_filter_depth(const uint16_t *d, int cols, int rows,
+                                 float depth_scale, float cutoff, float *raw,
+                                 float *filtered) {
+  const float inv = (float)(1.0 / (double)depth_scale);
+#pragma omp parallel for schedule(static)
+  for (int y = 0; y < rows; ++y)
+    for (int x = 0; x < cols; ++x) {
+      float center = (float)d[y * cols + x] * inv;
+      raw[y * cols + x] = center < cutoff ? center : kNaN;
+      if (std::isnan(center)) { filtered[y * cols + x] = kNaN; continue; }
+      const int R = 2, D = R * 2 + 1;
+      int tx = std::min(x - D / 2 + D, cols - 1);
+      int ty = std::min(y - D / 2 + D, rows - 1);
+      float sum1 = 0, sum2 = 0;
+      for (int cy = std::max(y - D / 2, 0); cy < ty; ++cy)
+        for (int cx = std::max(x - D / 2, 0); cx < tx; ++cx) {
+          float val = (float)d[cy * cols + cx] * inv;
+          float space2 = (float)((x - cx) * (x - cx) + (y - cy) * (y - cy));
+          float color2 = (center - val) * (center - val);
+          float weight = std::exp(-(space2 * kSigSpace + color2 * kSigRange));
+          sum1 += val * weight;
+          sum2 += weight;
+        }
+      float fin = sum1 / sum2;
+      filtered[y * cols + x] = fin < cutoff ? fin : kNaN;
+    }
+}
+
+// PyrDownGaussKernel<float,float>, Pyrdown.cu:201-225 (note the reversed
+// kernel index (ty-cy-1)*5 + (tx-cx-1) and the exclusive window bound).
+extern "C" void sfo_pyrdown(const float *src, int sc, int sr, float *dst, int dc,
+                            int dr) {
+#pragma omp parallel for schedule(static)
+  for (int y = 0; y < dr; ++y)
+    for (int x = 0; x < dc; ++x) {
+      const int D = 5;
+      int tx = std::min(2 * x - D / 2 + D, sc - 1);
+      int ty = std::min(2 * y - D / 2 + D, sr - 1);
+      float sum = 0;
+      int count = 0;
+      for (int cy = std::max(0, 2 * y - D / 2); cy < ty; ++cy)
+        for (int cx = std::max(0, 2 * x - D / 2); cx < tx; ++cx) {
+          float v = src[cy * sc + cx];
+          if (!std::isnan(v)) {
+            float k = kGauss[(ty - cy - 1) * 5 + (tx - cx - 1)];
+            sum += v * k;
+            count = (int)((float)count + k);
+          }
+        }
+      dst[y * dc + x] = sum / (float)count;
+    }
+}
+
+// ComputeVMapKernel, Pyrdown.cu:123-145; launcher :147-158 passes 1.0/fx.
+// Invalid pixels are written as all-NaN (the reference sets only x = NaN
+// and leaves y, w unset; every consumer tests x only).
+extern "C" void sfo_vmap(const float *depth, int cols, int rows, float fx,
+                         float fy, float cx, float cy, float cutoff, float *vmap) {
+  const float invfx = (float)(1.0 / (double)fx), invfy = (float)(1.0 / (double)fy);
+#pragma omp parallel for schedule(static)
+  for (int y = 0; y < rows; ++y)
+    for (int x = 0; x < cols; ++x) {
+      float z = depth[y * cols + x];
+      float *v = vmap + 4 * (y * cols + x);
+      if (!std::isnan(z) && (double)z > 0.1 && z < cutoff) {
+        v[0] = z * ((float)x - cx) * invfx;
+        v[1] = z * ((float)y - cy) * invfy;
+        v[2] = z;
+        v[3] = 1.0f;
+      } else {
+        v[0] = v[1] = v[2] = v[3] = kNaN;
+      }
+    }
+}
+
+// ComputeNMapKernel, Pyrdown.cu:160-181.
+extern "C" void sfo_nmap(const float *vmap, int cols, int rows, float *nmap) {
+#pragma omp parallel for schedule(static)
+  for (int y = 0; y < rows; ++y)
+    for (int x = 0; x < cols; ++x) {
+      float *n = nmap + 4 * (y * cols + x);
+      if (x == cols - 1 || y == rows - 1) { n[0] = n[1] = n[2] = n[3] = kNaN; continue; }
+      const float *c = vmap + 4 * (y * cols + x);
+      const float *r = vmap + 4 * (y * cols + x + 1);
+      const float *d = vmap + 4 * ((y + 1) * cols + x);
+      if (!std::isnan(c[0]) && !std::isnan(r[0]) && !std::isnan(d[0])) {
+        f3 a = {r[0] - c[0], r[1] - c[1], r[2] - c[2]};
+        f3 b = {d[0] - c[0], d[1] - c[1], d[2] - c[2]};
+        f3 q = normalised(cross(a, b));
+        n[0] = q.x; n[1] = q.y; n[2] = q.z; n[3] = 1.0f;
+      } else {
+        n[0] = n[1] = n[2] = n[3] = kNaN;
+      }
+    }
+}
+
+// ResizeMapKernel, Pyrdown.cu:318-346.  normalised(float4) includes w in
+// the norm (VectorMath.h:328-330, 344-346).  The reference guards on the
+// source size but launches over the destination (an out-of-bounds access
+// when a destination side is not a multiple of 8); here the loop runs over
+// the destination, which yields the same in-bounds values.
+extern "C" void sfo_resize(const float *vsrc, const float *nsrc, int sc, int sr,
+                           float *vdst, float *ndst, int dc, int dr) {
+  (void)sr;
+#pragma omp parallel for schedule(static)
+  for (int y = 0; y < dr; ++y)
+    for (int x = 0; x < dc; ++x) {
+      const float *v00 = vsrc + 4 * ((2 * y) * sc + 2 * x), *v01 = v00 + 4;
+      const float *v10 = vsrc + 4 * ((2 * y + 1) * sc + 2 * x), *v11 = v10 + 4;
+      const float *n00 = nsrc + 4 * ((2 * y) * sc + 2 * x), *n01 = n00 + 4;
+      const float *n10 = nsrc + 4 * ((2 * y + 1) * sc + 2 * x), *n11 = n10 + 4;
+      float *vd = vdst + 4 * (y * dc + x), *nd = ndst + 4 * (y * dc + x);
+      if (std::isnan(v00[0]) || std::isnan(v01[0]) || std::isnan(v10[0]) || std::isnan(v11[0])) {
+        vd[0] = vd[1] = vd[2] = vd[3] = kNaN;
+      } else {
+        for (int k = 0; k < 4; ++k) vd[k] = (((v00[k] + v01[k]) + v10[k]) + v11[k]) / 4.0f;
+      }
+      if (std::isnan(n00[0]) || std::isnan(n01[0]) || std::isnan(n10[0]) || std::isnan(n11[0])) {
+        nd[0] = nd[1] = nd[2] = nd[3] = kNaN;
+      } else {
+        float s[4];
+        for (int k = 0; k < 4; ++k) s[k] = (((n00[k] + n01[k]) + n10[k]) + n11[k]) / 4.0f;
+        float len = std::sqrt(s[0] * s[0] + s[1] * s[1] + s[2] * s[2] + s[3] * s[3]);
+        for (int k = 0; k < 4; ++k) nd[k] = s[k] / len;
+      }
+    }
+}
+
+// ======================================================================= ICP
+namespace {
+
+// ICPReduce::searchPoint + getRow, Tracking/Reduction.cu:228-290, FP32
+// reference semantics.  `1.0 / z` and `+ 0.5` are double in the reference.
+bool icp_row_f32(const float *vc4, const float *vl_map, const float *nc4,
+                 const float *nl_map, int cols, int rows, const m3 &Rc,
+                 f3 tc, const m3 &Rl, const m3 &RlInv, f3 tl, float fx,
+                 float fy, float cx, float cy, float *row7) {
+  f3 vcurr_c = {vc4[0], vc4[1], vc4[2]};
+  if (std::isnan(vcurr_c.x) || (double)vcurr_c.z < 1e-3) return false;
+  f3 vcurr_g = mul(Rc, vcurr_c) + tc;
+  f3 vcurr_p = mul(RlInv, vcurr_g - tl);
+  float invz = (float)(1.0 / (double)vcurr_p.z);
+  int u = f2i((double)(vcurr_p.x * invz * fx + cx) + 0.5);
+  int v = f2i((double)(vcurr_p.y * invz * fy + cy) + 0.5);
+  if (u < 0 || v < 0 || u >= cols || v >= rows) return false;
+  const float *vl4 = vl_map + 4 * (v * cols + u);
+  const float *nl4 = nl_map + 4 * (v * cols + u);
+  f3 vlast_g = mul(Rl, mk3(vl4[0], vl4[1], vl4[2])) + tl;
+  f3 ncurr_c = {nc4[0], nc4[1], nc4[2]};
+  f3 ncurr_g = mul(Rc, ncurr_c);
+  f3 nlast_c = {nl4[0], nl4[1], nl4[2]};
+  f3 nlast_g = mul(Rl, nlast_c);
+  float dist = norm(vlast_g - vcurr_g);
+  float sine = norm(cross(ncurr_g, nlast_g));
+  const float angleThresh = (float)0.6, distThresh = (float)0.1;  // Reduction.cu:361-362
+  if (!(sine < angleThresh && dist <= distThresh && !std::isnan(ncurr_c.x) &&
+        !std::isnan(nlast_c.x)))
+    return false;
+  f3 nlast = mul(RlInv, nlast_g);
+  f3 vcurr = mul(RlInv, vcurr_g - tl);
+  f3 vlast = mul(RlInv, vlast_g - tl);
+  f3 mn = -nlast;
+  f3 cr = cross(nlast, vlast);
+  row7[0] = mn.x; row7[1] = mn.y; row7[2] = mn.z;
+  row7[3] = cr.x; row7[4] = cr.y; row7[5] = cr.z;
+  row7[6] = dot(mn, vcurr - vlast);
+  return true;
+}
+
+// The same row computed entirely in double (error-budget oracle).
+struct d3 { double x, y, z; };
+inline d3 operator+(d3 a, d3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline d3 operator-(d3 a, d3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline double ddot(d3 a, d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline d3 dcross(d3 a, d3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline double dnorm(d3 a) { return std::sqrt(ddot(a, a)); }
+struct dm3 { double m[9]; };
+inline d3 dmul(const dm3 &R, d3 a) {
+  return {R.m[0] * a.x + R.m[1] * a.y + R.m[2] * a.z, R.m[3] * a.x + R.m[4] * a.y + R.m[5] * a.z,
+          R.m[6] * a.x + R.m[7] * a.y + R.m[8] * a.z};
+}
+bool icp_row_f64(const float *vc4, const float *vl_map, const float *nc4,
+                 const float *nl_map, int cols, int rows, const dm3 &Rc, d3 tc,
+                 const dm3 &Rl, const dm3 &RlInv, d3 tl, double fx, double fy,
+                 double cx, double cy, double *row7) {
+  d3 vcurr_c = {vc4[0], vc4[1], vc4[2]};
+  if (std::isnan(vcurr_c.x) || vcurr_c.z < 1e-3) return false;
+  d3 vcurr_g = dmul(Rc, vcurr_c) + tc;
+  d3 vcurr_p = dmul(RlInv, vcurr_g - tl);
+  double invz = 1.0 / vcurr_p.z;
+  int u = f2i(vcurr_p.x * invz * fx + cx + 0.5);
+  int v = f2i(vcurr_p.y * invz * fy + cy + 0.5);
+  if (u < 0 || v < 0 || u >= cols || v >= rows) return false;
+  const float *vl4 = vl_map + 4 * (v * cols + u);
+  const float *nl4 = nl_map + 4 * (v * cols + u);
+  d3 vlast_g = dmul(Rl, d3{vl4[0], vl4[1], vl4[2]}) + tl;
+  d3 ncurr_g = dmul(Rc, d3{nc4[0], nc4[1], nc4[2]});
+  d3 nlast_g = dmul(Rl, d3{nl4[0], nl4[1], nl4[2]});
+  double dist = dnorm(vlast_g - vcurr_g);
+  double sine = dnorm(dcross(ncurr_g, nlast_g));
+  if (!(sine < 0.6 && dist <= 0.1 && !std::isnan(nc4[0]) && !std::isnan(nl4[0]))) return false;
+  d3 nlast = dmul(RlInv, nlast_g);
+  d3 vcurr = dmul(RlInv, vcurr_g - tl);
+  d3 vlast = dmul(RlInv, vlast_g - tl);
+  d3 cr = dcross(nlast, vlast);
+  row7[0] = -nlast.x; row7[1] = -nlast.y; row7[2] = -nlast.z;
+  row7[3] = cr.x; row7[4] = cr.y; row7[5] = cr.z;
+  row7[6] = -(nlast.x * (vcurr.x - vlast.x) + nlast.y * (vcurr.y - vlast.y) + nlast.z * (vcurr.z - vlast.z));
+  return true;
+}
+
+}  // namespace
+
+// Per-pixel 29-vectors (Reduction.cu:281-289): upper triangle of [J|r]^T[J|r]
+// (28 products) and the found flag.
+extern "C" void sfo_icp_rows(const float *vcurr, const float *vlast,
+                             const float *ncurr, const float *nlast, int cols,
+                             int rows, const float *Rcurr, const float *tcurr,
+                             const float *Rlast, const float *RlastInv,
+                             const float *tlast, float fx, float fy, float cx,
+                             float cy, float *rows29) {
+  m3 Rc = m3_from(Rcurr), Rl = m3_from(Rlast), RlI = m3_from(RlastInv);
+  f3 tc = f3_from(tcurr), tl = f3_from(tlast);
+  const int N = cols * rows;
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < N; ++i) {
+    float row[7] = {0, 0, 0, 0, 0, 0, 0};
+    bool found = icp_row_f32(vcurr + 4 * i, vlast, ncurr + 4 * i, nlast, cols, rows, Rc, tc, Rl,
+                             RlI, tl, fx, fy, cx, cy, row);
+    float *o = rows29 + 29 * (size_t)i;
+    int k = 0;
+    for (int a = 0; a < 7; ++a)
+      for (int b = a; b < 7; ++b) o[k++] = row[a] * row[b];
+    o[28] = (float)found;
+  }
+}
+
+// icpStepKernel + Reduce<float,29> (Reduction.cu:292-385): the 29 sums.  The
+// reference sums in float in a launch-shape-dependent order; the oracle sums
+// the same FP32 per-pixel products in double (per-thread partials combined
+// in thread order, so the result is deterministic for a thread count).
+namespace {
+// Sum of the 29 per-pixel terms.  fp64 == 0: FP32 rows (reference
+// semantics) from the float pose; fp64 == 1: rows in double from the
+// double pose.  Per-chunk partials combined in chunk order.
+void icp_sums_impl(const float *vcurr, const float *vlast, const float *ncurr,
+                   const float *nlast, int cols, int rows, const m3 &Rc, f3 tc,
+                   const m3 &Rl, const m3 &RlI, f3 tl, const dm3 &dRc, d3 dtc,
+                   const dm3 &dRl, const dm3 &dRlI, d3 dtl, float fx, float fy,
+                   float cx, float cy, int fp64, double *out29) {
+  const int N = cols * rows;
+  for (int k = 0; k < 29; ++k) out29[k] = 0;
+  const int kChunks = 64;
+  std::vector<double> part((size_t)kChunks * 29, 0.0);
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < kChunks; ++c) {
+    double *p = &part[(size_t)c * 29];
+    int i0 = (int)((long long)N * c / kChunks), i1 = (int)((long long)N * (c + 1) / kChunks);
+    for (int i = i0; i < i1; ++i) {
+      if (fp64) {
+        double row[7] = {0, 0, 0, 0, 0, 0, 0};
+        bool found = icp_row_f64(vcurr + 4 * i, vlast, ncurr + 4 * i, nlast, cols, rows, dRc, dtc,
+                                 dRl, dRlI, dtl, fx, fy, cx, cy, row);
+        if (!found) continue;
+        int k = 0;
+        for (int a = 0; a < 7; ++a)
+          for (int b = a; b < 7; ++b) p[k++] += row[a] * row[b];
+        p[28] += 1.0;
+      } else {
+        float row[7] = {0, 0, 0, 0, 0, 0, 0};
+        bool found = icp_row_f32(vcurr + 4 * i, vlast, ncurr + 4 * i, nlast, cols, rows, Rc, tc,
+                                 Rl, RlI, tl, fx, fy, cx, cy, row);
+        if (!found) continue;
+        int k = 0;
+        for (int a = 0; a < 7; ++a)
+          for (int b = a; b < 7; ++b) p[k++] += (double)(row[a] * row[b]);
+        p[28] += 1.0;
+      }
+    }
+  }
+  for (int c = 0; c < kChunks; ++c)
+    for (int k = 0; k < 29; ++k) out29[k] += part[(size_t)c * 29 + k];
+}
+}  // namespace
+
+// icpStepKernel + Reduce<float,29> (Reduction.cu:292-385): the 29 sums.  The
+// reference sums in float in a launch-shape-dependent order; the oracle sums
+// the same FP32 per-pixel products in double.
+extern "C" void sfo_icp_sums(const float *vcurr, const float *vlast,
+                             const float *ncurr, const float *nlast, int cols,
+                             int rows, const float *Rcurr, const float *tcurr,
+                             const float *Rlast, const float *RlastInv,
+                             const float *tlast, float fx, float fy, float cx,
+                             float cy, int fp64, double *out29) {
+  m3 Rc = m3_from(Rcurr), Rl = m3_from(Rlast), RlI = m3_from(RlastInv);
+  f3 tc = f3_from(tcurr), tl = f3_from(tlast);
+  dm3 dRc, dRl, dRlI;
+  for (int k = 0; k < 9; ++k) { dRc.m[k] = Rcurr[k]; dRl.m[k] = Rlast[k]; dRlI.m[k] = RlastInv[k]; }
+  d3 dtc{tcurr[0], tcurr[1], tcurr[2]}, dtl{tlast[0], tlast[1], tlast[2]};
+  icp_sums_impl(vcurr, vlast, ncurr, nlast, cols, rows, Rc, tc, Rl, RlI, tl, dRc, dtc, dRl, dRlI,
+                dtl, fx, fy, cx, cy, fp64, out29);
+}
+
+// CreateMatrix<6,7>, Reduction.cu:6-16.
+extern "C" void sfo_create_matrix(const double *s, double *A, double *b) {
+  int shift = 0;
+  for (int i = 0; i < 6; ++i)
+    for (int j = i; j < 7; ++j) {
+      double value = s[shift++];
+      if (j == 6) b[i] = value;
+      else A[j * 6 + i] = A[i * 6 + j] = value;
+    }
+}
+
+// Eigen::LDLT (Tracking.cc:493): LDL^T with symmetric pivoting on the
+// largest remaining diagonal; a zero pivot zeroes that component of the
+// solution (Eigen's LDLT::solve rule).
+extern "C" void sfo_ldlt_solve6(const double *A36, const double *b6, double *x6) {
+  double a[6][6];
+  int perm[6];
+  for (int i = 0; i < 6; ++i) { perm[i] = i; for (int j = 0; j < 6; ++j) a[i][j] = A36[i * 6 + j]; }
+  double d[6];
+  // Right-looking: a[k..][k..] is the Schur complement, columns < k hold L.
+  for (int k = 0; k < 6; ++k) {
+    int piv = k;
+    double best = std::fabs(a[k][k]);
+    for (int i = k + 1; i < 6; ++i) if (std::fabs(a[i][i]) > best) { best = std::fabs(a[i][i]); piv = i; }
+    if (piv != k) {
+      for (int j = 0; j < 6; ++j) std::swap(a[k][j], a[piv][j]);
+      for (int i = 0; i < 6; ++i) std::swap(a[i][k], a[i][piv]);
+      std::swap(perm[k], perm[piv]);
+    }
+    double dk = a[k][k];
+    d[k] = dk;
+    double l[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = k + 1; i < 6; ++i) l[i] = (dk != 0.0) ? a[i][k] / dk : 0.0;
+    for (int i = k + 1; i < 6; ++i)
+      for (int j = k + 1; j < 6; ++j) a[i][j] -= l[i] * dk * l[j];
+    for (int i = k + 1; i < 6; ++i) { a[i][k] = l[i]; a[k][i] = 0.0; }
+  }
+  double y[6];
+  for (int i = 0; i < 6; ++i) y[i] = b6[perm[i]];
+  for (int i = 0; i < 6; ++i) for (int j = 0; j < i; ++j) y[i] -= a[i][j] * y[j];
+  const double tol = std::numeric_limits<double>::min();
+  for (int i = 0; i < 6; ++i) y[i] = (std::fabs(d[i]) > tol) ? y[i] / d[i] : 0.0;
+  for (int i = 5; i >= 0; --i) for (int j = i + 1; j < 6; ++j) y[i] -= a[j][i] * y[j];
+  for (int i = 0; i < 6; ++i) x6[perm[i]] = y[i];
+}
+
+// Sophus::SE3d::exp (Tracking.cc:494): twist (upsilon, omega), rotation via
+// the unit quaternion of SO3::expAndTheta, translation V * upsilon with the
+// left Jacobian V = I + (1-cos t)/t^2 W + (t - sin t)/t^3 W^2.
+extern "C" void sfo_se3_exp(const double *xi, double *T) {
+  const double ups[3] = {xi[0], xi[1], xi[2]}, w[3] = {xi[3], xi[4], xi[5]};
+  const double eps = 1e-10;
+  double th2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+  double th = std::sqrt(th2);
+  double real_f, imag_f;
+  if (th2 < eps * eps) {
+    double th4 = th2 * th2;
+    imag_f = 0.5 - (1.0 / 48.0) * th2 + (1.0 / 3840.0) * th4;
+    real_f = 1.0 - (1.0 / 8.0) * th2 + (1.0 / 384.0) * th4;
+  } else {
+    imag_f = std::sin(0.5 * th) / th;
+    real_f = std::cos(0.5 * th);
+  }
+  double qw = real_f, qx = imag_f * w[0], qy = imag_f * w[1], qz = imag_f * w[2];
+  double tx = 2 * qx, ty = 2 * qy, tz = 2 * qz;
+  double twx = tx * qw, twy = ty * qw, twz = tz * qw, txx = tx * qx, txy = ty * qx, txz = tz * qx;
+  double tyy = ty * qy, tyz = tz * qy, tzz = tz * qz;
+  double R[9] = {1 - (tyy + tzz), txy - twz, txz + twy, txy + twz, 1 - (txx + tzz),
+                 tyz - twx, txz - twy, tyz + twx, 1 - (txx + tyy)};
+  double W[9] = {0, -w[2], w[1], w[2], 0, -w[0], -w[1], w[0], 0};
+  double W2[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double s = 0;
+      for (int k = 0; k < 3; ++k) s += W[i * 3 + k] * W[k * 3 + j];
+      W2[i * 3 + j] = s;
+    }
+  double V[9];
+  if (th < eps) {
+    for (int k = 0; k < 9; ++k) V[k] = R[k];
+  } else {
+    double c1 = (1 - std::cos(th)) / th2, c2 = (th - std::sin(th)) / (th2 * th);
+    for (int k = 0; k < 9; ++k) V[k] = (k % 4 == 0 ? 1.0 : 0.0) + c1 * W[k] + c2 * W2[k];
+  }
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j) T[i * 4 + j] = R[i * 3 + j];
+    T[i * 4 + 3] = V[i * 3 + 0] * ups[0] + V[i * 3 + 1] * ups[1] + V[i * 3 + 2] * ups[2];
+  }
+  T[12] = T[13] = T[14] = 0; T[15] = 1;
+}
+
+namespace {
+void mat4_mul(const double *A, const double *B, double *C) {
+  double t[16];
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) {
+      double s = 0;
+      for (int k = 0; k < 4; ++k) s += A[i * 4 + k] * B[k * 4 + j];
+      t[i * 4 + j] = s;
+    }
+  memcpy(C, t, sizeof(t));
+}
+void se3_inv(const double *T, double *I) {
+  double t[16];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) t[i * 4 + j] = T[j * 4 + i];
+  for (int i = 0; i < 3; ++i) t[i * 4 + 3] = -(t[i * 4 + 0] * T[3] + t[i * 4 + 1] * T[7] + t[i * 4 + 2] * T[11]);
+  t[12] = t[13] = t[14] = 0; t[15] = 1;
+  memcpy(I, t, sizeof(t));
+}
+// Frame::GpuRotation / GpuInvRotation / GpuTranslation, Core/Frame.cc:626-645.
+void pose_to_gpu(const double *P, float *R, float *Rinv, float *t) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) { R[i * 3 + j] = (float)P[i * 4 + j]; Rinv[i * 3 + j] = (float)P[j * 4 + i]; }
+  for (int i = 0; i < 3; ++i) t[i] = (float)P[i * 4 + 3];
+}
+// |sin(eulerAngles(0,1,2))| (Tracking.cc:505-510): the norm is the same for
+// both of Eigen's solution branches.
+double euler_sin_norm(const double *P) {
+  double r02 = std::max(-1.0, std::min(1.0, P[2]));
+  double b = std::asin(r02);
+  double a = std::atan2(-P[6], P[10]);
+  double c = std::atan2(-P[1], P[0]);
+  double sa = std::sin(a), sb = std::sin(b), sc = std::sin(c);
+  return std::sqrt(sa * sa + sb * sb + sc * sc);
+}
+}  // namespace
+
+// Tracker::ComputeSE3(icpOnly=true, iter, thresh), Tracking.cc:369-517.
+extern "C" int sfo_compute_se3(int levels, const int *cols, const int *rows,
+                               const float *const *vnext, const float *const *nnext,
+                               const float *const *vlast, const float *const *nlast,
+                               const float *K, const int *iters, const int *min_count,
+                               float thresh, const double *last_pose, double *next_pose,
+                               int fp64, double *stats) {
+  double lastPose[16], pose[16], delta[16], candidate[16];
+  memcpy(lastPose, last_pose, sizeof(lastPose));
+  memcpy(pose, next_pose, sizeof(pose));
+  for (int k = 0; k < 16; ++k) delta[k] = (k % 5 == 0) ? 1.0 : 0.0;
+  float rgbError = 0, icpError = 0, lastError = 100.f, currError = 0, candidateICP = 0;
+  const float w = 1e-4f;
+  int breakCount = 0, its = 0, icpCount = 0;
+  float Rl[9], RlI[9], tl[3];
+  pose_to_gpu(lastPose, Rl, RlI, tl);
+  for (int i = levels - 1; i >= 0; --i) {
+    const int div = 1 << i;
+    const float fx = K[0] / (float)div, fy = K[1] / (float)div, cx = K[2] / (float)div, cy = K[3] / (float)div;
+    for (int j = 0; j < iters[i]; ++j) {
+      float Rc[9], RcI[9], tc[3];
+      pose_to_gpu(next_pose, Rc, RcI, tc);
+      double s[29], A[36], b[6], x[6], dT[16], dInv[16];
+      {
+        dm3 dRc, dRl, dRlI;
+        for (int r = 0; r < 3; ++r)
+          for (int c = 0; c < 3; ++c) {
+            dRc.m[r * 3 + c] = next_pose[r * 4 + c];
+            dRl.m[r * 3 + c] = lastPose[r * 4 + c];
+            dRlI.m[r * 3 + c] = lastPose[c * 4 + r];
+          }
+        d3 dtc{next_pose[3], next_pose[7], next_pose[11]}, dtl{lastPose[3], lastPose[7], lastPose[11]};
+        icp_sums_impl(vnext[i], vlast[i], nnext[i], nlast[i], cols[i], rows[i], m3_from(Rc),
+                      f3_from(tc), m3_from(Rl), m3_from(RlI), f3_from(tl), dRc, dtc, dRl, dRlI,
+                      dtl, fx, fy, cx, cy, fp64, s);
+      }
+      ++its;
+      float residual[2] = {(float)s[27], (float)s[28]};
+      sfo_create_matrix(s, A, b);
+      icpError = std::sqrt(residual[0]) / residual[1];
+      icpCount = (int)residual[1];
+      if (std::isnan(icpError) || icpCount < min_count[i]) {
+        memcpy(next_pose, lastPose, sizeof(lastPose));
+        if (stats) { stats[0] = icpError; stats[1] = icpCount; stats[2] = its; stats[3] = 1; }
+        return 0;
+      }
+      currError = rgbError * w + icpError;
+      if (lastError < currError) {
+        breakCount++;
+        if (breakCount == 1) memcpy(candidate, next_pose, sizeof(candidate));
+        candidateICP = icpError;  // outside the inner if (Tracking.cc:463-465)
+      } else {
+        breakCount = 0;
+      }
+      if (breakCount > 2) {
+        memcpy(next_pose, candidate, sizeof(candidate));
+        icpError = candidateICP;
+        break;
+      }
+      lastError = currError;
+      sfo_ldlt_solve6(A, b, x);
+      sfo_se3_exp(x, dT);
+      mat4_mul(dT, delta, delta);
+      se3_inv(delta, dInv);
+      mat4_mul(lastPose, dInv, next_pose);
+    }
+    if (breakCount > 2) break;
+  }
+  double pinv[16], p[16];
+  se3_inv(pose, pinv);
+  mat4_mul(pinv, next_pose, p);
+  double tn = std::sqrt(p[3] * p[3] + p[7] * p[7] + p[11] * p[11]);
+  double an = euler_sin_norm(p);
+  int ok = (icpError < thresh) && (an <= 0.1 && tn <= 0.1);
+  if (!ok) memcpy(next_pose, lastPose, sizeof(lastPose));
+  if (stats) { stats[0] = icpError; stats[1] = icpCount; stats[2] = its; stats[3] = ok ? 0 : 2; }
+  return ok;
+}
+
+// ======================================================================= map
+struct sfo_map {
+  sfo_config c;
+  float voxelSizeInv, blockWidth, stepScale;  // DeviceMap.h:186-189
+  uint32_t numEntries;
+  std::vector<sfo_entry> entries, visible;
+  std::vector<sfo_voxel> voxels;
+  std::vector<int> heap, mutex;
+  int heapCounter = 0, entryPtr = 1;
+  unsigned noVisible = 0;
+};
+
+namespace {
+// DeviceMap::Hash, Mapping/DeviceMap.cu:3-10.  `% NumBuckets` is taken on
+// the unsigned conversion of the signed product-xor (NumBuckets is uint).
+inline uint32_t hash_pos(const sfo_map &m, i3 p) {
+  uint32_t h = ((uint32_t)p.x * 73856093u) ^ ((uint32_t)p.y * 19349669u) ^ ((uint32_t)p.z * 83492791u);
+  return h % m.c.num_buckets;
+}
+inline bool pos_eq(const sfo_entry &e, i3 p) { return e.x == p.x && e.y == p.y && e.z == p.z; }
+// voxelPosToBlockPos, DeviceMap.cu:169-180.
+inline i3 vox2block(i3 v) {
+  if (v.x < 0) v.x -= 7;
+  if (v.y < 0) v.y -= 7;
+  if (v.z < 0) v.z -= 7;
+  return {v.x / 8, v.y / 8, v.z / 8};
+}
+// voxelPosToLocalIdx, DeviceMap.cu:186-201,218-220.
+inline int vox2local(i3 v) {
+  int lx = v.x % 8, ly = v.y % 8, lz = v.z % 8;
+  if (lx < 0) lx += 8;
+  if (ly < 0) ly += 8;
+  if (lz < 0) lz += 8;
+  return lz * 64 + ly * 8 + lx;
+}
+// DeviceMap::CreateEntry, DeviceMap.cu:12-21.
+sfo_entry create_entry(sfo_map &m, i3 p, int offset) {
+  int old = m.heapCounter--;
+  if (old >= 0) {
+    int ptr = m.heap[old];
+    if (ptr != -1) return {p.x, p.y, p.z, ptr * 512, offset, {0, 0, 0}};
+  }
+  return {p.x, p.y, p.z, -1, 0, {0, 0, 0}};
+}
+// DeviceMap::CreateBlock, DeviceMap.cu:23-69, executed serially (the bucket
+// mutex never contends).
+void create_block(sfo_map &m, i3 p) {
+  uint32_t bucket = hash_pos(m, p);
+  sfo_entry *e = &m.entries[bucket];
+  sfo_entry *empty = nullptr;
+  if (pos_eq(*e, p) && e->ptr != -1) return;
+  if (e->ptr == -1) empty = e;
+  while (e->offset > 0) {
+    e = &m.entries[m.c.num_buckets + e->offset - 1];
+    if (pos_eq(*e, p) && e->ptr != -1) return;
+    if (e->ptr == -1 && !empty) empty = e;
+  }
+  if (empty) {
+    *empty = create_entry(m, p, e->offset);
+  } else {
+    int offset = m.entryPtr++;
+    if (offset <= (int)m.c.num_excess) {
+      m.entries[m.c.num_buckets + offset - 1] = create_entry(m, p, 0);
+      e->offset = offset;
+    }
+  }
+}
+// DeviceMap::FindEntry, DeviceMap.cu:141-154.
+const sfo_entry *find_entry(const sfo_map &m, i3 p) {
+  uint32_t bucket = hash_pos(m, p);
+  const sfo_entry *e = &m.entries[bucket];
+  if (e->ptr != -1 && pos_eq(*e, p)) return e;
+  while (e->offset > 0) {
+    e = &m.entries[m.c.num_buckets + e->offset - 1];
+    if (pos_eq(*e, p) && e->ptr != -1) return e;
+  }
+  return nullptr;
+}
+}  // namespace
+
+extern "C" sfo_map *sfo_map_create(const sfo_config *cfg) {
+  sfo_map *m = new sfo_map();
+  m->c = *cfg;
+  m->voxelSizeInv = (float)(1.0 / (double)cfg->voxel_size);
+  m->blockWidth = cfg->voxel_size * 8.0f;
+  m->stepScale = (float)(0.5 * (double)cfg->trunc_dist * (double)m->voxelSizeInv);
+  m->numEntries = cfg->num_buckets + cfg->num_excess;
+  m->entries.resize(m->numEntries);
+  m->visible.resize(m->numEntries);
+  m->voxels.resize((size_t)cfg->num_sdf_blocks * 512);
+  m->heap.resize(cfg->num_sdf_blocks);
+  m->mutex.resize(cfg->num_buckets);
+  sfo_map_reset(m);
+  return m;
+}
+extern "C" void sfo_map_destroy(sfo_map *m) { delete m; }
+
+// ResetHashKernel + ResetSdfBlockKernel, FuseMap.cu:1251-1289.  release()
+// leaves `offset` untouched; the reference relies on freshly allocated
+// (zeroed) memory, so reset writes offset = 0.
+extern "C" void sfo_map_reset(sfo_map *m) {
+  for (auto &e : m->entries) e = {0, 0, 0, -1, 0, {0, 0, 0}};
+  for (auto &e : m->visible) e = {0, 0, 0, -1, 0, {0, 0, 0}};
+  for (auto &x : m->mutex) x = -1;
+  for (uint32_t x = 0; x < m->c.num_sdf_blocks; ++x) m->heap[x] = (int)m->c.num_sdf_blocks - (int)x - 1;
+  sfo_voxel rel;
+  memset(&rel, 0, sizeof(rel));
+  rel.sdf = kNaN;
+  for (auto &v : m->voxels) {
+    uint8_t keep = v.obj_idx;  // release() does not touch obj_idx
+    v = rel;
+    v.obj_idx = keep;
+  }
+  m->heapCounter = (int)m->c.num_sdf_blocks - 1;
+  m->entryPtr = 1;
+  m->noVisible = 0;
+}
+extern "C" sfo_entry *sfo_map_entries(sfo_map *m) { return m->entries.data(); }
+extern "C" sfo_voxel *sfo_map_voxels(sfo_map *m) { return m->voxels.data(); }
+extern "C" sfo_entry *sfo_map_visible(sfo_map *m) { return m->visible.data(); }
+extern "C" int *sfo_map_heap(sfo_map *m) { return m->heap.data(); }
+extern "C" void sfo_map_counters(sfo_map *m, int *out) {
+  int alloc = 0;
+  for (auto &e : m->entries) alloc += e.ptr >= 0;
+  out[0] = m->heapCounter; out[1] = m->entryPtr; out[2] = (int)m->noVisible; out[3] = alloc;
+}
+
+// Fusion::CreateBlocks, FuseMap.cu:92-132 (unproject :35-44), serial order.
+extern "C" void sfo_alloc(sfo_map *m, const float *depth, int cols, int rows,
+                          const float *R, const float *t, float fx, float fy,
+                          float cx, float cy) {
+  m3 Rv = m3_from(R);
+  f3 tv = f3_from(t);
+  const float invfx = (float)(1.0 / (double)fx), invfy = (float)(1.0 / (double)fy);
+  const float dmin = m->c.depth_min, dmax = m->c.depth_max;
+  for (int y = 0; y < rows; ++y)
+    for (int x = 0; x < cols; ++x) {
+      float z = depth[y * cols + x];
+      if (std::isnan(z) || z < dmin || z > dmax) continue;
+      float thresh = m->c.trunc_dist / 2.0f;
+      float z_near = std::fmax(dmin, z - thresh);
+      float z_far = std::fmin(dmax, z + thresh);
+      if (z_near >= z_far) continue;
+      f3 pn = {z_near * ((float)x - cx) * invfx, z_near * ((float)y - cy) * invfy, z_near};
+      f3 pf = {z_far * ((float)x - cx) * invfx, z_far * ((float)y - cy) * invfy, z_far};
+      f3 pt_near = (mul(Rv, pn) + tv) * m->voxelSizeInv;
+      f3 pt_far = (mul(Rv, pf) + tv) * m->voxelSizeInv;
+      f3 dir = pt_far - pt_near;
+      float length = norm(dir);
+      int nSteps = f2i(std::ceil(2.0 * (double)length));
+      dir = dir / (float)(nSteps - 1);
+      for (int i = 0; i < nSteps; ++i) {
+        create_block(*m, vox2block(floor3(pt_near)));
+        pt_near = pt_near + dir;
+      }
+    }
+}
+
+namespace {
+struct Cam {
+  m3 R, Rinv;
+  f3 t;
+  float fx, fy, cx, cy;
+  int cols, rows;
+  float dmin, dmax;
+};
+// Fusion::CheckVertexVisibility, FuseMap.cu:46-56 (project :27-33).
+inline bool vertex_visible(const Cam &c, f3 p3) {
+  f3 pt = mul(c.Rinv, p3 - c.t);
+  if (pt.z < 1e-3f) return false;
+  float px = c.fx * pt.x / pt.z + c.cx;
+  float py = c.fy * pt.y / pt.z + c.cy;
+  return px >= 0 && py >= 0 && px < (float)c.cols && py < (float)c.rows && pt.z >= c.dmin &&
+         pt.z <= c.dmax;
+}
+// Fusion::CheckBlockVisibility, FuseMap.cu:58-90 (the corner walk order).
+bool block_visible(const Cam &c, const sfo_map &m, i3 pos) {
+  float s = m.blockWidth;
+  f3 k = {(float)pos.x * s, (float)pos.y * s, (float)pos.z * s};
+  if (vertex_visible(c, k)) return true;
+  k.z += s; if (vertex_visible(c, k)) return true;
+  k.y += s; if (vertex_visible(c, k)) return true;
+  k.x += s; if (vertex_visible(c, k)) return true;
+  k.z -= s; if (vertex_visible(c, k)) return true;
+  k.y -= s; if (vertex_visible(c, k)) return true;
+  k.x -= s; k.y += s; if (vertex_visible(c, k)) return true;
+  k.x += s; k.y -= s; k.z += s; if (vertex_visible(c, k)) return true;
+  return false;
+}
+}  // namespace
+
+// Fusion::CheckFullVisibility + ComputeOffset, FuseMap.cu:134-168 and
+// Utility/ParallelScan.h:1-49: the visible set, compacted in entry order.
+extern "C" unsigned sfo_visibility(sfo_map *m, const float *R, const float *Rinv,
+                                   const float *t, int cols, int rows, float fx,
+                                   float fy, float cx, float cy, float depth_max,
+                                   float depth_min) {
+  Cam c{m3_from(R), m3_from(Rinv), f3_from(t), fx, fy, cx, cy, cols, rows, depth_min, depth_max};
+  unsigned n = 0;
+  for (uint32_t x = 0; x < m->numEntries; ++x) {
+    const sfo_entry &e = m->entries[x];
+    if (e.ptr != -1 && block_visible(c, *m, {e.x, e.y, e.z})) {
+      if (n < m->numEntries) m->visible[n] = e;
+      ++n;
+    }
+  }
+  m->noVisible = n;
+  return n;
+}
+
+namespace {
+// project(): FuseMap.cu:27-33 then make_int2 (truncation, VectorMath.h:28-30).
+inline bool voxel_pixel(const Cam &c, const sfo_map &m, i3 blk, int lx, int ly, int lz, f3 &pos,
+                        int &u, int &v) {
+  f3 w = {(float)(blk.x * 8 + lx) * m.c.voxel_size, (float)(blk.y * 8 + ly) * m.c.voxel_size,
+          (float)(blk.z * 8 + lz) * m.c.voxel_size};
+  pos = mul(c.Rinv, w - c.t);
+  u = f2i(c.fx * pos.x / pos.z + c.cx);
+  v = f2i(c.fy * pos.y / pos.z + c.cy);
+  return !(u < 0 || v < 0 || u >= c.cols || v >= c.rows);
+}
+}  // namespace
+
+// Fusion::createVoxels, FuseMap.cu:432-507 (one update per visible voxel).
+extern "C" void sfo_integrate(sfo_map *m, const float *depth, const uint8_t *rgb,
+                              int cols, int rows, const float *Rinv, const float *t,
+                              float fx, float fy, float cx, float cy,
+                              float depth_max, float depth_min) {
+  Cam c{{}, m3_from(Rinv), f3_from(t), fx, fy, cx, cy, cols, rows, depth_min, depth_max};
+  const float thresh = m->c.trunc_dist;
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int b = 0; b < (int)m->noVisible; ++b) {
+    const sfo_entry &entry = m->visible[b];
+    if (entry.ptr == -1) continue;
+    i3 blk = {entry.x, entry.y, entry.z};
+    for (int lz = 0; lz < 8; ++lz)
+      for (int ly = 0; ly < 8; ++ly)
+        for (int lx = 0; lx < 8; ++lx) {
+          f3 pos;
+          int u, v;
+          if (!voxel_pixel(c, *m, blk, lx, ly, lz, pos, u, v)) continue;
+          float dp = depth[v * cols + u];
+          if (std::isnan(dp) || dp > c.dmax || dp < c.dmin) continue;
+          float sdf = dp - pos.z;
+          if (!(sdf >= -thresh)) continue;
+          sdf = std::fmin(1.0f, sdf / thresh);
+          const uint8_t *px = rgb + 3 * (v * cols + u);
+          f3 val = {(float)px[0], (float)px[1], (float)px[2]};
+          sfo_voxel &prev = m->voxels[(size_t)entry.ptr + lz * 64 + ly * 8 + lx];
+          if (prev.weight == 0) {
+            uint8_t keep = prev.obj_idx;  // Voxel::operator= skips obj_idx
+            memset(&prev, 0, sizeof(prev));
+            prev.obj_idx = keep;
+            prev.sdf = sdf;
+            prev.weight = 1;
+            prev.color[0] = f2u8(val.x); prev.color[1] = f2u8(val.y); prev.color[2] = f2u8(val.z);
+          } else {
+            if (prev.label == 0) {
+              // (make_float3(color) * weight) resolves to operator*(float3,int)
+              // -> int3 (VectorMath.h:231-233), then int3 + float3 -> float3.
+              int wgt = prev.weight;
+              float r0 = ((float)(f2i((float)prev.color[0] * (float)wgt)) + val.x) / (float)(wgt + 1);
+              float r1 = ((float)(f2i((float)prev.color[1] * (float)wgt)) + val.y) / (float)(wgt + 1);
+              float r2 = ((float)(f2i((float)prev.color[2] * (float)wgt)) + val.z) / (float)(wgt + 1);
+              prev.color[0] = f2u8(r0); prev.color[1] = f2u8(r1); prev.color[2] = f2u8(r2);
+            }
+            prev.sdf = (prev.sdf * (float)prev.weight + sdf) / (float)(prev.weight + 1);
+            prev.weight = (uint8_t)std::min(255, prev.weight + 1);
+          }
+        }
+  }
+}
+
+// Fusion::analyzeSemantics, FuseMap.cu:509-668, one update per voxel (the
+// (8,8) launch of AnalyzeMapSemantics, FuseMap.cu:1234-1236).
+extern "C" void sfo_semantics(sfo_map *m, const float *depth, const uint8_t *rgb,
+                              const float *nmap, const uint8_t *mask,
+                              int num_detection, int cols, int rows,
+                              const float *Rinv, const float *t, float fx,
+                              float fy, float cx, float cy, float depth_max,
+                              float depth_min) {
+  Cam c{{}, m3_from(Rinv), f3_from(t), fx, fy, cx, cy, cols, rows, depth_min, depth_max};
+  const float thresh = m->c.trunc_dist;
+  const int pal[3] = {(int)(std::pow(2, 25) - 1), (int)(std::pow(2, 15) - 1), (int)(std::pow(2, 21) - 1)};
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int b = 0; b < (int)m->noVisible; ++b) {
+    const sfo_entry &entry = m->visible[b];
+    if (entry.ptr == -1) continue;
+    i3 blk = {entry.x, entry.y, entry.z};
+    for (int lz = 0; lz < 8; ++lz)
+      for (int ly = 0; ly < 8; ++ly)
+        for (int lx = 0; lx < 8; ++lx) {
+          f3 pos;
+          int u, v;
+          if (!voxel_pixel(c, *m, blk, lx, ly, lz, pos, u, v)) continue;
+          float dp = depth[v * cols + u];
+          if (std::isnan(dp) || dp > c.dmax || dp < c.dmin) continue;
+          const float *nl = nmap + 4 * (v * cols + u);
+          if (std::isnan(nl[0])) continue;
+          float sdf = dp - pos.z;
+          if (!(sdf >= -thresh)) continue;
+          f3 val;
+          uint8_t label;
+          const uint8_t *px = rgb + 3 * (v * cols + u);
+          if (num_detection > 0) {
+            label = mask[v * cols + u];
+            if (label == 0) {
+              val = {(float)px[0], (float)px[1], (float)px[2]};
+            } else {
+              // pallete[k] * int(label) wraps in 32-bit on the GPU.
+              int p0 = (int)((uint32_t)pal[0] * (uint32_t)label) % 255;
+              int p1 = (int)((uint32_t)pal[1] * (uint32_t)label) % 255;
+              int p2 = (int)((uint32_t)pal[2] * (uint32_t)label) % 255;
+              val = {(float)p0, (float)p1, (float)p2};
+            }
+          } else {
+            label = 0;
+            val = {(float)px[0], (float)px[1], (float)px[2]};
+          }
+          sfo_voxel &prev = m->voxels[(size_t)entry.ptr + lz * 64 + ly * 8 + lx];
+          if (prev.weight == 0) continue;
+          if (label != 0) {
+            if (label == prev.label) {
+              prev.count = (uint8_t)std::min(255, prev.count + 1);
+              prev.color[0] = f2u8(val.x); prev.color[1] = f2u8(val.y); prev.color[2] = f2u8(val.z);
+            } else {
+              if (label == prev.label_2) {
+                prev.count_2 = (uint8_t)std::min(255, prev.count_2 + 1);
+                prev.color_2[0] = f2u8(val.x); prev.color_2[1] = f2u8(val.y); prev.color_2[2] = f2u8(val.z);
+              } else if (prev.count_2 < 7) {
+                prev.label_2 = label;
+                prev.count_2 = 1;
+                prev.color_2[0] = f2u8(val.x); prev.color_2[1] = f2u8(val.y); prev.color_2[2] = f2u8(val.z);
+              }
+              if ((prev.count < prev.count_2 && prev.label != 0) ||
+                  (prev.count < prev.count_2 * 2 && prev.label == 0)) {
+                std::swap(prev.label, prev.label_2);
+                std::swap(prev.count, prev.count_2);
+                for (int k = 0; k < 3; ++k) std::swap(prev.color[k], prev.color_2[k]);
+              }
+            }
+          } else {
+            // w = nl . normalised(make_float4(pos)) (FuseMap.cu:641), float4 dot
+            float len = std::sqrt(pos.x * pos.x + pos.y * pos.y + pos.z * pos.z + 1.0f * 1.0f);
+            float a0 = pos.x / len, a1 = pos.y / len, a2 = pos.z / len, a3 = 1.0f / len;
+            float wgt = nl[0] * a0 + nl[1] * a1 + nl[2] * a2 + nl[3] * a3;
+            if (prev.label != 0) {
+              if (prev.count < 7) {
+                prev.label_2 = prev.label;
+                for (int k = 0; k < 3; ++k) prev.color_2[k] = prev.color[k];
+                prev.count_2 = prev.count;
+                prev.label = 0;
+                prev.count = 1;
+                f3 vv = val / 255.f;
+                f3 old = mk3((float)prev.color[0], (float)prev.color[1], (float)prev.color[2]) / 255.f;
+                float a = wgt * 0.2f;
+                f3 res = (a * vv + (1 - wgt * 0.2f) * old) * 255.f;
+                prev.color[0] = f2u8(res.x); prev.color[1] = f2u8(res.y); prev.color[2] = f2u8(res.z);
+              }
+            } else {
+              prev.count = (uint8_t)std::min(255, prev.count + 1);
+            }
+          }
+        }
+  }
+}
+
+extern "C" unsigned sfo_fuse(sfo_map *m, const float *depth, const uint8_t *rgb,
+                             const float *nmap, const uint8_t *mask,
+                             int num_detection, int cols, int rows, const float *R,
+                             const float *Rinv, const float *t, float fx, float fy,
+                             float cx, float cy) {
+  sfo_alloc(m, depth, cols, rows, R, t, fx, fy, cx, cy);
+  unsigned n = sfo_visibility(m, R, Rinv, t, cols, rows, fx, fy, cx, cy, m->c.depth_max, m->c.depth_min);
+  if (n == 0) return 0;
+  sfo_integrate(m, depth, rgb, cols, rows, Rinv, t, fx, fy, cx, cy, m->c.depth_max, m->c.depth_min);
+  if (num_detection > 0)
+    sfo_semantics(m, depth, rgb, nmap, mask, num_detection, cols, rows, Rinv, t, fx, fy, cx, cy,
+                  m->c.depth_max, m->c.depth_min);
+  return n;
+}
+
+namespace {
+struct RBlock { int16_t ulx, uly, lrx, lry; float zmin, zmax; };
+// Projection::projectBlock, RenderScene.cu:54-112.
+bool project_block(const sfo_map &m, i3 pos, const m3 &Rinv, f3 t, float fx, float fy, float cx,
+                   float cy, int zc, int zr, float dmax, float dmin, RBlock &b) {
+  b.ulx = (int16_t)zc; b.uly = (int16_t)zr; b.lrx = -1; b.lry = -1;
+  b.zmin = dmax; b.zmax = dmin;
+  for (int corner = 0; corner < 8; ++corner) {
+    i3 tmp = pos;
+    tmp.x += (corner & 1) ? 1 : 0;
+    tmp.y += (corner & 2) ? 1 : 0;
+    tmp.z += (corner & 4) ? 1 : 0;
+    f3 p3 = {(float)(int)((uint32_t)tmp.x * 8u) * m.c.voxel_size,
+             (float)(int)((uint32_t)tmp.y * 8u) * m.c.voxel_size,
+             (float)(int)((uint32_t)tmp.z * 8u) * m.c.voxel_size};
+    p3 = mul(Rinv, p3 - t);
+    if ((double)p3.z < 2e-1) continue;
+    float px = (fx * p3.x / p3.z + cx) / 8.0f;
+    float py = (fy * p3.y / p3.z + cy) / 8.0f;
+    if ((float)b.ulx > std::floor(px)) b.ulx = (int16_t)f2i(std::floor(px));
+    if ((float)b.lrx < std::ceil(px)) b.lrx = (int16_t)f2i(std::ceil(px));
+    if ((float)b.uly > std::floor(py)) b.uly = (int16_t)f2i(std::floor(py));
+    if ((float)b.lry < std::ceil(py)) b.lry = (int16_t)f2i(std::ceil(py));
+    if (b.zmin > p3.z) b.zmin = p3.z;
+    if (b.zmax < p3.z) b.zmax = p3.z;
+  }
+  if (b.ulx < 0) b.ulx = 0;
+  if (b.uly < 0) b.uly = 0;
+  if (b.lrx >= zc) b.lrx = (int16_t)(zc - 1);
+  if (b.lry >= zr) b.lry = (int16_t)(zr - 1);
+  if (b.ulx > b.lrx) return false;
+  if (b.uly > b.lry) return false;
+  if (b.zmin < dmin) b.zmin = dmin;
+  if (b.zmax < dmin) return false;
+  return true;
+}
+}  // namespace
+
+// Projection::operator() + createRenderingBlockList + fillBlocks,
+// RenderScene.cu:114-190, and CreateRenderingBlocks :210-289.  Each
+// visible block lays down the tiles (y < ny, x < ny) of
+// createRenderingBlockList (its x < ny bound and the un-offset lowerRight
+// kept), each tile filled as fillBlocks does; blocks do not overwrite each
+// other's list slots and no slot beyond the count is filled.
+extern "C" int sfo_zrange(sfo_map *m, float *zmin, float *zmax, int zc, int zr,
+                          float depth_max, float depth_min, const float *Rinv,
+                          const float *t, float fx, float fy, float cx, float cy,
+                          void *blocks_out, int max_blocks, unsigned *nblocks) {
+  if (nblocks) *nblocks = 0;
+  if (m->noVisible == 0) return 0;
+  for (int i = 0; i < zc * zr; ++i) { zmin[i] = 100.f; zmax[i] = 0.f; }
+  m3 RI = m3_from(Rinv);
+  f3 tv = f3_from(t);
+  unsigned total = 0;
+  RBlock *out = (RBlock *)blocks_out;
+  for (unsigned k = 0; k < m->noVisible; ++k) {
+    const sfo_entry &e = m->visible[k];
+    if (e.ptr == -1) continue;
+    RBlock b;
+    if (!project_block(*m, {e.x, e.y, e.z}, RI, tv, fx, fy, cx, cy, zc, zr, depth_max, depth_min, b))
+      continue;
+    // RenderScene.cu:147-151: dx = (float)LR.x - UL.x + 1; __float2int_ru(dx/16)
+    float dx = (float)b.lrx - (float)b.ulx + 1.0f;
+    float dy = (float)b.lry - (float)b.uly + 1.0f;
+    int nx = f2i(std::ceil(dx / 16.0f)), ny = f2i(std::ceil(dy / 16.0f));
+    unsigned required = (unsigned)(nx * ny);
+    if (total + required >= m->c.max_rendering_blocks) continue;
+    unsigned slot = 0;
+    for (int y = 0; y < ny; ++y)
+      for (int x = 0; x < ny; ++x) {
+        RBlock tb;
+        tb.ulx = (int16_t)(b.ulx + x * 16);
+        tb.uly = (int16_t)(b.uly + y * 16);
+        tb.lrx = (int16_t)(b.ulx + 16);
+        tb.lry = (int16_t)(b.uly + 16);
+        if (tb.lrx > b.lrx) tb.lrx = b.lrx;
+        if (tb.lry > b.lry) tb.lry = b.lry;
+        tb.zmin = b.zmin; tb.zmax = b.zmax;
+        if (slot < required) {
+          if (out && (int)(total + slot) < max_blocks) out[total + slot] = tb;
+          ++slot;
+        }
+        for (int ty = 0; ty < 16; ++ty)
+          for (int tx = 0; tx < 16; ++tx) {
+            int xpos = tb.ulx + tx, ypos = tb.uly + ty;
+            if (xpos > tb.lrx || xpos >= zc) continue;
+            if (ypos > tb.lry || ypos >= zr) continue;
+            float &a = zmin[ypos * zc + xpos];
+            float &c2 = zmax[ypos * zc + xpos];
+            a = std::fmin(tb.zmin, a);
+            c2 = std::fmax(tb.zmax, c2);
+          }
+      }
+    for (; slot < required; ++slot) {
+      RBlock eb{1, 1, 0, 0, b.zmin, b.zmax};
+      if (out && (int)(total + slot) < max_blocks) out[total + slot] = eb;
+    }
+    total += required;
+  }
+  if (nblocks) *nblocks = total;
+  return total > 0;
+}
+
+namespace {
+// Rendering (RenderScene.cu:291-489) with DeviceMap::FindVoxel's per-ray
+// entry cache (DeviceMap.cu:116-133).  The reference's cache starts as
+// HashEntry() = {pos (0,0,0), ptr -1}; a ray entering block (0,0,0) before
+// any other block would read voxelBlocks[idx - 1].  Here the cache starts
+// empty, so such a lookup goes to the hash table.
+struct RayCache { i3 pos; int ptr; bool set; };
+struct VoxelRead { float sdf; uint8_t weight; };
+
+inline VoxelRead find_voxel(const sfo_map &m, f3 pt, RayCache &cache, bool &valid) {
+  i3 p = floor3(pt);
+  i3 bp = vox2block(p);
+  if (cache.set && bp.x == cache.pos.x && bp.y == cache.pos.y && bp.z == cache.pos.z) {
+    valid = true;
+    const sfo_voxel &v = m.voxels[(size_t)cache.ptr + vox2local(p)];
+    return {v.sdf, v.weight};
+  }
+  const sfo_entry *e = find_entry(m, bp);
+  if (!e) { valid = false; return {kNaN, 0}; }
+  valid = true;
+  cache.pos = bp; cache.ptr = e->ptr; cache.set = true;
+  const sfo_voxel &v = m.voxels[(size_t)e->ptr + vox2local(p)];
+  return {v.sdf, v.weight};
+}
+inline float read_sdf(const sfo_map &m, f3 pt, RayCache &c, bool &valid) {
+  VoxelRead v = find_voxel(m, pt, c, valid);
+  if (v.weight == 0) valid = false;
+  return v.sdf;
+}
+inline float read_sdf_interp(const sfo_map &m, f3 pt, RayCache &c, bool &valid) {
+  f3 fl = {std::floor(pt.x), std::floor(pt.y), std::floor(pt.z)};
+  f3 xyz = pt - fl;
+  float s0, s1, r0, r1, r2, r3;
+  s0 = find_voxel(m, pt, c, valid).sdf;
+  s1 = find_voxel(m, pt + mk3(1, 0, 0), c, valid).sdf;
+  r0 = (1.0f - xyz.x) * s0 + xyz.x * s1;
+  s0 = find_voxel(m, pt + mk3(0, 1, 0), c, valid).sdf;
+  s1 = find_voxel(m, pt + mk3(1, 1, 0), c, valid).sdf;
+  r1 = (1.0f - xyz.x) * s0 + xyz.x * s1;
+  r2 = (1.0f - xyz.y) * r0 + xyz.y * r1;
+  s0 = find_voxel(m, pt + mk3(0, 0, 1), c, valid).sdf;
+  s1 = find_voxel(m, pt + mk3(1, 0, 1), c, valid).sdf;
+  r0 = (1.0f - xyz.x) * s0 + xyz.x * s1;
+  s0 = find_voxel(m, pt + mk3(0, 1, 1), c, valid).sdf;
+  s1 = find_voxel(m, pt + mk3(1, 1, 1), c, valid).sdf;
+  r1 = (1.0f - xyz.x) * s0 + xyz.x * s1;
+  r3 = (1.0f - xyz.y) * r0 + xyz.y * r1;
+  return (1.0f - xyz.z) * r2 + xyz.z * r3;
+}
+inline bool read_normal(const sfo_map &m, f3 pt, RayCache &c, const m3 &Rinv, f3 &n) {
+  bool valid;
+  float s[6];
+  const f3 offs[6] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+  for (int k = 0; k < 6; ++k) {
+    s[k] = read_sdf_interp(m, pt + offs[k], c, valid);
+    if (std::isnan(s[k]) || s[k] == 1.0f || !valid) return false;
+  }
+  n = mk3(s[0] - s[1], s[2] - s[3], s[4] - s[5]);
+  n = normalised(mul(Rinv, n));
+  return true;
+}
+}  // namespace
+
+extern "C" void sfo_raycast(sfo_map *m, float *vmap, float *nmap, int cols, int rows,
+                            const float *zmin, const float *zmax, int zc, int zr,
+                            const float *R, const float *Rinv, const float *t,
+                            float invfx, float invfy, float cx, float cy) {
+  m3 Rv = m3_from(R), RI = m3_from(Rinv);
+  f3 tv = f3_from(t);
+  const float vsi = m->voxelSizeInv;
+  (void)zr;
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int y = 0; y < rows; ++y)
+    for (int x = 0; x < cols; ++x) {
+      float *vo = vmap + 4 * (y * cols + x), *no = nmap + 4 * (y * cols + x);
+      vo[0] = vo[1] = vo[2] = vo[3] = kNaN;
+      no[0] = no[1] = no[2] = no[3] = kNaN;
+      int lx = f2i(std::floor((float)x / 8.0f)), ly = f2i(std::floor((float)y / 8.0f));
+      float zx = zmin[ly * zc + lx], zy = zmax[ly * zc + lx];
+      if ((double)zy < 1e-3 || (double)zx < 1e-3 || std::isnan(zx) || std::isnan(zy)) continue;
+      float sdf = 1.0f;
+      f3 p;
+      p.z = zx;
+      p.x = p.z * ((float)x - cx) * invfx;
+      p.y = p.z * ((float)y - cy) * invfy;
+      float dist_s = norm(p) * vsi;
+      f3 block_s = (mul(Rv, p) + tv) * vsi;
+      p.z = zy;
+      p.x = p.z * ((float)x - cx) * invfx;
+      p.y = p.z * ((float)y - cy) * invfy;
+      float dist_e = norm(p) * vsi;
+      f3 block_e = (mul(Rv, p) + tv) * vsi;
+      f3 dir = normalised(block_e - block_s);
+      f3 result = block_s;
+      bool valid_sdf = false, found_pt = false, behind = false;
+      float step, prev_sdf;
+      RayCache cache{{0, 0, 0}, -1, false};
+      while (dist_s < dist_e) {
+        prev_sdf = sdf;
+        sdf = read_sdf(*m, result, cache, valid_sdf);
+        if (!valid_sdf) {
+          step = 8.0f;
+        } else {
+          if (sdf <= 0.1f && sdf >= -0.5f) sdf = read_sdf_interp(*m, result, cache, valid_sdf);
+          if (prev_sdf < 0.f && sdf >= 0.f) { behind = true; break; }
+          if (prev_sdf > 0.f && sdf <= 0.f) break;
+          step = 1.0f;
+        }
+        result = result + step * dir;
+        dist_s += step;
+      }
+      if (behind) continue;
+      if (sdf <= 0.0f) {
+        step = sdf * m->stepScale;
+        result = result + step * dir;
+        sdf = read_sdf_interp(*m, result, cache, valid_sdf);
+        step = sdf * m->stepScale;
+        result = result + step * dir;
+        found_pt = true;
+      }
+      if (found_pt) {
+        f3 n;
+        if (read_normal(*m, result, cache, RI, n)) {
+          f3 r = mul(RI, result * m->c.voxel_size - tv);
+          vo[0] = r.x; vo[1] = r.y; vo[2] = r.z; vo[3] = 1.0f;
+          no[0] = n.x; no[1] = n.y; no[2] = n.z; no[3] = 1.0f;
+        }
+      }
+    }
+}
+
+// =============================================================== whole loop
+struct sfo_frame {
+  std::vector<float> raw;
+  std::vector<std::vector<float>> depth, vmap, nmap;
+  double pose[16];
+};
+struct sfo_system {
+  sfo_map *map = nullptr;
+  int cols, rows, levels;
+  float K[4], depth_scale, cutoff, icp_thresh;
+  std::vector<int> iters, min_count;
+  sfo_frame fa, fb;
+  sfo_frame *next = &fa, *last = &fb;
+  int state = 1;  // 1 = init, 0 = tracking (Tracking.cc:65-119)
+  double init_pose[16];
+  std::vector<float> zmin, zmax;
+  int zc, zr;
+};
+
+namespace {
+void frame_alloc(sfo_frame &f, int cols, int rows, int L) {
+  f.raw.assign((size_t)cols * rows, 0);
+  f.depth.resize(L); f.vmap.resize(L); f.nmap.resize(L);
+  for (int l = 0; l < L; ++l) {
+    size_t n = (size_t)(cols >> l) * (rows >> l);
+    f.depth[l].assign(n, 0); f.vmap[l].assign(4 * n, 0); f.nmap[l].assign(4 * n, 0);
+  }
+}
+// Frame::FillImages depth part, Core/Frame.cc:68-92.
+void fill_images(sfo_system *s, sfo_frame &f, const uint16_t *d) {
+  sfo_filter_depth(d, s->cols, s->rows, s->depth_scale, s->cutoff, f.raw.data(), f.depth[0].data());
+  for (int l = 1; l < s->levels; ++l)
+    sfo_pyrdown(f.depth[l - 1].data(), s->cols >> (l - 1), s->rows >> (l - 1), f.depth[l].data(),
+                s->cols >> l, s->rows >> l);
+  for (int l = 0; l < s->levels; ++l) {
+    float div = (float)(1 << l);
+    sfo_vmap(f.depth[l].data(), s->cols >> l, s->rows >> l, s->K[0] / div, s->K[1] / div,
+             s->K[2] / div, s->K[3] / div, s->cutoff, f.vmap[l].data());
+    sfo_nmap(f.vmap[l].data(), s->cols >> l, s->rows >> l, f.nmap[l].data());
+  }
+}
+// Frame::ResizeImages, Core/Frame.cc:94-98.
+void resize_images(sfo_system *s, sfo_frame &f) {
+  for (int l = 1; l < s->levels; ++l)
+    sfo_resize(f.vmap[l - 1].data(), f.nmap[l - 1].data(), s->cols >> (l - 1), s->rows >> (l - 1),
+               f.vmap[l].data(), f.nmap[l].data(), s->cols >> l, s->rows >> l);
+}
+}  // namespace
+
+extern "C" sfo_system *sfo_system_create(const sfo_config *cfg, int cols, int rows,
+                                         int levels, const float *K, float depth_scale,
+                                         float depth_cutoff, const int *iters,
+                                         const int *min_count, float icp_thresh,
+                                         const double *init_pose) {
+  sfo_system *s = new sfo_system();
+  s->map = sfo_map_create(cfg);
+  s->cols = cols; s->rows = rows; s->levels = levels;
+  memcpy(s->K, K, sizeof(s->K));
+  s->depth_scale = depth_scale; s->cutoff = depth_cutoff; s->icp_thresh = icp_thresh;
+  s->iters.assign(iters, iters + levels);
+  s->min_count.assign(min_count, min_count + levels);
+  frame_alloc(s->fa, cols, rows, levels);
+  frame_alloc(s->fb, cols, rows, levels);
+  for (int k = 0; k < 16; ++k) s->init_pose[k] = init_pose ? init_pose[k] : (k % 5 == 0 ? 1.0 : 0.0);
+  s->zc = (cols + 7) / 8; s->zr = (rows + 7) / 8;
+  s->zmin.assign((size_t)s->zc * s->zr, 0); s->zmax.assign((size_t)s->zc * s->zr, 0);
+  return s;
+}
+extern "C" void sfo_system_destroy(sfo_system *s) { sfo_map_destroy(s->map); delete s; }
+extern "C" sfo_map *sfo_system_map(sfo_system *s) { return s->map; }
+extern "C" const float *sfo_system_vmap(sfo_system *s, int l) { return s->last->vmap[l].data(); }
+extern "C" const float *sfo_system_nmap(sfo_system *s, int l) { return s->last->nmap[l].data(); }
+
+// System::GrabImage (Core/System.cc:131-270) with Tracker::GrabFrame /
+// Track / TrackFrame (Tracking.cc:65-173,246-280): icp-only tracking, no
+// keyframes / SURF / relocalisation (a lost frame is skipped and the next
+// frame is tracked against the same model).
+extern "C" int sfo_system_grab(sfo_system *s, const uint16_t *depth, const uint8_t *rgb,
+                               const uint8_t *mask, int num_detection, double *pose_out,
+                               double *stats) {
+  resize_images(s, *s->last);
+  fill_images(s, *s->next, depth);
+  int tracked = 1;
+  double st[4] = {0, 0, 0, 0};
+  if (s->state == 1) {
+    memcpy(s->next->pose, s->init_pose, sizeof(s->init_pose));
+    std::swap(s->next, s->last);
+    s->state = 0;
+  } else {
+    memcpy(s->next->pose, s->last->pose, sizeof(s->last->pose));
+    std::vector<int> cols(s->levels), rows(s->levels);
+    std::vector<const float *> vn(s->levels), nn(s->levels), vl(s->levels), nl(s->levels);
+    for (int l = 0; l < s->levels; ++l) {
+      cols[l] = s->cols >> l; rows[l] = s->rows >> l;
+      vn[l] = s->next->vmap[l].data(); nn[l] = s->next->nmap[l].data();
+      vl[l] = s->last->vmap[l].data(); nl[l] = s->last->nmap[l].data();
+    }
+    tracked = sfo_compute_se3(s->levels, cols.data(), rows.data(), vn.data(), nn.data(), vl.data(),
+                              nl.data(), s->K, s->iters.data(), s->min_count.data(), s->icp_thresh,
+                              s->last->pose, s->next->pose, 0, st);
+    if (tracked) std::swap(s->next, s->last);
+  }
+  unsigned nvis = 0;
+  if (tracked) {
+    sfo_frame &f = *s->last;
+    float R[9], RI[9], t[3];
+    pose_to_gpu(f.pose, R, RI, t);
+    nvis = sfo_fuse(s->map, f.raw.data(), rgb, f.nmap[0].data(), mask, num_detection, s->cols,
+                    s->rows, R, RI, t, s->K[0], s->K[1], s->K[2], s->K[3]);
+    // Mapping::RayTrace (Mapping.cc:142-161): raycast only if the z-range
+    // pass produced rendering blocks; else vmap[0]/nmap[0] keep the
+    // measured maps.
+    if (sfo_zrange(s->map, s->zmin.data(), s->zmax.data(), s->zc, s->zr, s->map->c.depth_max,
+                   s->map->c.depth_min, RI, t, s->K[0], s->K[1], s->K[2], s->K[3], nullptr, 0,
+                   nullptr)) {
+      sfo_raycast(s->map, f.vmap[0].data(), f.nmap[0].data(), s->cols, s->rows, s->zmin.data(),
+                  s->zmax.data(), s->zc, s->zr, R, RI, t, (float)(1.0 / (double)s->K[0]),
+                  (float)(1.0 / (double)s->K[1]), s->K[2], s->K[3]);
+    }
+  }
+  if (pose_out) memcpy(pose_out, s->last->pose, sizeof(s->last->pose));
+  if (stats) {
+    int c[4];
+    sfo_map_counters(s->map, c);
+    stats[0] = st[0]; stats[1] = st[1]; stats[2] = st[2]; stats[3] = st[3];
+    stats[4] = nvis; stats[5] = c[0]; stats[6] = c[1]; stats[7] = c[3];
+  }
+  return tracked;
+}

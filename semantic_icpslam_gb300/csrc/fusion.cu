@@ -1,0 +1,611 @@
+// Voxel-block hash allocation, visible-block compaction and TSDF / weight /
+// colour / label integration.
+//
+// Reference: Mapping/DeviceMap.cu (Hash :3-10, CreateEntry :12-21,
+// CreateBlock :23-69, FindEntry :141-154), Mapping/FuseMap.cu
+// (CreateBlocks :92-132, CheckFullVisibility :134-168, createVoxels
+// :432-507, analyzeSemantics :509-668, ResetHash/ResetSdfBlock
+// :1251-1304) and Utility/ParallelScan.h (ComputeOffset).
+//
+// GB300 form:
+//  * Allocation is two lock-free passes.  Probe: every raw-depth pixel walks
+//    its truncation segment; a block missing from the table is entered once
+//    into an epoch-tagged request set (64-bit CAS) and pushed onto its
+//    bucket's request list (atomicExch).  Insert: one thread per bucket with
+//    requests runs the reference's CreateBlock serially for that bucket's
+//    requests, so no allocation is lost to the bucket mutex race and no
+//    block is entered twice; heap pops (atomicSub) and excess slots
+//    (atomicAdd) are the reference's.
+//  * An index of allocated entries replaces the full-table scan of
+//    CheckFullVisibility; visible entries are appended with one atomic per
+//    warp.  The z-range tiles of the raycast (Projection + fillBlocks) are
+//    laid down in the same pass.
+//  * Integration is a persistent grid over the visible list, one voxel per
+//    thread with 128-bit loads and stores; label fusion runs on the same
+//    voxel in the same pass.
+#include "sf_kernels.cuh"
+#include "sf_render.cuh"
+
+namespace sf {
+
+MapConst make_map_const(const sf_map_config &cfg) {
+  MapConst c;
+  c.voxel_size = cfg.voxel_size;
+  c.voxel_size_inv = (float)(1.0 / (double)cfg.voxel_size);  // DeviceMap.h:186
+  c.block_width = cfg.voxel_size * 8.0f;                     // :187
+  c.trunc_dist = cfg.trunc_dist;
+  c.step_scale = (float)(0.5 * (double)cfg.trunc_dist * (double)c.voxel_size_inv);  // :189
+  c.depth_min = cfg.depth_min;
+  c.depth_max = cfg.depth_max;
+  c.num_buckets = cfg.num_buckets;
+  c.num_excess = cfg.num_excess;
+  c.num_sdf_blocks = cfg.num_sdf_blocks;
+  c.num_entries = cfg.num_buckets + cfg.num_excess;
+  c.max_rendering_blocks = cfg.max_rendering_blocks;
+  return c;
+}
+
+namespace {
+
+__device__ __forceinline__ unsigned grid_tid() { return blockIdx.x * blockDim.x + threadIdx.x; }
+__device__ __forceinline__ unsigned grid_stride() { return gridDim.x * blockDim.x; }
+
+// Warp-aggregated append: one atomicAdd per warp for the lanes in `active`.
+__device__ __forceinline__ unsigned warp_append(unsigned *counter, bool want) {
+  unsigned mask = __ballot_sync(__activemask(), want);
+  if (!want) return 0;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(mask) - 1;
+  unsigned base = 0;
+  if (lane == leader) base = atomicAdd(counter, (unsigned)__popc(mask));
+  base = __shfl_sync(mask, base, leader);
+  return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+// ---------------------------------------------------------------- reset
+__global__ void k_reset_entries(DevMap m, int *bucket_head) {
+  for (unsigned i = grid_tid(); i < m.c.num_entries; i += grid_stride()) {
+    int4 *e = (int4 *)(m.entries + i);
+    e[0] = make_int4(0, 0, 0, -1);
+    e[1] = make_int4(0, 0, 0, 0);
+    int4 *v = (int4 *)(m.visible + i);
+    v[0] = make_int4(0, 0, 0, -1);
+    v[1] = make_int4(0, 0, 0, 0);
+    if (i < m.c.num_buckets) {
+      m.bucket_mutex[i] = -1;
+      if (bucket_head) bucket_head[i] = -1;
+    }
+  }
+}
+
+// ResetSdfBlockKernel (FuseMap.cu:1268-1289): heap[x] = N-1-x and every
+// voxel released (sdf NaN, all counters 0; obj_idx is left as is).
+__global__ void k_reset_voxels(DevMap m) {
+  const size_t nvox = (size_t)m.c.num_sdf_blocks * 512;
+  for (size_t i = grid_tid(); i < nvox; i += grid_stride()) {
+    uint4 *p = (uint4 *)(m.voxels + i);
+    uint4 v = *p;
+    v.x = 0x7fffffffu;
+    v.y = 0u;
+    v.z = 0u;
+    v.w &= 0xff000000u;
+    *p = v;
+    if (i < m.c.num_sdf_blocks) m.heap[i] = (int)m.c.num_sdf_blocks - (int)i - 1;
+  }
+  if (grid_tid() == 0) {
+    *m.heap_counter = (int)m.c.num_sdf_blocks - 1;
+    *m.entry_ptr = 1;
+    *m.alloc_count = 0;
+    *m.no_visible = 0;
+  }
+}
+
+__global__ void k_rebuild_index(DevMap m) {
+  for (unsigned i = grid_tid(); i < m.c.num_entries; i += grid_stride()) {
+    int ptr = m.entries[i].ptr;
+    bool alloc = ptr >= 0;
+    unsigned slot = warp_append((unsigned *)m.alloc_count, alloc);
+    if (alloc) m.alloc_list[slot] = (int)i;
+  }
+}
+
+// ------------------------------------------------------------ allocation
+constexpr int kProbeLimit = 128;
+
+__device__ __forceinline__ unsigned long long req_key(i3 p, unsigned epoch) {
+  return ((unsigned long long)(epoch & 0xffffu) << 48) |
+         ((unsigned long long)((unsigned)p.x & 0xffffu) << 32) |
+         ((unsigned long long)((unsigned)p.y & 0xffffu) << 16) | (unsigned long long)((unsigned)p.z & 0xffffu);
+}
+
+// Enters p into the request set.  Returns 1 if this thread entered it
+// first, 0 if it was already requested this epoch, -1 if the set is full.
+__device__ int request_once(const FuseScratch &f, i3 p, unsigned epoch) {
+  const unsigned long long key = req_key(p, epoch);
+  uint32_t h = ((uint32_t)p.x * 0x9E3779B1u) ^ ((uint32_t)p.y * 0x85EBCA77u) ^ ((uint32_t)p.z * 0xC2B2AE3Du);
+  h ^= h >> 15;
+  const uint32_t mask = f.req_cap - 1;
+  uint32_t idx = h & mask;
+  for (int k = 0; k < kProbeLimit; ++k) {
+    unsigned long long cur = __ldcg(f.req_set + idx);
+    if (cur == key) return 0;
+    if ((unsigned)(cur >> 48) != (epoch & 0xffffu)) {
+      unsigned long long prev = atomicCAS(f.req_set + idx, cur, key);
+      if (prev == cur) return 1;
+      if (prev == key) return 0;
+    }
+    idx = (idx + 1) & mask;
+  }
+  return -1;
+}
+
+// Fusion::CreateBlocks (FuseMap.cu:92-132), probe pass.
+__global__ void k_alloc_probe(DevMap m, FuseScratch f, sf_image depth, const Cam *cam,
+                              const int *run_flag, uint32_t *flags) {
+  if (run_flag && *run_flag == 0) return;
+  const Cam c = *cam;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= depth.cols || y >= depth.rows) return;
+  const float dmin = m.c.depth_min, dmax = m.c.depth_max;
+  float z = row_ptr<const float>(depth, y)[x];
+  if (isnan(z) || z < dmin || z > dmax) return;
+  const float thresh = m.c.trunc_dist / 2.0f;
+  float z_near = fmaxf(dmin, z - thresh);
+  float z_far = fminf(dmax, z + thresh);
+  if (z_near >= z_far) return;
+  f3 pn = mk3(z_near * ((float)x - c.cx) * c.invfx, z_near * ((float)y - c.cy) * c.invfy, z_near);
+  f3 pf = mk3(z_far * ((float)x - c.cx) * c.invfx, z_far * ((float)y - c.cy) * c.invfy, z_far);
+  f3 pt_near = (mul(c.R, pn) + c.t) * m.c.voxel_size_inv;
+  f3 pt_far = (mul(c.R, pf) + c.t) * m.c.voxel_size_inv;
+  f3 dir = pt_far - pt_near;
+  float length = norm(dir);
+  // A non-finite pose would make the walk unbounded; such a pixel is skipped.
+  if (!(length < 65536.0f)) return;
+  // (int)ceil(2.0 * length): 2*length is exact in float.
+  int nSteps = (int)ceilf(2.0f * length);
+  dir = dir / (float)(nSteps - 1);
+  const unsigned epoch = f.counters[2];
+  i3 last;
+  last.x = 0x7fffffff; last.y = 0; last.z = 0;
+  for (int i = 0; i < nSteps; ++i) {
+    i3 bp = vox2block(floor3(pt_near));
+    pt_near = pt_near + dir;
+    if (bp.x == last.x && bp.y == last.y && bp.z == last.z) continue;
+    last = bp;
+    if (find_block(m, bp) >= 0) continue;
+    if (bp.x < -32767 || bp.x > 32767 || bp.y < -32767 || bp.y > 32767 || bp.z < -32767 ||
+        bp.z > 32767) {
+      atomicOr(flags, SF_FLAG_COORD_RANGE);
+      continue;
+    }
+    int r = request_once(f, bp, epoch);
+    if (r < 0) { atomicOr(flags, SF_FLAG_DEDUP_FULL); continue; }
+    if (r == 0) continue;
+    unsigned slot = atomicAdd(&f.counters[0], 1u);
+    if (slot >= f.pend_cap) { atomicOr(flags, SF_FLAG_PENDING_FULL); continue; }
+    int bucket = (int)hash_block(bp, m.c.num_buckets);
+    f.pending[slot] = make_int4(bp.x, bp.y, bp.z, bucket);
+    int prev = atomicExch(f.bucket_head + bucket, (int)slot);
+    f.pending_next[slot] = prev;
+    if (prev == -1) {
+      unsigned d = atomicAdd(&f.counters[1], 1u);
+      f.dirty[d] = bucket;  // d < pend_cap: one dirty bucket per pending slot at most
+    }
+  }
+}
+
+// DeviceMap::CreateEntry (DeviceMap.cu:12-21).
+__device__ __forceinline__ void create_entry(DevMap &m, i3 p, int offset, int4 &h0, int &off_out,
+                                             uint32_t *flags) {
+  int old = atomicSub(m.heap_counter, 1);
+  if (old >= 0) {
+    int ptr = m.heap[old];
+    if (ptr != -1) {
+      h0 = make_int4(p.x, p.y, p.z, ptr * 512);
+      off_out = offset;
+      return;
+    }
+  }
+  atomicOr(flags, SF_FLAG_HEAP_EMPTY);
+  h0 = make_int4(p.x, p.y, p.z, -1);
+  off_out = 0;
+}
+
+__device__ __forceinline__ void write_entry(DevMap &m, unsigned idx, int4 h0, int off) {
+  int4 *e = (int4 *)(m.entries + idx);
+  e[0] = h0;
+  e[1] = make_int4(off, 0, 0, 0);
+  if (h0.w >= 0) {
+    int slot = atomicAdd(m.alloc_count, 1);
+    m.alloc_list[slot] = (int)idx;
+  }
+}
+
+// DeviceMap::CreateBlock (DeviceMap.cu:23-69) for one bucket, serially.
+__device__ void create_block_serial(DevMap &m, i3 p, uint32_t bucket, uint32_t *flags) {
+  unsigned idx = bucket;
+  int4 h = entry_head(m.entries + idx);
+  if (h.x == p.x && h.y == p.y && h.z == p.z && h.w != -1) return;
+  int empty = (h.w == -1) ? (int)idx : -1;
+  int off = m.entries[idx].offset;
+  unsigned last = idx;
+  int guard = 0;
+  while (off > 0) {
+    idx = m.c.num_buckets + (unsigned)off - 1u;
+    h = entry_head(m.entries + idx);
+    if (h.x == p.x && h.y == p.y && h.z == p.z && h.w != -1) return;
+    if (h.w == -1 && empty < 0) empty = (int)idx;
+    last = idx;
+    off = m.entries[idx].offset;
+    if (++guard > (int)m.c.num_excess) return;
+  }
+  int4 h0;
+  int o;
+  if (empty >= 0) {
+    create_entry(m, p, m.entries[last].offset, h0, o, flags);
+    write_entry(m, (unsigned)empty, h0, o);
+  } else {
+    int offset = atomicAdd(m.entry_ptr, 1);
+    if (offset <= (int)m.c.num_excess) {
+      create_entry(m, p, 0, h0, o, flags);
+      write_entry(m, m.c.num_buckets + (unsigned)offset - 1u, h0, o);
+      m.entries[last].offset = offset;
+    } else {
+      atomicOr(flags, SF_FLAG_EXCESS_FULL);
+    }
+  }
+}
+
+__global__ void k_alloc_insert(DevMap m, FuseScratch f, const int *run_flag, uint32_t *flags) {
+  if (run_flag && *run_flag == 0) return;
+  const unsigned ndirty = min(f.counters[1], f.pend_cap);
+  for (unsigned d = grid_tid(); d < ndirty; d += grid_stride()) {
+    const int bucket = f.dirty[d];
+    int i = f.bucket_head[bucket];
+    int guard = 0;
+    while (i >= 0 && guard++ < (int)f.pend_cap) {
+      int4 q = f.pending[i];
+      i3 p;
+      p.x = q.x; p.y = q.y; p.z = q.z;
+      create_block_serial(m, p, (uint32_t)bucket, flags);
+      i = f.pending_next[i];
+    }
+    f.bucket_head[bucket] = -1;
+  }
+}
+
+// Clears the per-frame counters and advances the request epoch.  The
+// probe pass reads counters[2]; the epoch skips 0 (the empty-slot value).
+__global__ void k_alloc_begin(FuseScratch f, const int *run_flag) {
+  if (run_flag && *run_flag == 0) return;
+  f.counters[0] = 0;
+  f.counters[1] = 0;
+  unsigned e = (f.counters[2] + 1u) & 0xffffu;
+  if (e == 0) e = 1;
+  f.counters[2] = e;
+}
+
+// Clears the request set when the 16-bit epoch wraps (every 65535 frames).
+__global__ void k_clear_req(FuseScratch f) {
+  if (f.counters[2] != 1u) return;
+  for (unsigned i = grid_tid(); i < f.req_cap; i += grid_stride()) f.req_set[i] = 0ull;
+}
+
+// ------------------------------------------------------------ visibility
+// Fusion::CheckVertexVisibility (FuseMap.cu:46-56).
+__device__ __forceinline__ bool vertex_visible(const Cam &c, f3 p3) {
+  f3 pt = mul(c.Rinv, p3 - c.t);
+  if (pt.z < 1e-3f) return false;
+  float px = c.fx * pt.x / pt.z + c.cx;
+  float py = c.fy * pt.y / pt.z + c.cy;
+  return px >= 0 && py >= 0 && px < (float)c.cols && py < (float)c.rows && pt.z >= c.dmin &&
+         pt.z <= c.dmax;
+}
+
+// Fusion::CheckBlockVisibility (FuseMap.cu:58-90), corner walk order kept.
+__device__ __forceinline__ bool block_visible(const Cam &c, float s, i3 pos) {
+  f3 k = mk3((float)pos.x * s, (float)pos.y * s, (float)pos.z * s);
+  if (vertex_visible(c, k)) return true;
+  k.z += s; if (vertex_visible(c, k)) return true;
+  k.y += s; if (vertex_visible(c, k)) return true;
+  k.x += s; if (vertex_visible(c, k)) return true;
+  k.z -= s; if (vertex_visible(c, k)) return true;
+  k.y -= s; if (vertex_visible(c, k)) return true;
+  k.x -= s; k.y += s; if (vertex_visible(c, k)) return true;
+  k.x += s; k.y -= s; k.z += s; if (vertex_visible(c, k)) return true;
+  return false;
+}
+
+__global__ void k_visibility(DevMap m, const Cam *cam, sf_image zmin, sf_image zmax, int do_z,
+                             unsigned *rendered, const int *run_flag, uint32_t *flags) {
+  if (run_flag && *run_flag == 0) return;
+  const Cam c = *cam;
+  const unsigned n = (unsigned)*m.alloc_count;
+  // grid-stride with whole warps so warp_append sees converged lanes
+  for (unsigned base = blockIdx.x * blockDim.x; base < n; base += grid_stride()) {
+    const unsigned k = base + threadIdx.x;
+    bool vis = false;
+    int4 h0 = make_int4(0, 0, 0, -1);
+    int4 h1 = make_int4(0, 0, 0, 0);
+    unsigned idx = 0;
+    if (k < n) {
+      idx = (unsigned)m.alloc_list[k];
+      h0 = entry_head(m.entries + idx);
+      h1 = __ldcg((const int4 *)(m.entries + idx) + 1);
+      i3 pos; pos.x = h0.x; pos.y = h0.y; pos.z = h0.z;
+      vis = h0.w != -1 && block_visible(c, m.c.block_width, pos);
+    }
+    unsigned slot = warp_append(m.no_visible, vis);
+    if (vis) {
+      if (slot < m.c.num_entries) {
+        int4 *o = (int4 *)(m.visible + slot);
+        o[0] = h0;
+        o[1] = h1;
+      } else {
+        atomicOr(flags, SF_FLAG_VISIBLE_FULL);
+      }
+      if (do_z) {
+        sf_rendering_block b;
+        i3 pos; pos.x = h0.x; pos.y = h0.y; pos.z = h0.z;
+        if (project_block(pos, m.c.voxel_size, c.Rinv, c.t, c.fx, c.fy, c.cx, c.cy, zmin.cols,
+                          zmin.rows, m.c.depth_max, m.c.depth_min, b)) {
+          fill_block_tiles(b, zmin, zmax);
+          if (*rendered == 0u) atomicExch(rendered, 1u);
+        }
+      }
+    }
+  }
+}
+
+__global__ void k_zrange_init(sf_image zmin, sf_image zmax) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= zmin.cols || y >= zmin.rows) return;
+  row_ptr<float>(zmin, y)[x] = 100.f;
+  row_ptr<float>(zmax, y)[x] = 0.f;
+}
+
+__global__ void k_vis_begin(DevMap m, unsigned *rendered, const int *run_flag) {
+  if (run_flag && *run_flag == 0) return;
+  *m.no_visible = 0u;
+  if (rendered) *rendered = 0u;
+}
+
+// -------------------------------------------------------------- integrate
+union VoxelU {
+  uint4 u;
+  sf_voxel v;
+};
+
+// Fusion::createVoxels per voxel (FuseMap.cu:453-505).
+__device__ __forceinline__ bool integrate_voxel(sf_voxel &prev, float sdf, f3 val) {
+  if (prev.weight == 0) {
+    prev.sdf = sdf;
+    prev.weight = 1;
+    prev.color[0] = f2u8(val.x); prev.color[1] = f2u8(val.y); prev.color[2] = f2u8(val.z);
+    prev.label = 0; prev.count = 0; prev.label_2 = 0; prev.count_2 = 0;
+    prev.color_2[0] = 0; prev.color_2[1] = 0; prev.color_2[2] = 0;
+    return true;
+  }
+  if (prev.label == 0) {
+    // make_float3(color) * weight is operator*(float3,int) -> int3
+    // (VectorMath.h:231-233); int3 + float3 -> float3; / (w+1).
+    const int w = prev.weight;
+    float r0 = ((float)(int)((float)prev.color[0] * (float)w) + val.x) / (float)(w + 1);
+    float r1 = ((float)(int)((float)prev.color[1] * (float)w) + val.y) / (float)(w + 1);
+    float r2 = ((float)(int)((float)prev.color[2] * (float)w) + val.z) / (float)(w + 1);
+    prev.color[0] = f2u8(r0); prev.color[1] = f2u8(r1); prev.color[2] = f2u8(r2);
+  }
+  prev.sdf = (prev.sdf * (float)prev.weight + sdf) / (float)(prev.weight + 1);
+  prev.weight = (uint8_t)min(255, prev.weight + 1);
+  return true;
+}
+
+// Fusion::analyzeSemantics per voxel (FuseMap.cu:582-664).
+__device__ __forceinline__ void semantic_voxel(sf_voxel &prev, uint8_t label, f3 val, float4 nl,
+                                               f3 pos) {
+  if (prev.weight == 0) return;
+  if (label != 0) {
+    if (label == prev.label) {
+      prev.count = (uint8_t)min(255, prev.count + 1);
+      prev.color[0] = f2u8(val.x); prev.color[1] = f2u8(val.y); prev.color[2] = f2u8(val.z);
+    } else {
+      if (label == prev.label_2) {
+        prev.count_2 = (uint8_t)min(255, prev.count_2 + 1);
+        prev.color_2[0] = f2u8(val.x); prev.color_2[1] = f2u8(val.y); prev.color_2[2] = f2u8(val.z);
+      } else if (prev.count_2 < 7) {
+        prev.label_2 = label;
+        prev.count_2 = 1;
+        prev.color_2[0] = f2u8(val.x); prev.color_2[1] = f2u8(val.y); prev.color_2[2] = f2u8(val.z);
+      }
+      if ((prev.count < prev.count_2 && prev.label != 0) ||
+          (prev.count < prev.count_2 * 2 && prev.label == 0)) {
+        uint8_t t = prev.label; prev.label = prev.label_2; prev.label_2 = t;
+        t = prev.count; prev.count = prev.count_2; prev.count_2 = t;
+        for (int k = 0; k < 3; ++k) { t = prev.color[k]; prev.color[k] = prev.color_2[k]; prev.color_2[k] = t; }
+      }
+    }
+  } else {
+    // w = nl . normalised(make_float4(pos)) with the float4 norm.
+    float len = sqrtf(pos.x * pos.x + pos.y * pos.y + pos.z * pos.z + 1.0f * 1.0f);
+    float a0 = pos.x / len, a1 = pos.y / len, a2 = pos.z / len, a3 = 1.0f / len;
+    float w = nl.x * a0 + nl.y * a1 + nl.z * a2 + nl.w * a3;
+    if (prev.label != 0) {
+      if (prev.count < 7) {
+        prev.label_2 = prev.label;
+        prev.color_2[0] = prev.color[0]; prev.color_2[1] = prev.color[1]; prev.color_2[2] = prev.color[2];
+        prev.count_2 = prev.count;
+        prev.label = 0;
+        prev.count = 1;
+        f3 vv = val / 255.f;
+        f3 old = mk3((float)prev.color[0], (float)prev.color[1], (float)prev.color[2]) / 255.f;
+        float a = w * 0.2f;
+        f3 res = (a * vv + (1 - w * 0.2f) * old) * 255.f;
+        prev.color[0] = f2u8(res.x); prev.color[1] = f2u8(res.y); prev.color[2] = f2u8(res.z);
+      }
+    } else {
+      prev.count = (uint8_t)min(255, prev.count + 1);
+    }
+  }
+}
+
+constexpr int kIntThreads = 256;
+
+__global__ void __launch_bounds__(kIntThreads) k_integrate(DevMap m, sf_image depth, sf_image rgb,
+                                                           sf_image nmap, sf_image mask,
+                                                           int num_detection, const Cam *cam,
+                                                           int do_int, int do_sem,
+                                                           const int *run_flag) {
+  if (run_flag && *run_flag == 0) return;
+  const Cam c = *cam;
+  const unsigned nvis = min(*m.no_visible, m.c.num_entries);
+  const float thresh = m.c.trunc_dist;
+  const float voxel = m.c.voxel_size;
+  const int pal0 = 33554431, pal1 = 32767, pal2 = 2097151;  // 2^25-1, 2^15-1, 2^21-1 (FuseMap.cu:18)
+  for (unsigned b = blockIdx.x; b < nvis; b += gridDim.x) {
+    const int4 h = __ldcg((const int4 *)(m.visible + b));
+    if (h.w == -1) continue;
+    for (int li = threadIdx.x; li < 512; li += kIntThreads) {
+      const int lx = li & 7, ly = (li >> 3) & 7, lz = li >> 6;
+      f3 w3 = mk3((float)(h.x * 8 + lx) * voxel, (float)(h.y * 8 + ly) * voxel,
+                  (float)(h.z * 8 + lz) * voxel);
+      f3 pos = mul(c.Rinv, w3 - c.t);
+      int u = (int)(c.fx * pos.x / pos.z + c.cx);
+      int v = (int)(c.fy * pos.y / pos.z + c.cy);
+      if (u < 0 || v < 0 || u >= c.cols || v >= c.rows) continue;
+      float dp = __ldg(row_ptr<const float>(depth, v) + u);
+      if (isnan(dp) || dp > c.dmax || dp < c.dmin) continue;
+      float sdf = dp - pos.z;
+      if (!(sdf >= -thresh)) continue;
+      const uint8_t *px = row_ptr<const uint8_t>(rgb, v) + 3 * u;
+      uint4 *vp = (uint4 *)(m.voxels + h.w) + li;
+      VoxelU vx;
+      vx.u = *vp;
+      bool dirty = false;
+      if (do_int) {
+        f3 val = mk3((float)px[0], (float)px[1], (float)px[2]);
+        dirty = integrate_voxel(vx.v, fminf(1.0f, sdf / thresh), val);
+      }
+      if (do_sem) {
+        float4 nl = __ldg(row_ptr<const float4>(nmap, v) + u);
+        if (!isnan(nl.x)) {
+          uint8_t label;
+          f3 val;
+          if (num_detection > 0) {
+            label = __ldg(row_ptr<const uint8_t>(mask, v) + u);
+            if (label == 0) {
+              val = mk3((float)px[0], (float)px[1], (float)px[2]);
+            } else {
+              int p0 = (int)((unsigned)pal0 * (unsigned)label) % 255;
+              int p1 = (int)((unsigned)pal1 * (unsigned)label) % 255;
+              int p2 = (int)((unsigned)pal2 * (unsigned)label) % 255;
+              val = mk3((float)p0, (float)p1, (float)p2);
+            }
+          } else {
+            label = 0;
+            val = mk3((float)px[0], (float)px[1], (float)px[2]);
+          }
+          semantic_voxel(vx.v, label, val, nl, pos);
+          dirty = true;
+        }
+      }
+      if (dirty) *vp = vx.u;
+    }
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- host side
+int fuse_scratch_init(FuseScratch &f, const MapConst &c, int max_pixels) {
+  uint32_t want = 1;
+  while (want < (uint32_t)max_pixels * 2u && want < (1u << 24)) want <<= 1;
+  f.req_cap = want < (1u << 16) ? (1u << 16) : want;
+  f.pend_cap = f.req_cap / 2;
+  if (cudaMalloc(&f.req_set, sizeof(unsigned long long) * f.req_cap) != cudaSuccess) return SF_ERR_CUDA;
+  if (cudaMemset(f.req_set, 0, sizeof(unsigned long long) * f.req_cap) != cudaSuccess) return SF_ERR_CUDA;
+  if (cudaMalloc(&f.pending, sizeof(int4) * f.pend_cap) != cudaSuccess) return SF_ERR_CUDA;
+  if (cudaMalloc(&f.pending_next, sizeof(int) * f.pend_cap) != cudaSuccess) return SF_ERR_CUDA;
+  if (cudaMalloc(&f.dirty, sizeof(int) * f.pend_cap) != cudaSuccess) return SF_ERR_CUDA;
+  if (cudaMalloc(&f.bucket_head, sizeof(int) * c.num_buckets) != cudaSuccess) return SF_ERR_CUDA;
+  if (cudaMemset(f.bucket_head, 0xff, sizeof(int) * c.num_buckets) != cudaSuccess) return SF_ERR_CUDA;
+  if (cudaMalloc(&f.counters, sizeof(unsigned) * 4) != cudaSuccess) return SF_ERR_CUDA;
+  if (cudaMemset(f.counters, 0, sizeof(unsigned) * 4) != cudaSuccess) return SF_ERR_CUDA;
+  return SF_OK;
+}
+
+void fuse_scratch_free(FuseScratch &f) {
+  cudaFree(f.req_set);
+  cudaFree(f.pending);
+  cudaFree(f.pending_next);
+  cudaFree(f.dirty);
+  cudaFree(f.bucket_head);
+  cudaFree(f.counters);
+  f = FuseScratch();
+}
+
+static int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
+void launch_map_reset(const DevMap &m, cudaStream_t s) {
+  const int g = sm_count() * 8;
+  k_reset_entries<<<g, 256, 0, s>>>(m, nullptr);
+  k_reset_voxels<<<g, 256, 0, s>>>(m);
+}
+
+void launch_rebuild_index(const DevMap &m, cudaStream_t s) {
+  cudaMemsetAsync(m.alloc_count, 0, sizeof(int), s);
+  k_rebuild_index<<<sm_count() * 8, 256, 0, s>>>(m);
+}
+
+void launch_alloc(const DevMap &m, const FuseScratch &f, const sf_image &depth, const Cam *c,
+                  const int *run_flag, uint32_t *flags, cudaStream_t s) {
+  k_alloc_begin<<<1, 1, 0, s>>>(f, run_flag);
+  k_clear_req<<<sm_count() * 4, 256, 0, s>>>(f);
+  dim3 blk(32, 8);
+  dim3 grd((depth.cols + 31) / 32, (depth.rows + 7) / 8);
+  k_alloc_probe<<<grd, blk, 0, s>>>(m, f, depth, c, run_flag, flags);
+  k_alloc_insert<<<sm_count() * 2, 128, 0, s>>>(m, f, run_flag, flags);
+}
+
+void launch_zrange_init(const sf_image &zmin, const sf_image &zmax, cudaStream_t s) {
+  dim3 blk(32, 8);
+  dim3 grd((zmin.cols + 31) / 32, (zmin.rows + 7) / 8);
+  k_zrange_init<<<grd, blk, 0, s>>>(zmin, zmax);
+}
+
+void launch_visibility(const DevMap &m, const FuseScratch &f, const Cam *c, const sf_image *zmin,
+                       const sf_image *zmax, const int *run_flag, uint32_t *flags,
+                       cudaStream_t s) {
+  unsigned *rendered = f.counters + 3;
+  k_vis_begin<<<1, 1, 0, s>>>(m, rendered, run_flag);
+  sf_image zn = {}, zx = {};
+  if (zmin && zmax) {
+    launch_zrange_init(*zmin, *zmax, s);
+    zn = *zmin;
+    zx = *zmax;
+  }
+  k_visibility<<<sm_count() * 4, 256, 0, s>>>(m, c, zn, zx, (zmin && zmax) ? 1 : 0, rendered,
+                                              run_flag, flags);
+}
+
+void launch_integrate(const DevMap &m, const sf_image &depth, const sf_image &rgb,
+                      const sf_image *nmap, const sf_image *mask, int num_detection, const Cam *c,
+                      bool integrate, bool semantics, const int *run_flag, cudaStream_t s) {
+  sf_image nm = nmap ? *nmap : sf_image{};
+  sf_image mk = mask ? *mask : sf_image{};
+  const bool sem = semantics && nmap && (num_detection <= 0 || mask);
+  k_integrate<<<sm_count() * 8, kIntThreads, 0, s>>>(m, depth, rgb, nm, mk, num_detection, c,
+                                                     integrate ? 1 : 0, sem ? 1 : 0, run_flag);
+}
+
+}  // namespace sf

@@ -1,0 +1,218 @@
+// Depth pyramid: bilateral filter, Gaussian pyramid, vertex and normal maps,
+// and the 2x2 vertex/normal downsampling of the raycast maps.
+//
+// Reference: Tracking/Pyrdown.cu (FilterDepthKernel :72-108,
+// ComputeVMapKernel :123-145, ComputeNMapKernel :160-181,
+// PyrDownGaussKernel :201-225, ResizeMapKernel :318-346) driven by
+// Frame::FillImages / ResizeImages (Core/Frame.cc:68-98).
+//
+// GB300 layout: a pyramid level is two launches, not four: the vertex and
+// normal maps of a level come from one kernel that recomputes the two
+// neighbouring vertices from depth instead of round-tripping the vertex map
+// through memory.  All maps are dense (step = cols * sizeof), 16-byte
+// float4 stores are coalesced across a warp.
+#include "sf_kernels.cuh"
+
+namespace sf {
+
+__constant__ float c_gauss[25] = {1, 4, 6, 4, 1, 4, 16, 24, 16, 4, 6, 24, 36,
+                                  24, 6, 4, 16, 24, 16, 4, 1, 4, 6, 4, 1};
+
+// FilterDepthKernel (Pyrdown.cu:72-108).  sigSpace = 0.5/16, sigRange =
+// 0.5/0.25 (Pyrdown.cu:3-4).  The window's upper bound is exclusive, as in
+// the reference.
+__global__ void k_filter_depth(sf_image depth, sf_image raw, sf_image filt, float inv_scale,
+                               float cutoff) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= depth.cols || y >= depth.rows) return;
+  const float sig_space = 0.03125f, sig_range = 2.0f;
+  float center = (float)row_ptr<const uint16_t>(depth, y)[x] * inv_scale;
+  row_ptr<float>(raw, y)[x] = center < cutoff ? center : nanf_bits();
+  const int tx = min(x + 3, depth.cols - 1);
+  const int ty = min(y + 3, depth.rows - 1);
+  float sum1 = 0.f, sum2 = 0.f;
+  for (int cy = max(y - 2, 0); cy < ty; ++cy) {
+    const uint16_t *drow = row_ptr<const uint16_t>(depth, cy);
+    for (int cx = max(x - 2, 0); cx < tx; ++cx) {
+      float val = (float)__ldg(drow + cx) * inv_scale;
+      float space2 = (float)((x - cx) * (x - cx) + (y - cy) * (y - cy));
+      float color2 = (center - val) * (center - val);
+      float weight = expf(-(space2 * sig_space + color2 * sig_range));
+      sum1 += val * weight;
+      sum2 += weight;
+    }
+  }
+  float fin = sum1 / sum2;
+  row_ptr<float>(filt, y)[x] = fin < cutoff ? fin : nanf_bits();
+}
+
+// PyrDownGaussKernel<float,float> (Pyrdown.cu:201-225): NaN-skipping 5x5
+// Gaussian normalised by the used weights, reversed kernel index.
+__device__ __forceinline__ float pyrdown_px(const sf_image &src, int x, int y) {
+  const int tx = min(2 * x + 3, src.cols - 1);
+  const int ty = min(2 * y + 3, src.rows - 1);
+  float sum = 0.f;
+  int count = 0;
+  for (int cy = max(0, 2 * y - 2); cy < ty; ++cy) {
+    const float *srow = row_ptr<const float>(src, cy);
+    for (int cx = max(0, 2 * x - 2); cx < tx; ++cx) {
+      float v = __ldg(srow + cx);
+      if (!isnan(v)) {
+        float k = c_gauss[(ty - cy - 1) * 5 + (tx - cx - 1)];
+        sum += v * k;
+        count = (int)((float)count + k);
+      }
+    }
+  }
+  return sum / (float)count;
+}
+
+__global__ void k_pyrdown(sf_image src, sf_image dst) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= dst.cols || y >= dst.rows) return;
+  row_ptr<float>(dst, y)[x] = pyrdown_px(src, x, y);
+}
+
+// ComputeVMapKernel (Pyrdown.cu:123-145): z in (0.1, cutoff), 0.1 compared
+// in double as in the reference.
+__device__ __forceinline__ float4 vertex_at(const sf_image &depth, int x, int y, float invfx,
+                                            float invfy, float cx, float cy, float cutoff) {
+  float z = __ldg(row_ptr<const float>(depth, y) + x);
+  if (!isnan(z) && (double)z > 0.1 && z < cutoff) {
+    return make_float4(z * ((float)x - cx) * invfx, z * ((float)y - cy) * invfy, z, 1.0f);
+  }
+  return nan4();
+}
+
+// ComputeVMap + ComputeNMap fused (Pyrdown.cu:123-181).
+__global__ void k_vnmap(sf_image depth, sf_image vmap, sf_image nmap, float invfx, float invfy,
+                        float cx, float cy, float cutoff) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= depth.cols || y >= depth.rows) return;
+  float4 vc = vertex_at(depth, x, y, invfx, invfy, cx, cy, cutoff);
+  row_ptr<float4>(vmap, y)[x] = vc;
+  float4 n = nan4();
+  if (x != depth.cols - 1 && y != depth.rows - 1) {
+    float4 vr = vertex_at(depth, x + 1, y, invfx, invfy, cx, cy, cutoff);
+    float4 vd = vertex_at(depth, x, y + 1, invfx, invfy, cx, cy, cutoff);
+    if (!isnan(vc.x) && !isnan(vr.x) && !isnan(vd.x)) {
+      f3 a = mk3(vr.x - vc.x, vr.y - vc.y, vr.z - vc.z);
+      f3 b = mk3(vd.x - vc.x, vd.y - vc.y, vd.z - vc.z);
+      f3 q = normalised(cross(a, b));
+      n = make_float4(q.x, q.y, q.z, 1.0f);
+    }
+  }
+  row_ptr<float4>(nmap, y)[x] = n;
+}
+
+// Separate vertex-map and normal-map kernels for the reference-shaped
+// launchers (ComputeVMap / ComputeNMap).
+__global__ void k_vmap(sf_image depth, sf_image vmap, float invfx, float invfy, float cx, float cy,
+                       float cutoff) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= depth.cols || y >= depth.rows) return;
+  row_ptr<float4>(vmap, y)[x] = vertex_at(depth, x, y, invfx, invfy, cx, cy, cutoff);
+}
+
+__global__ void k_nmap(sf_image vmap, sf_image nmap) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= vmap.cols || y >= vmap.rows) return;
+  float4 n = nan4();
+  if (x != vmap.cols - 1 && y != vmap.rows - 1) {
+    float4 vc = row_ptr<const float4>(vmap, y)[x];
+    float4 vr = row_ptr<const float4>(vmap, y)[x + 1];
+    float4 vd = row_ptr<const float4>(vmap, y + 1)[x];
+    if (!isnan(vc.x) && !isnan(vr.x) && !isnan(vd.x)) {
+      f3 a = mk3(vr.x - vc.x, vr.y - vc.y, vr.z - vc.z);
+      f3 b = mk3(vd.x - vc.x, vd.y - vc.y, vd.z - vc.z);
+      f3 q = normalised(cross(a, b));
+      n = make_float4(q.x, q.y, q.z, 1.0f);
+    }
+  }
+  row_ptr<float4>(nmap, y)[x] = n;
+}
+
+// ResizeMapKernel (Pyrdown.cu:318-346): 2x2 mean, any NaN -> NaN; normals
+// normalised as float4 (w included in the norm, VectorMath.h:328-346).
+// Guarded on the destination size (the reference guards on the source).
+__global__ void k_resize(sf_image vsrc, sf_image nsrc, sf_image vdst, sf_image ndst) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= vdst.cols || y >= vdst.rows) return;
+  const float4 *v0 = row_ptr<const float4>(vsrc, 2 * y) + 2 * x;
+  const float4 *v1 = row_ptr<const float4>(vsrc, 2 * y + 1) + 2 * x;
+  const float4 *n0 = row_ptr<const float4>(nsrc, 2 * y) + 2 * x;
+  const float4 *n1 = row_ptr<const float4>(nsrc, 2 * y + 1) + 2 * x;
+  float4 a = v0[0], b = v0[1], c = v1[0], d = v1[1];
+  float4 out;
+  if (isnan(a.x) || isnan(b.x) || isnan(c.x) || isnan(d.x)) {
+    out = nan4();
+  } else {
+    out.x = (((a.x + b.x) + c.x) + d.x) / 4.0f;
+    out.y = (((a.y + b.y) + c.y) + d.y) / 4.0f;
+    out.z = (((a.z + b.z) + c.z) + d.z) / 4.0f;
+    out.w = (((a.w + b.w) + c.w) + d.w) / 4.0f;
+  }
+  row_ptr<float4>(vdst, y)[x] = out;
+  a = n0[0]; b = n0[1]; c = n1[0]; d = n1[1];
+  if (isnan(a.x) || isnan(b.x) || isnan(c.x) || isnan(d.x)) {
+    out = nan4();
+  } else {
+    float s0 = (((a.x + b.x) + c.x) + d.x) / 4.0f;
+    float s1 = (((a.y + b.y) + c.y) + d.y) / 4.0f;
+    float s2 = (((a.z + b.z) + c.z) + d.z) / 4.0f;
+    float s3 = (((a.w + b.w) + c.w) + d.w) / 4.0f;
+    float len = sqrtf(s0 * s0 + s1 * s1 + s2 * s2 + s3 * s3);
+    out = make_float4(s0 / len, s1 / len, s2 / len, s3 / len);
+  }
+  row_ptr<float4>(ndst, y)[x] = out;
+}
+
+// ------------------------------------------------------------- launchers
+static inline dim3 grid2d(int cols, int rows, dim3 blk) {
+  return dim3((cols + blk.x - 1) / blk.x, (rows + blk.y - 1) / blk.y);
+}
+
+void launch_filter_depth(const sf_image &depth, const sf_image &raw, const sf_image &filt,
+                         float depth_scale, float cutoff, cudaStream_t s) {
+  dim3 blk(32, 8);
+  const float inv = (float)(1.0 / (double)depth_scale);
+  k_filter_depth<<<grid2d(depth.cols, depth.rows, blk), blk, 0, s>>>(depth, raw, filt, inv, cutoff);
+}
+
+void launch_pyrdown(const sf_image &src, const sf_image &dst, cudaStream_t s) {
+  dim3 blk(32, 8);
+  k_pyrdown<<<grid2d(dst.cols, dst.rows, blk), blk, 0, s>>>(src, dst);
+}
+
+void launch_vnmap(const sf_image &depth, const sf_image &vmap, const sf_image &nmap, float fx,
+                  float fy, float cx, float cy, float cutoff, cudaStream_t s) {
+  dim3 blk(32, 8);
+  k_vnmap<<<grid2d(depth.cols, depth.rows, blk), blk, 0, s>>>(
+      depth, vmap, nmap, (float)(1.0 / (double)fx), (float)(1.0 / (double)fy), cx, cy, cutoff);
+}
+
+void launch_vmap(const sf_image &depth, const sf_image &vmap, float fx, float fy, float cx,
+                 float cy, float cutoff, cudaStream_t s) {
+  dim3 blk(32, 8);
+  k_vmap<<<grid2d(depth.cols, depth.rows, blk), blk, 0, s>>>(
+      depth, vmap, (float)(1.0 / (double)fx), (float)(1.0 / (double)fy), cx, cy, cutoff);
+}
+
+void launch_nmap(const sf_image &vmap, const sf_image &nmap, cudaStream_t s) {
+  dim3 blk(32, 8);
+  k_nmap<<<grid2d(vmap.cols, vmap.rows, blk), blk, 0, s>>>(vmap, nmap);
+}
+
+void launch_resize(const sf_image &vsrc, const sf_image &nsrc, const sf_image &vdst,
+                   const sf_image &ndst, cudaStream_t s) {
+  dim3 blk(32, 8);
+  k_resize<<<grid2d(vdst.cols, vdst.rows, blk), blk, 0, s>>>(vsrc, nsrc, vdst, ndst);
+}
+
+}  // namespace sf

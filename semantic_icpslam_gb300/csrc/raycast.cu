@@ -1,0 +1,276 @@
+// Rendering-block z-range and the block-skipping trilinear raycast.
+//
+// Reference: Mapping/RenderScene.cu (Projection :9-191,
+// CreateRenderingBlocks :210-289, Rendering :291-489, Raycast :495-537)
+// with DeviceMap::FindVoxel's per-ray entry cache (DeviceMap.cu:116-133).
+//
+// GB300 form: the per-frame path lays the z-range tiles down during the
+// visibility pass (fusion.cu), so no rendering-block list is materialised,
+// downloaded or re-read; the list form below serves the reference-shaped
+// CreateRenderingBlocks entry point.  Float z-ranges are positive, so the
+// reference's CAS-loop float min/max become single integer atomicMin/Max
+// on the bit patterns.  The raycast reads only the first 8 bytes of a
+// voxel (sdf, weight) per sample.
+#include "sf_kernels.cuh"
+#include "sf_render.cuh"
+
+namespace sf {
+
+
+namespace {
+
+// Projection::operator() (RenderScene.cu:134-165) in list form: each valid
+// block reserves nx*ny slots and fills them with the tiles (y < ny, x < ny)
+// of createRenderingBlockList (:114-132); reserved slots beyond ny*ny hold
+// empty tiles.
+__global__ void k_project_blocks(DevMap m, uint32_t nvis, const Cam *cam, int zc, int zr,
+                                 sf_rendering_block *list, uint32_t *count, uint32_t cap,
+                                 uint32_t *flags) {
+  const Cam c = *cam;
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < nvis; k += gridDim.x * blockDim.x) {
+    int4 h = __ldcg((const int4 *)(m.visible + k));
+    if (h.w == -1) continue;
+    i3 pos; pos.x = h.x; pos.y = h.y; pos.z = h.z;
+    sf_rendering_block b;
+    if (!project_block(pos, m.c.voxel_size, c.Rinv, c.t, c.fx, c.fy, c.cx, c.cy, zc, zr, c.dmax,
+                       c.dmin, b))
+      continue;
+    float dx = (float)b.lrx - (float)b.ulx + 1.0f;
+    float dy = (float)b.lry - (float)b.uly + 1.0f;
+    int nx = (int)ceilf(dx / 16.0f), ny = (int)ceilf(dy / 16.0f);
+    unsigned required = (unsigned)(nx * ny);
+    unsigned off = atomicAdd(count, required);
+    if (off + required >= cap) {
+      atomicOr(flags, SF_FLAG_RENDER_FULL);
+      atomicSub(count, required);
+      continue;
+    }
+    unsigned slot = 0;
+    for (int y = 0; y < ny && slot < required; ++y)
+      for (int x = 0; x < ny && slot < required; ++x) {
+        sf_rendering_block t;
+        t.ulx = (int16_t)(b.ulx + x * 16);
+        t.uly = (int16_t)(b.uly + y * 16);
+        t.lrx = (int16_t)(b.ulx + 16);
+        t.lry = (int16_t)(b.uly + 16);
+        if (t.lrx > b.lrx) t.lrx = b.lrx;
+        if (t.lry > b.lry) t.lry = b.lry;
+        t.zmin = b.zmin;
+        t.zmax = b.zmax;
+        list[off + slot++] = t;
+      }
+    for (; slot < required; ++slot) {
+      sf_rendering_block e;
+      e.ulx = 1; e.uly = 1; e.lrx = 0; e.lry = 0;
+      e.zmin = b.zmin; e.zmax = b.zmax;
+      list[off + slot] = e;
+    }
+  }
+}
+
+// Projection::fillBlocks (RenderScene.cu:167-190), one 16x16 CTA per tile.
+__global__ void k_fill_blocks(sf_image zmin, sf_image zmax, const sf_rendering_block *list,
+                              uint32_t n) {
+  const unsigned blk = blockIdx.x;
+  if (blk >= n) return;
+  const sf_rendering_block b = list[blk];
+  int xpos = b.ulx + (int)threadIdx.x;
+  if (xpos > b.lrx || xpos >= zmin.cols) return;
+  int ypos = b.uly + (int)threadIdx.y;
+  if (ypos > b.lry || ypos >= zmin.rows) return;
+  atomicMin(row_ptr<int>(zmin, ypos) + xpos, __float_as_int(b.zmin));
+  atomicMax(row_ptr<int>(zmax, ypos) + xpos, __float_as_int(b.zmax));
+}
+
+// ---------------------------------------------------------------- raycast
+struct RayCache {
+  int x, y, z, ptr;
+  bool set;
+};
+
+struct VoxelRead {
+  float sdf;
+  unsigned weight;
+};
+
+// DeviceMap::FindVoxel(float3, cache, valid) (DeviceMap.cu:116-133).  The
+// cache starts empty (the reference's default HashEntry would alias block
+// (0,0,0) to voxel index -1).
+__device__ __forceinline__ VoxelRead find_voxel(const DevMap &m, f3 pt, RayCache &c, bool &valid) {
+  i3 p = floor3(pt);
+  i3 bp = vox2block(p);
+  int ptr;
+  if (c.set && bp.x == c.x && bp.y == c.y && bp.z == c.z) {
+    ptr = c.ptr;
+  } else {
+    ptr = find_block(m, bp);
+    if (ptr < 0) {
+      valid = false;
+      VoxelRead r;
+      r.sdf = nanf_bits();
+      r.weight = 0;
+      return r;
+    }
+    c.x = bp.x; c.y = bp.y; c.z = bp.z; c.ptr = ptr; c.set = true;
+  }
+  valid = true;
+  uint2 raw = __ldg((const uint2 *)(m.voxels + ptr + vox2local(p)));
+  VoxelRead r;
+  r.sdf = __uint_as_float(raw.x);
+  r.weight = raw.y & 0xffu;
+  return r;
+}
+
+// Rendering::readSdf (RenderScene.cu:303-308).
+__device__ __forceinline__ float read_sdf(const DevMap &m, f3 pt, RayCache &c, bool &valid) {
+  VoxelRead v = find_voxel(m, pt, c, valid);
+  if (v.weight == 0) valid = false;
+  return v.sdf;
+}
+
+// Rendering::readSdfInterped (RenderScene.cu:310-343).
+__device__ __forceinline__ float read_sdf_interp(const DevMap &m, f3 pt, RayCache &c, bool &valid) {
+  f3 xyz3 = pt - mk3(floorf(pt.x), floorf(pt.y), floorf(pt.z));
+  float s0, s1, r0, r1, r2, r3;
+  s0 = find_voxel(m, pt, c, valid).sdf;
+  s1 = find_voxel(m, pt + mk3(1, 0, 0), c, valid).sdf;
+  r0 = (1.0f - xyz3.x) * s0 + xyz3.x * s1;
+  s0 = find_voxel(m, pt + mk3(0, 1, 0), c, valid).sdf;
+  s1 = find_voxel(m, pt + mk3(1, 1, 0), c, valid).sdf;
+  r1 = (1.0f - xyz3.x) * s0 + xyz3.x * s1;
+  r2 = (1.0f - xyz3.y) * r0 + xyz3.y * r1;
+  s0 = find_voxel(m, pt + mk3(0, 0, 1), c, valid).sdf;
+  s1 = find_voxel(m, pt + mk3(1, 0, 1), c, valid).sdf;
+  r0 = (1.0f - xyz3.x) * s0 + xyz3.x * s1;
+  s0 = find_voxel(m, pt + mk3(0, 1, 1), c, valid).sdf;
+  s1 = find_voxel(m, pt + mk3(1, 1, 1), c, valid).sdf;
+  r1 = (1.0f - xyz3.x) * s0 + xyz3.x * s1;
+  r3 = (1.0f - xyz3.y) * r0 + xyz3.y * r1;
+  return (1.0f - xyz3.z) * r2 + xyz3.z * r3;
+}
+
+// Rendering::readNormal (RenderScene.cu:345-378).
+__device__ __forceinline__ bool read_normal(const DevMap &m, f3 pt, RayCache &c, const m3 &Rinv,
+                                            f3 &n) {
+  bool valid;
+  float s[6];
+  const f3 offs[6] = {mk3(1, 0, 0), mk3(-1, 0, 0), mk3(0, 1, 0),
+                      mk3(0, -1, 0), mk3(0, 0, 1), mk3(0, 0, -1)};
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    s[k] = read_sdf_interp(m, pt + offs[k], c, valid);
+    if (isnan(s[k]) || s[k] == 1.0f || !valid) return false;
+  }
+  n = mk3(s[0] - s[1], s[2] - s[3], s[4] - s[5]);
+  n = normalised(mul(Rinv, n));
+  return true;
+}
+
+// Rendering::operator() (RenderScene.cu:380-488).
+__global__ void __launch_bounds__(64) k_raycast(DevMap m, sf_image vmap, sf_image nmap, sf_image zmin,
+                                                sf_image zmax, const Cam *cam,
+                                                const unsigned *rendered, sf_image fb_v,
+                                                sf_image fb_n, const int *run_flag) {
+  if (run_flag && *run_flag == 0) return;
+  const Cam c = *cam;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= vmap.cols || y >= vmap.rows) return;
+  if (rendered && *rendered == 0u) {
+    // Mapping::RayTrace skips Raycast: the maps keep the frame's own maps.
+    if (fb_v.data) {
+      row_ptr<float4>(vmap, y)[x] = __ldg(row_ptr<const float4>(fb_v, y) + x);
+      row_ptr<float4>(nmap, y)[x] = __ldg(row_ptr<const float4>(fb_n, y) + x);
+    }
+    return;
+  }
+  float4 vout = nan4(), nout = nan4();
+  const int lx = (int)floorf((float)x / 8.0f), ly = (int)floorf((float)y / 8.0f);
+  const float zx = __ldg(row_ptr<const float>(zmin, ly) + lx);
+  const float zy = __ldg(row_ptr<const float>(zmax, ly) + lx);
+  if (!((double)zy < 1e-3 || (double)zx < 1e-3 || isnan(zx) || isnan(zy))) {
+    const float vsi = m.c.voxel_size_inv;
+    float sdf = 1.0f;
+    f3 p;
+    p.z = zx;
+    p.x = p.z * ((float)x - c.cx) * c.invfx;
+    p.y = p.z * ((float)y - c.cy) * c.invfy;
+    float dist_s = norm(p) * vsi;
+    f3 block_s = (mul(c.R, p) + c.t) * vsi;
+    p.z = zy;
+    p.x = p.z * ((float)x - c.cx) * c.invfx;
+    p.y = p.z * ((float)y - c.cy) * c.invfy;
+    float dist_e = norm(p) * vsi;
+    f3 block_e = (mul(c.R, p) + c.t) * vsi;
+    f3 dir = normalised(block_e - block_s);
+    f3 result = block_s;
+    bool valid_sdf = false, found_pt = false, behind = false;
+    float step, prev_sdf;
+    RayCache cache;
+    cache.x = cache.y = cache.z = 0;
+    cache.ptr = -1;
+    cache.set = false;
+    while (dist_s < dist_e) {
+      prev_sdf = sdf;
+      sdf = read_sdf(m, result, cache, valid_sdf);
+      if (!valid_sdf) {
+        step = 8.0f;
+      } else {
+        if (sdf <= 0.1f && sdf >= -0.5f) sdf = read_sdf_interp(m, result, cache, valid_sdf);
+        if (prev_sdf < 0.f && sdf >= 0.f) { behind = true; break; }
+        if (prev_sdf > 0.f && sdf <= 0.f) break;
+        step = 1.0f;
+      }
+      result = result + step * dir;
+      dist_s += step;
+    }
+    if (!behind) {
+      if (sdf <= 0.0f) {
+        step = sdf * m.c.step_scale;
+        result = result + step * dir;
+        sdf = read_sdf_interp(m, result, cache, valid_sdf);
+        step = sdf * m.c.step_scale;
+        result = result + step * dir;
+        found_pt = true;
+      }
+      if (found_pt) {
+        f3 n;
+        if (read_normal(m, result, cache, c.Rinv, n)) {
+          f3 r = mul(c.Rinv, result * m.c.voxel_size - c.t);
+          vout = make_float4(r.x, r.y, r.z, 1.0f);
+          nout = make_float4(n.x, n.y, n.z, 1.0f);
+        }
+      }
+    }
+  }
+  row_ptr<float4>(vmap, y)[x] = vout;
+  row_ptr<float4>(nmap, y)[x] = nout;
+}
+
+}  // namespace
+
+void launch_rendering_blocks(const DevMap &m, uint32_t nvis, const sf_image &zmin,
+                             sf_rendering_block *list, uint32_t *count, const Cam *c,
+                             uint32_t *flags, cudaStream_t s) {
+  k_project_blocks<<<256, 256, 0, s>>>(m, nvis, c, zmin.cols, zmin.rows, list, count,
+                                       m.c.max_rendering_blocks, flags);
+}
+
+void launch_fill_blocks(const sf_image &zmin, const sf_image &zmax,
+                        const sf_rendering_block *list, uint32_t nblocks, cudaStream_t s) {
+  if (nblocks == 0) return;
+  k_fill_blocks<<<nblocks, dim3(16, 16), 0, s>>>(zmin, zmax, list, nblocks);
+}
+
+void launch_raycast(const DevMap &m, const sf_image &vmap, const sf_image &nmap,
+                    const sf_image &zmin, const sf_image &zmax, const Cam *c,
+                    const unsigned *rendered, const sf_image *fallback_v,
+                    const sf_image *fallback_n, const int *run_flag, cudaStream_t s) {
+  dim3 blk(8, 8);
+  dim3 grd((vmap.cols + 7) / 8, (vmap.rows + 7) / 8);
+  sf_image fv = fallback_v ? *fallback_v : sf_image{};
+  sf_image fn = fallback_n ? *fallback_n : sf_image{};
+  k_raycast<<<grd, blk, 0, s>>>(m, vmap, nmap, zmin, zmax, c, rendered, fv, fn, run_flag);
+}
+
+}  // namespace sf

@@ -1,0 +1,115 @@
+// Internal (C++) interface between the kernel files and the C ABI layer.
+#ifndef SF_KERNELS_CUH_
+#define SF_KERNELS_CUH_
+
+#include "sf_device.cuh"
+#include "sf_solve.h"
+
+namespace sf {
+
+constexpr int kMaxLevels = 4;
+
+// ------------------------------------------------------------- pyramid
+void launch_filter_depth(const sf_image &depth, const sf_image &raw, const sf_image &filt,
+                         float depth_scale, float cutoff, cudaStream_t s);
+void launch_pyrdown(const sf_image &src, const sf_image &dst, cudaStream_t s);
+void launch_vnmap(const sf_image &depth, const sf_image &vmap, const sf_image &nmap, float fx,
+                  float fy, float cx, float cy, float cutoff, cudaStream_t s);
+void launch_vmap(const sf_image &depth, const sf_image &vmap, float fx, float fy, float cx,
+                 float cy, float cutoff, cudaStream_t s);
+void launch_nmap(const sf_image &vmap, const sf_image &nmap, cudaStream_t s);
+void launch_resize(const sf_image &vsrc, const sf_image &nsrc, const sf_image &vdst,
+                   const sf_image &ndst, cudaStream_t s);
+
+// ----------------------------------------------------------------- ICP
+struct IcpLevelArgs {
+  sf_image vc, nc, vl, nl;   // current (measured) and last (model) maps
+  float fx, fy, cx, cy;
+  int iters, min_count;
+};
+
+struct IcpWorkspace {
+  double *partials = nullptr;  // [2][29][max_blocks]
+  double *sums = nullptr;      // [29]
+  unsigned *barrier = nullptr; // [2] arrival count, generation
+  TrackCtl *ctl = nullptr;     // device copy of the tracking state
+  int max_blocks = 0;          // co-resident CTAs of the persistent kernel
+  int threads = 0;
+};
+
+int icp_workspace_init(IcpWorkspace &w);
+void icp_workspace_free(IcpWorkspace &w);
+
+// Plain form: one partial-sum launch + one reduction launch; the 29 FP64
+// sums land in w.sums (device).  Pose given as float matrices.
+void launch_icp_step(const IcpWorkspace &w, const IcpLevelArgs &L, const m3 &Rc, f3 tc,
+                     const m3 &Rl, const m3 &RlInv, f3 tl, cudaStream_t s);
+
+// Persistent form: every level and iteration of Tracker::ComputeSE3 in one
+// cooperative launch.  last_pose: device double[16]; result in *w.ctl.
+// run_flag (device int, may be null): when 0 the kernel does nothing.
+cudaError_t launch_icp_persistent(const IcpWorkspace &w, const IcpLevelArgs *levels, int nlevels,
+                                  float thresh, const double *last_pose, const int *run_flag,
+                                  uint32_t *flags, cudaStream_t s);
+
+// -------------------------------------------------------------- fusion
+struct FuseScratch {
+  // allocation requests (lock-free dedupe set keyed by epoch | block pos)
+  unsigned long long *req_set = nullptr;  // [req_cap] (power of 2)
+  uint32_t req_cap = 0;
+  int4 *pending = nullptr;                // [pend_cap] {x, y, z, bucket}
+  int *pending_next = nullptr;            // [pend_cap]
+  uint32_t pend_cap = 0;
+  int *bucket_head = nullptr;             // [num_buckets], -1 when idle
+  int *dirty = nullptr;                   // [pend_cap] buckets with requests
+  unsigned *counters = nullptr;           // [4] pending, dirty, epoch, any_rendered
+};
+
+int fuse_scratch_init(FuseScratch &f, const MapConst &c, int max_pixels);
+void fuse_scratch_free(FuseScratch &f);
+
+struct Cam {
+  m3 R, Rinv;
+  f3 t;
+  float fx, fy, cx, cy, invfx, invfy;
+  int cols, rows;
+  float dmin, dmax;
+};
+
+void launch_map_reset(const DevMap &m, cudaStream_t s);
+void launch_rebuild_index(const DevMap &m, cudaStream_t s);
+// Fusion::CreateBlocks (FuseMap.cu:92-132) as probe + insert passes.
+void launch_alloc(const DevMap &m, const FuseScratch &f, const sf_image &depth, const Cam *c,
+                  const int *run_flag, uint32_t *flags, cudaStream_t s);
+// CheckFullVisibility (FuseMap.cu:134-168) over the allocated-entry index.
+// When zmin/zmax images are given, also lays down the z-range tiles of
+// Projection + fillBlocks (RenderScene.cu:54-190) for each visible block.
+void launch_visibility(const DevMap &m, const FuseScratch &f, const Cam *c, const sf_image *zmin,
+                       const sf_image *zmax, const int *run_flag, uint32_t *flags,
+                       cudaStream_t s);
+// createVoxels (+ analyzeSemantics when mask != null), FuseMap.cu:432-668.
+void launch_integrate(const DevMap &m, const sf_image &depth, const sf_image &rgb,
+                      const sf_image *nmap, const sf_image *mask, int num_detection, const Cam *c,
+                      bool integrate, bool semantics, const int *run_flag, cudaStream_t s);
+void launch_zrange_init(const sf_image &zmin, const sf_image &zmax, cudaStream_t s);
+
+// -------------------------------------------------------------- raycast
+// Projection over the visible list into a rendering-block list + fill.
+void launch_rendering_blocks(const DevMap &m, uint32_t nvis, const sf_image &zmin,
+                             sf_rendering_block *list, uint32_t *count, const Cam *c,
+                             uint32_t *flags, cudaStream_t s);
+void launch_fill_blocks(const sf_image &zmin, const sf_image &zmax,
+                        const sf_rendering_block *list, uint32_t nblocks, cudaStream_t s);
+// Rendering (RenderScene.cu:291-489).  fallback_v/n (may be null): when
+// *rendered == 0 the output is a copy of the fallback maps (the reference
+// skips the raycast and keeps the frame's own maps).
+void launch_raycast(const DevMap &m, const sf_image &vmap, const sf_image &nmap,
+                    const sf_image &zmin, const sf_image &zmax, const Cam *c,
+                    const unsigned *rendered, const sf_image *fallback_v,
+                    const sf_image *fallback_n, const int *run_flag, cudaStream_t s);
+
+// Converts host map config into device constants (DeviceMap.h:166-189).
+MapConst make_map_const(const sf_map_config &cfg);
+
+}  // namespace sf
+#endif

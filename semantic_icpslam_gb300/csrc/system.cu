@@ -1,0 +1,527 @@
+// The per-frame loop: System::GrabImage (Core/System.cc:131-270) with
+// Tracker::GrabFrame / Track / TrackFrame / ComputeSE3(icpOnly)
+// (Tracking/Tracking.cc:65-173, 246-280, 369-517), Mapping::FuseColor and
+// Mapping::RayTrace (Mapping/Mapping.cc:76-161).
+//
+// Buffers: the current frame's measured pyramid (raw + filtered depth,
+// vertex and normal maps per level) and the model maps (the last tracked
+// frame's raycast at level 0, 2x2-downsampled below).  The reference keeps
+// two Frame objects and swaps them after a tracked frame; here the model
+// maps are written in place (raycast, or the measured level-0 maps when no
+// block renders), which leaves the same data where ICP reads it.
+//
+// Three execution forms of the same kernels:
+//  * plain   - host-driven: ICP downloads 29 sums per iteration and solves
+//              on the host; the visible count is downloaded as the
+//              reference does.  The "plain per-launch" comparison form.
+//  * eager   - device-driven: one persistent ICP kernel, tracking decision
+//              and camera on the device, no host synchronisation.
+//  * graph   - the eager form captured once as a CUDA graph and replayed.
+#include <cstddef>
+#include <cstring>
+#include <new>
+
+#include "sf_kernels.cuh"
+
+namespace sf {
+cudaStream_t ctx_stream(sf_context *c);
+IcpWorkspace &ctx_icp(sf_context *c);
+uint32_t *ctx_flags(sf_context *c);
+DevMap &map_dev(sf_map *m);
+FuseScratch &map_scratch(sf_map *m);
+int map_ensure_scratch(sf_map *m, int pixels);
+const sf_map_config &map_cfg(sf_map *m);
+
+struct SysDev {
+  double last_pose[16];
+  int state;     // 1 = initialise on the next frame, 0 = tracking
+  int icp_run;   // this frame runs ICP
+  int run;       // this frame is tracked: mapping runs
+  int accepted;
+  int first;     // this frame was the initialisation frame
+  int pad_;
+  Cam cam;       // camera of this frame's mapping pass
+};
+
+namespace {
+
+__global__ void k_sys_pre(SysDev *s) {
+  s->icp_run = (s->state == 0) ? 1 : 0;
+}
+
+// Track() outcome (Tracking.cc:65-119) and the mapping camera
+// (Frame::GpuRotation / GpuInvRotation / GpuTranslation, Frame.cc:626-645).
+__global__ void k_sys_post(SysDev *s, const TrackCtl *ctl, Cam tmpl) {
+  int tracked;
+  if (s->state == 1) {
+    tracked = 1;
+    s->first = 1;
+    s->accepted = 1;
+    s->state = 0;
+  } else {
+    s->first = 0;
+    tracked = ctl->accepted;
+    s->accepted = ctl->accepted;
+    if (tracked)
+      for (int k = 0; k < 16; ++k) s->last_pose[k] = ctl->next_pose[k];
+  }
+  s->run = tracked;
+  const double *P = s->last_pose;
+  Cam c = tmpl;
+  c.R.rx = mk3((float)P[0], (float)P[1], (float)P[2]);
+  c.R.ry = mk3((float)P[4], (float)P[5], (float)P[6]);
+  c.R.rz = mk3((float)P[8], (float)P[9], (float)P[10]);
+  c.Rinv.rx = mk3((float)P[0], (float)P[4], (float)P[8]);
+  c.Rinv.ry = mk3((float)P[1], (float)P[5], (float)P[9]);
+  c.Rinv.rz = mk3((float)P[2], (float)P[6], (float)P[10]);
+  c.t = mk3((float)P[3], (float)P[7], (float)P[11]);
+  s->cam = c;
+}
+
+__global__ void k_sys_stats(const SysDev *s, const TrackCtl *ctl, DevMap m, const uint32_t *flags,
+                            sf_frame_stats *out) {
+  sf_frame_stats st;
+  st.tracked = s->run;
+  st.accepted = s->accepted;
+  if (s->first) {
+    st.fail = 0; st.iterations = 0; st.icp_error = 0.f; st.icp_count = 0;
+  } else {
+    st.fail = ctl->stop;
+    st.iterations = ctl->iters_run;
+    st.icp_error = ctl->icpError;
+    st.icp_count = ctl->icpCount;
+  }
+  st.visible = s->run ? *m.no_visible : 0u;
+  st.heap_counter = *m.heap_counter;
+  st.entry_ptr = *m.entry_ptr;
+  st.allocated = *m.alloc_count;
+  st.flags = *flags;
+  for (int k = 0; k < 16; ++k) st.pose[k] = s->last_pose[k];
+  *out = st;
+}
+
+template <class T>
+inline T *dev_field(SysDev *base, size_t off) {
+  return (T *)((char *)base + off);
+}
+
+inline sf_image img(void *p, int cols, int rows, size_t elem) {
+  sf_image i;
+  i.data = p;
+  i.step = (size_t)cols * elem;
+  i.cols = cols;
+  i.rows = rows;
+  return i;
+}
+
+}  // namespace
+}  // namespace sf
+
+using namespace sf;
+
+struct sf_system {
+  sf_context *ctx = nullptr;
+  sf_map *map = nullptr;
+  sf_system_config cfg;
+  int L = 3, zc = 0, zr = 0;
+  // device buffers
+  uint16_t *d_depth16 = nullptr;
+  uint8_t *d_rgb = nullptr, *d_mask = nullptr;
+  float *d_raw = nullptr;
+  float *d_depth[kMaxLevels] = {};
+  float4 *d_vmap[kMaxLevels] = {}, *d_nmap[kMaxLevels] = {};
+  float4 *d_mv[kMaxLevels] = {}, *d_mn[kMaxLevels] = {};
+  float *d_zmin = nullptr, *d_zmax = nullptr;
+  SysDev *d_sys = nullptr;
+  sf_frame_stats *d_stats = nullptr;
+  // pinned host staging
+  uint16_t *h_depth16 = nullptr;
+  uint8_t *h_rgb = nullptr, *h_mask = nullptr;
+  sf_frame_stats *h_stats = nullptr;
+  // plain-form host state
+  double last_pose[16];
+  int state = 1;
+  TrackCtl ctl;
+  Cam tmpl;
+  // graph
+  cudaGraphExec_t gexec = nullptr;
+  int graph_sem = -1;  // semantics flag the graph was captured with
+  int num_detection_captured = 0;
+};
+
+namespace {
+
+int alloc_all(sf_system *s) {
+  const int C = s->cfg.cols, R = s->cfg.rows;
+  const size_t np = (size_t)C * R;
+  auto A = [&](void **p, size_t bytes) { return cudaMalloc(p, bytes) == cudaSuccess; };
+  bool ok = A((void **)&s->d_depth16, np * 2) && A((void **)&s->d_rgb, np * 3) &&
+            A((void **)&s->d_mask, np) && A((void **)&s->d_raw, np * 4) &&
+            A((void **)&s->d_zmin, (size_t)s->zc * s->zr * 4) &&
+            A((void **)&s->d_zmax, (size_t)s->zc * s->zr * 4) &&
+            A((void **)&s->d_sys, sizeof(SysDev)) && A((void **)&s->d_stats, sizeof(sf_frame_stats));
+  for (int l = 0; ok && l < s->L; ++l) {
+    const size_t n = (size_t)(C >> l) * (R >> l);
+    ok = A((void **)&s->d_depth[l], n * 4) && A((void **)&s->d_vmap[l], n * 16) &&
+         A((void **)&s->d_nmap[l], n * 16) && A((void **)&s->d_mv[l], n * 16) &&
+         A((void **)&s->d_mn[l], n * 16);
+  }
+  ok = ok && cudaMallocHost(&s->h_depth16, np * 2) == cudaSuccess &&
+       cudaMallocHost(&s->h_rgb, np * 3) == cudaSuccess &&
+       cudaMallocHost(&s->h_mask, np) == cudaSuccess &&
+       cudaMallocHost(&s->h_stats, sizeof(sf_frame_stats)) == cudaSuccess;
+  if (ok) ok = cudaMemset(s->d_mask, 0, np) == cudaSuccess;
+  return ok ? SF_OK : SF_ERR_CUDA;
+}
+
+void free_all(sf_system *s) {
+  cudaFree(s->d_depth16); cudaFree(s->d_rgb); cudaFree(s->d_mask); cudaFree(s->d_raw);
+  cudaFree(s->d_zmin); cudaFree(s->d_zmax); cudaFree(s->d_sys); cudaFree(s->d_stats);
+  for (int l = 0; l < kMaxLevels; ++l) {
+    cudaFree(s->d_depth[l]); cudaFree(s->d_vmap[l]); cudaFree(s->d_nmap[l]);
+    cudaFree(s->d_mv[l]); cudaFree(s->d_mn[l]);
+  }
+  if (s->h_depth16) cudaFreeHost(s->h_depth16);
+  if (s->h_rgb) cudaFreeHost(s->h_rgb);
+  if (s->h_mask) cudaFreeHost(s->h_mask);
+  if (s->h_stats) cudaFreeHost(s->h_stats);
+  if (s->gexec) cudaGraphExecDestroy(s->gexec);
+}
+
+// Frame::FillImages depth part (Core/Frame.cc:68-92).
+void enqueue_pyramid(sf_system *s, cudaStream_t st) {
+  const int C = s->cfg.cols, R = s->cfg.rows;
+  launch_filter_depth(img(s->d_depth16, C, R, 2), img(s->d_raw, C, R, 4), img(s->d_depth[0], C, R, 4),
+                      s->cfg.depth_scale, s->cfg.depth_cutoff, st);
+  for (int l = 0; l < s->L; ++l) {
+    const int c = C >> l, r = R >> l;
+    if (l > 0)
+      launch_pyrdown(img(s->d_depth[l - 1], C >> (l - 1), R >> (l - 1), 4), img(s->d_depth[l], c, r, 4), st);
+    const float div = (float)(1 << l);
+    launch_vnmap(img(s->d_depth[l], c, r, 4), img(s->d_vmap[l], c, r, 16), img(s->d_nmap[l], c, r, 16),
+                 s->cfg.K.fx / div, s->cfg.K.fy / div, s->cfg.K.cx / div, s->cfg.K.cy / div,
+                 s->cfg.depth_cutoff, st);
+  }
+}
+
+void icp_levels(sf_system *s, IcpLevelArgs *lv) {
+  const int C = s->cfg.cols, R = s->cfg.rows;
+  for (int l = 0; l < s->L; ++l) {
+    const int c = C >> l, r = R >> l;
+    const float div = (float)(1 << l);
+    lv[l].vc = img(s->d_vmap[l], c, r, 16);
+    lv[l].nc = img(s->d_nmap[l], c, r, 16);
+    lv[l].vl = img(s->d_mv[l], c, r, 16);
+    lv[l].nl = img(s->d_mn[l], c, r, 16);
+    lv[l].fx = s->cfg.K.fx / div; lv[l].fy = s->cfg.K.fy / div;
+    lv[l].cx = s->cfg.K.cx / div; lv[l].cy = s->cfg.K.cy / div;
+    lv[l].iters = s->cfg.iters[l];
+    lv[l].min_count = s->cfg.min_count[l];
+  }
+}
+
+// Mapping::FuseColor + Mapping::RayTrace and the next frame's
+// Frame::ResizeImages, every launch gated by `run` (device) when given.
+void enqueue_mapping(sf_system *s, const Cam *cam, const int *run, int num_detection,
+                     cudaStream_t st) {
+  const int C = s->cfg.cols, R = s->cfg.rows;
+  DevMap &m = map_dev(s->map);
+  FuseScratch &f = map_scratch(s->map);
+  uint32_t *flags = ctx_flags(s->ctx);
+  sf_image depth = img(s->d_raw, C, R, 4), rgb = img(s->d_rgb, C, R, 3);
+  sf_image nm0 = img(s->d_nmap[0], C, R, 16), mask = img(s->d_mask, C, R, 1);
+  sf_image zmin = img(s->d_zmin, s->zc, s->zr, 4), zmax = img(s->d_zmax, s->zc, s->zr, 4);
+  launch_alloc(m, f, depth, cam, run, flags, st);
+  launch_visibility(m, f, cam, &zmin, &zmax, run, flags, st);
+  launch_integrate(m, depth, rgb, &nm0, &mask, num_detection, cam, true, num_detection > 0, run, st);
+  sf_image fv = img(s->d_vmap[0], C, R, 16), fn = img(s->d_nmap[0], C, R, 16);
+  launch_raycast(m, img(s->d_mv[0], C, R, 16), img(s->d_mn[0], C, R, 16), zmin, zmax, cam,
+                 f.counters + 3, &fv, &fn, run, st);
+  for (int l = 1; l < s->L; ++l)
+    launch_resize(img(s->d_mv[l - 1], C >> (l - 1), R >> (l - 1), 16),
+                  img(s->d_mn[l - 1], C >> (l - 1), R >> (l - 1), 16),
+                  img(s->d_mv[l], C >> l, R >> l, 16), img(s->d_mn[l], C >> l, R >> l, 16), st);
+}
+
+// Device-driven frame (eager and graph forms).
+cudaError_t enqueue_device_frame(sf_system *s, int num_detection, cudaStream_t st) {
+  IcpWorkspace &w = ctx_icp(s->ctx);
+  enqueue_pyramid(s, st);
+  k_sys_pre<<<1, 1, 0, st>>>(s->d_sys);
+  IcpLevelArgs lv[kMaxLevels];
+  icp_levels(s, lv);
+  cudaError_t e = cudaMemsetAsync(w.barrier, 0, sizeof(unsigned), st);
+  if (e != cudaSuccess) return e;
+  e = launch_icp_persistent(w, lv, s->L, s->cfg.icp_thresh, dev_field<double>(s->d_sys, offsetof(SysDev, last_pose)),
+                            dev_field<int>(s->d_sys, offsetof(SysDev, icp_run)),
+                            ctx_flags(s->ctx), st);
+  if (e != cudaSuccess) return e;
+  k_sys_post<<<1, 1, 0, st>>>(s->d_sys, w.ctl, s->tmpl);
+  enqueue_mapping(s, dev_field<Cam>(s->d_sys, offsetof(SysDev, cam)),
+                  dev_field<int>(s->d_sys, offsetof(SysDev, run)), num_detection, st);
+  k_sys_stats<<<1, 1, 0, st>>>(s->d_sys, w.ctl, map_dev(s->map), ctx_flags(s->ctx), s->d_stats);
+  return cudaGetLastError();
+}
+
+// Host-driven frame (plain per-launch form).
+int run_plain_frame(sf_system *s, int num_detection) {
+  cudaStream_t st = ctx_stream(s->ctx);
+  IcpWorkspace &w = ctx_icp(s->ctx);
+  enqueue_pyramid(s, st);
+  int tracked;
+  bool first = false;
+  if (s->state == 1) {
+    tracked = 1;
+    first = true;
+    s->state = 0;
+    ctl_begin(s->ctl, s->last_pose);
+    s->ctl.accepted = 1;
+  } else {
+    IcpLevelArgs lv[kMaxLevels];
+    icp_levels(s, lv);
+    ctl_begin(s->ctl, s->last_pose);
+    double sums[29];
+    for (int l = s->L - 1; l >= 0 && !s->ctl.stop; --l) {
+      for (int j = 0; j < lv[l].iters; ++j) {
+        m3 Rc, Rci, Rl, Rli;
+        f3 tc, tl;
+        auto tofl = [](const double *P, m3 &R, m3 &Ri, f3 &t) {
+          R.rx = {(float)P[0], (float)P[1], (float)P[2]};
+          R.ry = {(float)P[4], (float)P[5], (float)P[6]};
+          R.rz = {(float)P[8], (float)P[9], (float)P[10]};
+          Ri.rx = {(float)P[0], (float)P[4], (float)P[8]};
+          Ri.ry = {(float)P[1], (float)P[5], (float)P[9]};
+          Ri.rz = {(float)P[2], (float)P[6], (float)P[10]};
+          t = {(float)P[3], (float)P[7], (float)P[11]};
+        };
+        tofl(s->ctl.next_pose, Rc, Rci, tc);
+        tofl(s->ctl.last_pose, Rl, Rli, tl);
+        launch_icp_step(w, lv[l], Rc, tc, Rl, Rli, tl, st);
+        if (cudaMemcpyAsync(sums, w.sums, sizeof(sums), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess)
+          return SF_ERR_CUDA;
+        if (!ctl_step(s->ctl, sums, lv[l].min_count)) break;
+      }
+    }
+    ctl_finish(s->ctl, s->cfg.icp_thresh);
+    tracked = s->ctl.accepted;
+    if (tracked) memcpy(s->last_pose, s->ctl.next_pose, sizeof(s->last_pose));
+  }
+  // host -> device state (camera, pose, decision) for the mapping pass
+  SysDev sd;
+  memset(&sd, 0, sizeof(sd));
+  memcpy(sd.last_pose, s->last_pose, sizeof(sd.last_pose));
+  sd.state = 0;
+  sd.run = tracked;
+  sd.accepted = s->ctl.accepted;
+  sd.first = first ? 1 : 0;
+  const double *P = s->last_pose;
+  sd.cam = s->tmpl;
+  sd.cam.R.rx = {(float)P[0], (float)P[1], (float)P[2]};
+  sd.cam.R.ry = {(float)P[4], (float)P[5], (float)P[6]};
+  sd.cam.R.rz = {(float)P[8], (float)P[9], (float)P[10]};
+  sd.cam.Rinv.rx = {(float)P[0], (float)P[4], (float)P[8]};
+  sd.cam.Rinv.ry = {(float)P[1], (float)P[5], (float)P[9]};
+  sd.cam.Rinv.rz = {(float)P[2], (float)P[6], (float)P[10]};
+  sd.cam.t = {(float)P[3], (float)P[7], (float)P[11]};
+  if (cudaMemcpyAsync(s->d_sys, &sd, sizeof(sd), cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return SF_ERR_CUDA;
+  if (cudaMemcpyAsync(w.ctl, &s->ctl, sizeof(TrackCtl), cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return SF_ERR_CUDA;
+  if (tracked) {
+    DevMap &m = map_dev(s->map);
+    FuseScratch &f = map_scratch(s->map);
+    const int C = s->cfg.cols, R = s->cfg.rows;
+    uint32_t *flags = ctx_flags(s->ctx);
+    sf_image depth = img(s->d_raw, C, R, 4), rgb = img(s->d_rgb, C, R, 3);
+    sf_image nm0 = img(s->d_nmap[0], C, R, 16), mask = img(s->d_mask, C, R, 1);
+    sf_image zmin = img(s->d_zmin, s->zc, s->zr, 4), zmax = img(s->d_zmax, s->zc, s->zr, 4);
+    const Cam *cam = dev_field<Cam>(s->d_sys, offsetof(SysDev, cam));
+    launch_alloc(m, f, depth, cam, nullptr, flags, st);
+    launch_visibility(m, f, cam, &zmin, &zmax, nullptr, flags, st);
+    uint32_t nvis = 0;  // FuseMapColor downloads the visible count (FuseMap.cu:1116)
+    if (cudaMemcpyAsync(&nvis, m.no_visible, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return SF_ERR_CUDA;
+    if (nvis > 0)
+      launch_integrate(m, depth, rgb, &nm0, &mask, num_detection, cam, true, num_detection > 0,
+                       nullptr, st);
+    sf_image fv = img(s->d_vmap[0], C, R, 16), fn = img(s->d_nmap[0], C, R, 16);
+    launch_raycast(m, img(s->d_mv[0], C, R, 16), img(s->d_mn[0], C, R, 16), zmin, zmax, cam,
+                   f.counters + 3, &fv, &fn, nullptr, st);
+    for (int l = 1; l < s->L; ++l)
+      launch_resize(img(s->d_mv[l - 1], C >> (l - 1), R >> (l - 1), 16),
+                    img(s->d_mn[l - 1], C >> (l - 1), R >> (l - 1), 16),
+                    img(s->d_mv[l], C >> l, R >> l, 16), img(s->d_mn[l], C >> l, R >> l, 16), st);
+  }
+  k_sys_stats<<<1, 1, 0, st>>>(s->d_sys, w.ctl, map_dev(s->map), ctx_flags(s->ctx), s->d_stats);
+  return cudaGetLastError() == cudaSuccess ? SF_OK : SF_ERR_CUDA;
+}
+
+int run_frame(sf_system *s, int num_detection) {
+  cudaStream_t st = ctx_stream(s->ctx);
+  if (s->cfg.use_graph == 0) return run_plain_frame(s, num_detection);
+  if (s->cfg.use_graph == 2) {  // eager device-driven
+    return enqueue_device_frame(s, num_detection, st) == cudaSuccess ? SF_OK : SF_ERR_CUDA;
+  }
+  const int sem = num_detection > 0 ? 1 : 0;
+  if (!s->gexec || s->graph_sem != sem || (sem && s->num_detection_captured != num_detection)) {
+    if (s->gexec) { cudaGraphExecDestroy(s->gexec); s->gexec = nullptr; }
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return SF_ERR_CUDA;
+    cudaError_t e = enqueue_device_frame(s, num_detection, st);
+    cudaError_t e2 = cudaStreamEndCapture(st, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess || !g) {
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      return SF_ERR_CUDA;
+    }
+    e = cudaGraphInstantiate(&s->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { s->gexec = nullptr; return SF_ERR_CUDA; }
+    s->graph_sem = sem;
+    s->num_detection_captured = num_detection;
+  }
+  return cudaGraphLaunch(s->gexec, st) == cudaSuccess ? SF_OK : SF_ERR_CUDA;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sf_system_create(sf_context *ctx, const sf_system_config *cfg, const double init_pose[16],
+                     sf_system **out) {
+  if (!ctx || !cfg || !out) return SF_ERR_INVALID;
+  *out = nullptr;
+  if (cfg->cols <= 0 || cfg->rows <= 0 || cfg->levels < 1 || cfg->levels > kMaxLevels ||
+      (cfg->cols >> (cfg->levels - 1)) < 2 || (cfg->rows >> (cfg->levels - 1)) < 2 ||
+      cfg->depth_scale <= 0 || cfg->K.fx <= 0 || cfg->K.fy <= 0)
+    return SF_ERR_INVALID;
+  sf_system *s = new (std::nothrow) sf_system();
+  if (!s) return SF_ERR_INVALID;
+  s->ctx = ctx;
+  s->cfg = *cfg;
+  s->L = cfg->levels;
+  s->zc = cfg->zrange_cols > 0 ? cfg->zrange_cols : (cfg->cols + 7) / 8;
+  s->zr = cfg->zrange_rows > 0 ? cfg->zrange_rows : (cfg->rows + 7) / 8;
+  for (int k = 0; k < 16; ++k) s->last_pose[k] = init_pose ? init_pose[k] : (k % 5 == 0 ? 1.0 : 0.0);
+  int st = sf_map_create(&cfg->map, &s->map);
+  if (st == SF_OK) st = alloc_all(s);
+  if (st == SF_OK) st = map_ensure_scratch(s->map, cfg->cols * cfg->rows);
+  if (st == SF_OK) {
+    Cam &c = s->tmpl;
+    memset(&c, 0, sizeof(c));
+    c.fx = cfg->K.fx; c.fy = cfg->K.fy; c.cx = cfg->K.cx; c.cy = cfg->K.cy;
+    c.invfx = (float)(1.0 / (double)cfg->K.fx);
+    c.invfy = (float)(1.0 / (double)cfg->K.fy);
+    c.cols = cfg->cols; c.rows = cfg->rows;
+    c.dmin = cfg->map.depth_min; c.dmax = cfg->map.depth_max;
+    SysDev sd;
+    memset(&sd, 0, sizeof(sd));
+    memcpy(sd.last_pose, s->last_pose, sizeof(sd.last_pose));
+    sd.state = 1;
+    if (cudaMemcpy(s->d_sys, &sd, sizeof(sd), cudaMemcpyHostToDevice) != cudaSuccess) st = SF_ERR_CUDA;
+    ctl_begin(s->ctl, s->last_pose);
+  }
+  if (st != SF_OK) {
+    sf_system_destroy(s);
+    return st;
+  }
+  *out = s;
+  return SF_OK;
+}
+
+int sf_system_destroy(sf_system *s) {
+  if (!s) return SF_ERR_INVALID;
+  if (s->ctx) cudaStreamSynchronize(ctx_stream(s->ctx));
+  free_all(s);
+  if (s->map) sf_map_destroy(s->map);
+  delete s;
+  return SF_OK;
+}
+
+int sf_system_grab(sf_system *s, const uint16_t *depth, const uint8_t *rgb, const uint8_t *mask,
+                   int num_detection, sf_frame_stats *stats) {
+  if (!s || !depth || !rgb) return SF_ERR_INVALID;
+  if (num_detection > 0 && !mask) return SF_ERR_INVALID;
+  cudaStream_t st = ctx_stream(s->ctx);
+  const size_t np = (size_t)s->cfg.cols * s->cfg.rows;
+  // host -> pinned staging -> device
+  memcpy(s->h_depth16, depth, np * 2);
+  memcpy(s->h_rgb, rgb, np * 3);
+  if (cudaMemcpyAsync(s->d_depth16, s->h_depth16, np * 2, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(s->d_rgb, s->h_rgb, np * 3, cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return SF_ERR_CUDA;
+  if (num_detection > 0) {
+    memcpy(s->h_mask, mask, np);
+    if (cudaMemcpyAsync(s->d_mask, s->h_mask, np, cudaMemcpyHostToDevice, st) != cudaSuccess)
+      return SF_ERR_CUDA;
+  }
+  int r = run_frame(s, num_detection);
+  if (r) return r;
+  if (cudaMemcpyAsync(s->h_stats, s->d_stats, sizeof(sf_frame_stats), cudaMemcpyDeviceToHost, st) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return SF_ERR_CUDA;
+  if (stats) *stats = *s->h_stats;
+  return SF_OK;
+}
+
+int sf_system_grab_device(sf_system *s, const uint16_t *depth, const uint8_t *rgb,
+                          const uint8_t *mask, int num_detection) {
+  if (!s || !depth || !rgb) return SF_ERR_INVALID;
+  if (num_detection > 0 && !mask) return SF_ERR_INVALID;
+  cudaStream_t st = ctx_stream(s->ctx);
+  const size_t np = (size_t)s->cfg.cols * s->cfg.rows;
+  if (depth != s->d_depth16 &&
+      cudaMemcpyAsync(s->d_depth16, depth, np * 2, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+    return SF_ERR_CUDA;
+  if (rgb != s->d_rgb && cudaMemcpyAsync(s->d_rgb, rgb, np * 3, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+    return SF_ERR_CUDA;
+  if (num_detection > 0 && mask != s->d_mask &&
+      cudaMemcpyAsync(s->d_mask, mask, np, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+    return SF_ERR_CUDA;
+  return run_frame(s, num_detection);
+}
+
+int sf_system_stats(sf_system *s, sf_frame_stats *stats) {
+  if (!s || !stats) return SF_ERR_INVALID;
+  cudaStream_t st = ctx_stream(s->ctx);
+  if (cudaMemcpyAsync(s->h_stats, s->d_stats, sizeof(sf_frame_stats), cudaMemcpyDeviceToHost, st) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return SF_ERR_CUDA;
+  *stats = *s->h_stats;
+  return SF_OK;
+}
+
+int sf_system_model_maps(sf_system *s, int level, sf_image *vmap, sf_image *nmap) {
+  if (!s || level < 0 || level >= s->L || !vmap || !nmap) return SF_ERR_INVALID;
+  const int c = s->cfg.cols >> level, r = s->cfg.rows >> level;
+  *vmap = img(s->d_mv[level], c, r, 16);
+  *nmap = img(s->d_mn[level], c, r, 16);
+  return SF_OK;
+}
+
+int sf_system_frame_maps(sf_system *s, int level, sf_image *vmap, sf_image *nmap, sf_image *depth) {
+  if (!s || level < 0 || level >= s->L) return SF_ERR_INVALID;
+  const int c = s->cfg.cols >> level, r = s->cfg.rows >> level;
+  if (vmap) *vmap = img(s->d_vmap[level], c, r, 16);
+  if (nmap) *nmap = img(s->d_nmap[level], c, r, 16);
+  if (depth) *depth = img(s->d_depth[level], c, r, 4);
+  return SF_OK;
+}
+
+int sf_system_get_map(sf_system *s, sf_map **map) {
+  if (!s || !map) return SF_ERR_INVALID;
+  *map = s->map;
+  return SF_OK;
+}
+
+int sf_system_pose_device(sf_system *s, double **last_pose) {
+  if (!s || !last_pose) return SF_ERR_INVALID;
+  *last_pose = dev_field<double>(s->d_sys, offsetof(SysDev, last_pose));
+  return SF_OK;
+}
+
+}  // extern "C"

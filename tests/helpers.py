@@ -1,0 +1,79 @@
+"""Shared helpers for the parity tests (inputs, device buffers, comparisons)."""
+import functools
+
+import numpy as np
+
+C1 = dict(cols=320, rows=240, K=(262.5, 262.5, 159.5, 119.5))
+C2 = dict(cols=640, rows=480, K=(525.0, 525.0, 319.5, 239.5))
+MAP_C1 = dict(voxel_size=0.01, trunc_dist=0.03, num_buckets=1 << 18, num_excess=1 << 16, num_sdf_blocks=1 << 16)
+MAP_C2 = dict(voxel_size=0.005, trunc_dist=0.04, num_buckets=1 << 20, num_excess=1 << 18,
+              num_sdf_blocks=1 << 17)
+
+
+@functools.lru_cache(maxsize=8)
+def sequence(cols, rows, K, n, scene=0, trajectory=0, seed=1, dropout=0.0, label_flip=0.0, noise=1.0,
+             n_objects=0):
+    """Frames (depth u16, rgb, mask, gt pose) of a seeded synthetic sequence."""
+    from semantic_icpslam_gb300 import Synth
+    s = Synth(cols, rows, K, scene=scene, trajectory=trajectory, seed=seed, dropout=dropout,
+              label_flip=label_flip, noise=noise, n_objects=n_objects)
+    return [s.frame(i) for i in range(n)]
+
+
+def cuda(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def empty(shape, dtype):
+    import torch
+    return torch.empty(shape, dtype=dtype, device="cuda")
+
+
+def host(t):
+    import torch
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def same_nan(a, b):
+    """Bitwise equality treating any NaN as equal to any NaN."""
+    a = np.asarray(a)
+    b = np.asarray(b)
+    na, nb = np.isnan(a), np.isnan(b)
+    return np.array_equal(na, nb) and np.array_equal(a[~na], b[~nb])
+
+
+def image_to_host(ctx, im, dtype, channels=1):
+    n = im.rows * im.cols * channels
+    a = ctx.download(im.data, dtype, n)
+    return a.reshape((im.rows, im.cols, channels)) if channels > 1 else a.reshape((im.rows, im.cols))
+
+
+def map_to_host(ctx, m):
+    """(entries, voxels, visible) of a device map as numpy structured arrays."""
+    from oracle.oracle import ENTRY_DTYPE, VOXEL_DTYPE
+    a = m.arrays()
+    e = ctx.download(a.hash_entries, ENTRY_DTYPE, m.num_entries)
+    v = ctx.download(a.voxel_blocks, VOXEL_DTYPE, m.cfg.num_sdf_blocks * 512)
+    vis = ctx.download(a.visible_entries, ENTRY_DTYPE, m.num_entries)
+    return e, v, vis
+
+
+def block_table(entries):
+    """{(x,y,z): ptr} of allocated entries (ptr >= 0)."""
+    sel = entries[entries["ptr"] >= 0]
+    return {(int(a), int(b), int(c)): int(p) for a, b, c, p in zip(sel["x"], sel["y"], sel["z"], sel["ptr"])}
+
+
+def positions(entries, n=None):
+    e = entries if n is None else entries[:n]
+    return set(zip(e["x"].tolist(), e["y"].tolist(), e["z"].tolist()))
+
+
+def voxels_by_pos(entries, voxels):
+    t = block_table(entries)
+    keys = sorted(t)
+    if not keys:
+        return keys, np.zeros((0, 512), voxels.dtype)
+    return keys, np.stack([voxels[t[k]:t[k] + 512] for k in keys])
