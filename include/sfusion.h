@@ -103,6 +103,9 @@ int sf_context_stream(sf_context *ctx, void **stream_out);
 int sf_context_sync(sf_context *ctx);
 /* Last device-side overflow / error flags recorded by the context. */
 int sf_context_flags(sf_context *ctx, uint32_t *flags_out);
+/* Process-wide number of kernels this library has launched (a CUDA-graph
+ * replay counts the kernel nodes it runs). */
+int sf_kernel_launches(uint64_t *out);
 /* Copies `bytes` between any two host/device pointers (unified addressing)
  * on the context stream and waits for it. */
 int sf_memcpy(sf_context *ctx, void *dst, const void *src, size_t bytes);
@@ -270,6 +273,11 @@ int sf_system_model_maps(sf_system *sys, int level, sf_image *vmap, sf_image *nm
 int sf_system_frame_maps(sf_system *sys, int level, sf_image *vmap, sf_image *nmap,
                          sf_image *depth);
 int sf_system_get_map(sf_system *sys, sf_map **map);
+/* Stage timing with CUDA events on the system's stream (eager device form,
+ * use_graph == 2): ms[7] = pyramid, ICP, allocation, visibility + z-range,
+ * integration, raycast, resize + stats of the last frame. */
+int sf_system_set_timing(sf_system *sys, int enable);
+int sf_system_stage_ms(sf_system *sys, float ms[7]);
 /* Device pointers to the pose state: last (tracked) pose, double[16]. */
 int sf_system_pose_device(sf_system *sys, double **last_pose);
 

@@ -90,6 +90,7 @@ SIGNATURES = {
     "sf_context_sync": [vp],
     "sf_context_flags": [vp, U32P],
     "sf_memcpy": [vp, vp, vp, C.c_size_t],
+    "sf_kernel_launches": [C.POINTER(C.c_uint64)],
     "sf_map_create": [C.POINTER(MapConfig), pvp],
     "sf_map_wrap": [C.POINTER(MapConfig), C.POINTER(DeviceMap), pvp],
     "sf_map_destroy": [vp],
@@ -124,6 +125,8 @@ SIGNATURES = {
     "sf_system_model_maps": [vp, C.c_int, C.POINTER(Image), C.POINTER(Image)],
     "sf_system_frame_maps": [vp, C.c_int, C.POINTER(Image), C.POINTER(Image), C.POINTER(Image)],
     "sf_system_get_map": [vp, pvp],
+    "sf_system_set_timing": [vp, C.c_int],
+    "sf_system_stage_ms": [vp, F32P],
     "sf_system_pose_device": [vp, C.POINTER(C.POINTER(C.c_double))],
     "sf_synth_create": [C.POINTER(SynthConfig), pvp],
     "sf_synth_destroy": [vp],

@@ -8,6 +8,7 @@
 // asynchronous on it.  The context stream is a blocking stream, so work the
 // caller issues on the legacy default stream orders after it, as the
 // reference's default-stream cudaMemcpy calls expect.
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -153,6 +154,12 @@ int sf_context_flags(sf_context *ctx, uint32_t *flags_out) {
   if (!ctx || !flags_out) return SF_ERR_INVALID;
   SF_CHECK(cudaMemcpyAsync(flags_out, ctx->flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
   SF_CHECK(cudaStreamSynchronize(ctx->stream));
+  return SF_OK;
+}
+
+int sf_kernel_launches(uint64_t *out) {
+  if (!out) return SF_ERR_INVALID;
+  *out = (uint64_t)launches_total();
   return SF_OK;
 }
 
@@ -538,6 +545,9 @@ int sf_Raycast(sf_context *ctx, sf_map *m, sf_image vmap, sf_image nmap, sf_imag
 
 // Accessors used by system.cu.
 namespace sf {
+static std::atomic<unsigned long long> g_launches{0};
+void note_launch(unsigned long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+unsigned long long launches_total() { return g_launches.load(std::memory_order_relaxed); }
 cudaStream_t ctx_stream(sf_context *c) { return c->stream; }
 IcpWorkspace &ctx_icp(sf_context *c) { return c->icp; }
 uint32_t *ctx_flags(sf_context *c) { return c->flags; }

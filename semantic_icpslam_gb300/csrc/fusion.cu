@@ -558,36 +558,36 @@ static int sm_count() {
 
 void launch_map_reset(const DevMap &m, cudaStream_t s) {
   const int g = sm_count() * 8;
-  k_reset_entries<<<g, 256, 0, s>>>(m, nullptr);
-  k_reset_voxels<<<g, 256, 0, s>>>(m);
+  k_reset_entries<<<g, 256, 0, s>>>(m, nullptr); note_launch();
+  k_reset_voxels<<<g, 256, 0, s>>>(m); note_launch();
 }
 
 void launch_rebuild_index(const DevMap &m, cudaStream_t s) {
   cudaMemsetAsync(m.alloc_count, 0, sizeof(int), s);
-  k_rebuild_index<<<sm_count() * 8, 256, 0, s>>>(m);
+  k_rebuild_index<<<sm_count() * 8, 256, 0, s>>>(m); note_launch();
 }
 
 void launch_alloc(const DevMap &m, const FuseScratch &f, const sf_image &depth, const Cam *c,
                   const int *run_flag, uint32_t *flags, cudaStream_t s) {
-  k_alloc_begin<<<1, 1, 0, s>>>(f, run_flag);
-  k_clear_req<<<sm_count() * 4, 256, 0, s>>>(f);
+  k_alloc_begin<<<1, 1, 0, s>>>(f, run_flag); note_launch();
+  k_clear_req<<<sm_count() * 4, 256, 0, s>>>(f); note_launch();
   dim3 blk(32, 8);
   dim3 grd((depth.cols + 31) / 32, (depth.rows + 7) / 8);
-  k_alloc_probe<<<grd, blk, 0, s>>>(m, f, depth, c, run_flag, flags);
-  k_alloc_insert<<<sm_count() * 2, 128, 0, s>>>(m, f, run_flag, flags);
+  k_alloc_probe<<<grd, blk, 0, s>>>(m, f, depth, c, run_flag, flags); note_launch();
+  k_alloc_insert<<<sm_count() * 2, 128, 0, s>>>(m, f, run_flag, flags); note_launch();
 }
 
 void launch_zrange_init(const sf_image &zmin, const sf_image &zmax, cudaStream_t s) {
   dim3 blk(32, 8);
   dim3 grd((zmin.cols + 31) / 32, (zmin.rows + 7) / 8);
-  k_zrange_init<<<grd, blk, 0, s>>>(zmin, zmax);
+  k_zrange_init<<<grd, blk, 0, s>>>(zmin, zmax); note_launch();
 }
 
 void launch_visibility(const DevMap &m, const FuseScratch &f, const Cam *c, const sf_image *zmin,
                        const sf_image *zmax, const int *run_flag, uint32_t *flags,
                        cudaStream_t s) {
   unsigned *rendered = f.counters + 3;
-  k_vis_begin<<<1, 1, 0, s>>>(m, rendered, run_flag);
+  k_vis_begin<<<1, 1, 0, s>>>(m, rendered, run_flag); note_launch();
   sf_image zn = {}, zx = {};
   if (zmin && zmax) {
     launch_zrange_init(*zmin, *zmax, s);
@@ -595,7 +595,7 @@ void launch_visibility(const DevMap &m, const FuseScratch &f, const Cam *c, cons
     zx = *zmax;
   }
   k_visibility<<<sm_count() * 4, 256, 0, s>>>(m, c, zn, zx, (zmin && zmax) ? 1 : 0, rendered,
-                                              run_flag, flags);
+                                              run_flag, flags); note_launch();
 }
 
 void launch_integrate(const DevMap &m, const sf_image &depth, const sf_image &rgb,
@@ -605,7 +605,7 @@ void launch_integrate(const DevMap &m, const sf_image &depth, const sf_image &rg
   sf_image mk = mask ? *mask : sf_image{};
   const bool sem = semantics && nmap && (num_detection <= 0 || mask);
   k_integrate<<<sm_count() * 8, kIntThreads, 0, s>>>(m, depth, rgb, nm, mk, num_detection, c,
-                                                     integrate ? 1 : 0, sem ? 1 : 0, run_flag);
+                                                     integrate ? 1 : 0, sem ? 1 : 0, run_flag); note_launch();
 }
 
 }  // namespace sf

@@ -289,8 +289,8 @@ void launch_icp_step(const IcpWorkspace &w, const IcpLevelArgs &L, const m3 &Rc,
   PoseF p;
   p.Rc = Rc; p.tc = tc; p.Rl = Rl; p.RlI = RlInv; p.tl = tl;
   const int nb = w.max_blocks;
-  k_icp_partials<<<nb, kThreads, 0, s>>>(L, p, w.partials, w.max_blocks);
-  k_icp_reduce<<<1, kThreads, 0, s>>>(w.partials, nb, w.max_blocks, w.sums);
+  k_icp_partials<<<nb, kThreads, 0, s>>>(L, p, w.partials, w.max_blocks); note_launch();
+  k_icp_reduce<<<1, kThreads, 0, s>>>(w.partials, nb, w.max_blocks, w.sums); note_launch();
 }
 
 cudaError_t launch_icp_persistent(const IcpWorkspace &w, const IcpLevelArgs *levels, int nlevels,
@@ -317,6 +317,7 @@ cudaError_t launch_icp_persistent(const IcpWorkspace &w, const IcpLevelArgs *lev
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  note_launch();
   return cudaLaunchKernelEx(&cfg, k_icp_persistent, a);
 }
 

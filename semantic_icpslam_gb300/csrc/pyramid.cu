@@ -182,37 +182,37 @@ void launch_filter_depth(const sf_image &depth, const sf_image &raw, const sf_im
                          float depth_scale, float cutoff, cudaStream_t s) {
   dim3 blk(32, 8);
   const float inv = (float)(1.0 / (double)depth_scale);
-  k_filter_depth<<<grid2d(depth.cols, depth.rows, blk), blk, 0, s>>>(depth, raw, filt, inv, cutoff);
+  k_filter_depth<<<grid2d(depth.cols, depth.rows, blk), blk, 0, s>>>(depth, raw, filt, inv, cutoff); note_launch();
 }
 
 void launch_pyrdown(const sf_image &src, const sf_image &dst, cudaStream_t s) {
   dim3 blk(32, 8);
-  k_pyrdown<<<grid2d(dst.cols, dst.rows, blk), blk, 0, s>>>(src, dst);
+  k_pyrdown<<<grid2d(dst.cols, dst.rows, blk), blk, 0, s>>>(src, dst); note_launch();
 }
 
 void launch_vnmap(const sf_image &depth, const sf_image &vmap, const sf_image &nmap, float fx,
                   float fy, float cx, float cy, float cutoff, cudaStream_t s) {
   dim3 blk(32, 8);
   k_vnmap<<<grid2d(depth.cols, depth.rows, blk), blk, 0, s>>>(
-      depth, vmap, nmap, (float)(1.0 / (double)fx), (float)(1.0 / (double)fy), cx, cy, cutoff);
+      depth, vmap, nmap, (float)(1.0 / (double)fx), (float)(1.0 / (double)fy), cx, cy, cutoff); note_launch();
 }
 
 void launch_vmap(const sf_image &depth, const sf_image &vmap, float fx, float fy, float cx,
                  float cy, float cutoff, cudaStream_t s) {
   dim3 blk(32, 8);
   k_vmap<<<grid2d(depth.cols, depth.rows, blk), blk, 0, s>>>(
-      depth, vmap, (float)(1.0 / (double)fx), (float)(1.0 / (double)fy), cx, cy, cutoff);
+      depth, vmap, (float)(1.0 / (double)fx), (float)(1.0 / (double)fy), cx, cy, cutoff); note_launch();
 }
 
 void launch_nmap(const sf_image &vmap, const sf_image &nmap, cudaStream_t s) {
   dim3 blk(32, 8);
-  k_nmap<<<grid2d(vmap.cols, vmap.rows, blk), blk, 0, s>>>(vmap, nmap);
+  k_nmap<<<grid2d(vmap.cols, vmap.rows, blk), blk, 0, s>>>(vmap, nmap); note_launch();
 }
 
 void launch_resize(const sf_image &vsrc, const sf_image &nsrc, const sf_image &vdst,
                    const sf_image &ndst, cudaStream_t s) {
   dim3 blk(32, 8);
-  k_resize<<<grid2d(vdst.cols, vdst.rows, blk), blk, 0, s>>>(vsrc, nsrc, vdst, ndst);
+  k_resize<<<grid2d(vdst.cols, vdst.rows, blk), blk, 0, s>>>(vsrc, nsrc, vdst, ndst); note_launch();
 }
 
 }  // namespace sf

@@ -253,13 +253,13 @@ void launch_rendering_blocks(const DevMap &m, uint32_t nvis, const sf_image &zmi
                              sf_rendering_block *list, uint32_t *count, const Cam *c,
                              uint32_t *flags, cudaStream_t s) {
   k_project_blocks<<<256, 256, 0, s>>>(m, nvis, c, zmin.cols, zmin.rows, list, count,
-                                       m.c.max_rendering_blocks, flags);
+                                       m.c.max_rendering_blocks, flags); note_launch();
 }
 
 void launch_fill_blocks(const sf_image &zmin, const sf_image &zmax,
                         const sf_rendering_block *list, uint32_t nblocks, cudaStream_t s) {
   if (nblocks == 0) return;
-  k_fill_blocks<<<nblocks, dim3(16, 16), 0, s>>>(zmin, zmax, list, nblocks);
+  k_fill_blocks<<<nblocks, dim3(16, 16), 0, s>>>(zmin, zmax, list, nblocks); note_launch();
 }
 
 void launch_raycast(const DevMap &m, const sf_image &vmap, const sf_image &nmap,
@@ -270,7 +270,7 @@ void launch_raycast(const DevMap &m, const sf_image &vmap, const sf_image &nmap,
   dim3 grd((vmap.cols + 7) / 8, (vmap.rows + 7) / 8);
   sf_image fv = fallback_v ? *fallback_v : sf_image{};
   sf_image fn = fallback_n ? *fallback_n : sf_image{};
-  k_raycast<<<grd, blk, 0, s>>>(m, vmap, nmap, zmin, zmax, c, rendered, fv, fn, run_flag);
+  k_raycast<<<grd, blk, 0, s>>>(m, vmap, nmap, zmin, zmax, c, rendered, fv, fn, run_flag); note_launch();
 }
 
 }  // namespace sf

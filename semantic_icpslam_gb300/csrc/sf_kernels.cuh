@@ -111,5 +111,10 @@ void launch_raycast(const DevMap &m, const sf_image &vmap, const sf_image &nmap,
 // Converts host map config into device constants (DeviceMap.h:166-189).
 MapConst make_map_const(const sf_map_config &cfg);
 
+// Process-wide count of kernel launches issued by this library (graph
+// replays add the kernel nodes of the replayed graph).
+void note_launch(unsigned long long n = 1);
+unsigned long long launches_total();
+
 }  // namespace sf
 #endif

@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 namespace {
@@ -173,7 +174,7 @@ void build_scene(sf_synth &s) {
       double ang = r.range(0, 6.283185307179586);
       double extent = std::max(p.h.x, std::max(p.h.y, p.h.z)) * 1.42;
       double dist = r.range(1.15 + extent, 2.2);
-      p.c = {centre.x + dist * std::cos(ang), centre.y + dist * std::sin(ang), r.range(-1.5 + p.h.z, 0.6)};
+      p.c = {centre.x + dist * std::cos(ang), centre.y + dist * std::sin(ang), r.range(-1.5 + p.h.z, -0.4)};
       for (int q = 0; q < 3; ++q) p.rgb[q] = r.range(40, 230);
       p.cls = (uint8_t)(1 + (int)(r.next() * 80) % 80);
       s.prims.push_back(p);
@@ -211,18 +212,18 @@ void pose_at(const sf_synth &s, int i, double T[16]) {
     double phi = r.range(0, 6.283185307179586) + i * (0.02 / 0.5);
     pos = {3.0 + 0.5 * std::cos(phi), -3.0 + 0.5 * std::sin(phi), 0.05 * std::sin(i * 0.05)};
     yaw = yaw0 + i * 1.0 * deg;
-    pitch = 4.0 * deg * std::sin(i * 0.031);
+    pitch = -15.0 * deg + 4.0 * deg * std::sin(i * 0.031);
   } else if (c.trajectory == SF_TRAJ_SPLINE) {
     // ~1.5 cm per frame along a closed Catmull-Rom spline (0.01 of a
     // segment per frame), yaw drifting ~0.8 degree per frame
     pos = catmull(s.ctrl, i * 0.01);
     yaw = yaw0 + i * 0.8 * deg + 10.0 * deg * std::sin(i * 0.013);
-    pitch = 6.0 * deg * std::sin(i * 0.021);
+    pitch = -15.0 * deg + 6.0 * deg * std::sin(i * 0.021);
   } else {
     // corridor: forward along +x at 1.5 cm per frame
     pos = {1.6 + i * 0.015, -3.0 + 0.2 * std::sin(i * 0.004), 0.1 * std::sin(i * 0.007)};
     yaw = 8.0 * deg * std::sin(i * 0.006);
-    pitch = 3.0 * deg * std::sin(i * 0.011);
+    pitch = -10.0 * deg + 3.0 * deg * std::sin(i * 0.011);
   }
   V3 f = {std::cos(yaw) * std::cos(pitch), std::sin(yaw) * std::cos(pitch), std::sin(pitch)};
   V3 right = unit(V3{f.y, -f.x, 0.0});
@@ -264,7 +265,9 @@ extern "C" int sf_synth_frame(const sf_synth *s, int i, uint16_t *depth, uint8_t
   if (pose) memcpy(pose, T, sizeof(T));
   V3 o = {T[3], T[7], T[11]};
   const uint64_t seed = c.seed;
-  for (int v = 0; v < c.rows; ++v)
+  // rows are independent: render them on all host threads
+  auto render_rows = [&](int v0, int v1) {
+  for (int v = v0; v < v1; ++v)
     for (int u = 0; u < c.cols; ++u) {
       const size_t idx = (size_t)v * c.cols + u;
       V3 dc = {(u - c.cx) / c.fx, (v - c.cy) / c.fy, 1.0};
@@ -304,5 +307,14 @@ extern "C" int sf_synth_frame(const sf_synth *s, int i, uint16_t *depth, uint8_t
         mask[idx] = cls;
       }
     }
+  };
+  unsigned nt = std::thread::hardware_concurrency();
+  nt = nt == 0 ? 1 : (nt > 64 ? 64 : nt);
+  if ((int)nt > c.rows) nt = (unsigned)c.rows;
+  std::vector<std::thread> pool;
+  for (unsigned k = 1; k < nt; ++k)
+    pool.emplace_back(render_rows, (int)((long)c.rows * k / nt), (int)((long)c.rows * (k + 1) / nt));
+  render_rows(0, (int)((long)c.rows / nt));
+  for (auto &th : pool) th.join();
   return 0;
 }

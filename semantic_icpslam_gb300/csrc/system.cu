@@ -146,10 +146,20 @@ struct sf_system {
   // graph
   cudaGraphExec_t gexec = nullptr;
   int graph_sem = -1;  // semantics flag the graph was captured with
+  unsigned long long graph_kernels = 0;  // kernel launches recorded in the graph
   int num_detection_captured = 0;
+  // stage timing (eager form only): events at the stage boundaries
+  int timing = 0;
+  cudaEvent_t ev[8] = {};
 };
 
 namespace {
+
+// Stage boundary marker: 0 start, 1 pyramid, 2 ICP, 3 allocation,
+// 4 visibility + z-range, 5 integration, 6 raycast, 7 resize + stats.
+void mark(sf_system *s, cudaStream_t st, int i) {
+  if (s->timing && s->ev[i]) cudaEventRecord(s->ev[i], st);
+}
 
 int alloc_all(sf_system *s) {
   const int C = s->cfg.cols, R = s->cfg.rows;
@@ -186,6 +196,8 @@ void free_all(sf_system *s) {
   if (s->h_mask) cudaFreeHost(s->h_mask);
   if (s->h_stats) cudaFreeHost(s->h_stats);
   if (s->gexec) cudaGraphExecDestroy(s->gexec);
+  for (auto &e : s->ev)
+    if (e) cudaEventDestroy(e);
 }
 
 // Frame::FillImages depth part (Core/Frame.cc:68-92).
@@ -232,11 +244,15 @@ void enqueue_mapping(sf_system *s, const Cam *cam, const int *run, int num_detec
   sf_image nm0 = img(s->d_nmap[0], C, R, 16), mask = img(s->d_mask, C, R, 1);
   sf_image zmin = img(s->d_zmin, s->zc, s->zr, 4), zmax = img(s->d_zmax, s->zc, s->zr, 4);
   launch_alloc(m, f, depth, cam, run, flags, st);
+  mark(s, st, 3);
   launch_visibility(m, f, cam, &zmin, &zmax, run, flags, st);
+  mark(s, st, 4);
   launch_integrate(m, depth, rgb, &nm0, &mask, num_detection, cam, true, num_detection > 0, run, st);
+  mark(s, st, 5);
   sf_image fv = img(s->d_vmap[0], C, R, 16), fn = img(s->d_nmap[0], C, R, 16);
   launch_raycast(m, img(s->d_mv[0], C, R, 16), img(s->d_mn[0], C, R, 16), zmin, zmax, cam,
                  f.counters + 3, &fv, &fn, run, st);
+  mark(s, st, 6);
   for (int l = 1; l < s->L; ++l)
     launch_resize(img(s->d_mv[l - 1], C >> (l - 1), R >> (l - 1), 16),
                   img(s->d_mn[l - 1], C >> (l - 1), R >> (l - 1), 16),
@@ -246,8 +262,10 @@ void enqueue_mapping(sf_system *s, const Cam *cam, const int *run, int num_detec
 // Device-driven frame (eager and graph forms).
 cudaError_t enqueue_device_frame(sf_system *s, int num_detection, cudaStream_t st) {
   IcpWorkspace &w = ctx_icp(s->ctx);
+  mark(s, st, 0);
   enqueue_pyramid(s, st);
-  k_sys_pre<<<1, 1, 0, st>>>(s->d_sys);
+  mark(s, st, 1);
+  k_sys_pre<<<1, 1, 0, st>>>(s->d_sys); note_launch();
   IcpLevelArgs lv[kMaxLevels];
   icp_levels(s, lv);
   cudaError_t e = cudaMemsetAsync(w.barrier, 0, sizeof(unsigned), st);
@@ -256,10 +274,12 @@ cudaError_t enqueue_device_frame(sf_system *s, int num_detection, cudaStream_t s
                             dev_field<int>(s->d_sys, offsetof(SysDev, icp_run)),
                             ctx_flags(s->ctx), st);
   if (e != cudaSuccess) return e;
-  k_sys_post<<<1, 1, 0, st>>>(s->d_sys, w.ctl, s->tmpl);
+  k_sys_post<<<1, 1, 0, st>>>(s->d_sys, w.ctl, s->tmpl); note_launch();
+  mark(s, st, 2);
   enqueue_mapping(s, dev_field<Cam>(s->d_sys, offsetof(SysDev, cam)),
                   dev_field<int>(s->d_sys, offsetof(SysDev, run)), num_detection, st);
-  k_sys_stats<<<1, 1, 0, st>>>(s->d_sys, w.ctl, map_dev(s->map), ctx_flags(s->ctx), s->d_stats);
+  k_sys_stats<<<1, 1, 0, st>>>(s->d_sys, w.ctl, map_dev(s->map), ctx_flags(s->ctx), s->d_stats); note_launch();
+  mark(s, st, 7);
   return cudaGetLastError();
 }
 
@@ -354,7 +374,7 @@ int run_plain_frame(sf_system *s, int num_detection) {
                     img(s->d_mn[l - 1], C >> (l - 1), R >> (l - 1), 16),
                     img(s->d_mv[l], C >> l, R >> l, 16), img(s->d_mn[l], C >> l, R >> l, 16), st);
   }
-  k_sys_stats<<<1, 1, 0, st>>>(s->d_sys, w.ctl, map_dev(s->map), ctx_flags(s->ctx), s->d_stats);
+  k_sys_stats<<<1, 1, 0, st>>>(s->d_sys, w.ctl, map_dev(s->map), ctx_flags(s->ctx), s->d_stats); note_launch();
   return cudaGetLastError() == cudaSuccess ? SF_OK : SF_ERR_CUDA;
 }
 
@@ -368,9 +388,13 @@ int run_frame(sf_system *s, int num_detection) {
   if (!s->gexec || s->graph_sem != sem || (sem && s->num_detection_captured != num_detection)) {
     if (s->gexec) { cudaGraphExecDestroy(s->gexec); s->gexec = nullptr; }
     cudaGraph_t g = nullptr;
+    const unsigned long long before = launches_total();
     if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return SF_ERR_CUDA;
     cudaError_t e = enqueue_device_frame(s, num_detection, st);
     cudaError_t e2 = cudaStreamEndCapture(st, &g);
+    // captured launches are recorded, not run: count them per replay instead
+    s->graph_kernels = launches_total() - before;
+    note_launch(0ull - s->graph_kernels);
     if (e != cudaSuccess || e2 != cudaSuccess || !g) {
       if (g) cudaGraphDestroy(g);
       cudaGetLastError();
@@ -382,7 +406,9 @@ int run_frame(sf_system *s, int num_detection) {
     s->graph_sem = sem;
     s->num_detection_captured = num_detection;
   }
-  return cudaGraphLaunch(s->gexec, st) == cudaSuccess ? SF_OK : SF_ERR_CUDA;
+  if (cudaGraphLaunch(s->gexec, st) != cudaSuccess) return SF_ERR_CUDA;
+  note_launch(s->graph_kernels);
+  return SF_OK;
 }
 
 }  // namespace
@@ -509,6 +535,24 @@ int sf_system_frame_maps(sf_system *s, int level, sf_image *vmap, sf_image *nmap
   if (vmap) *vmap = img(s->d_vmap[level], c, r, 16);
   if (nmap) *nmap = img(s->d_nmap[level], c, r, 16);
   if (depth) *depth = img(s->d_depth[level], c, r, 4);
+  return SF_OK;
+}
+
+int sf_system_set_timing(sf_system *s, int enable) {
+  if (!s) return SF_ERR_INVALID;
+  if (enable && s->cfg.use_graph == 1) return SF_ERR_STATE;  // events are not captured
+  if (enable && !s->ev[0])
+    for (auto &e : s->ev)
+      if (cudaEventCreate(&e) != cudaSuccess) return SF_ERR_CUDA;
+  s->timing = enable ? 1 : 0;
+  return SF_OK;
+}
+
+int sf_system_stage_ms(sf_system *s, float ms[7]) {
+  if (!s || !ms || !s->timing) return SF_ERR_INVALID;
+  if (cudaEventSynchronize(s->ev[7]) != cudaSuccess) return SF_ERR_CUDA;
+  for (int i = 0; i < 7; ++i)
+    if (cudaEventElapsedTime(&ms[i], s->ev[i], s->ev[i + 1]) != cudaSuccess) return SF_ERR_CUDA;
   return SF_OK;
 }
 
