@@ -158,8 +158,9 @@ def test_map_and_raytrace_vs_reference(env):
         nm = cuda(O.nmap(O.vmap(filt, *_K(g), 3.0)))  # oracle == reference here (pinned)
         R, RI, t = sf.pose_to_gpu(g["pose%d" % i])
         nvis = C.c_uint32()
-        sf.call("sf_FuseMapColor", ctx.h, m.h, sf.image(raw), sf.image(cuda(g["rgb%d" % i])), sf.image(nm),
-                sf.image(cuda(g["mask%d" % i])), 10 if i >= 2 else 0, R, RI, t, *_K(g), 3.0, 0.1, C.byref(nvis))
+        rgb, mask = cuda(g["rgb%d" % i]), cuda(g["mask%d" % i])  # keep the device buffers alive
+        sf.call("sf_FuseMapColor", ctx.h, m.h, sf.image(raw), sf.image(rgb), sf.image(nm),
+                sf.image(mask), 10 if i >= 2 else 0, R, RI, t, *_K(g), 3.0, 0.1, C.byref(nvis))
         cnt = m.counters(ctx)
         ref = g["counters"][i]
         assert cnt[0] == ref[0] and cnt[1] == ref[1] and cnt[3] == ref[3], "frame %d" % i
