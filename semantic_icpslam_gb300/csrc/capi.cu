@@ -535,7 +535,9 @@ int sf_Raycast(sf_context *ctx, sf_map *m, sf_image vmap, sf_image nmap, sf_imag
   c.invfy = invfy;
   int st = upload_cam(ctx, c);
   if (st) return st;
-  launch_raycast(m->d, vmap, nmap, zmin, zmax, ctx->cam, nullptr, nullptr, nullptr, nullptr,
+  if ((st = ensure_scratch(m, vmap.cols * vmap.rows))) return st;
+  launch_window_build(m->d, m->scratch, ctx->cam, ctx->stream);
+  launch_raycast(m->d, m->scratch, vmap, nmap, zmin, zmax, ctx->cam, nullptr, nullptr, nullptr, nullptr,
                  ctx->stream);
   SF_CHECK(cudaGetLastError());
   return SF_OK;

@@ -317,11 +317,13 @@ __device__ __forceinline__ bool block_visible(const Cam &c, float s, i3 pos) {
   return false;
 }
 
-__global__ void k_visibility(DevMap m, const Cam *cam, sf_image zmin, sf_image zmax, int do_z,
-                             unsigned *rendered, const int *run_flag, uint32_t *flags) {
+__global__ void k_visibility(DevMap m, FuseScratch f, const Cam *cam, sf_image zmin, sf_image zmax,
+                             int do_z, unsigned *rendered, const int *run_flag, uint32_t *flags) {
   if (run_flag && *run_flag == 0) return;
   const Cam c = *cam;
   const unsigned n = (unsigned)*m.alloc_count;
+  int win[6];
+  for (int k = 0; k < 6; ++k) win[k] = f.win[k];
   // grid-stride with whole warps so warp_append sees converged lanes
   for (unsigned base = blockIdx.x * blockDim.x; base < n; base += grid_stride()) {
     const unsigned k = base + threadIdx.x;
@@ -335,6 +337,9 @@ __global__ void k_visibility(DevMap m, const Cam *cam, sf_image zmin, sf_image z
       h1 = __ldcg((const int4 *)(m.entries + idx) + 1);
       i3 pos; pos.x = h0.x; pos.y = h0.y; pos.z = h0.z;
       vis = h0.w != -1 && block_visible(c, m.c.block_width, pos);
+      // every allocated block inside the frustum box goes into the window
+      const int cell = window_cell(win, pos);
+      if (cell >= 0) f.win_cells[cell] = h0.w;
     }
     unsigned slot = warp_append(m.no_visible, vis);
     if (vis) {
@@ -366,10 +371,30 @@ __global__ void k_zrange_init(sf_image zmin, sf_image zmax) {
   row_ptr<float>(zmax, y)[x] = 0.f;
 }
 
-__global__ void k_vis_begin(DevMap m, unsigned *rendered, const int *run_flag) {
+// Per-frame start of the visibility pass: counters and the window box.
+__global__ void k_vis_begin(DevMap m, FuseScratch f, const Cam *cam, unsigned *rendered,
+                            const int *run_flag) {
   if (run_flag && *run_flag == 0) return;
   *m.no_visible = 0u;
   if (rendered) *rendered = 0u;
+  window_setup(*cam, m.c.block_width, m.c.depth_min, m.c.depth_max, f.win_cap, f.win);
+}
+
+// Clears the window cells and (when given) the z-range images.
+__global__ void k_vis_clear(FuseScratch f, sf_image zmin, sf_image zmax, int do_z,
+                            const int *run_flag) {
+  if (run_flag && *run_flag == 0) return;
+  const unsigned ncell = (unsigned)f.win[3] * (unsigned)f.win[4] * (unsigned)f.win[5];
+  const unsigned nz = do_z ? (unsigned)(zmin.cols * zmin.rows) : 0u;
+  const unsigned n = ncell > nz ? ncell : nz;
+  for (unsigned i = grid_tid(); i < n; i += grid_stride()) {
+    if (i < ncell) f.win_cells[i] = -1;
+    if (i < nz) {
+      const int y = (int)(i / (unsigned)zmin.cols), x = (int)(i % (unsigned)zmin.cols);
+      row_ptr<float>(zmin, y)[x] = 100.f;
+      row_ptr<float>(zmax, y)[x] = 0.f;
+    }
+  }
 }
 
 // -------------------------------------------------------------- integrate
@@ -532,6 +557,10 @@ int fuse_scratch_init(FuseScratch &f, const MapConst &c, int max_pixels) {
   if (cudaMemset(f.bucket_head, 0xff, sizeof(int) * c.num_buckets) != cudaSuccess) return SF_ERR_CUDA;
   if (cudaMalloc(&f.counters, sizeof(unsigned) * 4) != cudaSuccess) return SF_ERR_CUDA;
   if (cudaMemset(f.counters, 0, sizeof(unsigned) * 4) != cudaSuccess) return SF_ERR_CUDA;
+  f.win_cap = 1u << 23;
+  if (cudaMalloc(&f.win, sizeof(int) * 8) != cudaSuccess) return SF_ERR_CUDA;
+  if (cudaMemset(f.win, 0, sizeof(int) * 8) != cudaSuccess) return SF_ERR_CUDA;
+  if (cudaMalloc(&f.win_cells, sizeof(int) * (size_t)f.win_cap) != cudaSuccess) return SF_ERR_CUDA;
   return SF_OK;
 }
 
@@ -542,6 +571,8 @@ void fuse_scratch_free(FuseScratch &f) {
   cudaFree(f.dirty);
   cudaFree(f.bucket_head);
   cudaFree(f.counters);
+  cudaFree(f.win);
+  cudaFree(f.win_cells);
   f = FuseScratch();
 }
 
@@ -587,15 +618,12 @@ void launch_visibility(const DevMap &m, const FuseScratch &f, const Cam *c, cons
                        const sf_image *zmax, const int *run_flag, uint32_t *flags,
                        cudaStream_t s) {
   unsigned *rendered = f.counters + 3;
-  k_vis_begin<<<1, 1, 0, s>>>(m, rendered, run_flag); note_launch();
-  sf_image zn = {}, zx = {};
-  if (zmin && zmax) {
-    launch_zrange_init(*zmin, *zmax, s);
-    zn = *zmin;
-    zx = *zmax;
-  }
-  k_visibility<<<sm_count() * 4, 256, 0, s>>>(m, c, zn, zx, (zmin && zmax) ? 1 : 0, rendered,
-                                              run_flag, flags); note_launch();
+  const bool do_z = zmin && zmax;
+  sf_image zn = do_z ? *zmin : sf_image{}, zx = do_z ? *zmax : sf_image{};
+  k_vis_begin<<<1, 1, 0, s>>>(m, f, c, rendered, run_flag); note_launch();
+  k_vis_clear<<<sm_count() * 8, 256, 0, s>>>(f, zn, zx, do_z ? 1 : 0, run_flag); note_launch();
+  k_visibility<<<sm_count() * 4, 256, 0, s>>>(m, f, c, zn, zx, do_z ? 1 : 0, rendered, run_flag,
+                                              flags); note_launch();
 }
 
 void launch_integrate(const DevMap &m, const sf_image &depth, const sf_image &rgb,

@@ -14,6 +14,7 @@
 // 6x6 LDLT solve and SE(3) update, so all CTAs hold the same pose without a
 // second barrier.  Partials are double-buffered by iteration parity.
 #include "sf_kernels.cuh"
+#include "sf_solve_warp.cuh"
 
 namespace sf {
 
@@ -196,6 +197,7 @@ struct PersistentArgs {
 
 __global__ void __launch_bounds__(kThreads) k_icp_persistent(PersistentArgs a) {
   __shared__ TrackCtl ctl;
+  __shared__ WarpSolveScratch wsolve;
   __shared__ PoseF pose;
   __shared__ double bsum[29];
   __shared__ double sums[29];
@@ -223,7 +225,7 @@ __global__ void __launch_bounds__(kThreads) k_icp_persistent(PersistentArgs a) {
       if (threadIdx.x < 29) part[(size_t)threadIdx.x * a.stride + blockIdx.x] = bsum[threadIdx.x];
       grid_barrier(a.barrier, nb, a.flags);
       cross_block_sum(part, nb, a.stride, sums);
-      if (threadIdx.x == 0) ctl_step(ctl, sums, L.min_count);
+      if (threadIdx.x < 32) ctl_step_warp(ctl, sums, L.min_count, wsolve);
       __syncthreads();
       buf ^= 1;
       if (ctl.stop) break;

@@ -83,96 +83,104 @@ __global__ void k_fill_blocks(sf_image zmin, sf_image zmax, const sf_rendering_b
 }
 
 // ---------------------------------------------------------------- raycast
-struct RayCache {
-  int x, y, z, ptr;
-  bool set;
+// Block lookup for the ray: the frame's block-pointer window, the hash table
+// (DeviceMap::FindEntry) outside it.  Equal to FindEntry for every block,
+// so the per-ray entry cache of DeviceMap::FindVoxel (DeviceMap.cu:116-133)
+// has nothing left to save and is not kept.  (The reference's cache starts
+// as {pos (0,0,0), ptr -1}, which would alias block (0,0,0) to voxel index
+// -1; that aliasing is not reproduced.)
+struct RayCtx {
+  const DevMap *m;
+  const int *cells;
+  int win[6];
 };
+
+__device__ __forceinline__ int block_ptr(const RayCtx &r, i3 bp) {
+  const int cell = window_cell(r.win, bp);
+  if (cell >= 0) return __ldg(r.cells + cell);
+  return find_block(*r.m, bp);
+}
 
 struct VoxelRead {
   float sdf;
   unsigned weight;
+  bool found;
 };
 
-// DeviceMap::FindVoxel(float3, cache, valid) (DeviceMap.cu:116-133).  The
-// cache starts empty (the reference's default HashEntry would alias block
-// (0,0,0) to voxel index -1).
-__device__ __forceinline__ VoxelRead find_voxel(const DevMap &m, f3 pt, RayCache &c, bool &valid) {
-  i3 p = floor3(pt);
-  i3 bp = vox2block(p);
-  int ptr;
-  if (c.set && bp.x == c.x && bp.y == c.y && bp.z == c.z) {
-    ptr = c.ptr;
-  } else {
-    ptr = find_block(m, bp);
-    if (ptr < 0) {
-      valid = false;
-      VoxelRead r;
-      r.sdf = nanf_bits();
-      r.weight = 0;
-      return r;
-    }
-    c.x = bp.x; c.y = bp.y; c.z = bp.z; c.ptr = ptr; c.set = true;
+// DeviceMap::FindVoxel(float3, cache, valid): a missing block reads as
+// Voxel() (sdf NaN, weight 0) and valid = false.
+__device__ __forceinline__ VoxelRead read_voxel(const RayCtx &r, f3 pt) {
+  const i3 p = floor3(pt);
+  const int ptr = block_ptr(r, vox2block(p));
+  VoxelRead v;
+  if (ptr < 0) {
+    v.sdf = nanf_bits();
+    v.weight = 0;
+    v.found = false;
+    return v;
   }
-  valid = true;
-  uint2 raw = __ldg((const uint2 *)(m.voxels + ptr + vox2local(p)));
-  VoxelRead r;
-  r.sdf = __uint_as_float(raw.x);
-  r.weight = raw.y & 0xffu;
-  return r;
+  const uint2 raw = __ldg((const uint2 *)(r.m->voxels + ptr + vox2local(p)));
+  v.sdf = __uint_as_float(raw.x);
+  v.weight = raw.y & 0xffu;
+  v.found = true;
+  return v;
 }
 
 // Rendering::readSdf (RenderScene.cu:303-308).
-__device__ __forceinline__ float read_sdf(const DevMap &m, f3 pt, RayCache &c, bool &valid) {
-  VoxelRead v = find_voxel(m, pt, c, valid);
-  if (v.weight == 0) valid = false;
+__device__ __forceinline__ float read_sdf(const RayCtx &r, f3 pt, bool &valid) {
+  VoxelRead v = read_voxel(r, pt);
+  valid = v.found && v.weight != 0;
   return v.sdf;
 }
 
-// Rendering::readSdfInterped (RenderScene.cu:310-343).
-__device__ __forceinline__ float read_sdf_interp(const DevMap &m, f3 pt, RayCache &c, bool &valid) {
-  f3 xyz3 = pt - mk3(floorf(pt.x), floorf(pt.y), floorf(pt.z));
-  float s0, s1, r0, r1, r2, r3;
-  s0 = find_voxel(m, pt, c, valid).sdf;
-  s1 = find_voxel(m, pt + mk3(1, 0, 0), c, valid).sdf;
-  r0 = (1.0f - xyz3.x) * s0 + xyz3.x * s1;
-  s0 = find_voxel(m, pt + mk3(0, 1, 0), c, valid).sdf;
-  s1 = find_voxel(m, pt + mk3(1, 1, 0), c, valid).sdf;
-  r1 = (1.0f - xyz3.x) * s0 + xyz3.x * s1;
-  r2 = (1.0f - xyz3.y) * r0 + xyz3.y * r1;
-  s0 = find_voxel(m, pt + mk3(0, 0, 1), c, valid).sdf;
-  s1 = find_voxel(m, pt + mk3(1, 0, 1), c, valid).sdf;
-  r0 = (1.0f - xyz3.x) * s0 + xyz3.x * s1;
-  s0 = find_voxel(m, pt + mk3(0, 1, 1), c, valid).sdf;
-  s1 = find_voxel(m, pt + mk3(1, 1, 1), c, valid).sdf;
-  r1 = (1.0f - xyz3.x) * s0 + xyz3.x * s1;
-  r3 = (1.0f - xyz3.y) * r0 + xyz3.y * r1;
+// Rendering::readSdfInterped (RenderScene.cu:310-343).  The eight corner
+// reads are independent; `valid` is the last corner's (pt + (1,1,1)), as
+// each FindVoxel call overwrites it in the reference.
+__device__ __forceinline__ float read_sdf_interp(const RayCtx &r, f3 pt, bool &valid) {
+  const f3 xyz3 = pt - mk3(floorf(pt.x), floorf(pt.y), floorf(pt.z));
+  const VoxelRead c000 = read_voxel(r, pt);
+  const VoxelRead c100 = read_voxel(r, pt + mk3(1, 0, 0));
+  const VoxelRead c010 = read_voxel(r, pt + mk3(0, 1, 0));
+  const VoxelRead c110 = read_voxel(r, pt + mk3(1, 1, 0));
+  const VoxelRead c001 = read_voxel(r, pt + mk3(0, 0, 1));
+  const VoxelRead c101 = read_voxel(r, pt + mk3(1, 0, 1));
+  const VoxelRead c011 = read_voxel(r, pt + mk3(0, 1, 1));
+  const VoxelRead c111 = read_voxel(r, pt + mk3(1, 1, 1));
+  float r0 = (1.0f - xyz3.x) * c000.sdf + xyz3.x * c100.sdf;
+  float r1 = (1.0f - xyz3.x) * c010.sdf + xyz3.x * c110.sdf;
+  const float r2 = (1.0f - xyz3.y) * r0 + xyz3.y * r1;
+  r0 = (1.0f - xyz3.x) * c001.sdf + xyz3.x * c101.sdf;
+  r1 = (1.0f - xyz3.x) * c011.sdf + xyz3.x * c111.sdf;
+  const float r3 = (1.0f - xyz3.y) * r0 + xyz3.y * r1;
+  valid = c111.found;
   return (1.0f - xyz3.z) * r2 + xyz3.z * r3;
 }
 
 // Rendering::readNormal (RenderScene.cu:345-378).
-__device__ __forceinline__ bool read_normal(const DevMap &m, f3 pt, RayCache &c, const m3 &Rinv,
-                                            f3 &n) {
+__device__ __forceinline__ bool read_normal(const RayCtx &r, f3 pt, const m3 &Rinv, f3 &n) {
   bool valid;
-  float s[6];
-  const f3 offs[6] = {mk3(1, 0, 0), mk3(-1, 0, 0), mk3(0, 1, 0),
-                      mk3(0, -1, 0), mk3(0, 0, 1), mk3(0, 0, -1)};
-#pragma unroll
-  for (int k = 0; k < 6; ++k) {
-    s[k] = read_sdf_interp(m, pt + offs[k], c, valid);
-    if (isnan(s[k]) || s[k] == 1.0f || !valid) return false;
-  }
-  n = mk3(s[0] - s[1], s[2] - s[3], s[4] - s[5]);
-  n = normalised(mul(Rinv, n));
+  const float s0 = read_sdf_interp(r, pt + mk3(1, 0, 0), valid);
+  if (isnan(s0) || s0 == 1.0f || !valid) return false;
+  const float s1 = read_sdf_interp(r, pt + mk3(-1, 0, 0), valid);
+  if (isnan(s1) || s1 == 1.0f || !valid) return false;
+  const float s2 = read_sdf_interp(r, pt + mk3(0, 1, 0), valid);
+  if (isnan(s2) || s2 == 1.0f || !valid) return false;
+  const float s3 = read_sdf_interp(r, pt + mk3(0, -1, 0), valid);
+  if (isnan(s3) || s3 == 1.0f || !valid) return false;
+  const float s4 = read_sdf_interp(r, pt + mk3(0, 0, 1), valid);
+  if (isnan(s4) || s4 == 1.0f || !valid) return false;
+  const float s5 = read_sdf_interp(r, pt + mk3(0, 0, -1), valid);
+  if (isnan(s5) || s5 == 1.0f || !valid) return false;
+  n = normalised(mul(Rinv, mk3(s0 - s1, s2 - s3, s4 - s5)));
   return true;
 }
 
 // Rendering::operator() (RenderScene.cu:380-488).
-__global__ void __launch_bounds__(64) k_raycast(DevMap m, sf_image vmap, sf_image nmap, sf_image zmin,
-                                                sf_image zmax, const Cam *cam,
-                                                const unsigned *rendered, sf_image fb_v,
-                                                sf_image fb_n, const int *run_flag) {
+__global__ void __launch_bounds__(128) k_raycast(DevMap m, FuseScratch f, sf_image vmap, sf_image nmap,
+                                                 sf_image zmin, sf_image zmax, const Cam *cam,
+                                                 const unsigned *rendered, sf_image fb_v,
+                                                 sf_image fb_n, const int *run_flag) {
   if (run_flag && *run_flag == 0) return;
-  const Cam c = *cam;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= vmap.cols || y >= vmap.rows) return;
@@ -184,6 +192,11 @@ __global__ void __launch_bounds__(64) k_raycast(DevMap m, sf_image vmap, sf_imag
     }
     return;
   }
+  const Cam c = *cam;
+  RayCtx r;
+  r.m = &m;
+  r.cells = f.win_cells;
+  for (int k = 0; k < 6; ++k) r.win[k] = f.win[k];
   float4 vout = nan4(), nout = nan4();
   const int lx = (int)floorf((float)x / 8.0f), ly = (int)floorf((float)y / 8.0f);
   const float zx = __ldg(row_ptr<const float>(zmin, ly) + lx);
@@ -196,27 +209,23 @@ __global__ void __launch_bounds__(64) k_raycast(DevMap m, sf_image vmap, sf_imag
     p.x = p.z * ((float)x - c.cx) * c.invfx;
     p.y = p.z * ((float)y - c.cy) * c.invfy;
     float dist_s = norm(p) * vsi;
-    f3 block_s = (mul(c.R, p) + c.t) * vsi;
+    const f3 block_s = (mul(c.R, p) + c.t) * vsi;
     p.z = zy;
     p.x = p.z * ((float)x - c.cx) * c.invfx;
     p.y = p.z * ((float)y - c.cy) * c.invfy;
-    float dist_e = norm(p) * vsi;
-    f3 block_e = (mul(c.R, p) + c.t) * vsi;
-    f3 dir = normalised(block_e - block_s);
+    const float dist_e = norm(p) * vsi;
+    const f3 block_e = (mul(c.R, p) + c.t) * vsi;
+    const f3 dir = normalised(block_e - block_s);
     f3 result = block_s;
-    bool valid_sdf = false, found_pt = false, behind = false;
+    bool valid_sdf = false, behind = false;
     float step, prev_sdf;
-    RayCache cache;
-    cache.x = cache.y = cache.z = 0;
-    cache.ptr = -1;
-    cache.set = false;
     while (dist_s < dist_e) {
       prev_sdf = sdf;
-      sdf = read_sdf(m, result, cache, valid_sdf);
+      sdf = read_sdf(r, result, valid_sdf);
       if (!valid_sdf) {
         step = 8.0f;
       } else {
-        if (sdf <= 0.1f && sdf >= -0.5f) sdf = read_sdf_interp(m, result, cache, valid_sdf);
+        if (sdf <= 0.1f && sdf >= -0.5f) sdf = read_sdf_interp(r, result, valid_sdf);
         if (prev_sdf < 0.f && sdf >= 0.f) { behind = true; break; }
         if (prev_sdf > 0.f && sdf <= 0.f) break;
         step = 1.0f;
@@ -224,27 +233,43 @@ __global__ void __launch_bounds__(64) k_raycast(DevMap m, sf_image vmap, sf_imag
       result = result + step * dir;
       dist_s += step;
     }
-    if (!behind) {
-      if (sdf <= 0.0f) {
-        step = sdf * m.c.step_scale;
-        result = result + step * dir;
-        sdf = read_sdf_interp(m, result, cache, valid_sdf);
-        step = sdf * m.c.step_scale;
-        result = result + step * dir;
-        found_pt = true;
-      }
-      if (found_pt) {
-        f3 n;
-        if (read_normal(m, result, cache, c.Rinv, n)) {
-          f3 r = mul(c.Rinv, result * m.c.voxel_size - c.t);
-          vout = make_float4(r.x, r.y, r.z, 1.0f);
-          nout = make_float4(n.x, n.y, n.z, 1.0f);
-        }
+    if (!behind && sdf <= 0.0f) {
+      step = sdf * m.c.step_scale;
+      result = result + step * dir;
+      sdf = read_sdf_interp(r, result, valid_sdf);
+      step = sdf * m.c.step_scale;
+      result = result + step * dir;
+      f3 n;
+      if (read_normal(r, result, c.Rinv, n)) {
+        const f3 q = mul(c.Rinv, result * m.c.voxel_size - c.t);
+        vout = make_float4(q.x, q.y, q.z, 1.0f);
+        nout = make_float4(n.x, n.y, n.z, 1.0f);
       }
     }
   }
   row_ptr<float4>(vmap, y)[x] = vout;
   row_ptr<float4>(nmap, y)[x] = nout;
+}
+
+// Builds the block window for the reference-shaped Raycast entry point.
+__global__ void k_window_build_setup(DevMap m, FuseScratch f, const Cam *cam) {
+  window_setup(*cam, m.c.block_width, m.c.depth_min, m.c.depth_max, f.win_cap, f.win);
+}
+__global__ void k_window_build_clear(FuseScratch f) {
+  const unsigned n = (unsigned)f.win[3] * (unsigned)f.win[4] * (unsigned)f.win[5];
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    f.win_cells[i] = -1;
+}
+__global__ void k_window_build_fill(DevMap m, FuseScratch f) {
+  const unsigned n = (unsigned)*m.alloc_count;
+  int win[6];
+  for (int k = 0; k < 6; ++k) win[k] = f.win[k];
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int4 h = entry_head(m.entries + m.alloc_list[k]);
+    i3 pos; pos.x = h.x; pos.y = h.y; pos.z = h.z;
+    const int cell = window_cell(win, pos);
+    if (cell >= 0 && h.w >= 0) f.win_cells[cell] = h.w;
+  }
 }
 
 }  // namespace
@@ -262,15 +287,21 @@ void launch_fill_blocks(const sf_image &zmin, const sf_image &zmax,
   k_fill_blocks<<<nblocks, dim3(16, 16), 0, s>>>(zmin, zmax, list, nblocks); note_launch();
 }
 
-void launch_raycast(const DevMap &m, const sf_image &vmap, const sf_image &nmap,
+void launch_raycast(const DevMap &m, const FuseScratch &f, const sf_image &vmap, const sf_image &nmap,
                     const sf_image &zmin, const sf_image &zmax, const Cam *c,
                     const unsigned *rendered, const sf_image *fallback_v,
                     const sf_image *fallback_n, const int *run_flag, cudaStream_t s) {
-  dim3 blk(8, 8);
-  dim3 grd((vmap.cols + 7) / 8, (vmap.rows + 7) / 8);
+  dim3 blk(8, 16);
+  dim3 grd((vmap.cols + 7) / 8, (vmap.rows + 15) / 16);
   sf_image fv = fallback_v ? *fallback_v : sf_image{};
   sf_image fn = fallback_n ? *fallback_n : sf_image{};
-  k_raycast<<<grd, blk, 0, s>>>(m, vmap, nmap, zmin, zmax, c, rendered, fv, fn, run_flag); note_launch();
+  k_raycast<<<grd, blk, 0, s>>>(m, f, vmap, nmap, zmin, zmax, c, rendered, fv, fn, run_flag); note_launch();
+}
+
+void launch_window_build(const DevMap &m, const FuseScratch &f, const Cam *c, cudaStream_t s) {
+  k_window_build_setup<<<1, 1, 0, s>>>(m, f, c); note_launch();
+  k_window_build_clear<<<256, 256, 0, s>>>(f); note_launch();
+  k_window_build_fill<<<256, 256, 0, s>>>(m, f); note_launch();
 }
 
 }  // namespace sf

@@ -63,6 +63,13 @@ struct FuseScratch {
   int *bucket_head = nullptr;             // [num_buckets], -1 when idle
   int *dirty = nullptr;                   // [pend_cap] buckets with requests
   unsigned *counters = nullptr;           // [4] pending, dirty, epoch, any_rendered
+  // Dense block-pointer window over the camera frustum's bounding box,
+  // rebuilt with the visible set every frame: cell = the block's voxel
+  // index (ptr) or -1.  win = {ox, oy, oz, nx, ny, nz}.  Lookups outside the
+  // window go to the hash table, so the window only accelerates.
+  int *win = nullptr;                     // [8]
+  int *win_cells = nullptr;               // [win_cap]
+  uint32_t win_cap = 0;
 };
 
 int fuse_scratch_init(FuseScratch &f, const MapConst &c, int max_pixels);
@@ -103,10 +110,13 @@ void launch_fill_blocks(const sf_image &zmin, const sf_image &zmax,
 // Rendering (RenderScene.cu:291-489).  fallback_v/n (may be null): when
 // *rendered == 0 the output is a copy of the fallback maps (the reference
 // skips the raycast and keeps the frame's own maps).
-void launch_raycast(const DevMap &m, const sf_image &vmap, const sf_image &nmap,
+void launch_raycast(const DevMap &m, const FuseScratch &f, const sf_image &vmap, const sf_image &nmap,
                     const sf_image &zmin, const sf_image &zmax, const Cam *c,
                     const unsigned *rendered, const sf_image *fallback_v,
                     const sf_image *fallback_n, const int *run_flag, cudaStream_t s);
+// Block-pointer window for camera c from the allocated-entry index (the
+// per-frame path builds it inside launch_visibility).
+void launch_window_build(const DevMap &m, const FuseScratch &f, const Cam *c, cudaStream_t s);
 
 // Converts host map config into device constants (DeviceMap.h:166-189).
 MapConst make_map_const(const sf_map_config &cfg);

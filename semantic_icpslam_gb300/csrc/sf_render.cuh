@@ -3,9 +3,48 @@
 #ifndef SF_RENDER_CUH_
 #define SF_RENDER_CUH_
 
-#include "sf_device.cuh"
+#include "sf_kernels.cuh"
 
 namespace sf {
+
+// ------------------------------------------------- block-pointer window
+// Bounding box, in block coordinates, of the camera frustum between depth
+// dmin and dmax (+ margins for the raycast's interpolation and normal
+// offsets).  Float arithmetic is fine here: the window only accelerates
+// lookups; any block outside it is found through the hash table.
+__device__ __forceinline__ void window_setup(const Cam &c, float bw, float dmin, float dmax,
+                                             uint32_t cap, int *win) {
+  float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+  const float us[2] = {0.f, (float)c.cols}, vs[2] = {0.f, (float)c.rows};
+  const float zs[2] = {dmin, dmax + 2.0f * bw};
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b)
+      for (int k = 0; k < 2; ++k) {
+        f3 pc = mk3((us[a] - c.cx) / c.fx * zs[k], (vs[b] - c.cy) / c.fy * zs[k], zs[k]);
+        f3 pw = mul(c.R, pc) + c.t;
+        const float p[3] = {pw.x, pw.y, pw.z};
+        for (int d = 0; d < 3; ++d) { lo[d] = fminf(lo[d], p[d]); hi[d] = fmaxf(hi[d], p[d]); }
+      }
+  int o[3], n[3];
+  long long total = 1;
+  for (int d = 0; d < 3; ++d) {
+    if (!(lo[d] > -1.0e7f && hi[d] < 1.0e7f)) { win[3] = win[4] = win[5] = 0; return; }
+    int a = (int)floorf(lo[d] / bw) - 1, b = (int)floorf(hi[d] / bw) + 1;
+    o[d] = a;
+    n[d] = b - a + 1;
+    total *= n[d];
+  }
+  if (total > (long long)cap) { win[3] = win[4] = win[5] = 0; return; }
+  win[0] = o[0]; win[1] = o[1]; win[2] = o[2];
+  win[3] = n[0]; win[4] = n[1]; win[5] = n[2];
+}
+
+// Cell of block bp in the window, or -1 when outside.
+__device__ __forceinline__ int window_cell(const int *win, i3 bp) {
+  const unsigned x = (unsigned)(bp.x - win[0]), y = (unsigned)(bp.y - win[1]), z = (unsigned)(bp.z - win[2]);
+  if (x >= (unsigned)win[3] || y >= (unsigned)win[4] || z >= (unsigned)win[5]) return -1;
+  return (int)((z * (unsigned)win[4] + y) * (unsigned)win[3] + x);
+}
 
 // Projection::projectBlock (RenderScene.cu:54-112).
 __device__ __forceinline__ bool project_block(i3 pos, float voxel, const m3 &Rinv, f3 t, float fx, float fy,

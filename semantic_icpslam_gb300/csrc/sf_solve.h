@@ -66,8 +66,10 @@ SF_HD void ldlt_solve6(const double *A36, const double *b6, double *x6) {
     for (int j = 0; j < i; ++j) y[i] -= a[i * 6 + j] * y[j];
   const double tol = 2.2250738585072014e-308;  // smallest normal double
   for (int i = 0; i < 6; ++i) y[i] = (fabs(d[i]) > tol) ? y[i] / d[i] : 0.0;
-  for (int i = 5; i >= 0; --i)
-    for (int j = i + 1; j < 6; ++j) y[i] -= a[j * 6 + i] * y[j];
+  // back substitution with j descending (the order the warp-parallel
+  // device version can reproduce bit for bit)
+  for (int j = 5; j >= 1; --j)
+    for (int i = j - 1; i >= 0; --i) y[i] -= a[j * 6 + i] * y[j];
   for (int i = 0; i < 6; ++i) x6[perm[i]] = y[i];
 }
 

@@ -250,7 +250,7 @@ void enqueue_mapping(sf_system *s, const Cam *cam, const int *run, int num_detec
   launch_integrate(m, depth, rgb, &nm0, &mask, num_detection, cam, true, num_detection > 0, run, st);
   mark(s, st, 5);
   sf_image fv = img(s->d_vmap[0], C, R, 16), fn = img(s->d_nmap[0], C, R, 16);
-  launch_raycast(m, img(s->d_mv[0], C, R, 16), img(s->d_mn[0], C, R, 16), zmin, zmax, cam,
+  launch_raycast(m, f, img(s->d_mv[0], C, R, 16), img(s->d_mn[0], C, R, 16), zmin, zmax, cam,
                  f.counters + 3, &fv, &fn, run, st);
   mark(s, st, 6);
   for (int l = 1; l < s->L; ++l)
@@ -367,7 +367,7 @@ int run_plain_frame(sf_system *s, int num_detection) {
       launch_integrate(m, depth, rgb, &nm0, &mask, num_detection, cam, true, num_detection > 0,
                        nullptr, st);
     sf_image fv = img(s->d_vmap[0], C, R, 16), fn = img(s->d_nmap[0], C, R, 16);
-    launch_raycast(m, img(s->d_mv[0], C, R, 16), img(s->d_mn[0], C, R, 16), zmin, zmax, cam,
+    launch_raycast(m, f, img(s->d_mv[0], C, R, 16), img(s->d_mn[0], C, R, 16), zmin, zmax, cam,
                    f.counters + 3, &fv, &fn, nullptr, st);
     for (int l = 1; l < s->L; ++l)
       launch_resize(img(s->d_mv[l - 1], C >> (l - 1), R >> (l - 1), 16),
