@@ -275,6 +275,10 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--map-blocks", type=int, default=19,
+                    help="log2 of the voxel-block heap (2^19 blocks = 4 GB of voxels)")
+    ap.add_argument("--quick", action="store_true",
+                    help="only the CUDA-graph timing (for profiler runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -294,6 +298,7 @@ def main():
     sf.load()
     ctx = sf.Context()
     n = args.steps + args.warmup
+    MAP["num_sdf_blocks"] = 1 << args.map_blocks
     frames = make_frames(n, rank)
 
     # headline: CUDA graph, inputs in HBM
@@ -315,6 +320,11 @@ def main():
                             "(%.0f MB); map state carried across frames as in the loop" % (n, n * COLS * ROWS * 5 / 1e6)},
            "gpu_launches": int(g["launches"]), "clocks": g["clocks"]}
 
+    if args.quick:
+        ctx.close()
+        if rank == 0:
+            print(json.dumps(out), flush=True)
+        return
     # per-stage timing pass (eager device-driven form, same kernels)
     tp = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 2, barrier, timing=True)
     integ_b, ray_b, V = algorithmic_bytes(tp["stats"])

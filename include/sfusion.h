@@ -106,6 +106,11 @@ int sf_context_flags(sf_context *ctx, uint32_t *flags_out);
 /* Process-wide number of kernels this library has launched (a CUDA-graph
  * replay counts the kernel nodes it runs). */
 int sf_kernel_launches(uint64_t *out);
+/* Tracing of the persistent ICP kernel: when enabled, CTA 0 records SM
+ * clocks at six phase boundaries of each iteration (start, pixels
+ * accumulated, block total written, grid barrier passed, cross-block sum,
+ * solve) into 64 x 8 slots; out (may be NULL) receives them. */
+int sf_icp_profile(sf_context *ctx, int enable, uint64_t *out);
 /* Copies `bytes` between any two host/device pointers (unified addressing)
  * on the context stream and waits for it. */
 int sf_memcpy(sf_context *ctx, void *dst, const void *src, size_t bytes);

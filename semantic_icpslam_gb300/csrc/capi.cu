@@ -157,6 +157,17 @@ int sf_context_flags(sf_context *ctx, uint32_t *flags_out) {
   return SF_OK;
 }
 
+int sf_icp_profile(sf_context *ctx, int enable, uint64_t *out) {
+  if (!ctx) return SF_ERR_INVALID;
+  ctx->icp.profile = enable ? 1 : 0;
+  if (out) {
+    SF_CHECK(cudaMemcpyAsync(out, ctx->icp.prof, sizeof(uint64_t) * 64 * 8, cudaMemcpyDeviceToHost,
+                             ctx->stream));
+    SF_CHECK(cudaStreamSynchronize(ctx->stream));
+  }
+  return SF_OK;
+}
+
 int sf_kernel_launches(uint64_t *out) {
   if (!out) return SF_ERR_INVALID;
   *out = (uint64_t)launches_total();

@@ -21,6 +21,7 @@ namespace sf {
 namespace {
 
 constexpr int kThreads = 512;
+constexpr int kProfIters = 64;
 constexpr int kWarps = kThreads / 32;
 
 struct PoseF {
@@ -193,7 +194,15 @@ struct PersistentArgs {
   const double *last_pose;
   const int *run_flag;
   uint32_t *flags;
+  unsigned long long *prof;  // optional per-iteration phase clocks of CTA 0
 };
+
+// Phase clock of CTA 0 (SM cycles): 0 iteration start, 1 pixels
+// accumulated, 2 block total written, 3 grid barrier passed, 4 cross-block
+// sum done, 5 solve done.
+__device__ __forceinline__ void prof_mark(const PersistentArgs &a, int it, int k) {
+  if (a.prof && blockIdx.x == 0 && threadIdx.x == 0 && it < kProfIters) a.prof[it * 8 + k] = clock64();
+}
 
 __global__ void __launch_bounds__(kThreads) k_icp_persistent(PersistentArgs a) {
   __shared__ TrackCtl ctl;
@@ -208,10 +217,11 @@ __global__ void __launch_bounds__(kThreads) k_icp_persistent(PersistentArgs a) {
   const int nb = gridDim.x;
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const int gstride = nb * blockDim.x;
-  int buf = 0;
+  int buf = 0, it = 0;
   for (int l = a.levels - 1; l >= 0; --l) {
     const IcpLevelArgs &L = a.lv[l];
-    for (int j = 0; j < L.iters; ++j) {
+    for (int j = 0; j < L.iters; ++j, ++it) {
+      prof_mark(a, it, 0);
       if (threadIdx.x == 0) {
         m3 dummy;
         pose_to_float(ctl.next_pose, pose.Rc, dummy, pose.tc);
@@ -220,13 +230,18 @@ __global__ void __launch_bounds__(kThreads) k_icp_persistent(PersistentArgs a) {
       __syncthreads();
       float acc[29];
       icp_accumulate(L, pose, gtid, gstride, acc);
+      prof_mark(a, it, 1);
       block_reduce29(acc, wpart, bsum);
       double *part = a.partials + (size_t)buf * 29 * a.stride;
       if (threadIdx.x < 29) part[(size_t)threadIdx.x * a.stride + blockIdx.x] = bsum[threadIdx.x];
+      prof_mark(a, it, 2);
       grid_barrier(a.barrier, nb, a.flags);
+      prof_mark(a, it, 3);
       cross_block_sum(part, nb, a.stride, sums);
+      prof_mark(a, it, 4);
       if (threadIdx.x < 32) ctl_step_warp(ctl, sums, L.min_count, wsolve);
       __syncthreads();
+      prof_mark(a, it, 5);
       buf ^= 1;
       if (ctl.stop) break;
     }
@@ -275,6 +290,8 @@ int icp_workspace_init(IcpWorkspace &w) {
   if (cudaMalloc(&w.barrier, sizeof(unsigned) * 2) != cudaSuccess) return SF_ERR_CUDA;
   if (cudaMemset(w.barrier, 0, sizeof(unsigned) * 2) != cudaSuccess) return SF_ERR_CUDA;
   if (cudaMalloc(&w.ctl, sizeof(TrackCtl)) != cudaSuccess) return SF_ERR_CUDA;
+  if (cudaMalloc(&w.prof, sizeof(unsigned long long) * 8 * kProfIters) != cudaSuccess) return SF_ERR_CUDA;
+  if (cudaMemset(w.prof, 0, sizeof(unsigned long long) * 8 * kProfIters) != cudaSuccess) return SF_ERR_CUDA;
   return SF_OK;
 }
 
@@ -283,6 +300,7 @@ void icp_workspace_free(IcpWorkspace &w) {
   cudaFree(w.sums);
   cudaFree(w.barrier);
   cudaFree(w.ctl);
+  cudaFree(w.prof);
   w = IcpWorkspace();
 }
 
@@ -309,6 +327,7 @@ cudaError_t launch_icp_persistent(const IcpWorkspace &w, const IcpLevelArgs *lev
   a.last_pose = last_pose;
   a.run_flag = run_flag;
   a.flags = flags;
+  a.prof = w.profile ? w.prof : nullptr;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(w.max_blocks);
   cfg.blockDim = dim3(kThreads);

@@ -35,6 +35,8 @@ struct IcpWorkspace {
   TrackCtl *ctl = nullptr;     // device copy of the tracking state
   int max_blocks = 0;          // co-resident CTAs of the persistent kernel
   int threads = 0;
+  unsigned long long *prof = nullptr;  // [64][8] phase clocks of CTA 0
+  int profile = 0;                     // record phase clocks when set
 };
 
 int icp_workspace_init(IcpWorkspace &w);
