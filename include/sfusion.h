@@ -35,7 +35,8 @@ enum {
   SF_ERR_OVERFLOW = 3,  /* a fixed-capacity list overflowed (counted)      */
   SF_ERR_TIMEOUT = 4,   /* a bounded device wait gave up                   */
   SF_ERR_NO_DEVICE = 5, /* no CUDA device                                  */
-  SF_ERR_STATE = 6      /* call not valid in the object's current state    */
+  SF_ERR_STATE = 6,     /* call not valid in the object's current state    */
+  SF_ERR_TOO_LARGE = 7  /* input beyond a fixed buffer's stated maximum    */
 };
 
 /* ----------------------------------------------------------- POD layouts */
@@ -166,6 +167,30 @@ int sf_ICPStep(sf_context *ctx, sf_image next_vmap, sf_image last_vmap,
                sf_float3 tcurr, sf_mat3 Rlast, sf_mat3 RlastInv,
                sf_float3 tlast, sf_intrinsics K, float residual[2],
                double matrixA[36], double vectorB[6]);
+
+/* sf_ICPStep without any device allocation.  No counterpart in the
+ * reference: it is for callers that cannot allocate device memory, such as
+ * a host application whose allocator owns all device memory, or a
+ * real-time loop that must not pay for cudaMalloc's implicit device
+ * synchronisation.  Such callers cannot create an sf_context either, so
+ * this call takes only a stream (a cudaStream_t; NULL = the legacy default
+ * stream) and the same inputs and host outputs as sf_ICPStep.
+ * Its scratch (one FP64 partial per CTA for each of the 29 sums, plus the
+ * sums) is a fixed array of 464.25 KiB inside the library's device
+ * image.  Every GPU that loads the library holds it until the process
+ * exits.  Images of more than SF_ICP_STATIC_MAX_PIXELS pixels return
+ * SF_ERR_TOO_LARGE before any GPU work.
+ * The first call on each device looks up the array's device address.
+ * Make that first call before any stream capture.
+ * All calls share the one array, so calls that overlap on the GPU (other
+ * streams, other host threads) race and give wrong sums.  The call
+ * synchronises `stream` before it returns. */
+#define SF_ICP_STATIC_MAX_PIXELS 4194304 /* 2048 x 2048 */
+int sf_ICPStep_static(void *stream, sf_image next_vmap, sf_image last_vmap,
+                      sf_image next_nmap, sf_image last_nmap, sf_mat3 Rcurr,
+                      sf_float3 tcurr, sf_mat3 Rlast, sf_mat3 RlastInv,
+                      sf_float3 tlast, sf_intrinsics K, float residual[2],
+                      double matrixA[36], double vectorB[6]);
 
 /* Tracker::ComputeSE3(icpOnly = true, iter, thresh) (Tracking/Tracking.cc
  * :369-517) as ONE persistent cooperative launch: every level (coarse to

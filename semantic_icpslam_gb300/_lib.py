@@ -10,9 +10,11 @@ import threading
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libsfusion.so")
 
-SF_OK, SF_ERR_INVALID, SF_ERR_CUDA, SF_ERR_OVERFLOW, SF_ERR_TIMEOUT, SF_ERR_NO_DEVICE, SF_ERR_STATE = range(7)
+(SF_OK, SF_ERR_INVALID, SF_ERR_CUDA, SF_ERR_OVERFLOW, SF_ERR_TIMEOUT, SF_ERR_NO_DEVICE, SF_ERR_STATE,
+ SF_ERR_TOO_LARGE) = range(8)
 STATUS_NAMES = {0: "SF_OK", 1: "SF_ERR_INVALID", 2: "SF_ERR_CUDA", 3: "SF_ERR_OVERFLOW",
-                4: "SF_ERR_TIMEOUT", 5: "SF_ERR_NO_DEVICE", 6: "SF_ERR_STATE"}
+                4: "SF_ERR_TIMEOUT", 5: "SF_ERR_NO_DEVICE", 6: "SF_ERR_STATE", 7: "SF_ERR_TOO_LARGE"}
+ICP_STATIC_MAX_PIXELS = 4194304  # SF_ICP_STATIC_MAX_PIXELS
 
 FLAG_NAMES = {1 << 0: "DEDUP_FULL", 1 << 1: "PENDING_FULL", 1 << 2: "HEAP_EMPTY", 1 << 3: "EXCESS_FULL",
               1 << 4: "VISIBLE_FULL", 1 << 5: "RENDER_FULL", 1 << 6: "BARRIER_TIMEOUT",
@@ -108,6 +110,8 @@ SIGNATURES = {
                         Intrinsics, C.c_float, C.c_float],
     "sf_ICPStep": [vp, Image, Image, Image, Image, Mat3, Float3, Mat3, Mat3, Float3, Intrinsics, F32P,
                    F64P, F64P],
+    "sf_ICPStep_static": [vp, Image, Image, Image, Image, Mat3, Float3, Mat3, Mat3, Float3, Intrinsics,
+                          F32P, F64P, F64P],
     "sf_ComputeSE3": [vp, C.c_int, C.POINTER(Image), C.POINTER(Image), C.POINTER(Image), C.POINTER(Image),
                       Intrinsics, I32P, I32P, C.c_float, F64P, F64P, I32P, F32P],
     "sf_CheckBlockVisibility": [vp, vp, Mat3, Mat3, Float3, C.c_int, C.c_int] + [C.c_float] * 6 + [U32P],

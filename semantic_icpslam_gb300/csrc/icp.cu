@@ -13,6 +13,8 @@
 // CTA sums the partials in FP64 in the same fixed order and runs the same
 // 6x6 LDLT solve and SE(3) update, so all CTAs hold the same pose without a
 // second barrier.  Partials are double-buffered by iteration parity.
+#include <mutex>
+
 #include "sf_kernels.cuh"
 #include "sf_solve_warp.cuh"
 
@@ -343,3 +345,90 @@ cudaError_t launch_icp_persistent(const IcpWorkspace &w, const IcpLevelArgs *lev
 }
 
 }  // namespace sf
+
+// ------------------------------------------------- ICP step, no allocation
+// sf_ICPStep for callers that cannot allocate device memory (a host whose
+// own allocator owns the device, or a loop that must not pay for
+// cudaMalloc's implicit device synchronisation).  Its scratch is a fixed
+// array in this library's device image instead of a context workspace:
+// one CTA per kStaticPixPerCta pixels, each writing one FP64 partial per
+// sum, then the 29 sums.  Every partial a call reads is written by the
+// same call first, so nothing needs clearing between calls.  Calls that
+// overlap on the GPU share the array and race.
+namespace sf {
+namespace {
+
+constexpr int kStaticPixPerCta = kThreads * 4;
+constexpr int kStaticMaxCtas = SF_ICP_STATIC_MAX_PIXELS / kStaticPixPerCta;
+static_assert(kStaticMaxCtas * kStaticPixPerCta == SF_ICP_STATIC_MAX_PIXELS, "whole CTAs");
+constexpr int kStaticSumsOffset = 29 * kStaticMaxCtas;
+
+// [29][kStaticMaxCtas] partials, then 29 sums (padded): 464.25 KiB.
+static __device__ __align__(256) double g_icp_static[kStaticSumsOffset + 32];
+
+constexpr int kStaticMaxDevices = 64;
+std::mutex g_icp_static_mu;
+double *g_icp_static_addr[kStaticMaxDevices] = {};
+
+// Device address of g_icp_static on the current device, looked up on the
+// first call per device.  The name g_icp_static in host code is only a
+// host-side stand-in, never a device pointer.
+int icp_static_scratch(double **out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return SF_ERR_NO_DEVICE;
+  if (dev < 0 || dev >= kStaticMaxDevices) return SF_ERR_INVALID;
+  std::lock_guard<std::mutex> lock(g_icp_static_mu);
+  if (!g_icp_static_addr[dev]) {
+    double *p = nullptr;
+    if (cudaGetSymbolAddress((void **)&p, g_icp_static) != cudaSuccess || !p) return SF_ERR_CUDA;
+    g_icp_static_addr[dev] = p;
+  }
+  *out = g_icp_static_addr[dev];
+  return SF_OK;
+}
+
+bool static_img_ok(const sf_image &im, const sf_image &like) {
+  return im.data && im.cols > 0 && im.rows > 0 && im.step >= (size_t)im.cols * 16 &&
+         im.cols == like.cols && im.rows == like.rows;
+}
+
+}  // namespace
+}  // namespace sf
+
+extern "C" int sf_ICPStep_static(void *stream, sf_image next_vmap, sf_image last_vmap,
+                                 sf_image next_nmap, sf_image last_nmap, sf_mat3 Rcurr,
+                                 sf_float3 tcurr, sf_mat3 Rlast, sf_mat3 RlastInv,
+                                 sf_float3 tlast, sf_intrinsics K, float residual[2],
+                                 double matrixA[36], double vectorB[6]) {
+  using namespace sf;
+  if (!residual || !matrixA || !vectorB) return SF_ERR_INVALID;
+  const sf_image *ims[4] = {&next_vmap, &last_vmap, &next_nmap, &last_nmap};
+  for (auto im : ims)
+    if (!static_img_ok(*im, next_vmap)) return SF_ERR_INVALID;
+  const long long pixels = (long long)next_vmap.cols * next_vmap.rows;
+  if (pixels > SF_ICP_STATIC_MAX_PIXELS) return SF_ERR_TOO_LARGE;
+  double *scratch = nullptr;
+  int st = icp_static_scratch(&scratch);
+  if (st != SF_OK) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  IcpLevelArgs L;
+  L.vc = next_vmap; L.nc = next_nmap; L.vl = last_vmap; L.nl = last_nmap;
+  L.fx = K.fx; L.fy = K.fy; L.cx = K.cx; L.cy = K.cy;
+  L.iters = 1; L.min_count = 0;
+  PoseF p;
+  p.Rc = to_m3(Rcurr); p.tc = to_f3(tcurr);
+  p.Rl = to_m3(Rlast); p.RlI = to_m3(RlastInv); p.tl = to_f3(tlast);
+  const int nb = (int)((pixels + kStaticPixPerCta - 1) / kStaticPixPerCta);
+  double *sums_dev = scratch + kStaticSumsOffset;
+  k_icp_partials<<<nb, kThreads, 0, s>>>(L, p, scratch, kStaticMaxCtas); note_launch();
+  k_icp_reduce<<<1, kThreads, 0, s>>>(scratch, nb, kStaticMaxCtas, sums_dev); note_launch();
+  if (cudaGetLastError() != cudaSuccess) return SF_ERR_CUDA;
+  double sums[29];
+  if (cudaMemcpyAsync(sums, sums_dev, sizeof(sums), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return SF_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return SF_ERR_CUDA;
+  create_matrix(sums, matrixA, vectorB);
+  residual[0] = (float)sums[27];
+  residual[1] = (float)sums[28];
+  return SF_OK;
+}
