@@ -110,7 +110,9 @@ int sf_kernel_launches(uint64_t *out);
 /* Tracing of the persistent ICP kernel: when enabled, CTA 0 records SM
  * clocks at six phase boundaries of each iteration (start, pixels
  * accumulated, block total written, grid barrier passed, cross-block sum,
- * solve) into 64 x 8 slots; out (may be NULL) receives them. */
+ * solve) into slots 0-5 of 64 x 16 slots, the global timer (ns) at the
+ * iteration start into slot 6, and clocks inside the solve into slots
+ * 8-13; out (may be NULL, else 64 * 16 values) receives them. */
 int sf_icp_profile(sf_context *ctx, int enable, uint64_t *out);
 /* Copies `bytes` between any two host/device pointers (unified addressing)
  * on the context stream and waits for it. */

@@ -161,7 +161,7 @@ int sf_icp_profile(sf_context *ctx, int enable, uint64_t *out) {
   if (!ctx) return SF_ERR_INVALID;
   ctx->icp.profile = enable ? 1 : 0;
   if (out) {
-    SF_CHECK(cudaMemcpyAsync(out, ctx->icp.prof, sizeof(uint64_t) * 64 * 8, cudaMemcpyDeviceToHost,
+    SF_CHECK(cudaMemcpyAsync(out, ctx->icp.prof, sizeof(uint64_t) * 64 * 16, cudaMemcpyDeviceToHost,
                              ctx->stream));
     SF_CHECK(cudaStreamSynchronize(ctx->stream));
   }

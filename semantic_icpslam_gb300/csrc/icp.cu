@@ -16,15 +16,26 @@
 #include <mutex>
 
 #include "sf_kernels.cuh"
-#include "sf_solve_warp.cuh"
+
+// Tracing slots of the solve phases (set per iteration in CTA 0 when
+// tracing is on, else null); read by SF_SOLVE_MARK inside the solve.
+__shared__ unsigned long long *s_solve_marks;
+#define SF_SOLVE_MARK(k)                                           \
+  do {                                                             \
+    if ((threadIdx.x & 31) == 0 && s_solve_marks) s_solve_marks[k] = clock64(); \
+  } while (0)
+#include "sf_icp_solve.cuh"
 
 namespace sf {
 
 namespace {
 
-constexpr int kThreads = 512;
+constexpr int kThreads = 512;    // plain-form kernels
+constexpr int kPThreads = 1024;  // persistent kernel: one CTA per SM
 constexpr int kProfIters = 64;
+constexpr int kProfSlots = 16;  // per iteration: 0-5 phases, 6 globaltimer, 8-13 solve steps
 constexpr int kWarps = kThreads / 32;
+constexpr int kPWarps = kPThreads / 32;
 
 struct PoseF {
   m3 Rc, Rl, RlI;
@@ -108,69 +119,114 @@ __device__ __forceinline__ void icp_accumulate(const IcpLevelArgs &L, const Pose
   }
 }
 
-// Compensated warp tree: Knuth's TwoSum at every level, errors carried in a
-// second float; lane 0 ends with (sum, err).
-__device__ __forceinline__ void warp_reduce_comp(float &s, float &e) {
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    float s2 = __shfl_down_sync(0xffffffffu, s, off);
-    float e2 = __shfl_down_sync(0xffffffffu, e, off);
-    float t = s + s2;
-    float bb = t - s;
-    float err = (s - (t - bb)) + (s2 - bb);
-    s = t;
-    e = e + e2 + err;
-  }
+// Float-float (hi + lo) accumulation: Knuth's TwoSum on the leading parts,
+// the rounding errors and trailing parts carried in lo.  About 2^-47
+// relative per addition, on the FP32 pipe.
+struct ff {
+  float s, e;
+};
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+  const float t = a.s + b.s;
+  const float bb = t - a.s;
+  const float err = (a.s - (t - bb)) + (b.s - bb);
+  return ff{t, a.e + b.e + err};
+}
+__device__ __forceinline__ ff ff_shfl_xor(ff a, int off) {
+  return ff{__shfl_xor_sync(0xffffffffu, a.s, off), __shfl_xor_sync(0xffffffffu, a.e, off)};
+}
+// (hi, lo) with |lo| <= ulp(hi) / 2.
+__device__ __forceinline__ float2 ff_norm(ff a) {
+  const float hi = a.s + a.e;
+  return make_float2(hi, a.e - (hi - a.s));
 }
 
-// Block total of the 29 terms as doubles in smem out[29].
-__device__ __forceinline__ void block_reduce29(float acc[29], float2 (*wpart)[29], double *out) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+// Transposing butterfly over the 29 accumulators of a warp: at each level
+// a lane keeps half of its components, adds the partner's copy of them and
+// hands over the other half, so lane l ends with the compensated warp total
+// of component l (components 29..31 are zero) after 31 shuffle pairs
+// instead of 29 separate trees.
+__device__ __forceinline__ ff warp_transpose_reduce29(const float acc[29]) {
+  const int lane = threadIdx.x & 31;
+  ff v16[16];
+  {
+    const bool hi = lane & 16;
 #pragma unroll
-  for (int k = 0; k < 29; ++k) {
-    float s = acc[k], e = 0.f;
-    warp_reduce_comp(s, e);
-    if (lane == 0) wpart[warp][k] = make_float2(s, e);
-  }
-  __syncthreads();
-  if (threadIdx.x < 29) {
-    double t = 0.0;
-    for (int w = 0; w < kWarps; ++w) t += (double)wpart[w][threadIdx.x].x + (double)wpart[w][threadIdx.x].y;
-    out[threadIdx.x] = t;
-  }
-  __syncthreads();
-}
-
-// Bounded sense-reversing grid barrier.  All CTAs are co-resident (the
-// kernel is launched cooperatively); the spin still gives up after a fixed
-// number of polls and records SF_FLAG_BARRIER_TIMEOUT.
-__device__ __forceinline__ void grid_barrier(unsigned *bar, unsigned nblocks, uint32_t *flags) {
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    volatile unsigned *gen = bar + 1;
-    unsigned g = *gen;
-    __threadfence();
-    unsigned arrived = atomicAdd(bar, 1u);
-    if (arrived == nblocks - 1) {
-      atomicExch(bar, 0u);
-      __threadfence();
-      atomicAdd(bar + 1, 1u);
-    } else {
-      unsigned polls = 0;
-      while (*gen == g) {
-        if (++polls > (1u << 22)) {
-          atomicOr(flags, SF_FLAG_BARRIER_TIMEOUT);
-          break;
-        }
-        __nanosleep(64);
-      }
+    for (int m = 0; m < 16; ++m) {
+      const float lo_c = acc[m];
+      const float hi_c = (m + 16 < 29) ? acc[m + 16] : 0.f;
+      const float send = hi ? lo_c : hi_c;
+      const float keep = hi ? hi_c : lo_c;
+      const float recv = __shfl_xor_sync(0xffffffffu, send, 16);
+      v16[m] = ff_add(ff{keep, 0.f}, ff{recv, 0.f});
     }
-    __threadfence();
+  }
+  ff v8[8];
+  {
+    const bool hi = lane & 8;
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      const ff send = hi ? v16[m] : v16[m + 8];
+      const ff keep = hi ? v16[m + 8] : v16[m];
+      v8[m] = ff_add(keep, ff_shfl_xor(send, 8));
+    }
+  }
+  ff v4[4];
+  {
+    const bool hi = lane & 4;
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const ff send = hi ? v8[m] : v8[m + 4];
+      const ff keep = hi ? v8[m + 4] : v8[m];
+      v4[m] = ff_add(keep, ff_shfl_xor(send, 4));
+    }
+  }
+  ff v2[2];
+  {
+    const bool hi = lane & 2;
+#pragma unroll
+    for (int m = 0; m < 2; ++m) {
+      const ff send = hi ? v4[m] : v4[m + 2];
+      const ff keep = hi ? v4[m + 2] : v4[m];
+      v2[m] = ff_add(keep, ff_shfl_xor(send, 2));
+    }
+  }
+  const bool hi = lane & 1;
+  const ff send = hi ? v2[0] : v2[1];
+  const ff keep = hi ? v2[1] : v2[0];
+  return ff_add(keep, ff_shfl_xor(send, 1));
+}
+
+// Block total of the 29 terms as normalised float-float pairs in smem
+// out[29]: warp butterflies, then the NW warp totals of each component are
+// added with a shuffle tree (16 warps: two components per warp, lanes
+// 0..15 and 16..31; 32 warps: warp c takes component c).  wpart rows are
+// padded to 33 so the column reads hit distinct banks.
+template <int NW>
+__device__ __forceinline__ void block_reduce29(const float acc[29], ff (*wpart)[33], float2 *out) {
+  static_assert(NW == 16 || NW == 32, "16 or 32 warps");
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  wpart[warp][lane] = warp_transpose_reduce29(acc);
+  __syncthreads();
+  if (NW == 16) {
+    if (warp < 15) {
+      const int c = 2 * warp + (lane >> 4);
+      ff v = (c < 29) ? wpart[lane & 15][c] : ff{0.f, 0.f};
+#pragma unroll
+      for (int off = 8; off > 0; off >>= 1) v = ff_add(v, ff_shfl_xor(v, off));
+      if ((lane & 15) == 0 && c < 29) out[c] = ff_norm(v);
+    }
+  } else {
+    if (warp < 29) {
+      ff v = wpart[lane][warp];
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) v = ff_add(v, ff_shfl_xor(v, off));
+      if (lane == 0) out[warp] = ff_norm(v);
+    }
   }
   __syncthreads();
 }
 
-// Sum of partials[29][nb] per component in FP64, fixed order: warp w sums
+// Sum of FP64 partials[29][nb] per component, fixed order: warp w sums
 // component w; lanes stride over CTAs, then a shuffle tree.
 __device__ __forceinline__ void cross_block_sum(const double *part, int nb, int stride,
                                                 double *sums) {
@@ -185,13 +241,34 @@ __device__ __forceinline__ void cross_block_sum(const double *part, int nb, int 
   __syncthreads();
 }
 
+// The same over float-float partials (float2 [29][stride]), accumulated on
+// the FP32 pipe (an FP64 sum would take ~64 cycles per add and warp on
+// this part).  Fixed order.
+template <int NW>
+__device__ __forceinline__ void cross_block_sum_ff(const float2 *part, int nb, int stride,
+                                                   double *sums) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int c = warp; c < 29; c += NW) {
+    ff t{0.f, 0.f};
+    for (int b = lane; b < nb; b += 32) {
+      const float2 p = __ldcg(part + (size_t)c * stride + b);
+      t = ff_add(t, ff{p.x, p.y});
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) t = ff_add(t, ff_shfl_xor(t, off));
+    if (lane == 0) sums[c] = (double)t.s + (double)t.e;
+  }
+  __syncthreads();
+}
+
 struct PersistentArgs {
   IcpLevelArgs lv[kMaxLevels];
   int levels;
   float thresh;
-  double *partials;  // [2][29][max_blocks]
+  float2 *partials;  // [2][29][max_blocks] float-float CTA totals
   int stride;        // max_blocks
-  unsigned *barrier;
+  unsigned *barrier; // [2] arrivals, generation
+  double *pub;       // [29] sums published by the last CTA to arrive
   TrackCtl *ctl;
   const double *last_pose;
   const int *run_flag;
@@ -200,21 +277,84 @@ struct PersistentArgs {
 };
 
 // Phase clock of CTA 0 (SM cycles): 0 iteration start, 1 pixels
-// accumulated, 2 block total written, 3 grid barrier passed, 4 cross-block
-// sum done, 5 solve done.
+// accumulated, 2 block total written, 3 arrived at the barrier, 4 the 29
+// sums in hand, 5 solve done.
 __device__ __forceinline__ void prof_mark(const PersistentArgs &a, int it, int k) {
-  if (a.prof && blockIdx.x == 0 && threadIdx.x == 0 && it < kProfIters) a.prof[it * 8 + k] = clock64();
+  if (a.prof && blockIdx.x == 0 && threadIdx.x == 0 && it < kProfIters) {
+    a.prof[it * kProfSlots + k] = clock64();
+    if (k == 0) {
+      unsigned long long ns;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(ns));
+      a.prof[it * kProfSlots + 6] = ns;
+    }
+  }
 }
 
-__global__ void __launch_bounds__(kThreads) k_icp_persistent(PersistentArgs a) {
+// End of an iteration's accumulation, after every CTA has written its 29
+// partials: a bounded barrier in which the last CTA to arrive sums all
+// partials (fixed order) and publishes the 29 sums before it opens the
+// barrier; the others wait and read them.  Only one CTA reads the partials,
+// and every CTA ends with the same 29 doubles in sums.  A wait that runs
+// past 2^22 polls records SF_FLAG_BARRIER_TIMEOUT and goes on.
+__device__ __forceinline__ void reduce_at_barrier(const PersistentArgs &a, const float2 *part, int nb,
+                                                  double *sums, int it) {
+  __shared__ unsigned s_gen;
+  __shared__ int s_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned *gen = a.barrier + 1;
+    const unsigned g = *gen;
+    __threadfence();
+    const unsigned arrived = atomicAdd(a.barrier, 1u);
+    s_gen = g;
+    s_last = (arrived == (unsigned)nb - 1u);
+    __threadfence();
+  }
+  __syncthreads();
+  prof_mark(a, it, 3);
+  if (s_last) {
+    cross_block_sum_ff<kPWarps>(part, nb, a.stride, sums);
+    if (threadIdx.x < 29) {
+      a.pub[threadIdx.x] = sums[threadIdx.x];
+      __threadfence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      atomicExch(a.barrier, 0u);
+      __threadfence();
+      atomicAdd(a.barrier + 1, 1u);
+    }
+  } else {
+    if (threadIdx.x == 0) {
+      volatile unsigned *gen = a.barrier + 1;
+      unsigned polls = 0;
+      while (*gen == s_gen) {
+        if (++polls > (1u << 22)) {
+          atomicOr(a.flags, SF_FLAG_BARRIER_TIMEOUT);
+          break;
+        }
+        __nanosleep(32);
+      }
+      __threadfence();
+    }
+    __syncthreads();
+    if (threadIdx.x < 29) sums[threadIdx.x] = __ldcg(a.pub + threadIdx.x);
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kPThreads, 1) k_icp_persistent(PersistentArgs a) {
   __shared__ TrackCtl ctl;
-  __shared__ WarpSolveScratch wsolve;
+  __shared__ IcpSolveSmem ssolve;
   __shared__ PoseF pose;
-  __shared__ double bsum[29];
+  __shared__ float2 bsum[29];
   __shared__ double sums[29];
-  __shared__ float2 wpart[kWarps][29];
+  __shared__ ff wpart[kPWarps][33];
   if (a.run_flag && *a.run_flag == 0) return;  // uniform across the grid
-  if (threadIdx.x == 0) ctl_begin(ctl, a.last_pose);
+  if (threadIdx.x == 0) {
+    ctl_begin(ctl, a.last_pose);
+    s_solve_marks = nullptr;
+  }
   __syncthreads();
   const int nb = gridDim.x;
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -233,15 +373,19 @@ __global__ void __launch_bounds__(kThreads) k_icp_persistent(PersistentArgs a) {
       float acc[29];
       icp_accumulate(L, pose, gtid, gstride, acc);
       prof_mark(a, it, 1);
-      block_reduce29(acc, wpart, bsum);
-      double *part = a.partials + (size_t)buf * 29 * a.stride;
-      if (threadIdx.x < 29) part[(size_t)threadIdx.x * a.stride + blockIdx.x] = bsum[threadIdx.x];
+      block_reduce29<kPWarps>(acc, wpart, bsum);
+      float2 *part = a.partials + (size_t)buf * 29 * a.stride;
+      if (threadIdx.x < 29) {
+        part[(size_t)threadIdx.x * a.stride + blockIdx.x] = bsum[threadIdx.x];
+        __threadfence();
+      }
       prof_mark(a, it, 2);
-      grid_barrier(a.barrier, nb, a.flags);
-      prof_mark(a, it, 3);
-      cross_block_sum(part, nb, a.stride, sums);
+      reduce_at_barrier(a, part, nb, sums, it);
       prof_mark(a, it, 4);
-      if (threadIdx.x < 32) ctl_step_warp(ctl, sums, L.min_count, wsolve);
+      if (threadIdx.x == 0)
+        s_solve_marks = (a.prof && blockIdx.x == 0 && it < kProfIters) ? a.prof + it * kProfSlots + 8 : nullptr;
+      __syncwarp();
+      if (threadIdx.x < 32) ctl_step_fast(ctl, sums, L.min_count, ssolve);
       __syncthreads();
       prof_mark(a, it, 5);
       buf ^= 1;
@@ -249,21 +393,23 @@ __global__ void __launch_bounds__(kThreads) k_icp_persistent(PersistentArgs a) {
     }
     if (ctl.stop) break;
   }
-  if (threadIdx.x == 0) {
-    ctl_finish(ctl, a.thresh);
-    if (blockIdx.x == 0) *a.ctl = ctl;
-  }
+  if (threadIdx.x == 0) s_solve_marks = nullptr;
+  __syncwarp();
+  if (threadIdx.x < 32) ctl_finish_fast(ctl, a.thresh, ssolve);
+  __syncthreads();
+  if (threadIdx.x == 0 && blockIdx.x == 0) *a.ctl = ctl;
 }
 
 // Plain form, launch 1: per-CTA FP64 partials.
 __global__ void __launch_bounds__(kThreads) k_icp_partials(IcpLevelArgs L, PoseF p, double *part,
                                                            int stride) {
-  __shared__ double bsum[29];
-  __shared__ float2 wpart[kWarps][29];
+  __shared__ float2 bsum[29];
+  __shared__ ff wpart[kWarps][33];
   float acc[29];
   icp_accumulate(L, p, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, acc);
-  block_reduce29(acc, wpart, bsum);
-  if (threadIdx.x < 29) part[(size_t)threadIdx.x * stride + blockIdx.x] = bsum[threadIdx.x];
+  block_reduce29<kWarps>(acc, wpart, bsum);
+  if (threadIdx.x < 29)
+    part[(size_t)threadIdx.x * stride + blockIdx.x] = (double)bsum[threadIdx.x].x + (double)bsum[threadIdx.x].y;
 }
 
 // Plain form, launch 2: FP64 sum of the partials (Reduce<float,29>).
@@ -281,19 +427,19 @@ int icp_workspace_init(IcpWorkspace &w) {
   if (cudaGetDevice(&dev) != cudaSuccess) return SF_ERR_CUDA;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_icp_persistent, kThreads, 0) !=
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_icp_persistent, kPThreads, 0) !=
       cudaSuccess)
     return SF_ERR_CUDA;
   if (per_sm < 1 || !coop) return SF_ERR_CUDA;
   w.max_blocks = sms * per_sm;
-  w.threads = kThreads;
+  w.threads = kPThreads;
   if (cudaMalloc(&w.partials, sizeof(double) * 2 * 29 * (size_t)w.max_blocks) != cudaSuccess) return SF_ERR_CUDA;
   if (cudaMalloc(&w.sums, sizeof(double) * 29) != cudaSuccess) return SF_ERR_CUDA;
   if (cudaMalloc(&w.barrier, sizeof(unsigned) * 2) != cudaSuccess) return SF_ERR_CUDA;
   if (cudaMemset(w.barrier, 0, sizeof(unsigned) * 2) != cudaSuccess) return SF_ERR_CUDA;
   if (cudaMalloc(&w.ctl, sizeof(TrackCtl)) != cudaSuccess) return SF_ERR_CUDA;
-  if (cudaMalloc(&w.prof, sizeof(unsigned long long) * 8 * kProfIters) != cudaSuccess) return SF_ERR_CUDA;
-  if (cudaMemset(w.prof, 0, sizeof(unsigned long long) * 8 * kProfIters) != cudaSuccess) return SF_ERR_CUDA;
+  if (cudaMalloc(&w.prof, sizeof(unsigned long long) * kProfSlots * kProfIters) != cudaSuccess) return SF_ERR_CUDA;
+  if (cudaMemset(w.prof, 0, sizeof(unsigned long long) * kProfSlots * kProfIters) != cudaSuccess) return SF_ERR_CUDA;
   return SF_OK;
 }
 
@@ -322,9 +468,11 @@ cudaError_t launch_icp_persistent(const IcpWorkspace &w, const IcpLevelArgs *lev
   for (int l = 0; l < nlevels && l < kMaxLevels; ++l) a.lv[l] = levels[l];
   a.levels = nlevels;
   a.thresh = thresh;
-  a.partials = w.partials;
+  static_assert(sizeof(float2) == sizeof(double), "partials: 8-byte slots in either form");
+  a.partials = reinterpret_cast<float2 *>(w.partials);
   a.stride = w.max_blocks;
   a.barrier = w.barrier;
+  a.pub = w.sums;
   a.ctl = w.ctl;
   a.last_pose = last_pose;
   a.run_flag = run_flag;
@@ -332,7 +480,7 @@ cudaError_t launch_icp_persistent(const IcpWorkspace &w, const IcpLevelArgs *lev
   a.prof = w.profile ? w.prof : nullptr;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(w.max_blocks);
-  cfg.blockDim = dim3(kThreads);
+  cfg.blockDim = dim3(kPThreads);
   cfg.dynamicSmemBytes = 0;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];

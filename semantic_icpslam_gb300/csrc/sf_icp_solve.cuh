@@ -1,0 +1,350 @@
+// Per-iteration control, 6x6 solve and SE(3) update of the persistent ICP
+// kernel, run by one warp.
+//
+// GB300's FP64 path is narrow: a warp has one FP64 instruction in flight
+// at a time, about 64 cycles each whether the next one depends on it or
+// not (conversions and compares to/from double included), and the SM
+// retires one FP64 warp instruction per ~19 cycles.  Lanes are free, FP64
+// instructions are not, so this form keeps the mathematics of
+// sf::ctl_step (sf_solve.h), which restates Tracker::ComputeSE3
+// (Tracking/Tracking.cc:449-499), with as few FP64 instructions per warp as
+// it can:
+//  - A x = b by Gauss-Jordan elimination of the augmented 6x7 matrix held
+//    in lane registers (element e = 7*i + j: lane e, then lane e-32), two
+//    FP64 instructions per register and step.  The pivot order is LDLT's
+//    symmetric pivoting (largest remaining |diagonal|, first on ties,
+//    compared on the integer bits; every uneliminated row carries the same
+//    scale, so the comparison is LDLT's), a zero pivot zeroes its
+//    component as in the LDLT solve, and instead of dividing, each step
+//    rescales the updated rows by an exact power of two through exponent
+//    arithmetic.  The six divisions x_i = b_i / a_ii run side by side.
+//  - exp(x) in Rodrigues form, R = I + c_a W + c_1 W^2 and
+//    t = u + c_1 (w x u) + c_2 (w x (w x u)), with c_a = sin(t)/t,
+//    c_1 = (1 - cos t)/t^2, c_2 = (t - sin t)/t^3: the same rotation and
+//    left Jacobian as Sophus's quaternion form.  For t < 0.1 rad the
+//    coefficients are their Taylor series in x = t^2: the leading two
+//    terms in FP64, the rest (below 1e-4 of the total, truncated below
+//    1e-20) in FP32, which keeps each coefficient within 1e-13 absolute.
+//    Larger angles take the trigonometric form.
+//  - pose products as FMA chains, one matrix element per lane.
+// Results agree with the host ctl_step to rounding (about 1e-15 relative
+// on well-conditioned systems); they are not bit-identical.
+#ifndef SF_ICP_SOLVE_CUH_
+#define SF_ICP_SOLVE_CUH_
+
+#include "sf_solve.h"
+
+// Optional phase-clock hook (a no-op unless defined before inclusion).
+#ifndef SF_SOLVE_MARK
+#define SF_SOLVE_MARK(k)
+#endif
+
+namespace sf {
+
+struct IcpSolveSmem {
+  double R[9];
+  double delta[12];  // updated delta (top 3 rows)
+  double dInv[12];   // its inverse (top 3 rows)
+};
+
+// Element e (0..41) of the augmented matrix held as (r0: e = lane,
+// r1: e = 32 + lane).  Every lane must call it.
+__device__ __forceinline__ double aug_get(double r0, double r1, int e) {
+  const double v0 = __shfl_sync(0xffffffffu, r0, e & 31);
+  const double v1 = __shfl_sync(0xffffffffu, r1, e & 31);
+  return e < 32 ? v0 : v1;
+}
+
+// v * 2^sh by exponent arithmetic (no FP64 instruction).  Zero and
+// subnormal inputs pass unchanged; results past the exponent range flush
+// to signed zero or saturate to infinity.
+__device__ __forceinline__ double scale_pow2(double v, int sh) {
+  const long long b = __double_as_longlong(v);
+  const int e = (int)((b >> 52) & 0x7ff);
+  const long long sign = b & (long long)0x8000000000000000ull;
+  const int ne = e + sh;
+  long long r = b + ((long long)sh << 52);
+  r = ne <= 0 ? sign : r;
+  r = ne >= 0x7ff ? (sign | 0x7ff0000000000000ll) : r;
+  r = (e == 0 || e == 0x7ff) ? b : r;
+  return __longlong_as_double(r);
+}
+
+// Solves A x = b for the 27 upper-triangle sums of CreateMatrix<6,7>
+// (Tracking/Reduction.cu:6-16); every lane returns x[0..5].
+__device__ __forceinline__ void warp_solve6(const double *sums, double x[6]) {
+  const int lane = threadIdx.x & 31;
+  // augmented [A | b]: row i, column j (j == 6 is b); A symmetric from the
+  // upper triangle, row i of the sums starts at 7i - i(i-1)/2
+  auto sum_at = [&](int e) {
+    const int i = e / 7, j = e - 7 * (e / 7);
+    const int r = i < j ? i : j, q = i < j ? j : i;
+    return j == 6 ? sums[7 * i - i * (i - 1) / 2 + (6 - i)] : sums[7 * r - r * (r - 1) / 2 + (q - r)];
+  };
+  double r0 = sum_at(lane);
+  double r1 = lane < 10 ? sum_at(32 + lane) : 0.0;
+  const int i0 = lane / 7, j0 = lane - 7 * (lane / 7);
+  const int e1 = lane < 10 ? 32 + lane : 41;
+  const int i1 = e1 / 7, j1 = e1 - 7 * (e1 / 7);
+  unsigned done = 0, zero = 0;
+#pragma unroll 1
+  for (int step = 0; step < 6; ++step) {
+    double d[6];
+    d[0] = __shfl_sync(0xffffffffu, r0, 0);
+    d[1] = __shfl_sync(0xffffffffu, r0, 8);
+    d[2] = __shfl_sync(0xffffffffu, r0, 16);
+    d[3] = __shfl_sync(0xffffffffu, r0, 24);
+    d[4] = __shfl_sync(0xffffffffu, r1, 0);
+    d[5] = __shfl_sync(0xffffffffu, r1, 8);
+    // largest |diagonal| among the uneliminated rows, first on ties; the
+    // magnitude bits of a double order like the values
+    int k = -1;
+    unsigned long long best = 0;
+    double akk = 0.0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      const unsigned long long key = (unsigned long long)__double_as_longlong(d[i]) & 0x7fffffffffffffffull;
+      const bool take = !((done >> i) & 1u) && (k < 0 || key > best);
+      best = take ? key : best;
+      k = take ? i : k;
+      akk = take ? d[i] : akk;
+    }
+    if (best == 0) {  // every remaining pivot is zero: those components are 0
+      zero = 0x3fu & ~done;
+      break;
+    }
+    done |= 1u << k;
+    const int ek = (int)((__double_as_longlong(akk) >> 52) & 0x7ff);
+    const int sh = ek == 0 ? 0 : 1023 - ek;  // |akk| * 2^sh in [1, 2)
+    const double aik0 = aug_get(r0, r1, i0 * 7 + k);
+    const double akj0 = aug_get(r0, r1, k * 7 + j0);
+    const double aik1 = aug_get(r0, r1, i1 * 7 + k);
+    const double akj1 = aug_get(r0, r1, k * 7 + j1);
+    const double u0 = fma(akk, r0, -(aik0 * akj0));
+    const double u1 = fma(akk, r1, -(aik1 * akj1));
+    r0 = (i0 == k) ? r0 : ((j0 == k) ? 0.0 : scale_pow2(u0, sh));
+    r1 = (lane >= 10 || i1 == k) ? r1 : ((j1 == k) ? 0.0 : scale_pow2(u1, sh));
+  }
+  // x_i = b_i / a_ii: lane i gathers row i's b (element 7i+6) and pivot
+  // (element 8i); the six divisions run side by side
+  const int row = lane < 6 ? lane : 0;
+  const double bi = aug_get(r0, r1, row * 7 + 6);
+  const double ai = aug_get(r0, r1, row * 8);
+  const double xi = ((zero >> row) & 1u) ? 0.0 : bi / ai;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) x[i] = __shfl_sync(0xffffffffu, xi, i);
+}
+
+// One iteration given the 29 sums in shared memory; all 32 lanes of the
+// calling warp.  Same contract and state transitions as sf::ctl_step.
+__device__ bool ctl_step_fast(TrackCtl &c, const double *sums, int min_count, IcpSolveSmem &s) {
+  const int lane = threadIdx.x & 31;
+  SF_SOLVE_MARK(0);
+  int code = 0, copy_cand = 0;
+  if (lane == 0) {
+    c.iters_run++;
+    float residual0 = (float)sums[27], residual1 = (float)sums[28];
+    c.icpError = sqrtf(residual0) / residual1;
+    c.icpCount = (int)residual1;
+    if (isnan(c.icpError) || c.icpCount < min_count) {
+      c.stop = 1;
+      code = 1;
+    } else {
+      const float rgbError = 0.f, wgt = 1e-4f;
+      float currError = rgbError * wgt + c.icpError;
+      if (c.lastError < currError) {
+        c.breakCount++;
+        copy_cand = (c.breakCount == 1);
+        c.candidateICP = c.icpError;  // outside the inner if (Tracking.cc:463-465)
+      } else {
+        c.breakCount = 0;
+      }
+      if (c.breakCount > 2) {
+        c.icpError = c.candidateICP;
+        c.stop = 2;
+        code = 2;
+      } else {
+        c.lastError = currError;
+      }
+    }
+  }
+  code = __shfl_sync(0xffffffffu, code, 0);
+  copy_cand = __shfl_sync(0xffffffffu, copy_cand, 0);
+  __syncwarp();
+  if (copy_cand && lane < 16) c.candidate[lane] = c.next_pose[lane];
+  __syncwarp();
+  if (code == 1) {
+    if (lane < 16) c.next_pose[lane] = c.last_pose[lane];
+    __syncwarp();
+    return false;
+  }
+  if (code == 2) {
+    if (lane < 16) c.next_pose[lane] = c.candidate[lane];
+    __syncwarp();
+    return false;
+  }
+
+  SF_SOLVE_MARK(1);
+  double x[6];
+  warp_solve6(sums, x);
+  SF_SOLVE_MARK(2);
+  const double u0 = x[0], u1 = x[1], u2 = x[2];
+  const double w0 = x[3], w1 = x[4], w2 = x[5];
+  const double th2 = fma(w2, w2, fma(w1, w1, w0 * w0));
+  double ca, c1, c2;
+  if (th2 < 0.01) {
+    // sin t / t = 1 - x/6 + x^2/120 - ..., (1 - cos t)/t^2 = 1/2 - x/24 + ...,
+    // (t - sin t)/t^3 = 1/6 - x/120 + ..., x = t^2
+    const float xf = (float)th2;
+    const float ca_tail = xf * (1.f / 120 + xf * (-1.f / 5040 + xf * (1.f / 362880 + xf * (-1.f / 39916800))));
+    const float c1_tail = xf * (1.f / 720 + xf * (-1.f / 40320 + xf * (1.f / 3628800 + xf * (-1.f / 479001600))));
+    const float c2_tail = xf * (1.f / 5040 + xf * (-1.f / 362880 + xf * (1.f / 39916800 + xf * (-1.f / 6227020800.f))));
+    ca = fma(th2, -1.0 / 6 + (double)ca_tail, 1.0);
+    c1 = fma(th2, -1.0 / 24 + (double)c1_tail, 0.5);
+    c2 = fma(th2, -1.0 / 120 + (double)c2_tail, 1.0 / 6);
+  } else {
+    const double th = sqrt(th2);
+    double v = 0.0;
+    if (lane == 0) v = sin(th);
+    if (lane == 1) v = cos(th);
+    const double sn = __shfl_sync(0xffffffffu, v, 0), cs = __shfl_sync(0xffffffffu, v, 1);
+    ca = sn / th;
+    c1 = (1 - cs) / th2;
+    c2 = (th - sn) / (th2 * th);
+  }
+  SF_SOLVE_MARK(3);
+  // R_ij = delta_ij + c_a W_ij + c_1 (w_i w_j - delta_ij t^2), lanes 0..8;
+  // W = [w]x: W01 = -w2, W02 = w1, W12 = -w0 and W^T = -W
+  {
+    const int i = lane < 9 ? lane / 3 : 0, j = lane < 9 ? lane - 3 * (lane / 3) : 0;
+    const int kk = 3 - i - j;  // the third axis when i != j
+    const double wi = i == 0 ? w0 : (i == 1 ? w1 : w2);
+    const double wj = j == 0 ? w0 : (j == 1 ? w1 : w2);
+    const double wk = kk == 0 ? w0 : (kk == 1 ? w1 : w2);
+    const bool cyc = (j == i + 1) || (i == 2 && j == 0);
+    const double Wij = (i == j) ? 0.0 : (cyc ? -wk : wk);
+    const double dl = (i == j) ? 1.0 : 0.0;
+    const double w2ij = fma(-dl, th2, wi * wj);
+    const double r = fma(c1, w2ij, fma(ca, Wij, dl));
+    if (lane < 9) s.R[lane] = r;
+  }
+  // t = u + c_1 (w x u) + c_2 (w x (w x u)); below 1e-10 rad Sophus uses
+  // V = R, so t = R u.  Lane i < 3 computes component i.
+  double ti;
+  const int ci = lane < 3 ? lane : 0;
+  if (th2 < 1e-20) {
+    __syncwarp();
+    ti = s.R[ci * 3 + 0] * u0;
+    ti = fma(s.R[ci * 3 + 1], u1, ti);
+    ti = fma(s.R[ci * 3 + 2], u2, ti);
+  } else {
+    // (cj, ck): the next two axes after ci, cyclically
+    const int cj = ci == 2 ? 0 : ci + 1, ck = ci == 0 ? 2 : ci - 1;
+    const double wj = cj == 0 ? w0 : (cj == 1 ? w1 : w2), wk = ck == 0 ? w0 : (ck == 1 ? w1 : w2);
+    const double uj = cj == 0 ? u0 : (cj == 1 ? u1 : u2), uk = ck == 0 ? u0 : (ck == 1 ? u1 : u2);
+    const double ui = ci == 0 ? u0 : (ci == 1 ? u1 : u2);
+    const double a = fma(wj, uk, -(wk * uj));  // (w x u)_i
+    const double aj = __shfl_sync(0xffffffffu, a, cj), ak = __shfl_sync(0xffffffffu, a, ck);
+    const double b = fma(wj, ak, -(wk * aj));  // (w x (w x u))_i
+    ti = fma(c2, b, fma(c1, a, ui));
+  }
+  const double t0 = __shfl_sync(0xffffffffu, ti, 0);
+  const double t1 = __shfl_sync(0xffffffffu, ti, 1);
+  const double t2 = __shfl_sync(0xffffffffu, ti, 2);
+  __syncwarp();
+  SF_SOLVE_MARK(4);
+  // delta = exp(x) * delta (top 3 rows; the bottom row stays 0 0 0 1)
+  if (lane < 12) {
+    const int i = lane >> 2, j = lane & 3;
+    const double *D = c.delta;
+    double v = s.R[i * 3 + 0] * D[0 * 4 + j];
+    v = fma(s.R[i * 3 + 1], D[1 * 4 + j], v);
+    v = fma(s.R[i * 3 + 2], D[2 * 4 + j], v);
+    if (j == 3) v += (i == 0 ? t0 : (i == 1 ? t1 : t2));
+    s.delta[lane] = v;
+  }
+  __syncwarp();
+  if (lane < 12) c.delta[lane] = s.delta[lane];
+  // dInv = [D^T, -D^T t]
+  if (lane < 12) {
+    const int i = lane >> 2, j = lane & 3;
+    const double *D = s.delta;
+    double v;
+    if (j < 3) {
+      v = D[j * 4 + i];
+    } else {
+      v = -(D[0 * 4 + i] * D[3]);
+      v = fma(-D[1 * 4 + i], D[7], v);
+      v = fma(-D[2 * 4 + i], D[11], v);
+    }
+    s.dInv[lane] = v;
+  }
+  __syncwarp();
+  // next = last * dInv
+  if (lane < 16) {
+    const int i = lane >> 2, j = lane & 3;
+    double v;
+    if (i == 3) {
+      v = (j == 3) ? 1.0 : 0.0;
+    } else {
+      const double *L = c.last_pose;
+      v = L[i * 4 + 0] * s.dInv[0 * 4 + j];
+      v = fma(L[i * 4 + 1], s.dInv[1 * 4 + j], v);
+      v = fma(L[i * 4 + 2], s.dInv[2 * 4 + j], v);
+      if (j == 3) v += L[i * 4 + 3];
+    }
+    c.next_pose[lane] = v;
+  }
+  __syncwarp();
+  SF_SOLVE_MARK(5);
+  return true;
+}
+
+// Acceptance gate of sf::ctl_finish (Tracking.cc:505-516) for one warp.
+// p = start^-1 * next = [S^T N, S^T (t_next - t_start)], one element per
+// lane.  |sin| of the three Euler angles (eulerAngles(0, 1, 2)) comes from
+// the matrix entries instead of asin / atan2 / sin: sin b = r02,
+// |sin a| = |r12| / |(r12, r22)|, |sin c| = |r01| / |(r00, r01)|, the same
+// for both of Eigen's solution branches.
+__device__ void ctl_finish_fast(TrackCtl &c, float thresh, IcpSolveSmem &s) {
+  const int lane = threadIdx.x & 31;
+  if (c.stop == 1) {
+    if (lane == 0) c.accepted = 0;
+    __syncwarp();
+    return;
+  }
+  if (lane < 12) {
+    const int i = lane >> 2, j = lane & 3;
+    const double *S = c.start_pose, *N = c.next_pose;
+    double v;
+    if (j < 3) {
+      v = S[0 * 4 + i] * N[0 * 4 + j];
+      v = fma(S[1 * 4 + i], N[1 * 4 + j], v);
+      v = fma(S[2 * 4 + i], N[2 * 4 + j], v);
+    } else {
+      v = S[0 * 4 + i] * (N[3] - S[3]);
+      v = fma(S[1 * 4 + i], N[7] - S[7], v);
+      v = fma(S[2 * 4 + i], N[11] - S[11], v);
+    }
+    s.delta[lane] = v;
+  }
+  __syncwarp();
+  int accepted = 0;
+  if (lane == 0) {
+    const double *p = s.delta;
+    const double tn = sqrt(p[3] * p[3] + p[7] * p[7] + p[11] * p[11]);
+    const double r02 = p[2] < -1.0 ? -1.0 : (p[2] > 1.0 ? 1.0 : p[2]);
+    const double ha = p[6] * p[6] + p[10] * p[10], hc = p[0] * p[0] + p[1] * p[1];
+    const double sa2 = ha > 0.0 ? (p[6] * p[6]) / ha : 0.0;
+    const double sc2 = hc > 0.0 ? (p[1] * p[1]) / hc : 0.0;
+    const double an = sqrt(sa2 + r02 * r02 + sc2);
+    accepted = (c.icpError < thresh) && (an <= 0.1 && tn <= 0.1);
+    c.accepted = accepted;
+  }
+  accepted = __shfl_sync(0xffffffffu, accepted, 0);
+  if (!accepted && lane < 16) c.next_pose[lane] = c.last_pose[lane];
+  __syncwarp();
+}
+
+}  // namespace sf
+#endif
