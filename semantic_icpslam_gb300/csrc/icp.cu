@@ -30,8 +30,14 @@ namespace sf {
 
 namespace {
 
-constexpr int kThreads = 512;    // plain-form kernels
-constexpr int kPThreads = 1024;  // persistent kernel: one CTA per SM
+// Persistent-kernel CTA size (a multiple of 32, at most 1024).  512 threads
+// with the registers that one CTA per SM allows (about 124) measured
+// fastest on GB300, ahead of 768 and 1024 threads at 64-85 registers.
+#ifndef SF_ICP_PTHREADS
+#define SF_ICP_PTHREADS 512
+#endif
+constexpr int kThreads = 512;               // plain-form kernels
+constexpr int kPThreads = SF_ICP_PTHREADS;  // persistent kernel
 constexpr int kProfIters = 64;
 constexpr int kProfSlots = 16;  // per iteration: 0-5 phases, 6 globaltimer, 8-13 solve steps
 constexpr int kWarps = kThreads / 32;
@@ -41,17 +47,6 @@ struct PoseF {
   m3 Rc, Rl, RlI;
   f3 tc, tl;
 };
-
-// Frame::GpuRotation / GpuInvRotation / GpuTranslation (Core/Frame.cc:626-645).
-__host__ __device__ inline void pose_to_float(const double *P, m3 &R, m3 &Rinv, f3 &t) {
-  R.rx.x = (float)P[0]; R.rx.y = (float)P[1]; R.rx.z = (float)P[2];
-  R.ry.x = (float)P[4]; R.ry.y = (float)P[5]; R.ry.z = (float)P[6];
-  R.rz.x = (float)P[8]; R.rz.y = (float)P[9]; R.rz.z = (float)P[10];
-  Rinv.rx.x = (float)P[0]; Rinv.rx.y = (float)P[4]; Rinv.rx.z = (float)P[8];
-  Rinv.ry.x = (float)P[1]; Rinv.ry.y = (float)P[5]; Rinv.ry.z = (float)P[9];
-  Rinv.rz.x = (float)P[2]; Rinv.rz.y = (float)P[6]; Rinv.rz.z = (float)P[10];
-  t.x = (float)P[3]; t.y = (float)P[7]; t.z = (float)P[11];
-}
 
 // (int)((double)t + 0.5) of Reduction.cu:239-240 evaluated in float: the
 // double sum is exact for every float t, so the result is floor(t) +
@@ -65,57 +60,98 @@ __device__ __forceinline__ int round_half_up(float t) {
   return (t > -1.5f) ? 0 : -1;
 }
 
-// ICPReduce::searchPoint + getRow (Reduction.cu:228-279).
-__device__ __forceinline__ bool icp_row(const IcpLevelArgs &L, int x, int y, const PoseF &p,
-                                        float row[7]) {
-  float4 vc4 = __ldg(row_ptr<const float4>(L.vc, y) + x);
-  f3 vcurr_c = xyz(vc4);
-  if (isnan(vcurr_c.x) || (double)vcurr_c.z < 1e-3) return false;
-  f3 vcurr_g = mul(p.Rc, vcurr_c) + p.tc;
-  f3 vcurr_p = mul(p.RlI, vcurr_g - p.tl);
+// Frame::GpuRotation / GpuInvRotation / GpuTranslation (Core/Frame.cc
+// :626-645) of the current and last poses, one element per lane of the
+// calling warp (one FP64 conversion instruction, not 21 in one thread).
+__device__ __forceinline__ void pose_to_float_warp(const double *Pc, const double *Pl, PoseF &p) {
+  const int lane = threadIdx.x & 31;
+  if (lane < 9) {
+    const int i = lane / 3, j = lane - 3 * (lane / 3);
+    const float rc = (float)Pc[i * 4 + j], rl = (float)Pl[i * 4 + j];
+    (&p.Rc.rx.x)[lane] = rc;
+    (&p.Rl.rx.x)[lane] = rl;
+    (&p.RlI.rx.x)[j * 3 + i] = rl;
+  } else if (lane < 12) {
+    const int i = lane - 9;
+    (&p.tc.x)[i] = (float)Pc[i * 4 + 3];
+    (&p.tl.x)[i] = (float)Pl[i * 4 + 3];
+  }
+}
+static_assert(sizeof(m3) == 9 * sizeof(float) && sizeof(f3) == 3 * sizeof(float), "packed pose");
+
+// ICPReduce::searchPoint + getRow (Reduction.cu:228-279), split at the
+// dependent loads: icp_project maps a current vertex to the model pixel
+// (u, v), icp_finish takes the three loads and returns the row.
+struct IcpProj {
+  f3 vg;  // current vertex in the world frame
+  int u, v;
+  bool ok;
+};
+
+__device__ __forceinline__ IcpProj icp_project(const IcpLevelArgs &L, const PoseF &p, float4 vc4) {
+  IcpProj q;
+  q.ok = false;
+  q.u = 0;
+  q.v = 0;
+  const f3 vcurr_c = xyz(vc4);
+  q.vg = mul(p.Rc, vcurr_c) + p.tc;
+  // (double)z < 1e-3 of the reference is exactly z < 0.001f for a float z
+  if (isnan(vcurr_c.x) || vcurr_c.z < 0.001f) return q;
+  const f3 vcurr_p = mul(p.RlI, q.vg - p.tl);
   // (float)(1.0 / (double)z): double rounding is innocuous for division,
   // so this equals the correctly rounded float quotient.
-  float invz = __fdiv_rn(1.0f, vcurr_p.z);
-  int u = round_half_up(vcurr_p.x * invz * L.fx + L.cx);
-  int v = round_half_up(vcurr_p.y * invz * L.fy + L.cy);
-  if (u < 0 || v < 0 || u >= L.vc.cols || v >= L.vc.rows) return false;
-  float4 vl4 = __ldg(row_ptr<const float4>(L.vl, v) + u);
-  float4 nl4 = __ldg(row_ptr<const float4>(L.nl, v) + u);
-  float4 nc4 = __ldg(row_ptr<const float4>(L.nc, y) + x);
-  f3 vlast_g = mul(p.Rl, xyz(vl4)) + p.tl;
-  f3 ncurr_g = mul(p.Rc, xyz(nc4));
-  f3 nlast_g = mul(p.Rl, xyz(nl4));
-  float dist = norm(vlast_g - vcurr_g);
-  float sine = norm(cross(ncurr_g, nlast_g));
+  const float invz = __fdiv_rn(1.0f, vcurr_p.z);
+  q.u = round_half_up(vcurr_p.x * invz * L.fx + L.cx);
+  q.v = round_half_up(vcurr_p.y * invz * L.fy + L.cy);
+  q.ok = !(q.u < 0 || q.v < 0 || q.u >= L.vc.cols || q.v >= L.vc.rows);
+  return q;
+}
+
+__device__ __forceinline__ bool icp_finish(const PoseF &p, const IcpProj &q, float4 vl4, float4 nl4,
+                                           float4 nc4, float row[7]) {
+  const f3 vlast_g = mul(p.Rl, xyz(vl4)) + p.tl;
+  const f3 ncurr_g = mul(p.Rc, xyz(nc4));
+  const f3 nlast_g = mul(p.Rl, xyz(nl4));
+  const float dist = norm(vlast_g - q.vg);
+  const float sine = norm(cross(ncurr_g, nlast_g));
   if (!(sine < 0.6f && dist <= 0.1f && !isnan(nc4.x) && !isnan(nl4.x))) return false;
-  f3 nlast = mul(p.RlI, nlast_g);
-  f3 vcurr = mul(p.RlI, vcurr_g - p.tl);
-  f3 vlast = mul(p.RlI, vlast_g - p.tl);
-  f3 mn = -nlast;
-  f3 cr = cross(nlast, vlast);
+  const f3 nlast = mul(p.RlI, nlast_g);
+  const f3 vcurr = mul(p.RlI, q.vg - p.tl);
+  const f3 vlast = mul(p.RlI, vlast_g - p.tl);
+  const f3 mn = -nlast;
+  const f3 cr = cross(nlast, vlast);
   row[0] = mn.x; row[1] = mn.y; row[2] = mn.z;
   row[3] = cr.x; row[4] = cr.y; row[5] = cr.z;
   row[6] = dot(mn, vcurr - vlast);
   return true;
 }
 
-// Accumulates the 29 terms (Reduction.cu:281-289) of this thread's pixels.
+__device__ __forceinline__ void icp_add_row(float acc[29], const float row[7]) {
+  int k = 0;
+#pragma unroll
+  for (int a = 0; a < 7; ++a)
+#pragma unroll
+    for (int b = a; b < 7; ++b) acc[k++] += row[a] * row[b];
+  acc[28] += 1.0f;
+}
+
+// Accumulates the 29 terms (Reduction.cu:281-289) of this thread's pixels
+// i = gtid, gtid + gstride, ... in that order.
 __device__ __forceinline__ void icp_accumulate(const IcpLevelArgs &L, const PoseF &p, int gtid,
                                                int gstride, float acc[29]) {
 #pragma unroll
   for (int k = 0; k < 29; ++k) acc[k] = 0.f;
-  const int N = L.vc.cols * L.vc.rows;
+  const int cols = L.vc.cols;
+  const int N = cols * L.vc.rows;
   for (int i = gtid; i < N; i += gstride) {
-    const int y = i / L.vc.cols;
-    const int x = i - y * L.vc.cols;
+    const int y = i / cols, x = i - y * cols;
+    const IcpProj q = icp_project(L, p, __ldg(row_ptr<const float4>(L.vc, y) + x));
+    if (!q.ok) continue;
+    const float4 vl = __ldg(row_ptr<const float4>(L.vl, q.v) + q.u);
+    const float4 nl = __ldg(row_ptr<const float4>(L.nl, q.v) + q.u);
+    const float4 nc = __ldg(row_ptr<const float4>(L.nc, y) + x);
     float row[7];
-    if (!icp_row(L, x, y, p, row)) continue;
-    int k = 0;
-#pragma unroll
-    for (int a = 0; a < 7; ++a)
-#pragma unroll
-      for (int b = a; b < 7; ++b) acc[k++] += row[a] * row[b];
-    acc[28] += 1.0f;
+    if (icp_finish(p, q, vl, nl, nc, row)) icp_add_row(acc, row);
   }
 }
 
@@ -197,31 +233,20 @@ __device__ __forceinline__ ff warp_transpose_reduce29(const float acc[29]) {
 }
 
 // Block total of the 29 terms as normalised float-float pairs in smem
-// out[29]: warp butterflies, then the NW warp totals of each component are
-// added with a shuffle tree (16 warps: two components per warp, lanes
-// 0..15 and 16..31; 32 warps: warp c takes component c).  wpart rows are
-// padded to 33 so the column reads hit distinct banks.
+// out[29]: warp butterflies, then for each component the NW warp totals
+// are added with a shuffle tree (warp w takes components w, w + NW, ...).
+// wpart rows are padded to 33 so the column reads hit distinct banks.
 template <int NW>
 __device__ __forceinline__ void block_reduce29(const float acc[29], ff (*wpart)[33], float2 *out) {
-  static_assert(NW == 16 || NW == 32, "16 or 32 warps");
+  static_assert(NW >= 1 && NW <= 32, "1..32 warps");
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   wpart[warp][lane] = warp_transpose_reduce29(acc);
   __syncthreads();
-  if (NW == 16) {
-    if (warp < 15) {
-      const int c = 2 * warp + (lane >> 4);
-      ff v = (c < 29) ? wpart[lane & 15][c] : ff{0.f, 0.f};
+  for (int c = warp; c < 29; c += NW) {
+    ff v = (lane < NW) ? wpart[lane][c] : ff{0.f, 0.f};
 #pragma unroll
-      for (int off = 8; off > 0; off >>= 1) v = ff_add(v, ff_shfl_xor(v, off));
-      if ((lane & 15) == 0 && c < 29) out[c] = ff_norm(v);
-    }
-  } else {
-    if (warp < 29) {
-      ff v = wpart[lane][warp];
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) v = ff_add(v, ff_shfl_xor(v, off));
-      if (lane == 0) out[warp] = ff_norm(v);
-    }
+    for (int off = 16; off > 0; off >>= 1) v = ff_add(v, ff_shfl_xor(v, off));
+    if (lane == 0) out[c] = ff_norm(v);
   }
   __syncthreads();
 }
@@ -364,11 +389,7 @@ __global__ void __launch_bounds__(kPThreads, 1) k_icp_persistent(PersistentArgs 
     const IcpLevelArgs &L = a.lv[l];
     for (int j = 0; j < L.iters; ++j, ++it) {
       prof_mark(a, it, 0);
-      if (threadIdx.x == 0) {
-        m3 dummy;
-        pose_to_float(ctl.next_pose, pose.Rc, dummy, pose.tc);
-        pose_to_float(ctl.last_pose, pose.Rl, pose.RlI, pose.tl);
-      }
+      if (threadIdx.x < 32) pose_to_float_warp(ctl.next_pose, ctl.last_pose, pose);
       __syncthreads();
       float acc[29];
       icp_accumulate(L, pose, gtid, gstride, acc);

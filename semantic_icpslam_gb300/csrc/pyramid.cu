@@ -75,12 +75,13 @@ __global__ void k_pyrdown(sf_image src, sf_image dst) {
   row_ptr<float>(dst, y)[x] = pyrdown_px(src, x, y);
 }
 
-// ComputeVMapKernel (Pyrdown.cu:123-145): z in (0.1, cutoff), 0.1 compared
-// in double as in the reference.
+// ComputeVMapKernel (Pyrdown.cu:123-145): z in (0.1, cutoff), where the
+// reference compares (double)z > 0.1.  No float lies in (0.1, 0.1f], so for
+// a float z that is exactly z >= 0.1f, with no FP64 instruction.
 __device__ __forceinline__ float4 vertex_at(const sf_image &depth, int x, int y, float invfx,
                                             float invfy, float cx, float cy, float cutoff) {
   float z = __ldg(row_ptr<const float>(depth, y) + x);
-  if (!isnan(z) && (double)z > 0.1 && z < cutoff) {
+  if (!isnan(z) && z >= 0.1f && z < cutoff) {
     return make_float4(z * ((float)x - cx) * invfx, z * ((float)y - cy) * invfy, z, 1.0f);
   }
   return nan4();

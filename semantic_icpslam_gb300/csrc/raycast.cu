@@ -201,7 +201,9 @@ __global__ void __launch_bounds__(128) k_raycast(DevMap m, FuseScratch f, sf_ima
   const int lx = (int)floorf((float)x / 8.0f), ly = (int)floorf((float)y / 8.0f);
   const float zx = __ldg(row_ptr<const float>(zmin, ly) + lx);
   const float zy = __ldg(row_ptr<const float>(zmax, ly) + lx);
-  if (!((double)zy < 1e-3 || (double)zx < 1e-3 || isnan(zx) || isnan(zy))) {
+  // (double)z < 1e-3 of the reference: no float lies in [1e-3, 0.001f), so
+  // for a float z that is exactly z < 0.001f
+  if (!(zy < 0.001f || zx < 0.001f || isnan(zx) || isnan(zy))) {
     const float vsi = m.c.voxel_size_inv;
     float sdf = 1.0f;
     f3 p;

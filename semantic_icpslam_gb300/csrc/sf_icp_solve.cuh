@@ -9,15 +9,14 @@
 // sf::ctl_step (sf_solve.h), which restates Tracker::ComputeSE3
 // (Tracking/Tracking.cc:449-499), with as few FP64 instructions per warp as
 // it can:
-//  - A x = b by Gauss-Jordan elimination of the augmented 6x7 matrix held
-//    in lane registers (element e = 7*i + j: lane e, then lane e-32), two
-//    FP64 instructions per register and step.  The pivot order is LDLT's
-//    symmetric pivoting (largest remaining |diagonal|, first on ties,
-//    compared on the integer bits; every uneliminated row carries the same
-//    scale, so the comparison is LDLT's), a zero pivot zeroes its
-//    component as in the LDLT solve, and instead of dividing, each step
-//    rescales the updated rows by an exact power of two through exponent
-//    arithmetic.  The six divisions x_i = b_i / a_ii run side by side.
+//  - A x = b by Gauss-Jordan elimination of the augmented 6x7 matrix, two
+//    elements per lane, two FP64 instructions per element and step.  The
+//    pivot order is LDLT's symmetric pivoting (largest remaining
+//    |diagonal|; every uneliminated row carries the same scale, so the
+//    comparison is LDLT's), a zero pivot zeroes its component as in the
+//    LDLT solve, and instead of dividing, each step rescales the updated
+//    rows by an exact power of two through exponent arithmetic.  The six
+//    divisions x_i = b_i / a_ii run side by side.
 //  - exp(x) in Rodrigues form, R = I + c_a W + c_1 W^2 and
 //    t = u + c_1 (w x u) + c_2 (w x (w x u)), with c_a = sin(t)/t,
 //    c_1 = (1 - cos t)/t^2, c_2 = (t - sin t)/t^3: the same rotation and
@@ -42,95 +41,81 @@
 namespace sf {
 
 struct IcpSolveSmem {
+  double a[6][8];    // augmented [A | b], row stride 8
   double R[9];
   double delta[12];  // updated delta (top 3 rows)
   double dInv[12];   // its inverse (top 3 rows)
 };
 
-// Element e (0..41) of the augmented matrix held as (r0: e = lane,
-// r1: e = 32 + lane).  Every lane must call it.
-__device__ __forceinline__ double aug_get(double r0, double r1, int e) {
-  const double v0 = __shfl_sync(0xffffffffu, r0, e & 31);
-  const double v1 = __shfl_sync(0xffffffffu, r1, e & 31);
-  return e < 32 ? v0 : v1;
-}
-
-// v * 2^sh by exponent arithmetic (no FP64 instruction).  Zero and
-// subnormal inputs pass unchanged; results past the exponent range flush
-// to signed zero or saturate to infinity.
+// v * 2^sh by exponent arithmetic on the high word (no FP64 instruction).
+// Zero, subnormal, infinite and NaN inputs pass unchanged; a result below
+// the normal range flushes to signed zero, one above it saturates to
+// infinity.
 __device__ __forceinline__ double scale_pow2(double v, int sh) {
-  const long long b = __double_as_longlong(v);
-  const int e = (int)((b >> 52) & 0x7ff);
-  const long long sign = b & (long long)0x8000000000000000ull;
+  const int hi = __double2hiint(v), lo = __double2loint(v);
+  const int e = (hi >> 20) & 0x7ff;
   const int ne = e + sh;
-  long long r = b + ((long long)sh << 52);
-  r = ne <= 0 ? sign : r;
-  r = ne >= 0x7ff ? (sign | 0x7ff0000000000000ll) : r;
-  r = (e == 0 || e == 0x7ff) ? b : r;
-  return __longlong_as_double(r);
+  int rhi = hi + (sh << 20), rlo = lo;
+  if (ne <= 0) { rhi = hi & (int)0x80000000; rlo = 0; }
+  if (ne >= 0x7ff) { rhi = (hi & (int)0x80000000) | 0x7ff00000; rlo = 0; }
+  if (e == 0 || e == 0x7ff) { rhi = hi; rlo = lo; }
+  return __hiloint2double(rhi, rlo);
 }
 
 // Solves A x = b for the 27 upper-triangle sums of CreateMatrix<6,7>
-// (Tracking/Reduction.cu:6-16); every lane returns x[0..5].
-__device__ __forceinline__ void warp_solve6(const double *sums, double x[6]) {
+// (Tracking/Reduction.cu:6-16); every lane returns x[0..5].  Lane l owns
+// elements e = l and e = l + 32 (< 42) of the row-major augmented matrix
+// (e = 7 i + j), keeps them in registers and mirrors them in s.a for the
+// other lanes' reads.  The pivot is found with one warp max over keys made
+// of the top 28 bits of |a_ii| (exponent and 17 mantissa bits) and 7 - i
+// in the low 3 bits: diagonals within 2^-17 of each other count as equal
+// and the lower index wins, as on an exact tie.
+__device__ __forceinline__ void warp_solve6(const double *sums, double x[6], IcpSolveSmem &s) {
   const int lane = threadIdx.x & 31;
-  // augmented [A | b]: row i, column j (j == 6 is b); A symmetric from the
-  // upper triangle, row i of the sums starts at 7i - i(i-1)/2
-  auto sum_at = [&](int e) {
-    const int i = e / 7, j = e - 7 * (e / 7);
+  auto sum_at = [&](int i, int j) {
     const int r = i < j ? i : j, q = i < j ? j : i;
     return j == 6 ? sums[7 * i - i * (i - 1) / 2 + (6 - i)] : sums[7 * r - r * (r - 1) / 2 + (q - r)];
   };
-  double r0 = sum_at(lane);
-  double r1 = lane < 10 ? sum_at(32 + lane) : 0.0;
   const int i0 = lane / 7, j0 = lane - 7 * (lane / 7);
-  const int e1 = lane < 10 ? 32 + lane : 41;
-  const int i1 = e1 / 7, j1 = e1 - 7 * (e1 / 7);
+  const bool has1 = lane < 10;
+  const int i1 = has1 ? (lane + 32) / 7 : 5, j1 = has1 ? (lane + 32) - 7 * ((lane + 32) / 7) : 6;
+  double r0 = sum_at(i0, j0);
+  double r1 = has1 ? sum_at(i1, j1) : 0.0;
+  s.a[i0][j0] = r0;
+  if (has1) s.a[i1][j1] = r1;
+  __syncwarp();
   unsigned done = 0, zero = 0;
 #pragma unroll 1
   for (int step = 0; step < 6; ++step) {
-    double d[6];
-    d[0] = __shfl_sync(0xffffffffu, r0, 0);
-    d[1] = __shfl_sync(0xffffffffu, r0, 8);
-    d[2] = __shfl_sync(0xffffffffu, r0, 16);
-    d[3] = __shfl_sync(0xffffffffu, r0, 24);
-    d[4] = __shfl_sync(0xffffffffu, r1, 0);
-    d[5] = __shfl_sync(0xffffffffu, r1, 8);
-    // largest |diagonal| among the uneliminated rows, first on ties; the
-    // magnitude bits of a double order like the values
-    int k = -1;
-    unsigned long long best = 0;
-    double akk = 0.0;
-#pragma unroll
-    for (int i = 0; i < 6; ++i) {
-      const unsigned long long key = (unsigned long long)__double_as_longlong(d[i]) & 0x7fffffffffffffffull;
-      const bool take = !((done >> i) & 1u) && (k < 0 || key > best);
-      best = take ? key : best;
-      k = take ? i : k;
-      akk = take ? d[i] : akk;
+    unsigned key = 0;
+    if (lane < 6 && !((done >> lane) & 1u)) {
+      const unsigned hi = (unsigned)__double2hiint(s.a[lane][lane]) & 0x7fffffffu;
+      key = hi < 0x00100000u ? 0u : ((hi & ~7u) | (7u - lane));  // zero / subnormal: no pivot
     }
+    const unsigned best = __reduce_max_sync(0xffffffffu, key);
     if (best == 0) {  // every remaining pivot is zero: those components are 0
       zero = 0x3fu & ~done;
       break;
     }
+    const int k = 7 - (int)(best & 7u);
     done |= 1u << k;
-    const int ek = (int)((__double_as_longlong(akk) >> 52) & 0x7ff);
-    const int sh = ek == 0 ? 0 : 1023 - ek;  // |akk| * 2^sh in [1, 2)
-    const double aik0 = aug_get(r0, r1, i0 * 7 + k);
-    const double akj0 = aug_get(r0, r1, k * 7 + j0);
-    const double aik1 = aug_get(r0, r1, i1 * 7 + k);
-    const double akj1 = aug_get(r0, r1, k * 7 + j1);
+    const double akk = s.a[k][k];
+    const int ek = (__double2hiint(akk) >> 20) & 0x7ff;
+    const int sh = 1023 - ek;  // |akk| * 2^sh in [1, 2)
+    const double aik0 = s.a[i0][k], akj0 = s.a[k][j0];
+    const double aik1 = s.a[i1][k], akj1 = s.a[k][j1];
     const double u0 = fma(akk, r0, -(aik0 * akj0));
     const double u1 = fma(akk, r1, -(aik1 * akj1));
     r0 = (i0 == k) ? r0 : ((j0 == k) ? 0.0 : scale_pow2(u0, sh));
-    r1 = (lane >= 10 || i1 == k) ? r1 : ((j1 == k) ? 0.0 : scale_pow2(u1, sh));
+    r1 = (!has1 || i1 == k) ? r1 : ((j1 == k) ? 0.0 : scale_pow2(u1, sh));
+    __syncwarp();
+    s.a[i0][j0] = r0;
+    if (has1) s.a[i1][j1] = r1;
+    __syncwarp();
   }
-  // x_i = b_i / a_ii: lane i gathers row i's b (element 7i+6) and pivot
-  // (element 8i); the six divisions run side by side
+  // x_i = b_i / a_ii, the six divisions side by side in lanes 0..5
   const int row = lane < 6 ? lane : 0;
-  const double bi = aug_get(r0, r1, row * 7 + 6);
-  const double ai = aug_get(r0, r1, row * 8);
-  const double xi = ((zero >> row) & 1u) ? 0.0 : bi / ai;
+  const double xi = ((zero >> row) & 1u) ? 0.0 : s.a[row][6] / s.a[row][row];
 #pragma unroll
   for (int i = 0; i < 6; ++i) x[i] = __shfl_sync(0xffffffffu, xi, i);
 }
@@ -186,7 +171,7 @@ __device__ bool ctl_step_fast(TrackCtl &c, const double *sums, int min_count, Ic
 
   SF_SOLVE_MARK(1);
   double x[6];
-  warp_solve6(sums, x);
+  warp_solve6(sums, x, s);
   SF_SOLVE_MARK(2);
   const double u0 = x[0], u1 = x[1], u2 = x[2];
   const double w0 = x[3], w1 = x[4], w2 = x[5];

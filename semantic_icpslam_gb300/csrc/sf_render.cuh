@@ -59,7 +59,7 @@ __device__ __forceinline__ bool project_block(i3 pos, float voxel, const m3 &Rin
     f3 p3 = mk3((float)(int)((unsigned)tx * 8u) * voxel, (float)(int)((unsigned)ty * 8u) * voxel,
                 (float)(int)((unsigned)tz * 8u) * voxel);
     p3 = mul(Rinv, p3 - t);
-    if ((double)p3.z < 2e-1) continue;
+    if (p3.z < 0.2f) continue;  // (double)z < 2e-1: no float lies in [0.2, 0.2f)
     float px = (fx * p3.x / p3.z + cx) / 8.0f;
     float py = (fy * p3.y / p3.z + cy) / 8.0f;
     if ((float)b.ulx > floorf(px)) b.ulx = (int16_t)(int)floorf(px);
