@@ -90,15 +90,32 @@ __global__ void k_fill_blocks(sf_image zmin, sf_image zmax, const sf_rendering_b
 // as {pos (0,0,0), ptr -1}, which would alias block (0,0,0) to voxel index
 // -1; that aliasing is not reproduced.)
 struct RayCtx {
-  const DevMap *m;
+  const sf_voxel *voxels;
   const int *cells;
   int win[6];
+  const sf_hash_entry *entries;
+  uint32_t num_buckets, num_excess;
 };
 
-__device__ __forceinline__ int block_ptr(const RayCtx &r, i3 bp) {
-  const int cell = window_cell(r.win, bp);
-  if (cell >= 0) return __ldg(r.cells + cell);
-  return find_block(*r.m, bp);
+// Hash-table lookup (DeviceMap::FindEntry) for a block outside the window;
+// rare, so kept out of line to keep the inlined sample code small.
+__device__ __noinline__ int block_ptr_hash(const sf_hash_entry *entries, uint32_t num_buckets,
+                                           uint32_t num_excess, int bx, int by, int bz) {
+  DevMap m;
+  m.entries = const_cast<sf_hash_entry *>(entries);
+  m.c.num_buckets = num_buckets;
+  m.c.num_excess = num_excess;
+  i3 p;
+  p.x = bx; p.y = by; p.z = bz;
+  return find_block(m, p);
+}
+
+// Voxel index of block (bx, by, bz), or -1.
+__device__ __forceinline__ int block_ptr(const RayCtx &r, int bx, int by, int bz) {
+  const unsigned x = (unsigned)(bx - r.win[0]), y = (unsigned)(by - r.win[1]), z = (unsigned)(bz - r.win[2]);
+  if (x < (unsigned)r.win[3] && y < (unsigned)r.win[4] && z < (unsigned)r.win[5])
+    return __ldg(r.cells + (int)((z * (unsigned)r.win[4] + y) * (unsigned)r.win[3] + x));
+  return block_ptr_hash(r.entries, r.num_buckets, r.num_excess, bx, by, bz);
 }
 
 struct VoxelRead {
@@ -107,11 +124,11 @@ struct VoxelRead {
   bool found;
 };
 
-// DeviceMap::FindVoxel(float3, cache, valid): a missing block reads as
-// Voxel() (sdf NaN, weight 0) and valid = false.
-__device__ __forceinline__ VoxelRead read_voxel(const RayCtx &r, f3 pt) {
-  const i3 p = floor3(pt);
-  const int ptr = block_ptr(r, vox2block(p));
+// Voxel (vx, vy, vz) of the block whose voxel index is ptr (block
+// coordinates are v >> 3, local ones v & 7, as worldPosToVoxelPos /
+// voxelPosToLocalIdx compute them).  A missing block reads as Voxel()
+// (sdf NaN, weight 0) with found = false, as DeviceMap::FindVoxel does.
+__device__ __forceinline__ VoxelRead voxel_in(const RayCtx &r, int ptr, int vx, int vy, int vz) {
   VoxelRead v;
   if (ptr < 0) {
     v.sdf = nanf_bits();
@@ -119,33 +136,46 @@ __device__ __forceinline__ VoxelRead read_voxel(const RayCtx &r, f3 pt) {
     v.found = false;
     return v;
   }
-  const uint2 raw = __ldg((const uint2 *)(r.m->voxels + ptr + vox2local(p)));
+  const uint2 raw = __ldg((const uint2 *)(r.voxels + ptr + ((vz & 7) * 64 + (vy & 7) * 8 + (vx & 7))));
   v.sdf = __uint_as_float(raw.x);
   v.weight = raw.y & 0xffu;
   v.found = true;
   return v;
 }
 
-// Rendering::readSdf (RenderScene.cu:303-308).
-__device__ __forceinline__ float read_sdf(const RayCtx &r, f3 pt, bool &valid) {
-  VoxelRead v = read_voxel(r, pt);
-  valid = v.found && v.weight != 0;
-  return v.sdf;
+__device__ __forceinline__ VoxelRead read_voxel(const RayCtx &r, f3 pt) {
+  const i3 p = floor3(pt);
+  return voxel_in(r, block_ptr(r, p.x >> 3, p.y >> 3, p.z >> 3), p.x, p.y, p.z);
 }
 
-// Rendering::readSdfInterped (RenderScene.cu:310-343).  The eight corner
-// reads are independent; `valid` is the last corner's (pt + (1,1,1)), as
-// each FindVoxel call overwrites it in the reference.
-__device__ __forceinline__ float read_sdf_interp(const RayCtx &r, f3 pt, bool &valid) {
+// Rendering::readSdfInterped (RenderScene.cu:310-343).  The corners are
+// the reference's floor3(pt + offset); per axis that is floor(pt) or
+// floor(pt + 1), so six floors give all eight.  Corners that share a block
+// share one lookup.  `valid` is the last corner's (pt + (1,1,1)), as each
+// FindVoxel call overwrites it in the reference.
+__device__ __forceinline__ float sdf_interp(const RayCtx &r, f3 pt, bool &valid) {
   const f3 xyz3 = pt - mk3(floorf(pt.x), floorf(pt.y), floorf(pt.z));
-  const VoxelRead c000 = read_voxel(r, pt);
-  const VoxelRead c100 = read_voxel(r, pt + mk3(1, 0, 0));
-  const VoxelRead c010 = read_voxel(r, pt + mk3(0, 1, 0));
-  const VoxelRead c110 = read_voxel(r, pt + mk3(1, 1, 0));
-  const VoxelRead c001 = read_voxel(r, pt + mk3(0, 0, 1));
-  const VoxelRead c101 = read_voxel(r, pt + mk3(1, 0, 1));
-  const VoxelRead c011 = read_voxel(r, pt + mk3(0, 1, 1));
-  const VoxelRead c111 = read_voxel(r, pt + mk3(1, 1, 1));
+  const i3 a = floor3(pt);
+  const i3 b = floor3(pt + mk3(1, 1, 1));
+  const int ax = a.x >> 3, ay = a.y >> 3, az = a.z >> 3;
+  const int bx = b.x >> 3, by = b.y >> 3, bz = b.z >> 3;
+  const bool sx = ax == bx, sy = ay == by, sz = az == bz;
+  const int p000 = block_ptr(r, ax, ay, az);
+  const int p100 = sx ? p000 : block_ptr(r, bx, ay, az);
+  const int p010 = sy ? p000 : block_ptr(r, ax, by, az);
+  const int p110 = sx ? p010 : (sy ? p100 : block_ptr(r, bx, by, az));
+  const int p001 = sz ? p000 : block_ptr(r, ax, ay, bz);
+  const int p101 = sx ? p001 : (sz ? p100 : block_ptr(r, bx, ay, bz));
+  const int p011 = sy ? p001 : (sz ? p010 : block_ptr(r, ax, by, bz));
+  const int p111 = sx ? p011 : (sy ? p101 : (sz ? p110 : block_ptr(r, bx, by, bz)));
+  const VoxelRead c000 = voxel_in(r, p000, a.x, a.y, a.z);
+  const VoxelRead c100 = voxel_in(r, p100, b.x, a.y, a.z);
+  const VoxelRead c010 = voxel_in(r, p010, a.x, b.y, a.z);
+  const VoxelRead c110 = voxel_in(r, p110, b.x, b.y, a.z);
+  const VoxelRead c001 = voxel_in(r, p001, a.x, a.y, b.z);
+  const VoxelRead c101 = voxel_in(r, p101, b.x, a.y, b.z);
+  const VoxelRead c011 = voxel_in(r, p011, a.x, b.y, b.z);
+  const VoxelRead c111 = voxel_in(r, p111, b.x, b.y, b.z);
   float r0 = (1.0f - xyz3.x) * c000.sdf + xyz3.x * c100.sdf;
   float r1 = (1.0f - xyz3.x) * c010.sdf + xyz3.x * c110.sdf;
   const float r2 = (1.0f - xyz3.y) * r0 + xyz3.y * r1;
@@ -156,26 +186,54 @@ __device__ __forceinline__ float read_sdf_interp(const RayCtx &r, f3 pt, bool &v
   return (1.0f - xyz3.z) * r2 + xyz3.z * r3;
 }
 
-// Rendering::readNormal (RenderScene.cu:345-378).
-__device__ __forceinline__ bool read_normal(const RayCtx &r, f3 pt, const m3 &Rinv, f3 &n) {
+struct SdfValid {
+  float sdf;
   bool valid;
-  const float s0 = read_sdf_interp(r, pt + mk3(1, 0, 0), valid);
-  if (isnan(s0) || s0 == 1.0f || !valid) return false;
-  const float s1 = read_sdf_interp(r, pt + mk3(-1, 0, 0), valid);
-  if (isnan(s1) || s1 == 1.0f || !valid) return false;
-  const float s2 = read_sdf_interp(r, pt + mk3(0, 1, 0), valid);
-  if (isnan(s2) || s2 == 1.0f || !valid) return false;
-  const float s3 = read_sdf_interp(r, pt + mk3(0, -1, 0), valid);
-  if (isnan(s3) || s3 == 1.0f || !valid) return false;
-  const float s4 = read_sdf_interp(r, pt + mk3(0, 0, 1), valid);
-  if (isnan(s4) || s4 == 1.0f || !valid) return false;
-  const float s5 = read_sdf_interp(r, pt + mk3(0, 0, -1), valid);
-  if (isnan(s5) || s5 == 1.0f || !valid) return false;
-  n = normalised(mul(Rinv, mk3(s0 - s1, s2 - s3, s4 - s5)));
-  return true;
+};
+
+// Out-of-line copy for the marching loop and the surface refinement
+// (arguments by value so the caller's context stays in registers).
+__device__ __noinline__ SdfValid read_sdf_interp(const RayCtx r, f3 pt) {
+  SdfValid o;
+  o.sdf = sdf_interp(r, pt, o.valid);
+  return o;
 }
 
-// Rendering::operator() (RenderScene.cu:380-488).
+struct NormalOut {
+  f3 n;
+  bool ok;
+};
+
+// Rendering::readNormal (RenderScene.cu:345-378).  The six interpolations
+// are independent, so all of them are issued before the reference's checks
+// run in its order (the early returns only decide the output).
+__device__ __noinline__ NormalOut read_normal(const RayCtx r, f3 pt, const m3 Rinv) {
+  NormalOut o;
+  o.ok = false;
+  bool v0, v1, v2, v3, v4, v5;
+  const float s0 = sdf_interp(r, pt + mk3(1, 0, 0), v0);
+  const float s1 = sdf_interp(r, pt + mk3(-1, 0, 0), v1);
+  const float s2 = sdf_interp(r, pt + mk3(0, 1, 0), v2);
+  const float s3 = sdf_interp(r, pt + mk3(0, -1, 0), v3);
+  const float s4 = sdf_interp(r, pt + mk3(0, 0, 1), v4);
+  const float s5 = sdf_interp(r, pt + mk3(0, 0, -1), v5);
+  if (isnan(s0) || s0 == 1.0f || !v0) return o;
+  if (isnan(s1) || s1 == 1.0f || !v1) return o;
+  if (isnan(s2) || s2 == 1.0f || !v2) return o;
+  if (isnan(s3) || s3 == 1.0f || !v3) return o;
+  if (isnan(s4) || s4 == 1.0f || !v4) return o;
+  if (isnan(s5) || s5 == 1.0f || !v5) return o;
+  o.n = normalised(mul(Rinv, mk3(s0 - s1, s2 - s3, s4 - s5)));
+  o.ok = true;
+  return o;
+}
+
+constexpr int kSpec = 4;  // march samples read ahead together
+
+// Rendering::operator() (RenderScene.cu:380-488).  The march reads kSpec
+// samples ahead at once, at the positions a run of 1-voxel steps would
+// reach (the same float additions), then replays the reference's loop over
+// them in order; an 8-voxel step or the end of the range ends the run.
 __global__ void __launch_bounds__(128) k_raycast(DevMap m, FuseScratch f, sf_image vmap, sf_image nmap,
                                                  sf_image zmin, sf_image zmax, const Cam *cam,
                                                  const unsigned *rendered, sf_image fb_v,
@@ -194,9 +252,12 @@ __global__ void __launch_bounds__(128) k_raycast(DevMap m, FuseScratch f, sf_ima
   }
   const Cam c = *cam;
   RayCtx r;
-  r.m = &m;
+  r.voxels = m.voxels;
   r.cells = f.win_cells;
   for (int k = 0; k < 6; ++k) r.win[k] = f.win[k];
+  r.entries = m.entries;
+  r.num_buckets = m.c.num_buckets;
+  r.num_excess = m.c.num_excess;
   float4 vout = nan4(), nout = nan4();
   const int lx = (int)floorf((float)x / 8.0f), ly = (int)floorf((float)y / 8.0f);
   const float zx = __ldg(row_ptr<const float>(zmin, ly) + lx);
@@ -219,33 +280,71 @@ __global__ void __launch_bounds__(128) k_raycast(DevMap m, FuseScratch f, sf_ima
     const f3 block_e = (mul(c.R, p) + c.t) * vsi;
     const f3 dir = normalised(block_e - block_s);
     f3 result = block_s;
-    bool valid_sdf = false, behind = false;
-    float step, prev_sdf;
-    while (dist_s < dist_e) {
-      prev_sdf = sdf;
-      sdf = read_sdf(r, result, valid_sdf);
-      if (!valid_sdf) {
-        step = 8.0f;
-      } else {
-        if (sdf <= 0.1f && sdf >= -0.5f) sdf = read_sdf_interp(r, result, valid_sdf);
-        if (prev_sdf < 0.f && sdf >= 0.f) { behind = true; break; }
-        if (prev_sdf > 0.f && sdf <= 0.f) break;
-        step = 1.0f;
+    bool valid_sdf = false, behind = false, done = false;
+    while (!done && dist_s < dist_e) {
+      f3 pos[kSpec];
+      float ds[kSpec];
+      VoxelRead v[kSpec];
+      pos[0] = result;
+      ds[0] = dist_s;
+#pragma unroll
+      for (int i = 1; i < kSpec; ++i) {
+        pos[i] = pos[i - 1] + 1.0f * dir;
+        ds[i] = ds[i - 1] + 1.0f;
       }
-      result = result + step * dir;
-      dist_s += step;
+#pragma unroll
+      for (int i = 0; i < kSpec; ++i) v[i] = read_voxel(r, pos[i]);
+      bool run = true;  // still on the speculated run of 1-voxel steps
+#pragma unroll
+      for (int i = 0; i < kSpec; ++i) {
+        if (!run) break;
+        if (i > 0 && !(ds[i] < dist_e)) {  // the while condition fails here
+          result = pos[i];
+          dist_s = ds[i];
+          done = true;
+          break;
+        }
+        const float prev_sdf = sdf;
+        sdf = v[i].sdf;
+        valid_sdf = v[i].found && v[i].weight != 0;
+        if (!valid_sdf) {  // 8-voxel step: the run ends
+          result = pos[i] + 8.0f * dir;
+          dist_s = ds[i] + 8.0f;
+          run = false;
+          break;
+        }
+        if (sdf <= 0.1f && sdf >= -0.5f) {
+          const SdfValid sv = read_sdf_interp(r, pos[i]);
+          sdf = sv.sdf;
+          valid_sdf = sv.valid;
+        }
+        if (prev_sdf < 0.f && sdf >= 0.f) {
+          behind = true;
+          done = true;
+          break;
+        }
+        if (prev_sdf > 0.f && sdf <= 0.f) {
+          result = pos[i];
+          done = true;
+          break;
+        }
+        if (i == kSpec - 1) {  // every speculated sample consumed
+          result = pos[i] + 1.0f * dir;
+          dist_s = ds[i] + 1.0f;
+        }
+      }
     }
     if (!behind && sdf <= 0.0f) {
+      float step = sdf * m.c.step_scale;
+      result = result + step * dir;
+      sdf = read_sdf_interp(r, result).sdf;
       step = sdf * m.c.step_scale;
       result = result + step * dir;
-      sdf = read_sdf_interp(r, result, valid_sdf);
-      step = sdf * m.c.step_scale;
-      result = result + step * dir;
-      f3 n;
-      if (read_normal(r, result, c.Rinv, n)) {
+      const NormalOut no = read_normal(r, result, c.Rinv);
+      if (no.ok) {
         const f3 q = mul(c.Rinv, result * m.c.voxel_size - c.t);
         vout = make_float4(q.x, q.y, q.z, 1.0f);
-        nout = make_float4(n.x, n.y, n.z, 1.0f);
+        nout = make_float4(no.n.x, no.n.y, no.n.z, 1.0f);
       }
     }
   }
