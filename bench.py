@@ -62,7 +62,7 @@ class ClockSampler:
         self.lines = []
         try:
             self.p = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
-                                       "-i", str(gpu_index), "-lms", "200"], stdout=subprocess.PIPE,
+                                       "-i", str(gpu_index), "-lms", "20"], stdout=subprocess.PIPE,
                                       stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -270,7 +270,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=280)  # 300 frames with the warm-up, as the workload names
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-plain", action="store_true")
