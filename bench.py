@@ -230,6 +230,57 @@ def omp_threads():
     return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
 
 
+def time_reloc(sf, ctx, frames, n=256, reps=10, seed=5):
+    """RelocScoreBatch on the workload: n candidate poses (the true pose and
+    seeded 5 cm / 5 deg perturbations) scored against one 640x480 frame in one
+    launch, after the sequence's first frames are fused.  Time per call through
+    the C ABI (host poses in, host scores out)."""
+    import ctypes as C
+    s = sf.System(ctx, sys_cfg(sf, 2), init_pose=frames[0][3])
+    for i in range(min(8, len(frames) - 1)):
+        s.grab(frames[i][0], frames[i][1])
+    k = min(8, len(frames) - 1)
+    s.grab(frames[k][0], frames[k][1])
+    vmap, _, _ = s.frame_maps(0)
+    P = np.array(s.stats().pose[:], np.float64).reshape(4, 4)
+    rng = np.random.default_rng(seed)
+    cand = [P]
+    for _ in range(n - 1):
+        w = rng.normal(0, np.deg2rad(5.0), 3)
+        th = np.linalg.norm(w)
+        Kx = np.array([[0, -w[2], w[1]], [w[2], 0, -w[0]], [-w[1], w[0], 0]]) / max(th, 1e-12)
+        Q = P.copy()
+        Q[:3, :3] = (np.eye(3) + np.sin(th) * Kx + (1 - np.cos(th)) * Kx @ Kx) @ P[:3, :3]
+        Q[:3, 3] += rng.normal(0, 0.05, 3)
+        cand.append(Q)
+    poses = np.ascontiguousarray(np.array(cand), np.float64)
+    out = (sf._lib.RelocScore * n)()
+    m = s.map()
+    pp = poses.ctypes.data_as(C.POINTER(C.c_double))
+    sf.call("sf_RelocScoreBatch", ctx.h, m.h, vmap, 1, pp, n, 0.5, out)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        sf.call("sf_RelocScoreBatch", ctx.h, m.h, vmap, 1, pp, n, 0.5, out)
+    ms = (time.perf_counter() - t0) * 1e3 / reps
+    inl = np.array([o.inliers for o in out])
+    s.close()
+    return {"candidates": n, "pixels": int(COLS * ROWS), "ms_per_call": round(ms, 3),
+            "candidate_pixels_per_s": round(n * COLS * ROWS / (ms * 1e-3), 1),
+            "true_pose_rank": int((inl > inl[0]).sum()),
+            "note": "one launch per call; sigma 5 cm / 5 deg candidates around the tracked pose of frame %d" % k}
+
+
+def load_traffic(kernel):
+    """dram__bytes_read.sum + dram__bytes_write.sum of one launch of the kernel
+    on this workload, from the committed ncu summary (null if absent)."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", "roofline_traffic_640x480.json")
+    try:
+        with open(path) as f:
+            return int(json.load(f)["kernels"]["k_" + kernel]["dram_bytes"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
 def algorithmic_bytes(stats_list):
     """Compulsory bytes per frame of the integration and raycast stages
     (per-unit figures in the design doc): integration V*512*32 + 8WH (voxel
@@ -340,8 +391,12 @@ def main():
     out["kernels"] = kern
     out["visible_blocks_mean"] = round(V, 1)
     d = kern[dom]
+    traffic = load_traffic(dom)
     out["roofline"] = {"kernel": dom, "bound": "hbm", "achieved": d["achieved_gbs"], "peak": peak, "unit": "GB/s",
-                       "frac": d["frac_of_%s_hbm" % peak_kind], "peak_source": peak_kind, "traffic": None}
+                       "frac": d["frac_of_%s_hbm" % peak_kind], "peak_source": peak_kind,
+                       "traffic": traffic, "algorithmic_bytes": d["algorithmic_bytes"],
+                       "traffic_source": "profiles/roofline_traffic_640x480.json (ncu dram bytes, one launch)"
+                       if traffic else None}
 
     if not args.no_plain:
         p = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 0, barrier)
@@ -355,6 +410,7 @@ def main():
                   "h2d_bytes_per_step": COLS * ROWS * (2 + 3), "d2h_bytes_per_step": 208,
                   "tracked_frames": int(tracked)}
     out["pose_err_fp64_max"] = pose_error_fp64(sf, ctx, frames, 6)
+    out["reloc"] = time_reloc(sf, ctx, frames)
     if rank == 0 and not args.no_cpu:
         ncpu = 6
         fps_cpu = cpu_reference(frames, ncpu)

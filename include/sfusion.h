@@ -250,6 +250,26 @@ int sf_Raycast(sf_context *ctx, sf_map *map, sf_image vmap, sf_image nmap,
                sf_mat3 RviewInv, sf_float3 tview, float invfx, float invfy,
                float cx, float cy);
 
+/* -------------------------------------------------------- relocalisation */
+/* RelocScoreBatch: scores n candidate poses against one frame in a single
+ * launch (no kernel of the reference corresponds; the reference relocalises
+ * with SURF keypoints outside this loop).  poses: host double[n][16],
+ * camera -> world as Tracker's poses are; vmap: the frame's float4 vertex
+ * map in its camera frame (any pyramid level).  For every stride-th column
+ * and row, a vertex moved into the map by a candidate is sampled with
+ * readSdfInterped (Mapping/RenderScene.cu:310-343); a valid, finite sample
+ * counts in `valid` and, when |sdf| < inlier_sdf (normalised TSDF), in
+ * `inliers`.  sum_abs_sdf is summed in a fixed order (deterministic),
+ * mean_abs_sdf = sum / valid (NaN when valid is 0).  scores_out: host [n].
+ * 1 <= n <= 65536. */
+typedef struct {
+  uint32_t valid, inliers;
+  float sum_abs_sdf, mean_abs_sdf;
+} sf_reloc_score;
+int sf_RelocScoreBatch(sf_context *ctx, sf_map *map, sf_image vmap, int stride,
+                       const double *poses, int n, float inlier_sdf,
+                       sf_reloc_score *scores_out);
+
 /* ------------------------------------------------------- whole frame loop */
 /* System::GrabImage (Core/System.cc:131-270) with Tracker::GrabFrame /
  * Track / ComputeSE3(icpOnly) (Tracking/Tracking.cc:65-173,246-280,369-517),

@@ -27,6 +27,7 @@ VOXEL_DTYPE = np.dtype([("sdf", "<f4"), ("weight", "u1"), ("color", "u1", 3),
                         ("count_2", "u1"), ("color_2", "u1", 3), ("obj_idx", "u1")])
 RBLOCK_DTYPE = np.dtype([("ulx", "<i2"), ("uly", "<i2"), ("lrx", "<i2"), ("lry", "<i2"),
                          ("zmin", "<f4"), ("zmax", "<f4")])
+RELOC_DTYPE = np.dtype([("valid", "<u4"), ("inliers", "<u4"), ("sum_abs_sdf", "<f4"), ("mean_abs_sdf", "<f4")])
 assert ENTRY_DTYPE.itemsize == 32 and VOXEL_DTYPE.itemsize == 16 and RBLOCK_DTYPE.itemsize == 16
 
 
@@ -72,6 +73,7 @@ def lib():
                 "sfo_fuse": (C.c_uint, [vp, F32P, U8P, F32P, U8P, C.c_int, C.c_int, C.c_int, F32P, F32P, F32P] + [C.c_float] * 4),
                 "sfo_zrange": (C.c_int, [vp, F32P, F32P, C.c_int, C.c_int, C.c_float, C.c_float, F32P, F32P]
                                + [C.c_float] * 4 + [vp, C.c_int, C.POINTER(C.c_uint)]),
+                "sfo_reloc_score": (None, [vp, F32P, C.c_int, C.c_int, C.c_int, F32P, C.c_int, C.c_float, vp]),
                 "sfo_raycast": (None, [vp, F32P, F32P, C.c_int, C.c_int, F32P, F32P, C.c_int, C.c_int,
                                        F32P, F32P, F32P] + [C.c_float] * 4),
                 "sfo_system_create": (vp, [C.POINTER(Config), C.c_int, C.c_int, C.c_int, F32P, C.c_float,
@@ -310,6 +312,17 @@ class Map:
                               self.cfg.depth_min, _p(RI, F32P), _p(t, F32P), *map(float, K),
                               blocks.ctypes.data_as(C.c_void_p), max_blocks, C.byref(n))
         return bool(ok), zmin, zmax, blocks[:min(n.value, max_blocks)], n.value
+
+    def reloc_score(self, vmap, stride, poses, inlier_sdf):
+        """RelocScoreBatch: scores of candidate poses (n x 4 x 4, camera -> world)."""
+        vm = _f32(vmap)
+        rows, cols = vm.shape[:2]
+        poses = np.asarray(poses, np.float64).reshape(-1, 4, 4)
+        pf = np.concatenate([poses[:, :3, :3].reshape(-1, 9), poses[:, :3, 3]], axis=1).astype(np.float32)
+        out = np.zeros(len(poses), RELOC_DTYPE)
+        lib().sfo_reloc_score(self.h, _p(vm, F32P), cols, rows, int(stride), _p(np.ascontiguousarray(pf), F32P),
+                              len(poses), float(inlier_sdf), out.ctypes.data_as(C.c_void_p))
+        return out
 
     def raycast(self, P, K, cols, rows, zmin, zmax):
         zmin, zmax = _f32(zmin), _f32(zmax)

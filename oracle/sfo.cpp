@@ -1210,6 +1210,79 @@ extern "C" void sfo_raycast(sfo_map *m, float *vmap, float *nmap, int cols, int 
     }
 }
 
+// RelocScoreBatch of the GB300 loop (no reference kernel; see
+// semantic_icpslam_gb300/csrc/reloc.cu): per candidate, every stride-th
+// vertex moved into the map by (R | t) and read with readSdfInterped
+// (RenderScene.cu:310-343).  The float sums follow the kernel's order:
+// 256 per-thread sums over samples i = t, t + 256, ..., a shuffle-down tree
+// per warp, then over the eight warp sums.  out: n records of
+// {uint32 valid, uint32 inliers, float sum, float mean}.
+extern "C" void sfo_reloc_score(sfo_map *m, const float *vmap, int cols, int rows, int stride,
+                                const float *poses, int n, float inlier_sdf, void *out) {
+  struct Rec { uint32_t valid, inliers; float sum, mean; };
+  Rec *rec = static_cast<Rec *>(out);
+  const int sc = (cols + stride - 1) / stride, sr = (rows + stride - 1) / stride;
+  const int N = sc * sr;
+  const float vsi = m->voxelSizeInv;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int k = 0; k < n; ++k) {
+    const float *P = poses + 12 * (size_t)k;
+    m3 R;
+    R.rx = {P[0], P[1], P[2]};
+    R.ry = {P[3], P[4], P[5]};
+    R.rz = {P[6], P[7], P[8]};
+    const f3 t = {P[9], P[10], P[11]};
+    float tsum[256];
+    uint32_t tvalid[256], tinl[256];
+    for (int th = 0; th < 256; ++th) {
+      float sum = 0.f;
+      uint32_t valid = 0, inl = 0;
+      RayCache cache{{0, 0, 0}, -1, false};
+      for (int i = th; i < N; i += 256) {
+        const int y = (i / sc) * stride, x = (i % sc) * stride;
+        const float *v = vmap + 4 * ((size_t)y * cols + x);
+        if (std::isnan(v[0])) continue;
+        const f3 pt = (mul(R, f3{v[0], v[1], v[2]}) + t) * vsi;
+        bool ok;
+        const float sdf = read_sdf_interp(*m, pt, cache, ok);
+        if (!ok || std::isnan(sdf)) continue;
+        ++valid;
+        const float a = std::fabs(sdf);
+        if (a < inlier_sdf) ++inl;
+        sum += a;
+      }
+      tsum[th] = sum;
+      tvalid[th] = valid;
+      tinl[th] = inl;
+    }
+    float wsum[8];
+    uint32_t wvalid[8], winl[8];
+    for (int w = 0; w < 8; ++w) {
+      float *v = tsum + 32 * w;
+      uint32_t *a = tvalid + 32 * w, *b = tinl + 32 * w;
+      for (int off = 16; off > 0; off >>= 1)
+        for (int l = 0; l < off; ++l) {
+          v[l] = v[l] + v[l + off];
+          a[l] += a[l + off];
+          b[l] += b[l + off];
+        }
+      wsum[w] = v[0];
+      wvalid[w] = a[0];
+      winl[w] = b[0];
+    }
+    for (int off = 4; off > 0; off >>= 1)
+      for (int l = 0; l < off; ++l) {
+        wsum[l] = wsum[l] + wsum[l + off];
+        wvalid[l] += wvalid[l + off];
+        winl[l] += winl[l + off];
+      }
+    rec[k].valid = wvalid[0];
+    rec[k].inliers = winl[0];
+    rec[k].sum = wsum[0];
+    rec[k].mean = wvalid[0] ? wsum[0] / (float)wvalid[0] : std::numeric_limits<float>::quiet_NaN();
+  }
+}
+
 // =============================================================== whole loop
 struct sfo_frame {
   std::vector<float> raw;

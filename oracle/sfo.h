@@ -112,6 +112,8 @@ int sfo_zrange(sfo_map *m, float *zmin, float *zmax, int zc, int zr,
                const float *t, float fx, float fy, float cx, float cy,
                void *blocks_out, int max_blocks, unsigned *nblocks);
 // Raycast (RenderScene.cu:291-537).
+void sfo_reloc_score(sfo_map *m, const float *vmap, int cols, int rows, int stride,
+                     const float *poses, int n, float inlier_sdf, void *out);
 void sfo_raycast(sfo_map *m, float *vmap, float *nmap, int cols, int rows,
                  const float *zmin, const float *zmax, int zc, int zr,
                  const float *R, const float *Rinv, const float *t, float invfx,

@@ -43,6 +43,11 @@ class Image(C.Structure):
     _fields_ = [("data", C.c_void_p), ("step", C.c_size_t), ("cols", C.c_int), ("rows", C.c_int)]
 
 
+class RelocScore(C.Structure):
+    _fields_ = [("valid", C.c_uint32), ("inliers", C.c_uint32), ("sum_abs_sdf", C.c_float),
+                ("mean_abs_sdf", C.c_float)]
+
+
 class MapConfig(C.Structure):
     _fields_ = [("voxel_size", C.c_float), ("trunc_dist", C.c_float), ("depth_min", C.c_float),
                 ("depth_max", C.c_float), ("num_buckets", C.c_uint32), ("num_excess", C.c_uint32),
@@ -112,6 +117,7 @@ SIGNATURES = {
                    F64P, F64P],
     "sf_ICPStep_static": [vp, Image, Image, Image, Image, Mat3, Float3, Mat3, Mat3, Float3, Intrinsics,
                           F32P, F64P, F64P],
+    "sf_RelocScoreBatch": [vp, vp, Image, C.c_int, F64P, C.c_int, C.c_float, C.POINTER(RelocScore)],
     "sf_ComputeSE3": [vp, C.c_int, C.POINTER(Image), C.POINTER(Image), C.POINTER(Image), C.POINTER(Image),
                       Intrinsics, I32P, I32P, C.c_float, F64P, F64P, I32P, F32P],
     "sf_CheckBlockVisibility": [vp, vp, Mat3, Mat3, Float3, C.c_int, C.c_int] + [C.c_float] * 6 + [U32P],

@@ -28,6 +28,9 @@ struct sf_context {
   double *host_sums = nullptr;  // pinned [29]
   double *pose = nullptr;       // device [16]
   TrackCtl *host_ctl = nullptr; // pinned
+  float *reloc_poses = nullptr;           // device [reloc_cap][12]
+  sf_reloc_score *reloc_scores = nullptr; // device [reloc_cap]
+  int reloc_cap = 0;
 };
 
 struct sf_map {
@@ -133,6 +136,8 @@ int sf_context_destroy(sf_context *ctx) {
   if (ctx->host_sums) cudaFreeHost(ctx->host_sums);
   cudaFree(ctx->pose);
   if (ctx->host_ctl) cudaFreeHost(ctx->host_ctl);
+  cudaFree(ctx->reloc_poses);
+  cudaFree(ctx->reloc_scores);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return SF_OK;
@@ -443,6 +448,40 @@ int sf_ComputeSE3(sf_context *ctx, int levels, const sf_image *nv, const sf_imag
     stats_out[3] = c.icpCount;
   }
   if (icp_error_out) *icp_error_out = c.icpError;
+  return SF_OK;
+}
+
+// -------------------------------------------------------- relocalisation
+int sf_RelocScoreBatch(sf_context *ctx, sf_map *m, sf_image vmap, int stride, const double *poses, int n,
+                       float inlier_sdf, sf_reloc_score *scores_out) {
+  if (!ctx || !m || !poses || !scores_out || n < 1 || n > 65536 || stride < 1 || !img_ok(vmap, 16))
+    return SF_ERR_INVALID;
+  if (n > ctx->reloc_cap) {
+    SF_CHECK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(ctx->reloc_poses);
+    cudaFree(ctx->reloc_scores);
+    ctx->reloc_poses = nullptr;
+    ctx->reloc_scores = nullptr;
+    ctx->reloc_cap = 0;
+    SF_CHECK(cudaMalloc(&ctx->reloc_poses, sizeof(float) * 12 * (size_t)n));
+    SF_CHECK(cudaMalloc(&ctx->reloc_scores, sizeof(sf_reloc_score) * (size_t)n));
+    ctx->reloc_cap = n;
+  }
+  // Frame::GpuRotation / GpuTranslation (Core/Frame.cc:626-645) per candidate
+  std::vector<float> hp(12 * (size_t)n);
+  for (int k = 0; k < n; ++k) {
+    const double *P = poses + 16 * (size_t)k;
+    float *q = hp.data() + 12 * (size_t)k;
+    const int src[12] = {0, 1, 2, 4, 5, 6, 8, 9, 10, 3, 7, 11};
+    for (int i = 0; i < 12; ++i) q[i] = (float)P[src[i]];
+  }
+  SF_CHECK(cudaMemcpyAsync(ctx->reloc_poses, hp.data(), sizeof(float) * hp.size(), cudaMemcpyHostToDevice,
+                           ctx->stream));
+  launch_reloc_score(m->d, vmap, stride, ctx->reloc_poses, n, inlier_sdf, ctx->reloc_scores, ctx->stream);
+  SF_CHECK(cudaGetLastError());
+  SF_CHECK(cudaMemcpyAsync(scores_out, ctx->reloc_scores, sizeof(sf_reloc_score) * (size_t)n,
+                           cudaMemcpyDeviceToHost, ctx->stream));
+  SF_CHECK(cudaStreamSynchronize(ctx->stream));
   return SF_OK;
 }
 

@@ -13,6 +13,7 @@
 // voxel (sdf, weight) per sample.
 #include "sf_kernels.cuh"
 #include "sf_render.cuh"
+#include "sf_sample.cuh"
 
 namespace sf {
 
@@ -83,109 +84,6 @@ __global__ void k_fill_blocks(sf_image zmin, sf_image zmax, const sf_rendering_b
 }
 
 // ---------------------------------------------------------------- raycast
-// Block lookup for the ray: the frame's block-pointer window, the hash table
-// (DeviceMap::FindEntry) outside it.  Equal to FindEntry for every block,
-// so the per-ray entry cache of DeviceMap::FindVoxel (DeviceMap.cu:116-133)
-// has nothing left to save and is not kept.  (The reference's cache starts
-// as {pos (0,0,0), ptr -1}, which would alias block (0,0,0) to voxel index
-// -1; that aliasing is not reproduced.)
-struct RayCtx {
-  const sf_voxel *voxels;
-  const int *cells;
-  int win[6];
-  const sf_hash_entry *entries;
-  uint32_t num_buckets, num_excess;
-};
-
-// Hash-table lookup (DeviceMap::FindEntry) for a block outside the window;
-// rare, so kept out of line to keep the inlined sample code small.
-__device__ __noinline__ int block_ptr_hash(const sf_hash_entry *entries, uint32_t num_buckets,
-                                           uint32_t num_excess, int bx, int by, int bz) {
-  DevMap m;
-  m.entries = const_cast<sf_hash_entry *>(entries);
-  m.c.num_buckets = num_buckets;
-  m.c.num_excess = num_excess;
-  i3 p;
-  p.x = bx; p.y = by; p.z = bz;
-  return find_block(m, p);
-}
-
-// Voxel index of block (bx, by, bz), or -1.
-__device__ __forceinline__ int block_ptr(const RayCtx &r, int bx, int by, int bz) {
-  const unsigned x = (unsigned)(bx - r.win[0]), y = (unsigned)(by - r.win[1]), z = (unsigned)(bz - r.win[2]);
-  if (x < (unsigned)r.win[3] && y < (unsigned)r.win[4] && z < (unsigned)r.win[5])
-    return __ldg(r.cells + (int)((z * (unsigned)r.win[4] + y) * (unsigned)r.win[3] + x));
-  return block_ptr_hash(r.entries, r.num_buckets, r.num_excess, bx, by, bz);
-}
-
-struct VoxelRead {
-  float sdf;
-  unsigned weight;
-  bool found;
-};
-
-// Voxel (vx, vy, vz) of the block whose voxel index is ptr (block
-// coordinates are v >> 3, local ones v & 7, as worldPosToVoxelPos /
-// voxelPosToLocalIdx compute them).  A missing block reads as Voxel()
-// (sdf NaN, weight 0) with found = false, as DeviceMap::FindVoxel does.
-__device__ __forceinline__ VoxelRead voxel_in(const RayCtx &r, int ptr, int vx, int vy, int vz) {
-  VoxelRead v;
-  if (ptr < 0) {
-    v.sdf = nanf_bits();
-    v.weight = 0;
-    v.found = false;
-    return v;
-  }
-  const uint2 raw = __ldg((const uint2 *)(r.voxels + ptr + ((vz & 7) * 64 + (vy & 7) * 8 + (vx & 7))));
-  v.sdf = __uint_as_float(raw.x);
-  v.weight = raw.y & 0xffu;
-  v.found = true;
-  return v;
-}
-
-__device__ __forceinline__ VoxelRead read_voxel(const RayCtx &r, f3 pt) {
-  const i3 p = floor3(pt);
-  return voxel_in(r, block_ptr(r, p.x >> 3, p.y >> 3, p.z >> 3), p.x, p.y, p.z);
-}
-
-// Rendering::readSdfInterped (RenderScene.cu:310-343).  The corners are
-// the reference's floor3(pt + offset); per axis that is floor(pt) or
-// floor(pt + 1), so six floors give all eight.  Corners that share a block
-// share one lookup.  `valid` is the last corner's (pt + (1,1,1)), as each
-// FindVoxel call overwrites it in the reference.
-__device__ __forceinline__ float sdf_interp(const RayCtx &r, f3 pt, bool &valid) {
-  const f3 xyz3 = pt - mk3(floorf(pt.x), floorf(pt.y), floorf(pt.z));
-  const i3 a = floor3(pt);
-  const i3 b = floor3(pt + mk3(1, 1, 1));
-  const int ax = a.x >> 3, ay = a.y >> 3, az = a.z >> 3;
-  const int bx = b.x >> 3, by = b.y >> 3, bz = b.z >> 3;
-  const bool sx = ax == bx, sy = ay == by, sz = az == bz;
-  const int p000 = block_ptr(r, ax, ay, az);
-  const int p100 = sx ? p000 : block_ptr(r, bx, ay, az);
-  const int p010 = sy ? p000 : block_ptr(r, ax, by, az);
-  const int p110 = sx ? p010 : (sy ? p100 : block_ptr(r, bx, by, az));
-  const int p001 = sz ? p000 : block_ptr(r, ax, ay, bz);
-  const int p101 = sx ? p001 : (sz ? p100 : block_ptr(r, bx, ay, bz));
-  const int p011 = sy ? p001 : (sz ? p010 : block_ptr(r, ax, by, bz));
-  const int p111 = sx ? p011 : (sy ? p101 : (sz ? p110 : block_ptr(r, bx, by, bz)));
-  const VoxelRead c000 = voxel_in(r, p000, a.x, a.y, a.z);
-  const VoxelRead c100 = voxel_in(r, p100, b.x, a.y, a.z);
-  const VoxelRead c010 = voxel_in(r, p010, a.x, b.y, a.z);
-  const VoxelRead c110 = voxel_in(r, p110, b.x, b.y, a.z);
-  const VoxelRead c001 = voxel_in(r, p001, a.x, a.y, b.z);
-  const VoxelRead c101 = voxel_in(r, p101, b.x, a.y, b.z);
-  const VoxelRead c011 = voxel_in(r, p011, a.x, b.y, b.z);
-  const VoxelRead c111 = voxel_in(r, p111, b.x, b.y, b.z);
-  float r0 = (1.0f - xyz3.x) * c000.sdf + xyz3.x * c100.sdf;
-  float r1 = (1.0f - xyz3.x) * c010.sdf + xyz3.x * c110.sdf;
-  const float r2 = (1.0f - xyz3.y) * r0 + xyz3.y * r1;
-  r0 = (1.0f - xyz3.x) * c001.sdf + xyz3.x * c101.sdf;
-  r1 = (1.0f - xyz3.x) * c011.sdf + xyz3.x * c111.sdf;
-  const float r3 = (1.0f - xyz3.y) * r0 + xyz3.y * r1;
-  valid = c111.found;
-  return (1.0f - xyz3.z) * r2 + xyz3.z * r3;
-}
-
 struct SdfValid {
   float sdf;
   bool valid;

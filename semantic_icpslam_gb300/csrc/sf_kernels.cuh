@@ -120,6 +120,11 @@ void launch_raycast(const DevMap &m, const FuseScratch &f, const sf_image &vmap,
 // per-frame path builds it inside launch_visibility).
 void launch_window_build(const DevMap &m, const FuseScratch &f, const Cam *c, cudaStream_t s);
 
+// ------------------------------------------------------ relocalisation
+// n candidate poses (float rows R | t, 12 per pose) scored in one launch.
+void launch_reloc_score(const DevMap &m, const sf_image &vmap, int stride, const float *poses, int n,
+                        float inlier_sdf, sf_reloc_score *out, cudaStream_t s);
+
 // Converts host map config into device constants (DeviceMap.h:166-189).
 MapConst make_map_const(const sf_map_config &cfg);
 
