@@ -250,6 +250,25 @@ int sf_Raycast(sf_context *ctx, sf_map *map, sf_image vmap, sf_image nmap,
                sf_mat3 RviewInv, sf_float3 tview, float invfx, float invfy,
                float cx, float cy);
 
+/* RaycastAdjoint: gradient of sf_Raycast's outputs (same map, z-range,
+ * pose and intrinsics) with respect to the camera pose and the TSDF values
+ * the rendering read.  No kernel of the reference corresponds; the raycast
+ * it differentiates is Rendering::operator() (RenderScene.cu:380-488).
+ * grad_vmap / grad_nmap: float4 images of dL/d(vertex) and dL/d(normal)
+ * (w ignored, NaN treated as 0; grad_nmap.data may be NULL).  Each ray is
+ * marched again and its discrete outcome held fixed; the gradient flows
+ * through the two refinement steps, the normal's six interpolations and
+ * the ray's ends and direction.  grad_pose_out (host double[6]): dL/dxi for
+ * T(xi) = exp(xi) T, T = [Rview | tview] camera -> world, xi = (rho, omega)
+ * translation first, summed over pixels in a fixed order.  grad_sdf
+ * (device, may be NULL): one float per voxel index (heap block * 512 +
+ * local), ADDED to (float atomics, so the order of additions varies). */
+int sf_RaycastAdjoint(sf_context *ctx, sf_map *map, sf_image zrange_min,
+                      sf_image zrange_max, sf_mat3 Rview, sf_mat3 RviewInv,
+                      sf_float3 tview, float invfx, float invfy, float cx,
+                      float cy, sf_image grad_vmap, sf_image grad_nmap,
+                      float *grad_sdf, double grad_pose_out[6]);
+
 /* -------------------------------------------------------- relocalisation */
 /* RelocScoreBatch: scores n candidate poses against one frame in a single
  * launch (no kernel of the reference corresponds; the reference relocalises

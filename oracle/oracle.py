@@ -74,6 +74,9 @@ def lib():
                 "sfo_zrange": (C.c_int, [vp, F32P, F32P, C.c_int, C.c_int, C.c_float, C.c_float, F32P, F32P]
                                + [C.c_float] * 4 + [vp, C.c_int, C.POINTER(C.c_uint)]),
                 "sfo_reloc_score": (None, [vp, F32P, C.c_int, C.c_int, C.c_int, F32P, C.c_int, C.c_float, vp]),
+                "sfo_raycast_smooth_f64": (C.c_double, [vp, F32P, F32P, C.c_int, C.c_int, F32P, F32P, C.c_int,
+                                                        C.c_int, F64P, C.c_float, C.c_float, C.c_float, C.c_float,
+                                                        F64P, C.c_longlong, C.c_double]),
                 "sfo_raycast": (None, [vp, F32P, F32P, C.c_int, C.c_int, F32P, F32P, C.c_int, C.c_int,
                                        F32P, F32P, F32P] + [C.c_float] * 4),
                 "sfo_system_create": (vp, [C.POINTER(Config), C.c_int, C.c_int, C.c_int, F32P, C.c_float,
@@ -323,6 +326,23 @@ class Map:
         lib().sfo_reloc_score(self.h, _p(vm, F32P), cols, rows, int(stride), _p(np.ascontiguousarray(pf), F32P),
                               len(poses), float(inlier_sdf), out.ctypes.data_as(C.c_void_p))
         return out
+
+    def raycast_smooth_f64(self, P, K, zmin, zmax, gv, gn, xi=(0, 0, 0, 0, 0, 0), vox=-1, delta=0.0):
+        """FP64 reference of RaycastAdjoint: sum(gv . v + gn . n) at exp(xi) P with voxel `vox` moved by delta,
+        the march's decisions fixed by the float march at P."""
+        zmin, zmax = _f32(zmin), _f32(zmax)
+        zr, zc = zmin.shape
+        gv = _f32(gv)
+        rows, cols = gv.shape[:2]
+        fx, fy, cx, cy = map(float, K)
+        invfx = np.float32(1.0 / np.float64(np.float32(fx)))
+        invfy = np.float32(1.0 / np.float64(np.float32(fy)))
+        T = np.ascontiguousarray(P, np.float64)
+        x = np.ascontiguousarray(xi, np.float64)
+        gnp = _p(_f32(gn), F32P) if gn is not None else None
+        return lib().sfo_raycast_smooth_f64(self.h, _p(gv, F32P), gnp, cols, rows, _p(zmin, F32P), _p(zmax, F32P),
+                                            zc, zr, _p(T, F64P), float(invfx), float(invfy), cx, cy, _p(x, F64P),
+                                            int(vox), float(delta))
 
     def raycast(self, P, K, cols, rows, zmin, zmax):
         zmin, zmax = _f32(zmin), _f32(zmax)

@@ -1283,6 +1283,182 @@ extern "C" void sfo_reloc_score(sfo_map *m, const float *vmap, int cols, int row
   }
 }
 
+// RaycastAdjoint's FP64 reference (test infrastructure).  For every pixel
+// the float march of sfo_raycast (same samples, same decisions) fixes where
+// the surface lies, and the float forward fixes the interpolation cells
+// (and the raw sample's voxel), as the adjoint holds them; the smooth rest
+// of the raycast is then evaluated in double from the map's float values,
+// for the pose exp(xi) T (xi = (rho, omega), translation first) and with
+// voxel index `vox` moved by `delta`:
+//   p0 = bs + S_res dir, sample = bs + S_smp dir, sdf_c = interp(sample) or
+//   the sample's voxel, p1 = p0 + ss sdf_c dir, p2 = p1 + ss interp(p1) dir,
+//   v = R^T (p2 voxel - t), n = normalised(R^T g) (g from the six
+//   interpolations at p2 +- e).
+// Returns L = sum over rendered pixels of gv . v + gn . n, whose central
+// differences in xi and in delta check the GPU adjoint.
+namespace {
+inline d3 dd(f3 a) { return {a.x, a.y, a.z}; }
+inline d3 operator*(d3 a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+inline d3 dmul(const double *R, d3 a) {  // R row-major 3x3 in a 4x4
+  return {R[0] * a.x + R[1] * a.y + R[2] * a.z, R[4] * a.x + R[5] * a.y + R[6] * a.z,
+          R[8] * a.x + R[9] * a.y + R[10] * a.z};
+}
+inline d3 dmulT(const double *R, d3 a) {
+  return {R[0] * a.x + R[4] * a.y + R[8] * a.z, R[1] * a.x + R[5] * a.y + R[9] * a.z,
+          R[2] * a.x + R[6] * a.y + R[10] * a.z};
+}
+inline double voxel_f64(const sfo_map &m, int vx, int vy, int vz, long long vox, double delta, bool &found) {
+  i3 p{vx, vy, vz};
+  const sfo_entry *e = find_entry(m, vox2block(p));
+  if (!e) { found = false; return std::numeric_limits<double>::quiet_NaN(); }
+  found = true;
+  const long long idx = (long long)e->ptr + vox2local(p);
+  return (double)m.voxels[idx].sdf + (idx == vox ? delta : 0.0);
+}
+// Trilinear interpolation over the cell with corner `base` (fixed by the
+// float march), extended linearly when pt leaves the cell.
+inline double interp_f64(const sfo_map &m, d3 pt, i3 base, long long vox, double delta, bool &valid) {
+  const d3 f = {pt.x - base.x, pt.y - base.y, pt.z - base.z};
+  const int ax = base.x, ay = base.y, az = base.z;
+  double c[8];
+  bool found = true;
+  for (int k = 0; k < 8; ++k)
+    c[k] = voxel_f64(m, ax + (k & 1), ay + ((k >> 1) & 1), az + ((k >> 2) & 1), vox, delta, found);
+  valid = found;
+  const double r0 = (1 - f.x) * c[0] + f.x * c[1], r1 = (1 - f.x) * c[2] + f.x * c[3];
+  const double r2 = (1 - f.y) * r0 + f.y * r1;
+  const double q0 = (1 - f.x) * c[4] + f.x * c[5], q1 = (1 - f.x) * c[6] + f.x * c[7];
+  const double r3 = (1 - f.y) * q0 + f.y * q1;
+  return (1 - f.z) * r2 + f.z * r3;
+}
+}  // namespace
+
+extern "C" double sfo_raycast_smooth_f64(sfo_map *m, const float *gv, const float *gn, int cols, int rows,
+                                         const float *zmin, const float *zmax, int zc, int zr,
+                                         const double *T, float invfx, float invfy, float cx, float cy,
+                                         const double *xi, long long vox, double delta) {
+  (void)zr;
+  // the float pose of the march (Frame::GpuRotation / GpuInvRotation / GpuTranslation)
+  m3 Rv, RI;
+  Rv.rx = {(float)T[0], (float)T[1], (float)T[2]};
+  Rv.ry = {(float)T[4], (float)T[5], (float)T[6]};
+  Rv.rz = {(float)T[8], (float)T[9], (float)T[10]};
+  RI.rx = {(float)T[0], (float)T[4], (float)T[8]};
+  RI.ry = {(float)T[1], (float)T[5], (float)T[9]};
+  RI.rz = {(float)T[2], (float)T[6], (float)T[10]};
+  const f3 tv = {(float)T[3], (float)T[7], (float)T[11]};
+  // the perturbed FP64 pose
+  double E[16], Tx[16];
+  sfo_se3_exp(xi, E);
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) {
+      double a = 0;
+      for (int k = 0; k < 4; ++k) a += E[i * 4 + k] * T[k * 4 + j];
+      Tx[i * 4 + j] = a;
+    }
+  const d3 tx = {Tx[3], Tx[7], Tx[11]};
+  const float vsi = m->voxelSizeInv;
+  const double vs = m->c.voxel_size, ss = m->stepScale;
+  double L = 0.0;
+#pragma omp parallel for schedule(dynamic, 4) reduction(+ : L)
+  for (int y = 0; y < rows; ++y)
+    for (int x = 0; x < cols; ++x) {
+      const float *g1 = gv + 4 * ((size_t)y * cols + x);
+      const float *g2 = gn ? gn + 4 * ((size_t)y * cols + x) : nullptr;
+      int lx = f2i(std::floor((float)x / 8.0f)), ly = f2i(std::floor((float)y / 8.0f));
+      float zx = zmin[ly * zc + lx], zy = zmax[ly * zc + lx];
+      if ((double)zy < 1e-3 || (double)zx < 1e-3 || std::isnan(zx) || std::isnan(zy)) continue;
+      // the float march (sfo_raycast's loop, with the positions recorded)
+      float sdf = 1.0f;
+      f3 p;
+      p.z = zx;
+      p.x = p.z * ((float)x - cx) * invfx;
+      p.y = p.z * ((float)y - cy) * invfy;
+      float dist_s = norm(p) * vsi;
+      const float dist0 = dist_s;
+      const f3 pcs = p;
+      f3 block_s = (mul(Rv, p) + tv) * vsi;
+      p.z = zy;
+      p.x = p.z * ((float)x - cx) * invfx;
+      p.y = p.z * ((float)y - cy) * invfy;
+      float dist_e = norm(p) * vsi;
+      const f3 pce = p;
+      f3 block_e = (mul(Rv, p) + tv) * vsi;
+      f3 dir = normalised(block_e - block_s);
+      f3 result = block_s;
+      bool valid_sdf = false, behind = false, interp = false;
+      float step, prev_sdf, s_smp = 0.f, s_res = 0.f;
+      f3 sample_pos = result;
+      RayCache cache{{0, 0, 0}, -1, false};
+      while (dist_s < dist_e) {
+        prev_sdf = sdf;
+        sdf = read_sdf(*m, result, cache, valid_sdf);
+        s_smp = dist_s - dist0;
+        sample_pos = result;
+        interp = false;
+        if (!valid_sdf) {
+          step = 8.0f;
+        } else {
+          if (sdf <= 0.1f && sdf >= -0.5f) {
+            sdf = read_sdf_interp(*m, result, cache, valid_sdf);
+            interp = true;
+          }
+          if (prev_sdf < 0.f && sdf >= 0.f) { behind = true; break; }
+          if (prev_sdf > 0.f && sdf <= 0.f) break;
+          step = 1.0f;
+        }
+        result = result + step * dir;
+        dist_s += step;
+      }
+      s_res = dist_s - dist0;
+      if (behind || !(sdf <= 0.0f)) continue;
+      // the float forward: its validity (sfo_raycast) and the cells it read
+      i3 cell_smp, cell_p1, cell_n[6];
+      {
+        f3 r1 = result + (sdf * m->stepScale) * dir;
+        float s1 = read_sdf_interp(*m, r1, cache, valid_sdf);
+        f3 r2 = r1 + (s1 * m->stepScale) * dir;
+        f3 n;
+        if (!read_normal(*m, r2, cache, RI, n)) continue;
+        cell_smp = floor3(sample_pos);
+        cell_p1 = floor3(r1);
+        const f3 offs[6] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+        for (int k = 0; k < 6; ++k) cell_n[k] = floor3(r2 + offs[k]);
+      }
+      // the smooth part in double at exp(xi) T
+      const d3 ws = dmul(Tx, dd(pcs)) + tx, we = dmul(Tx, dd(pce)) + tx;
+      const d3 bs = ws * (double)vsi, be = we * (double)vsi;
+      const d3 dv = be - bs;
+      const d3 dr = dv * (1.0 / std::sqrt(ddot(dv, dv)));
+      const d3 p0 = bs + dr * (double)s_res, smp = bs + dr * (double)s_smp;
+      bool ok;
+      double sc;
+      if (interp) {
+        sc = interp_f64(*m, smp, cell_smp, vox, delta, ok);
+      } else {
+        sc = voxel_f64(*m, cell_smp.x, cell_smp.y, cell_smp.z, vox, delta, ok);
+      }
+      const d3 q1 = p0 + dr * (ss * sc);
+      const double s1 = interp_f64(*m, q1, cell_p1, vox, delta, ok);
+      const d3 q2 = q1 + dr * (ss * s1);
+      const d3 v = dmulT(Tx, q2 * vs - tx);
+      double Lp = g1[0] * v.x + g1[1] * v.y + g1[2] * v.z;
+      if (g2) {
+        const d3 e[6] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+        double sv[6];
+        for (int k = 0; k < 6; ++k) sv[k] = interp_f64(*m, q2 + e[k], cell_n[k], vox, delta, ok);
+        const d3 gr = {sv[0] - sv[1], sv[2] - sv[3], sv[4] - sv[5]};
+        const d3 u = dmulT(Tx, gr);
+        const d3 n = u * (1.0 / std::sqrt(ddot(u, u)));
+        Lp += g2[0] * n.x + g2[1] * n.y + g2[2] * n.z;
+      }
+      // a pixel whose double evaluation reaches an unobserved voxel (NaN
+      // sdf) where the float one did not is left out
+      if (std::isfinite(Lp)) L += Lp;
+    }
+  return L;
+}
+
 // =============================================================== whole loop
 struct sfo_frame {
   std::vector<float> raw;

@@ -114,6 +114,10 @@ int sfo_zrange(sfo_map *m, float *zmin, float *zmax, int zc, int zr,
 // Raycast (RenderScene.cu:291-537).
 void sfo_reloc_score(sfo_map *m, const float *vmap, int cols, int rows, int stride,
                      const float *poses, int n, float inlier_sdf, void *out);
+double sfo_raycast_smooth_f64(sfo_map *m, const float *gv, const float *gn, int cols, int rows,
+                              const float *zmin, const float *zmax, int zc, int zr, const double *T,
+                              float invfx, float invfy, float cx, float cy, const double *xi,
+                              long long vox, double delta);
 void sfo_raycast(sfo_map *m, float *vmap, float *nmap, int cols, int rows,
                  const float *zmin, const float *zmax, int zc, int zr,
                  const float *R, const float *Rinv, const float *t, float invfx,

@@ -31,6 +31,9 @@ struct sf_context {
   float *reloc_poses = nullptr;           // device [reloc_cap][12]
   sf_reloc_score *reloc_scores = nullptr; // device [reloc_cap]
   int reloc_cap = 0;
+  float *adj_part = nullptr;              // device [adj_cap][6] pose partials
+  double *adj_pose = nullptr;             // device [6]
+  int adj_cap = 0;
 };
 
 struct sf_map {
@@ -138,6 +141,8 @@ int sf_context_destroy(sf_context *ctx) {
   if (ctx->host_ctl) cudaFreeHost(ctx->host_ctl);
   cudaFree(ctx->reloc_poses);
   cudaFree(ctx->reloc_scores);
+  cudaFree(ctx->adj_part);
+  cudaFree(ctx->adj_pose);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return SF_OK;
@@ -590,6 +595,41 @@ int sf_Raycast(sf_context *ctx, sf_map *m, sf_image vmap, sf_image nmap, sf_imag
   launch_raycast(m->d, m->scratch, vmap, nmap, zmin, zmax, ctx->cam, nullptr, nullptr, nullptr, nullptr,
                  ctx->stream);
   SF_CHECK(cudaGetLastError());
+  return SF_OK;
+}
+
+int sf_RaycastAdjoint(sf_context *ctx, sf_map *m, sf_image zmin, sf_image zmax, sf_mat3 Rview,
+                      sf_mat3 RviewInv, sf_float3 tview, float invfx, float invfy, float cx, float cy,
+                      sf_image grad_vmap, sf_image grad_nmap, float *grad_sdf, double grad_pose_out[6]) {
+  if (!ctx || !m || !grad_pose_out || !img_ok(grad_vmap, 16) || !img_ok(zmin, 4) || !img_ok(zmax, 4))
+    return SF_ERR_INVALID;
+  if (grad_nmap.data && (!img_ok(grad_nmap, 16) || grad_nmap.cols != grad_vmap.cols ||
+                         grad_nmap.rows != grad_vmap.rows))
+    return SF_ERR_INVALID;
+  Cam c = make_cam(Rview, RviewInv, tview, 1.0f, 1.0f, cx, cy, grad_vmap.cols, grad_vmap.rows,
+                   m->cfg.depth_min, m->cfg.depth_max);
+  c.invfx = invfx;
+  c.invfy = invfy;
+  int st = upload_cam(ctx, c);
+  if (st) return st;
+  if ((st = ensure_scratch(m, grad_vmap.cols * grad_vmap.rows))) return st;
+  const int nb = raycast_adjoint_blocks(grad_vmap.cols, grad_vmap.rows);
+  if (nb > ctx->adj_cap) {
+    SF_CHECK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(ctx->adj_part);
+    ctx->adj_part = nullptr;
+    ctx->adj_cap = 0;
+    SF_CHECK(cudaMalloc(&ctx->adj_part, sizeof(float) * 6 * (size_t)nb));
+    ctx->adj_cap = nb;
+  }
+  if (!ctx->adj_pose) SF_CHECK(cudaMalloc(&ctx->adj_pose, sizeof(double) * 6));
+  launch_window_build(m->d, m->scratch, ctx->cam, ctx->stream);
+  launch_raycast_adjoint(m->d, m->scratch, zmin, zmax, ctx->cam, grad_vmap, grad_nmap, grad_sdf, ctx->adj_part,
+                         ctx->adj_pose, ctx->stream);
+  SF_CHECK(cudaGetLastError());
+  SF_CHECK(cudaMemcpyAsync(grad_pose_out, ctx->adj_pose, sizeof(double) * 6, cudaMemcpyDeviceToHost,
+                           ctx->stream));
+  SF_CHECK(cudaStreamSynchronize(ctx->stream));
   return SF_OK;
 }
 

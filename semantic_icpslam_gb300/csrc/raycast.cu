@@ -128,6 +128,118 @@ __device__ __noinline__ NormalOut read_normal(const RayCtx r, f3 pt, const m3 Ri
 
 constexpr int kSpec = 4;  // march samples read ahead together
 
+// One ray's march, Rendering::operator() (RenderScene.cu:395-447): the
+// ray from the z-range's near to far point, 8-voxel steps through empty or
+// unobserved space, 1-voxel steps in observed voxels, readSdfInterped near
+// the surface, and the stop at a sign change.  The march reads kSpec
+// samples ahead at once, at the positions a run of 1-voxel steps would
+// reach (the same float additions), then replays the loop over them in
+// order; an 8-voxel step or the end of the range ends the run.  Besides the
+// reference's state it records, for the adjoint, how far along the ray the
+// final position and the sample that gave the final sdf lie.
+struct MarchState {
+  f3 block_s, block_e, dir;  // ray ends and direction (voxel units)
+  f3 ps, pe;                 // the same ends in the world frame (metres)
+  f3 result;                 // final position
+  float sdf;                 // final sdf
+  f3 sample;                 // position of the sample that gave sdf
+  float s_result, s_sample;  // distances of result and of sdf's sample from block_s
+  bool interp;               // sdf came from readSdfInterped
+  bool behind;
+};
+
+__device__ __forceinline__ void march_ray(const RayCtx &r, const Cam &c, float vsi, int x, int y, float zx,
+                                          float zy, MarchState &ms) {
+  float sdf = 1.0f;
+  f3 p;
+  p.z = zx;
+  p.x = p.z * ((float)x - c.cx) * c.invfx;
+  p.y = p.z * ((float)y - c.cy) * c.invfy;
+  float dist_s = norm(p) * vsi;
+  const float dist0 = dist_s;
+  ms.ps = mul(c.R, p) + c.t;
+  const f3 block_s = ms.ps * vsi;
+  p.z = zy;
+  p.x = p.z * ((float)x - c.cx) * c.invfx;
+  p.y = p.z * ((float)y - c.cy) * c.invfy;
+  const float dist_e = norm(p) * vsi;
+  ms.pe = mul(c.R, p) + c.t;
+  const f3 block_e = ms.pe * vsi;
+  const f3 dir = normalised(block_e - block_s);
+  f3 result = block_s;
+  bool valid_sdf = false, behind = false, done = false, interp = false;
+  float s_sample = 0.f;
+  f3 sample = block_s;
+  while (!done && dist_s < dist_e) {
+    f3 pos[kSpec];
+    float ds[kSpec];
+    VoxelRead v[kSpec];
+    pos[0] = result;
+    ds[0] = dist_s;
+#pragma unroll
+    for (int i = 1; i < kSpec; ++i) {
+      pos[i] = pos[i - 1] + 1.0f * dir;
+      ds[i] = ds[i - 1] + 1.0f;
+    }
+#pragma unroll
+    for (int i = 0; i < kSpec; ++i) v[i] = read_voxel(r, pos[i]);
+    bool run = true;  // still on the speculated run of 1-voxel steps
+#pragma unroll
+    for (int i = 0; i < kSpec; ++i) {
+      if (!run) break;
+      if (i > 0 && !(ds[i] < dist_e)) {  // the while condition fails here
+        result = pos[i];
+        dist_s = ds[i];
+        done = true;
+        break;
+      }
+      const float prev_sdf = sdf;
+      sdf = v[i].sdf;
+      s_sample = ds[i] - dist0;
+      sample = pos[i];
+      interp = false;
+      valid_sdf = v[i].found && v[i].weight != 0;
+      if (!valid_sdf) {  // 8-voxel step: the run ends
+        result = pos[i] + 8.0f * dir;
+        dist_s = ds[i] + 8.0f;
+        run = false;
+        break;
+      }
+      if (sdf <= 0.1f && sdf >= -0.5f) {
+        const SdfValid sv = read_sdf_interp(r, pos[i]);
+        sdf = sv.sdf;
+        valid_sdf = sv.valid;
+        interp = true;
+      }
+      if (prev_sdf < 0.f && sdf >= 0.f) {
+        behind = true;
+        done = true;
+        break;
+      }
+      if (prev_sdf > 0.f && sdf <= 0.f) {
+        result = pos[i];
+        dist_s = ds[i];
+        done = true;
+        break;
+      }
+      if (i == kSpec - 1) {  // every speculated sample consumed
+        result = pos[i] + 1.0f * dir;
+        dist_s = ds[i] + 1.0f;
+      }
+    }
+  }
+  ms.block_s = block_s;
+  ms.block_e = block_e;
+  ms.dir = dir;
+  ms.result = result;
+  ms.sdf = sdf;
+  ms.s_result = dist_s - dist0;
+  ms.s_sample = s_sample;
+  ms.sample = sample;
+  ms.interp = interp;
+  ms.behind = behind;
+}
+
 // Rendering::operator() (RenderScene.cu:380-488).  The march reads kSpec
 // samples ahead at once, at the positions a run of 1-voxel steps would
 // reach (the same float additions), then replays the reference's loop over
@@ -163,75 +275,12 @@ __global__ void __launch_bounds__(128) k_raycast(DevMap m, FuseScratch f, sf_ima
   // (double)z < 1e-3 of the reference: no float lies in [1e-3, 0.001f), so
   // for a float z that is exactly z < 0.001f
   if (!(zy < 0.001f || zx < 0.001f || isnan(zx) || isnan(zy))) {
-    const float vsi = m.c.voxel_size_inv;
-    float sdf = 1.0f;
-    f3 p;
-    p.z = zx;
-    p.x = p.z * ((float)x - c.cx) * c.invfx;
-    p.y = p.z * ((float)y - c.cy) * c.invfy;
-    float dist_s = norm(p) * vsi;
-    const f3 block_s = (mul(c.R, p) + c.t) * vsi;
-    p.z = zy;
-    p.x = p.z * ((float)x - c.cx) * c.invfx;
-    p.y = p.z * ((float)y - c.cy) * c.invfy;
-    const float dist_e = norm(p) * vsi;
-    const f3 block_e = (mul(c.R, p) + c.t) * vsi;
-    const f3 dir = normalised(block_e - block_s);
-    f3 result = block_s;
-    bool valid_sdf = false, behind = false, done = false;
-    while (!done && dist_s < dist_e) {
-      f3 pos[kSpec];
-      float ds[kSpec];
-      VoxelRead v[kSpec];
-      pos[0] = result;
-      ds[0] = dist_s;
-#pragma unroll
-      for (int i = 1; i < kSpec; ++i) {
-        pos[i] = pos[i - 1] + 1.0f * dir;
-        ds[i] = ds[i - 1] + 1.0f;
-      }
-#pragma unroll
-      for (int i = 0; i < kSpec; ++i) v[i] = read_voxel(r, pos[i]);
-      bool run = true;  // still on the speculated run of 1-voxel steps
-#pragma unroll
-      for (int i = 0; i < kSpec; ++i) {
-        if (!run) break;
-        if (i > 0 && !(ds[i] < dist_e)) {  // the while condition fails here
-          result = pos[i];
-          dist_s = ds[i];
-          done = true;
-          break;
-        }
-        const float prev_sdf = sdf;
-        sdf = v[i].sdf;
-        valid_sdf = v[i].found && v[i].weight != 0;
-        if (!valid_sdf) {  // 8-voxel step: the run ends
-          result = pos[i] + 8.0f * dir;
-          dist_s = ds[i] + 8.0f;
-          run = false;
-          break;
-        }
-        if (sdf <= 0.1f && sdf >= -0.5f) {
-          const SdfValid sv = read_sdf_interp(r, pos[i]);
-          sdf = sv.sdf;
-          valid_sdf = sv.valid;
-        }
-        if (prev_sdf < 0.f && sdf >= 0.f) {
-          behind = true;
-          done = true;
-          break;
-        }
-        if (prev_sdf > 0.f && sdf <= 0.f) {
-          result = pos[i];
-          done = true;
-          break;
-        }
-        if (i == kSpec - 1) {  // every speculated sample consumed
-          result = pos[i] + 1.0f * dir;
-          dist_s = ds[i] + 1.0f;
-        }
-      }
-    }
+    MarchState ms;
+    march_ray(r, c, m.c.voxel_size_inv, x, y, zx, zy, ms);
+    f3 result = ms.result;
+    const f3 dir = ms.dir;
+    float sdf = ms.sdf;
+    const bool behind = ms.behind;
     if (!behind && sdf <= 0.0f) {
       float step = sdf * m.c.step_scale;
       result = result + step * dir;
@@ -248,6 +297,159 @@ __global__ void __launch_bounds__(128) k_raycast(DevMap m, FuseScratch f, sf_ima
   }
   row_ptr<float4>(vmap, y)[x] = vout;
   row_ptr<float4>(nmap, y)[x] = nout;
+}
+
+// RaycastAdjoint: gradient of the raycast's vertex and normal maps with
+// respect to the camera pose and the TSDF values the rendering read.  Each
+// ray is marched again with march_ray (the same samples and decisions), so
+// nothing is stored between the forward and backward passes.  The march's
+// outcome (where the sign change lies, which samples were interpolated) is
+// piecewise constant and held fixed; the gradient flows through
+//   p1 = p0 + ss * sdf_c * dir,  p2 = p1 + ss * interp(p1) * dir,
+//   v = R^T (p2 * voxel - t),  n = normalised(R^T g),
+//   g = (s(p2+x) - s(p2-x), s(p2+y) - s(p2-y), s(p2+z) - s(p2-z)),
+// the ray's ends (world points R p + t) and its direction.  The pose is
+// perturbed on the left, T(xi) = exp(xi) T, with xi = (rho, omega) in
+// Sophus's order (translation first).  TSDF gradients are added into
+// grad_sdf at the voxel index (ptr + local) with atomics; the pose gradient
+// is summed per CTA in a fixed order into pose_part.
+__global__ void __launch_bounds__(128) k_raycast_adjoint(DevMap m, FuseScratch f, sf_image zmin,
+                                                         sf_image zmax, const Cam *cam, sf_image gv_img,
+                                                         sf_image gn_img, float *grad_sdf, float *pose_part) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  float gp[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if (x < gv_img.cols && y < gv_img.rows) {
+    const float4 gv4 = __ldg(row_ptr<const float4>(gv_img, y) + x);
+    const float4 gn4 = gn_img.data ? __ldg(row_ptr<const float4>(gn_img, y) + x) : make_float4(0.f, 0.f, 0.f, 0.f);
+    f3 gv = xyz(gv4), gn = xyz(gn4);
+    if (isnan(gv.x) || isnan(gv.y) || isnan(gv.z)) gv = mk3(0.f, 0.f, 0.f);
+    if (isnan(gn.x) || isnan(gn.y) || isnan(gn.z)) gn = mk3(0.f, 0.f, 0.f);
+    const Cam c = *cam;
+    const int lx = (int)floorf((float)x / 8.0f), ly = (int)floorf((float)y / 8.0f);
+    const float zx = __ldg(row_ptr<const float>(zmin, ly) + lx);
+    const float zy = __ldg(row_ptr<const float>(zmax, ly) + lx);
+    const bool any = gv.x != 0.f || gv.y != 0.f || gv.z != 0.f || gn.x != 0.f || gn.y != 0.f || gn.z != 0.f;
+    if (any && !(zy < 0.001f || zx < 0.001f || isnan(zx) || isnan(zy))) {
+      RayCtx r;
+      r.voxels = m.voxels;
+      r.cells = f.win_cells;
+      for (int k = 0; k < 6; ++k) r.win[k] = f.win[k];
+      r.entries = m.entries;
+      r.num_buckets = m.c.num_buckets;
+      r.num_excess = m.c.num_excess;
+      MarchState ms;
+      march_ray(r, c, m.c.voxel_size_inv, x, y, zx, zy, ms);
+      if (!ms.behind && ms.sdf <= 0.0f) {
+        const float ss = m.c.step_scale, vs = m.c.voxel_size;
+        const f3 dir = ms.dir;
+        const f3 p1 = ms.result + (ms.sdf * ss) * dir;
+        const float s1 = read_sdf_interp(r, p1).sdf;
+        const f3 p2 = p1 + (s1 * ss) * dir;
+        const f3 ex = mk3(1, 0, 0), ey = mk3(0, 1, 0), ez = mk3(0, 0, 1);
+        bool v0, v1, v2, v3, v4, v5;
+        const float n0 = sdf_interp(r, p2 + ex, v0), n1 = sdf_interp(r, p2 + mk3(-1, 0, 0), v1);
+        const float n2 = sdf_interp(r, p2 + ey, v2), n3 = sdf_interp(r, p2 + mk3(0, -1, 0), v3);
+        const float n4 = sdf_interp(r, p2 + ez, v4), n5 = sdf_interp(r, p2 + mk3(0, 0, -1), v5);
+        const bool ok = !(isnan(n0) || n0 == 1.0f || !v0) && !(isnan(n1) || n1 == 1.0f || !v1) &&
+                        !(isnan(n2) || n2 == 1.0f || !v2) && !(isnan(n3) || n3 == 1.0f || !v3) &&
+                        !(isnan(n4) || n4 == 1.0f || !v4) && !(isnan(n5) || n5 == 1.0f || !v5);
+        if (ok) {
+          // vertex v = R^T (q - t), q = p2 * voxel
+          const f3 q = p2 * vs;
+          const f3 gq = mul(c.R, gv);
+          f3 grho = -gq;
+          f3 gom = cross(gq, q);
+          f3 gp2 = gq * vs;
+          // normal n = u / |u|, u = R^T g
+          const f3 gr = mk3(n0 - n1, n2 - n3, n4 - n5);
+          const f3 u = mul(c.Rinv, gr);
+          const float un = norm(u);
+          const f3 nn = u / un;
+          const f3 gu = (gn - nn * dot(nn, gn)) / un;
+          const f3 ggr = mul(c.R, gu);
+          gom = gom + cross(ggr, gr);
+          gp2 = gp2 + ggr.x * sdf_interp_bwd(r, p2 + ex, ggr.x, grad_sdf);
+          gp2 = gp2 - ggr.x * sdf_interp_bwd(r, p2 + mk3(-1, 0, 0), -ggr.x, grad_sdf);
+          gp2 = gp2 + ggr.y * sdf_interp_bwd(r, p2 + ey, ggr.y, grad_sdf);
+          gp2 = gp2 - ggr.y * sdf_interp_bwd(r, p2 + mk3(0, -1, 0), -ggr.y, grad_sdf);
+          gp2 = gp2 + ggr.z * sdf_interp_bwd(r, p2 + ez, ggr.z, grad_sdf);
+          gp2 = gp2 - ggr.z * sdf_interp_bwd(r, p2 + mk3(0, 0, -1), -ggr.z, grad_sdf);
+          // p2 = p1 + ss * s1 * dir
+          f3 gp1 = gp2;
+          const float gs1 = ss * dot(dir, gp2);
+          f3 gdir = (ss * s1) * gp2;
+          gp1 = gp1 + gs1 * sdf_interp_bwd(r, p1, gs1, grad_sdf);
+          // p1 = p0 + ss * sdf_c * dir; sdf_c read at ms.sample
+          const f3 gp0 = gp1;
+          const float gsc = ss * dot(dir, gp1);
+          gdir = gdir + (ss * ms.sdf) * gp1;
+          f3 gsmp = mk3(0.f, 0.f, 0.f);
+          if (ms.interp) {
+            gsmp = gsc * sdf_interp_bwd(r, ms.sample, gsc, grad_sdf);
+          } else if (grad_sdf && gsc != 0.f) {
+            const i3 pv = floor3(ms.sample);
+            const int ptr = block_ptr(r, pv.x >> 3, pv.y >> 3, pv.z >> 3);
+            if (ptr >= 0) atomicAdd(grad_sdf + ptr + ((pv.z & 7) * 64 + (pv.y & 7) * 8 + (pv.x & 7)), gsc);
+          }
+          // p0 = block_s + s_result * dir, sample = block_s + s_sample * dir
+          f3 gbs = gp0 + gsmp;
+          gdir = gdir + ms.s_result * gp0 + ms.s_sample * gsmp;
+          // dir = normalised(block_e - block_s)
+          const f3 d = ms.block_e - ms.block_s;
+          const float dn = norm(d);
+          const f3 gd = (gdir - dir * dot(dir, gdir)) / dn;
+          const f3 gbe = gd;
+          gbs = gbs - gd;
+          // block_s = (R p + t) / voxel, block_e likewise; world points move by omega x w + rho
+          const float vsi = m.c.voxel_size_inv;
+          const f3 gws = gbs * vsi, gwe = gbe * vsi;
+          grho = grho + gws + gwe;
+          gom = gom + cross(ms.ps, gws) + cross(ms.pe, gwe);
+          gp[0] = grho.x; gp[1] = grho.y; gp[2] = grho.z;
+          gp[3] = gom.x; gp[4] = gom.y; gp[5] = gom.z;
+        }
+      }
+    }
+  }
+  // fixed-order CTA sum of the pose gradient
+  __shared__ float wpart[4][6];
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x, lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    float v = gp[k];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if (lane == 0) wpart[warp][k] = v;
+  }
+  __syncthreads();
+  if (tid < 6) {
+    const float v = ((wpart[0][tid] + wpart[1][tid]) + wpart[2][tid]) + wpart[3][tid];
+    pose_part[(size_t)(blockIdx.y * gridDim.x + blockIdx.x) * 6 + tid] = v;
+  }
+}
+
+// Sum of the CTA pose partials in FP64, fixed order.
+__global__ void k_pose_grad_sum(const float *part, int n, double *out) {
+  __shared__ double w[8][6];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (int i = threadIdx.x; i < n; i += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < 6; ++k) acc[k] += (double)part[(size_t)i * 6 + k];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    double v = acc[k];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if (lane == 0) w[warp][k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double v = 0.0;
+    for (int q = 0; q < (int)(blockDim.x / 32); ++q) v += w[q][threadIdx.x];
+    out[threadIdx.x] = v;
+  }
 }
 
 // Builds the block window for the reference-shaped Raycast entry point.
@@ -295,6 +497,17 @@ void launch_raycast(const DevMap &m, const FuseScratch &f, const sf_image &vmap,
   sf_image fv = fallback_v ? *fallback_v : sf_image{};
   sf_image fn = fallback_n ? *fallback_n : sf_image{};
   k_raycast<<<grd, blk, 0, s>>>(m, f, vmap, nmap, zmin, zmax, c, rendered, fv, fn, run_flag); note_launch();
+}
+
+int raycast_adjoint_blocks(int cols, int rows) { return ((cols + 7) / 8) * ((rows + 15) / 16); }
+
+void launch_raycast_adjoint(const DevMap &m, const FuseScratch &f, const sf_image &zmin, const sf_image &zmax,
+                            const Cam *c, const sf_image &gv, const sf_image &gn, float *grad_sdf,
+                            float *pose_part, double *pose_out, cudaStream_t s) {
+  dim3 blk(8, 16);
+  dim3 grd((gv.cols + 7) / 8, (gv.rows + 15) / 16);
+  k_raycast_adjoint<<<grd, blk, 0, s>>>(m, f, zmin, zmax, c, gv, gn, grad_sdf, pose_part); note_launch();
+  k_pose_grad_sum<<<1, 256, 0, s>>>(pose_part, (int)(grd.x * grd.y), pose_out); note_launch();
 }
 
 void launch_window_build(const DevMap &m, const FuseScratch &f, const Cam *c, cudaStream_t s) {

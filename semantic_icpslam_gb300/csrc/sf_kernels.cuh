@@ -116,6 +116,14 @@ void launch_raycast(const DevMap &m, const FuseScratch &f, const sf_image &vmap,
                     const sf_image &zmin, const sf_image &zmax, const Cam *c,
                     const unsigned *rendered, const sf_image *fallback_v,
                     const sf_image *fallback_n, const int *run_flag, cudaStream_t s);
+// RaycastAdjoint: gradients of launch_raycast's maps w.r.t. the pose (left
+// se(3) perturbation, 6 doubles into pose_out) and TSDF values (added into
+// grad_sdf, one float per voxel index; may be null).  pose_part holds
+// raycast_adjoint_blocks() x 6 floats.
+int raycast_adjoint_blocks(int cols, int rows);
+void launch_raycast_adjoint(const DevMap &m, const FuseScratch &f, const sf_image &zmin, const sf_image &zmax,
+                            const Cam *c, const sf_image &gv, const sf_image &gn, float *grad_sdf,
+                            float *pose_part, double *pose_out, cudaStream_t s);
 // Block-pointer window for camera c from the allocated-entry index (the
 // per-frame path builds it inside launch_visibility).
 void launch_window_build(const DevMap &m, const FuseScratch &f, const Cam *c, cudaStream_t s);

@@ -112,6 +112,40 @@ __device__ __forceinline__ float sdf_interp(const RayCtx &r, f3 pt, bool &valid)
   return (1.0f - xyz3.z) * r2 + xyz3.z * r3;
 }
 
+
+// Adjoint of sdf_interp at pt: adds g * (corner weight) to grad_sdf at each
+// corner's voxel index (ptr + local) and returns d sdf_interp / d pt.  The
+// corners and weights are sdf_interp's.  Corners in missing blocks get no
+// gradient (their NaN value already makes the forward output invalid).
+__device__ __forceinline__ f3 sdf_interp_bwd(const RayCtx &r, f3 pt, float g, float *grad_sdf) {
+  const f3 f = pt - mk3(floorf(pt.x), floorf(pt.y), floorf(pt.z));
+  const i3 a = floor3(pt);
+  const i3 b = floor3(pt + mk3(1, 1, 1));
+  float c[8];
+  int idx[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int vx = (k & 1) ? b.x : a.x, vy = (k & 2) ? b.y : a.y, vz = (k & 4) ? b.z : a.z;
+    const int ptr = block_ptr(r, vx >> 3, vy >> 3, vz >> 3);
+    idx[k] = ptr < 0 ? -1 : ptr + ((vz & 7) * 64 + (vy & 7) * 8 + (vx & 7));
+    c[k] = ptr < 0 ? 0.f : __ldg(&r.voxels[idx[k]].sdf);
+  }
+  const float wx[2] = {1.0f - f.x, f.x}, wy[2] = {1.0f - f.y, f.y}, wz[2] = {1.0f - f.z, f.z};
+  if (grad_sdf && g != 0.f) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      if (idx[k] >= 0) atomicAdd(grad_sdf + idx[k], g * (wx[k & 1] * wy[(k >> 1) & 1] * wz[(k >> 2) & 1]));
+  }
+  // d/dfx, d/dfy, d/dfz of the trilinear form
+  const float dx = wz[0] * (wy[0] * (c[1] - c[0]) + wy[1] * (c[3] - c[2])) +
+                   wz[1] * (wy[0] * (c[5] - c[4]) + wy[1] * (c[7] - c[6]));
+  const float dy = wz[0] * (wx[0] * (c[2] - c[0]) + wx[1] * (c[3] - c[1])) +
+                   wz[1] * (wx[0] * (c[6] - c[4]) + wx[1] * (c[7] - c[5]));
+  const float dz = wy[0] * (wx[0] * (c[4] - c[0]) + wx[1] * (c[5] - c[1])) +
+                   wy[1] * (wx[0] * (c[6] - c[2]) + wx[1] * (c[7] - c[3]));
+  return mk3(dx, dy, dz);
+}
+
 }  // namespace
 }  // namespace sf
 #endif
