@@ -477,7 +477,13 @@ __device__ __forceinline__ void semantic_voxel(sf_voxel &prev, uint8_t label, f3
 
 constexpr int kIntThreads = 256;
 
-__global__ void __launch_bounds__(kIntThreads) k_integrate(DevMap m, sf_image depth, sf_image rgb,
+// Eight 256-thread CTAs per SM (32 registers, a few spilled bytes): the
+// kernel waits on its voxel loads, and full occupancy hides that best
+// (measured on GB300 against 3-6 CTAs per SM).
+#ifndef SF_INT_MINB
+#define SF_INT_MINB 8
+#endif
+__global__ void __launch_bounds__(kIntThreads, SF_INT_MINB) k_integrate(DevMap m, sf_image depth, sf_image rgb,
                                                            sf_image nmap, sf_image mask,
                                                            int num_detection, const Cam *cam,
                                                            int do_int, int do_sem,
