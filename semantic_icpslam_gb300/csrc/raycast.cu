@@ -244,7 +244,14 @@ __device__ __forceinline__ void march_ray(const RayCtx &r, const Cam &c, float v
 // samples ahead at once, at the positions a run of 1-voxel steps would
 // reach (the same float additions), then replays the reference's loop over
 // them in order; an 8-voxel step or the end of the range ends the run.
-__global__ void __launch_bounds__(128) k_raycast(DevMap m, FuseScratch f, sf_image vmap, sf_image nmap,
+// Eight 128-thread CTAs per SM (64 registers): the march is latency-bound
+// and gains more from the extra warps than it loses to a few spilled
+// values (measured on GB300: 1, 6, 8, 12 and 16 CTAs per SM; 12 and more
+// spill too much).
+#ifndef SF_RC_MINB
+#define SF_RC_MINB 8
+#endif
+__global__ void __launch_bounds__(128, SF_RC_MINB) k_raycast(DevMap m, FuseScratch f, sf_image vmap, sf_image nmap,
                                                  sf_image zmin, sf_image zmax, const Cam *cam,
                                                  const unsigned *rendered, sf_image fb_v,
                                                  sf_image fb_n, const int *run_flag) {
