@@ -293,18 +293,59 @@ def algorithmic_bytes(stats_list):
     return integ.mean(), ray.mean(), V.mean()
 
 
+def time_reference_cuda(frames, steps, warmup):
+    """The reference's own CUDA launchers (oracle/_ref/gpu_c2/librefgpu.so,
+    built by oracle/ref_shim/build_ref_gpu.py) in System::GrabImage's order,
+    ICP-only, host buffers in: frames/s over `steps` frames after `warmup`."""
+    import ctypes as C
+    lib_path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "oracle", "_ref", "gpu_c2", "librefgpu.so")
+    if not os.path.exists(lib_path):
+        return {"unavailable": "the reference's CUDA build is not present (oracle/_ref/gpu_c2 not prepared)"}
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return {"unavailable": "no GPU"}
+    except ImportError:
+        return {"unavailable": "no torch"}
+    L = C.CDLL(lib_path)
+    L.refgpu_create.restype = C.c_void_p
+    L.refgpu_create.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_float), C.c_float, C.c_float, C.POINTER(C.c_double)]
+    L.refgpu_grab.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]
+    L.refgpu_destroy.argtypes = [C.c_void_p]
+    K4 = (C.c_float * 4)(*K)
+    init = np.ascontiguousarray(frames[0][3], np.float64)
+    h = L.refgpu_create(COLS, ROWS, K4, 1000.0, 3.0, init.ctypes.data_as(C.POINTER(C.c_double)))
+    if not h:
+        return {"unavailable": "refgpu_create failed"}
+    pose = np.zeros(16, np.float64)
+    n = min(len(frames), steps + warmup)
+    tracked = 0
+    err = 0.0
+    for i in range(n):
+        if i == warmup:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+        d, rgb = np.ascontiguousarray(frames[i][0]), np.ascontiguousarray(frames[i][1])
+        tracked += L.refgpu_grab(h, d.ctypes.data, rgb.ctypes.data, pose.ctypes.data_as(C.POINTER(C.c_double)))
+        err = max(err, float(np.abs(pose.reshape(4, 4)[:3, 3] - frames[i][3][:3, 3]).max()))
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    L.refgpu_destroy(h)
+    timed = n - warmup
+    return {"value": round(timed / dt, 3), "unit": "frames/s", "steps": timed, "warmup": warmup,
+            "tracked_frames": int(tracked), "max_translation_error_vs_ground_truth_m": round(err, 5),
+            "kind": "reference CUDA build (Tracking/*.cu, Mapping/*.cu for sm_103a), ICP-only ComputeSE3, "
+                    "host buffers in, the reference's per-launch synchronisation"}
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
     n = max(4, min(12, args.steps + 1))
-    frames = make_frames(n)
+    frames = make_frames(max(n, min(args.steps + args.warmup, 300)))
     threads = omp_threads()
-    vals = []
-    for _ in range(max(1, args.warmup if args.warmup < 2 else 1)):
-        pass
-    fps = cpu_reference(frames, n)
-    vals.append(fps)
+    fps = cpu_reference(frames[:n], n)
     line = {"impl": "reference", "metric": METRIC, "value": round(fps, 4), "unit": "frames/s", "n_gpus": args.gpus,
             "steps": n - 1, "warmup": 1, "ms_per_step": round(1000.0 / fps, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 6x6 solve)",
@@ -315,6 +356,7 @@ def run_reference(args):
                                        "(the reference's algorithm restated in C++/OpenMP, pinned bit-exact to "
                                        "the reference's own kernels)" % (n - 1)},
             "e2e": {"value": round(fps, 4), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    line["reference_cuda"] = time_reference_cuda(frames, min(args.steps, len(frames) - args.warmup), args.warmup)
     print(json.dumps(line), flush=True)
 
 

@@ -155,7 +155,7 @@ def patch_sources(name, text, cfg):
     if name == "DeviceMap.h":
         def sub(field, value):
             nonlocal text
-            pat = re.compile(r"(static constexpr \w+ %s = )[^;]+;" % field)
+            pat = re.compile(r"^(\s*static constexpr \w+ %s = )[^;]+;" % field, re.M)
             assert pat.search(text), field
             text = pat.sub(lambda m: m.group(1) + str(value) + ";", text, count=1)
         sub("VoxelSize", cfg["VoxelSize"])
