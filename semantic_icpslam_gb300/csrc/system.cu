@@ -268,7 +268,7 @@ cudaError_t enqueue_device_frame(sf_system *s, int num_detection, cudaStream_t s
   k_sys_pre<<<1, 1, 0, st>>>(s->d_sys); note_launch();
   IcpLevelArgs lv[kMaxLevels];
   icp_levels(s, lv);
-  cudaError_t e = cudaMemsetAsync(w.barrier, 0, sizeof(unsigned), st);
+  cudaError_t e = icp_persistent_reset(w, st);
   if (e != cudaSuccess) return e;
   e = launch_icp_persistent(w, lv, s->L, s->cfg.icp_thresh, dev_field<double>(s->d_sys, offsetof(SysDev, last_pose)),
                             dev_field<int>(s->d_sys, offsetof(SysDev, icp_run)),
@@ -472,17 +472,20 @@ int sf_system_grab(sf_system *s, const uint16_t *depth, const uint8_t *rgb, cons
   if (num_detection > 0 && !mask) return SF_ERR_INVALID;
   cudaStream_t st = ctx_stream(s->ctx);
   const size_t np = (size_t)s->cfg.cols * s->cfg.rows;
-  // host -> pinned staging -> device
-  memcpy(s->h_depth16, depth, np * 2);
-  memcpy(s->h_rgb, rgb, np * 3);
-  if (cudaMemcpyAsync(s->d_depth16, s->h_depth16, np * 2, cudaMemcpyHostToDevice, st) != cudaSuccess ||
-      cudaMemcpyAsync(s->d_rgb, s->h_rgb, np * 3, cudaMemcpyHostToDevice, st) != cudaSuccess)
+  // host -> device: straight from the caller's buffer when it is pinned
+  // (page-locked or registered), through the pinned staging buffer when not
+  auto upload = [&](void *dst, const void *src, void *staging, size_t n) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, src) == cudaSuccess && a.type == cudaMemoryTypeHost)
+      return cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, st);
+    cudaGetLastError();  // an unregistered pointer is not an error here
+    memcpy(staging, src, n);
+    return cudaMemcpyAsync(dst, staging, n, cudaMemcpyHostToDevice, st);
+  };
+  if (upload(s->d_depth16, depth, s->h_depth16, np * 2) != cudaSuccess ||
+      upload(s->d_rgb, rgb, s->h_rgb, np * 3) != cudaSuccess)
     return SF_ERR_CUDA;
-  if (num_detection > 0) {
-    memcpy(s->h_mask, mask, np);
-    if (cudaMemcpyAsync(s->d_mask, s->h_mask, np, cudaMemcpyHostToDevice, st) != cudaSuccess)
-      return SF_ERR_CUDA;
-  }
+  if (num_detection > 0 && upload(s->d_mask, mask, s->h_mask, np) != cudaSuccess) return SF_ERR_CUDA;
   int r = run_frame(s, num_detection);
   if (r) return r;
   if (cudaMemcpyAsync(s->h_stats, s->d_stats, sizeof(sf_frame_stats), cudaMemcpyDeviceToHost, st) !=
