@@ -440,7 +440,7 @@ int sf_ComputeSE3(sf_context *ctx, int levels, const sf_image *nv, const sf_imag
     L[l].min_count = min_count[l];
   }
   SF_CHECK(cudaMemcpyAsync(ctx->pose, last_pose, 16 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-  SF_CHECK(cudaMemsetAsync(ctx->icp.barrier, 0, sizeof(unsigned), ctx->stream));
+  SF_CHECK(icp_persistent_reset(ctx->icp, ctx->stream));
   SF_CHECK(launch_icp_persistent(ctx->icp, L, levels, thresh, ctx->pose, nullptr, ctx->flags, ctx->stream));
   SF_CHECK(cudaMemcpyAsync(ctx->host_ctl, ctx->icp.ctl, sizeof(TrackCtl), cudaMemcpyDeviceToHost, ctx->stream));
   SF_CHECK(cudaStreamSynchronize(ctx->stream));

@@ -8,11 +8,11 @@
 //
 // GB300 form: one persistent cooperative kernel runs every pyramid level and
 // iteration.  Per iteration each CTA reduces its pixels' 29 products
-// (FP32 per-pixel, compensated FP32 warp trees, FP64 block total), writes one
-// FP64 partial per component, and crosses a bounded grid barrier; then every
-// CTA sums the partials in FP64 in the same fixed order and runs the same
-// 6x6 LDLT solve and SE(3) update, so all CTAs hold the same pose without a
-// second barrier.  Partials are double-buffered by iteration parity.
+// (FP32 per pixel, compensated FP32 warp and block trees), adds the block
+// totals into exact fixed-point accumulators with fire-and-forget atomics
+// and crosses a bounded grid barrier; then every CTA reads the same 29
+// totals and runs the same 6x6 solve and SE(3) update, so all CTAs hold the
+// same pose without a second barrier.  Accumulators rotate over three sets.
 #include <mutex>
 
 #include "sf_kernels.cuh"
@@ -266,34 +266,67 @@ __device__ __forceinline__ void cross_block_sum(const double *part, int nb, int 
   __syncthreads();
 }
 
-// The same over float-float partials (float2 [29][stride]), accumulated on
-// the FP32 pipe (an FP64 sum would take ~64 cycles per add and warp on
-// this part).  Fixed order.
-template <int NW>
-__device__ __forceinline__ void cross_block_sum_ff(const float2 *part, int nb, int stride,
-                                                   double *sums) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int c = warp; c < 29; c += NW) {
-    ff t{0.f, 0.f};
-    for (int b = lane; b < nb; b += 32) {
-      const float2 p = __ldcg(part + (size_t)c * stride + b);
-      t = ff_add(t, ff{p.x, p.y});
-    }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) t = ff_add(t, ff_shfl_xor(t, off));
-    if (lane == 0) sums[c] = (double)t.s + (double)t.e;
+// Exact cross-CTA sums.  A CTA's float-float total of a component becomes
+// an integer, value * 2^kFixFrac (truncated below 2^-kFixFrac), cut into
+// three kLimbBits-bit limbs (the top one signed) that are added into three
+// 64-bit accumulators with fire-and-forget atomics.  Limbs of up to 2^21
+// addends sum without overflow and without carries between limbs, and
+// integer addition is exact and independent of order, so the totals do not
+// depend on which CTA arrives first and every CTA reads the same 29 values
+// once the barrier opens.  A fourth slot counts addends beyond 2^64 in
+// magnitude (or not finite); such a component reads as NaN.
+constexpr int kFixFrac = 60;
+constexpr int kLimbBits = 42;
+constexpr int kFixSlots = 4;  // limbs 0-2, out-of-range count
+constexpr unsigned long long kLimbMask = (1ull << kLimbBits) - 1ull;
+
+__device__ __forceinline__ __int128 f32_to_fix(float f, bool &bad) {
+  const unsigned b = __float_as_uint(f);
+  const int ex = (b >> 23) & 0xff;
+  if (ex == 0) return 0;  // zero or subnormal: below 2^-126
+  const int sh = ex - 150 + kFixFrac;  // |f| = m * 2^(ex - 150)
+  if (sh > 100) {  // |f| >= 2^64, infinite or NaN
+    bad = true;
+    return 0;
   }
-  __syncthreads();
+  const unsigned m = (b & 0x7fffffu) | 0x800000u;
+  const __int128 v = sh >= 0 ? ((__int128)m << sh) : (sh > -24 ? (__int128)(m >> -sh) : (__int128)0);
+  return (b >> 31) ? -v : v;
 }
+
+__device__ __forceinline__ void red_add_u64(unsigned long long *p, unsigned long long v) {
+  asm volatile("red.relaxed.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// Adds a CTA's float-float total (hi, lo) into the accumulator slots d.
+__device__ __forceinline__ void fix_add(unsigned long long *d, float2 v) {
+  bool bad = false;
+  const __int128 x = f32_to_fix(v.x, bad) + f32_to_fix(v.y, bad);
+  red_add_u64(d + 0, (unsigned long long)x & kLimbMask);
+  red_add_u64(d + 1, (unsigned long long)(x >> kLimbBits) & kLimbMask);
+  red_add_u64(d + 2, (unsigned long long)(long long)(x >> (2 * kLimbBits)));
+  if (bad) red_add_u64(d + 3, 1ull);
+}
+
+// The accumulated total of slots d as a double (one rounding when the
+// integer fits 64 bits, else at most two, relative 2^-52).
+__device__ __forceinline__ double fix_total(const unsigned long long *d) {
+  const unsigned long long a0 = __ldcg(d + 0), a1 = __ldcg(d + 1), a2 = __ldcg(d + 2);
+  if (__ldcg(d + 3) != 0ull) return __longlong_as_double(0x7ff8000000000000ll);
+  const __int128 t = ((__int128)(long long)a2 << (2 * kLimbBits)) + ((__int128)a1 << kLimbBits) + (__int128)a0;
+  const long long hi = (long long)(t >> 64);
+  const unsigned long long lo = (unsigned long long)t;
+  if (hi == ((long long)lo >> 63)) return (double)(long long)lo * 0x1p-60;
+  return fma((double)hi, 0x1p4, (double)lo * 0x1p-60);
+}
+static_assert(kFixFrac == 60, "fix_total's scale factors");
 
 struct PersistentArgs {
   IcpLevelArgs lv[kMaxLevels];
   int levels;
   float thresh;
-  float2 *partials;  // [2][29][max_blocks] float-float CTA totals
-  int stride;        // max_blocks
-  unsigned *barrier; // [2] arrivals, generation
-  double *pub;       // [29] sums published by the last CTA to arrive
+  unsigned *arrivals;        // grid barrier count, zero at launch
+  unsigned long long *fix;   // [3][29][kFixSlots] accumulators, zero at launch
   TrackCtl *ctl;
   const double *last_pose;
   const int *run_flag;
@@ -302,8 +335,8 @@ struct PersistentArgs {
 };
 
 // Phase clock of CTA 0 (SM cycles): 0 iteration start, 1 pixels
-// accumulated, 2 block total written, 3 arrived at the barrier, 4 the 29
-// sums in hand, 5 solve done.
+// accumulated, 2 block total sent, 3 barrier passed, 4 the 29 sums in
+// hand, 5 solve done.
 __device__ __forceinline__ void prof_mark(const PersistentArgs &a, int it, int k) {
   if (a.prof && blockIdx.x == 0 && threadIdx.x == 0 && it < kProfIters) {
     a.prof[it * kProfSlots + k] = clock64();
@@ -315,55 +348,27 @@ __device__ __forceinline__ void prof_mark(const PersistentArgs &a, int it, int k
   }
 }
 
-// End of an iteration's accumulation, after every CTA has written its 29
-// partials: a bounded barrier in which the last CTA to arrive sums all
-// partials (fixed order) and publishes the 29 sums before it opens the
-// barrier; the others wait and read them.  Only one CTA reads the partials,
-// and every CTA ends with the same 29 doubles in sums.  A wait that runs
-// past 2^22 polls records SF_FLAG_BARRIER_TIMEOUT and goes on.
-__device__ __forceinline__ void reduce_at_barrier(const PersistentArgs &a, const float2 *part, int nb,
-                                                  double *sums, int it) {
-  __shared__ unsigned s_gen;
-  __shared__ int s_last;
+// Grid barrier of iteration it (counted from 0 in this launch): the
+// arrival count only grows, so the barrier is open once it reaches
+// nb * (it + 1).  Thread 0 releases the CTA's accumulator adds with its
+// arrival and acquires everyone else's with the poll that sees the count.
+// A wait that runs past 2^22 polls records SF_FLAG_BARRIER_TIMEOUT and
+// goes on.
+__device__ __forceinline__ void grid_barrier(const PersistentArgs &a, int nb, int it) {
   __syncthreads();
   if (threadIdx.x == 0) {
-    volatile unsigned *gen = a.barrier + 1;
-    const unsigned g = *gen;
-    __threadfence();
-    const unsigned arrived = atomicAdd(a.barrier, 1u);
-    s_gen = g;
-    s_last = (arrived == (unsigned)nb - 1u);
-    __threadfence();
-  }
-  __syncthreads();
-  prof_mark(a, it, 3);
-  if (s_last) {
-    cross_block_sum_ff<kPWarps>(part, nb, a.stride, sums);
-    if (threadIdx.x < 29) {
-      a.pub[threadIdx.x] = sums[threadIdx.x];
-      __threadfence();
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      atomicExch(a.barrier, 0u);
-      __threadfence();
-      atomicAdd(a.barrier + 1, 1u);
-    }
-  } else {
-    if (threadIdx.x == 0) {
-      volatile unsigned *gen = a.barrier + 1;
-      unsigned polls = 0;
-      while (*gen == s_gen) {
-        if (++polls > (1u << 22)) {
-          atomicOr(a.flags, SF_FLAG_BARRIER_TIMEOUT);
-          break;
-        }
-        __nanosleep(32);
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(a.arrivals) : "memory");
+    const unsigned target = (unsigned)nb * (unsigned)(it + 1);
+    unsigned polls = 0, seen;
+    for (;;) {
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(seen) : "l"(a.arrivals) : "memory");
+      if ((int)(seen - target) >= 0) break;
+      if (++polls > (1u << 22)) {
+        atomicOr(a.flags, SF_FLAG_BARRIER_TIMEOUT);
+        break;
       }
-      __threadfence();
+      __nanosleep(32);
     }
-    __syncthreads();
-    if (threadIdx.x < 29) sums[threadIdx.x] = __ldcg(a.pub + threadIdx.x);
   }
   __syncthreads();
 }
@@ -384,7 +389,7 @@ __global__ void __launch_bounds__(kPThreads, 1) k_icp_persistent(PersistentArgs 
   const int nb = gridDim.x;
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const int gstride = nb * blockDim.x;
-  int buf = 0, it = 0;
+  int set = 0, it = 0;  // set = it % 3
   for (int l = a.levels - 1; l >= 0; --l) {
     const IcpLevelArgs &L = a.lv[l];
     for (int j = 0; j < L.iters; ++j, ++it) {
@@ -395,13 +400,19 @@ __global__ void __launch_bounds__(kPThreads, 1) k_icp_persistent(PersistentArgs 
       icp_accumulate(L, pose, gtid, gstride, acc);
       prof_mark(a, it, 1);
       block_reduce29<kPWarps>(acc, wpart, bsum);
-      float2 *part = a.partials + (size_t)buf * 29 * a.stride;
-      if (threadIdx.x < 29) {
-        part[(size_t)threadIdx.x * a.stride + blockIdx.x] = bsum[threadIdx.x];
-        __threadfence();
-      }
+      unsigned long long *fx = a.fix + (size_t)set * 29 * kFixSlots;
+      if (threadIdx.x < 29) fix_add(fx + threadIdx.x * kFixSlots, bsum[threadIdx.x]);
       prof_mark(a, it, 2);
-      reduce_at_barrier(a, part, nb, sums, it);
+      grid_barrier(a, nb, it);
+      prof_mark(a, it, 3);
+      if (threadIdx.x < 29) sums[threadIdx.x] = fix_total(fx + threadIdx.x * kFixSlots);
+      // Every CTA read the previous iteration's set before it arrived here,
+      // so CTA 0 clears it for iteration it + 2; its clearing is released
+      // with its next arrival, before anyone can add into it.
+      const int prev = set == 0 ? 2 : set - 1;
+      if (blockIdx.x == 0 && threadIdx.x < 29 * kFixSlots)
+        __stcg(a.fix + (size_t)prev * 29 * kFixSlots + threadIdx.x, 0ull);
+      __syncthreads();
       prof_mark(a, it, 4);
       if (threadIdx.x == 0)
         s_solve_marks = (a.prof && blockIdx.x == 0 && it < kProfIters) ? a.prof + it * kProfSlots + 8 : nullptr;
@@ -409,7 +420,7 @@ __global__ void __launch_bounds__(kPThreads, 1) k_icp_persistent(PersistentArgs 
       if (threadIdx.x < 32) ctl_step_fast(ctl, sums, L.min_count, ssolve);
       __syncthreads();
       prof_mark(a, it, 5);
-      buf ^= 1;
+      set = set == 2 ? 0 : set + 1;
       if (ctl.stop) break;
     }
     if (ctl.stop) break;
@@ -443,6 +454,12 @@ __global__ void __launch_bounds__(kThreads) k_icp_reduce(const double *part, int
 
 }  // namespace
 
+constexpr size_t kBarrierBytes = 256 + sizeof(unsigned long long) * 3 * 29 * kFixSlots;
+
+cudaError_t icp_persistent_reset(const IcpWorkspace &w, cudaStream_t s) {
+  return cudaMemsetAsync(w.barrier, 0, kBarrierBytes, s);
+}
+
 int icp_workspace_init(IcpWorkspace &w) {
   int dev = 0, sms = 0, per_sm = 0, coop = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return SF_ERR_CUDA;
@@ -456,8 +473,9 @@ int icp_workspace_init(IcpWorkspace &w) {
   w.threads = kPThreads;
   if (cudaMalloc(&w.partials, sizeof(double) * 2 * 29 * (size_t)w.max_blocks) != cudaSuccess) return SF_ERR_CUDA;
   if (cudaMalloc(&w.sums, sizeof(double) * 29) != cudaSuccess) return SF_ERR_CUDA;
-  if (cudaMalloc(&w.barrier, sizeof(unsigned) * 2) != cudaSuccess) return SF_ERR_CUDA;
-  if (cudaMemset(w.barrier, 0, sizeof(unsigned) * 2) != cudaSuccess) return SF_ERR_CUDA;
+  if (cudaMalloc(&w.barrier, kBarrierBytes) != cudaSuccess) return SF_ERR_CUDA;
+  if (cudaMemset(w.barrier, 0, kBarrierBytes) != cudaSuccess) return SF_ERR_CUDA;
+  w.fix = reinterpret_cast<unsigned long long *>(reinterpret_cast<char *>(w.barrier) + 256);
   if (cudaMalloc(&w.ctl, sizeof(TrackCtl)) != cudaSuccess) return SF_ERR_CUDA;
   if (cudaMalloc(&w.prof, sizeof(unsigned long long) * kProfSlots * kProfIters) != cudaSuccess) return SF_ERR_CUDA;
   if (cudaMemset(w.prof, 0, sizeof(unsigned long long) * kProfSlots * kProfIters) != cudaSuccess) return SF_ERR_CUDA;
@@ -489,11 +507,8 @@ cudaError_t launch_icp_persistent(const IcpWorkspace &w, const IcpLevelArgs *lev
   for (int l = 0; l < nlevels && l < kMaxLevels; ++l) a.lv[l] = levels[l];
   a.levels = nlevels;
   a.thresh = thresh;
-  static_assert(sizeof(float2) == sizeof(double), "partials: 8-byte slots in either form");
-  a.partials = reinterpret_cast<float2 *>(w.partials);
-  a.stride = w.max_blocks;
-  a.barrier = w.barrier;
-  a.pub = w.sums;
+  a.arrivals = w.barrier;
+  a.fix = w.fix;
   a.ctl = w.ctl;
   a.last_pose = last_pose;
   a.run_flag = run_flag;

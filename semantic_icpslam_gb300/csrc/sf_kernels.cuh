@@ -31,7 +31,8 @@ struct IcpLevelArgs {
 struct IcpWorkspace {
   double *partials = nullptr;  // [2][29][max_blocks]
   double *sums = nullptr;      // [29]
-  unsigned *barrier = nullptr; // [2] arrival count, generation
+  unsigned *barrier = nullptr; // persistent kernel: arrival count, then (at +256 B) fix
+  unsigned long long *fix = nullptr;  // [3][29][4] fixed-point accumulators
   TrackCtl *ctl = nullptr;     // device copy of the tracking state
   int max_blocks = 0;          // co-resident CTAs of the persistent kernel
   int threads = 0;
@@ -46,6 +47,10 @@ void icp_workspace_free(IcpWorkspace &w);
 // sums land in w.sums (device).  Pose given as float matrices.
 void launch_icp_step(const IcpWorkspace &w, const IcpLevelArgs &L, const m3 &Rc, f3 tc,
                      const m3 &Rl, const m3 &RlInv, f3 tl, cudaStream_t s);
+
+// Zeroes the persistent kernel's barrier count and accumulators (one memset);
+// enqueue it before each launch_icp_persistent.
+cudaError_t icp_persistent_reset(const IcpWorkspace &w, cudaStream_t s);
 
 // Persistent form: every level and iteration of Tracker::ComputeSE3 in one
 // cooperative launch.  last_pose: device double[16]; result in *w.ctl.
