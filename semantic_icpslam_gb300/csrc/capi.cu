@@ -381,10 +381,16 @@ int sf_BuildPyramid(sf_context *ctx, sf_image depth_u16, sf_image raw, const sf_
                     const sf_image *vmaps, const sf_image *nmaps, int levels, sf_intrinsics K,
                     float depth_scale, float depth_cutoff) {
   if (!ctx || !depths || !vmaps || !nmaps || levels < 1 || levels > kMaxLevels) return SF_ERR_INVALID;
+  for (int l = 0; l < levels; ++l)
+    if (!img_ok(depths[l], 4) || !img_ok(vmaps[l], 16) || !img_ok(nmaps[l], 16)) return SF_ERR_INVALID;
   int st = sf_FilterDepth(ctx, depth_u16, raw, depths[0], depth_scale, depth_cutoff);
   if (st) return st;
+  if (pyramid_levels_fusable(depths, vmaps, nmaps, levels)) {
+    launch_pyramid_levels(depths, vmaps, nmaps, levels, K.fx, K.fy, K.cx, K.cy, depth_cutoff, ctx->stream);
+    SF_CHECK(cudaGetLastError());
+    return SF_OK;
+  }
   for (int l = 0; l < levels; ++l) {
-    if (!img_ok(depths[l], 4) || !img_ok(vmaps[l], 16) || !img_ok(nmaps[l], 16)) return SF_ERR_INVALID;
     if (l > 0) launch_pyrdown(depths[l - 1], depths[l], ctx->stream);
     const float div = (float)(1 << l);
     launch_vnmap(depths[l], vmaps[l], nmaps[l], K.fx / div, K.fy / div, K.cx / div, K.cy / div,

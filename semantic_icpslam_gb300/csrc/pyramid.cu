@@ -78,13 +78,26 @@ __global__ void k_pyrdown(sf_image src, sf_image dst) {
 // ComputeVMapKernel (Pyrdown.cu:123-145): z in (0.1, cutoff), where the
 // reference compares (double)z > 0.1.  No float lies in (0.1, 0.1f], so for
 // a float z that is exactly z >= 0.1f, with no FP64 instruction.
-__device__ __forceinline__ float4 vertex_at(const sf_image &depth, int x, int y, float invfx,
-                                            float invfy, float cx, float cy, float cutoff) {
-  float z = __ldg(row_ptr<const float>(depth, y) + x);
+__device__ __forceinline__ float4 vertex_of(float z, int x, int y, float invfx, float invfy, float cx,
+                                            float cy, float cutoff) {
   if (!isnan(z) && z >= 0.1f && z < cutoff) {
     return make_float4(z * ((float)x - cx) * invfx, z * ((float)y - cy) * invfy, z, 1.0f);
   }
   return nan4();
+}
+__device__ __forceinline__ float4 vertex_at(const sf_image &depth, int x, int y, float invfx,
+                                            float invfy, float cx, float cy, float cutoff) {
+  return vertex_of(__ldg(row_ptr<const float>(depth, y) + x), x, y, invfx, invfy, cx, cy, cutoff);
+}
+
+// ComputeNMapKernel's normal (Pyrdown.cu:160-181) from the vertex and its
+// right and lower neighbours.
+__device__ __forceinline__ float4 normal_of(float4 vc, float4 vr, float4 vd) {
+  if (isnan(vc.x) || isnan(vr.x) || isnan(vd.x)) return nan4();
+  f3 a = mk3(vr.x - vc.x, vr.y - vc.y, vr.z - vc.z);
+  f3 b = mk3(vd.x - vc.x, vd.y - vc.y, vd.z - vc.z);
+  f3 q = normalised(cross(a, b));
+  return make_float4(q.x, q.y, q.z, 1.0f);
 }
 
 // ComputeVMap + ComputeNMap fused (Pyrdown.cu:123-181).
@@ -99,15 +112,117 @@ __global__ void k_vnmap(sf_image depth, sf_image vmap, sf_image nmap, float invf
   if (x != depth.cols - 1 && y != depth.rows - 1) {
     float4 vr = vertex_at(depth, x + 1, y, invfx, invfy, cx, cy, cutoff);
     float4 vd = vertex_at(depth, x, y + 1, invfx, invfy, cx, cy, cutoff);
-    if (!isnan(vc.x) && !isnan(vr.x) && !isnan(vd.x)) {
-      f3 a = mk3(vr.x - vc.x, vr.y - vc.y, vr.z - vc.z);
-      f3 b = mk3(vd.x - vc.x, vd.y - vc.y, vd.z - vc.z);
-      f3 q = normalised(cross(a, b));
-      n = make_float4(q.x, q.y, q.z, 1.0f);
-    }
+    n = normal_of(vc, vr, vd);
   }
   row_ptr<float4>(nmap, y)[x] = n;
 }
+
+// Levels 1..NL-1 of the Gaussian pyramid and the vertex and normal maps of
+// every level, from the filtered level-0 depth, in one launch.  A CTA owns
+// an 8x8 tile of the coarsest level and the 2^l times larger tiles under
+// it; it stages in shared memory the region of each level that its windows
+// reach (the 5x5 PyrDownGauss taps of the level below, the right and lower
+// neighbours of the normals) and recomputes the halo instead of waiting
+// for other CTAs.  Every value is computed with the same operations, in
+// the same order, as k_pyrdown and k_vnmap, so the maps are bit-identical
+// to theirs.
+template <int NL>
+struct PyrTile {
+  // region of level l, relative to the tile origin: [lo, hi] inclusive
+  __host__ __device__ static constexpr int lo(int l) { return l >= NL - 1 ? 0 : 2 * lo(l + 1) - 2; }
+  __host__ __device__ static constexpr int hi(int l) { return l >= NL - 1 ? 8 : 2 * hi(l + 1) + 2; }
+  __host__ __device__ static constexpr int n(int l) { return hi(l) - lo(l) + 1; }
+  __host__ __device__ static constexpr int tile(int l) { return 8 << (NL - 1 - l); }
+  __host__ __device__ static constexpr int off(int l) { return l == 0 ? 0 : off(l - 1) + n(l - 1) * n(l - 1); }
+  __host__ __device__ static constexpr int total() { return off(NL); }
+};
+
+__global__ void __launch_bounds__(256) k_pyramid_levels_2(PyramidArgs a);
+__global__ void __launch_bounds__(256) k_pyramid_levels_3(PyramidArgs a);
+__global__ void __launch_bounds__(256) k_pyramid_levels_4(PyramidArgs a);
+
+template <int NL>
+__device__ __forceinline__ void pyramid_levels(const PyramidArgs &a) {
+  using T = PyrTile<NL>;
+  __shared__ float s[T::total()];
+  const int X = blockIdx.x, Y = blockIdx.y;
+  {  // level 0 region
+    constexpr int n = T::n(0);
+    const int ox = X * T::tile(0) + T::lo(0), oy = Y * T::tile(0) + T::lo(0);
+    const sf_image &d = a.depth[0];
+    for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
+      const int yy = i / n, xx = i - yy * n;
+      const int gx = ox + xx, gy = oy + yy;
+      if (gx >= 0 && gy >= 0 && gx < d.cols && gy < d.rows) s[i] = __ldg(row_ptr<const float>(d, gy) + gx);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int l = 1; l < NL; ++l) {
+    const int n = T::n(l), np = T::n(l - 1);
+    const int t = T::tile(l);
+    const int ox = X * t + T::lo(l), oy = Y * t + T::lo(l);
+    const int opx = 2 * X * t + T::lo(l - 1), opy = 2 * Y * t + T::lo(l - 1);
+    const sf_image &d = a.depth[l];
+    const int pc = a.depth[l - 1].cols, pr = a.depth[l - 1].rows;
+    const float *src = s + T::off(l - 1);
+    for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
+      const int yy = i / n, xx = i - yy * n;
+      const int x = ox + xx, y = oy + yy;
+      if (x < 0 || y < 0 || x >= d.cols || y >= d.rows) continue;
+      // pyrdown_px over the staged level below
+      const int tx = min(2 * x + 3, pc - 1);
+      const int ty = min(2 * y + 3, pr - 1);
+      float sum = 0.f;
+      int count = 0;
+      for (int cy = max(0, 2 * y - 2); cy < ty; ++cy) {
+        const float *srow = src + (cy - opy) * np - opx;
+        for (int cx = max(0, 2 * x - 2); cx < tx; ++cx) {
+          float v = srow[cx];
+          if (!isnan(v)) {
+            float k = c_gauss[(ty - cy - 1) * 5 + (tx - cx - 1)];
+            sum += v * k;
+            count = (int)((float)count + k);
+          }
+        }
+      }
+      const float v = sum / (float)count;
+      s[T::off(l) + i] = v;
+      if (xx >= -T::lo(l) && xx < t - T::lo(l) && yy >= -T::lo(l) && yy < t - T::lo(l))
+        row_ptr<float>(d, y)[x] = v;
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int l = 0; l < NL; ++l) {
+    const int n = T::n(l), t = T::tile(l);
+    const int ox = X * t + T::lo(l), oy = Y * t + T::lo(l);
+    const sf_image &d = a.depth[l];
+    const PyramidLevelK k = a.k[l];
+    const float *z = s + T::off(l);
+    for (int i = threadIdx.x; i < t * t; i += blockDim.x) {
+      const int ty = i / t, tx = i - ty * t;
+      const int x = X * t + tx, y = Y * t + ty;
+      if (x >= d.cols || y >= d.rows) continue;
+      const int r = (y - oy) * n + (x - ox);
+      const float4 vc = vertex_of(z[r], x, y, k.invfx, k.invfy, k.cx, k.cy, a.cutoff);
+      row_ptr<float4>(a.vmap[l], y)[x] = vc;
+      float4 nm = nan4();
+      if (x != d.cols - 1 && y != d.rows - 1) {
+        const float4 vr = vertex_of(z[r + 1], x + 1, y, k.invfx, k.invfy, k.cx, k.cy, a.cutoff);
+        const float4 vd = vertex_of(z[r + n], x, y + 1, k.invfx, k.invfy, k.cx, k.cy, a.cutoff);
+        nm = normal_of(vc, vr, vd);
+      }
+      row_ptr<float4>(a.nmap[l], y)[x] = nm;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_pyramid_levels_2(PyramidArgs a) { pyramid_levels<2>(a); }
+__global__ void __launch_bounds__(256) k_pyramid_levels_3(PyramidArgs a) { pyramid_levels<3>(a); }
+__global__ void __launch_bounds__(256) k_pyramid_levels_4(PyramidArgs a) { pyramid_levels<4>(a); }
+static_assert(PyrTile<3>::n(0) == 45 && PyrTile<3>::n(1) == 21 && PyrTile<3>::n(2) == 9, "tile regions");
+static_assert(PyrTile<4>::total() * sizeof(float) <= 48 * 1024, "static shared memory");
 
 // Separate vertex-map and normal-map kernels for the reference-shaped
 // launchers (ComputeVMap / ComputeNMap).
@@ -189,6 +304,39 @@ void launch_filter_depth(const sf_image &depth, const sf_image &raw, const sf_im
 void launch_pyrdown(const sf_image &src, const sf_image &dst, cudaStream_t s) {
   dim3 blk(32, 8);
   k_pyrdown<<<grid2d(dst.cols, dst.rows, blk), blk, 0, s>>>(src, dst); note_launch();
+}
+
+bool pyramid_levels_fusable(const sf_image *depths, const sf_image *vmaps, const sf_image *nmaps, int levels) {
+  if (levels < 2 || levels > kMaxLevels) return false;
+  for (int l = 0; l < levels; ++l) {
+    if (vmaps[l].cols != depths[l].cols || vmaps[l].rows != depths[l].rows) return false;
+    if (nmaps[l].cols != depths[l].cols || nmaps[l].rows != depths[l].rows) return false;
+    if (l > 0 && (depths[l].cols != depths[l - 1].cols >> 1 || depths[l].rows != depths[l - 1].rows >> 1))
+      return false;
+  }
+  return depths[0].cols > 0 && depths[0].rows > 0;
+}
+
+void launch_pyramid_levels(const sf_image *depths, const sf_image *vmaps, const sf_image *nmaps, int levels,
+                           float fx, float fy, float cx, float cy, float cutoff, cudaStream_t s) {
+  PyramidArgs a;
+  for (int l = 0; l < levels; ++l) {
+    a.depth[l] = depths[l];
+    a.vmap[l] = vmaps[l];
+    a.nmap[l] = nmaps[l];
+    const float div = (float)(1 << l);  // the per-level intrinsics of launch_vnmap's callers
+    a.k[l].invfx = (float)(1.0 / (double)(fx / div));
+    a.k[l].invfy = (float)(1.0 / (double)(fy / div));
+    a.k[l].cx = cx / div;
+    a.k[l].cy = cy / div;
+  }
+  a.cutoff = cutoff;
+  const int t0 = 8 << (levels - 1);
+  const dim3 grid((depths[0].cols + t0 - 1) / t0, (depths[0].rows + t0 - 1) / t0);
+  if (levels == 2) k_pyramid_levels_2<<<grid, 256, 0, s>>>(a);
+  else if (levels == 3) k_pyramid_levels_3<<<grid, 256, 0, s>>>(a);
+  else k_pyramid_levels_4<<<grid, 256, 0, s>>>(a);
+  note_launch();
 }
 
 void launch_vnmap(const sf_image &depth, const sf_image &vmap, const sf_image &nmap, float fx,

@@ -21,6 +21,22 @@ void launch_nmap(const sf_image &vmap, const sf_image &nmap, cudaStream_t s);
 void launch_resize(const sf_image &vsrc, const sf_image &nsrc, const sf_image &vdst,
                    const sf_image &ndst, cudaStream_t s);
 
+// Levels 1..levels-1 of the pyramid from the filtered depths[0], and every
+// level's vertex and normal maps, in one launch (2 <= levels <= kMaxLevels;
+// the level sizes must halve (floor) and the maps match their depth).
+// fx .. cy are level 0's intrinsics.
+struct PyramidLevelK {
+  float invfx, invfy, cx, cy;
+};
+struct PyramidArgs {
+  sf_image depth[kMaxLevels], vmap[kMaxLevels], nmap[kMaxLevels];
+  PyramidLevelK k[kMaxLevels];
+  float cutoff;
+};
+bool pyramid_levels_fusable(const sf_image *depths, const sf_image *vmaps, const sf_image *nmaps, int levels);
+void launch_pyramid_levels(const sf_image *depths, const sf_image *vmaps, const sf_image *nmaps, int levels,
+                           float fx, float fy, float cx, float cy, float cutoff, cudaStream_t s);
+
 // ----------------------------------------------------------------- ICP
 struct IcpLevelArgs {
   sf_image vc, nc, vl, nl;   // current (measured) and last (model) maps

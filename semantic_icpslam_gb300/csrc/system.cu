@@ -205,6 +205,17 @@ void enqueue_pyramid(sf_system *s, cudaStream_t st) {
   const int C = s->cfg.cols, R = s->cfg.rows;
   launch_filter_depth(img(s->d_depth16, C, R, 2), img(s->d_raw, C, R, 4), img(s->d_depth[0], C, R, 4),
                       s->cfg.depth_scale, s->cfg.depth_cutoff, st);
+  if (s->L >= 2) {
+    sf_image d[kMaxLevels], v[kMaxLevels], n[kMaxLevels];
+    for (int l = 0; l < s->L; ++l) {
+      d[l] = img(s->d_depth[l], C >> l, R >> l, 4);
+      v[l] = img(s->d_vmap[l], C >> l, R >> l, 16);
+      n[l] = img(s->d_nmap[l], C >> l, R >> l, 16);
+    }
+    launch_pyramid_levels(d, v, n, s->L, s->cfg.K.fx, s->cfg.K.fy, s->cfg.K.cx, s->cfg.K.cy, s->cfg.depth_cutoff,
+                          st);
+    return;
+  }
   for (int l = 0; l < s->L; ++l) {
     const int c = C >> l, r = R >> l;
     if (l > 0)
