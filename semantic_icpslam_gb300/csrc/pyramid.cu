@@ -6,11 +6,14 @@
 // PyrDownGaussKernel :201-225, ResizeMapKernel :318-346) driven by
 // Frame::FillImages / ResizeImages (Core/Frame.cc:68-98).
 //
-// GB300 layout: a pyramid level is two launches, not four: the vertex and
-// normal maps of a level come from one kernel that recomputes the two
-// neighbouring vertices from depth instead of round-tripping the vertex map
-// through memory.  All maps are dense (step = cols * sizeof), 16-byte
-// float4 stores are coalesced across a warp.
+// GB300 layout: the whole pyramid is two launches.  The bilateral filter
+// stages its tile in shared memory; then one kernel makes every coarser
+// level and every level's vertex and normal maps from tiles staged in
+// shared memory (k_pyramid_levels_*), recomputing the halos it needs
+// rather than round-tripping levels and vertex maps through memory.  The
+// per-operation kernels (k_pyrdown, k_vnmap, k_vmap, k_nmap) serve the
+// reference-shaped entry points.  All maps are dense (step = cols *
+// sizeof), 16-byte float4 stores are coalesced across a warp.
 #include "sf_kernels.cuh"
 
 namespace sf {
@@ -21,34 +24,80 @@ __constant__ float c_gauss[25] = {1, 4, 6, 4, 1, 4, 16, 24, 16, 4, 6, 24, 36,
 // FilterDepthKernel (Pyrdown.cu:72-108).  sigSpace = 0.5/16, sigRange =
 // 0.5/0.25 (Pyrdown.cu:3-4).  The window's upper bound is exclusive, as in
 // the reference.
-__global__ void k_filter_depth(sf_image depth, sf_image raw, sf_image filt, float inv_scale,
-                               float cutoff) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+//
+// A CTA filters a 32x8 tile.  The depths of the tile and its 2-pixel halo
+// are converted to metres once and staged in shared memory; a pixel whose
+// whole 5x5 window lies inside the image takes the fully unrolled taps
+// (space2 * sigSpace is then a constant), the others the clipped loops.
+// Both visit the taps in the reference's order with the same operations
+// (space2 * 2^-5 and color2 * 2 are exact), so the filtered depth is the
+// same as a per-pixel global-memory form's.
+constexpr int kFiltTX = 32, kFiltTY = 8;
+constexpr int kFiltSX = kFiltTX + 4, kFiltSY = kFiltTY + 4;
+
+__global__ void __launch_bounds__(kFiltTX * kFiltTY) k_filter_depth(sf_image depth, sf_image raw, sf_image filt,
+                                                                    float inv_scale, float cutoff) {
+  __shared__ float s_m[kFiltSY][kFiltSX];
+  const int x0 = blockIdx.x * kFiltTX, y0 = blockIdx.y * kFiltTY;
+  const int tid = threadIdx.y * kFiltTX + threadIdx.x;
+  constexpr int kN = kFiltSX * kFiltSY, kPer = (kN + kFiltTX * kFiltTY - 1) / (kFiltTX * kFiltTY);
+  float stage[kPer];
+#pragma unroll
+  for (int k = 0; k < kPer; ++k) {
+    const int i = tid + k * kFiltTX * kFiltTY;
+    const int gx = x0 - 2 + i % kFiltSX, gy = y0 - 2 + i / kFiltSX;
+    stage[k] = (i < kN && gx >= 0 && gy >= 0 && gx < depth.cols && gy < depth.rows)
+                   ? (float)__ldg(row_ptr<const uint16_t>(depth, gy) + gx) * inv_scale
+                   : 0.f;
+  }
+#pragma unroll
+  for (int k = 0; k < kPer; ++k) {
+    const int i = tid + k * kFiltTX * kFiltTY;
+    if (i < kN) s_m[i / kFiltSX][i % kFiltSX] = stage[k];
+  }
+  __syncthreads();
+  const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
   if (x >= depth.cols || y >= depth.rows) return;
   const float sig_space = 0.03125f, sig_range = 2.0f;
-  float center = (float)row_ptr<const uint16_t>(depth, y)[x] * inv_scale;
+  const int lx = threadIdx.x + 2, ly = threadIdx.y + 2;
+  const float center = s_m[ly][lx];
   row_ptr<float>(raw, y)[x] = center < cutoff ? center : nanf_bits();
-  const int tx = min(x + 3, depth.cols - 1);
-  const int ty = min(y + 3, depth.rows - 1);
   float sum1 = 0.f, sum2 = 0.f;
-  for (int cy = max(y - 2, 0); cy < ty; ++cy) {
-    const uint16_t *drow = row_ptr<const uint16_t>(depth, cy);
-    for (int cx = max(x - 2, 0); cx < tx; ++cx) {
-      float val = (float)__ldg(drow + cx) * inv_scale;
-      float space2 = (float)((x - cx) * (x - cx) + (y - cy) * (y - cy));
-      float color2 = (center - val) * (center - val);
-      float weight = expf(-(space2 * sig_space + color2 * sig_range));
-      sum1 += val * weight;
-      sum2 += weight;
+  if (x >= 2 && y >= 2 && x + 3 <= depth.cols - 1 && y + 3 <= depth.rows - 1) {
+#pragma unroll
+    for (int dy = -2; dy <= 2; ++dy) {
+#pragma unroll
+      for (int dx = -2; dx <= 2; ++dx) {
+        const float val = s_m[ly + dy][lx + dx];
+        const float space2 = (float)(dx * dx + dy * dy);
+        const float color2 = (center - val) * (center - val);
+        const float weight = expf(-(space2 * sig_space + color2 * sig_range));
+        sum1 += val * weight;
+        sum2 += weight;
+      }
+    }
+  } else {
+    const int tx = min(x + 3, depth.cols - 1);
+    const int ty = min(y + 3, depth.rows - 1);
+    for (int cy = max(y - 2, 0); cy < ty; ++cy) {
+      for (int cx = max(x - 2, 0); cx < tx; ++cx) {
+        const float val = s_m[cy - y0 + 2][cx - x0 + 2];
+        const float space2 = (float)((x - cx) * (x - cx) + (y - cy) * (y - cy));
+        const float color2 = (center - val) * (center - val);
+        const float weight = expf(-(space2 * sig_space + color2 * sig_range));
+        sum1 += val * weight;
+        sum2 += weight;
+      }
     }
   }
-  float fin = sum1 / sum2;
+  const float fin = sum1 / sum2;
   row_ptr<float>(filt, y)[x] = fin < cutoff ? fin : nanf_bits();
 }
 
 // PyrDownGaussKernel<float,float> (Pyrdown.cu:201-225): NaN-skipping 5x5
-// Gaussian normalised by the used weights, reversed kernel index.
+// Gaussian normalised by the used weights, reversed kernel index.  The
+// reference's count = (int)((float)count + k) only ever adds small integers
+// (the weights sum to 256), so it is the integer sum of the used weights.
 __device__ __forceinline__ float pyrdown_px(const sf_image &src, int x, int y) {
   const int tx = min(2 * x + 3, src.cols - 1);
   const int ty = min(2 * y + 3, src.rows - 1);
@@ -61,8 +110,30 @@ __device__ __forceinline__ float pyrdown_px(const sf_image &src, int x, int y) {
       if (!isnan(v)) {
         float k = c_gauss[(ty - cy - 1) * 5 + (tx - cx - 1)];
         sum += v * k;
-        count = (int)((float)count + k);
+        count += (int)k;
       }
+    }
+  }
+  return sum / (float)count;
+}
+
+// The same with the whole window inside the source: p points at tap
+// (2x - 2, 2y - 2) of a row-major array with row stride `stride`.  The
+// weights are symmetric, so the reversed index reads the same table; the
+// taps are selects, not branches (every library file is built without
+// multiply-add contraction, so sum + v * k rounds twice as above).
+__device__ __forceinline__ float pyrdown_interior(const float *p, int stride) {
+  constexpr int g[5] = {1, 4, 6, 4, 1};
+  float sum = 0.f;
+  int count = 0;
+#pragma unroll
+  for (int r = 0; r < 5; ++r) {
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      const float v = p[r * stride + c];
+      const bool ok = !isnan(v);
+      sum = ok ? sum + v * (float)(g[r] * g[c]) : sum;
+      count += ok ? g[r] * g[c] : 0;
     }
   }
   return sum / (float)count;
@@ -137,24 +208,31 @@ struct PyrTile {
   __host__ __device__ static constexpr int total() { return off(NL); }
 };
 
-__global__ void __launch_bounds__(256) k_pyramid_levels_2(PyramidArgs a);
-__global__ void __launch_bounds__(256) k_pyramid_levels_3(PyramidArgs a);
-__global__ void __launch_bounds__(256) k_pyramid_levels_4(PyramidArgs a);
+// 512 threads, two CTAs per SM: a 640x480 frame's 300 tiles run in one wave.
+constexpr int kPyrThreads = 512;
 
 template <int NL>
 __device__ __forceinline__ void pyramid_levels(const PyramidArgs &a) {
   using T = PyrTile<NL>;
   __shared__ float s[T::total()];
   const int X = blockIdx.x, Y = blockIdx.y;
-  {  // level 0 region
-    constexpr int n = T::n(0);
+  {  // level 0 region: all of a thread's loads in flight before the stores
+    constexpr int n = T::n(0), kPer = (n * n + kPyrThreads - 1) / kPyrThreads;
     const int ox = X * T::tile(0) + T::lo(0), oy = Y * T::tile(0) + T::lo(0);
     const sf_image &d = a.depth[0];
-    for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
+    float v[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer; ++k) {
+      const int i = threadIdx.x + kPyrThreads * k;
       const int yy = i / n, xx = i - yy * n;
       const int gx = ox + xx, gy = oy + yy;
-      if (gx >= 0 && gy >= 0 && gx < d.cols && gy < d.rows) s[i] = __ldg(row_ptr<const float>(d, gy) + gx);
+      v[k] = (i < n * n && gx >= 0 && gy >= 0 && gx < d.cols && gy < d.rows)
+                 ? __ldg(row_ptr<const float>(d, gy) + gx)
+                 : 0.f;
     }
+#pragma unroll
+    for (int k = 0; k < kPer; ++k)
+      if (threadIdx.x + kPyrThreads * k < n * n) s[threadIdx.x + kPyrThreads * k] = v[k];
   }
   __syncthreads();
 #pragma unroll
@@ -171,22 +249,27 @@ __device__ __forceinline__ void pyramid_levels(const PyramidArgs &a) {
       const int x = ox + xx, y = oy + yy;
       if (x < 0 || y < 0 || x >= d.cols || y >= d.rows) continue;
       // pyrdown_px over the staged level below
-      const int tx = min(2 * x + 3, pc - 1);
-      const int ty = min(2 * y + 3, pr - 1);
-      float sum = 0.f;
-      int count = 0;
-      for (int cy = max(0, 2 * y - 2); cy < ty; ++cy) {
-        const float *srow = src + (cy - opy) * np - opx;
-        for (int cx = max(0, 2 * x - 2); cx < tx; ++cx) {
-          float v = srow[cx];
-          if (!isnan(v)) {
-            float k = c_gauss[(ty - cy - 1) * 5 + (tx - cx - 1)];
-            sum += v * k;
-            count = (int)((float)count + k);
+      float v;
+      if (x >= 1 && y >= 1 && 2 * x + 3 <= pc - 1 && 2 * y + 3 <= pr - 1) {
+        v = pyrdown_interior(src + (2 * y - 2 - opy) * np + (2 * x - 2 - opx), np);
+      } else {
+        const int tx = min(2 * x + 3, pc - 1);
+        const int ty = min(2 * y + 3, pr - 1);
+        float sum = 0.f;
+        int count = 0;
+        for (int cy = max(0, 2 * y - 2); cy < ty; ++cy) {
+          const float *srow = src + (cy - opy) * np - opx;
+          for (int cx = max(0, 2 * x - 2); cx < tx; ++cx) {
+            float sv = srow[cx];
+            if (!isnan(sv)) {
+              float k = c_gauss[(ty - cy - 1) * 5 + (tx - cx - 1)];
+              sum += sv * k;
+              count += (int)k;
+            }
           }
         }
+        v = sum / (float)count;
       }
-      const float v = sum / (float)count;
       s[T::off(l) + i] = v;
       if (xx >= -T::lo(l) && xx < t - T::lo(l) && yy >= -T::lo(l) && yy < t - T::lo(l))
         row_ptr<float>(d, y)[x] = v;
@@ -218,9 +301,9 @@ __device__ __forceinline__ void pyramid_levels(const PyramidArgs &a) {
   }
 }
 
-__global__ void __launch_bounds__(256) k_pyramid_levels_2(PyramidArgs a) { pyramid_levels<2>(a); }
-__global__ void __launch_bounds__(256) k_pyramid_levels_3(PyramidArgs a) { pyramid_levels<3>(a); }
-__global__ void __launch_bounds__(256) k_pyramid_levels_4(PyramidArgs a) { pyramid_levels<4>(a); }
+__global__ void __launch_bounds__(kPyrThreads, 2) k_pyramid_levels_2(PyramidArgs a) { pyramid_levels<2>(a); }
+__global__ void __launch_bounds__(kPyrThreads, 2) k_pyramid_levels_3(PyramidArgs a) { pyramid_levels<3>(a); }
+__global__ void __launch_bounds__(kPyrThreads, 2) k_pyramid_levels_4(PyramidArgs a) { pyramid_levels<4>(a); }
 static_assert(PyrTile<3>::n(0) == 45 && PyrTile<3>::n(1) == 21 && PyrTile<3>::n(2) == 9, "tile regions");
 static_assert(PyrTile<4>::total() * sizeof(float) <= 48 * 1024, "static shared memory");
 
@@ -296,7 +379,7 @@ static inline dim3 grid2d(int cols, int rows, dim3 blk) {
 
 void launch_filter_depth(const sf_image &depth, const sf_image &raw, const sf_image &filt,
                          float depth_scale, float cutoff, cudaStream_t s) {
-  dim3 blk(32, 8);
+  dim3 blk(kFiltTX, kFiltTY);
   const float inv = (float)(1.0 / (double)depth_scale);
   k_filter_depth<<<grid2d(depth.cols, depth.rows, blk), blk, 0, s>>>(depth, raw, filt, inv, cutoff); note_launch();
 }
@@ -333,9 +416,9 @@ void launch_pyramid_levels(const sf_image *depths, const sf_image *vmaps, const 
   a.cutoff = cutoff;
   const int t0 = 8 << (levels - 1);
   const dim3 grid((depths[0].cols + t0 - 1) / t0, (depths[0].rows + t0 - 1) / t0);
-  if (levels == 2) k_pyramid_levels_2<<<grid, 256, 0, s>>>(a);
-  else if (levels == 3) k_pyramid_levels_3<<<grid, 256, 0, s>>>(a);
-  else k_pyramid_levels_4<<<grid, 256, 0, s>>>(a);
+  if (levels == 2) k_pyramid_levels_2<<<grid, kPyrThreads, 0, s>>>(a);
+  else if (levels == 3) k_pyramid_levels_3<<<grid, kPyrThreads, 0, s>>>(a);
+  else k_pyramid_levels_4<<<grid, kPyrThreads, 0, s>>>(a);
   note_launch();
 }
 
