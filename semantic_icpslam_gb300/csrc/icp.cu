@@ -84,6 +84,7 @@ static_assert(sizeof(m3) == 9 * sizeof(float) && sizeof(f3) == 3 * sizeof(float)
 // (u, v), icp_finish takes the three loads and returns the row.
 struct IcpProj {
   f3 vg;  // current vertex in the world frame
+  f3 vp;  // the same in the last camera's frame
   int u, v;
   bool ok;
 };
@@ -98,6 +99,7 @@ __device__ __forceinline__ IcpProj icp_project(const IcpLevelArgs &L, const Pose
   // (double)z < 1e-3 of the reference is exactly z < 0.001f for a float z
   if (isnan(vcurr_c.x) || vcurr_c.z < 0.001f) return q;
   const f3 vcurr_p = mul(p.RlI, q.vg - p.tl);
+  q.vp = vcurr_p;
   // (float)(1.0 / (double)z): double rounding is innocuous for division,
   // so this equals the correctly rounded float quotient.
   const float invz = __fdiv_rn(1.0f, vcurr_p.z);
@@ -116,7 +118,7 @@ __device__ __forceinline__ bool icp_finish(const PoseF &p, const IcpProj &q, flo
   const float sine = norm(cross(ncurr_g, nlast_g));
   if (!(sine < 0.6f && dist <= 0.1f && !isnan(nc4.x) && !isnan(nl4.x))) return false;
   const f3 nlast = mul(p.RlI, nlast_g);
-  const f3 vcurr = mul(p.RlI, q.vg - p.tl);
+  const f3 vcurr = q.vp;  // mul(p.RlI, q.vg - p.tl), computed by icp_project
   const f3 vlast = mul(p.RlI, vlast_g - p.tl);
   const f3 mn = -nlast;
   const f3 cr = cross(nlast, vlast);
@@ -126,32 +128,59 @@ __device__ __forceinline__ bool icp_finish(const PoseF &p, const IcpProj &q, flo
   return true;
 }
 
+// The 28 products of the row, each fused into its running sum (one
+// rounding per term; the per-thread order of pixels is kept).
 __device__ __forceinline__ void icp_add_row(float acc[29], const float row[7]) {
   int k = 0;
 #pragma unroll
   for (int a = 0; a < 7; ++a)
 #pragma unroll
-    for (int b = a; b < 7; ++b) acc[k++] += row[a] * row[b];
+    for (int b = a; b < 7; ++b, ++k) acc[k] = fmaf(row[a], row[b], acc[k]);
   acc[28] += 1.0f;
 }
 
 // Accumulates the 29 terms (Reduction.cu:281-289) of this thread's pixels
-// i = gtid, gtid + gstride, ... in that order.
+// i = gtid, gtid + gstride, ... in that order.  Pixels go in batches of
+// kIcpBatch: the batch's current vertices are loaded together, then its
+// model gathers, so a thread waits for two memory round trips per batch
+// instead of two per pixel.
+#ifndef SF_ICP_BATCH
+#define SF_ICP_BATCH 2
+#endif
+constexpr int kIcpBatch = SF_ICP_BATCH;
+
 __device__ __forceinline__ void icp_accumulate(const IcpLevelArgs &L, const PoseF &p, int gtid,
                                                int gstride, float acc[29]) {
 #pragma unroll
   for (int k = 0; k < 29; ++k) acc[k] = 0.f;
   const int cols = L.vc.cols;
   const int N = cols * L.vc.rows;
-  for (int i = gtid; i < N; i += gstride) {
-    const int y = i / cols, x = i - y * cols;
-    const IcpProj q = icp_project(L, p, __ldg(row_ptr<const float4>(L.vc, y) + x));
-    if (!q.ok) continue;
-    const float4 vl = __ldg(row_ptr<const float4>(L.vl, q.v) + q.u);
-    const float4 nl = __ldg(row_ptr<const float4>(L.nl, q.v) + q.u);
-    const float4 nc = __ldg(row_ptr<const float4>(L.nc, y) + x);
-    float row[7];
-    if (icp_finish(p, q, vl, nl, nc, row)) icp_add_row(acc, row);
+  for (int i0 = gtid; i0 < N; i0 += kIcpBatch * gstride) {
+    float4 vc[kIcpBatch];
+    int xs[kIcpBatch], ys[kIcpBatch];
+#pragma unroll
+    for (int b = 0; b < kIcpBatch; ++b) {
+      const int i = i0 + b * gstride;
+      ys[b] = i / cols;
+      xs[b] = i - ys[b] * cols;
+      vc[b] = i < N ? __ldg(row_ptr<const float4>(L.vc, ys[b]) + xs[b]) : nan4();
+    }
+    IcpProj q[kIcpBatch];
+    float4 vl[kIcpBatch], nl[kIcpBatch], nc[kIcpBatch];
+#pragma unroll
+    for (int b = 0; b < kIcpBatch; ++b) {
+      q[b] = icp_project(L, p, vc[b]);
+      if (q[b].ok) {
+        vl[b] = __ldg(row_ptr<const float4>(L.vl, q[b].v) + q[b].u);
+        nl[b] = __ldg(row_ptr<const float4>(L.nl, q[b].v) + q[b].u);
+        nc[b] = __ldg(row_ptr<const float4>(L.nc, ys[b]) + xs[b]);
+      }
+    }
+#pragma unroll
+    for (int b = 0; b < kIcpBatch; ++b) {
+      float row[7];
+      if (q[b].ok && icp_finish(p, q[b], vl[b], nl[b], nc[b], row)) icp_add_row(acc, row);
+    }
   }
 }
 
@@ -387,7 +416,10 @@ __global__ void __launch_bounds__(kPThreads, 1) k_icp_persistent(PersistentArgs 
   }
   __syncthreads();
   const int nb = gridDim.x;
-  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  // Warp w of CTA b takes the 32-pixel runs w * nb + b (+ multiples of the
+  // grid): every CTA's work is spread over the whole image, which evens out
+  // the CTAs' arrival at the barrier; each warp's loads stay coalesced.
+  const int gtid = ((threadIdx.x >> 5) * nb + blockIdx.x) * 32 + (threadIdx.x & 31);
   const int gstride = nb * blockDim.x;
   int set = 0, it = 0;  // set = it % 3
   for (int l = a.levels - 1; l >= 0; --l) {

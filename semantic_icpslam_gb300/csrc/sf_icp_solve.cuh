@@ -25,7 +25,9 @@
 //    terms in FP64, the rest (below 1e-4 of the total, truncated below
 //    1e-20) in FP32, which keeps each coefficient within 1e-13 absolute.
 //    Larger angles take the trigonometric form.
-//  - pose products as FMA chains, one matrix element per lane.
+//  - the pose as next = next * exp(-x), which equals the reference's
+//    last * delta^-1 after delta = exp(x) delta (the accumulated delta is
+//    not kept), as FMA chains, one matrix element per lane.
 // Results agree with the host ctl_step to rounding (about 1e-15 relative
 // on well-conditioned systems); they are not bit-identical.
 #ifndef SF_ICP_SOLVE_CUH_
@@ -42,9 +44,8 @@ namespace sf {
 
 struct IcpSolveSmem {
   double a[6][8];    // augmented [A | b], row stride 8
-  double R[9];
-  double delta[12];  // updated delta (top 3 rows)
-  double dInv[12];   // its inverse (top 3 rows)
+  double R[9];       // rotation of exp(-x), row-major
+  double delta[12];  // translation of exp(-x); the acceptance gate's relative pose
 };
 
 // v * 2^sh by exponent arithmetic on the high word (no FP64 instruction).
@@ -198,8 +199,11 @@ __device__ bool ctl_step_fast(TrackCtl &c, const double *sums, int min_count, Ic
     c2 = (th - sn) / (th2 * th);
   }
   SF_SOLVE_MARK(3);
-  // R_ij = delta_ij + c_a W_ij + c_1 (w_i w_j - delta_ij t^2), lanes 0..8;
-  // W = [w]x: W01 = -w2, W02 = w1, W12 = -w0 and W^T = -W
+  // next = last * (exp(x) delta)^-1 = next * exp(x)^-1 = next * exp(-x):
+  // exp(-x) = [R^T | t'] with R^T_ij = R_ji = delta_ij - c_a W_ij +
+  // c_1 (w_i w_j - delta_ij t^2) (W = [w]x: W01 = -w2, W02 = w1, W12 = -w0,
+  // W^T = -W) in lanes 0..8, and t' = -(u - c_1 (w x u) + c_2 (w x (w x u)))
+  // (below 1e-10 rad Sophus's V is R, so t' = -R^T u) in lanes 0..2.
   {
     const int i = lane < 9 ? lane / 3 : 0, j = lane < 9 ? lane - 3 * (lane / 3) : 0;
     const int kk = 3 - i - j;  // the third axis when i != j
@@ -210,18 +214,16 @@ __device__ bool ctl_step_fast(TrackCtl &c, const double *sums, int min_count, Ic
     const double Wij = (i == j) ? 0.0 : (cyc ? -wk : wk);
     const double dl = (i == j) ? 1.0 : 0.0;
     const double w2ij = fma(-dl, th2, wi * wj);
-    const double r = fma(c1, w2ij, fma(ca, Wij, dl));
-    if (lane < 9) s.R[lane] = r;
+    const double r = fma(c1, w2ij, fma(-ca, Wij, dl));
+    if (lane < 9) s.R[lane] = r;  // R^T, row-major
   }
-  // t = u + c_1 (w x u) + c_2 (w x (w x u)); below 1e-10 rad Sophus uses
-  // V = R, so t = R u.  Lane i < 3 computes component i.
   double ti;
   const int ci = lane < 3 ? lane : 0;
   if (th2 < 1e-20) {
     __syncwarp();
-    ti = s.R[ci * 3 + 0] * u0;
-    ti = fma(s.R[ci * 3 + 1], u1, ti);
-    ti = fma(s.R[ci * 3 + 2], u2, ti);
+    ti = -(s.R[ci * 3 + 0] * u0);
+    ti = fma(-s.R[ci * 3 + 1], u1, ti);
+    ti = fma(-s.R[ci * 3 + 2], u2, ti);
   } else {
     // (cj, ck): the next two axes after ci, cyclically
     const int cj = ci == 2 ? 0 : ci + 1, ck = ci == 0 ? 2 : ci - 1;
@@ -231,55 +233,28 @@ __device__ bool ctl_step_fast(TrackCtl &c, const double *sums, int min_count, Ic
     const double a = fma(wj, uk, -(wk * uj));  // (w x u)_i
     const double aj = __shfl_sync(0xffffffffu, a, cj), ak = __shfl_sync(0xffffffffu, a, ck);
     const double b = fma(wj, ak, -(wk * aj));  // (w x (w x u))_i
-    ti = fma(c2, b, fma(c1, a, ui));
+    ti = fma(-c2, b, fma(c1, a, -ui));
   }
-  const double t0 = __shfl_sync(0xffffffffu, ti, 0);
-  const double t1 = __shfl_sync(0xffffffffu, ti, 1);
-  const double t2 = __shfl_sync(0xffffffffu, ti, 2);
+  if (lane < 3) s.delta[lane] = ti;  // t'
   __syncwarp();
   SF_SOLVE_MARK(4);
-  // delta = exp(x) * delta (top 3 rows; the bottom row stays 0 0 0 1)
+  // next_ij = sum_k next_ik exp(-x)_kj, lanes 0..11 (the bottom row stays)
+  double v = 0.0;
   if (lane < 12) {
     const int i = lane >> 2, j = lane & 3;
-    const double *D = c.delta;
-    double v = s.R[i * 3 + 0] * D[0 * 4 + j];
-    v = fma(s.R[i * 3 + 1], D[1 * 4 + j], v);
-    v = fma(s.R[i * 3 + 2], D[2 * 4 + j], v);
-    if (j == 3) v += (i == 0 ? t0 : (i == 1 ? t1 : t2));
-    s.delta[lane] = v;
-  }
-  __syncwarp();
-  if (lane < 12) c.delta[lane] = s.delta[lane];
-  // dInv = [D^T, -D^T t]
-  if (lane < 12) {
-    const int i = lane >> 2, j = lane & 3;
-    const double *D = s.delta;
-    double v;
+    const double *N = c.next_pose;
     if (j < 3) {
-      v = D[j * 4 + i];
+      v = N[i * 4 + 0] * s.R[0 * 3 + j];
+      v = fma(N[i * 4 + 1], s.R[1 * 3 + j], v);
+      v = fma(N[i * 4 + 2], s.R[2 * 3 + j], v);
     } else {
-      v = -(D[0 * 4 + i] * D[3]);
-      v = fma(-D[1 * 4 + i], D[7], v);
-      v = fma(-D[2 * 4 + i], D[11], v);
+      v = fma(N[i * 4 + 0], s.delta[0], N[i * 4 + 3]);
+      v = fma(N[i * 4 + 1], s.delta[1], v);
+      v = fma(N[i * 4 + 2], s.delta[2], v);
     }
-    s.dInv[lane] = v;
   }
   __syncwarp();
-  // next = last * dInv
-  if (lane < 16) {
-    const int i = lane >> 2, j = lane & 3;
-    double v;
-    if (i == 3) {
-      v = (j == 3) ? 1.0 : 0.0;
-    } else {
-      const double *L = c.last_pose;
-      v = L[i * 4 + 0] * s.dInv[0 * 4 + j];
-      v = fma(L[i * 4 + 1], s.dInv[1 * 4 + j], v);
-      v = fma(L[i * 4 + 2], s.dInv[2 * 4 + j], v);
-      if (j == 3) v += L[i * 4 + 3];
-    }
-    c.next_pose[lane] = v;
-  }
+  if (lane < 12) c.next_pose[lane] = v;
   __syncwarp();
   SF_SOLVE_MARK(5);
   return true;
