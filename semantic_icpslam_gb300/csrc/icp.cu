@@ -304,9 +304,18 @@ __device__ __forceinline__ void cross_block_sum(const double *part, int nb, int 
 // depend on which CTA arrives first and every CTA reads the same 29 values
 // once the barrier opens.  A fourth slot counts addends beyond 2^64 in
 // magnitude (or not finite); such a component reads as NaN.
+//
+// Atomics on one address serialise in L2: with all CTAs adding into one
+// set of 29 x 3 words, the adds and the fence behind them took ~4 us per
+// iteration on GB300.  CTA b therefore adds into group b % kFixGroups, and
+// readers sum the groups (integer sums, so still exact and order-free).
+// Eight groups measured as fast as sixteen (about 1 us over a bare grid
+// barrier) with half the reads.
 constexpr int kFixFrac = 60;
 constexpr int kLimbBits = 42;
 constexpr int kFixSlots = 4;  // limbs 0-2, out-of-range count
+constexpr int kFixGroups = 8;
+constexpr int kFixSet = kFixGroups * 29 * kFixSlots;  // words per accumulator set
 constexpr unsigned long long kLimbMask = (1ull << kLimbBits) - 1ull;
 
 __device__ __forceinline__ __int128 f32_to_fix(float f, bool &bad) {
@@ -337,11 +346,12 @@ __device__ __forceinline__ void fix_add(unsigned long long *d, float2 v) {
   if (bad) red_add_u64(d + 3, 1ull);
 }
 
-// The accumulated total of slots d as a double (one rounding when the
-// integer fits 64 bits, else at most two, relative 2^-52).
-__device__ __forceinline__ double fix_total(const unsigned long long *d) {
-  const unsigned long long a0 = __ldcg(d + 0), a1 = __ldcg(d + 1), a2 = __ldcg(d + 2);
-  if (__ldcg(d + 3) != 0ull) return __longlong_as_double(0x7ff8000000000000ll);
+// The total of the limb sums a0..a2 (and out-of-range count bad) as a
+// double (one rounding when the integer fits 64 bits, else at most two,
+// relative 2^-52).
+__device__ __forceinline__ double fix_total(unsigned long long a0, unsigned long long a1, unsigned long long a2,
+                                            unsigned long long bad) {
+  if (bad != 0ull) return __longlong_as_double(0x7ff8000000000000ll);
   const __int128 t = ((__int128)(long long)a2 << (2 * kLimbBits)) + ((__int128)a1 << kLimbBits) + (__int128)a0;
   const long long hi = (long long)(t >> 64);
   const unsigned long long lo = (unsigned long long)t;
@@ -355,7 +365,7 @@ struct PersistentArgs {
   int levels;
   float thresh;
   unsigned *arrivals;        // grid barrier count, zero at launch
-  unsigned long long *fix;   // [3][29][kFixSlots] accumulators, zero at launch
+  unsigned long long *fix;   // [3][kFixGroups][29][kFixSlots] accumulators, zero at launch
   TrackCtl *ctl;
   const double *last_pose;
   const int *run_flag;
@@ -409,6 +419,7 @@ __global__ void __launch_bounds__(kPThreads, 1) k_icp_persistent(PersistentArgs 
   __shared__ float2 bsum[29];
   __shared__ double sums[29];
   __shared__ ff wpart[kPWarps][33];
+  __shared__ unsigned long long sfix[kFixGroups * 29][kFixSlots];
   if (a.run_flag && *a.run_flag == 0) return;  // uniform across the grid
   if (threadIdx.x == 0) {
     ctl_begin(ctl, a.last_pose);
@@ -432,18 +443,32 @@ __global__ void __launch_bounds__(kPThreads, 1) k_icp_persistent(PersistentArgs 
       icp_accumulate(L, pose, gtid, gstride, acc);
       prof_mark(a, it, 1);
       block_reduce29<kPWarps>(acc, wpart, bsum);
-      unsigned long long *fx = a.fix + (size_t)set * 29 * kFixSlots;
-      if (threadIdx.x < 29) fix_add(fx + threadIdx.x * kFixSlots, bsum[threadIdx.x]);
+      unsigned long long *fx = a.fix + (size_t)set * kFixSet;
+      if (threadIdx.x < 29)
+        fix_add(fx + ((blockIdx.x % kFixGroups) * 29 + threadIdx.x) * kFixSlots, bsum[threadIdx.x]);
       prof_mark(a, it, 2);
       grid_barrier(a, nb, it);
       prof_mark(a, it, 3);
-      if (threadIdx.x < 29) sums[threadIdx.x] = fix_total(fx + threadIdx.x * kFixSlots);
+      for (int k = threadIdx.x; k < kFixGroups * 29; k += blockDim.x) {
+        const ulonglong2 *d = reinterpret_cast<const ulonglong2 *>(fx + (size_t)k * kFixSlots);
+        const ulonglong2 x = __ldcg(d), y = __ldcg(d + 1);
+        sfix[k][0] = x.x; sfix[k][1] = x.y; sfix[k][2] = y.x; sfix[k][3] = y.y;
+      }
+      __syncthreads();
+      if (threadIdx.x < 29) {
+        unsigned long long t[kFixSlots] = {0ull, 0ull, 0ull, 0ull};
+#pragma unroll
+        for (int g = 0; g < kFixGroups; ++g)
+#pragma unroll
+          for (int q = 0; q < kFixSlots; ++q) t[q] += sfix[g * 29 + threadIdx.x][q];
+        sums[threadIdx.x] = fix_total(t[0], t[1], t[2], t[3]);
+      }
       // Every CTA read the previous iteration's set before it arrived here,
       // so CTA 0 clears it for iteration it + 2; its clearing is released
       // with its next arrival, before anyone can add into it.
       const int prev = set == 0 ? 2 : set - 1;
-      if (blockIdx.x == 0 && threadIdx.x < 29 * kFixSlots)
-        __stcg(a.fix + (size_t)prev * 29 * kFixSlots + threadIdx.x, 0ull);
+      if (blockIdx.x == 0)
+        for (int k = threadIdx.x; k < kFixSet; k += blockDim.x) __stcg(a.fix + (size_t)prev * kFixSet + k, 0ull);
       __syncthreads();
       prof_mark(a, it, 4);
       if (threadIdx.x == 0)
@@ -486,7 +511,7 @@ __global__ void __launch_bounds__(kThreads) k_icp_reduce(const double *part, int
 
 }  // namespace
 
-constexpr size_t kBarrierBytes = 256 + sizeof(unsigned long long) * 3 * 29 * kFixSlots;
+constexpr size_t kBarrierBytes = 256 + sizeof(unsigned long long) * 3 * kFixSet;
 
 cudaError_t icp_persistent_reset(const IcpWorkspace &w, cudaStream_t s) {
   return cudaMemsetAsync(w.barrier, 0, kBarrierBytes, s);

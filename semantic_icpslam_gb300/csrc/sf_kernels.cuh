@@ -48,7 +48,7 @@ struct IcpWorkspace {
   double *partials = nullptr;  // [2][29][max_blocks]
   double *sums = nullptr;      // [29]
   unsigned *barrier = nullptr; // persistent kernel: arrival count, then (at +256 B) fix
-  unsigned long long *fix = nullptr;  // [3][29][4] fixed-point accumulators
+  unsigned long long *fix = nullptr;  // [3][8][29][4] fixed-point accumulators (sets, CTA groups)
   TrackCtl *ctl = nullptr;     // device copy of the tracking state
   int max_blocks = 0;          // co-resident CTAs of the persistent kernel
   int threads = 0;
