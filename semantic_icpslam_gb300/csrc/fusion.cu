@@ -142,48 +142,25 @@ __device__ int request_once(const FuseScratch &f, i3 p, unsigned epoch) {
 // Fusion::CreateBlocks (FuseMap.cu:92-132), probe pass.
 __global__ void k_alloc_probe(DevMap m, FuseScratch f, sf_image depth, const Cam *cam,
                               const int *run_flag, uint32_t *flags) {
-  if (run_flag && *run_flag == 0) return;
+  if (run_flag && *run_flag == 0) return;  // the same for every thread
   const Cam c = *cam;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  if (x >= depth.cols || y >= depth.rows) return;
-  const float dmin = m.c.depth_min, dmax = m.c.depth_max;
-  float z = row_ptr<const float>(depth, y)[x];
-  if (isnan(z) || z < dmin || z > dmax) return;
-  const float thresh = m.c.trunc_dist / 2.0f;
-  float z_near = fmaxf(dmin, z - thresh);
-  float z_far = fminf(dmax, z + thresh);
-  if (z_near >= z_far) return;
-  f3 pn = mk3(z_near * ((float)x - c.cx) * c.invfx, z_near * ((float)y - c.cy) * c.invfy, z_near);
-  f3 pf = mk3(z_far * ((float)x - c.cx) * c.invfx, z_far * ((float)y - c.cy) * c.invfy, z_far);
-  f3 pt_near = (mul(c.R, pn) + c.t) * m.c.voxel_size_inv;
-  f3 pt_far = (mul(c.R, pf) + c.t) * m.c.voxel_size_inv;
-  f3 dir = pt_far - pt_near;
-  float length = norm(dir);
-  // A non-finite pose would make the walk unbounded; such a pixel is skipped.
-  if (!(length < 65536.0f)) return;
-  // (int)ceil(2.0 * length): 2*length is exact in float.
-  int nSteps = (int)ceilf(2.0f * length);
-  dir = dir / (float)(nSteps - 1);
   const unsigned epoch = f.counters[2];
-  i3 last;
-  last.x = 0x7fffffff; last.y = 0; last.z = 0;
-  for (int i = 0; i < nSteps; ++i) {
-    i3 bp = vox2block(floor3(pt_near));
-    pt_near = pt_near + dir;
-    if (bp.x == last.x && bp.y == last.y && bp.z == last.z) continue;
-    last = bp;
-    if (find_block(m, bp) >= 0) continue;
+  // One block of the walk, in walk order: skip it if allocated, else
+  // request it once per frame and chain it into its bucket's pending list.
+  auto visit = [&](i3 bp, int found) {
+    if (found >= 0) return;
     if (bp.x < -32767 || bp.x > 32767 || bp.y < -32767 || bp.y > 32767 || bp.z < -32767 ||
         bp.z > 32767) {
       atomicOr(flags, SF_FLAG_COORD_RANGE);
-      continue;
+      return;
     }
     int r = request_once(f, bp, epoch);
-    if (r < 0) { atomicOr(flags, SF_FLAG_DEDUP_FULL); continue; }
-    if (r == 0) continue;
+    if (r < 0) { atomicOr(flags, SF_FLAG_DEDUP_FULL); return; }
+    if (r == 0) return;
     unsigned slot = atomicAdd(&f.counters[0], 1u);
-    if (slot >= f.pend_cap) { atomicOr(flags, SF_FLAG_PENDING_FULL); continue; }
+    if (slot >= f.pend_cap) { atomicOr(flags, SF_FLAG_PENDING_FULL); return; }
     int bucket = (int)hash_block(bp, m.c.num_buckets);
     f.pending[slot] = make_int4(bp.x, bp.y, bp.z, bucket);
     int prev = atomicExch(f.bucket_head + bucket, (int)slot);
@@ -192,6 +169,92 @@ __global__ void k_alloc_probe(DevMap m, FuseScratch f, sf_image depth, const Cam
       unsigned d = atomicAdd(&f.counters[1], 1u);
       f.dirty[d] = bucket;  // d < pend_cap: one dirty bucket per pending slot at most
     }
+  };
+  // The segment of the pixel's ray within trunc/2 of the measured depth,
+  // sampled at half-voxel steps (the walk of FuseMapColor's allocation).
+  int nSteps = 0;
+  f3 pt_near = mk3(0.f, 0.f, 0.f), dir = pt_near;
+  if (x < depth.cols && y < depth.rows) {
+    const float dmin = m.c.depth_min, dmax = m.c.depth_max;
+    const float z = row_ptr<const float>(depth, y)[x];
+    const float thresh = m.c.trunc_dist / 2.0f;
+    const float z_near = fmaxf(dmin, z - thresh);
+    const float z_far = fminf(dmax, z + thresh);
+    if (!isnan(z) && z >= dmin && z <= dmax && z_near < z_far) {
+      f3 pn = mk3(z_near * ((float)x - c.cx) * c.invfx, z_near * ((float)y - c.cy) * c.invfy, z_near);
+      f3 pf = mk3(z_far * ((float)x - c.cx) * c.invfx, z_far * ((float)y - c.cy) * c.invfy, z_far);
+      pt_near = (mul(c.R, pn) + c.t) * m.c.voxel_size_inv;
+      const f3 pt_far = (mul(c.R, pf) + c.t) * m.c.voxel_size_inv;
+      dir = pt_far - pt_near;
+      const float length = norm(dir);
+      // A non-finite pose would make the walk unbounded; such a pixel is skipped.
+      if (length < 65536.0f) {
+        // (int)ceil(2.0 * length): 2*length is exact in float.
+        nSteps = (int)ceilf(2.0f * length);
+        dir = dir / (float)(nSteps - 1);
+      }
+    }
+  }
+  // The walk visits each run of samples in one block once.  The first
+  // kAllocAhead distinct blocks are collected first (a ray through the
+  // truncation band crosses two to four blocks).  Neighbouring pixels'
+  // rays cross the same blocks, so within a warp only the lowest lane
+  // holding a given block at a given position of its walk looks it up and
+  // visits it (visits are idempotent within a frame: the others would find
+  // it requested); the leaders' bucket entries are loaded together.  A
+  // longer walk goes on block by block from where the collection stopped.
+  constexpr int kAllocAhead = 4;
+  i3 blk[kAllocAhead];
+  int nblk = 0, i = 0;
+  i3 last;
+  last.x = 0x7fffffff; last.y = 0; last.z = 0;
+  for (; i < nSteps; ++i) {
+    const i3 bp = vox2block(floor3(pt_near));
+    if (bp.x == last.x && bp.y == last.y && bp.z == last.z) {
+      pt_near = pt_near + dir;
+      continue;
+    }
+    if (nblk == kAllocAhead) break;  // step i is visited below
+#pragma unroll
+    for (int k = 0; k < kAllocAhead; ++k)
+      if (k == nblk) blk[k] = bp;
+    ++nblk;
+    last = bp;
+    pt_near = pt_near + dir;
+  }
+  const int lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31;
+  bool lead[kAllocAhead];
+  int4 head[kAllocAhead];
+  int off[kAllocAhead];
+#pragma unroll
+  for (int k = 0; k < kAllocAhead; ++k) {
+    const bool has = k < nblk;
+    const unsigned long long key =
+        has ? ((unsigned long long)(blk[k].x & 0x1fffff) | ((unsigned long long)(blk[k].y & 0x1fffff) << 21) |
+               ((unsigned long long)(blk[k].z & 0x1fffff) << 42))
+            : ~0ull;
+    const unsigned same = __match_any_sync(0xffffffffu, key);
+    const int src = __ffs(same) - 1;
+    const int lx = __shfl_sync(0xffffffffu, blk[k].x, src), ly = __shfl_sync(0xffffffffu, blk[k].y, src),
+              lz = __shfl_sync(0xffffffffu, blk[k].z, src);
+    // a key shared by two different blocks (coordinates 2^21 blocks apart)
+    // leaves both lanes leading
+    lead[k] = has && (src == lane || lx != blk[k].x || ly != blk[k].y || lz != blk[k].z);
+    if (lead[k]) {
+      const sf_hash_entry *e = m.entries + hash_block(blk[k], m.c.num_buckets);
+      head[k] = entry_head(e);
+      off[k] = entry_offset(e);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < kAllocAhead; ++k)
+    if (lead[k]) visit(blk[k], find_block_from(m, blk[k], head[k], off[k]));
+  for (; i < nSteps; ++i) {
+    i3 bp = vox2block(floor3(pt_near));
+    pt_near = pt_near + dir;
+    if (bp.x == last.x && bp.y == last.y && bp.z == last.z) continue;
+    last = bp;
+    visit(bp, find_block(m, bp));
   }
 }
 

@@ -123,21 +123,23 @@ __device__ __forceinline__ int4 entry_head(const sf_hash_entry *e) { return __ld
 __device__ __forceinline__ int entry_offset(const sf_hash_entry *e) { return __ldcg(&e->offset); }
 
 // DeviceMap::FindEntry (DeviceMap.cu:141-154).  Returns ptr (>= 0) or -1.
-__device__ __forceinline__ int find_block(const DevMap &m, i3 p) {
-  uint32_t b = hash_block(p, m.c.num_buckets);
-  const sf_hash_entry *e = m.entries + b;
-  int4 h = entry_head(e);
+// The lookup given the head and offset of p's bucket entry, already loaded
+// (so that several lookups can have their first loads in flight at once).
+__device__ __forceinline__ int find_block_from(const DevMap &m, i3 p, int4 h, int off) {
   if (h.w != -1 && h.x == p.x && h.y == p.y && h.z == p.z) return h.w;
-  int off = entry_offset(e);
   int guard = 0;
   while (off > 0) {
-    e = m.entries + (m.c.num_buckets + (uint32_t)off - 1u);
+    const sf_hash_entry *e = m.entries + (m.c.num_buckets + (uint32_t)off - 1u);
     h = entry_head(e);
     if (h.x == p.x && h.y == p.y && h.z == p.z && h.w != -1) return h.w;
     off = entry_offset(e);
     if (++guard > (int)m.c.num_excess) break;  // corrupted chain: stop
   }
   return -1;
+}
+__device__ __forceinline__ int find_block(const DevMap &m, i3 p) {
+  const sf_hash_entry *e = m.entries + hash_block(p, m.c.num_buckets);
+  return find_block_from(m, p, entry_head(e), entry_offset(e));
 }
 
 // ------------------------------------------------------- device flags
