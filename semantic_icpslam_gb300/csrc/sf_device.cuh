@@ -97,9 +97,12 @@ struct DevMap {
 
 // DeviceMap::Hash (Mapping/DeviceMap.cu:3-10).  NumBuckets is unsigned, so
 // the signed product-xor is taken modulo NumBuckets as an unsigned value.
+// A power-of-two bucket count (every shipped map size) takes the mask,
+// which equals the remainder and avoids the ~20-instruction integer
+// division; any other count divides.
 __device__ __forceinline__ uint32_t hash_block(i3 p, uint32_t nb) {
   uint32_t h = ((uint32_t)p.x * 73856093u) ^ ((uint32_t)p.y * 19349669u) ^ ((uint32_t)p.z * 83492791u);
-  return h % nb;
+  return (nb & (nb - 1u)) == 0u ? (h & (nb - 1u)) : h % nb;
 }
 // voxelPosToBlockPos (DeviceMap.cu:169-180)
 __device__ __forceinline__ i3 vox2block(i3 v) {
