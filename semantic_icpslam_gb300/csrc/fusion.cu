@@ -120,7 +120,7 @@ __device__ __forceinline__ unsigned long long req_key(i3 p, unsigned epoch) {
 
 // Enters p into the request set.  Returns 1 if this thread entered it
 // first, 0 if it was already requested this epoch, -1 if the set is full.
-__device__ int request_once(const FuseScratch &f, i3 p, unsigned epoch) {
+__device__ __forceinline__ int request_once(const FuseScratch &f, i3 p, unsigned epoch) {
   const unsigned long long key = req_key(p, epoch);
   uint32_t h = ((uint32_t)p.x * 0x9E3779B1u) ^ ((uint32_t)p.y * 0x85EBCA77u) ^ ((uint32_t)p.z * 0xC2B2AE3Du);
   h ^= h >> 15;
@@ -140,36 +140,43 @@ __device__ int request_once(const FuseScratch &f, i3 p, unsigned epoch) {
 }
 
 // Fusion::CreateBlocks (FuseMap.cu:92-132), probe pass.
-__global__ void k_alloc_probe(DevMap m, FuseScratch f, sf_image depth, const Cam *cam,
+// One block of the allocation walk: skip it if allocated (found >= 0),
+// else request it once per frame and chain it into its bucket's pending
+// list.
+__device__ __forceinline__ void alloc_visit(const DevMap &m, const FuseScratch &f, uint32_t *flags,
+                                            unsigned epoch, i3 bp, int found) {
+  if (found >= 0) return;
+  if (bp.x < -32767 || bp.x > 32767 || bp.y < -32767 || bp.y > 32767 || bp.z < -32767 ||
+      bp.z > 32767) {
+    atomicOr(flags, SF_FLAG_COORD_RANGE);
+    return;
+  }
+  int r = request_once(f, bp, epoch);
+  if (r < 0) { atomicOr(flags, SF_FLAG_DEDUP_FULL); return; }
+  if (r == 0) return;
+  unsigned slot = atomicAdd(&f.counters[0], 1u);
+  if (slot >= f.pend_cap) { atomicOr(flags, SF_FLAG_PENDING_FULL); return; }
+  int bucket = (int)hash_block(bp, m.c.num_buckets);
+  f.pending[slot] = make_int4(bp.x, bp.y, bp.z, bucket);
+  int prev = atomicExch(f.bucket_head + bucket, (int)slot);
+  f.pending_next[slot] = prev;
+  if (prev == -1) {
+    unsigned d = atomicAdd(&f.counters[1], 1u);
+    f.dirty[d] = bucket;  // d < pend_cap: one dirty bucket per pending slot at most
+  }
+}
+
+constexpr int kAllocThreads = 256;  // a 32x8 tile of pixels per CTA
+
+__global__ void __launch_bounds__(kAllocThreads, 5) k_alloc_probe(DevMap m, FuseScratch f, sf_image depth,
+                                                               const Cam *cam,
                               const int *run_flag, uint32_t *flags) {
   if (run_flag && *run_flag == 0) return;  // the same for every thread
   const Cam c = *cam;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const unsigned epoch = f.counters[2];
-  // One block of the walk, in walk order: skip it if allocated, else
-  // request it once per frame and chain it into its bucket's pending list.
-  auto visit = [&](i3 bp, int found) {
-    if (found >= 0) return;
-    if (bp.x < -32767 || bp.x > 32767 || bp.y < -32767 || bp.y > 32767 || bp.z < -32767 ||
-        bp.z > 32767) {
-      atomicOr(flags, SF_FLAG_COORD_RANGE);
-      return;
-    }
-    int r = request_once(f, bp, epoch);
-    if (r < 0) { atomicOr(flags, SF_FLAG_DEDUP_FULL); return; }
-    if (r == 0) return;
-    unsigned slot = atomicAdd(&f.counters[0], 1u);
-    if (slot >= f.pend_cap) { atomicOr(flags, SF_FLAG_PENDING_FULL); return; }
-    int bucket = (int)hash_block(bp, m.c.num_buckets);
-    f.pending[slot] = make_int4(bp.x, bp.y, bp.z, bucket);
-    int prev = atomicExch(f.bucket_head + bucket, (int)slot);
-    f.pending_next[slot] = prev;
-    if (prev == -1) {
-      unsigned d = atomicAdd(&f.counters[1], 1u);
-      f.dirty[d] = bucket;  // d < pend_cap: one dirty bucket per pending slot at most
-    }
-  };
+  auto visit = [&](i3 bp, int found) { alloc_visit(m, f, flags, epoch, bp, found); };
   // The segment of the pixel's ray within trunc/2 of the measured depth,
   // sampled at half-voxel steps (the walk of FuseMapColor's allocation).
   int nSteps = 0;
@@ -202,26 +209,55 @@ __global__ void k_alloc_probe(DevMap m, FuseScratch f, sf_image depth, const Cam
   // holding a given block at a given position of its walk looks it up and
   // visits it (visits are idempotent within a frame: the others would find
   // it requested); the leaders' bucket entries are loaded together.  A
-  // longer walk goes on block by block from where the collection stopped.
+  // longer walk visits its further blocks as it meets them.
+  //
+  // Samples step by about half a voxel, so the walk tracks its block's
+  // voxel bounds [8b, 8b + 8) and moves b by one per axis when a sample
+  // leaves them: floor(floor(p) / 8) = b iff 8b <= p < 8b + 8, and the
+  // bounds are exact floats while |b| < 2^20 (otherwise, or for the first
+  // sample, the block comes from vox2block(floor3(p)) as in the reference).
+  // Float-to-int conversions thus run once per ray, not once per sample.
   constexpr int kAllocAhead = 4;
-  i3 blk[kAllocAhead];
-  int nblk = 0, i = 0;
-  i3 last;
-  last.x = 0x7fffffff; last.y = 0; last.z = 0;
-  for (; i < nSteps; ++i) {
-    const i3 bp = vox2block(floor3(pt_near));
-    if (bp.x == last.x && bp.y == last.y && bp.z == last.z) {
+  __shared__ i3 s_blk[kAllocThreads][kAllocAhead];
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  int nblk = 0;
+  {
+    i3 last;
+    last.x = 0x7fffffff; last.y = 0; last.z = 0;
+    f3 lo = mk3(1.f, 1.f, 1.f), hi = mk3(0.f, 0.f, 0.f);  // empty: no exact bounds
+    bool exact = false;
+    for (int i = 0; i < nSteps; ++i) {
+      const f3 p = pt_near;
       pt_near = pt_near + dir;
-      continue;
+      i3 bp;
+      if (exact) {
+        const int dx = (int)(p.x >= hi.x) - (int)(p.x < lo.x);
+        const int dy = (int)(p.y >= hi.y) - (int)(p.y < lo.y);
+        const int dz = (int)(p.z >= hi.z) - (int)(p.z < lo.z);
+        if ((dx | dy | dz) == 0) continue;
+        bp.x = last.x + dx; bp.y = last.y + dy; bp.z = last.z + dz;
+      } else {
+        bp = vox2block(floor3(p));
+        if (bp.x == last.x && bp.y == last.y && bp.z == last.z) continue;
+      }
+      last = bp;
+      const int lim = 1 << 20;
+      exact = bp.x > -lim && bp.x < lim && bp.y > -lim && bp.y < lim && bp.z > -lim && bp.z < lim;
+      if (exact) {
+        lo = mk3((float)(8 * bp.x), (float)(8 * bp.y), (float)(8 * bp.z));
+        hi = mk3((float)(8 * bp.x + 8), (float)(8 * bp.y + 8), (float)(8 * bp.z + 8));
+      }
+      if (nblk < kAllocAhead) {
+        s_blk[tid][nblk] = bp;
+        ++nblk;
+      } else {
+        visit(bp, find_block(m, bp));  // a fifth block or later (rare)
+      }
     }
-    if (nblk == kAllocAhead) break;  // step i is visited below
-#pragma unroll
-    for (int k = 0; k < kAllocAhead; ++k)
-      if (k == nblk) blk[k] = bp;
-    ++nblk;
-    last = bp;
-    pt_near = pt_near + dir;
   }
+  i3 blk[kAllocAhead];
+#pragma unroll
+  for (int k = 0; k < kAllocAhead; ++k) blk[k] = s_blk[tid][k];
   const int lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31;
   bool lead[kAllocAhead];
   int4 head[kAllocAhead];
@@ -249,13 +285,6 @@ __global__ void k_alloc_probe(DevMap m, FuseScratch f, sf_image depth, const Cam
 #pragma unroll
   for (int k = 0; k < kAllocAhead; ++k)
     if (lead[k]) visit(blk[k], find_block_from(m, blk[k], head[k], off[k]));
-  for (; i < nSteps; ++i) {
-    i3 bp = vox2block(floor3(pt_near));
-    pt_near = pt_near + dir;
-    if (bp.x == last.x && bp.y == last.y && bp.z == last.z) continue;
-    last = bp;
-    visit(bp, find_block(m, bp));
-  }
 }
 
 // DeviceMap::CreateEntry (DeviceMap.cu:12-21).
