@@ -44,6 +44,7 @@ namespace sf {
 
 struct IcpSolveSmem {
   double a[6][8];    // augmented [A | b], row stride 8
+  int code, copy_cand;  // the stop decision of ctl_decide
   double R[9];       // rotation of exp(-x), row-major
   double delta[12];  // translation of exp(-x); the acceptance gate's relative pose
 };
@@ -121,55 +122,56 @@ __device__ __forceinline__ void warp_solve6(const double *sums, double x[6], Icp
   for (int i = 0; i < 6; ++i) x[i] = __shfl_sync(0xffffffffu, xi, i);
 }
 
-// One iteration given the 29 sums in shared memory; all 32 lanes of the
-// calling warp.  Same contract and state transitions as sf::ctl_step.
-__device__ bool ctl_step_fast(TrackCtl &c, const double *sums, int min_count, IcpSolveSmem &s) {
-  const int lane = threadIdx.x & 31;
-  SF_SOLVE_MARK(0);
-  int code = 0, copy_cand = 0;
-  if (lane == 0) {
-    c.iters_run++;
-    float residual0 = (float)sums[27], residual1 = (float)sums[28];
-    c.icpError = sqrtf(residual0) / residual1;
-    c.icpCount = (int)residual1;
-    if (isnan(c.icpError) || c.icpCount < min_count) {
-      c.stop = 1;
-      code = 1;
+// Tracker::ComputeSE3's per-iteration bookkeeping (Tracking.cc:449-479) for
+// one lane: the residual and inlier count, the stop tests and the
+// break-count / candidate logic.  Returns 0 to go on, 1 to stop on too few
+// inliers or a NaN error (next = last), 2 to stop on three rises in a row
+// (next = the candidate); *copy_cand asks for the current pose to become
+// the candidate first.
+__device__ __forceinline__ int ctl_decide(TrackCtl &c, const double *sums, int min_count, int *copy_cand) {
+  int code = 0;
+  *copy_cand = 0;
+  c.iters_run++;
+  float residual0 = (float)sums[27], residual1 = (float)sums[28];
+  c.icpError = sqrtf(residual0) / residual1;
+  c.icpCount = (int)residual1;
+  if (isnan(c.icpError) || c.icpCount < min_count) {
+    c.stop = 1;
+    code = 1;
+  } else {
+    const float rgbError = 0.f, wgt = 1e-4f;
+    float currError = rgbError * wgt + c.icpError;
+    if (c.lastError < currError) {
+      c.breakCount++;
+      *copy_cand = (c.breakCount == 1);
+      c.candidateICP = c.icpError;  // outside the inner if (Tracking.cc:463-465)
     } else {
-      const float rgbError = 0.f, wgt = 1e-4f;
-      float currError = rgbError * wgt + c.icpError;
-      if (c.lastError < currError) {
-        c.breakCount++;
-        copy_cand = (c.breakCount == 1);
-        c.candidateICP = c.icpError;  // outside the inner if (Tracking.cc:463-465)
-      } else {
-        c.breakCount = 0;
-      }
-      if (c.breakCount > 2) {
-        c.icpError = c.candidateICP;
-        c.stop = 2;
-        code = 2;
-      } else {
-        c.lastError = currError;
-      }
+      c.breakCount = 0;
+    }
+    if (c.breakCount > 2) {
+      c.icpError = c.candidateICP;
+      c.stop = 2;
+      code = 2;
+    } else {
+      c.lastError = currError;
     }
   }
-  code = __shfl_sync(0xffffffffu, code, 0);
-  copy_cand = __shfl_sync(0xffffffffu, copy_cand, 0);
-  __syncwarp();
-  if (copy_cand && lane < 16) c.candidate[lane] = c.next_pose[lane];
-  __syncwarp();
-  if (code == 1) {
-    if (lane < 16) c.next_pose[lane] = c.last_pose[lane];
-    __syncwarp();
-    return false;
-  }
-  if (code == 2) {
-    if (lane < 16) c.next_pose[lane] = c.candidate[lane];
-    __syncwarp();
-    return false;
-  }
+  return code;
+}
 
+// One iteration given the 29 sums in shared memory, run by threads 0..63
+// (two warps): lane 0 of warp 1 takes the stop decision while warp 0
+// solves and builds exp(-x), so the two overlap; after a named barrier,
+// warp 0 applies the decision (or the update).  Same contract and state
+// transitions as sf::ctl_step; warp 0 returns whether to go on.
+__device__ bool ctl_step_fast(TrackCtl &c, const double *sums, int min_count, IcpSolveSmem &s) {
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x >= 32) {  // warp 1
+    if (lane == 0) s.code = ctl_decide(c, sums, min_count, &s.copy_cand);
+    asm volatile("bar.sync 1, 64;" ::: "memory");
+    return false;
+  }
+  SF_SOLVE_MARK(0);
   SF_SOLVE_MARK(1);
   double x[6];
   warp_solve6(sums, x, s);
@@ -236,7 +238,22 @@ __device__ bool ctl_step_fast(TrackCtl &c, const double *sums, int min_count, Ic
     ti = fma(-c2, b, fma(c1, a, -ui));
   }
   if (lane < 3) s.delta[lane] = ti;  // t'
-  __syncwarp();
+  asm volatile("bar.sync 1, 64;" ::: "memory");
+  {
+    const int code = s.code;
+    if (s.copy_cand && lane < 16) c.candidate[lane] = c.next_pose[lane];
+    __syncwarp();
+    if (code == 1) {
+      if (lane < 16) c.next_pose[lane] = c.last_pose[lane];
+      __syncwarp();
+      return false;
+    }
+    if (code == 2) {
+      if (lane < 16) c.next_pose[lane] = c.candidate[lane];
+      __syncwarp();
+      return false;
+    }
+  }
   SF_SOLVE_MARK(4);
   // next_ij = sum_k next_ik exp(-x)_kj, lanes 0..11 (the bottom row stays)
   double v = 0.0;
