@@ -474,7 +474,7 @@ __global__ void __launch_bounds__(kPThreads, 1) k_icp_persistent(PersistentArgs 
       if (threadIdx.x == 0)
         s_solve_marks = (a.prof && blockIdx.x == 0 && it < kProfIters) ? a.prof + it * kProfSlots + 8 : nullptr;
       __syncwarp();
-      if (threadIdx.x < 64) ctl_step_fast(ctl, sums, L.min_count, ssolve);
+      if (threadIdx.x < 96) ctl_step_fast(ctl, sums, L.min_count, ssolve);
       __syncthreads();
       prof_mark(a, it, 5);
       set = set == 2 ? 0 : set + 1;

@@ -1,5 +1,5 @@
 // Per-iteration control, 6x6 solve and SE(3) update of the persistent ICP
-// kernel, run by one warp.
+// kernel, run by three warps.
 //
 // GB300's FP64 path is narrow: a warp has one FP64 instruction in flight
 // at a time, about 64 cycles each whether the next one depends on it or
@@ -9,8 +9,9 @@
 // sf::ctl_step (sf_solve.h), which restates Tracker::ComputeSE3
 // (Tracking/Tracking.cc:449-499), with as few FP64 instructions per warp as
 // it can:
-//  - A x = b by Gauss-Jordan elimination of the augmented 6x7 matrix, two
-//    elements per lane, two FP64 instructions per element and step.  The
+//  - A x = b by Gauss-Jordan elimination of the augmented 6x7 matrix, one
+//    element per thread over two warps (two schedulers issue their FP64
+//    updates side by side), two FP64 instructions per element and step.  The
 //    pivot order is LDLT's symmetric pivoting (largest remaining
 //    |diagonal|; every uneliminated row carries the same scale, so the
 //    comparison is LDLT's), a zero pivot zeroes its component as in the
@@ -43,7 +44,7 @@
 namespace sf {
 
 struct IcpSolveSmem {
-  double a[6][8];    // augmented [A | b], row stride 8
+  double a[2][6][8];  // augmented [A | b], row stride 8, double-buffered
   int code, copy_cand;  // the stop decision of ctl_decide
   double R[9];       // rotation of exp(-x), row-major
   double delta[12];  // translation of exp(-x); the acceptance gate's relative pose
@@ -65,33 +66,35 @@ __device__ __forceinline__ double scale_pow2(double v, int sh) {
 }
 
 // Solves A x = b for the 27 upper-triangle sums of CreateMatrix<6,7>
-// (Tracking/Reduction.cu:6-16); every lane returns x[0..5].  Lane l owns
-// elements e = l and e = l + 32 (< 42) of the row-major augmented matrix
-// (e = 7 i + j), keeps them in registers and mirrors them in s.a for the
-// other lanes' reads.  The pivot is found with one warp max over keys made
-// of the top 28 bits of |a_ii| (exponent and 17 mantissa bits) and 7 - i
-// in the low 3 bits: diagonals within 2^-17 of each other count as equal
-// and the lower index wins, as on an exact tie.
-__device__ __forceinline__ void warp_solve6(const double *sums, double x[6], IcpSolveSmem &s) {
-  const int lane = threadIdx.x & 31;
+// (Tracking/Reduction.cu:6-16), run by threads 0..63 (two warps, named
+// barrier 1); warp 0 returns x[0..5] in every lane.  Thread e < 42 owns
+// element e = 7 i + j of the row-major augmented matrix, keeps it in a
+// register and publishes it in s.a[buffer], double-buffered so that one
+// barrier per step separates a step's reads from the next step's writes;
+// the two warps' FP64 updates run on different schedulers side by side.
+// The pivot is found with one warp max over keys made of the top 28 bits
+// of |a_ii| (exponent and 17 mantissa bits) and 7 - i in the low 3 bits:
+// diagonals within 2^-17 of each other count as equal and the lower index
+// wins, as on an exact tie.
+__device__ __forceinline__ void solve6_two_warps(const double *sums, double x[6], IcpSolveSmem &s) {
+  const int lane = threadIdx.x & 31, e = threadIdx.x;
   auto sum_at = [&](int i, int j) {
     const int r = i < j ? i : j, q = i < j ? j : i;
     return j == 6 ? sums[7 * i - i * (i - 1) / 2 + (6 - i)] : sums[7 * r - r * (r - 1) / 2 + (q - r)];
   };
-  const int i0 = lane / 7, j0 = lane - 7 * (lane / 7);
-  const bool has1 = lane < 10;
-  const int i1 = has1 ? (lane + 32) / 7 : 5, j1 = has1 ? (lane + 32) - 7 * ((lane + 32) / 7) : 6;
-  double r0 = sum_at(i0, j0);
-  double r1 = has1 ? sum_at(i1, j1) : 0.0;
-  s.a[i0][j0] = r0;
-  if (has1) s.a[i1][j1] = r1;
-  __syncwarp();
+  const bool has = e < 42;
+  const int i0 = has ? e / 7 : 5, j0 = has ? e - 7 * (e / 7) : 6;
+  double r = has ? sum_at(i0, j0) : 0.0;
+  if (has) s.a[0][i0][j0] = r;
+  asm volatile("bar.sync 1, 64;" ::: "memory");
   unsigned done = 0, zero = 0;
+  int cur = 0;
 #pragma unroll 1
   for (int step = 0; step < 6; ++step) {
+    const double(*A)[8] = s.a[cur];
     unsigned key = 0;
     if (lane < 6 && !((done >> lane) & 1u)) {
-      const unsigned hi = (unsigned)__double2hiint(s.a[lane][lane]) & 0x7fffffffu;
+      const unsigned hi = (unsigned)__double2hiint(A[lane][lane]) & 0x7fffffffu;
       key = hi < 0x00100000u ? 0u : ((hi & ~7u) | (7u - lane));  // zero / subnormal: no pivot
     }
     const unsigned best = __reduce_max_sync(0xffffffffu, key);
@@ -101,23 +104,20 @@ __device__ __forceinline__ void warp_solve6(const double *sums, double x[6], Icp
     }
     const int k = 7 - (int)(best & 7u);
     done |= 1u << k;
-    const double akk = s.a[k][k];
+    const double akk = A[k][k];
     const int ek = (__double2hiint(akk) >> 20) & 0x7ff;
     const int sh = 1023 - ek;  // |akk| * 2^sh in [1, 2)
-    const double aik0 = s.a[i0][k], akj0 = s.a[k][j0];
-    const double aik1 = s.a[i1][k], akj1 = s.a[k][j1];
-    const double u0 = fma(akk, r0, -(aik0 * akj0));
-    const double u1 = fma(akk, r1, -(aik1 * akj1));
-    r0 = (i0 == k) ? r0 : ((j0 == k) ? 0.0 : scale_pow2(u0, sh));
-    r1 = (!has1 || i1 == k) ? r1 : ((j1 == k) ? 0.0 : scale_pow2(u1, sh));
-    __syncwarp();
-    s.a[i0][j0] = r0;
-    if (has1) s.a[i1][j1] = r1;
-    __syncwarp();
+    const double aik = A[i0][k], akj = A[k][j0];
+    const double u = fma(akk, r, -(aik * akj));
+    r = (i0 == k) ? r : ((j0 == k) ? 0.0 : scale_pow2(u, sh));
+    cur ^= 1;
+    if (has) s.a[cur][i0][j0] = r;
+    asm volatile("bar.sync 1, 64;" ::: "memory");
   }
+  if (threadIdx.x >= 32) return;
   // x_i = b_i / a_ii, the six divisions side by side in lanes 0..5
   const int row = lane < 6 ? lane : 0;
-  const double xi = ((zero >> row) & 1u) ? 0.0 : s.a[row][6] / s.a[row][row];
+  const double xi = ((zero >> row) & 1u) ? 0.0 : s.a[cur][row][6] / s.a[cur][row][row];
 #pragma unroll
   for (int i = 0; i < 6; ++i) x[i] = __shfl_sync(0xffffffffu, xi, i);
 }
@@ -159,22 +159,23 @@ __device__ __forceinline__ int ctl_decide(TrackCtl &c, const double *sums, int m
   return code;
 }
 
-// One iteration given the 29 sums in shared memory, run by threads 0..63
-// (two warps): lane 0 of warp 1 takes the stop decision while warp 0
-// solves and builds exp(-x), so the two overlap; after a named barrier,
-// warp 0 applies the decision (or the update).  Same contract and state
-// transitions as sf::ctl_step; warp 0 returns whether to go on.
+// One iteration given the 29 sums in shared memory, run by threads 0..95
+// (three warps): lane 0 of warp 2 takes the stop decision while warps 0
+// and 1 solve and warp 0 builds exp(-x), so the three overlap; after named
+// barrier 2, warp 0 applies the decision (or the update).  Same contract
+// and state transitions as sf::ctl_step; warp 0 returns whether to go on.
 __device__ bool ctl_step_fast(TrackCtl &c, const double *sums, int min_count, IcpSolveSmem &s) {
   const int lane = threadIdx.x & 31;
-  if (threadIdx.x >= 32) {  // warp 1
+  if (threadIdx.x >= 64) {  // warp 2
     if (lane == 0) s.code = ctl_decide(c, sums, min_count, &s.copy_cand);
-    asm volatile("bar.sync 1, 64;" ::: "memory");
+    asm volatile("bar.sync 2, 64;" ::: "memory");
     return false;
   }
   SF_SOLVE_MARK(0);
   SF_SOLVE_MARK(1);
   double x[6];
-  warp_solve6(sums, x, s);
+  solve6_two_warps(sums, x, s);
+  if (threadIdx.x >= 32) return false;  // warp 1
   SF_SOLVE_MARK(2);
   const double u0 = x[0], u1 = x[1], u2 = x[2];
   const double w0 = x[3], w1 = x[4], w2 = x[5];
@@ -238,7 +239,7 @@ __device__ bool ctl_step_fast(TrackCtl &c, const double *sums, int min_count, Ic
     ti = fma(-c2, b, fma(c1, a, -ui));
   }
   if (lane < 3) s.delta[lane] = ti;  // t'
-  asm volatile("bar.sync 1, 64;" ::: "memory");
+  asm volatile("bar.sync 2, 64;" ::: "memory");
   {
     const int code = s.code;
     if (s.copy_cand && lane < 16) c.candidate[lane] = c.next_pose[lane];
