@@ -114,9 +114,16 @@ __device__ __forceinline__ bool icp_finish(const PoseF &p, const IcpProj &q, flo
   const f3 vlast_g = mul(p.Rl, xyz(vl4)) + p.tl;
   const f3 ncurr_g = mul(p.Rc, xyz(nc4));
   const f3 nlast_g = mul(p.Rl, xyz(nl4));
-  const float dist = norm(vlast_g - q.vg);
-  const float sine = norm(cross(ncurr_g, nlast_g));
-  if (!(sine < 0.6f && dist <= 0.1f && !isnan(nc4.x) && !isnan(nl4.x))) return false;
+  // dist = norm(vlast_g - vg) <= 0.1f and sine = norm(ncurr_g x nlast_g)
+  // < 0.6f without the square roots: sqrtf is correctly rounded and
+  // monotone, so sqrtf(d) <= 0.1f iff d <= 0x3c23d70b (0.010000001f) and
+  // sqrtf(s) < 0.6f iff s < 0x3eb851ec (0.36f), the squared norms being
+  // the same dot products norm() takes.
+  const f3 dv = vlast_g - q.vg, cr_n = cross(ncurr_g, nlast_g);
+  const float dist2 = dot(dv, dv), sine2 = dot(cr_n, cr_n);
+  if (!(sine2 < __int_as_float(0x3eb851ec) && dist2 <= __int_as_float(0x3c23d70b) && !isnan(nc4.x) &&
+        !isnan(nl4.x)))
+    return false;
   const f3 nlast = mul(p.RlI, nlast_g);
   const f3 vcurr = q.vp;  // mul(p.RlI, q.vg - p.tl), computed by icp_project
   const f3 vlast = mul(p.RlI, vlast_g - p.tl);
@@ -155,14 +162,30 @@ __device__ __forceinline__ void icp_accumulate(const IcpLevelArgs &L, const Pose
   for (int k = 0; k < 29; ++k) acc[k] = 0.f;
   const int cols = L.vc.cols;
   const int N = cols * L.vc.rows;
+  // i / cols through the float reciprocal: for i < 2^24 the product's two
+  // roundings put it within (i / cols) 2^-23 < 1 of the quotient, so the
+  // truncated estimate is off by at most one, which the remainder test
+  // corrects.  Larger images divide.
+  const float inv_cols = 1.0f / (float)cols;
+  const bool small = N < (1 << 24) - kIcpBatch * gstride;
   for (int i0 = gtid; i0 < N; i0 += kIcpBatch * gstride) {
     float4 vc[kIcpBatch];
     int xs[kIcpBatch], ys[kIcpBatch];
 #pragma unroll
     for (int b = 0; b < kIcpBatch; ++b) {
       const int i = i0 + b * gstride;
-      ys[b] = i / cols;
-      xs[b] = i - ys[b] * cols;
+      int y, x;
+      if (small) {
+        y = (int)((float)i * inv_cols);
+        x = i - y * cols;
+        if (x < 0) { --y; x += cols; }
+        if (x >= cols) { ++y; x -= cols; }
+      } else {
+        y = i / cols;
+        x = i - y * cols;
+      }
+      ys[b] = y;
+      xs[b] = x;
       vc[b] = i < N ? __ldg(row_ptr<const float4>(L.vc, ys[b]) + xs[b]) : nan4();
     }
     IcpProj q[kIcpBatch];
