@@ -102,26 +102,124 @@ struct NormalOut {
   bool ok;
 };
 
+// One axis of readNormal's six interpolation points pt + e (e = (+-1, 0, 0)
+// and so on): the coordinate is v0 = p + 0 for the four points that do not
+// move along this axis and vP = p + 1, vM = p + (-1) for the two that do.
+// For each, readSdfInterped's corners are floor(v) and floor(v + 1) (the
+// reference's make_int3 floor of float sums) and its weight v - floorf(v).
+// The axis is regular when the corners chain up, floor(vM + 1) = floor(v0)
+// and floor(v0 + 1) = floor(vP), so that the six cubes use the four
+// coordinates c[0] = floor(vM) .. c[3] = floor(vP + 1) and at most two
+// blocks: c[0] >> 3 and c[3] >> 3 differ by at most one.
+struct NormalAxis {
+  int c[4];
+  float f0, fP, fM;
+  bool regular;
+};
+
+__device__ __forceinline__ int floor1(float a) {
+  const int b = (int)a;
+  return (float)b > a ? b - 1 : b;
+}
+
+__device__ __forceinline__ NormalAxis normal_axis(float p) {
+  NormalAxis n;
+  const float v0 = p + 0.0f, vP = p + 1.0f, vM = p + (-1.0f);
+  const int a0 = floor1(v0), b0 = floor1(v0 + 1.0f);
+  const int aP = floor1(vP), bP = floor1(vP + 1.0f);
+  const int aM = floor1(vM), bM = floor1(vM + 1.0f);
+  n.f0 = v0 - floorf(v0);
+  n.fP = vP - floorf(vP);
+  n.fM = vM - floorf(vM);
+  n.c[0] = aM; n.c[1] = a0; n.c[2] = b0; n.c[3] = bP;
+  n.regular = bM == a0 && b0 == aP && (unsigned)((bP >> 3) - (aM >> 3)) <= 1u;
+  return n;
+}
+
+// readSdfInterped's trilinear form on the eight corner values (c000 ..
+// c111 in the reference's order) with weights (fx, fy, fz).
+__device__ __forceinline__ float trilerp(float fx, float fy, float fz, float c000, float c100, float c010,
+                                         float c110, float c001, float c101, float c011, float c111) {
+  float r0 = (1.0f - fx) * c000 + fx * c100;
+  float r1 = (1.0f - fx) * c010 + fx * c110;
+  const float r2 = (1.0f - fy) * r0 + fy * r1;
+  r0 = (1.0f - fx) * c001 + fx * c101;
+  r1 = (1.0f - fx) * c011 + fx * c111;
+  const float r3 = (1.0f - fy) * r0 + fy * r1;
+  return (1.0f - fz) * r2 + fz * r3;
+}
+
 // Rendering::readNormal (RenderScene.cu:345-378).  The six interpolations
-// are independent, so all of them are issued before the reference's checks
-// run in its order (the early returns only decide the output).
+// (pt +- one voxel along each axis) read 48 corners, of which 32 are
+// distinct when every axis is regular (the usual case): the 2x2x2 cube
+// around pt and a 2x2 face beyond it on each side.  Those 32 voxels are
+// read once, through at most eight block lookups, and each interpolation
+// takes its corners from them with the reference's arithmetic and order;
+// otherwise the six interpolations run as readSdfInterped does.  The
+// reference's checks then run in its order (the early returns only decide
+// the output).
 __device__ __noinline__ NormalOut read_normal(const RayCtx r, f3 pt, const m3 Rinv) {
   NormalOut o;
   o.ok = false;
-  bool v0, v1, v2, v3, v4, v5;
-  const float s0 = sdf_interp(r, pt + mk3(1, 0, 0), v0);
-  const float s1 = sdf_interp(r, pt + mk3(-1, 0, 0), v1);
-  const float s2 = sdf_interp(r, pt + mk3(0, 1, 0), v2);
-  const float s3 = sdf_interp(r, pt + mk3(0, -1, 0), v3);
-  const float s4 = sdf_interp(r, pt + mk3(0, 0, 1), v4);
-  const float s5 = sdf_interp(r, pt + mk3(0, 0, -1), v5);
-  if (isnan(s0) || s0 == 1.0f || !v0) return o;
-  if (isnan(s1) || s1 == 1.0f || !v1) return o;
-  if (isnan(s2) || s2 == 1.0f || !v2) return o;
-  if (isnan(s3) || s3 == 1.0f || !v3) return o;
-  if (isnan(s4) || s4 == 1.0f || !v4) return o;
-  if (isnan(s5) || s5 == 1.0f || !v5) return o;
-  o.n = normalised(mul(Rinv, mk3(s0 - s1, s2 - s3, s4 - s5)));
+  const NormalAxis X = normal_axis(pt.x), Y = normal_axis(pt.y), Z = normal_axis(pt.z);
+  float s[6];
+  bool v[6];
+  if (X.regular && Y.regular && Z.regular) {
+    // block pointers of the (lo | hi)^3 blocks; a bit per axis picks hi
+    const int lx = X.c[0] >> 3, ly = Y.c[0] >> 3, lz = Z.c[0] >> 3;
+    const int hx = X.c[3] >> 3, hy = Y.c[3] >> 3, hz = Z.c[3] >> 3;
+    const bool sx = lx == hx, sy = ly == hy, sz = lz == hz;
+    int P[8];
+    P[0] = block_ptr(r, lx, ly, lz);
+    P[1] = sx ? P[0] : block_ptr(r, hx, ly, lz);
+    P[2] = sy ? P[0] : block_ptr(r, lx, hy, lz);
+    P[3] = sx ? P[2] : (sy ? P[1] : block_ptr(r, hx, hy, lz));
+    P[4] = sz ? P[0] : block_ptr(r, lx, ly, hz);
+    P[5] = sx ? P[4] : (sz ? P[1] : block_ptr(r, hx, ly, hz));
+    P[6] = sy ? P[4] : (sz ? P[2] : block_ptr(r, lx, hy, hz));
+    P[7] = sx ? P[6] : (sy ? P[5] : (sz ? P[3] : block_ptr(r, hx, hy, hz)));
+    // voxel (X.c[i], Y.c[j], Z.c[k])
+    auto vox = [&](int i, int j, int k) {
+      const int bi = (X.c[i] >> 3) != lx, bj = (Y.c[j] >> 3) != ly, bk = (Z.c[k] >> 3) != lz;
+      const int q0 = bj ? (bk ? P[6] : P[2]) : (bk ? P[4] : P[0]);
+      const int q1 = bj ? (bk ? P[7] : P[3]) : (bk ? P[5] : P[1]);
+      return voxel_in(r, bi ? q1 : q0, X.c[i], Y.c[j], Z.c[k]);
+    };
+    // the 2x2x2 cube (coordinates 1, 2 on every axis)
+    VoxelRead k000 = vox(1, 1, 1), k100 = vox(2, 1, 1), k010 = vox(1, 2, 1), k110 = vox(2, 2, 1);
+    VoxelRead k001 = vox(1, 1, 2), k101 = vox(2, 1, 2), k011 = vox(1, 2, 2), k111 = vox(2, 2, 2);
+    // faces beyond it: x = c[0] (xm) and c[3] (xp), the same for y and z
+    VoxelRead xm00 = vox(0, 1, 1), xm10 = vox(0, 2, 1), xm01 = vox(0, 1, 2), xm11 = vox(0, 2, 2);
+    VoxelRead xp00 = vox(3, 1, 1), xp10 = vox(3, 2, 1), xp01 = vox(3, 1, 2), xp11 = vox(3, 2, 2);
+    VoxelRead ym00 = vox(1, 0, 1), ym10 = vox(2, 0, 1), ym01 = vox(1, 0, 2), ym11 = vox(2, 0, 2);
+    VoxelRead yp00 = vox(1, 3, 1), yp10 = vox(2, 3, 1), yp01 = vox(1, 3, 2), yp11 = vox(2, 3, 2);
+    VoxelRead zm00 = vox(1, 1, 0), zm10 = vox(2, 1, 0), zm01 = vox(1, 2, 0), zm11 = vox(2, 2, 0);
+    VoxelRead zp00 = vox(1, 1, 3), zp10 = vox(2, 1, 3), zp01 = vox(1, 2, 3), zp11 = vox(2, 2, 3);
+    // +x: x corners c[2], c[3]; -x: c[0], c[1]; y, z corners c[1], c[2]
+    s[0] = trilerp(X.fP, Y.f0, Z.f0, k100.sdf, xp00.sdf, k110.sdf, xp10.sdf, k101.sdf, xp01.sdf, k111.sdf, xp11.sdf);
+    v[0] = xp11.found;
+    s[1] = trilerp(X.fM, Y.f0, Z.f0, xm00.sdf, k000.sdf, xm10.sdf, k010.sdf, xm01.sdf, k001.sdf, xm11.sdf, k011.sdf);
+    v[1] = k011.found;
+    s[2] = trilerp(X.f0, Y.fP, Z.f0, k010.sdf, k110.sdf, yp00.sdf, yp10.sdf, k011.sdf, k111.sdf, yp01.sdf, yp11.sdf);
+    v[2] = yp11.found;
+    s[3] = trilerp(X.f0, Y.fM, Z.f0, ym00.sdf, ym10.sdf, k000.sdf, k100.sdf, ym01.sdf, ym11.sdf, k001.sdf, k101.sdf);
+    v[3] = k101.found;
+    s[4] = trilerp(X.f0, Y.f0, Z.fP, k001.sdf, k101.sdf, k011.sdf, k111.sdf, zp00.sdf, zp10.sdf, zp01.sdf, zp11.sdf);
+    v[4] = zp11.found;
+    s[5] = trilerp(X.f0, Y.f0, Z.fM, zm00.sdf, zm10.sdf, zm01.sdf, zm11.sdf, k000.sdf, k100.sdf, k010.sdf, k110.sdf);
+    v[5] = k110.found;
+  } else {
+    s[0] = sdf_interp(r, pt + mk3(1, 0, 0), v[0]);
+    s[1] = sdf_interp(r, pt + mk3(-1, 0, 0), v[1]);
+    s[2] = sdf_interp(r, pt + mk3(0, 1, 0), v[2]);
+    s[3] = sdf_interp(r, pt + mk3(0, -1, 0), v[3]);
+    s[4] = sdf_interp(r, pt + mk3(0, 0, 1), v[4]);
+    s[5] = sdf_interp(r, pt + mk3(0, 0, -1), v[5]);
+  }
+#pragma unroll
+  for (int k = 0; k < 6; ++k)
+    if (isnan(s[k]) || s[k] == 1.0f || !v[k]) return o;
+  o.n = normalised(mul(Rinv, mk3(s[0] - s[1], s[2] - s[3], s[4] - s[5])));
   o.ok = true;
   return o;
 }
