@@ -123,8 +123,10 @@ def launches(sf):
     return v.value
 
 
-def time_device_resident(sf, ctx, frames, steps, warmup, mode, barrier, timing=False):
-    """Frames/s with inputs already in HBM; CUDA events on the system stream."""
+def time_device_resident(sf, ctx, frames, steps, warmup, mode, barrier, timing=False, autotune=False):
+    """Frames/s with inputs already in HBM; CUDA events on the system stream.
+    With autotune, sf_system_autotune runs half-way through the warm-up
+    (its choice is recaptured in the graph before the timed frames)."""
     import torch
     dev = [(torch.from_numpy(d).cuda(), torch.from_numpy(c).cuda()) for d, c, _, _ in frames[:steps + warmup]]
     torch.cuda.synchronize()
@@ -133,8 +135,13 @@ def time_device_resident(sf, ctx, frames, steps, warmup, mode, barrier, timing=F
     stats = []
     if timing:
         sf.call("sf_system_set_timing", s.h, 1)
+    tune = None
     for i in range(warmup):
         s.grab_device(dev[i][0].data_ptr(), dev[i][1].data_ptr())
+        if autotune and i == warmup // 2:
+            cands, chosen = s.autotune(reps=10)
+            tune = {"chosen": {"ctas_per_sm": cands[chosen][0], "tile": [cands[chosen][1], cands[chosen][2]]},
+                    "raycast_ms": {"%dx%d/%d" % (x, y, m): round(ms, 4) for m, x, y, ms in cands}}
     ctx.sync()
     stream = torch.cuda.ExternalStream(ctx.stream)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -162,7 +169,7 @@ def time_device_resident(sf, ctx, frames, steps, warmup, mode, barrier, timing=F
     s.close()
     del dev
     return dict(elapsed=elapsed, launches=n_launch, clocks=clocks, stage_ms=stage_ms / max(steps, 1),
-                stats=stats, last=last)
+                stats=stats, last=last, autotune=tune)
 
 
 def pinned(a):
@@ -378,6 +385,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--map-blocks", type=int, default=19,
                     help="log2 of the voxel-block heap (2^19 blocks = 4 GB of voxels)")
+    ap.add_argument("--autotune", action="store_true",
+                    help="run sf_system_autotune during the warm-up of the headline form and keep its choice")
     ap.add_argument("--quick", action="store_true",
                     help="only the CUDA-graph timing (for profiler runs)")
     args = ap.parse_args()
@@ -403,7 +412,7 @@ def main():
     frames = make_frames(n, rank)
 
     # headline: CUDA graph, inputs in HBM
-    g = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 1, barrier)
+    g = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 1, barrier, autotune=args.autotune)
     elapsed = g["elapsed"]
     if ws > 1:
         import torch.distributed as dist
@@ -420,6 +429,8 @@ def main():
                       "l2": "inputs larger than L2: a new frame per step from a %d-frame sequence resident in HBM "
                             "(%.0f MB); map state carried across frames as in the loop" % (n, n * COLS * ROWS * 5 / 1e6)},
            "gpu_launches": int(g["launches"]), "clocks": g["clocks"]}
+    if g["autotune"]:
+        out["autotune"] = g["autotune"]
 
     if args.quick:
         ctx.close()

@@ -347,6 +347,22 @@ int sf_system_get_map(sf_system *sys, sf_map **map);
 /* Stage timing with CUDA events on the system's stream (eager device form,
  * use_graph == 2): ms[7] = pyramid, ICP, allocation, visibility + z-range,
  * integration, raycast, resize + stats of the last frame. */
+/* Autotune (new entry point; no counterpart in the reference).  Times the
+ * raycast of the last grabbed frame under each of its launch shapes
+ * (registers sized for 8 or 6 CTAs per SM; 8x16, 16x8 or 32x4 pixel
+ * tiles), reps launches each, on the system's stream, and keeps the
+ * fastest for the following frames (a captured frame graph is re-captured).
+ * Every shape computes the same maps, and the timing runs rewrite the same
+ * model maps, so the loop's results do not change.  Needs one grabbed
+ * frame; 1 <= reps <= 1000.  report (may be NULL) receives the timings. */
+typedef struct {
+  int candidates;
+  int chosen;
+  float ms[16];
+  int minb[16], tile_x[16], tile_y[16];
+} sf_autotune_report;
+int sf_system_autotune(sf_system *sys, int reps, sf_autotune_report *report);
+
 int sf_system_set_timing(sf_system *sys, int enable);
 int sf_system_stage_ms(sf_system *sys, float ms[7]);
 /* Device pointers to the pose state: last (tracked) pose, double[16]. */

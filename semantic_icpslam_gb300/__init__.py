@@ -149,6 +149,15 @@ class System:
     def grab_device(self, depth_ptr, rgb_ptr, mask_ptr=None, num_detection=0):
         call("sf_system_grab_device", self.h, depth_ptr, rgb_ptr, mask_ptr, num_detection)
 
+    def autotune(self, reps=20):
+        """sf_system_autotune: times the last frame's raycast under each
+        launch shape and keeps the fastest.  Returns a list of
+        (minb, tile_x, tile_y, ms) per candidate and the chosen index."""
+        rep = _lib.AutotuneReport()
+        call("sf_system_autotune", self.h, int(reps), C.byref(rep))
+        cands = [(rep.minb[i], rep.tile_x[i], rep.tile_y[i], rep.ms[i]) for i in range(rep.candidates)]
+        return cands, rep.chosen
+
     def stats(self):
         st = FrameStats()
         call("sf_system_stats", self.h, C.byref(st))

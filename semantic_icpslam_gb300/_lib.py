@@ -75,6 +75,11 @@ class FrameStats(C.Structure):
                 ("flags", C.c_uint32), ("pose", C.c_double * 16)]
 
 
+class AutotuneReport(C.Structure):
+    _fields_ = [("candidates", C.c_int), ("chosen", C.c_int), ("ms", C.c_float * 16), ("minb", C.c_int * 16),
+                ("tile_x", C.c_int * 16), ("tile_y", C.c_int * 16)]
+
+
 class SynthConfig(C.Structure):
     _fields_ = [("scene", C.c_int), ("trajectory", C.c_int), ("cols", C.c_int), ("rows", C.c_int),
                 ("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float), ("cy", C.c_float),
@@ -138,6 +143,7 @@ SIGNATURES = {
     "sf_system_frame_maps": [vp, C.c_int, C.POINTER(Image), C.POINTER(Image), C.POINTER(Image)],
     "sf_system_get_map": [vp, pvp],
     "sf_system_set_timing": [vp, C.c_int],
+    "sf_system_autotune": [vp, C.c_int, C.POINTER(AutotuneReport)],
     "sf_system_stage_ms": [vp, F32P],
     "sf_system_pose_device": [vp, C.POINTER(C.POINTER(C.c_double))],
     "sf_synth_create": [C.POINTER(SynthConfig), pvp],

@@ -342,17 +342,16 @@ __device__ __forceinline__ void march_ray(const RayCtx &r, const Cam &c, float v
 // samples ahead at once, at the positions a run of 1-voxel steps would
 // reach (the same float additions), then replays the reference's loop over
 // them in order; an 8-voxel step or the end of the range ends the run.
-// Eight 128-thread CTAs per SM (64 registers): the march is latency-bound
-// and gains more from the extra warps than it loses to a few spilled
-// values (measured on GB300: 1, 6, 8, 12 and 16 CTAs per SM; 12 and more
-// spill too much).
-#ifndef SF_RC_MINB
-#define SF_RC_MINB 8
-#endif
-__global__ void __launch_bounds__(128, SF_RC_MINB) k_raycast(DevMap m, FuseScratch f, sf_image vmap, sf_image nmap,
-                                                 sf_image zmin, sf_image zmax, const Cam *cam,
-                                                 const unsigned *rendered, sf_image fb_v,
-                                                 sf_image fb_n, const int *run_flag) {
+// 128-thread CTAs with the registers sized for MINB of them per SM: the
+// march is latency-bound and gains more from the extra warps than it
+// loses to a few spilled values (measured on GB300: 6 and 8 per SM are
+// best, 10 and more spill too much); both are built and the autotuner
+// picks between them and among tile shapes.
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) k_raycast(DevMap m, FuseScratch f, sf_image vmap, sf_image nmap,
+                                                       sf_image zmin, sf_image zmax, const Cam *cam,
+                                                       const unsigned *rendered, sf_image fb_v,
+                                                       sf_image fb_n, const int *run_flag) {
   if (run_flag && *run_flag == 0) return;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -593,15 +592,29 @@ void launch_fill_blocks(const sf_image &zmin, const sf_image &zmax,
   k_fill_blocks<<<nblocks, dim3(16, 16), 0, s>>>(zmin, zmax, list, nblocks); note_launch();
 }
 
+RaycastTune raycast_tune(int i) {
+  static const int shapes[3][2] = {{8, 16}, {16, 8}, {32, 4}};
+  RaycastTune t;
+  t.minb = i < 3 ? 8 : 6;
+  t.tx = shapes[i % 3][0];
+  t.ty = shapes[i % 3][1];
+  return t;
+}
+
 void launch_raycast(const DevMap &m, const FuseScratch &f, const sf_image &vmap, const sf_image &nmap,
                     const sf_image &zmin, const sf_image &zmax, const Cam *c,
                     const unsigned *rendered, const sf_image *fallback_v,
-                    const sf_image *fallback_n, const int *run_flag, cudaStream_t s) {
-  dim3 blk(8, 16);
-  dim3 grd((vmap.cols + 7) / 8, (vmap.rows + 15) / 16);
+                    const sf_image *fallback_n, const int *run_flag, cudaStream_t s,
+                    const RaycastTune &tune) {
+  const dim3 blk(tune.tx, tune.ty);
+  const dim3 grd((vmap.cols + tune.tx - 1) / tune.tx, (vmap.rows + tune.ty - 1) / tune.ty);
   sf_image fv = fallback_v ? *fallback_v : sf_image{};
   sf_image fn = fallback_n ? *fallback_n : sf_image{};
-  k_raycast<<<grd, blk, 0, s>>>(m, f, vmap, nmap, zmin, zmax, c, rendered, fv, fn, run_flag); note_launch();
+  if (tune.minb == 6)
+    k_raycast<6><<<grd, blk, 0, s>>>(m, f, vmap, nmap, zmin, zmax, c, rendered, fv, fn, run_flag);
+  else
+    k_raycast<8><<<grd, blk, 0, s>>>(m, f, vmap, nmap, zmin, zmax, c, rendered, fv, fn, run_flag);
+  note_launch();
 }
 
 int raycast_adjoint_blocks(int cols, int rows) { return ((cols + 7) / 8) * ((rows + 15) / 16); }

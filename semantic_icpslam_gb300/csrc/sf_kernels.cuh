@@ -133,10 +133,20 @@ void launch_fill_blocks(const sf_image &zmin, const sf_image &zmax,
 // Rendering (RenderScene.cu:291-489).  fallback_v/n (may be null): when
 // *rendered == 0 the output is a copy of the fallback maps (the reference
 // skips the raycast and keeps the frame's own maps).
+// Launch shape of the raycast: CTAs per SM the registers are sized for
+// (minb) and the pixel tile of a 128-thread CTA.  Every shape computes the
+// same maps; sf_system_autotune picks the fastest on the device at hand.
+struct RaycastTune {
+  int minb = 8;
+  int tx = 8, ty = 16;
+};
+constexpr int kRaycastTunes = 6;
+RaycastTune raycast_tune(int i);  // candidate i < kRaycastTunes; 0 is the default
 void launch_raycast(const DevMap &m, const FuseScratch &f, const sf_image &vmap, const sf_image &nmap,
                     const sf_image &zmin, const sf_image &zmax, const Cam *c,
                     const unsigned *rendered, const sf_image *fallback_v,
-                    const sf_image *fallback_n, const int *run_flag, cudaStream_t s);
+                    const sf_image *fallback_n, const int *run_flag, cudaStream_t s,
+                    const RaycastTune &tune = RaycastTune());
 // RaycastAdjoint: gradients of launch_raycast's maps w.r.t. the pose (left
 // se(3) perturbation, 6 doubles into pose_out) and TSDF values (added into
 // grad_sdf, one float per voxel index; may be null).  pose_part holds

@@ -151,6 +151,9 @@ struct sf_system {
   // stage timing (eager form only): events at the stage boundaries
   int timing = 0;
   cudaEvent_t ev[8] = {};
+  // raycast launch shape (sf_system_autotune)
+  RaycastTune rc_tune;
+  long long frames = 0;  // frames run (any form)
 };
 
 namespace {
@@ -262,7 +265,7 @@ void enqueue_mapping(sf_system *s, const Cam *cam, const int *run, int num_detec
   mark(s, st, 5);
   sf_image fv = img(s->d_vmap[0], C, R, 16), fn = img(s->d_nmap[0], C, R, 16);
   launch_raycast(m, f, img(s->d_mv[0], C, R, 16), img(s->d_mn[0], C, R, 16), zmin, zmax, cam,
-                 f.counters + 3, &fv, &fn, run, st);
+                 f.counters + 3, &fv, &fn, run, st, s->rc_tune);
   mark(s, st, 6);
   for (int l = 1; l < s->L; ++l)
     launch_resize(img(s->d_mv[l - 1], C >> (l - 1), R >> (l - 1), 16),
@@ -379,7 +382,7 @@ int run_plain_frame(sf_system *s, int num_detection) {
                        nullptr, st);
     sf_image fv = img(s->d_vmap[0], C, R, 16), fn = img(s->d_nmap[0], C, R, 16);
     launch_raycast(m, f, img(s->d_mv[0], C, R, 16), img(s->d_mn[0], C, R, 16), zmin, zmax, cam,
-                   f.counters + 3, &fv, &fn, nullptr, st);
+                   f.counters + 3, &fv, &fn, nullptr, st, s->rc_tune);
     for (int l = 1; l < s->L; ++l)
       launch_resize(img(s->d_mv[l - 1], C >> (l - 1), R >> (l - 1), 16),
                     img(s->d_mn[l - 1], C >> (l - 1), R >> (l - 1), 16),
@@ -391,6 +394,7 @@ int run_plain_frame(sf_system *s, int num_detection) {
 
 int run_frame(sf_system *s, int num_detection) {
   cudaStream_t st = ctx_stream(s->ctx);
+  ++s->frames;
   if (s->cfg.use_graph == 0) return run_plain_frame(s, num_detection);
   if (s->cfg.use_graph == 2) {  // eager device-driven
     return enqueue_device_frame(s, num_detection, st) == cudaSuccess ? SF_OK : SF_ERR_CUDA;
@@ -522,6 +526,63 @@ int sf_system_grab_device(sf_system *s, const uint16_t *depth, const uint8_t *rg
       cudaMemcpyAsync(s->d_mask, mask, np, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
     return SF_ERR_CUDA;
   return run_frame(s, num_detection);
+}
+
+int sf_system_autotune(sf_system *s, int reps, sf_autotune_report *report) {
+  if (!s || reps < 1 || reps > 1000) return SF_ERR_INVALID;
+  if (s->frames < 1) return SF_ERR_INVALID;  // needs one grabbed frame: the model maps' inputs
+  cudaStream_t st = ctx_stream(s->ctx);
+  const int C = s->cfg.cols, R = s->cfg.rows;
+  DevMap &m = map_dev(s->map);
+  FuseScratch &f = map_scratch(s->map);
+  const sf_image mv = img(s->d_mv[0], C, R, 16), mn = img(s->d_mn[0], C, R, 16);
+  const sf_image zmin = img(s->d_zmin, s->zc, s->zr, 4), zmax = img(s->d_zmax, s->zc, s->zr, 4);
+  const sf_image fv = img(s->d_vmap[0], C, R, 16), fn = img(s->d_nmap[0], C, R, 16);
+  const Cam *cam = dev_field<Cam>(s->d_sys, offsetof(SysDev, cam));
+  const int *run = dev_field<int>(s->d_sys, offsetof(SysDev, run));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    if (e0) cudaEventDestroy(e0);
+    return SF_ERR_CUDA;
+  }
+  // The last frame's raycast again, with each shape: its inputs are
+  // unchanged, so it rewrites the same model maps and the loop's state is
+  // untouched.
+  sf_autotune_report rep;
+  memset(&rep, 0, sizeof(rep));
+  rep.candidates = kRaycastTunes;
+  int best = 0;
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < kRaycastTunes && e == cudaSuccess; ++i) {
+    const RaycastTune t = raycast_tune(i);
+    launch_raycast(m, f, mv, mn, zmin, zmax, cam, f.counters + 3, &fv, &fn, run, st, t);  // warm-up
+    cudaEventRecord(e0, st);
+    for (int k = 0; k < reps; ++k)
+      launch_raycast(m, f, mv, mn, zmin, zmax, cam, f.counters + 3, &fv, &fn, run, st, t);
+    cudaEventRecord(e1, st);
+    e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    rep.ms[i] = ms / (float)reps;
+    rep.minb[i] = t.minb;
+    rep.tile_x[i] = t.tx;
+    rep.tile_y[i] = t.ty;
+    if (rep.ms[i] < rep.ms[best]) best = i;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (e != cudaSuccess) return SF_ERR_CUDA;
+  rep.chosen = best;
+  const RaycastTune t = raycast_tune(best);
+  if (t.minb != s->rc_tune.minb || t.tx != s->rc_tune.tx || t.ty != s->rc_tune.ty) {
+    s->rc_tune = t;
+    if (s->gexec) {  // recaptured with the new shape on the next frame
+      cudaGraphExecDestroy(s->gexec);
+      s->gexec = nullptr;
+    }
+  }
+  if (report) *report = rep;
+  return SF_OK;
 }
 
 int sf_system_stats(sf_system *s, sf_frame_stats *stats) {
