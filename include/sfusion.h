@@ -36,7 +36,8 @@ enum {
   SF_ERR_TIMEOUT = 4,   /* a bounded device wait gave up                   */
   SF_ERR_NO_DEVICE = 5, /* no CUDA device                                  */
   SF_ERR_STATE = 6,     /* call not valid in the object's current state    */
-  SF_ERR_TOO_LARGE = 7  /* input beyond a fixed buffer's stated maximum    */
+  SF_ERR_TOO_LARGE = 7, /* input beyond a fixed buffer's stated maximum    */
+  SF_ERR_IO = 8         /* a file could not be opened, read or written     */
 };
 
 /* ----------------------------------------------------------- POD layouts */
@@ -131,6 +132,22 @@ int sf_map_rebuild_index(sf_context *ctx, sf_map *map);
 /* Host copies of the map's counters: heapCounter, entryPtr, visible count,
  * allocated (ptr >= 0) entry count. */
 int sf_map_counters(sf_context *ctx, const sf_map *map, int out[4]);
+/* map.bin, byte for byte as System::WriteMapToDisk writes it
+ * (Core/System.cc:327-361, arrays of Mapping::DownloadToRAM,
+ * Mapping/Mapping.cc:220-235): four ints NumSdfBlocks, NumBuckets,
+ * NumVoxels, NumEntries; heapCounter, entryPtr (hashCounter), noVisibleBlocks;
+ * heapMem, bucketMutex, the voxels (16 B each), hashEntries and
+ * visibleEntries (32 B each); then the keypoint map (KeyMap::MaxKeys mutex
+ * ints and KeyMap::maxEntries 288-byte SURF records), which this library
+ * does not keep: it is written as a reset key map (mutexes -1, records
+ * zero, so every key invalid). */
+int sf_map_write(sf_context *ctx, const sf_map *map, const char *path);
+/* System::ReadMapFromDisk (Core/System.cc:363-403): the dense part of a
+ * map.bin into a map of the same sizes (header checked against the map's
+ * config, else SF_ERR_INVALID); the keypoint section is skipped.  The
+ * allocated-entry index is rebuilt.  SF_ERR_IO when the file cannot be
+ * read or is shorter than the dense part. */
+int sf_map_read(sf_context *ctx, sf_map *map, const char *path);
 
 /* ResetMap (Mapping/RenderScene.h:3; FuseMap.cu:1251-1304). */
 int sf_ResetMap(sf_context *ctx, sf_map *map);

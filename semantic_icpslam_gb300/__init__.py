@@ -6,6 +6,7 @@ launchers is plain CUDA memory; helpers accept torch CUDA tensors.  There is
 no CPU path: everything here calls libsfusion.so.
 """
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -116,6 +117,14 @@ class Map:
         out = (C.c_int * 4)()
         call("sf_map_counters", ctx.h, self.h, out)
         return list(out)
+
+    def write(self, ctx, path):
+        """map.bin in the reference's byte layout (System::WriteMapToDisk)."""
+        call("sf_map_write", ctx.h, self.h, os.fsencode(path))
+
+    def read(self, ctx, path):
+        """Loads a map.bin of this map's sizes (System::ReadMapFromDisk)."""
+        call("sf_map_read", ctx.h, self.h, os.fsencode(path))
 
 
 class System:

@@ -11,9 +11,10 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libsfusion.so")
 
 (SF_OK, SF_ERR_INVALID, SF_ERR_CUDA, SF_ERR_OVERFLOW, SF_ERR_TIMEOUT, SF_ERR_NO_DEVICE, SF_ERR_STATE,
- SF_ERR_TOO_LARGE) = range(8)
+ SF_ERR_TOO_LARGE, SF_ERR_IO) = range(9)
 STATUS_NAMES = {0: "SF_OK", 1: "SF_ERR_INVALID", 2: "SF_ERR_CUDA", 3: "SF_ERR_OVERFLOW",
-                4: "SF_ERR_TIMEOUT", 5: "SF_ERR_NO_DEVICE", 6: "SF_ERR_STATE", 7: "SF_ERR_TOO_LARGE"}
+                4: "SF_ERR_TIMEOUT", 5: "SF_ERR_NO_DEVICE", 6: "SF_ERR_STATE", 7: "SF_ERR_TOO_LARGE",
+                8: "SF_ERR_IO"}
 ICP_STATIC_MAX_PIXELS = 4194304  # SF_ICP_STATIC_MAX_PIXELS
 
 FLAG_NAMES = {1 << 0: "DEDUP_FULL", 1 << 1: "PENDING_FULL", 1 << 2: "HEAP_EMPTY", 1 << 3: "EXCESS_FULL",
@@ -110,6 +111,8 @@ SIGNATURES = {
     "sf_map_arrays": [vp, C.POINTER(DeviceMap)],
     "sf_map_rebuild_index": [vp, vp],
     "sf_map_counters": [vp, vp, I32P],
+    "sf_map_write": [vp, vp, C.c_char_p],
+    "sf_map_read": [vp, vp, C.c_char_p],
     "sf_ResetMap": [vp, vp],
     "sf_FilterDepth": [vp, Image, Image, Image, C.c_float, C.c_float],
     "sf_ComputeVMap": [vp, Image, Image, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float],

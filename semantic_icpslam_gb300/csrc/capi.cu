@@ -309,6 +309,130 @@ int sf_map_rebuild_index(sf_context *ctx, sf_map *m) {
   return SF_OK;
 }
 
+// ------------------------------------------------------------- map.bin
+namespace {
+
+constexpr int kRefMaxKeys = 100000;                  // KeyMap::MaxKeys (Mapping/DeviceMap.h:207)
+constexpr long long kRefKeyEntries = kRefMaxKeys * 5LL;  // KeyMap::maxEntries (:208-209)
+constexpr size_t kRefSurfBytes = 288;  // SURF: bool valid, float3 pos, float4 normal, float[64] (:129-138)
+constexpr size_t kMapIoChunk = 32u << 20;
+
+struct MapBinHeader {
+  int num_sdf_blocks, num_buckets, num_voxels, num_entries;
+};
+
+MapBinHeader map_bin_header(const sf_map_config &c) {
+  MapBinHeader h;
+  h.num_sdf_blocks = (int)c.num_sdf_blocks;
+  h.num_buckets = (int)c.num_buckets;
+  h.num_voxels = (int)(c.num_sdf_blocks * 512u);
+  h.num_entries = (int)(c.num_buckets + c.num_excess);
+  return h;
+}
+
+// Device array <-> file through a pinned staging buffer, chunk by chunk.
+int dev_to_file(std::FILE *f, const void *dev, size_t bytes, char *stage, cudaStream_t st) {
+  for (size_t off = 0; off < bytes; off += kMapIoChunk) {
+    const size_t n = bytes - off < kMapIoChunk ? bytes - off : kMapIoChunk;
+    SF_CHECK(cudaMemcpyAsync(stage, (const char *)dev + off, n, cudaMemcpyDeviceToHost, st));
+    SF_CHECK(cudaStreamSynchronize(st));
+    if (std::fwrite(stage, 1, n, f) != n) return SF_ERR_IO;
+  }
+  return SF_OK;
+}
+
+int file_to_dev(std::FILE *f, void *dev, size_t bytes, char *stage, cudaStream_t st) {
+  for (size_t off = 0; off < bytes; off += kMapIoChunk) {
+    const size_t n = bytes - off < kMapIoChunk ? bytes - off : kMapIoChunk;
+    SF_CHECK(cudaStreamSynchronize(st));  // the previous chunk has left the staging buffer
+    if (std::fread(stage, 1, n, f) != n) return SF_ERR_IO;
+    SF_CHECK(cudaMemcpyAsync((char *)dev + off, stage, n, cudaMemcpyHostToDevice, st));
+  }
+  SF_CHECK(cudaStreamSynchronize(st));
+  return SF_OK;
+}
+
+struct FileCloser {
+  std::FILE *f;
+  ~FileCloser() {
+    if (f) std::fclose(f);
+  }
+};
+struct PinnedBuffer {
+  char *p = nullptr;
+  ~PinnedBuffer() {
+    if (p) cudaFreeHost(p);
+  }
+};
+
+}  // namespace
+
+int sf_map_write(sf_context *ctx, const sf_map *m, const char *path) {
+  if (!ctx || !m || !path) return SF_ERR_INVALID;
+  const MapBinHeader h = map_bin_header(m->cfg);
+  FileCloser fc{std::fopen(path, "wb")};
+  if (!fc.f) return SF_ERR_IO;
+  PinnedBuffer stage;
+  SF_CHECK(cudaMallocHost(&stage.p, kMapIoChunk));
+  cudaStream_t st = ctx->stream;
+  int counters[3];
+  SF_CHECK(cudaMemcpyAsync(&counters[0], m->d.heap_counter, sizeof(int), cudaMemcpyDeviceToHost, st));
+  SF_CHECK(cudaMemcpyAsync(&counters[1], m->d.entry_ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
+  SF_CHECK(cudaMemcpyAsync(&counters[2], m->d.no_visible, sizeof(int), cudaMemcpyDeviceToHost, st));
+  SF_CHECK(cudaStreamSynchronize(st));
+  if (std::fwrite(&h, sizeof(h), 1, fc.f) != 1 || std::fwrite(counters, sizeof(int), 3, fc.f) != 3)
+    return SF_ERR_IO;
+  int r;
+  if ((r = dev_to_file(fc.f, m->d.heap, sizeof(int) * (size_t)h.num_sdf_blocks, stage.p, st)) ||
+      (r = dev_to_file(fc.f, m->d.bucket_mutex, sizeof(int) * (size_t)h.num_buckets, stage.p, st)) ||
+      (r = dev_to_file(fc.f, m->d.voxels, sizeof(sf_voxel) * (size_t)h.num_voxels, stage.p, st)) ||
+      (r = dev_to_file(fc.f, m->d.entries, sizeof(sf_hash_entry) * (size_t)h.num_entries, stage.p, st)) ||
+      (r = dev_to_file(fc.f, m->d.visible, sizeof(sf_hash_entry) * (size_t)h.num_entries, stage.p, st)))
+    return r;
+  // the keypoint map, reset (ResetKeyPoints, Mapping/FuseMap.cu:1306-1322)
+  std::memset(stage.p, 0xff, sizeof(int) * (size_t)kRefMaxKeys);
+  if (std::fwrite(stage.p, sizeof(int), kRefMaxKeys, fc.f) != (size_t)kRefMaxKeys) return SF_ERR_IO;
+  std::memset(stage.p, 0, kMapIoChunk);
+  for (long long left = kRefKeyEntries * (long long)kRefSurfBytes; left > 0;) {
+    const size_t n = left < (long long)kMapIoChunk ? (size_t)left : kMapIoChunk;
+    if (std::fwrite(stage.p, 1, n, fc.f) != n) return SF_ERR_IO;
+    left -= (long long)n;
+  }
+  if (std::fflush(fc.f) != 0) return SF_ERR_IO;
+  return SF_OK;
+}
+
+int sf_map_read(sf_context *ctx, sf_map *m, const char *path) {
+  if (!ctx || !m || !path) return SF_ERR_INVALID;
+  const MapBinHeader want = map_bin_header(m->cfg);
+  FileCloser fc{std::fopen(path, "rb")};
+  if (!fc.f) return SF_ERR_IO;
+  MapBinHeader h;
+  int counters[3];
+  if (std::fread(&h, sizeof(h), 1, fc.f) != 1) return SF_ERR_IO;
+  if (h.num_sdf_blocks != want.num_sdf_blocks || h.num_buckets != want.num_buckets ||
+      h.num_voxels != want.num_voxels || h.num_entries != want.num_entries)
+    return SF_ERR_INVALID;
+  if (std::fread(counters, sizeof(int), 3, fc.f) != 3) return SF_ERR_IO;
+  PinnedBuffer stage;
+  SF_CHECK(cudaMallocHost(&stage.p, kMapIoChunk));
+  cudaStream_t st = ctx->stream;
+  int r;
+  if ((r = file_to_dev(fc.f, m->d.heap, sizeof(int) * (size_t)h.num_sdf_blocks, stage.p, st)) ||
+      (r = file_to_dev(fc.f, m->d.bucket_mutex, sizeof(int) * (size_t)h.num_buckets, stage.p, st)) ||
+      (r = file_to_dev(fc.f, m->d.voxels, sizeof(sf_voxel) * (size_t)h.num_voxels, stage.p, st)) ||
+      (r = file_to_dev(fc.f, m->d.entries, sizeof(sf_hash_entry) * (size_t)h.num_entries, stage.p, st)) ||
+      (r = file_to_dev(fc.f, m->d.visible, sizeof(sf_hash_entry) * (size_t)h.num_entries, stage.p, st)))
+    return r;
+  SF_CHECK(cudaMemcpyAsync(m->d.heap_counter, &counters[0], sizeof(int), cudaMemcpyHostToDevice, st));
+  SF_CHECK(cudaMemcpyAsync(m->d.entry_ptr, &counters[1], sizeof(int), cudaMemcpyHostToDevice, st));
+  SF_CHECK(cudaMemcpyAsync(m->d.no_visible, &counters[2], sizeof(int), cudaMemcpyHostToDevice, st));
+  launch_rebuild_index(m->d, st);
+  SF_CHECK(cudaGetLastError());
+  SF_CHECK(cudaStreamSynchronize(st));
+  return SF_OK;
+}
+
 int sf_map_counters(sf_context *ctx, const sf_map *m, int out[4]) {
   if (!ctx || !m || !out) return SF_ERR_INVALID;
   SF_CHECK(cudaMemcpyAsync(out + 0, m->d.heap_counter, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
