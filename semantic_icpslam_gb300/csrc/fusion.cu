@@ -365,23 +365,17 @@ __global__ void k_alloc_insert(DevMap m, FuseScratch f, const int *run_flag, uin
     }
     f.bucket_head[bucket] = -1;
   }
+  // The 16-bit epoch wraps to 1 at the next frame: clear the request set
+  // now (the probe pass is over), so no entry of 65535 frames ago matches.
+  if (f.counters[2] == 0xffffu)
+    for (unsigned i = grid_tid(); i < f.req_cap; i += grid_stride()) f.req_set[i] = 0ull;
 }
 
 // Clears the per-frame counters and advances the request epoch.  The
 // probe pass reads counters[2]; the epoch skips 0 (the empty-slot value).
 __global__ void k_alloc_begin(FuseScratch f, const int *run_flag) {
   if (run_flag && *run_flag == 0) return;
-  f.counters[0] = 0;
-  f.counters[1] = 0;
-  unsigned e = (f.counters[2] + 1u) & 0xffffu;
-  if (e == 0) e = 1;
-  f.counters[2] = e;
-}
-
-// Clears the request set when the 16-bit epoch wraps (every 65535 frames).
-__global__ void k_clear_req(FuseScratch f) {
-  if (f.counters[2] != 1u) return;
-  for (unsigned i = grid_tid(); i < f.req_cap; i += grid_stride()) f.req_set[i] = 0ull;
+  alloc_frame_begin(f);
 }
 
 // ------------------------------------------------------------ visibility
@@ -464,19 +458,25 @@ __global__ void k_zrange_init(sf_image zmin, sf_image zmax) {
 }
 
 // Per-frame start of the visibility pass: counters and the window box.
-__global__ void k_vis_begin(DevMap m, FuseScratch f, const Cam *cam, unsigned *rendered,
-                            const int *run_flag) {
+// Start of the visibility pass: resets the visible count and the rendered
+// flag, sets the frame's block-pointer window (each CTA computes it for
+// itself; CTA 0 publishes it for the later passes), then clears the window
+// cells and (when given) the z-range images.
+__global__ void k_vis_start(DevMap m, FuseScratch f, const Cam *cam, unsigned *rendered, sf_image zmin,
+                            sf_image zmax, int do_z, const int *run_flag) {
   if (run_flag && *run_flag == 0) return;
-  *m.no_visible = 0u;
-  if (rendered) *rendered = 0u;
-  window_setup(*cam, m.c.block_width, m.c.depth_min, m.c.depth_max, f.win_cap, f.win);
-}
-
-// Clears the window cells and (when given) the z-range images.
-__global__ void k_vis_clear(FuseScratch f, sf_image zmin, sf_image zmax, int do_z,
-                            const int *run_flag) {
-  if (run_flag && *run_flag == 0) return;
-  const unsigned ncell = (unsigned)f.win[3] * (unsigned)f.win[4] * (unsigned)f.win[5];
+  __shared__ int win[8];
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 8; ++k) win[k] = 0;
+    window_setup(*cam, m.c.block_width, m.c.depth_min, m.c.depth_max, f.win_cap, win);
+    if (blockIdx.x == 0) {
+      *m.no_visible = 0u;
+      if (rendered) *rendered = 0u;
+      for (int k = 0; k < 6; ++k) f.win[k] = win[k];
+    }
+  }
+  __syncthreads();
+  const unsigned ncell = (unsigned)win[3] * (unsigned)win[4] * (unsigned)win[5];
   const unsigned nz = do_z ? (unsigned)(zmin.cols * zmin.rows) : 0u;
   const unsigned n = ncell > nz ? ncell : nz;
   for (unsigned i = grid_tid(); i < n; i += grid_stride()) {
@@ -697,9 +697,11 @@ void launch_rebuild_index(const DevMap &m, cudaStream_t s) {
 }
 
 void launch_alloc(const DevMap &m, const FuseScratch &f, const sf_image &depth, const Cam *c,
-                  const int *run_flag, uint32_t *flags, cudaStream_t s) {
-  k_alloc_begin<<<1, 1, 0, s>>>(f, run_flag); note_launch();
-  k_clear_req<<<sm_count() * 4, 256, 0, s>>>(f); note_launch();
+                  const int *run_flag, uint32_t *flags, cudaStream_t s, bool begin) {
+  if (begin) {
+    k_alloc_begin<<<1, 1, 0, s>>>(f, run_flag);
+    note_launch();
+  }
   dim3 blk(32, 8);
   dim3 grd((depth.cols + 31) / 32, (depth.rows + 7) / 8);
   k_alloc_probe<<<grd, blk, 0, s>>>(m, f, depth, c, run_flag, flags); note_launch();
@@ -718,8 +720,7 @@ void launch_visibility(const DevMap &m, const FuseScratch &f, const Cam *c, cons
   unsigned *rendered = f.counters + 3;
   const bool do_z = zmin && zmax;
   sf_image zn = do_z ? *zmin : sf_image{}, zx = do_z ? *zmax : sf_image{};
-  k_vis_begin<<<1, 1, 0, s>>>(m, f, c, rendered, run_flag); note_launch();
-  k_vis_clear<<<sm_count() * 8, 256, 0, s>>>(f, zn, zx, do_z ? 1 : 0, run_flag); note_launch();
+  k_vis_start<<<sm_count() * 8, 256, 0, s>>>(m, f, c, rendered, zn, zx, do_z ? 1 : 0, run_flag); note_launch();
   k_visibility<<<sm_count() * 4, 256, 0, s>>>(m, f, c, zn, zx, do_z ? 1 : 0, rendered, run_flag,
                                               flags); note_launch();
 }

@@ -391,7 +391,7 @@ struct PersistentArgs {
   unsigned long long *fix;   // [3][kFixGroups][29][kFixSlots] accumulators, zero at launch
   TrackCtl *ctl;
   const double *last_pose;
-  const int *run_flag;
+  const int *skip_flag;  // nonzero: the kernel does nothing
   uint32_t *flags;
   unsigned long long *prof;  // optional per-iteration phase clocks of CTA 0
 };
@@ -443,7 +443,7 @@ __global__ void __launch_bounds__(kPThreads, 1) k_icp_persistent(PersistentArgs 
   __shared__ double sums[29];
   __shared__ ff wpart[kPWarps][33];
   __shared__ unsigned long long sfix[kFixGroups * 29][kFixSlots];
-  if (a.run_flag && *a.run_flag == 0) return;  // uniform across the grid
+  if (a.skip_flag && *a.skip_flag != 0) return;  // uniform across the grid
   if (threadIdx.x == 0) {
     ctl_begin(ctl, a.last_pose);
     s_solve_marks = nullptr;
@@ -581,7 +581,7 @@ void launch_icp_step(const IcpWorkspace &w, const IcpLevelArgs &L, const m3 &Rc,
 }
 
 cudaError_t launch_icp_persistent(const IcpWorkspace &w, const IcpLevelArgs *levels, int nlevels,
-                                  float thresh, const double *last_pose, const int *run_flag,
+                                  float thresh, const double *last_pose, const int *skip_flag,
                                   uint32_t *flags, cudaStream_t s) {
   PersistentArgs a;
   for (int l = 0; l < nlevels && l < kMaxLevels; ++l) a.lv[l] = levels[l];
@@ -591,7 +591,7 @@ cudaError_t launch_icp_persistent(const IcpWorkspace &w, const IcpLevelArgs *lev
   a.fix = w.fix;
   a.ctl = w.ctl;
   a.last_pose = last_pose;
-  a.run_flag = run_flag;
+  a.skip_flag = skip_flag;
   a.flags = flags;
   a.prof = w.profile ? w.prof : nullptr;
   cudaLaunchConfig_t cfg = {};

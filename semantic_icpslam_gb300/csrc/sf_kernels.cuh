@@ -70,9 +70,9 @@ cudaError_t icp_persistent_reset(const IcpWorkspace &w, cudaStream_t s);
 
 // Persistent form: every level and iteration of Tracker::ComputeSE3 in one
 // cooperative launch.  last_pose: device double[16]; result in *w.ctl.
-// run_flag (device int, may be null): when 0 the kernel does nothing.
+// skip_flag (device int, may be null): when nonzero the kernel does nothing.
 cudaError_t launch_icp_persistent(const IcpWorkspace &w, const IcpLevelArgs *levels, int nlevels,
-                                  float thresh, const double *last_pose, const int *run_flag,
+                                  float thresh, const double *last_pose, const int *skip_flag,
                                   uint32_t *flags, cudaStream_t s);
 
 // -------------------------------------------------------------- fusion
@@ -95,6 +95,18 @@ struct FuseScratch {
   uint32_t win_cap = 0;
 };
 
+// Start of a frame's allocation pass: clears the per-frame counters and
+// advances the request epoch (skipping 0, the empty-slot value).  Run by
+// one thread before the probe pass.
+__device__ __forceinline__ void alloc_frame_begin(const FuseScratch &f) {
+  f.counters[0] = 0;
+  f.counters[1] = 0;
+  unsigned e = (f.counters[2] + 1u) & 0xffffu;
+  if (e == 0) e = 1;
+  f.counters[2] = e;
+}
+
+
 int fuse_scratch_init(FuseScratch &f, const MapConst &c, int max_pixels);
 void fuse_scratch_free(FuseScratch &f);
 
@@ -108,9 +120,11 @@ struct Cam {
 
 void launch_map_reset(const DevMap &m, cudaStream_t s);
 void launch_rebuild_index(const DevMap &m, cudaStream_t s);
-// Fusion::CreateBlocks (FuseMap.cu:92-132) as probe + insert passes.
+// Fusion::CreateBlocks (FuseMap.cu:92-132) as probe + insert passes.  With
+// begin = false the caller has run alloc_frame_begin itself (in its own
+// single-thread kernel, gated by the same run flag).
 void launch_alloc(const DevMap &m, const FuseScratch &f, const sf_image &depth, const Cam *c,
-                  const int *run_flag, uint32_t *flags, cudaStream_t s);
+                  const int *run_flag, uint32_t *flags, cudaStream_t s, bool begin = true);
 // CheckFullVisibility (FuseMap.cu:134-168) over the allocated-entry index.
 // When zmin/zmax images are given, also lays down the z-range tiles of
 // Projection + fillBlocks (RenderScene.cu:54-190) for each visible block.

@@ -34,8 +34,7 @@ const sf_map_config &map_cfg(sf_map *m);
 
 struct SysDev {
   double last_pose[16];
-  int state;     // 1 = initialise on the next frame, 0 = tracking
-  int icp_run;   // this frame runs ICP
+  int state;     // 1 = initialise on the next frame (ICP skipped), 0 = tracking
   int run;       // this frame is tracked: mapping runs
   int accepted;
   int first;     // this frame was the initialisation frame
@@ -45,13 +44,11 @@ struct SysDev {
 
 namespace {
 
-__global__ void k_sys_pre(SysDev *s) {
-  s->icp_run = (s->state == 0) ? 1 : 0;
-}
-
 // Track() outcome (Tracking.cc:65-119) and the mapping camera
-// (Frame::GpuRotation / GpuInvRotation / GpuTranslation, Frame.cc:626-645).
-__global__ void k_sys_post(SysDev *s, const TrackCtl *ctl, Cam tmpl) {
+// (Frame::GpuRotation / GpuInvRotation / GpuTranslation, Frame.cc:626-645);
+// when the frame is tracked, also the start of its allocation pass
+// (alloc_frame_begin), which would otherwise be a launch of its own.
+__global__ void k_sys_post(SysDev *s, const TrackCtl *ctl, Cam tmpl, FuseScratch f) {
   int tracked;
   if (s->state == 1) {
     tracked = 1;
@@ -66,6 +63,7 @@ __global__ void k_sys_post(SysDev *s, const TrackCtl *ctl, Cam tmpl) {
       for (int k = 0; k < 16; ++k) s->last_pose[k] = ctl->next_pose[k];
   }
   s->run = tracked;
+  if (tracked) alloc_frame_begin(f);
   const double *P = s->last_pose;
   Cam c = tmpl;
   c.R.rx = mk3((float)P[0], (float)P[1], (float)P[2]);
@@ -257,7 +255,7 @@ void enqueue_mapping(sf_system *s, const Cam *cam, const int *run, int num_detec
   sf_image depth = img(s->d_raw, C, R, 4), rgb = img(s->d_rgb, C, R, 3);
   sf_image nm0 = img(s->d_nmap[0], C, R, 16), mask = img(s->d_mask, C, R, 1);
   sf_image zmin = img(s->d_zmin, s->zc, s->zr, 4), zmax = img(s->d_zmax, s->zc, s->zr, 4);
-  launch_alloc(m, f, depth, cam, run, flags, st);
+  launch_alloc(m, f, depth, cam, run, flags, st, /*begin=*/run == nullptr);
   mark(s, st, 3);
   launch_visibility(m, f, cam, &zmin, &zmax, run, flags, st);
   mark(s, st, 4);
@@ -279,16 +277,15 @@ cudaError_t enqueue_device_frame(sf_system *s, int num_detection, cudaStream_t s
   mark(s, st, 0);
   enqueue_pyramid(s, st);
   mark(s, st, 1);
-  k_sys_pre<<<1, 1, 0, st>>>(s->d_sys); note_launch();
   IcpLevelArgs lv[kMaxLevels];
   icp_levels(s, lv);
   cudaError_t e = icp_persistent_reset(w, st);
   if (e != cudaSuccess) return e;
   e = launch_icp_persistent(w, lv, s->L, s->cfg.icp_thresh, dev_field<double>(s->d_sys, offsetof(SysDev, last_pose)),
-                            dev_field<int>(s->d_sys, offsetof(SysDev, icp_run)),
+                            dev_field<int>(s->d_sys, offsetof(SysDev, state)),
                             ctx_flags(s->ctx), st);
   if (e != cudaSuccess) return e;
-  k_sys_post<<<1, 1, 0, st>>>(s->d_sys, w.ctl, s->tmpl); note_launch();
+  k_sys_post<<<1, 1, 0, st>>>(s->d_sys, w.ctl, s->tmpl, map_scratch(s->map)); note_launch();
   mark(s, st, 2);
   enqueue_mapping(s, dev_field<Cam>(s->d_sys, offsetof(SysDev, cam)),
                   dev_field<int>(s->d_sys, offsetof(SysDev, run)), num_detection, st);
