@@ -268,6 +268,8 @@ __device__ __forceinline__ void march_ray(const RayCtx &r, const Cam &c, float v
   bool valid_sdf = false, behind = false, done = false, interp = false;
   float s_sample = 0.f;
   f3 sample = block_s;
+  BlockCache cache;
+  cache.bx = 0x7fffffff; cache.by = 0; cache.bz = 0; cache.ptr = -1;
   while (!done && dist_s < dist_e) {
     f3 pos[kSpec];
     float ds[kSpec];
@@ -279,8 +281,7 @@ __device__ __forceinline__ void march_ray(const RayCtx &r, const Cam &c, float v
       pos[i] = pos[i - 1] + 1.0f * dir;
       ds[i] = ds[i - 1] + 1.0f;
     }
-#pragma unroll
-    for (int i = 0; i < kSpec; ++i) v[i] = read_voxel(r, pos[i]);
+    read_voxels<kSpec>(r, pos, v, cache);
     bool run = true;  // still on the speculated run of 1-voxel steps
 #pragma unroll
     for (int i = 0; i < kSpec; ++i) {

@@ -74,6 +74,42 @@ __device__ __forceinline__ VoxelRead read_voxel(const RayCtx &r, f3 pt) {
   return voxel_in(r, block_ptr(r, p.x >> 3, p.y >> 3, p.z >> 3), p.x, p.y, p.z);
 }
 
+// A ray's last looked-up block (DeviceMap::FindVoxel's per-ray entry cache,
+// DeviceMap.cu:116-133): consecutive samples mostly fall in one block, and
+// a hit skips the lookup, so the voxel read is the sample's only dependent
+// load.  The cache changes no value (block_ptr is exact for every block).
+struct BlockCache {
+  int bx, by, bz, ptr;
+};
+
+// The voxels at n consecutive sample points, their block lookups issued
+// together: a sample in the cached block or in the previous sample's block
+// reuses that pointer.  The cache then holds the last sample's block.
+template <int N>
+__device__ __forceinline__ void read_voxels(const RayCtx &r, const f3 *pt, VoxelRead *v, BlockCache &cache) {
+  i3 p[N];
+  int ptr[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    p[i] = floor3(pt[i]);
+    const int bx = p[i].x >> 3, by = p[i].y >> 3, bz = p[i].z >> 3;
+    const bool same_prev =
+        i > 0 && bx == (p[i - 1].x >> 3) && by == (p[i - 1].y >> 3) && bz == (p[i - 1].z >> 3);
+    if (same_prev)
+      ptr[i] = ptr[i > 0 ? i - 1 : 0];
+    else if (bx == cache.bx && by == cache.by && bz == cache.bz)
+      ptr[i] = cache.ptr;
+    else
+      ptr[i] = block_ptr(r, bx, by, bz);
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) v[i] = voxel_in(r, ptr[i], p[i].x, p[i].y, p[i].z);
+  cache.bx = p[N - 1].x >> 3;
+  cache.by = p[N - 1].y >> 3;
+  cache.bz = p[N - 1].z >> 3;
+  cache.ptr = ptr[N - 1];
+}
+
 // Rendering::readSdfInterped (RenderScene.cu:310-343).  The corners are
 // the reference's floor3(pt + offset); per axis that is floor(pt) or
 // floor(pt + 1), so six floors give all eight.  Corners that share a block
