@@ -7,6 +7,7 @@ no CPU path: everything here calls libsfusion.so.
 """
 import ctypes as C
 import os
+import weakref
 
 import numpy as np
 
@@ -53,9 +54,12 @@ class Context:
         h = C.c_void_p()
         call("sf_context_create", C.byref(h))
         self.h = h
+        self._systems = weakref.WeakSet()  # closed before the context
 
     def close(self):
         if getattr(self, "h", None):
+            for s in list(getattr(self, "_systems", ())):
+                s.close()
             load().sf_context_destroy(self.h)
             self.h = None
 
@@ -138,6 +142,7 @@ class System:
         P = np.ascontiguousarray(P, np.float64)
         call("sf_system_create", ctx.h, C.byref(cfg), P.ctypes.data_as(_lib.F64P), C.byref(h))
         self.h = h
+        ctx._systems.add(self)
 
     def close(self):
         if getattr(self, "h", None):

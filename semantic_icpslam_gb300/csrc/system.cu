@@ -149,6 +149,10 @@ struct sf_system {
   // stage timing (eager form only): events at the stage boundaries
   int timing = 0;
   cudaEvent_t ev[8] = {};
+  // colour (and mask) uploads of sf_system_grab run on their own stream,
+  // overlapping the pyramid and ICP; integration waits for ev_inputs
+  cudaStream_t cstream = nullptr;
+  cudaEvent_t ev_inputs = nullptr, ev_prev = nullptr;
   // raycast launch shape (sf_system_autotune)
   RaycastTune rc_tune;
   long long frames = 0;  // frames run (any form)
@@ -182,6 +186,9 @@ int alloc_all(sf_system *s) {
        cudaMallocHost(&s->h_mask, np) == cudaSuccess &&
        cudaMallocHost(&s->h_stats, sizeof(sf_frame_stats)) == cudaSuccess;
   if (ok) ok = cudaMemset(s->d_mask, 0, np) == cudaSuccess;
+  ok = ok && cudaStreamCreateWithFlags(&s->cstream, cudaStreamNonBlocking) == cudaSuccess &&
+       cudaEventCreateWithFlags(&s->ev_inputs, cudaEventDisableTiming) == cudaSuccess &&
+       cudaEventCreateWithFlags(&s->ev_prev, cudaEventDisableTiming) == cudaSuccess;
   return ok ? SF_OK : SF_ERR_CUDA;
 }
 
@@ -199,6 +206,10 @@ void free_all(sf_system *s) {
   if (s->gexec) cudaGraphExecDestroy(s->gexec);
   for (auto &e : s->ev)
     if (e) cudaEventDestroy(e);
+  if (s->cstream) cudaStreamSynchronize(s->cstream);
+  if (s->ev_inputs) cudaEventDestroy(s->ev_inputs);
+  if (s->ev_prev) cudaEventDestroy(s->ev_prev);
+  if (s->cstream) cudaStreamDestroy(s->cstream);
 }
 
 // Frame::FillImages depth part (Core/Frame.cc:68-92).
@@ -259,6 +270,11 @@ void enqueue_mapping(sf_system *s, const Cam *cam, const int *run, int num_detec
   mark(s, st, 3);
   launch_visibility(m, f, cam, &zmin, &zmax, run, flags, st);
   mark(s, st, 4);
+  // the frame's colour and mask, uploaded on the copy stream (captured as
+  // an external event wait in the frame graph)
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(st, &cs);
+  cudaStreamWaitEvent(st, s->ev_inputs, cs == cudaStreamCaptureStatusActive ? cudaEventWaitExternal : 0);
   launch_integrate(m, depth, rgb, &nm0, &mask, num_detection, cam, true, num_detection > 0, run, st);
   mark(s, st, 5);
   sf_image fv = img(s->d_vmap[0], C, R, 16), fn = img(s->d_nmap[0], C, R, 16);
@@ -375,6 +391,7 @@ int run_plain_frame(sf_system *s, int num_detection) {
         cudaStreamSynchronize(st) != cudaSuccess)
       return SF_ERR_CUDA;
     if (nvis > 0)
+      cudaStreamWaitEvent(st, s->ev_inputs, 0);
       launch_integrate(m, depth, rgb, &nm0, &mask, num_detection, cam, true, num_detection > 0,
                        nullptr, st);
     sf_image fv = img(s->d_vmap[0], C, R, 16), fn = img(s->d_nmap[0], C, R, 16);
@@ -486,18 +503,24 @@ int sf_system_grab(sf_system *s, const uint16_t *depth, const uint8_t *rgb, cons
   const size_t np = (size_t)s->cfg.cols * s->cfg.rows;
   // host -> device: straight from the caller's buffer when it is pinned
   // (page-locked or registered), through the pinned staging buffer when not
-  auto upload = [&](void *dst, const void *src, void *staging, size_t n) {
+  auto upload = [&](void *dst, const void *src, void *staging, size_t n, cudaStream_t on) {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, src) == cudaSuccess && a.type == cudaMemoryTypeHost)
-      return cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, st);
+      return cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, on);
     cudaGetLastError();  // an unregistered pointer is not an error here
     memcpy(staging, src, n);
-    return cudaMemcpyAsync(dst, staging, n, cudaMemcpyHostToDevice, st);
+    return cudaMemcpyAsync(dst, staging, n, cudaMemcpyHostToDevice, on);
   };
-  if (upload(s->d_depth16, depth, s->h_depth16, np * 2) != cudaSuccess ||
-      upload(s->d_rgb, rgb, s->h_rgb, np * 3) != cudaSuccess)
+  // Depth on the frame's stream; colour and mask on the copy stream after
+  // the previous frame's work (their buffers are read by its integration),
+  // overlapping this frame's pyramid and ICP.
+  if (cudaEventRecord(s->ev_prev, st) != cudaSuccess || cudaStreamWaitEvent(s->cstream, s->ev_prev, 0) != cudaSuccess)
     return SF_ERR_CUDA;
-  if (num_detection > 0 && upload(s->d_mask, mask, s->h_mask, np) != cudaSuccess) return SF_ERR_CUDA;
+  if (upload(s->d_depth16, depth, s->h_depth16, np * 2, st) != cudaSuccess ||
+      upload(s->d_rgb, rgb, s->h_rgb, np * 3, s->cstream) != cudaSuccess)
+    return SF_ERR_CUDA;
+  if (num_detection > 0 && upload(s->d_mask, mask, s->h_mask, np, s->cstream) != cudaSuccess) return SF_ERR_CUDA;
+  if (cudaEventRecord(s->ev_inputs, s->cstream) != cudaSuccess) return SF_ERR_CUDA;
   int r = run_frame(s, num_detection);
   if (r) return r;
   if (cudaMemcpyAsync(s->h_stats, s->d_stats, sizeof(sf_frame_stats), cudaMemcpyDeviceToHost, st) !=
