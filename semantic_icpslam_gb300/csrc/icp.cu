@@ -22,7 +22,7 @@
 __shared__ unsigned long long *s_solve_marks;
 #define SF_SOLVE_MARK(k)                                           \
   do {                                                             \
-    if ((threadIdx.x & 31) == 0 && s_solve_marks) s_solve_marks[k] = clock64(); \
+    if (threadIdx.x == 0 && s_solve_marks) s_solve_marks[k] = clock64(); \
   } while (0)
 #include "sf_icp_solve.cuh"
 

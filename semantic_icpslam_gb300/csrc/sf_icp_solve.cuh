@@ -114,8 +114,7 @@ __device__ __forceinline__ void solve6_two_warps(const double *sums, double x[6]
     if (has) s.a[cur][i0][j0] = r;
     asm volatile("bar.sync 1, 64;" ::: "memory");
   }
-  if (threadIdx.x >= 32) return;
-  // x_i = b_i / a_ii, the six divisions side by side in lanes 0..5
+  // x_i = b_i / a_ii, the six divisions side by side in lanes 0..5 (of both warps)
   const int row = lane < 6 ? lane : 0;
   const double xi = ((zero >> row) & 1u) ? 0.0 : s.a[cur][row][6] / s.a[cur][row][row];
 #pragma unroll
@@ -161,53 +160,62 @@ __device__ __forceinline__ int ctl_decide(TrackCtl &c, const double *sums, int m
 
 // One iteration given the 29 sums in shared memory, run by threads 0..95
 // (three warps): lane 0 of warp 2 takes the stop decision while warps 0
-// and 1 solve and warp 0 builds exp(-x), so the three overlap; after named
-// barrier 2, warp 0 applies the decision (or the update).  Same contract
-// and state transitions as sf::ctl_step; warp 0 returns whether to go on.
+// and 1 solve and build exp(-x) (rotation on warp 0, translation on warp
+// 1), so the three overlap; after named barrier 2, warp 0 applies the
+// decision (or the update).  Same contract and state transitions as
+// sf::ctl_step; warp 0 returns whether to go on.
 __device__ bool ctl_step_fast(TrackCtl &c, const double *sums, int min_count, IcpSolveSmem &s) {
   const int lane = threadIdx.x & 31;
   if (threadIdx.x >= 64) {  // warp 2
     if (lane == 0) s.code = ctl_decide(c, sums, min_count, &s.copy_cand);
-    asm volatile("bar.sync 2, 64;" ::: "memory");
+    asm volatile("bar.sync 2, 96;" ::: "memory");
     return false;
   }
   SF_SOLVE_MARK(0);
   SF_SOLVE_MARK(1);
   double x[6];
   solve6_two_warps(sums, x, s);
-  if (threadIdx.x >= 32) return false;  // warp 1
-  SF_SOLVE_MARK(2);
+  // Warp 0 builds exp(-x)'s rotation, warp 1 its translation, side by side.
+  const bool tw = threadIdx.x >= 32;  // the translation warp
   const double u0 = x[0], u1 = x[1], u2 = x[2];
   const double w0 = x[3], w1 = x[4], w2 = x[5];
   const double th2 = fma(w2, w2, fma(w1, w1, w0 * w0));
-  double ca, c1, c2;
+  const bool tiny = th2 < 1e-20;  // below 1e-10 rad Sophus's V is R
+  double ca = 0.0, c1, c2 = 0.0;
   if (th2 < 0.01) {
     // sin t / t = 1 - x/6 + x^2/120 - ..., (1 - cos t)/t^2 = 1/2 - x/24 + ...,
     // (t - sin t)/t^3 = 1/6 - x/120 + ..., x = t^2
     const float xf = (float)th2;
-    const float ca_tail = xf * (1.f / 120 + xf * (-1.f / 5040 + xf * (1.f / 362880 + xf * (-1.f / 39916800))));
     const float c1_tail = xf * (1.f / 720 + xf * (-1.f / 40320 + xf * (1.f / 3628800 + xf * (-1.f / 479001600))));
-    const float c2_tail = xf * (1.f / 5040 + xf * (-1.f / 362880 + xf * (1.f / 39916800 + xf * (-1.f / 6227020800.f))));
-    ca = fma(th2, -1.0 / 6 + (double)ca_tail, 1.0);
     c1 = fma(th2, -1.0 / 24 + (double)c1_tail, 0.5);
-    c2 = fma(th2, -1.0 / 120 + (double)c2_tail, 1.0 / 6);
+    if (!tw || tiny) {
+      const float ca_tail = xf * (1.f / 120 + xf * (-1.f / 5040 + xf * (1.f / 362880 + xf * (-1.f / 39916800))));
+      ca = fma(th2, -1.0 / 6 + (double)ca_tail, 1.0);
+    }
+    if (tw && !tiny) {
+      const float c2_tail =
+          xf * (1.f / 5040 + xf * (-1.f / 362880 + xf * (1.f / 39916800 + xf * (-1.f / 6227020800.f))));
+      c2 = fma(th2, -1.0 / 120 + (double)c2_tail, 1.0 / 6);
+    }
   } else {
     const double th = sqrt(th2);
     double v = 0.0;
     if (lane == 0) v = sin(th);
     if (lane == 1) v = cos(th);
     const double sn = __shfl_sync(0xffffffffu, v, 0), cs = __shfl_sync(0xffffffffu, v, 1);
-    ca = sn / th;
     c1 = (1 - cs) / th2;
-    c2 = (th - sn) / (th2 * th);
+    if (tw)
+      c2 = (th - sn) / (th2 * th);
+    else
+      ca = sn / th;
   }
   SF_SOLVE_MARK(3);
   // next = last * (exp(x) delta)^-1 = next * exp(x)^-1 = next * exp(-x):
   // exp(-x) = [R^T | t'] with R^T_ij = R_ji = delta_ij - c_a W_ij +
   // c_1 (w_i w_j - delta_ij t^2) (W = [w]x: W01 = -w2, W02 = w1, W12 = -w0,
-  // W^T = -W) in lanes 0..8, and t' = -(u - c_1 (w x u) + c_2 (w x (w x u)))
-  // (below 1e-10 rad Sophus's V is R, so t' = -R^T u) in lanes 0..2.
-  {
+  // W^T = -W) in lanes 0..8 of warp 0, and t' = -(u - c_1 (w x u) +
+  // c_2 (w x (w x u))) (t' = -R^T u below 1e-10 rad) in lanes 0..2 of warp 1.
+  auto rot_t = [&]() {  // R^T_ij for lane 3 i + j (lanes 0..8)
     const int i = lane < 9 ? lane / 3 : 0, j = lane < 9 ? lane - 3 * (lane / 3) : 0;
     const int kk = 3 - i - j;  // the third axis when i != j
     const double wi = i == 0 ? w0 : (i == 1 ? w1 : w2);
@@ -217,29 +225,34 @@ __device__ bool ctl_step_fast(TrackCtl &c, const double *sums, int min_count, Ic
     const double Wij = (i == j) ? 0.0 : (cyc ? -wk : wk);
     const double dl = (i == j) ? 1.0 : 0.0;
     const double w2ij = fma(-dl, th2, wi * wj);
-    const double r = fma(c1, w2ij, fma(-ca, Wij, dl));
+    return fma(c1, w2ij, fma(-ca, Wij, dl));
+  };
+  if (!tw) {
+    const double r = rot_t();
     if (lane < 9) s.R[lane] = r;  // R^T, row-major
-  }
-  double ti;
-  const int ci = lane < 3 ? lane : 0;
-  if (th2 < 1e-20) {
-    __syncwarp();
-    ti = -(s.R[ci * 3 + 0] * u0);
-    ti = fma(-s.R[ci * 3 + 1], u1, ti);
-    ti = fma(-s.R[ci * 3 + 2], u2, ti);
   } else {
-    // (cj, ck): the next two axes after ci, cyclically
-    const int cj = ci == 2 ? 0 : ci + 1, ck = ci == 0 ? 2 : ci - 1;
-    const double wj = cj == 0 ? w0 : (cj == 1 ? w1 : w2), wk = ck == 0 ? w0 : (ck == 1 ? w1 : w2);
-    const double uj = cj == 0 ? u0 : (cj == 1 ? u1 : u2), uk = ck == 0 ? u0 : (ck == 1 ? u1 : u2);
-    const double ui = ci == 0 ? u0 : (ci == 1 ? u1 : u2);
-    const double a = fma(wj, uk, -(wk * uj));  // (w x u)_i
-    const double aj = __shfl_sync(0xffffffffu, a, cj), ak = __shfl_sync(0xffffffffu, a, ck);
-    const double b = fma(wj, ak, -(wk * aj));  // (w x (w x u))_i
-    ti = fma(-c2, b, fma(c1, a, -ui));
+    double ti;
+    const int ci = lane < 3 ? lane : 0;
+    if (tiny) {
+      const double r = rot_t();
+      ti = -(__shfl_sync(0xffffffffu, r, ci * 3 + 0) * u0);
+      ti = fma(-__shfl_sync(0xffffffffu, r, ci * 3 + 1), u1, ti);
+      ti = fma(-__shfl_sync(0xffffffffu, r, ci * 3 + 2), u2, ti);
+    } else {
+      // (cj, ck): the next two axes after ci, cyclically
+      const int cj = ci == 2 ? 0 : ci + 1, ck = ci == 0 ? 2 : ci - 1;
+      const double wj = cj == 0 ? w0 : (cj == 1 ? w1 : w2), wk = ck == 0 ? w0 : (ck == 1 ? w1 : w2);
+      const double uj = cj == 0 ? u0 : (cj == 1 ? u1 : u2), uk = ck == 0 ? u0 : (ck == 1 ? u1 : u2);
+      const double ui = ci == 0 ? u0 : (ci == 1 ? u1 : u2);
+      const double a = fma(wj, uk, -(wk * uj));  // (w x u)_i
+      const double aj = __shfl_sync(0xffffffffu, a, cj), ak = __shfl_sync(0xffffffffu, a, ck);
+      const double b = fma(wj, ak, -(wk * aj));  // (w x (w x u))_i
+      ti = fma(-c2, b, fma(c1, a, -ui));
+    }
+    if (lane < 3) s.delta[lane] = ti;  // t'
   }
-  if (lane < 3) s.delta[lane] = ti;  // t'
-  asm volatile("bar.sync 2, 64;" ::: "memory");
+  asm volatile("bar.sync 2, 96;" ::: "memory");
+  if (tw) return false;
   {
     const int code = s.code;
     if (s.copy_cand && lane < 16) c.candidate[lane] = c.next_pose[lane];
