@@ -36,6 +36,7 @@ COLS, ROWS = 640, 480
 K = (525.0, 525.0, 319.5, 239.5)
 MAP = dict(voxel_size=0.005, trunc_dist=0.04, num_buckets=1 << 20, num_excess=1 << 18, num_sdf_blocks=1 << 19)
 ITERS = (10, 5, 4)
+LEVELS, MIN_COUNT = 3, (2000, 1000, 100)
 SEQ = dict(trajectory=1, seed=2, dropout=0.02)
 WORKLOAD = ("640x480 room sequence (seeded spline trajectory, 2% dropout, Perlin RGB), 5 mm voxels, "
             "2^20 buckets, 4 cm truncation, 3-level ICP 10/5/4")
@@ -113,7 +114,28 @@ def make_frames(n, rank=0):
 
 
 def sys_cfg(sf, mode):
-    return sf.system_config(cols=COLS, rows=ROWS, K=K, iters=ITERS, use_graph=mode, **MAP)
+    return sf.system_config(cols=COLS, rows=ROWS, K=K, levels=LEVELS, iters=ITERS, min_count=MIN_COUNT,
+                            use_graph=mode, **MAP)
+
+
+def use_corridor_config():
+    """The 1280x720 corridor stress configuration (`--config c3`): 4-level
+    pyramid, 3 mm voxels, 2^22 buckets, 2.4 cm truncation, seeded corridor of
+    boxes and pillars walked forward at 1.5 cm per frame."""
+    global METRIC, COLS, ROWS, K, MAP, ITERS, LEVELS, MIN_COUNT, SEQ, WORKLOAD
+    METRIC = "frames/s ICP+fuse+raycast 1280x720 corridor stress (4 levels, 3 mm, 2^22 buckets)"
+    COLS, ROWS = 1280, 720
+    K = (1050.0, 1050.0, 639.5, 359.5)
+    MAP = dict(voxel_size=0.003, trunc_dist=0.024, num_buckets=1 << 22, num_excess=1 << 20,
+               num_sdf_blocks=1 << 21)
+    # the 160x90 level runs no ICP iteration and the depth noise is a quarter
+    # of the room's (the coarsest model level is too sparse in the corridor,
+    # and far-range noise fails the reference's acceptance test)
+    ITERS, LEVELS, MIN_COUNT = (10, 5, 4, 0), 4, (2000, 1000, 100, 0)
+    SEQ = dict(scene=1, trajectory=2, seed=2, dropout=0.02, noise=0.25)
+    WORKLOAD = ("1280x720 corridor sequence (20 m corridor of seeded boxes and pillars, forward at 1.5 cm per "
+                "frame, 2% dropout, noise x0.25, Perlin RGB), 3 mm voxels, 2^22 buckets, 2.4 cm truncation, "
+                "4-level pyramid, ICP 10/5/4/0")
 
 
 def launches(sf):
@@ -208,7 +230,7 @@ def pose_error_fp64(sf, ctx, frames, n):
         d, rgb, _, _ = frames[i]
         if i > 0:
             mv, mn = [], []
-            for l in range(3):
+            for l in range(LEVELS):
                 v, nm = s.model_maps(l)
                 mv.append(ctx.download(v.data, np.float32, v.rows * v.cols * 4).reshape(v.rows, v.cols, 4))
                 mn.append(ctx.download(nm.data, np.float32, nm.rows * nm.cols * 4).reshape(nm.rows, nm.cols, 4))
@@ -216,11 +238,11 @@ def pose_error_fp64(sf, ctx, frames, n):
         pose = np.array(st.pose[:]).reshape(4, 4)
         if i > 0:
             vs, ns = [], []
-            for l in range(3):
+            for l in range(LEVELS):
                 v, nm, _ = s.frame_maps(l)
                 vs.append(ctx.download(v.data, np.float32, v.rows * v.cols * 4).reshape(v.rows, v.cols, 4))
                 ns.append(ctx.download(nm.data, np.float32, nm.rows * nm.cols * 4).reshape(nm.rows, nm.cols, 4))
-            ok, P64, _ = O.compute_se3(vs, ns, mv, mn, K, ITERS, (2000, 1000, 100), 1e-4, prev, prev, fp64=True)
+            ok, P64, _ = O.compute_se3(vs, ns, mv, mn, K, ITERS, MIN_COUNT, 1e-4, prev, prev, fp64=True)
             if ok == bool(st.accepted):
                 worst = max(worst, float(np.abs(P64 - pose).max()))
             else:
@@ -385,6 +407,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--map-blocks", type=int, default=19,
                     help="log2 of the voxel-block heap (2^19 blocks = 4 GB of voxels)")
+    ap.add_argument("--config", default="c2", choices=["c2", "c3"],
+                    help="c2: the 640x480 room sequence (the headline); c3: the 1280x720 corridor stress run")
     ap.add_argument("--autotune", action="store_true",
                     help="run sf_system_autotune during the warm-up of the headline form and keep its choice")
     ap.add_argument("--quick", action="store_true",
@@ -393,6 +417,8 @@ def main():
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == "c3":
+        use_corridor_config()
 
     import torch
     ws, rank, local = dist_env()
@@ -452,7 +478,7 @@ def main():
     out["kernels"] = kern
     out["visible_blocks_mean"] = round(V, 1)
     d = kern[dom]
-    traffic = load_traffic(dom)
+    traffic = load_traffic(dom) if args.config == "c2" else None
     out["roofline"] = {"kernel": dom, "bound": "hbm", "achieved": d["achieved_gbs"], "peak": peak, "unit": "GB/s",
                        "frac": d["frac_of_%s_hbm" % peak_kind], "peak_source": peak_kind,
                        "traffic": traffic, "algorithmic_bytes": d["algorithmic_bytes"],
@@ -471,8 +497,9 @@ def main():
                   "h2d_bytes_per_step": COLS * ROWS * (2 + 3), "d2h_bytes_per_step": 208,
                   "tracked_frames": int(tracked)}
     out["pose_err_fp64_max"] = pose_error_fp64(sf, ctx, frames, 6)
-    out["reloc"] = time_reloc(sf, ctx, frames)
-    if rank == 0 and not args.no_cpu:
+    if args.config == "c2":
+        out["reloc"] = time_reloc(sf, ctx, frames)
+    if rank == 0 and not args.no_cpu and args.config == "c2":
         ncpu = 6
         fps_cpu = cpu_reference(frames, ncpu)
         out["cpu_baseline"] = {"value": round(fps_cpu, 4), "unit": "frames/s", "cores": omp_threads(),
