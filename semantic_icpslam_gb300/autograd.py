@@ -24,7 +24,7 @@ import torch
 from . import _lib
 from ._lib import Image, Intrinsics, MapConfig, call
 
-__all__ = ["TorchMap", "Renderer", "raycast", "refine_tsdf", "se3_exp"]
+__all__ = ["TorchMap", "Renderer", "raycast", "raycast_cpp", "refine_tsdf", "se3_exp"]
 
 
 def se3_exp(xi):
@@ -161,6 +161,27 @@ def raycast(xi, sdf, renderer, P):
     """Vertex and normal maps rendered at exp(xi) P, differentiable in xi and
     in sdf (the map's TSDF values, e.g. TorchMap.sdf())."""
     return _RaycastFn.apply(xi, sdf, renderer, P)
+
+
+def _torch_ext():
+    """The libtorch C++ extension (torch_ext/raycast_autograd.cpp, built next
+    to the library as sf_torch.so)."""
+    from . import sf_torch
+    return sf_torch
+
+
+def raycast_cpp(xi, sdf, renderer, P):
+    """raycast() through the libtorch C++ torch::autograd::Function: the same
+    forward and backward (sf_Raycast / sf_RaycastAdjoint), with the autograd
+    node implemented in C++."""
+    ext = _torch_ext()
+    if getattr(renderer, "_cpp", None) is None:
+        r = renderer
+        renderer._cpp = ext.renderer_create(r.ctx.h.value, r.map.h.value, r.cols, r.rows, *r.K, r.dmin, r.dmax,
+                                            r.blocks.shape[0])
+    Pt = torch.as_tensor(np.asarray(P, np.float64))
+    vm, nm = ext.raycast(xi, sdf, renderer._cpp, Pt)
+    return vm, nm
 
 
 def refine_tsdf(renderer, tmap, keyframes, steps=50, lr=0.01, betas=(0.9, 0.999), eps=1e-8):

@@ -83,5 +83,58 @@ def build(force=False, verbose=False, jobs=None):
     return LIB
 
 
+# The libtorch C++ autograd function (torch_ext/raycast_autograd.cpp): a
+# Python extension module linked against libtorch and libsfusion.so.
+TORCH_EXT_SRC = os.path.join(HERE, "torch_ext", "raycast_autograd.cpp")
+TORCH_EXT = os.path.join(HERE, "sf_torch.so")
+
+
+def _torch_ext_cmds():
+    import sysconfig
+    import torch
+    import torch.utils.cpp_extension as ce
+    inc = ce.include_paths() + [sysconfig.get_paths()["include"], INCLUDE]
+    obj = os.path.join(BUILD, "raycast_autograd.o")
+    cc = ["g++", "-O2", "-std=c++17", "-fPIC", "-D_GLIBCXX_USE_CXX11_ABI=%d" % int(torch._C._GLIBCXX_USE_CXX11_ABI),
+          "-DTORCH_EXTENSION_NAME=sf_torch", "-DTORCH_API_INCLUDE_EXTENSION_H"] + sum([["-I", i] for i in inc], [])
+    compile_cmd = cc + ["-c", TORCH_EXT_SRC, "-o", obj]
+    link_cmd = ["g++", "-shared", obj, "-o", TORCH_EXT + ".tmp", "-L", ce.library_paths()[0], "-lc10", "-ltorch",
+                "-ltorch_cpu", "-ltorch_python", "-L", HERE, "-lsfusion", "-Wl,-rpath,$ORIGIN",
+                "-Wl,-rpath," + ce.library_paths()[0]]
+    return obj, compile_cmd, link_cmd
+
+
+def build_all(force=False, verbose=False):
+    """libsfusion.so, then the torch extension (compiled alongside, linked
+    after).  A torch extension that cannot build is reported and skipped:
+    the library and its Python torch.autograd form do not need it."""
+    ext = None
+    try:
+        obj, compile_cmd, link_cmd = _torch_ext_cmds()
+        os.makedirs(BUILD, exist_ok=True)
+        if force or not os.path.exists(obj) or os.path.getmtime(TORCH_EXT_SRC) > os.path.getmtime(obj) or \
+                os.path.getmtime(os.path.join(INCLUDE, "sfusion.h")) > os.path.getmtime(obj):
+            ext = subprocess.Popen(compile_cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+    except Exception as e:  # no torch headers
+        print("torch extension skipped: %s" % e, file=sys.stderr)
+        link_cmd = None
+    lib = build(force=force, verbose=verbose)
+    if link_cmd is None:
+        return lib
+    if ext is not None:
+        out, err = ext.communicate()
+        if ext.returncode != 0:
+            print("torch extension skipped: compile failed\n%s" % err[-2000:], file=sys.stderr)
+            return lib
+    if force or not os.path.exists(TORCH_EXT) or os.path.getmtime(obj) > os.path.getmtime(TORCH_EXT) or \
+            os.path.getmtime(lib) > os.path.getmtime(TORCH_EXT):
+        r = subprocess.run(link_cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            print("torch extension skipped: link failed\n%s" % r.stderr[-2000:], file=sys.stderr)
+            return lib
+        os.replace(TORCH_EXT + ".tmp", TORCH_EXT)
+    return lib
+
+
 if __name__ == "__main__":
-    build(force="--force" in sys.argv, verbose=True)
+    build_all(force="--force" in sys.argv, verbose=True)

@@ -81,3 +81,32 @@ def test_refine_tsdf_lowers_keyframe_depth_loss(fused):
     assert torch.equal(torch.isnan(after), torch.isnan(before))            # unobserved voxels untouched
     assert float((after[observed] - before[observed]).abs().max()) > 0      # observed voxels moved
     assert float(after[observed].abs().max()) <= 1.0
+
+
+def test_cpp_autograd_function_matches_python(fused):
+    """The libtorch C++ torch::autograd::Function (sf_torch.raycast) renders
+    the same maps and backpropagates the same gradients as the Python form:
+    pose gradient exactly (a fixed-order reduction), TSDF gradient up to the
+    order of float atomics."""
+    import torch
+    sf, ag, ctx, tmap, r, seq = fused
+    P = seq[8][3]
+    g = torch.Generator(device="cuda").manual_seed(11)
+    outs = []
+    for fn in (ag.raycast, ag.raycast_cpp):
+        xi = torch.zeros(6, dtype=torch.float64, requires_grad=True)
+        sdf = tmap.sdf().detach().requires_grad_(True)
+        vm, nm = fn(xi, sdf, r, P)
+        assert vm.grad_fn is not None
+        if not outs:
+            wv = torch.randn(vm.shape, device="cuda", generator=g)
+            wn = torch.randn(nm.shape, device="cuda", generator=g)
+        loss = (torch.nan_to_num(vm) * wv).sum() + (torch.nan_to_num(nm) * wn).sum()
+        loss.backward()
+        outs.append((vm.detach(), nm.detach(), xi.grad.detach().clone(), sdf.grad.detach().clone()))
+    (v1, n1, x1, s1), (v2, n2, x2, s2) = outs
+    assert torch.equal(torch.nan_to_num(v1, 7.0), torch.nan_to_num(v2, 7.0))
+    assert torch.equal(torch.nan_to_num(n1, 7.0), torch.nan_to_num(n2, 7.0))
+    assert torch.equal(x1, x2) and x1.abs().max() > 0
+    scale = s1.abs().max()
+    assert scale > 0 and (s1 - s2).abs().max() <= 1e-5 * scale
