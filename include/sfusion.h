@@ -235,20 +235,29 @@ int sf_CheckBlockVisibility(sf_context *ctx, sf_map *map, sf_mat3 Rview,
                             uint32_t *host_data);
 /* FuseMapColor (RenderScene.h:45; FuseMap.cu:1039-1162): allocate blocks
  * along each raw-depth ray, compact the visible blocks, integrate
- * TSDF/weight/colour and, when num_detection > 0, fuse labels from `mask`.
+ * TSDF/weight/colour and, when num_detection > 0, fuse labels from `mask`
+ * and run the UnifyNeighbor pass (sf_UnifyNeighbor).
  * depth: float (raw metres), color: uchar3, nmap: float4, mask: uint8. */
 int sf_FuseMapColor(sf_context *ctx, sf_map *map, sf_image depth,
                     sf_image color, sf_image nmap, sf_image mask,
                     int num_detection, sf_mat3 Rview, sf_mat3 RviewInv,
                     sf_float3 tview, float fx, float fy, float cx, float cy,
                     float depth_max, float depth_min, uint32_t *host_data);
-/* AnalyzeMapSemantics (RenderScene.h:57; FuseMap.cu:1164-1247), without
- * the racy UnifyNeighbor pass. */
+/* AnalyzeMapSemantics (RenderScene.h:57; FuseMap.cu:1164-1247): visible
+ * blocks, the label pass, then the UnifyNeighbor pass. */
 int sf_AnalyzeMapSemantics(sf_context *ctx, sf_map *map, sf_image depth,
                            sf_image color, sf_image nmap, sf_image mask,
                            int num_detection, sf_mat3 Rview, sf_mat3 RviewInv,
                            sf_float3 tview, float fx, float fy, float cx,
                            float cy, float depth_max, float depth_min);
+/* UnifyNeighborKernel (FuseMap.cu:757-896, launched at :1158-1160 and
+ * :1244-1246): every labelled voxel (weight > 0) of the blocks in hash slots
+ * [0, visible count of the map's last visibility pass) takes the label most
+ * of its 26 neighbours carry.  Each voxel updates from the state at the
+ * start of the pass (the reference's in-place kernel races with its own
+ * neighbour reads).  The first call allocates 4 bytes per voxel of the
+ * block pool as the pass's output buffer. */
+int sf_UnifyNeighbor(sf_context *ctx, sf_map *map);
 
 /* -------------------------------------------------------------- raycast */
 /* CreateRenderingBlocks (RenderScene.h:20; RenderScene.cu:210-289).

@@ -70,7 +70,10 @@ def lib():
                 "sfo_visibility": (C.c_uint, [vp, F32P, F32P, F32P, C.c_int, C.c_int] + [C.c_float] * 6),
                 "sfo_integrate": (None, [vp, F32P, U8P, C.c_int, C.c_int, F32P, F32P] + [C.c_float] * 6),
                 "sfo_semantics": (None, [vp, F32P, U8P, F32P, U8P, C.c_int, C.c_int, C.c_int, F32P, F32P] + [C.c_float] * 6),
-                "sfo_fuse": (C.c_uint, [vp, F32P, U8P, F32P, U8P, C.c_int, C.c_int, C.c_int, F32P, F32P, F32P] + [C.c_float] * 4),
+                "sfo_unify_neighbor": (None, [vp]),
+                "sfo_map_set_no_visible": (None, [vp, C.c_uint]),
+                "sfo_fuse": (C.c_uint, [vp, F32P, U8P, F32P, U8P, C.c_int, C.c_int, C.c_int, F32P, F32P, F32P] + [C.c_float] * 4
+                             + [C.c_int]),
                 "sfo_zrange": (C.c_int, [vp, F32P, F32P, C.c_int, C.c_int, C.c_float, C.c_float, F32P, F32P]
                                + [C.c_float] * 4 + [vp, C.c_int, C.POINTER(C.c_uint)]),
                 "sfo_reloc_score": (None, [vp, F32P, C.c_int, C.c_int, C.c_int, F32P, C.c_int, C.c_float, vp]),
@@ -295,7 +298,22 @@ class Map:
                             num_detection, cols, rows, _p(RI, F32P), _p(t, F32P), *map(float, K),
                             self.cfg.depth_max, self.cfg.depth_min)
 
-    def fuse(self, depth, rgb, nmap_, mask, num_detection, P, K):
+    def unify_neighbor(self, nvis=None):
+        """Fusion::UnifyNeighbor over hash entries [0, noVisible); `nvis`
+        first sets noVisible."""
+        if nvis is not None:
+            lib().sfo_map_set_no_visible(self.h, int(nvis))
+        lib().sfo_unify_neighbor(self.h)
+
+    def analyze_semantics(self, depth, rgb, nmap_, mask, num_detection, P, K):
+        """AnalyzeMapSemantics (FuseMap.cu:1164-1247) after its visibility
+        pass: the label pass, then UnifyNeighbor."""
+        self.semantics(depth, rgb, nmap_, mask, num_detection, P, K)
+        self.unify_neighbor()
+
+    def fuse(self, depth, rgb, nmap_, mask, num_detection, P, K, unify=True):
+        """FuseMapColor.  unify=False stops before the UnifyNeighbor pass
+        (which then runs as unify_neighbor())."""
         depth, nmap_ = _f32(depth), _f32(nmap_)
         rgb = np.ascontiguousarray(rgb, np.uint8)
         rows, cols = depth.shape
@@ -303,7 +321,7 @@ class Map:
         R, RI, t = pose_to_gpu(P)
         return lib().sfo_fuse(self.h, _p(depth, F32P), _p(rgb, U8P), _p(nmap_, F32P), _p(mask, U8P),
                               num_detection, cols, rows, _p(R, F32P), _p(RI, F32P), _p(t, F32P),
-                              *map(float, K))
+                              *map(float, K), 1 if unify else 0)
 
     def zrange(self, P, K, zc, zr, max_blocks=0):
         _, RI, t = pose_to_gpu(P)

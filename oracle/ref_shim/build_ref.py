@@ -12,17 +12,21 @@ The rewrites only make the CUDA sources compile as serial host C++:
   * Utility/ParallelScan.h is replaced by a serial prefix offset;
   * DeviceMap's static constexpr constants take the golden configuration's
     values (voxel size, truncation, table sizes);
-  * FuseMapColor's SemanticAnalysisKernel launch uses the (8, 8) thread block
-    that AnalyzeMapSemantics uses (the (8, 8, 8) launch applies one update per
-    z-thread, a race on the GPU), and the racy UnifyNeighbor pass is left out
-    of both launchers;
+  * FuseMapColor's SemanticAnalysisKernel and UnifyNeighborKernel launches
+    use the (8, 8) thread block that AnalyzeMapSemantics uses (the (8, 8, 8)
+    launch applies one update per z-thread, a race on the GPU);
+  * UnifyNeighbor's in-place write of each voxel's label fields goes to a
+    copy of the voxel array taken at the launch, which replaces the array
+    after it, so every voxel updates from the pass-start state (on the GPU
+    neighbours read voxels other threads are rewriting, a race);
   * FuseMapColor's GarbageCollectKernel is left out: it only overwrites the
     visible-list copy's ptr with EntryToDelete, after which the label pass
     would index voxelBlocks[EntryToDelete + locId] (FuseMap.cu:176-207,
     518-582) instead of the block's own voxels;
   * a function computing ICPReduce::getRow per pixel is appended to
     Reduction.cu's copy (the reference reduces rows with warp shuffles,
-    which the serial emulation does not model).
+    which the serial emulation does not model), and one launching
+    UnifyNeighborKernel alone over a given grid to FuseMap.cu's copy.
 
 Nothing here is shipped or imported by the product.
 """
@@ -72,6 +76,18 @@ extern "C" void ref_icp_rows_impl(const float *vc, const float *vl, const float 
   icp.fx = fx; icp.fy = fy; icp.cx = cx; icp.cy = cy;
   icp.angleThresh = 0.6; icp.distThresh = 0.1;  // as ICPStep sets them
   for (int i = 0; i < cols * rows; ++i) icp.getRow(i, out29 + 29 * (size_t)i);
+}
+'''
+
+
+FUSE_APPENDIX = r'''
+// ---- appended by oracle/ref_shim/build_ref.py: UnifyNeighborKernel alone ----
+extern "C" void ref_unify_neighbor_impl(DeviceMap map, unsigned nvis) {
+  Fusion fuse;
+  fuse.map = map;
+  shim_unify_begin(map.voxelBlocks.data, map.voxelBlocks.size * sizeof(Voxel));
+  shim_launch_any(dim3(nvis), dim3(8, 8), [&] { UnifyNeighborKernel(fuse); });
+  shim_unify_end();
 }
 '''
 
@@ -176,14 +192,22 @@ def patch_sources(name, text, cfg):
         launch = "SemanticAnalysisKernel<<<block, thread>>>(fuse);"
         first = text.index(launch)
         text = text[:first] + "thread = dim3(8, 8);\n\t\t" + text[first:]
-        n_un = text.count("UnifyNeighborKernel<<<block, thread>>>(fuse);")
-        assert n_un == 2, n_un
-        text = text.replace("UnifyNeighborKernel<<<block, thread>>>(fuse);",
-                            "/* UnifyNeighbor pass left out by the recipe */")
+        # UnifyNeighbor writes `cur` in place while other threads read it as
+        # a neighbour; the write goes to the launch's copy of the voxel array
+        # instead (shim_unify_begin/end in include/cuda_runtime.h).
+        cur = "Voxel &cur = map.voxelBlocks[entry.ptr + locId];"
+        assert text.count(cur) == 1
+        text = text.replace(cur, "Voxel &cur = ((Voxel *)shim_unify_dst)[entry.ptr + locId];")
+        un = "UnifyNeighborKernel<<<block, thread>>>(fuse);"
+        assert text.count(un) == 2, text.count(un)
+        text = text.replace(un, "shim_unify_begin(fuse.map.voxelBlocks.data, fuse.map.voxelBlocks.size * "
+                                "sizeof(Voxel));\n\t\t" + un + "\n\t\tshim_unify_end();")
     if name.endswith(".cu"):
         text = rewrite_launches(text)
     if name == "Reduction.cu":
         text += ICP_APPENDIX
+    if name == "FuseMap.cu":
+        text += FUSE_APPENDIX
     return text
 
 

@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <vector>
 
 #define __device__
 #define __host__
@@ -182,5 +183,29 @@ template <class G, class B, class F>
 inline void shim_launch_any(G g, B b, F &&f) {
   shim_launch(dim3(g), dim3(b), f);
 }
+
+// Double buffer around the UnifyNeighbor launch: the pass writes each
+// voxel's label fields into a copy of the voxel array taken at the launch
+// while its neighbour lookups read the array itself, and the copy replaces
+// the array after the launch.  Every voxel then updates from the pass-start
+// state, the deterministic form of the in-place GPU pass.
+struct ShimUnifyBuffer {
+  std::vector<unsigned char> copy;
+  void *src = nullptr;
+};
+inline ShimUnifyBuffer &shim_unify_buffer() {
+  static ShimUnifyBuffer b;
+  return b;
+}
+inline void shim_unify_begin(void *voxels, size_t bytes) {
+  ShimUnifyBuffer &b = shim_unify_buffer();
+  b.src = voxels;
+  b.copy.assign((const unsigned char *)voxels, (const unsigned char *)voxels + bytes);
+}
+inline void shim_unify_end() {
+  ShimUnifyBuffer &b = shim_unify_buffer();
+  memcpy(b.src, b.copy.data(), b.copy.size());
+}
+#define shim_unify_dst ((void *)shim_unify_buffer().copy.data())
 
 #endif

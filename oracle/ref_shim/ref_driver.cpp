@@ -15,6 +15,7 @@ thread_local uint3 blockIdx;
 thread_local dim3 blockDim;
 thread_local dim3 gridDim;
 
+extern "C" void ref_unify_neighbor_impl(DeviceMap map, unsigned nvis);
 extern "C" void ref_icp_rows_impl(const float *, const float *, const float *, const float *, int, int,
                                   const float *, const float *, const float *, const float *,
                                   const float *, float, float, float, float, float *);
@@ -226,6 +227,13 @@ int ref_map_raytrace(void *mp, int cols, int rows, const float *R, const float *
 const void *ref_map_entries(void *mp) { return ((RefMap *)mp)->hashEntries.data; }
 const void *ref_map_visible(void *mp) { return ((RefMap *)mp)->visibleEntries.data; }
 const void *ref_map_voxels(void *mp) { return ((RefMap *)mp)->sdfBlock.data; }
+// UnifyNeighborKernel over hash slots [0, nvis) with the (8, 8) block of
+// AnalyzeMapSemantics (FuseMap.cu:1244-1246).
+void ref_map_unify(void *mp, unsigned nvis) {
+  RefMap &m = *(RefMap *)mp;
+  ref_unify_neighbor_impl(m.view(), nvis);
+}
+
 void ref_map_counters(void *mp, int *out) {
   RefMap &m = *(RefMap *)mp;
   m.heapCounter.download(out + 0);

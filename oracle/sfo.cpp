@@ -721,7 +721,14 @@ extern "C" void sfo_map_counters(sfo_map *m, int *out) {
   out[0] = m->heapCounter; out[1] = m->entryPtr; out[2] = (int)m->noVisible; out[3] = alloc;
 }
 
-// Fusion::CreateBlocks, FuseMap.cu:92-132 (unproject :35-44), serial order.
+extern "C" void sfo_map_set_no_visible(sfo_map *m, unsigned n) { m->noVisible = n; }
+
+// Fusion::CreateBlocks, FuseMap.cu:92-132 (unproject :35-44), run serially
+// in the launch order of its (16, 8) thread blocks (FuseMap.cu:1093-1096):
+// block rows, blocks, thread rows, threads.  The order decides which of two
+// blocks new in the same frame with the same bucket holds the bucket slot
+// (a race on the GPU); UnifyNeighbor's pass over hash slots [0, noVisible)
+// depends on it.
 extern "C" void sfo_alloc(sfo_map *m, const float *depth, int cols, int rows,
                           const float *R, const float *t, float fx, float fy,
                           float cx, float cy) {
@@ -729,27 +736,30 @@ extern "C" void sfo_alloc(sfo_map *m, const float *depth, int cols, int rows,
   f3 tv = f3_from(t);
   const float invfx = (float)(1.0 / (double)fx), invfy = (float)(1.0 / (double)fy);
   const float dmin = m->c.depth_min, dmax = m->c.depth_max;
-  for (int y = 0; y < rows; ++y)
-    for (int x = 0; x < cols; ++x) {
-      float z = depth[y * cols + x];
-      if (std::isnan(z) || z < dmin || z > dmax) continue;
-      float thresh = m->c.trunc_dist / 2.0f;
-      float z_near = std::fmax(dmin, z - thresh);
-      float z_far = std::fmin(dmax, z + thresh);
-      if (z_near >= z_far) continue;
-      f3 pn = {z_near * ((float)x - cx) * invfx, z_near * ((float)y - cy) * invfy, z_near};
-      f3 pf = {z_far * ((float)x - cx) * invfx, z_far * ((float)y - cy) * invfy, z_far};
-      f3 pt_near = (mul(Rv, pn) + tv) * m->voxelSizeInv;
-      f3 pt_far = (mul(Rv, pf) + tv) * m->voxelSizeInv;
-      f3 dir = pt_far - pt_near;
-      float length = norm(dir);
-      int nSteps = f2i(std::ceil(2.0 * (double)length));
-      dir = dir / (float)(nSteps - 1);
-      for (int i = 0; i < nSteps; ++i) {
-        create_block(*m, vox2block(floor3(pt_near)));
-        pt_near = pt_near + dir;
-      }
+  const int tiles_x = (cols + 15) / 16, tiles_y = (rows + 7) / 8;
+  for (int p = 0; p < tiles_x * tiles_y * 128; ++p) {
+    const int tile = p / 128, in = p % 128;
+    const int x = (tile % tiles_x) * 16 + in % 16, y = (tile / tiles_x) * 8 + in / 16;
+    if (x >= cols || y >= rows) continue;
+    float z = depth[y * cols + x];
+    if (std::isnan(z) || z < dmin || z > dmax) continue;
+    float thresh = m->c.trunc_dist / 2.0f;
+    float z_near = std::fmax(dmin, z - thresh);
+    float z_far = std::fmin(dmax, z + thresh);
+    if (z_near >= z_far) continue;
+    f3 pn = {z_near * ((float)x - cx) * invfx, z_near * ((float)y - cy) * invfy, z_near};
+    f3 pf = {z_far * ((float)x - cx) * invfx, z_far * ((float)y - cy) * invfy, z_far};
+    f3 pt_near = (mul(Rv, pn) + tv) * m->voxelSizeInv;
+    f3 pt_far = (mul(Rv, pf) + tv) * m->voxelSizeInv;
+    f3 dir = pt_far - pt_near;
+    float length = norm(dir);
+    int nSteps = f2i(std::ceil(2.0 * (double)length));
+    dir = dir / (float)(nSteps - 1);
+    for (int i = 0; i < nSteps; ++i) {
+      create_block(*m, vox2block(floor3(pt_near)));
+      pt_near = pt_near + dir;
     }
+  }
 }
 
 namespace {
@@ -961,18 +971,107 @@ extern "C" void sfo_semantics(sfo_map *m, const float *depth, const uint8_t *rgb
   }
 }
 
+// Fusion::UnifyNeighbor and UpdateNeighborLabel, FuseMap.cu:757-896: the
+// (8, 8) launch over hash entries [0, noVisible) (the kernel indexes
+// hashEntries[blockIdx.x] with a grid of noVisibleBlocks, FuseMap.cu:802-808,
+// :1158-1160, :1244).  One thread per (x, y) voxel column, its 4-slot
+// neighbour table kept across the column's z loop (declared outside it,
+// FuseMap.cu:812-816).  Every voxel updates from the pass-start state: new
+// label fields go to `out` and are applied after the pass.
+extern "C" void sfo_unify_neighbor(sfo_map *m) {
+  const float vs = m->c.voxel_size;
+  const float step = vs * (float)1;  // VoxelSize * r, r = 1 (FuseMap.cu:833)
+  const unsigned n = std::min<unsigned>(m->noVisible, m->numEntries);
+  // the 26 neighbours in UnifyNeighbor's order (FuseMap.cu:834-887)
+  static const int8_t kOrder[26][3] = {
+      {1, 0, 0},  {1, 1, 0},  {1, -1, 0},  {1, 0, 1},  {1, 0, -1},  {1, 1, 1},   {1, 1, -1},
+      {1, -1, 1}, {1, -1, -1}, {-1, 0, 0}, {-1, 1, 0}, {-1, -1, 0}, {-1, 0, 1},  {-1, 0, -1},
+      {-1, 1, 1}, {-1, 1, -1}, {-1, -1, 1}, {-1, -1, -1}, {0, 1, 0}, {0, 1, 1},  {0, 1, -1},
+      {0, -1, 0}, {0, -1, 1},  {0, -1, -1}, {0, 0, 1},  {0, 0, -1}};
+  struct Upd { size_t idx; uint8_t label, count, label_2, count_2; };
+  std::vector<Upd> out;
+  for (unsigned b = 0; b < n; ++b) {
+    const sfo_entry &entry = m->entries[b];
+    if (entry.ptr == -1) continue;
+    i3 bp = {(int)((uint32_t)entry.x * 8u), (int)((uint32_t)entry.y * 8u), (int)((uint32_t)entry.z * 8u)};
+    for (int ty = 0; ty < 8; ++ty)
+      for (int tx = 0; tx < 8; ++tx) {
+        int nl[4] = {-1, -1, -1, -1}, nc[4] = {0, 0, 0, 0}, nlc[4] = {0, 0, 0, 0};
+        for (int i = 0; i < 8; ++i) {
+          const size_t idx = (size_t)entry.ptr + i * 64 + ty * 8 + tx;
+          const sfo_voxel &cur = m->voxels[idx];
+          const int cur_label = cur.weight == 0 ? -1 : (int)cur.label;
+          if (cur_label == -1) continue;
+          // voxelPosToWorldPos (DeviceMap.cu:165-167): int3 * float
+          const f3 pos = {(float)(bp.x + tx) * vs, (float)(bp.y + ty) * vs, (float)(bp.z + i) * vs};
+          for (int k = 0; k < 26; ++k) {
+            f3 np = pos;
+            if (kOrder[k][0]) np.x = kOrder[k][0] > 0 ? pos.x + step : pos.x - step;
+            if (kOrder[k][1]) np.y = kOrder[k][1] > 0 ? pos.y + step : pos.y - step;
+            if (kOrder[k][2]) np.z = kOrder[k][2] > 0 ? pos.z + step : pos.z - step;
+            // FindVoxel(float3) -> worldPosToVoxelPos (DeviceMap.cu:83-95, 156-159)
+            const i3 v = floor3({np.x / vs, np.y / vs, np.z / vs});
+            const sfo_entry *e = find_entry(*m, vox2block(v));
+            if (!e) continue;
+            const sfo_voxel &nb = m->voxels[(size_t)e->ptr + vox2local(v)];
+            const int tmp_label = nb.weight == 0 ? -1 : (int)nb.label;
+            if (tmp_label == -1) continue;
+            for (int l = 0; l < 4; ++l) {
+              if (nl[l] == tmp_label) {
+                nc[l]++;
+                nlc[l] = nlc[l] > (int)nb.count ? nlc[l] : (int)nb.count;
+                break;
+              } else if (nl[l] == -1) {
+                nl[l] = tmp_label;
+                nc[l] = 1;
+                nlc[l] = (int)nb.count;
+                break;
+              }
+            }
+          }
+          int nei_label = -1, nei_count = 0, nei_lc = 0;
+          for (int j = 0; j < 4; ++j)
+            if (nl[j] != -1 && nlc[j] != 0 && nc[j] > nei_count) {
+              nei_label = nl[j];
+              nei_count = nc[j];
+              nei_lc = nlc[j];
+            }
+          Upd u{idx, cur.label, cur.count, cur.label_2, cur.count_2};
+          if (cur_label != nei_label) {
+            const int tmp = cur_label == (int)cur.label_2
+                                ? (nei_lc > (int)cur.count_2 ? nei_lc : (int)cur.count_2 + 5)
+                                : nei_lc;
+            u.label_2 = cur.label;
+            u.count_2 = cur.count;
+            u.label = (uint8_t)nei_label;
+            u.count = (uint8_t)tmp;
+          } else {
+            u.count = (uint8_t)nei_lc;
+          }
+          out.push_back(u);
+        }
+      }
+  }
+  for (const Upd &u : out) {
+    sfo_voxel &v = m->voxels[u.idx];
+    v.label = u.label; v.count = u.count; v.label_2 = u.label_2; v.count_2 = u.count_2;
+  }
+}
+
 extern "C" unsigned sfo_fuse(sfo_map *m, const float *depth, const uint8_t *rgb,
                              const float *nmap, const uint8_t *mask,
                              int num_detection, int cols, int rows, const float *R,
                              const float *Rinv, const float *t, float fx, float fy,
-                             float cx, float cy) {
+                             float cx, float cy, int unify) {
   sfo_alloc(m, depth, cols, rows, R, t, fx, fy, cx, cy);
   unsigned n = sfo_visibility(m, R, Rinv, t, cols, rows, fx, fy, cx, cy, m->c.depth_max, m->c.depth_min);
   if (n == 0) return 0;
   sfo_integrate(m, depth, rgb, cols, rows, Rinv, t, fx, fy, cx, cy, m->c.depth_max, m->c.depth_min);
-  if (num_detection > 0)
+  if (num_detection > 0) {
     sfo_semantics(m, depth, rgb, nmap, mask, num_detection, cols, rows, Rinv, t, fx, fy, cx, cy,
                   m->c.depth_max, m->c.depth_min);
+    if (unify) sfo_unify_neighbor(m);  // FuseMapColor, FuseMap.cu:1155-1160
+  }
   return n;
 }
 
@@ -1567,7 +1666,7 @@ extern "C" int sfo_system_grab(sfo_system *s, const uint16_t *depth, const uint8
     float R[9], RI[9], t[3];
     pose_to_gpu(f.pose, R, RI, t);
     nvis = sfo_fuse(s->map, f.raw.data(), rgb, f.nmap[0].data(), mask, num_detection, s->cols,
-                    s->rows, R, RI, t, s->K[0], s->K[1], s->K[2], s->K[3]);
+                    s->rows, R, RI, t, s->K[0], s->K[1], s->K[2], s->K[3], 1);
     // Mapping::RayTrace (Mapping.cc:142-161): raycast only if the z-range
     // pass produced rendering blocks; else vmap[0]/nmap[0] keep the
     // measured maps.

@@ -76,6 +76,8 @@ sfo_map *sfo_map_create(const sfo_config *cfg);
 void sfo_map_destroy(sfo_map *m);
 void sfo_map_reset(sfo_map *m);
 sfo_entry *sfo_map_entries(sfo_map *m);
+// Sets the visible count a state loaded into the map's arrays carries.
+void sfo_map_set_no_visible(sfo_map *m, unsigned n);
 sfo_voxel *sfo_map_voxels(sfo_map *m);
 sfo_entry *sfo_map_visible(sfo_map *m);
 int *sfo_map_heap(sfo_map *m);
@@ -97,12 +99,15 @@ void sfo_semantics(sfo_map *m, const float *depth, const uint8_t *rgb,
                    int cols, int rows, const float *Rinv, const float *t,
                    float fx, float fy, float cx, float cy, float depth_max,
                    float depth_min);
+// Fusion::UnifyNeighbor over hash entries [0, noVisible) (FuseMap.cu:757-896).
+void sfo_unify_neighbor(sfo_map *m);
 // FuseMapColor order (FuseMap.cu:1039-1162): alloc, visibility, integrate,
-// [semantics].  Returns the visible count.
+// [semantics, and UnifyNeighbor when unify != 0].  Returns the visible count.
 unsigned sfo_fuse(sfo_map *m, const float *depth, const uint8_t *rgb,
                   const float *nmap, const uint8_t *mask, int num_detection,
                   int cols, int rows, const float *R, const float *Rinv,
-                  const float *t, float fx, float fy, float cx, float cy);
+                  const float *t, float fx, float fy, float cx, float cy,
+                  int unify);
 // CreateRenderingBlocks (RenderScene.cu:210-289) into zmin/zmax images of
 // zc x zr floats.  Returns the reference's bool.  blocks_out (optional,
 // 4 shorts + 2 floats each) receives the rendering-block list; *nblocks the

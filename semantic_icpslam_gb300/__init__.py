@@ -122,6 +122,11 @@ class Map:
         call("sf_map_counters", ctx.h, self.h, out)
         return list(out)
 
+    def unify_neighbor(self, ctx):
+        """sf_UnifyNeighbor: the neighbour-label pass over hash slots
+        [0, visible count) (UnifyNeighborKernel)."""
+        call("sf_UnifyNeighbor", ctx.h, self.h)
+
     def write(self, ctx, path):
         """map.bin in the reference's byte layout (System::WriteMapToDisk)."""
         call("sf_map_write", ctx.h, self.h, os.fsencode(path))

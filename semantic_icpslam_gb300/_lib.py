@@ -134,6 +134,7 @@ SIGNATURES = {
                        + [U32P],
     "sf_AnalyzeMapSemantics": [vp, vp, Image, Image, Image, Image, C.c_int, Mat3, Mat3, Float3]
                               + [C.c_float] * 6,
+    "sf_UnifyNeighbor": [vp, vp],
     "sf_CreateRenderingBlocks": [vp, vp, Image, Image, C.c_float, C.c_float, vp, vp, Mat3, Float3, C.c_uint32]
                                 + [C.c_float] * 4 + [I32P],
     "sf_Raycast": [vp, vp, Image, Image, Image, Image, Mat3, Mat3, Float3] + [C.c_float] * 4,

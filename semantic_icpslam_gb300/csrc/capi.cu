@@ -656,6 +656,10 @@ int sf_FuseMapColor(sf_context *ctx, sf_map *m, sf_image depth, sf_image color, 
   launch_integrate(m->d, depth, color, num_detection > 0 ? &nmap : nullptr,
                    num_detection > 0 ? &mask : nullptr, num_detection, ctx->cam, true,
                    num_detection > 0, nullptr, ctx->stream);
+  if (num_detection > 0) {  // FuseMap.cu:1141-1160
+    if ((st = fuse_scratch_unify(m->scratch, m->d.c))) return st;
+    launch_unify_neighbor(m->d, m->scratch, nullptr, ctx->stream);
+  }
   SF_CHECK(cudaGetLastError());
   SF_CHECK(cudaStreamSynchronize(ctx->stream));
   return SF_OK;
@@ -676,6 +680,18 @@ int sf_AnalyzeMapSemantics(sf_context *ctx, sf_map *m, sf_image depth, sf_image 
   launch_visibility(m->d, m->scratch, ctx->cam, nullptr, nullptr, nullptr, ctx->flags, ctx->stream);
   launch_integrate(m->d, depth, color, &nmap, num_detection > 0 ? &mask : nullptr, num_detection,
                    ctx->cam, false, true, nullptr, ctx->stream);
+  if ((st = fuse_scratch_unify(m->scratch, m->d.c))) return st;
+  launch_unify_neighbor(m->d, m->scratch, nullptr, ctx->stream);
+  SF_CHECK(cudaGetLastError());
+  SF_CHECK(cudaStreamSynchronize(ctx->stream));
+  return SF_OK;
+}
+
+int sf_UnifyNeighbor(sf_context *ctx, sf_map *m) {
+  if (!ctx || !m) return SF_ERR_INVALID;
+  int st = fuse_scratch_unify(m->scratch, m->d.c);
+  if (st) return st;
+  launch_unify_neighbor(m->d, m->scratch, nullptr, ctx->stream);
   SF_CHECK(cudaGetLastError());
   SF_CHECK(cudaStreamSynchronize(ctx->stream));
   return SF_OK;

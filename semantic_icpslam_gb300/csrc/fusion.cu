@@ -4,8 +4,9 @@
 // Reference: Mapping/DeviceMap.cu (Hash :3-10, CreateEntry :12-21,
 // CreateBlock :23-69, FindEntry :141-154), Mapping/FuseMap.cu
 // (CreateBlocks :92-132, CheckFullVisibility :134-168, createVoxels
-// :432-507, analyzeSemantics :509-668, ResetHash/ResetSdfBlock
-// :1251-1304) and Utility/ParallelScan.h (ComputeOffset).
+// :432-507, analyzeSemantics :509-668, UnifyNeighbor :757-896,
+// ResetHash/ResetSdfBlock :1251-1304) and Utility/ParallelScan.h
+// (ComputeOffset).
 //
 // GB300 form:
 //  * Allocation is two lock-free passes.  Probe: every raw-depth pixel walks
@@ -23,6 +24,8 @@
 //  * Integration is a persistent grid over the visible list, one voxel per
 //    thread with 128-bit loads and stores; label fusion runs on the same
 //    voxel in the same pass.
+//  * UnifyNeighbor is two launches around a 4-byte-per-voxel buffer, so
+//    every voxel updates from the pass-start state.
 #include "sf_kernels.cuh"
 #include "sf_render.cuh"
 
@@ -567,6 +570,162 @@ __device__ __forceinline__ void semantic_voxel(sf_voxel &prev, uint8_t label, f3
   }
 }
 
+// ------------------------------------------------------ neighbour labels
+// Fusion::UnifyNeighbor + UpdateNeighborLabel (FuseMap.cu:757-896): for the
+// hash slots [0, noVisible) (the kernel indexes hashEntries[blockIdx.x] over
+// a grid of noVisibleBlocks), each labelled voxel takes the label most of
+// its 26 neighbours carry.  One thread per (x, y) voxel column, as the
+// (8, 8) launch; the 4-slot neighbour table lives across the column's z
+// loop as in the reference.  k_unify_compute writes each processed voxel's
+// new {label, count, label_2, count_2} word to `out` while reading only the
+// voxel array, and k_unify_apply copies the words back, so every voxel
+// updates from the pass-start state (in place, the reference's neighbours
+// read voxels other threads are rewriting).
+constexpr int kUnifyThreads = 64;
+
+// UnifyNeighbor's 26 offsets in its order (FuseMap.cu:834-887), as
+// (dx + 1) | (dy + 1) << 2 | (dz + 1) << 4.
+__constant__ uint8_t kUnifyOrder[26] = {
+    0x16, 0x1a, 0x12, 0x26, 0x06, 0x2a, 0x0a, 0x22, 0x02, 0x14, 0x18, 0x10, 0x24,
+    0x04, 0x28, 0x08, 0x20, 0x00, 0x19, 0x29, 0x09, 0x11, 0x21, 0x01, 0x25, 0x05};
+
+// make_int3(float) on one axis: floor (VectorMath.h:36-42).
+__device__ __forceinline__ int floor1i(float a) {
+  const int b = (int)a;
+  return (float)b > a ? b - 1 : b;
+}
+// worldPosToVoxelPos of pos - step, pos, pos + step on one axis
+// (DeviceMap.cu:156-159).
+struct AxisCands {
+  int lo, mid, hi;
+  __device__ __forceinline__ AxisCands(float pos, float step, float vs)
+      : lo(floor1i((pos - step) / vs)), mid(floor1i(pos / vs)), hi(floor1i((pos + step) / vs)) {}
+  __device__ __forceinline__ int at(unsigned d) const { return d == 0u ? lo : (d == 1u ? mid : hi); }
+};
+
+// UpdateNeighborLabel's 4-slot table (FuseMap.cu:757-796) in registers:
+// label (-1 = free), neighbours seen, and their largest count.
+struct NeighborTable {
+  int l0 = -1, l1 = -1, l2 = -1, l3 = -1;
+  int c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+  int lc0 = 0, lc1 = 0, lc2 = 0, lc3 = 0;
+  // The first slot holding `lab` counts it; else the first free slot takes
+  // it; a full table drops it.
+  __device__ __forceinline__ static bool slot(int &l, int &c, int &lc, int lab, int cnt) {
+    if (l == lab) {
+      ++c;
+      lc = lc > cnt ? lc : cnt;
+      return true;
+    }
+    if (l == -1) {
+      l = lab;
+      c = 1;
+      lc = cnt;
+      return true;
+    }
+    return false;
+  }
+  __device__ __forceinline__ void add(int lab, int cnt) {
+    if (slot(l0, c0, lc0, lab, cnt)) return;
+    if (slot(l1, c1, lc1, lab, cnt)) return;
+    if (slot(l2, c2, lc2, lab, cnt)) return;
+    slot(l3, c3, lc3, lab, cnt);
+  }
+  // The labelled slot (count > 0) seen most often; the first wins ties.
+  __device__ __forceinline__ static void pick(int l, int c, int lc, int &best_l, int &best_c, int &best_lc) {
+    if (l != -1 && lc != 0 && c > best_c) {
+      best_l = l;
+      best_c = c;
+      best_lc = lc;
+    }
+  }
+};
+
+__device__ __forceinline__ void unify_column(const DevMap &m, uint32_t *out, int4 h, int tx, int ty) {
+  const float vs = m.c.voxel_size;
+  const float step = vs * (float)1;  // VoxelSize * r, r = 1
+  const int bx = (int)((uint32_t)h.x * 8u), by = (int)((uint32_t)h.y * 8u), bz = (int)((uint32_t)h.z * 8u);
+  const AxisCands cx((float)(bx + tx) * vs, step, vs), cy((float)(by + ty) * vs, step, vs);
+  NeighborTable t;
+  i3 cache_pos = mk_i3(h.x, h.y, h.z);
+  int cache_ptr = h.w;
+  for (int i = 0; i < 8; ++i) {
+    const int idx = h.w + i * 64 + ty * 8 + tx;
+    const uint32_t *cw = (const uint32_t *)(m.voxels + idx);
+    const uint32_t w1 = __ldg(cw + 1), w2 = __ldg(cw + 2);
+    uint32_t res = w2;
+    if ((w1 & 0xffu) != 0u) {
+      const int cur_label = (int)(w2 & 0xffu);
+      const AxisCands cz((float)(bz + i) * vs, step, vs);
+      for (int k = 0; k < 26; ++k) {
+        const unsigned o = kUnifyOrder[k];
+        const i3 v = mk_i3(cx.at(o & 3u), cy.at((o >> 2) & 3u), cz.at((o >> 4) & 3u));
+        const i3 b = vox2block(v);
+        int ptr;
+        if (b.x == cache_pos.x && b.y == cache_pos.y && b.z == cache_pos.z) {
+          ptr = cache_ptr;
+        } else {
+          ptr = find_block(m, b);
+          cache_pos = b;
+          cache_ptr = ptr;
+        }
+        if (ptr < 0) continue;
+        const uint32_t *nw = (const uint32_t *)(m.voxels + ptr + vox2local(v));
+        if ((__ldg(nw + 1) & 0xffu) == 0u) continue;  // weight 0: label -1
+        const uint32_t n2 = __ldg(nw + 2);
+        const int lab = (int)(n2 & 0xffu), cnt = (int)((n2 >> 8) & 0xffu);
+        t.add(lab, cnt);
+      }
+      int nei_label = -1, nei_count = 0, nei_lc = 0;
+      t.pick(t.l0, t.c0, t.lc0, nei_label, nei_count, nei_lc);
+      t.pick(t.l1, t.c1, t.lc1, nei_label, nei_count, nei_lc);
+      t.pick(t.l2, t.c2, t.lc2, nei_label, nei_count, nei_lc);
+      t.pick(t.l3, t.c3, t.lc3, nei_label, nei_count, nei_lc);
+      const uint32_t count = (w2 >> 8) & 0xffu, label_2 = (w2 >> 16) & 0xffu, count_2 = w2 >> 24;
+      if (cur_label != nei_label) {
+        const int tmp = cur_label == (int)label_2 ? (nei_lc > (int)count_2 ? nei_lc : (int)count_2 + 5) : nei_lc;
+        res = ((uint32_t)nei_label & 0xffu) | (((uint32_t)tmp & 0xffu) << 8) | ((uint32_t)cur_label << 16) |
+              (count << 24);
+      } else {
+        res = (w2 & 0xffff00ffu) | (((uint32_t)nei_lc & 0xffu) << 8);
+      }
+    }
+    out[idx] = res;
+  }
+}
+
+__global__ void __launch_bounds__(kUnifyThreads) k_unify_compute(DevMap m, uint32_t *out, const int *run_flag) {
+  if (run_flag && *run_flag == 0) return;
+  const unsigned n = min(*m.no_visible, m.c.num_entries);
+  __shared__ int4 s_head[kUnifyThreads];
+  __shared__ int s_cnt;
+  const int tx = threadIdx.x & 7, ty = threadIdx.x >> 3;
+  for (unsigned base = blockIdx.x * kUnifyThreads; base < n; base += gridDim.x * kUnifyThreads) {
+    const unsigned e = base + threadIdx.x;
+    const int4 h = e < n ? entry_head(m.entries + e) : make_int4(0, 0, 0, -1);
+    if (threadIdx.x == 0) s_cnt = 0;
+    __syncthreads();
+    if (h.w != -1) s_head[atomicAdd(&s_cnt, 1)] = h;  // entries are independent: order free
+    __syncthreads();
+    const int cnt = s_cnt;
+    for (int k = 0; k < cnt; ++k) unify_column(m, out, s_head[k], tx, ty);
+    __syncthreads();
+  }
+}
+
+__global__ void k_unify_apply(DevMap m, const uint32_t *out, const int *run_flag) {
+  if (run_flag && *run_flag == 0) return;
+  const unsigned n = min(*m.no_visible, m.c.num_entries);
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (unsigned e = grid_tid() >> 5; e < n; e += nwarps) {
+    const int ptr = __ldcg(&m.entries[e].ptr);
+    if (ptr < 0) continue;
+    for (unsigned i = lane; i < 512u; i += 32u)
+      ((uint32_t *)(m.voxels + ptr + i))[2] = __ldcg(out + ptr + i);
+  }
+}
+
 constexpr int kIntThreads = 256;
 
 // Eight 256-thread CTAs per SM (32 registers, a few spilled bytes): the
@@ -671,6 +830,7 @@ void fuse_scratch_free(FuseScratch &f) {
   cudaFree(f.counters);
   cudaFree(f.win);
   cudaFree(f.win_cells);
+  cudaFree(f.unify_out);
   f = FuseScratch();
 }
 
@@ -723,6 +883,17 @@ void launch_visibility(const DevMap &m, const FuseScratch &f, const Cam *c, cons
   k_vis_start<<<sm_count() * 8, 256, 0, s>>>(m, f, c, rendered, zn, zx, do_z ? 1 : 0, run_flag); note_launch();
   k_visibility<<<sm_count() * 4, 256, 0, s>>>(m, f, c, zn, zx, do_z ? 1 : 0, rendered, run_flag,
                                               flags); note_launch();
+}
+
+void launch_unify_neighbor(const DevMap &m, const FuseScratch &f, const int *run_flag, cudaStream_t s) {
+  k_unify_compute<<<sm_count() * 16, kUnifyThreads, 0, s>>>(m, f.unify_out, run_flag); note_launch();
+  k_unify_apply<<<sm_count() * 4, 256, 0, s>>>(m, f.unify_out, run_flag); note_launch();
+}
+
+int fuse_scratch_unify(FuseScratch &f, const MapConst &c) {
+  if (f.unify_out) return SF_OK;
+  const size_t bytes = sizeof(uint32_t) * 512 * (size_t)c.num_sdf_blocks;
+  return cudaMalloc(&f.unify_out, bytes) == cudaSuccess ? SF_OK : SF_ERR_CUDA;
 }
 
 void launch_integrate(const DevMap &m, const sf_image &depth, const sf_image &rgb,

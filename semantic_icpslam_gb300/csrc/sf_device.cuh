@@ -20,6 +20,11 @@ namespace sf {
 struct f3 { float x, y, z; };
 struct m3 { f3 rx, ry, rz; };  // Matrix3f rows (Utility/VectorMath.h:360-375)
 struct i3 { int x, y, z; };
+__host__ __device__ __forceinline__ i3 mk_i3(int x, int y, int z) {
+  i3 r;
+  r.x = x; r.y = y; r.z = z;
+  return r;
+}
 
 __device__ __forceinline__ f3 mk3(float x, float y, float z) { f3 r; r.x = x; r.y = y; r.z = z; return r; }
 __device__ __forceinline__ f3 operator+(f3 a, f3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }

@@ -93,6 +93,9 @@ struct FuseScratch {
   int *win = nullptr;                     // [8]
   int *win_cells = nullptr;               // [win_cap]
   uint32_t win_cap = 0;
+  // UnifyNeighbor's new {label, count, label_2, count_2} words, indexed like
+  // the voxel array; allocated on the first pass with labels.
+  uint32_t *unify_out = nullptr;          // [num_sdf_blocks * 512]
 };
 
 // Start of a frame's allocation pass: clears the per-frame counters and
@@ -132,6 +135,10 @@ void launch_visibility(const DevMap &m, const FuseScratch &f, const Cam *c, cons
                        const sf_image *zmax, const int *run_flag, uint32_t *flags,
                        cudaStream_t s);
 // createVoxels (+ analyzeSemantics when mask != null), FuseMap.cu:432-668.
+// Fusion::UnifyNeighbor over hash slots [0, *no_visible) from the pass-start
+// state (two launches); needs fuse_scratch_unify first.
+int fuse_scratch_unify(FuseScratch &f, const MapConst &c);
+void launch_unify_neighbor(const DevMap &m, const FuseScratch &f, const int *run_flag, cudaStream_t s);
 void launch_integrate(const DevMap &m, const sf_image &depth, const sf_image &rgb,
                       const sf_image *nmap, const sf_image *mask, int num_detection, const Cam *c,
                       bool integrate, bool semantics, const int *run_flag, cudaStream_t s);

@@ -276,6 +276,7 @@ void enqueue_mapping(sf_system *s, const Cam *cam, const int *run, int num_detec
   cudaStreamIsCapturing(st, &cs);
   cudaStreamWaitEvent(st, s->ev_inputs, cs == cudaStreamCaptureStatusActive ? cudaEventWaitExternal : 0);
   launch_integrate(m, depth, rgb, &nm0, &mask, num_detection, cam, true, num_detection > 0, run, st);
+  if (num_detection > 0) launch_unify_neighbor(m, f, run, st);  // FuseMap.cu:1141-1160
   mark(s, st, 5);
   sf_image fv = img(s->d_vmap[0], C, R, 16), fn = img(s->d_nmap[0], C, R, 16);
   launch_raycast(m, f, img(s->d_mv[0], C, R, 16), img(s->d_mn[0], C, R, 16), zmin, zmax, cam,
@@ -390,10 +391,12 @@ int run_plain_frame(sf_system *s, int num_detection) {
     if (cudaMemcpyAsync(&nvis, m.no_visible, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
       return SF_ERR_CUDA;
-    if (nvis > 0)
+    if (nvis > 0) {
       cudaStreamWaitEvent(st, s->ev_inputs, 0);
       launch_integrate(m, depth, rgb, &nm0, &mask, num_detection, cam, true, num_detection > 0,
                        nullptr, st);
+      if (num_detection > 0) launch_unify_neighbor(m, f, nullptr, st);
+    }
     sf_image fv = img(s->d_vmap[0], C, R, 16), fn = img(s->d_nmap[0], C, R, 16);
     launch_raycast(m, f, img(s->d_mv[0], C, R, 16), img(s->d_mn[0], C, R, 16), zmin, zmax, cam,
                    f.counters + 3, &fv, &fn, nullptr, st, s->rc_tune);
@@ -409,6 +412,10 @@ int run_plain_frame(sf_system *s, int num_detection) {
 int run_frame(sf_system *s, int num_detection) {
   cudaStream_t st = ctx_stream(s->ctx);
   ++s->frames;
+  if (num_detection > 0) {  // UnifyNeighbor's output buffer, before any capture
+    int e = fuse_scratch_unify(map_scratch(s->map), map_dev(s->map).c);
+    if (e != SF_OK) return e;
+  }
   if (s->cfg.use_graph == 0) return run_plain_frame(s, num_detection);
   if (s->cfg.use_graph == 2) {  // eager device-driven
     return enqueue_device_frame(s, num_detection, st) == cudaSuccess ? SF_OK : SF_ERR_CUDA;

@@ -12,7 +12,8 @@ Fixture g1 (128x96 frames, fx = fy = 105, 10 mm voxels, 3 cm truncation,
 4096 buckets, 8192 excess, 16384 heap blocks): FilterDepth, PyrDownGauss,
 ComputeVMap, ComputeNMap, ResizeMap, per-pixel ICP rows, FuseMapColor over
 five frames (labels from frame 2 on), CheckBlockVisibility, AnalyzeMapSemantics,
-CreateRenderingBlocks + Raycast from two poses.
+CreateRenderingBlocks + Raycast from two poses, and UnifyNeighborKernel alone
+on a seeded label state (unify_state below).
 """
 import ctypes as C
 import hashlib
@@ -44,7 +45,7 @@ def load_ref():
     L.ref_map_visibility.restype = C.c_uint
     L.ref_map_raytrace.restype = C.c_int
     for n in ("ref_map_fuse", "ref_map_visibility", "ref_map_semantics", "ref_map_raytrace", "ref_map_counters",
-              "ref_map_entries", "ref_map_visible", "ref_map_voxels", "ref_map_destroy"):
+              "ref_map_unify", "ref_map_entries", "ref_map_visible", "ref_map_voxels", "ref_map_destroy"):
         getattr(L, n).argtypes = None
     return L
 
@@ -73,6 +74,69 @@ def block_digests(entries, voxels_ptr, n_sdf):
     sample = np.stack([vox[p * VOXEL_BYTES:(p + 512) * VOXEL_BYTES] for p in sel["ptr"][:32]]) if len(sel) else \
         np.zeros((0, 512 * VOXEL_BYTES), np.uint8)
     return pos, dig, sample
+
+
+def block_hash(p, nb):
+    x, y, z = (np.uint32(np.int64(c) & 0xffffffff) for c in p)
+    with np.errstate(over="ignore"):
+        h = (x * np.uint32(73856093)) ^ (y * np.uint32(19349669)) ^ (z * np.uint32(83492791))
+    return int(h) % nb
+
+
+def unify_state(n_buckets, n_entries, seed=3):
+    """A seeded map state for UnifyNeighbor: a 4x3x3 cluster of blocks
+    around the origin (negative coordinates included), three of its blocks
+    pushed to the excess list by far blocks entered first in their buckets,
+    and isolated blocks; labels from a small set so the 4-slot neighbour
+    tables fill and overflow; counts 0 (skipped neighbours) to 255 (the
+    count_2 + 5 wrap); a fifth of the voxels at weight 0.  Returns (entries,
+    voxels)."""
+    rng = np.random.default_rng(seed)
+    cluster = [(x, y, z) for x in range(-2, 2) for y in range(-1, 2) for z in range(-2, 1)]
+    far = []
+    for b in (cluster[4], cluster[17], cluster[30]):
+        want, k = block_hash(b, n_buckets), 0
+        while block_hash((100 + k, 50, 20), n_buckets) != want:
+            k += 1
+        far.append((100 + k, 50, 20))
+    blocks = far + cluster + [(40, -7, 3), (-33, 12, -9), (5, 5, 60), (-1, -60, 2)]
+    ent = np.zeros(n_entries, ENTRY)
+    ent["ptr"] = -1
+    next_off = 1
+    for k, p in enumerate(blocks):
+        b = block_hash(p, n_buckets)
+        if ent["ptr"][b] == -1:
+            ent["x"][b], ent["y"][b], ent["z"][b], ent["ptr"][b] = p[0], p[1], p[2], k * 512
+            continue
+        e = b
+        while ent["offset"][e] > 0:
+            e = n_buckets + ent["offset"][e] - 1
+        slot = n_buckets + next_off - 1
+        ent["x"][slot], ent["y"][slot], ent["z"][slot], ent["ptr"][slot] = p[0], p[1], p[2], k * 512
+        ent["offset"][e] = next_off
+        next_off += 1
+    nvox = len(blocks) * 512
+    vox = np.zeros((nvox, VOXEL_BYTES), np.uint8)
+    weight = rng.integers(1, 256, nvox)
+    weight[rng.random(nvox) < 0.2] = 0
+    labels = np.array([0, 3, 7, 9, 12, 40], np.uint8)
+    count = rng.integers(0, 12, nvox)
+    hi = rng.random(nvox) < 0.1
+    count[hi] = rng.integers(240, 256, int(hi.sum()))
+    count_2 = rng.integers(0, 12, nvox)
+    hi2 = rng.random(nvox) < 0.15
+    count_2[hi2] = rng.integers(248, 256, int(hi2.sum()))
+    vox[:, 4] = weight
+    vox[:, 8] = labels[rng.integers(0, len(labels), nvox)]
+    vox[:, 9] = count
+    vox[:, 10] = labels[rng.integers(0, len(labels), nvox)]
+    vox[:, 11] = count_2
+    same = rng.random(nvox) < 0.2  # label_2 == label on a fifth of the voxels
+    vox[same, 10] = vox[same, 8]
+    return ent, vox
+
+
+UNIFY_NVIS = (2048, 4096 + 8192)  # half the bucket slots; every slot
 
 
 def main():
@@ -204,6 +268,23 @@ def main():
     pos2, dig2, _ = block_digests(ent, L.ref_map_voxels(C.c_void_p(m)), n_sdf)
     out.update(sem_pos=pos2, sem_sha1=dig2)
     L.ref_map_destroy(C.c_void_p(m))
+
+    # UnifyNeighborKernel alone on a seeded state, per visible count
+    ent, vox = unify_state(int(consts[2]), n_entries)
+    out.update(uni_entries=ent.view(np.int32).reshape(n_entries, 8), uni_vox=vox,
+               uni_nvis=np.array(UNIFY_NVIS, np.int64))
+    for k, nvis in enumerate(UNIFY_NVIS):
+        m = L.ref_map_create()
+        C.memmove(L.ref_map_entries(C.c_void_p(m)), ent.ctypes.data, ent.nbytes)
+        C.memmove(L.ref_map_voxels(C.c_void_p(m)), vox.ctypes.data, vox.nbytes)
+        L.ref_map_unify(C.c_void_p(m), C.c_uint(nvis))
+        after = np.frombuffer((C.c_char * vox.nbytes).from_address(L.ref_map_voxels(C.c_void_p(m))),
+                              np.uint8).reshape(vox.shape).copy()
+        L.ref_map_destroy(C.c_void_p(m))
+        assert np.array_equal(np.delete(after, [8, 9, 10, 11], 1), np.delete(vox, [8, 9, 10, 11], 1))
+        out["uni_out%d" % k] = after[:, 8:12].copy()
+        print("unify nvis=%d: %d of %d voxels changed" % (nvis, int((after[:, 8:12] != vox[:, 8:12]).any(1).sum()),
+                                                          len(vox)))
 
     path = os.path.join(HERE, "g1.npz")
     np.savez_compressed(path, **out)

@@ -71,6 +71,28 @@ def positions(entries, n=None):
     return set(zip(e["x"].tolist(), e["y"].tolist(), e["z"].tolist()))
 
 
+def adopt_layout(omap, gpu_entries):
+    """Rewrites the oracle map's hash table into the device map's slot layout:
+    every slot holds the block the device map holds there, with the oracle's
+    voxel pointer for that block and the device map's chain offset.
+
+    Which of two blocks new in one frame with the same bucket takes the
+    bucket slot follows allocation order (a race in the reference and in the
+    device pass alike).  UnifyNeighbor visits hash slots [0, visible count),
+    so a comparison of that pass starts from the same layout on both sides."""
+    oe = omap.entries
+    optr = block_table(oe)
+    assert set(optr) == set(block_table(gpu_entries)), "allocated blocks differ"
+    new = np.zeros_like(oe)
+    for f in ("x", "y", "z", "offset"):
+        new[f] = gpu_entries[f]
+    new["ptr"] = -1
+    occ = np.nonzero(gpu_entries["ptr"] >= 0)[0]
+    new["ptr"][occ] = [optr[(int(gpu_entries["x"][i]), int(gpu_entries["y"][i]), int(gpu_entries["z"][i]))]
+                       for i in occ]
+    oe[:] = new
+
+
 def voxels_by_pos(entries, voxels):
     t = block_table(entries)
     keys = sorted(t)

@@ -25,8 +25,8 @@ def test_headers_declare_entry_points():
     names = declared_symbols()
     for must in ["sf_FilterDepth", "sf_ComputeVMap", "sf_ComputeNMap", "sf_PyrDownGauss", "sf_ResizeMap",
                  "sf_ICPStep", "sf_ResetMap", "sf_Raycast", "sf_CreateRenderingBlocks",
-                 "sf_CheckBlockVisibility", "sf_FuseMapColor", "sf_AnalyzeMapSemantics", "sf_ComputeSE3",
-                 "sf_system_grab"]:
+                 "sf_CheckBlockVisibility", "sf_FuseMapColor", "sf_AnalyzeMapSemantics", "sf_UnifyNeighbor",
+                 "sf_ComputeSE3", "sf_system_grab"]:
         assert must in names
 
 

@@ -9,7 +9,7 @@ label, count, label_2, count_2, colour_2) - all bit-exact.
 import numpy as np
 import pytest
 
-from tests.helpers import C1, C2, MAP_C1, MAP_C2, cuda, empty, host, map_to_host, positions, sequence, \
+from tests.helpers import C1, C2, MAP_C1, MAP_C2, adopt_layout, cuda, empty, host, map_to_host, positions, sequence, \
     voxels_by_pos
 
 pytestmark = pytest.mark.gpu
@@ -104,7 +104,10 @@ def test_label_fusion_bit_exact(lib):
         nvis = C.c_uint32()
         sf.call("sf_FuseMapColor", ctx.h, gmap.h, sf.image(f["raw"]), sf.image(f["rgb"]), sf.image(f["nmap"]),
                 sf.image(f["mask"]), 10, R, RI, t, *K, 3.0, 0.1, C.byref(nvis))
-        omap.fuse(f["raw_h"], rgb, f["nmap_h"], mask, 10, P, K)
+        # UnifyNeighbor visits hash slots [0, visible count): on the device layout
+        omap.fuse(f["raw_h"], rgb, f["nmap_h"], mask, 10, P, K, unify=False)
+        adopt_layout(omap, map_to_host(ctx, gmap)[0])
+        omap.unify_neighbor()
         _compare_maps(ctx, gmap, omap)
     e, v, _ = map_to_host(ctx, gmap)
     assert (v["count"] > 0).sum() > 1000 and (v["label"] > 0).sum() > 100
@@ -143,6 +146,8 @@ def test_analyze_semantics_and_visibility(lib):
             sf.image(f["mask"]), 10, R, RI, t, *K, 3.0, 0.1)
     omap.visibility(P, K, cfg["cols"], cfg["rows"])
     omap.semantics(f["raw_h"], rgb, f["nmap_h"], mask, 10, P, K)
+    adopt_layout(omap, map_to_host(ctx, gmap)[0])
+    omap.unify_neighbor()
     _compare_maps(ctx, gmap, omap)
     gmap.close()
 

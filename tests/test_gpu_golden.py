@@ -12,7 +12,7 @@ import os
 import numpy as np
 import pytest
 
-from tests.helpers import cuda, empty, host, map_to_host, same_nan
+from tests.helpers import adopt_layout, cuda, empty, host, map_to_host, same_nan
 
 pytestmark = pytest.mark.gpu
 
@@ -143,24 +143,41 @@ def _gpu_map(sf, g):
                   depth_max=float(np.float32(c[6])))
 
 
+def _oracle_map(g):
+    from oracle import oracle as O
+    c = g["consts"]
+    return O.Map(voxel_size=float(np.float32(c[0])), trunc_dist=float(np.float32(c[1])), num_buckets=int(c[2]),
+                 num_excess=int(c[3]), num_sdf_blocks=int(c[4]), depth_min=float(np.float32(c[5])),
+                 depth_max=float(np.float32(c[6])))
+
+
 def test_map_and_raytrace_vs_reference(env):
     """FuseMapColor x5 (labels from frame 2), then z-range + raycast from two
     poses: filtered depth differs by ulps, so the GPU fuses from its own raw
-    depth (bit-exact) and the reference's normal maps."""
+    depth (bit-exact) and the reference's normal maps.
+
+    The UnifyNeighbor pass of the labelled frames visits hash slots
+    [0, visible count), whose holders follow allocation order (a race on the
+    GPU), so the voxel bytes are checked against the oracle (pinned to these
+    fixtures by tests/test_oracle_golden.py) on the device map's slot layout;
+    the block set, counters and visible sets against the fixtures directly."""
     import torch
     sf, ctx, g = env
     m = _gpu_map(sf, g)
+    om = _oracle_map(g)
     cols, rows = g["depth0"].shape[1], g["depth0"].shape[0]
     from oracle import oracle as O
     for i in range(5):
         raw, _, _ = _gpu_frame(sf, ctx, g, i)
-        _, filt = O.filter_depth(g["depth%d" % i], 1000.0, 3.0)
-        nm = cuda(O.nmap(O.vmap(filt, *_K(g), 3.0)))  # oracle == reference here (pinned)
+        oraw, filt = O.filter_depth(g["depth%d" % i], 1000.0, 3.0)
+        nm_h = O.nmap(O.vmap(filt, *_K(g), 3.0))  # oracle == reference here (pinned)
+        nm = cuda(nm_h)
         R, RI, t = sf.pose_to_gpu(g["pose%d" % i])
         nvis = C.c_uint32()
+        ndet = 10 if i >= 2 else 0
         rgb, mask = cuda(g["rgb%d" % i]), cuda(g["mask%d" % i])  # keep the device buffers alive
         sf.call("sf_FuseMapColor", ctx.h, m.h, sf.image(raw), sf.image(rgb), sf.image(nm),
-                sf.image(mask), 10 if i >= 2 else 0, R, RI, t, *_K(g), 3.0, 0.1, C.byref(nvis))
+                sf.image(mask), ndet, R, RI, t, *_K(g), 3.0, 0.1, C.byref(nvis))
         cnt = m.counters(ctx)
         ref = g["counters"][i]
         assert cnt[0] == ref[0] and cnt[1] == ref[1] and cnt[3] == ref[3], "frame %d" % i
@@ -169,10 +186,16 @@ def test_map_and_raytrace_vs_reference(env):
         got = np.sort(np.stack([vis["x"][:nvis.value], vis["y"][:nvis.value], vis["z"][:nvis.value]], 1)
                       .astype(np.int32).view([("x", "<i4"), ("y", "<i4"), ("z", "<i4")]).ravel())
         assert np.array_equal(got, g["visible%d" % i])
+        om.fuse(host(raw), g["rgb%d" % i], nm_h, g["mask%d" % i], ndet, g["pose%d" % i], _K(g), unify=False)
+        if ndet > 0:
+            adopt_layout(om, e)
+            om.unify_neighbor()
     e, v, _ = map_to_host(ctx, m)
     pos, dig = _digests(e, v)
     assert np.array_equal(pos, g["map_pos"])
-    assert np.array_equal(dig, g["map_sha1"])
+    opos, odig = _digests(om.entries, om.voxels)
+    assert np.array_equal(pos, opos)
+    assert np.array_equal(dig, odig)
     for k, fi in enumerate((4, 5)):
         R, RI, t = sf.pose_to_gpu(g["pose%d" % fi])
         nvis = C.c_uint32()

@@ -162,7 +162,31 @@ def test_analyze_semantics(g):
     m.visibility(g["pose5"], _K(g), cols, rows)
     raw, _, nm = _frame(g, 4)
     m.visibility(g["pose4"], _K(g), cols, rows)
-    m.semantics(raw, g["rgb4"], nm, g["mask4"], 10, g["pose4"], _K(g))
+    m.analyze_semantics(raw, g["rgb4"], nm, g["mask4"], 10, g["pose4"], _K(g))
     pos, dig = _digests(m)
     assert np.array_equal(pos, g["sem_pos"])
     assert np.array_equal(dig, g["sem_sha1"])
+
+
+def load_unify_state(m, g):
+    """The seeded UnifyNeighbor state of the fixtures into an oracle map."""
+    from oracle.oracle import ENTRY_DTYPE
+    m.entries[:] = np.ascontiguousarray(g["uni_entries"]).view(ENTRY_DTYPE).ravel()
+    vox = g["uni_vox"]
+    m.voxels.view(np.uint8).reshape(-1, 16)[:len(vox)] = vox
+    return len(vox)
+
+
+def test_unify_neighbor(g):
+    """UnifyNeighborKernel alone on the seeded state (chains through the
+    excess list, full neighbour tables, zero counts, the count_2 + 5 wrap),
+    over half the bucket slots and over every slot."""
+    for k, nvis in enumerate(g["uni_nvis"]):
+        m = _oracle_map(g)
+        n = load_unify_state(m, g)
+        m.unify_neighbor(int(nvis))
+        got = m.voxels.view(np.uint8).reshape(-1, 16)[:n]
+        assert np.array_equal(got[:, 8:12], g["uni_out%d" % k]), "nvis %d" % nvis
+        assert np.array_equal(np.delete(got, [8, 9, 10, 11], 1), np.delete(g["uni_vox"], [8, 9, 10, 11], 1))
+    # the pass is not the identity on this state
+    assert (g["uni_out0"] != g["uni_vox"][:, 8:12]).any(1).sum() > 1000
