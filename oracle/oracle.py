@@ -19,6 +19,7 @@ F64P = C.POINTER(C.c_double)
 U16P = C.POINTER(C.c_uint16)
 U8P = C.POINTER(C.c_uint8)
 I32P = C.POINTER(C.c_int)
+I16P = C.POINTER(C.c_int16)
 
 ENTRY_DTYPE = np.dtype([("x", "<i4"), ("y", "<i4"), ("z", "<i4"), ("ptr", "<i4"),
                         ("offset", "<i4"), ("pad", "<i4", 3)])
@@ -58,6 +59,13 @@ def lib():
                 "sfo_se3_exp": (None, [F64P, F64P]),
                 "sfo_compute_se3": (C.c_int, [C.c_int, I32P, I32P, vp, vp, vp, vp, F32P, I32P, I32P,
                                               C.c_float, F64P, F64P, C.c_int, F64P]),
+                "sfo_compute_se3_ex": (C.c_int, [C.c_int, I32P, I32P] + [vp] * 8 + [F32P, I32P, I32P,
+                                                 C.c_float, F64P, F64P, C.c_int, F64P]),
+                "sfo_intensity": (None, [U8P, C.c_int, C.c_int, U8P]),
+                "sfo_pyrdown_u8": (None, [U8P, C.c_int, C.c_int, U8P, C.c_int, C.c_int]),
+                "sfo_sobel": (None, [U8P, C.c_int, C.c_int, I16P, I16P]),
+                "sfo_rgb_step": (None, [U8P, U8P, F32P, F32P, I16P, I16P, C.c_int, C.c_int, F64P, F64P]
+                                 + [C.c_float] * 4 + [C.c_int, F64P, I32P, F32P, F32P]),
                 "sfo_map_create": (vp, [C.POINTER(Config)]),
                 "sfo_map_destroy": (None, [vp]),
                 "sfo_map_reset": (None, [vp]),
@@ -86,6 +94,7 @@ def lib():
                                            C.c_float, I32P, I32P, C.c_float, F64P]),
                 "sfo_system_destroy": (None, [vp]),
                 "sfo_system_grab": (C.c_int, [vp, U16P, U8P, U8P, C.c_int, F64P, F64P]),
+                "sfo_system_set_rgb": (None, [vp, C.c_int]),
                 "sfo_system_map": (vp, [vp]),
                 "sfo_system_vmap": (vp, [vp, C.c_int]),
                 "sfo_system_nmap": (vp, [vp, C.c_int]),
@@ -205,11 +214,17 @@ def se3_exp(xi):
 
 
 def compute_se3(vnext, nnext, vlast, nlast, K, iters, min_count, thresh, last_pose, next_pose,
-                fp64=False):
+                fp64=False, rgb=None):
+    """Tracker::ComputeSE3.  rgb = (inext, ilast, dIdx, dIdy) per level adds
+    the photometric term (icpOnly = false); stats then has six entries."""
     L = len(vnext)
     keep = [_f32(a) for a in list(vnext) + list(nnext) + list(vlast) + list(nlast)]
+    if rgb is not None:
+        inext, ilast, dx, dy = rgb
+        keep += [np.ascontiguousarray(a, np.uint8) for a in list(inext) + list(ilast)]
+        keep += [np.ascontiguousarray(a, np.int16) for a in list(dx) + list(dy)]
     ptrs = [a.ctypes.data for a in keep]
-    arr = lambda k: (C.c_void_p * L)(*ptrs[k * L:(k + 1) * L])
+    arr = lambda k: (C.c_void_p * L)(*ptrs[k * L:(k + 1) * L]) if k * L < len(ptrs) else None
     cols = (C.c_int * L)(*[a.shape[1] for a in keep[:L]])
     rows = (C.c_int * L)(*[a.shape[0] for a in keep[:L]])
     Kf = np.asarray(K, np.float32)
@@ -217,10 +232,57 @@ def compute_se3(vnext, nnext, vlast, nlast, K, iters, min_count, thresh, last_po
     mc = np.asarray(min_count, np.int32)
     lp = np.ascontiguousarray(last_pose, np.float64)
     npose = np.ascontiguousarray(next_pose, np.float64).copy()
-    stats = np.zeros(4, np.float64)
-    ok = lib().sfo_compute_se3(L, cols, rows, arr(0), arr(1), arr(2), arr(3), _p(Kf, F32P), _p(it, I32P),
-                               _p(mc, I32P), thresh, _p(lp, F64P), _p(npose, F64P), int(fp64), _p(stats, F64P))
-    return bool(ok), npose, stats
+    stats = np.zeros(6, np.float64)
+    ok = lib().sfo_compute_se3_ex(L, cols, rows, arr(0), arr(1), arr(2), arr(3), arr(4), arr(5), arr(6), arr(7),
+                                  _p(Kf, F32P), _p(it, I32P), _p(mc, I32P), thresh, _p(lp, F64P),
+                                  _p(npose, F64P), int(fp64), _p(stats, F64P))
+    return bool(ok), npose, (stats if rgb is not None else stats[:4])
+
+
+def intensity(rgb):
+    """ImageToIntensity: uchar3 rows x cols x 3 -> uint8."""
+    rgb = np.ascontiguousarray(rgb, np.uint8)
+    rows, cols = rgb.shape[:2]
+    out = np.empty((rows, cols), np.uint8)
+    lib().sfo_intensity(_p(rgb, U8P), cols, rows, _p(out, U8P))
+    return out
+
+
+def pyrdown_u8(src):
+    """PyrDownGauss(unsigned char)."""
+    src = np.ascontiguousarray(src, np.uint8)
+    sr, sc = src.shape
+    dst = np.empty((sr // 2, sc // 2), np.uint8)
+    lib().sfo_pyrdown_u8(_p(src, U8P), sc, sr, _p(dst, U8P), sc // 2, sr // 2)
+    return dst
+
+
+def sobel(img):
+    """ComputeDerivativeImage: (dIdx, dIdy) int16."""
+    img = np.ascontiguousarray(img, np.uint8)
+    rows, cols = img.shape
+    dx = np.empty((rows, cols), np.int16)
+    dy = np.empty((rows, cols), np.int16)
+    lib().sfo_sobel(_p(img, U8P), cols, rows, _p(dx, I16P), _p(dy, I16P))
+    return dx, dy
+
+
+def rgb_step(inext, ilast, vnext, vlast, dIdx, dIdy, Pcurr, Plast, K, fp64=False, rows=False):
+    """RGBStep at the 4x4 poses: (sums29, (count, sum diff^2), sigma[, per-pixel rows])."""
+    inext, ilast = (np.ascontiguousarray(a, np.uint8) for a in (inext, ilast))
+    vnext, vlast = _f32(vnext), _f32(vlast)
+    dIdx, dIdy = (np.ascontiguousarray(a, np.int16) for a in (dIdx, dIdy))
+    r, c = inext.shape
+    Pc = np.ascontiguousarray(Pcurr, np.float64)
+    Pl = np.ascontiguousarray(Plast, np.float64)
+    out = np.zeros(29, np.float64)
+    res = np.zeros(2, np.int32)
+    sigma = np.zeros(1, np.float32)
+    per = np.zeros((r * c, 29), np.float32) if rows else None
+    lib().sfo_rgb_step(_p(inext, U8P), _p(ilast, U8P), _p(vnext, F32P), _p(vlast, F32P), _p(dIdx, I16P),
+                       _p(dIdy, I16P), c, r, _p(Pc, F64P), _p(Pl, F64P), *map(float, K), int(fp64), _p(out, F64P),
+                       _p(res, I32P), _p(sigma, F32P), _p(per, F32P) if rows else None)
+    return (out, (int(res[0]), int(res[1])), float(sigma[0])) + ((per,) if rows else ())
 
 
 def _view(ptr, dtype, n):
@@ -380,7 +442,7 @@ class System:
     """Oracle of the whole per-frame loop (System::GrabImage, System.cc:131-270)."""
 
     def __init__(self, map_kw, cols, rows, K, levels=3, iters=(10, 5, 4), min_count=(2000, 1000, 100),
-                 depth_scale=1000.0, depth_cutoff=3.0, icp_thresh=1e-4, init_pose=None):
+                 depth_scale=1000.0, depth_cutoff=3.0, icp_thresh=1e-4, init_pose=None, rgb_term=False):
         self.cfg = Config(map_kw["voxel_size"], map_kw["trunc_dist"], map_kw.get("depth_min", 0.1),
                           map_kw.get("depth_max", 3.0), map_kw["num_buckets"], map_kw["num_excess"],
                           map_kw["num_sdf_blocks"], map_kw.get("max_rendering_blocks", 260000))
@@ -393,6 +455,8 @@ class System:
         self.h = lib().sfo_system_create(C.byref(self.cfg), cols, rows, levels, _p(Kf, F32P), depth_scale,
                                          depth_cutoff, _p(it, I32P), _p(mc, I32P), icp_thresh, _p(ip, F64P))
         self.num_entries = self.cfg.num_buckets + self.cfg.num_excess
+        self.rgb_term = bool(rgb_term)
+        lib().sfo_system_set_rgb(self.h, int(self.rgb_term))
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -404,7 +468,7 @@ class System:
         rgb = np.ascontiguousarray(rgb, np.uint8)
         m = np.zeros(d.shape, np.uint8) if mask is None else np.ascontiguousarray(mask, np.uint8)
         pose = np.zeros(16, np.float64)
-        stats = np.zeros(8, np.float64)
+        stats = np.zeros(10, np.float64)
         ok = lib().sfo_system_grab(self.h, _p(d, U16P), _p(rgb, U8P), _p(m, U8P), num_detection,
                                    _p(pose, F64P), _p(stats, F64P))
         return bool(ok), pose.reshape(4, 4), stats

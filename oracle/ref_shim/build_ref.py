@@ -23,10 +23,11 @@ The rewrites only make the CUDA sources compile as serial host C++:
     visible-list copy's ptr with EntryToDelete, after which the label pass
     would index voxelBlocks[EntryToDelete + locId] (FuseMap.cu:176-207,
     518-582) instead of the block's own voxels;
-  * a function computing ICPReduce::getRow per pixel is appended to
-    Reduction.cu's copy (the reference reduces rows with warp shuffles,
-    which the serial emulation does not model), and one launching
-    UnifyNeighborKernel alone over a given grid to FuseMap.cu's copy.
+  * functions computing ICPReduce::getRow and RGBReduction's FindCorresp /
+    GetRow per pixel are appended to Reduction.cu's copy (the reference
+    reduces rows with warp shuffles, which the serial emulation does not
+    model), and one launching UnifyNeighborKernel alone over a given grid
+    to FuseMap.cu's copy.
 
 Nothing here is shipped or imported by the product.
 """
@@ -76,6 +77,48 @@ extern "C" void ref_icp_rows_impl(const float *vc, const float *vl, const float 
   icp.fx = fx; icp.fy = fy; icp.cx = cx; icp.cy = cy;
   icp.angleThresh = 0.6; icp.distThresh = 0.1;  // as ICPStep sets them
   for (int i = 0; i < cols * rows; ++i) icp.getRow(i, out29 + 29 * (size_t)i);
+}
+
+// ---- appended by oracle/ref_shim/build_ref.py: per-pixel RGB rows ----
+// RGBStep's two passes over every pixel (FindCorresp, then GetRow), with the
+// integer sums and sigma computed as RGBStep computes them between the two.
+extern "C" void ref_rgb_rows_impl(const unsigned char *inext, const unsigned char *ilast, const float *vn,
+                                  const float *vl, const short *dx, const short *dy, int cols, int rows,
+                                  const float *Rc, const float *RcI, const float *Rl, const float *RlI,
+                                  const float *tc, const float *tl, float fx, float fy, float cx, float cy,
+                                  int *res2, float *sigma, float *out29) {
+  RGBReduction rgb;
+  auto m3 = [](const float *R) {
+    Matrix3f M;
+    M.rowx = make_float3(R[0], R[1], R[2]);
+    M.rowy = make_float3(R[3], R[4], R[5]);
+    M.rowz = make_float3(R[6], R[7], R[8]);
+    return M;
+  };
+  std::vector<Residual> resid((size_t)cols * rows);
+  rgb.cols = cols; rgb.rows = rows; rgb.N = cols * rows;
+  rgb.nextImage.data = (unsigned char *)inext; rgb.nextImage.step = cols;
+  rgb.lastImage.data = (unsigned char *)ilast; rgb.lastImage.step = cols;
+  rgb.nextVMap.data = (float4 *)vn; rgb.nextVMap.step = sizeof(float4) * cols;
+  rgb.lastVMap.data = (float4 *)vl; rgb.lastVMap.step = sizeof(float4) * cols;
+  rgb.dIdx.data = (short *)dx; rgb.dIdx.step = sizeof(short) * cols;
+  rgb.dIdy.data = (short *)dy; rgb.dIdy.step = sizeof(short) * cols;
+  rgb.Rcurr = m3(Rc); rgb.RcurrInv = m3(RcI); rgb.Rlast = m3(Rl); rgb.RlastInv = m3(RlI);
+  rgb.tcurr = make_float3(tc[0], tc[1], tc[2]);
+  rgb.tlast = make_float3(tl[0], tl[1], tl[2]);
+  rgb.RGBResidual.data = resid.data(); rgb.RGBResidual.size = resid.size();
+  rgb.fx = fx; rgb.fy = fy; rgb.cx = cx; rgb.cy = cy;
+  int s0 = 0, s1 = 0;
+  for (int k = 0; k < cols * rows; ++k) {
+    int2 v = rgb.FindCorresp(k);
+    s0 += v.x;
+    s1 += v.y;
+  }
+  rgb.sigma = sqrt((float) s1 / (s0 == 0 ? 1 : s0));
+  for (int k = 0; k < cols * rows; ++k) rgb.GetRow(k, out29 + 29 * (size_t)k);
+  res2[0] = s0;
+  res2[1] = s1;
+  *sigma = rgb.sigma;
 }
 '''
 

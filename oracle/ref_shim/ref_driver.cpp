@@ -16,6 +16,10 @@ thread_local dim3 blockDim;
 thread_local dim3 gridDim;
 
 extern "C" void ref_unify_neighbor_impl(DeviceMap map, unsigned nvis);
+extern "C" void ref_rgb_rows_impl(const unsigned char *, const unsigned char *, const float *, const float *,
+                                  const short *, const short *, int, int, const float *, const float *,
+                                  const float *, const float *, const float *, const float *, float, float,
+                                  float, float, int *, float *, float *);
 extern "C" void ref_icp_rows_impl(const float *, const float *, const float *, const float *, int, int,
                                   const float *, const float *, const float *, const float *,
                                   const float *, float, float, float, float, float *);
@@ -136,6 +140,40 @@ void ref_icp_rows(const float *vc, const float *vl, const float *nc, const float
                   const float *Rc, const float *tc, const float *Rl, const float *RlInv, const float *tl,
                   float fx, float fy, float cx, float cy, float *out29) {
   ref_icp_rows_impl(vc, vl, nc, nl, cols, rows, Rc, tc, Rl, RlInv, tl, fx, fy, cx, cy, out29);
+}
+
+// Frame::FillImages' intensity part (Core/Frame.cc:74-84): ImageToIntensity,
+// PyrDownGauss(unsigned char), ComputeDerivativeImage.
+void ref_intensity(const uint8_t *rgb, int cols, int rows, uint8_t *out) {
+  DeviceArray2D<uchar3> c;
+  up(c, rgb, cols, rows);
+  DeviceArray2D<unsigned char> o(cols, rows);
+  ImageToIntensity(c, o);
+  down(o, out);
+}
+
+void ref_pyrdown_u8(const uint8_t *src, int sc, int sr, uint8_t *dst) {
+  DeviceArray2D<unsigned char> s, o(sc / 2, sr / 2);
+  up(s, src, sc, sr);
+  PyrDownGauss(s, o);
+  down(o, dst);
+}
+
+void ref_sobel(const uint8_t *img, int cols, int rows, int16_t *dx, int16_t *dy) {
+  DeviceArray2D<unsigned char> i;
+  up(i, img, cols, rows);
+  DeviceArray2D<short> x(cols, rows), y(cols, rows);
+  ComputeDerivativeImage(i, x, y);
+  down(x, dx);
+  down(y, dy);
+}
+
+void ref_rgb_rows(const uint8_t *inext, const uint8_t *ilast, const float *vn, const float *vl, const int16_t *dx,
+                  const int16_t *dy, int cols, int rows, const float *Rc, const float *RcI, const float *Rl,
+                  const float *RlI, const float *tc, const float *tl, float fx, float fy, float cx, float cy,
+                  int *res2, float *sigma, float *out29) {
+  ref_rgb_rows_impl(inext, ilast, vn, vl, dx, dy, cols, rows, Rc, RcI, Rl, RlI, tc, tl, fx, fy, cx, cy, res2,
+                    sigma, out29);
 }
 
 void *ref_map_create() { return new RefMap(); }

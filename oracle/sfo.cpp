@@ -387,6 +387,215 @@ extern "C" void sfo_icp_sums(const float *vcurr, const float *vlast,
                 dtl, fx, fy, cx, cy, fp64, out29);
 }
 
+// ================================================= photometric (RGB) term
+// ImageToIntensityKernel, Tracking/Pyrdown.cu:250-260: double weights, the
+// first byte weighted 0.7154 and the second 0.2125, as written.
+extern "C" void sfo_intensity(const uint8_t *rgb, int cols, int rows, uint8_t *out) {
+  for (int i = 0; i < cols * rows; ++i) {
+    const uint8_t *p = rgb + 3 * (size_t)i;
+    out[i] = (uint8_t)(int)(0.2125 * p[1] + 0.7154 * p[0] + 0.0721 * p[2]);
+  }
+}
+
+// PyrDownGaussKernel<unsigned char, unsigned char>, Pyrdown.cu:201-245.
+extern "C" void sfo_pyrdown_u8(const uint8_t *src, int sc, int sr, uint8_t *dst, int dc, int dr) {
+  for (int y = 0; y < dr; ++y)
+    for (int x = 0; x < dc; ++x) {
+      const int D = 5;
+      int tx = std::min(2 * x - D / 2 + D, sc - 1);
+      int ty = std::min(2 * y - D / 2 + D, sr - 1);
+      float sum = 0;
+      int count = 0;
+      for (int cy = std::max(0, 2 * y - D / 2); cy < ty; ++cy)
+        for (int cx = std::max(0, 2 * x - D / 2); cx < tx; ++cx) {
+          float k = kGauss[(ty - cy - 1) * 5 + (tx - cx - 1)];
+          sum += (float)src[cy * sc + cx] * k;
+          count = (int)((float)count + k);
+        }
+      dst[y * dc + x] = (uint8_t)(int)(sum / (float)count);
+    }
+}
+
+// ComputeDerivativeImageKernel, Pyrdown.cu:262-304: the 3x3 Sobel taps are
+// taken from index 8 downwards over the window clipped to the image, so at
+// the border the taps shift, as written.
+extern "C" void sfo_sobel(const uint8_t *img, int cols, int rows, int16_t *dx, int16_t *dy) {
+  static const float sx[9] = {1, 0, -1, 2, 0, -2, 1, 0, -1};
+  static const float sy[9] = {1, 2, 1, 0, 0, 0, -1, -2, -1};
+  for (int y = 0; y < rows; ++y)
+    for (int x = 0; x < cols; ++x) {
+      float dxv = 0, dyv = 0;
+      int k = 8;
+      for (int j = std::max(y - 1, 0); j <= std::min(y + 1, rows - 1); j++)
+        for (int i = std::max(x - 1, 0); i <= std::min(x + 1, cols - 1); i++) {
+          dxv += (float)img[j * cols + i] * sx[k];
+          dyv += (float)img[j * cols + i] * sy[k];
+          --k;
+        }
+      dx[y * cols + x] = (int16_t)f2i(dxv);
+      dy[y * cols + x] = (int16_t)f2i(dyv);
+    }
+}
+
+namespace {
+struct RgbCorr { int u, v, diff; };
+// Frame::GpuRotation / GpuInvRotation / GpuTranslation (Core/Frame.cc:626-645).
+void pose_f32(const double *P, float *R, float *Rinv, float *t) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) { R[i * 3 + j] = (float)P[i * 4 + j]; Rinv[i * 3 + j] = (float)P[j * 4 + i]; }
+  for (int i = 0; i < 3; ++i) t[i] = (float)P[i * 4 + 3];
+}
+// __float2int_rd: floor, saturating, NaN -> 0.
+inline int floor_i(float v) { return f2i(std::floor(v)); }
+// RGBReduction::FindCorresp, Reduction.cu:412-463.  `+ 0.5` is double and
+// the sum goes to __float2int_rd as a float.
+bool rgb_corresp(const uint8_t *inext, const uint8_t *ilast, const float *vnext, const float *vlast,
+                 const int16_t *dIdx, const int16_t *dIdy, int cols, int rows, int x, int y, const m3 &Rc,
+                 f3 tc, const m3 &RlI, f3 tl, float fx, float fy, float cx, float cy, RgbCorr &r) {
+  if (!(x >= 5 && x < cols - 5 && y >= 5 && y < rows - 5)) return false;
+  bool valid = true;
+  for (int u = std::max(y - 2, 0); u < std::min(y + 2, rows); ++u)
+    for (int v = std::max(x - 2, 0); v < std::min(x + 2, cols); ++v) valid = valid && (inext[u * cols + v] > 0);
+  if (!valid) return false;
+  const int gx = dIdx[y * cols + x], gy = dIdy[y * cols + x];
+  if (!(std::sqrt((float)(gx * gx + gy * gy)) > 0)) return false;
+  const float *vc = vnext + 4 * ((size_t)y * cols + x);
+  if (std::isnan(vc[0])) return false;
+  const f3 vcurr_g = mul(Rc, mk3(vc[0], vc[1], vc[2])) + tc;
+  const f3 vcl = mul(RlI, vcurr_g - tl);
+  const int u = floor_i((float)((double)(fx * vcl.x / vcl.z + cx) + 0.5));
+  const int v = floor_i((float)((double)(fy * vcl.y / vcl.z + cy) + 0.5));
+  if (!(u >= 0 && v >= 0 && u < cols && v < rows)) return false;
+  const float *vl = vlast + 4 * ((size_t)v * cols + u);
+  if (std::isnan(vl[0])) return false;
+  const float d0 = vl[0] - vc[0], d1 = vl[1] - vc[1], d2 = vl[2] - vc[2], d3 = vl[3] - vc[3];
+  if (!((double)std::sqrt(d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3) < 0.1)) return false;
+  if (ilast[v * cols + u] == 0) return false;
+  r.u = u;
+  r.v = v;
+  r.diff = (int)inext[y * cols + x] - (int)ilast[v * cols + u];
+  return true;
+}
+// RGBStep's sigma (Reduction.cu:621-622) from the two integer sums.
+float rgb_sigma(int count, int sumsq) {
+  return std::sqrt((float)sumsq / (float)(count == 0 ? 1 : count));
+}
+// RGBReduction::GetRow, Reduction.cu:483-517, FP32 reference semantics
+// (`/ 9.0` is double).
+void rgb_row_f32(const RgbCorr &r, float sigma, const float *vlast, const int16_t *dIdx, const int16_t *dIdy,
+                 int cols, int x, int y, const m3 &RcI, const m3 &Rl, f3 tl, f3 tc, float fx, float fy,
+                 float row[7]) {
+  float w = sigma + (float)std::abs(r.diff);
+  w = (double)w < 1e-3 ? 1.0f : 1.0f / w;
+  if ((double)sigma < 1e-6) w = 1.0f;
+  const float *vl = vlast + 4 * ((size_t)r.v * cols + r.u);
+  const f3 point = mul(RcI, ((mul(Rl, mk3(vl[0], vl[1], vl[2])) + tl) - tc));
+  const float gx = (float)((double)(float)dIdx[y * cols + x] / 9.0);
+  const float gy = (float)((double)(float)dIdy[y * cols + x] / 9.0);
+  const float invz = 1.0f / point.z;
+  f3 left;
+  left.x = gx * fx * invz;
+  left.y = gy * fy * invz;
+  left.z = -(left.x * point.x + left.y * point.y) * invz;
+  const f3 a = w * left, c = w * cross(point, left);
+  row[0] = a.x; row[1] = a.y; row[2] = a.z;
+  row[3] = c.x; row[4] = c.y; row[5] = c.z;
+  row[6] = -w * (float)r.diff;
+}
+// The same row in double from the double pose (error-budget oracle); the
+// correspondence and sigma are the FP32 ones.
+void rgb_row_f64(const RgbCorr &r, float sigma, const float *vlast, const int16_t *dIdx, const int16_t *dIdy,
+                 int cols, int x, int y, const dm3 &RcI, const dm3 &Rl, d3 tl, d3 tc, double fx, double fy,
+                 double row[7]) {
+  double w = (double)sigma + std::abs(r.diff);
+  w = w < 1e-3 ? 1.0 : 1.0 / w;
+  if ((double)sigma < 1e-6) w = 1.0;
+  const float *vl = vlast + 4 * ((size_t)r.v * cols + r.u);
+  const d3 point = dmul(RcI, (dmul(Rl, d3{vl[0], vl[1], vl[2]}) + tl) - tc);
+  const double gx = (double)dIdx[y * cols + x] / 9.0, gy = (double)dIdy[y * cols + x] / 9.0;
+  const double invz = 1.0 / point.z;
+  const d3 left = {gx * fx * invz, gy * fy * invz, 0.0};
+  const d3 l2 = {left.x, left.y, -(left.x * point.x + left.y * point.y) * invz};
+  const d3 c = dcross(point, l2);
+  row[0] = w * l2.x; row[1] = w * l2.y; row[2] = w * l2.z;
+  row[3] = w * c.x; row[4] = w * c.y; row[5] = w * c.z;
+  row[6] = -w * r.diff;
+}
+// ComputeResidualKernel + RgbStepKernel + both reductions (Reduction.cu
+// :465-481, :519-551, :561-642): res = {count, sum of diff^2} (int sums,
+// wrapping as the reference's), sigma, and the 29 sums (FP32 rows summed in
+// double, or FP64 rows).
+void rgb_sums_impl(const uint8_t *inext, const uint8_t *ilast, const float *vnext, const float *vlast,
+                   const int16_t *dIdx, const int16_t *dIdy, int cols, int rows, const double *Pc,
+                   const double *Pl, float fx, float fy, float cx, float cy, int fp64, double *out29,
+                   int *res2, float *sigma_out, float *rows29) {
+  float Rc[9], RcI[9], tcf[3], Rl[9], RlI[9], tlf[3];
+  pose_f32(Pc, Rc, RcI, tcf);
+  pose_f32(Pl, Rl, RlI, tlf);
+  const m3 mRc = m3_from(Rc), mRcI = m3_from(RcI), mRl = m3_from(Rl), mRlI = m3_from(RlI);
+  const f3 tc = f3_from(tcf), tl = f3_from(tlf);
+  dm3 dRcI, dRl;
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) { dRcI.m[r * 3 + c] = Pc[c * 4 + r]; dRl.m[r * 3 + c] = Pl[r * 4 + c]; }
+  const d3 dtc{Pc[3], Pc[7], Pc[11]}, dtl{Pl[3], Pl[7], Pl[11]};
+  const int N = cols * rows;
+  std::vector<RgbCorr> corr(N);
+  std::vector<uint8_t> ok(N, 0);
+  uint32_t cnt = 0, ssq = 0;
+  for (int i = 0; i < N; ++i) {
+    const int y = i / cols, x = i - y * cols;
+    if (rgb_corresp(inext, ilast, vnext, vlast, dIdx, dIdy, cols, rows, x, y, mRc, tc, mRlI, tl, fx, fy, cx,
+                    cy, corr[i])) {
+      ok[i] = 1;
+      cnt += 1u;
+      ssq += (uint32_t)(corr[i].diff * corr[i].diff);
+    }
+  }
+  res2[0] = (int)cnt;
+  res2[1] = (int)ssq;
+  const float sigma = rgb_sigma(res2[0], res2[1]);
+  if (sigma_out) *sigma_out = sigma;
+  for (int k = 0; k < 29; ++k) out29[k] = 0.0;
+  for (int i = 0; i < N; ++i) {
+    float *o = rows29 ? rows29 + 29 * (size_t)i : nullptr;
+    if (!ok[i]) {
+      if (o) for (int k = 0; k < 29; ++k) o[k] = 0.f;
+      continue;
+    }
+    const int y = i / cols, x = i - y * cols;
+    int k = 0;
+    if (fp64) {
+      double row[7];
+      rgb_row_f64(corr[i], sigma, vlast, dIdx, dIdy, cols, x, y, dRcI, dRl, dtl, dtc, fx, fy, row);
+      for (int a = 0; a < 7; ++a)
+        for (int b = a; b < 7; ++b) out29[k++] += row[a] * row[b];
+    } else {
+      float row[7];
+      rgb_row_f32(corr[i], sigma, vlast, dIdx, dIdy, cols, x, y, mRcI, mRl, tl, tc, fx, fy, row);
+      for (int a = 0; a < 7; ++a)
+        for (int b = a; b < 7; ++b, ++k) {
+          const float p = row[a] * row[b];
+          out29[k] += (double)p;
+          if (o) o[k] = p;
+        }
+      if (o) o[28] = 1.f;
+    }
+    out29[28] += 1.0;
+  }
+}
+}  // namespace
+
+// RGBStep (Reduction.cu:561-642) at the poses Pc (current estimate) and Pl
+// (last frame), 4x4 row-major double: the 29 sums, res = {count, sum of
+// diff^2}, sigma, and optionally the per-pixel FP32 29-vectors.
+extern "C" void sfo_rgb_step(const uint8_t *inext, const uint8_t *ilast, const float *vnext,
+                             const float *vlast, const int16_t *dIdx, const int16_t *dIdy, int cols,
+                             int rows, const double *Pc, const double *Pl, float fx, float fy, float cx,
+                             float cy, int fp64, double *out29, int *res2, float *sigma, float *rows29) {
+  rgb_sums_impl(inext, ilast, vnext, vlast, dIdx, dIdy, cols, rows, Pc, Pl, fx, fy, cx, cy, fp64, out29, res2,
+                sigma, rows29);
+}
+
 // CreateMatrix<6,7>, Reduction.cu:6-16.
 extern "C" void sfo_create_matrix(const double *s, double *A, double *b) {
   int shift = 0;
@@ -515,13 +724,23 @@ double euler_sin_norm(const double *P) {
 }
 }  // namespace
 
-// Tracker::ComputeSE3(icpOnly=true, iter, thresh), Tracking.cc:369-517.
-extern "C" int sfo_compute_se3(int levels, const int *cols, const int *rows,
-                               const float *const *vnext, const float *const *nnext,
-                               const float *const *vlast, const float *const *nlast,
-                               const float *K, const int *iters, const int *min_count,
-                               float thresh, const double *last_pose, double *next_pose,
-                               int fp64, double *stats) {
+// Tracker::ComputeSE3(icpOnly, iter, thresh), Tracking.cc:369-517.  With
+// inext == nullptr it is the icpOnly form; else each iteration first runs
+// RGBStep (:402-431) on the intensity pyramids inext / ilast and the next
+// frame's derivative images, fails on a NaN error or too few photometric
+// correspondences, and solves (A_rgb w + A_icp) x = b_rgb w + b_icp with
+// w = 1e-4f (:484-491).  stats[0..3] = {icpError, icpCount, iterations,
+// failure code}; with the RGB term stats[4..5] = {rgbError, rgbCount}.
+extern "C" int sfo_compute_se3_ex(int levels, const int *cols, const int *rows,
+                                  const float *const *vnext, const float *const *nnext,
+                                  const float *const *vlast, const float *const *nlast,
+                                  const uint8_t *const *inext, const uint8_t *const *ilast,
+                                  const int16_t *const *dIdx, const int16_t *const *dIdy,
+                                  const float *K, const int *iters, const int *min_count,
+                                  float thresh, const double *last_pose, double *next_pose,
+                                  int fp64, double *stats) {
+  const bool rgb = inext != nullptr;
+  int rgbCount = 0;
   double lastPose[16], pose[16], delta[16], candidate[16];
   memcpy(lastPose, last_pose, sizeof(lastPose));
   memcpy(pose, next_pose, sizeof(pose));
@@ -552,13 +771,35 @@ extern "C" int sfo_compute_se3(int levels, const int *cols, const int *rows,
                       dtl, fx, fy, cx, cy, fp64, s);
       }
       ++its;
+      double Argb[36], brgb[6];
+      if (rgb) {
+        double srgb[29];
+        int res2[2];
+        rgb_sums_impl(inext[i], ilast[i], vnext[i], vlast[i], dIdx[i], dIdy[i], cols[i], rows[i], next_pose,
+                      lastPose, fx, fy, cx, cy, fp64, srgb, res2, nullptr, nullptr);
+        float rres[2] = {(float)srgb[27], (float)srgb[28]};
+        sfo_create_matrix(srgb, Argb, brgb);
+        rgbError = std::sqrt(rres[0]) / rres[1];
+        rgbCount = (int)rres[1];
+        if (std::isnan(rgbError) || rgbCount < min_count[i]) {
+          memcpy(next_pose, lastPose, sizeof(lastPose));
+          if (stats) {
+            stats[0] = icpError; stats[1] = icpCount; stats[2] = its; stats[3] = 1;
+            stats[4] = rgbError; stats[5] = rgbCount;
+          }
+          return 0;
+        }
+      }
       float residual[2] = {(float)s[27], (float)s[28]};
       sfo_create_matrix(s, A, b);
       icpError = std::sqrt(residual[0]) / residual[1];
       icpCount = (int)residual[1];
       if (std::isnan(icpError) || icpCount < min_count[i]) {
         memcpy(next_pose, lastPose, sizeof(lastPose));
-        if (stats) { stats[0] = icpError; stats[1] = icpCount; stats[2] = its; stats[3] = 1; }
+        if (stats) {
+          stats[0] = icpError; stats[1] = icpCount; stats[2] = its; stats[3] = 1;
+          if (rgb) { stats[4] = rgbError; stats[5] = rgbCount; }
+        }
         return 0;
       }
       currError = rgbError * w + icpError;
@@ -575,6 +816,10 @@ extern "C" int sfo_compute_se3(int levels, const int *cols, const int *rows,
         break;
       }
       lastError = currError;
+      if (rgb) {
+        for (int k = 0; k < 36; ++k) A[k] = Argb[k] * (double)w + A[k];
+        for (int k = 0; k < 6; ++k) b[k] = brgb[k] * (double)w + b[k];
+      }
       sfo_ldlt_solve6(A, b, x);
       sfo_se3_exp(x, dT);
       mat4_mul(dT, delta, delta);
@@ -590,8 +835,22 @@ extern "C" int sfo_compute_se3(int levels, const int *cols, const int *rows,
   double an = euler_sin_norm(p);
   int ok = (icpError < thresh) && (an <= 0.1 && tn <= 0.1);
   if (!ok) memcpy(next_pose, lastPose, sizeof(lastPose));
-  if (stats) { stats[0] = icpError; stats[1] = icpCount; stats[2] = its; stats[3] = ok ? 0 : 2; }
+  if (stats) {
+    stats[0] = icpError; stats[1] = icpCount; stats[2] = its; stats[3] = ok ? 0 : 2;
+    if (rgb) { stats[4] = rgbError; stats[5] = rgbCount; }
+  }
   return ok;
+}
+
+// Tracker::ComputeSE3(icpOnly=true, iter, thresh).
+extern "C" int sfo_compute_se3(int levels, const int *cols, const int *rows,
+                               const float *const *vnext, const float *const *nnext,
+                               const float *const *vlast, const float *const *nlast,
+                               const float *K, const int *iters, const int *min_count,
+                               float thresh, const double *last_pose, double *next_pose,
+                               int fp64, double *stats) {
+  return sfo_compute_se3_ex(levels, cols, rows, vnext, nnext, vlast, nlast, nullptr, nullptr, nullptr, nullptr,
+                            K, iters, min_count, thresh, last_pose, next_pose, fp64, stats);
 }
 
 // ======================================================================= map
@@ -1562,6 +1821,8 @@ extern "C" double sfo_raycast_smooth_f64(sfo_map *m, const float *gv, const floa
 struct sfo_frame {
   std::vector<float> raw;
   std::vector<std::vector<float>> depth, vmap, nmap;
+  std::vector<std::vector<uint8_t>> image;        // intensity pyramid (photometric term)
+  std::vector<std::vector<int16_t>> dIdx, dIdy;   // its derivative images
   double pose[16];
 };
 struct sfo_system {
@@ -1572,6 +1833,7 @@ struct sfo_system {
   sfo_frame fa, fb;
   sfo_frame *next = &fa, *last = &fb;
   int state = 1;  // 1 = init, 0 = tracking (Tracking.cc:65-119)
+  int rgb = 0;    // 1: ComputeSE3(icpOnly = false), the reference's default
   double init_pose[16];
   std::vector<float> zmin, zmax;
   int zc, zr;
@@ -1581,10 +1843,22 @@ namespace {
 void frame_alloc(sfo_frame &f, int cols, int rows, int L) {
   f.raw.assign((size_t)cols * rows, 0);
   f.depth.resize(L); f.vmap.resize(L); f.nmap.resize(L);
+  f.image.resize(L); f.dIdx.resize(L); f.dIdy.resize(L);
   for (int l = 0; l < L; ++l) {
     size_t n = (size_t)(cols >> l) * (rows >> l);
     f.depth[l].assign(n, 0); f.vmap[l].assign(4 * n, 0); f.nmap[l].assign(4 * n, 0);
+    f.image[l].assign(n, 0); f.dIdx[l].assign(n, 0); f.dIdy[l].assign(n, 0);
   }
+}
+// Frame::FillImages intensity part, Core/Frame.cc:74-84 (run only with the
+// photometric term: nothing else reads it).
+void fill_intensity(sfo_system *s, sfo_frame &f, const uint8_t *rgb) {
+  sfo_intensity(rgb, s->cols, s->rows, f.image[0].data());
+  for (int l = 1; l < s->levels; ++l)
+    sfo_pyrdown_u8(f.image[l - 1].data(), s->cols >> (l - 1), s->rows >> (l - 1), f.image[l].data(),
+                   s->cols >> l, s->rows >> l);
+  for (int l = 0; l < s->levels; ++l)
+    sfo_sobel(f.image[l].data(), s->cols >> l, s->rows >> l, f.dIdx[l].data(), f.dIdy[l].data());
 }
 // Frame::FillImages depth part, Core/Frame.cc:68-92.
 void fill_images(sfo_system *s, sfo_frame &f, const uint16_t *d) {
@@ -1627,6 +1901,7 @@ extern "C" sfo_system *sfo_system_create(const sfo_config *cfg, int cols, int ro
   return s;
 }
 extern "C" void sfo_system_destroy(sfo_system *s) { sfo_map_destroy(s->map); delete s; }
+extern "C" void sfo_system_set_rgb(sfo_system *s, int on) { s->rgb = on != 0; }
 extern "C" sfo_map *sfo_system_map(sfo_system *s) { return s->map; }
 extern "C" const float *sfo_system_vmap(sfo_system *s, int l) { return s->last->vmap[l].data(); }
 extern "C" const float *sfo_system_nmap(sfo_system *s, int l) { return s->last->nmap[l].data(); }
@@ -1640,8 +1915,9 @@ extern "C" int sfo_system_grab(sfo_system *s, const uint16_t *depth, const uint8
                                double *stats) {
   resize_images(s, *s->last);
   fill_images(s, *s->next, depth);
+  if (s->rgb) fill_intensity(s, *s->next, rgb);
   int tracked = 1;
-  double st[4] = {0, 0, 0, 0};
+  double st[6] = {0, 0, 0, 0, 0, 0};
   if (s->state == 1) {
     memcpy(s->next->pose, s->init_pose, sizeof(s->init_pose));
     std::swap(s->next, s->last);
@@ -1650,14 +1926,19 @@ extern "C" int sfo_system_grab(sfo_system *s, const uint16_t *depth, const uint8
     memcpy(s->next->pose, s->last->pose, sizeof(s->last->pose));
     std::vector<int> cols(s->levels), rows(s->levels);
     std::vector<const float *> vn(s->levels), nn(s->levels), vl(s->levels), nl(s->levels);
+    std::vector<const uint8_t *> in(s->levels), il(s->levels);
+    std::vector<const int16_t *> gx(s->levels), gy(s->levels);
     for (int l = 0; l < s->levels; ++l) {
       cols[l] = s->cols >> l; rows[l] = s->rows >> l;
       vn[l] = s->next->vmap[l].data(); nn[l] = s->next->nmap[l].data();
       vl[l] = s->last->vmap[l].data(); nl[l] = s->last->nmap[l].data();
+      in[l] = s->next->image[l].data(); il[l] = s->last->image[l].data();
+      gx[l] = s->next->dIdx[l].data(); gy[l] = s->next->dIdy[l].data();
     }
-    tracked = sfo_compute_se3(s->levels, cols.data(), rows.data(), vn.data(), nn.data(), vl.data(),
-                              nl.data(), s->K, s->iters.data(), s->min_count.data(), s->icp_thresh,
-                              s->last->pose, s->next->pose, 0, st);
+    tracked = sfo_compute_se3_ex(s->levels, cols.data(), rows.data(), vn.data(), nn.data(), vl.data(),
+                                 nl.data(), s->rgb ? in.data() : nullptr, il.data(), gx.data(), gy.data(), s->K,
+                                 s->iters.data(), s->min_count.data(), s->icp_thresh, s->last->pose,
+                                 s->next->pose, 0, st);
     if (tracked) std::swap(s->next, s->last);
   }
   unsigned nvis = 0;
@@ -1684,6 +1965,7 @@ extern "C" int sfo_system_grab(sfo_system *s, const uint16_t *depth, const uint8
     sfo_map_counters(s->map, c);
     stats[0] = st[0]; stats[1] = st[1]; stats[2] = st[2]; stats[3] = st[3];
     stats[4] = nvis; stats[5] = c[0]; stats[6] = c[1]; stats[7] = c[3];
+    if (s->rgb) { stats[8] = st[4]; stats[9] = st[5]; }
   }
   return tracked;
 }

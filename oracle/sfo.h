@@ -71,6 +71,29 @@ int sfo_compute_se3(int levels, const int *cols, const int *rows,
                     const int *min_count, float thresh, const double *last_pose,
                     double *next_pose, int fp64, double *stats);
 
+// ---- photometric term (Pyrdown.cu:201-316, Reduction.cu:387-642) ----
+void sfo_intensity(const uint8_t *rgb, int cols, int rows, uint8_t *out);
+void sfo_pyrdown_u8(const uint8_t *src, int sc, int sr, uint8_t *dst, int dc, int dr);
+void sfo_sobel(const uint8_t *img, int cols, int rows, int16_t *dx, int16_t *dy);
+// RGBStep at the 4x4 poses Pc (current estimate) and Pl (last frame):
+// out29 sums, res2 = {count, sum of diff^2}, sigma; rows29 (optional) the
+// per-pixel FP32 29-vectors.  fp64 != 0 computes the rows in double.
+void sfo_rgb_step(const uint8_t *inext, const uint8_t *ilast, const float *vnext,
+                  const float *vlast, const int16_t *dIdx, const int16_t *dIdy,
+                  int cols, int rows, const double *Pc, const double *Pl, float fx,
+                  float fy, float cx, float cy, int fp64, double *out29, int *res2,
+                  float *sigma, float *rows29);
+// ComputeSE3 with the photometric term when inext != NULL (icpOnly = false);
+// stats[6] then ends with {rgbError, rgbCount}.
+int sfo_compute_se3_ex(int levels, const int *cols, const int *rows,
+                       const float *const *vnext, const float *const *nnext,
+                       const float *const *vlast, const float *const *nlast,
+                       const uint8_t *const *inext, const uint8_t *const *ilast,
+                       const int16_t *const *dIdx, const int16_t *const *dIdy,
+                       const float *K, const int *iters, const int *min_count,
+                       float thresh, const double *last_pose, double *next_pose,
+                       int fp64, double *stats);
+
 // ---- map (Mapping/DeviceMap.cu, FuseMap.cu, RenderScene.cu) ----
 sfo_map *sfo_map_create(const sfo_config *cfg);
 void sfo_map_destroy(sfo_map *m);
@@ -136,9 +159,13 @@ sfo_system *sfo_system_create(const sfo_config *cfg, int cols, int rows,
                               const int *min_count, float icp_thresh,
                               const double *init_pose);
 void sfo_system_destroy(sfo_system *s);
+// on != 0: track with the photometric term (ComputeSE3(icpOnly = false),
+// the reference's default, Tracking.cc:170).
+void sfo_system_set_rgb(sfo_system *s, int on);
 // Returns the tracking result (1 tracked / 0 lost); pose_out = the frame's
 // pose after tracking; stats[8] = {icpError, count, iters, fail, visible,
-// heapCounter, entryPtr, allocated}.
+// heapCounter, entryPtr, allocated}, with the photometric term
+// stats[10] (stats[8..9] = {rgbError, rgbCount}).
 int sfo_system_grab(sfo_system *s, const uint16_t *depth, const uint8_t *rgb,
                     const uint8_t *mask, int num_detection, double *pose_out,
                     double *stats);

@@ -10,7 +10,9 @@ synthetic inputs.  Run in the container that holds the reference sources:
 
 Fixture g1 (128x96 frames, fx = fy = 105, 10 mm voxels, 3 cm truncation,
 4096 buckets, 8192 excess, 16384 heap blocks): FilterDepth, PyrDownGauss,
-ComputeVMap, ComputeNMap, ResizeMap, per-pixel ICP rows, FuseMapColor over
+ComputeVMap, ComputeNMap, ResizeMap, per-pixel ICP rows, the intensity pyramid
+(ImageToIntensity, PyrDownGauss(uchar), ComputeDerivativeImage), per-pixel
+RGB rows (RGBStep's FindCorresp and GetRow), FuseMapColor over
 five frames (labels from frame 2 on), CheckBlockVisibility, AnalyzeMapSemantics,
 CreateRenderingBlocks + Raycast from two poses, and UnifyNeighborKernel alone
 on a seeded label state (unify_state below).
@@ -45,7 +47,8 @@ def load_ref():
     L.ref_map_visibility.restype = C.c_uint
     L.ref_map_raytrace.restype = C.c_int
     for n in ("ref_map_fuse", "ref_map_visibility", "ref_map_semantics", "ref_map_raytrace", "ref_map_counters",
-              "ref_map_unify", "ref_map_entries", "ref_map_visible", "ref_map_voxels", "ref_map_destroy"):
+              "ref_map_unify", "ref_map_entries", "ref_map_visible", "ref_map_voxels", "ref_map_destroy",
+              "ref_intensity", "ref_pyrdown_u8", "ref_sobel", "ref_rgb_rows"):
         getattr(L, n).argtypes = None
     return L
 
@@ -216,6 +219,46 @@ def main():
         out["icp_rows_sha1_%d" % l] = np.frombuffer(hashlib.sha1(rows29.tobytes()).digest(), np.uint8)
         if l == 2:
             out["icp_rows2"] = rows29
+
+    # intensity pyramid and derivative images of frames 0 and 1, then the
+    # per-pixel RGB rows (FindCorresp + GetRow) of frame 1 against frame 0 at
+    # the same halfway pose as the ICP rows
+    ipyr = []
+    for i in range(2):
+        rgb = frames[i][1]
+        imgs = [np.zeros((ROWS, COLS), np.uint8)]
+        L.ref_intensity(fptr(rgb), COLS, ROWS, fptr(imgs[0]))
+        for l in range(1, 3):
+            c, r = COLS >> l, ROWS >> l
+            imgs.append(np.zeros((r, c), np.uint8))
+            L.ref_pyrdown_u8(fptr(imgs[l - 1]), c * 2, r * 2, fptr(imgs[l]))
+        ders = []
+        for l in range(3):
+            c, r = COLS >> l, ROWS >> l
+            dx = np.zeros((r, c), np.int16)
+            dy = np.zeros((r, c), np.int16)
+            L.ref_sobel(fptr(imgs[l]), c, r, fptr(dx), fptr(dy))
+            ders.append((dx, dy))
+            out["f%d_int%d" % (i, l)] = imgs[l]
+            out["f%d_dx%d" % (i, l)] = dx
+            out["f%d_dy%d" % (i, l)] = dy
+        ipyr.append((imgs, ders))
+    Rc, RcI, tc = pose_parts(Pc)
+    for l in range(3):
+        c, r = COLS >> l, ROWS >> l
+        rows29 = np.zeros((r * c, 29), np.float32)
+        res2 = np.zeros(2, np.int32)
+        sigma = np.zeros(1, np.float32)
+        div = float(1 << l)
+        L.ref_rgb_rows(fptr(ipyr[1][0][l]), fptr(ipyr[0][0][l]), fptr(pyr[1][2][l]), fptr(pyr[0][2][l]),
+                       fptr(ipyr[1][1][l][0]), fptr(ipyr[1][1][l][1]), c, r, fptr(Rc), fptr(RcI), fptr(Rl),
+                       fptr(RlI), fptr(tc), fptr(tl), *[C.c_float(k / div) for k in K], fptr(res2), fptr(sigma),
+                       fptr(rows29))
+        out["rgb_res%d" % l] = res2
+        out["rgb_sigma%d" % l] = sigma
+        out["rgb_sums%d" % l] = rows29.astype(np.float64).sum(0)
+        out["rgb_rows_sha1_%d" % l] = np.frombuffer(hashlib.sha1(rows29.tobytes()).digest(), np.uint8)
+        print("rgb level %d: %d correspondences, sigma %.3f" % (l, res2[0], sigma[0]))
 
     # the map: FuseMapColor at ground-truth poses, labels from frame 2 on
     m = L.ref_map_create()

@@ -190,3 +190,32 @@ def test_unify_neighbor(g):
         assert np.array_equal(np.delete(got, [8, 9, 10, 11], 1), np.delete(g["uni_vox"], [8, 9, 10, 11], 1))
     # the pass is not the identity on this state
     assert (g["uni_out0"] != g["uni_vox"][:, 8:12]).any(1).sum() > 1000
+
+
+def test_intensity_pyramid(g):
+    """ImageToIntensity, PyrDownGauss(unsigned char), ComputeDerivativeImage."""
+    from oracle import oracle as O
+    for i in range(2):
+        img = O.intensity(g["rgb%d" % i])
+        for l in range(3):
+            if l > 0:
+                img = O.pyrdown_u8(img)
+            assert np.array_equal(img, g["f%d_int%d" % (i, l)]), "frame %d level %d" % (i, l)
+            dx, dy = O.sobel(img)
+            assert np.array_equal(dx, g["f%d_dx%d" % (i, l)])
+            assert np.array_equal(dy, g["f%d_dy%d" % (i, l)])
+
+
+def test_rgb_rows(g):
+    """RGBStep's correspondences, integer sums, sigma and per-pixel rows."""
+    from oracle import oracle as O
+    for l in range(3):
+        sums, res, sigma, rows = O.rgb_step(g["f1_int%d" % l], g["f0_int%d" % l], g["f1_vmap%d" % l],
+                                            g["f0_vmap%d" % l], g["f1_dx%d" % l], g["f1_dy%d" % l],
+                                            g["icp_pose_curr"], g["pose0"], _K(g, l), rows=True)
+        assert res == tuple(int(v) for v in g["rgb_res%d" % l]), "level %d" % l
+        assert np.float32(sigma) == g["rgb_sigma%d" % l][0]
+        assert np.array_equal(np.frombuffer(hashlib.sha1(rows.tobytes()).digest(), np.uint8),
+                              g["rgb_rows_sha1_%d" % l]), "level %d" % l
+        np.testing.assert_allclose(sums, g["rgb_sums%d" % l], rtol=1e-12)
+    assert g["rgb_res0"][0] > 5000
