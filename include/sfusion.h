@@ -226,6 +226,45 @@ int sf_ComputeSE3(sf_context *ctx, int levels, const sf_image *next_vmaps,
                   const int *min_count, float thresh, const double last_pose[16],
                   double next_pose_out[16], int stats_out[4], float *icp_error_out);
 
+/* ----------------------------------------------------- photometric term */
+/* ImageToIntensity (Tracking/Reduction.h:34; Pyrdown.cu:250-271): uchar3
+ * colour -> uint8 intensity, (int)(0.2125 g + 0.7154 r + 0.0721 b) with the
+ * reference's channel order. */
+int sf_ImageToIntensity(sf_context *ctx, sf_image rgb, sf_image image);
+/* PyrDownGauss(unsigned char) (Reduction.h:31; Pyrdown.cu:201-245). */
+int sf_PyrDownGauss_u8(sf_context *ctx, sf_image src, sf_image dst);
+/* ComputeDerivativeImage (Reduction.h:37; Pyrdown.cu:262-316): 3x3 Sobel
+ * of a uint8 image into int16 dx, dy. */
+int sf_ComputeDerivativeImage(sf_context *ctx, sf_image image, sf_image dx,
+                              sf_image dy);
+/* RGBStep (Reduction.h:81; Reduction.cu:561-642): the photometric rows of
+ * one level.  Images uint8 (intensity), float4 (vertex maps), int16 (the
+ * next frame's derivatives).  Writes residual = {sum of weighted squared
+ * differences, correspondences}, matrixA[36] and vectorB[6] to HOST memory,
+ * as ICPStep does.  Correspondences and sigma are exact; the sums agree
+ * with the reference's to FP32 rounding. */
+int sf_RGBStep(sf_context *ctx, sf_image next_image, sf_image last_image,
+               sf_image next_vmap, sf_image last_vmap, sf_image dIdx,
+               sf_image dIdy, sf_mat3 Rcurr, sf_mat3 RcurrInv, sf_mat3 Rlast,
+               sf_mat3 RlastInv, sf_float3 tcurr, sf_float3 tlast,
+               sf_intrinsics K, float residual[2], double matrixA[36],
+               double vectorB[6]);
+/* Tracker::ComputeSE3(icpOnly = false, ...) (Tracking/Tracking.cc:369-517),
+ * the reference's default tracking: sf_ComputeSE3 with RGBStep run in every
+ * iteration (its error and count tested first) and the solve of
+ * A_rgb 1e-4 + A_icp.  Per level: the next and last intensity images and
+ * the next frame's derivative images.  stats_out (may be NULL): {accepted,
+ * fail, iterations, icp_count, rgb_count, 0}; errors_out (may be NULL):
+ * {icp_error, rgb_error}. */
+int sf_ComputeSE3_rgbd(sf_context *ctx, int levels, const sf_image *next_vmaps,
+                       const sf_image *next_nmaps, const sf_image *last_vmaps,
+                       const sf_image *last_nmaps, const sf_image *next_images,
+                       const sf_image *last_images, const sf_image *next_dIdx,
+                       const sf_image *next_dIdy, sf_intrinsics K0,
+                       const int *iters, const int *min_count, float thresh,
+                       const double last_pose[16], double next_pose_out[16],
+                       int stats_out[6], float errors_out[2]);
+
 /* --------------------------------------------------------------- fusion */
 /* CheckBlockVisibility (RenderScene.h:40; FuseMap.cu:991-1037). */
 int sf_CheckBlockVisibility(sf_context *ctx, sf_map *map, sf_mat3 Rview,

@@ -125,6 +125,12 @@ SIGNATURES = {
                    F64P, F64P],
     "sf_ICPStep_static": [vp, Image, Image, Image, Image, Mat3, Float3, Mat3, Mat3, Float3, Intrinsics,
                           F32P, F64P, F64P],
+    "sf_ImageToIntensity": [vp, Image, Image],
+    "sf_PyrDownGauss_u8": [vp, Image, Image],
+    "sf_ComputeDerivativeImage": [vp, Image, Image, Image],
+    "sf_RGBStep": [vp] + [Image] * 6 + [Mat3] * 4 + [Float3, Float3, Intrinsics, F32P, F64P, F64P],
+    "sf_ComputeSE3_rgbd": [vp, C.c_int] + [C.POINTER(Image)] * 8 + [Intrinsics, I32P, I32P, C.c_float, F64P, F64P,
+                                                                    I32P, F32P],
     "sf_RaycastAdjoint": [vp, vp, Image, Image, Mat3, Mat3, Float3] + [C.c_float] * 4 + [Image, Image, vp, F64P],
     "sf_RelocScoreBatch": [vp, vp, Image, C.c_int, F64P, C.c_int, C.c_float, C.POINTER(RelocScore)],
     "sf_ComputeSE3": [vp, C.c_int, C.POINTER(Image), C.POINTER(Image), C.POINTER(Image), C.POINTER(Image),

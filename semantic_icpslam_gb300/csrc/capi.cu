@@ -586,6 +586,133 @@ int sf_ComputeSE3(sf_context *ctx, int levels, const sf_image *nv, const sf_imag
   return SF_OK;
 }
 
+// ------------------------------------------------------ photometric term
+int sf_ImageToIntensity(sf_context *ctx, sf_image rgb, sf_image image) {
+  if (!ctx || !img_ok(rgb, 3) || !img_ok(image, 1) || rgb.cols != image.cols || rgb.rows != image.rows)
+    return SF_ERR_INVALID;
+  launch_intensity(rgb, image, nullptr, nullptr, ctx->stream);
+  SF_CHECK(cudaGetLastError());
+  return SF_OK;
+}
+
+int sf_PyrDownGauss_u8(sf_context *ctx, sf_image src, sf_image dst) {
+  if (!ctx || !img_ok(src, 1) || !img_ok(dst, 1) || dst.cols > src.cols || dst.rows > src.rows)
+    return SF_ERR_INVALID;
+  launch_pyrdown_u8(src, dst, nullptr, nullptr, ctx->stream);
+  SF_CHECK(cudaGetLastError());
+  return SF_OK;
+}
+
+int sf_ComputeDerivativeImage(sf_context *ctx, sf_image image, sf_image dx, sf_image dy) {
+  if (!ctx || !img_ok(image, 1) || !img_ok(dx, 2) || !img_ok(dy, 2) || dx.cols != image.cols ||
+      dx.rows != image.rows || dy.cols != image.cols || dy.rows != image.rows)
+    return SF_ERR_INVALID;
+  launch_derivatives(&image, &dx, &dy, nullptr, 1, ctx->stream);
+  SF_CHECK(cudaGetLastError());
+  return SF_OK;
+}
+
+namespace {
+// Photometric inputs of one level, checked against the level's vertex map;
+// the candidate flags go to `cand` (rows x cols bytes of scratch).
+int rgb_level(sf_context *ctx, const sf_image &vmap, const sf_image &inext, const sf_image &ilast,
+              const sf_image &dx, const sf_image &dy, uint8_t *cand, RgbLevelArgs &R) {
+  const sf_image *u8[2] = {&inext, &ilast}, *s16[2] = {&dx, &dy};
+  for (auto im : u8)
+    if (!img_ok(*im, 1) || im->cols != vmap.cols || im->rows != vmap.rows) return SF_ERR_INVALID;
+  for (auto im : s16)
+    if (!img_ok(*im, 2) || im->cols != vmap.cols || im->rows != vmap.rows) return SF_ERR_INVALID;
+  R.inext = inext; R.ilast = ilast; R.dx = dx; R.dy = dy;
+  R.cand.data = cand; R.cand.step = (size_t)vmap.cols; R.cand.cols = vmap.cols; R.cand.rows = vmap.rows;
+  R.corr = ctx->icp.corr;
+  launch_rgb_cand(inext, dx, dy, R.cand, ctx->stream);
+  return SF_OK;
+}
+}  // namespace
+
+int sf_RGBStep(sf_context *ctx, sf_image next_image, sf_image last_image, sf_image next_vmap,
+               sf_image last_vmap, sf_image dIdx, sf_image dIdy, sf_mat3 Rcurr, sf_mat3 RcurrInv,
+               sf_mat3 Rlast, sf_mat3 RlastInv, sf_float3 tcurr, sf_float3 tlast, sf_intrinsics K,
+               float residual[2], double matrixA[36], double vectorB[6]) {
+  if (!ctx || !residual || !matrixA || !vectorB) return SF_ERR_INVALID;
+  if (!img_ok(next_vmap, 16) || !img_ok(last_vmap, 16) || last_vmap.cols != next_vmap.cols ||
+      last_vmap.rows != next_vmap.rows)
+    return SF_ERR_INVALID;
+  const size_t px = (size_t)next_vmap.cols * next_vmap.rows;
+  int st = icp_workspace_rgb(ctx->icp, px);
+  if (st) return st;
+  IcpLevelArgs L;
+  L.vc = next_vmap; L.vl = last_vmap; L.nc = next_vmap; L.nl = last_vmap;
+  L.fx = K.fx; L.fy = K.fy; L.cx = K.cx; L.cy = K.cy;
+  L.iters = 1; L.min_count = 0;
+  RgbLevelArgs R;
+  if ((st = rgb_level(ctx, next_vmap, next_image, last_image, dIdx, dIdy, ctx->icp.cand, R))) return st;
+  launch_rgb_step(ctx->icp, L, R, to_m3(Rcurr), to_m3(RcurrInv), to_f3(tcurr), to_m3(Rlast), to_m3(RlastInv),
+                  to_f3(tlast), ctx->stream);
+  SF_CHECK(cudaGetLastError());
+  SF_CHECK(cudaMemcpyAsync(ctx->host_sums, ctx->icp.sums + 29, 29 * sizeof(double), cudaMemcpyDeviceToHost,
+                           ctx->stream));
+  SF_CHECK(cudaStreamSynchronize(ctx->stream));
+  create_matrix(ctx->host_sums, matrixA, vectorB);
+  residual[0] = (float)ctx->host_sums[27];
+  residual[1] = (float)ctx->host_sums[28];
+  return SF_OK;
+}
+
+int sf_ComputeSE3_rgbd(sf_context *ctx, int levels, const sf_image *nv, const sf_image *nn,
+                       const sf_image *lv, const sf_image *ln, const sf_image *next_images,
+                       const sf_image *last_images, const sf_image *next_dIdx, const sf_image *next_dIdy,
+                       sf_intrinsics K, const int *iters, const int *min_count, float thresh,
+                       const double last_pose[16], double next_pose_out[16], int stats_out[6],
+                       float errors_out[2]) {
+  if (!ctx || levels < 1 || levels > kMaxLevels || !nv || !nn || !lv || !ln || !next_images || !last_images ||
+      !next_dIdx || !next_dIdy || !iters || !min_count || !last_pose || !next_pose_out)
+    return SF_ERR_INVALID;
+  const size_t px0 = (size_t)nv[0].cols * nv[0].rows;
+  int st = icp_workspace_rgb(ctx->icp, px0);
+  if (st) return st;
+  IcpLevelArgs L[kMaxLevels];
+  RgbLevelArgs R[kMaxLevels];
+  size_t cand_off = 0;
+  for (int l = 0; l < levels; ++l) {
+    const sf_image *ims[4] = {&nv[l], &nn[l], &lv[l], &ln[l]};
+    for (auto im : ims)
+      if (!img_ok(*im, 16) || im->cols != nv[l].cols || im->rows != nv[l].rows) return SF_ERR_INVALID;
+    if (iters[l] < 0) return SF_ERR_INVALID;
+    const size_t px = (size_t)nv[l].cols * nv[l].rows;
+    if (px > px0 || cand_off + px > 2 * px0) return SF_ERR_INVALID;
+    const float div = (float)(1 << l);
+    L[l].vc = nv[l]; L[l].nc = nn[l]; L[l].vl = lv[l]; L[l].nl = ln[l];
+    L[l].fx = K.fx / div; L[l].fy = K.fy / div; L[l].cx = K.cx / div; L[l].cy = K.cy / div;
+    L[l].iters = iters[l];
+    L[l].min_count = min_count[l];
+    if ((st = rgb_level(ctx, nv[l], next_images[l], last_images[l], next_dIdx[l], next_dIdy[l],
+                        ctx->icp.cand + cand_off, R[l])))
+      return st;
+    cand_off += px;
+  }
+  SF_CHECK(cudaMemcpyAsync(ctx->pose, last_pose, 16 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  SF_CHECK(icp_persistent_reset(ctx->icp, ctx->stream));
+  SF_CHECK(launch_icp_persistent(ctx->icp, L, levels, thresh, ctx->pose, nullptr, ctx->flags, ctx->stream, R));
+  SF_CHECK(cudaMemcpyAsync(ctx->host_ctl, ctx->icp.ctl, sizeof(TrackCtl), cudaMemcpyDeviceToHost, ctx->stream));
+  SF_CHECK(cudaStreamSynchronize(ctx->stream));
+  const TrackCtl &c = *ctx->host_ctl;
+  for (int k = 0; k < 16; ++k) next_pose_out[k] = c.next_pose[k];
+  if (stats_out) {
+    stats_out[0] = c.accepted;
+    stats_out[1] = c.stop;
+    stats_out[2] = c.iters_run;
+    stats_out[3] = c.icpCount;
+    stats_out[4] = c.rgbCount;
+    stats_out[5] = 0;
+  }
+  if (errors_out) {
+    errors_out[0] = c.icpError;
+    errors_out[1] = c.rgbError;
+  }
+  return SF_OK;
+}
+
 // -------------------------------------------------------- relocalisation
 int sf_RelocScoreBatch(sf_context *ctx, sf_map *m, sf_image vmap, int stride, const double *poses, int n,
                        float inlier_sdf, sf_reloc_score *scores_out) {

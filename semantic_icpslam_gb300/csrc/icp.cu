@@ -44,7 +44,7 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kPWarps = kPThreads / 32;
 
 struct PoseF {
-  m3 Rc, Rl, RlI;
+  m3 Rc, Rl, RlI, RcI;
   f3 tc, tl;
 };
 
@@ -69,6 +69,7 @@ __device__ __forceinline__ void pose_to_float_warp(const double *Pc, const doubl
     const int i = lane / 3, j = lane - 3 * (lane / 3);
     const float rc = (float)Pc[i * 4 + j], rl = (float)Pl[i * 4 + j];
     (&p.Rc.rx.x)[lane] = rc;
+    (&p.RcI.rx.x)[j * 3 + i] = rc;
     (&p.Rl.rx.x)[lane] = rl;
     (&p.RlI.rx.x)[j * 3 + i] = rl;
   } else if (lane < 12) {
@@ -205,6 +206,120 @@ __device__ __forceinline__ void icp_accumulate(const IcpLevelArgs &L, const Pose
       if (q[b].ok && icp_finish(p, q[b], vl[b], nl[b], nc[b], row)) icp_add_row(acc, row);
     }
   }
+}
+
+// ------------------------------------------------------ photometric term
+// RGBReduction::FindCorresp (Reduction.cu:412-463) for a pixel whose
+// pose-independent tests passed (its candidate flag): the current vertex
+// through the current and last poses to the last frame's pixel (u, v) --
+// `+ 0.5` is double and the sum reaches __float2int_rd as a float; the
+// double sum is exact, so that is the float sum rounded once -- then the
+// two vertices' float4 distance below 0.1 and a nonzero last intensity.
+// Returns {u | v << 16, diff}, or x = -1.
+__device__ __forceinline__ int2 rgb_find(const IcpLevelArgs &L, const RgbLevelArgs &R, const PoseF &p, int x,
+                                         int y) {
+  const int2 none = make_int2(-1, 0);
+  const float4 vc = __ldg(row_ptr<const float4>(L.vc, y) + x);
+  if (isnan(vc.x)) return none;
+  const f3 vg = mul(p.Rc, xyz(vc)) + p.tc;
+  const f3 vq = mul(p.RlI, vg - p.tl);
+  const int u = __float2int_rd(__fadd_rn(__fadd_rn(__fdiv_rn(__fmul_rn(L.fx, vq.x), vq.z), L.cx), 0.5f));
+  const int v = __float2int_rd(__fadd_rn(__fadd_rn(__fdiv_rn(__fmul_rn(L.fy, vq.y), vq.z), L.cy), 0.5f));
+  if (u < 0 || v < 0 || u >= L.vc.cols || v >= L.vc.rows) return none;
+  const float4 vl = __ldg(row_ptr<const float4>(L.vl, v) + u);
+  if (isnan(vl.x)) return none;
+  const float d0 = vl.x - vc.x, d1 = vl.y - vc.y, d2 = vl.z - vc.z, d3 = vl.w - vc.w;
+  // (double)sqrtf(n2) < 0.1 iff n2 < 0x3c23d70a (0.01f): sqrtf is
+  // correctly rounded and monotone
+  if (!(d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3 < __int_as_float(0x3c23d70a))) return none;
+  const int il = __ldg(row_ptr<const uint8_t>(R.ilast, v) + u);
+  if (il == 0) return none;
+  const int in = __ldg(row_ptr<const uint8_t>(R.inext, y) + x);
+  return make_int2(u | (v << 16), in - il);
+}
+
+// RGBReduction::GetRow (Reduction.cu:483-517): w = 1 / (sigma + |diff|)
+// (1 when that is below 1e-3, or when sigma < 1e-6), the last vertex in the
+// current camera, the gradient / 9 (the float quotient equals the
+// reference's double one for every short), and the row [w left,
+// w (point x left), -w diff].
+__device__ __forceinline__ void rgb_row(const IcpLevelArgs &L, const RgbLevelArgs &R, const PoseF &p,
+                                        float sigma, bool sigma_tiny, int x, int y, int2 c, float row[7]) {
+  const int u = c.x & 0xffff, v = c.x >> 16, diff = c.y;
+  float w = sigma + (float)abs(diff);
+  w = w < 0.001f ? 1.0f : __fdiv_rn(1.0f, w);  // (double)w < 1e-3 iff w < 0.001f
+  if (sigma_tiny) w = 1.0f;
+  const float4 vl = __ldg(row_ptr<const float4>(L.vl, v) + u);
+  const f3 point = mul(p.RcI, (mul(p.Rl, xyz(vl)) + p.tl) - p.tc);
+  const float gx = __fdiv_rn((float)__ldg(row_ptr<const short>(R.dx, y) + x), 9.0f);
+  const float gy = __fdiv_rn((float)__ldg(row_ptr<const short>(R.dy, y) + x), 9.0f);
+  const float invz = __fdiv_rn(1.0f, point.z);
+  f3 left;
+  left.x = gx * L.fx * invz;
+  left.y = gy * L.fy * invz;
+  left.z = -(left.x * point.x + left.y * point.y) * invz;
+  const f3 cr = cross(point, left);
+  row[0] = w * left.x; row[1] = w * left.y; row[2] = w * left.z;
+  row[3] = w * cr.x; row[4] = w * cr.y; row[5] = w * cr.z;
+  row[6] = -w * (float)diff;
+}
+
+// RGBStep's sigma (Reduction.cu:619-622) from the integer sums; sigma_tiny
+// is (double)sigma < 1e-6, i.e. sigma <= 1e-6f.
+__device__ __forceinline__ float rgb_sigma(unsigned cnt, unsigned ssq, bool &tiny) {
+  const int c = (int)cnt, q = (int)ssq;
+  const float sg = __fsqrt_rn(__fdiv_rn((float)q, (float)(c == 0 ? 1 : c)));
+  tiny = sg <= 1e-6f;
+  return sg;
+}
+
+// ComputeResidualKernel's pass (Reduction.cu:465-481) over this thread's
+// pixels i = gtid, gtid + gstride, ...: the correspondence of each goes to
+// R.corr[i]; cnt / ssq gather the count and sum of diff^2 (32-bit
+// wrapping sums, as the reference's int sums).
+__device__ __forceinline__ void rgb_residual_pass(const IcpLevelArgs &L, const RgbLevelArgs &R, const PoseF &p,
+                                                  int gtid, int gstride, unsigned &cnt, unsigned &ssq) {
+  const int cols = L.vc.cols, N = cols * L.vc.rows;
+  for (int i = gtid; i < N; i += gstride) {
+    const int y = i / cols, x = i - y * cols;
+    int2 c = make_int2(-1, 0);
+    if (__ldg(row_ptr<const uint8_t>(R.cand, y) + x)) c = rgb_find(L, R, p, x, y);
+    __stcg(R.corr + i, c);
+    if (c.x >= 0) {
+      cnt += 1u;
+      ssq += (unsigned)(c.y * c.y);
+    }
+  }
+}
+
+// RgbStepKernel's pass (Reduction.cu:519-551): the 29 terms of this
+// thread's pixels' rows.
+__device__ __forceinline__ void rgb_rows_pass(const IcpLevelArgs &L, const RgbLevelArgs &R, const PoseF &p,
+                                              float sigma, bool tiny, int gtid, int gstride, float acc[29]) {
+#pragma unroll
+  for (int k = 0; k < 29; ++k) acc[k] = 0.f;
+  const int cols = L.vc.cols, N = cols * L.vc.rows;
+  for (int i = gtid; i < N; i += gstride) {
+    const int2 c = __ldcg(R.corr + i);
+    if (c.x < 0) continue;
+    const int y = i / cols, x = i - y * cols;
+    float row[7];
+    rgb_row(L, R, p, sigma, tiny, x, y, c, row);
+    icp_add_row(acc, row);
+  }
+}
+
+// Block totals of the correspondence count and sum of diff^2 (wrapping
+// 32-bit sums) in s2[0..1], which must be zero on entry; valid after the
+// __syncthreads.
+__device__ __forceinline__ void block_sum2(unsigned cnt, unsigned ssq, unsigned *s2) {
+  cnt = __reduce_add_sync(0xffffffffu, cnt);
+  ssq = __reduce_add_sync(0xffffffffu, ssq);
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(s2, cnt);
+    atomicAdd(s2 + 1, ssq);
+  }
+  __syncthreads();
 }
 
 // Float-float (hi + lo) accumulation: Knuth's TwoSum on the leading parts,
@@ -385,10 +500,13 @@ static_assert(kFixFrac == 60, "fix_total's scale factors");
 
 struct PersistentArgs {
   IcpLevelArgs lv[kMaxLevels];
+  RgbLevelArgs rg[kMaxLevels];  // photometric form only
   int levels;
   float thresh;
   unsigned *arrivals;        // grid barrier count, zero at launch
   unsigned long long *fix;   // [3][kFixGroups][29][kFixSlots] accumulators, zero at launch
+  unsigned long long *fix_rgb;  // the same for the photometric sums, zero at launch
+  unsigned *rgb_res;         // [3][kFixGroups][2] count and sum of diff^2, zero at launch
   TrackCtl *ctl;
   const double *last_pose;
   const int *skip_flag;  // nonzero: the kernel does nothing
@@ -410,17 +528,17 @@ __device__ __forceinline__ void prof_mark(const PersistentArgs &a, int it, int k
   }
 }
 
-// Grid barrier of iteration it (counted from 0 in this launch): the
-// arrival count only grows, so the barrier is open once it reaches
-// nb * (it + 1).  Thread 0 releases the CTA's accumulator adds with its
-// arrival and acquires everyone else's with the poll that sees the count.
-// A wait that runs past 2^22 polls records SF_FLAG_BARRIER_TIMEOUT and
-// goes on.
-__device__ __forceinline__ void grid_barrier(const PersistentArgs &a, int nb, int it) {
+// Grid barrier number k (counted from 0 in this launch): the arrival
+// count only grows, so the barrier is open once it reaches nb * (k + 1).
+// Thread 0 releases the CTA's accumulator adds (and the stores its threads
+// made before the __syncthreads) with its arrival and acquires everyone
+// else's with the poll that sees the count.  A wait that runs past 2^22
+// polls records SF_FLAG_BARRIER_TIMEOUT and goes on.
+__device__ __forceinline__ void grid_barrier(const PersistentArgs &a, int nb, int k) {
   __syncthreads();
   if (threadIdx.x == 0) {
     asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(a.arrivals) : "memory");
-    const unsigned target = (unsigned)nb * (unsigned)(it + 1);
+    const unsigned target = (unsigned)nb * (unsigned)(k + 1);
     unsigned polls = 0, seen;
     for (;;) {
       asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(seen) : "l"(a.arrivals) : "memory");
@@ -435,12 +553,42 @@ __device__ __forceinline__ void grid_barrier(const PersistentArgs &a, int nb, in
   __syncthreads();
 }
 
+// The 29 totals of accumulator set fx (kFixGroups groups) into out
+// (threads 0..28); with sync_after the block then synchronises (else the
+// caller does before reading out or reusing sfix).
+__device__ __forceinline__ void read_fix_set(const unsigned long long *fx,
+                                             unsigned long long (*sfix)[kFixSlots], double *out,
+                                             bool sync_after) {
+  for (int k = threadIdx.x; k < kFixGroups * 29; k += blockDim.x) {
+    const ulonglong2 *d = reinterpret_cast<const ulonglong2 *>(fx + (size_t)k * kFixSlots);
+    const ulonglong2 x = __ldcg(d), y = __ldcg(d + 1);
+    sfix[k][0] = x.x; sfix[k][1] = x.y; sfix[k][2] = y.x; sfix[k][3] = y.y;
+  }
+  __syncthreads();
+  if (threadIdx.x < 29) {
+    unsigned long long t[kFixSlots] = {0ull, 0ull, 0ull, 0ull};
+#pragma unroll
+    for (int g = 0; g < kFixGroups; ++g)
+#pragma unroll
+      for (int q = 0; q < kFixSlots; ++q) t[q] += sfix[g * 29 + threadIdx.x][q];
+    out[threadIdx.x] = fix_total(t[0], t[1], t[2], t[3]);
+  }
+  if (sync_after) __syncthreads();
+}
+
+// RGB: each iteration also runs RGBStep (Tracking.cc:400-431): the
+// correspondence pass beside the ICP rows, a grid barrier for its count
+// and sum of diff^2 (sigma), the photometric rows, a second barrier, and
+// the solve of the combined system.
+template <bool RGB>
 __global__ void __launch_bounds__(kPThreads, 1) k_icp_persistent(PersistentArgs a) {
   __shared__ TrackCtl ctl;
   __shared__ IcpSolveSmem ssolve;
   __shared__ PoseF pose;
   __shared__ float2 bsum[29];
   __shared__ double sums[29];
+  __shared__ double rsums[RGB ? 29 : 1];
+  __shared__ unsigned s2[2];
   __shared__ ff wpart[kPWarps][33];
   __shared__ unsigned long long sfix[kFixGroups * 29][kFixSlots];
   if (a.skip_flag && *a.skip_flag != 0) return;  // uniform across the grid
@@ -461,43 +609,66 @@ __global__ void __launch_bounds__(kPThreads, 1) k_icp_persistent(PersistentArgs 
     for (int j = 0; j < L.iters; ++j, ++it) {
       prof_mark(a, it, 0);
       if (threadIdx.x < 32) pose_to_float_warp(ctl.next_pose, ctl.last_pose, pose);
+      if (RGB && threadIdx.x < 2) s2[threadIdx.x] = 0u;
       __syncthreads();
       float acc[29];
       icp_accumulate(L, pose, gtid, gstride, acc);
+      unsigned cnt = 0u, ssq = 0u;
+      if (RGB) rgb_residual_pass(L, a.rg[l], pose, gtid, gstride, cnt, ssq);
       prof_mark(a, it, 1);
       block_reduce29<kPWarps>(acc, wpart, bsum);
+      const int group = blockIdx.x % kFixGroups;
       unsigned long long *fx = a.fix + (size_t)set * kFixSet;
-      if (threadIdx.x < 29)
-        fix_add(fx + ((blockIdx.x % kFixGroups) * 29 + threadIdx.x) * kFixSlots, bsum[threadIdx.x]);
+      if (threadIdx.x < 29) fix_add(fx + (group * 29 + threadIdx.x) * kFixSlots, bsum[threadIdx.x]);
+      unsigned *rres = a.rgb_res + (size_t)set * kFixGroups * 2;
+      if (RGB) {
+        block_sum2(cnt, ssq, s2);
+        if (threadIdx.x < 2) atomicAdd(rres + group * 2 + threadIdx.x, s2[threadIdx.x]);
+      }
       prof_mark(a, it, 2);
-      grid_barrier(a, nb, it);
+      grid_barrier(a, nb, RGB ? 2 * it : it);
       prof_mark(a, it, 3);
-      for (int k = threadIdx.x; k < kFixGroups * 29; k += blockDim.x) {
-        const ulonglong2 *d = reinterpret_cast<const ulonglong2 *>(fx + (size_t)k * kFixSlots);
-        const ulonglong2 x = __ldcg(d), y = __ldcg(d + 1);
-        sfix[k][0] = x.x; sfix[k][1] = x.y; sfix[k][2] = y.x; sfix[k][3] = y.y;
+      unsigned long long *fxr = a.fix_rgb + (size_t)set * kFixSet;
+      if (RGB) {
+        // sigma from the grid's count and sum of diff^2, then the rows
+        if (threadIdx.x < 32) {
+          const int lane = threadIdx.x;
+          const unsigned v = lane < kFixGroups * 2 ? __ldcg(rres + lane) : 0u;
+          const unsigned c2 = __reduce_add_sync(0xffffffffu, (lane & 1) ? 0u : v);
+          const unsigned q2 = __reduce_add_sync(0xffffffffu, (lane & 1) ? v : 0u);
+          if (lane == 0) { s2[0] = c2; s2[1] = q2; }
+        }
+        __syncthreads();
+        bool tiny;
+        const float sigma = rgb_sigma(s2[0], s2[1], tiny);
+        rgb_rows_pass(L, a.rg[l], pose, sigma, tiny, gtid, gstride, acc);
+        block_reduce29<kPWarps>(acc, wpart, bsum);
+        if (threadIdx.x < 29) fix_add(fxr + (group * 29 + threadIdx.x) * kFixSlots, bsum[threadIdx.x]);
+        grid_barrier(a, nb, 2 * it + 1);
       }
-      __syncthreads();
-      if (threadIdx.x < 29) {
-        unsigned long long t[kFixSlots] = {0ull, 0ull, 0ull, 0ull};
-#pragma unroll
-        for (int g = 0; g < kFixGroups; ++g)
-#pragma unroll
-          for (int q = 0; q < kFixSlots; ++q) t[q] += sfix[g * 29 + threadIdx.x][q];
-        sums[threadIdx.x] = fix_total(t[0], t[1], t[2], t[3]);
+      read_fix_set(fx, sfix, sums, RGB);
+      if (RGB) {
+        read_fix_set(fxr, sfix, rsums, true);
+        // A = A_rgb w + A_icp, b = b_rgb w + b_icp (Tracking.cc:484-487)
+        if (threadIdx.x < 27) sums[threadIdx.x] = __dadd_rn(__dmul_rn(rsums[threadIdx.x], (double)1e-4f), sums[threadIdx.x]);
       }
-      // Every CTA read the previous iteration's set before it arrived here,
-      // so CTA 0 clears it for iteration it + 2; its clearing is released
-      // with its next arrival, before anyone can add into it.
+      // Every CTA read the previous iteration's sets before it arrived here,
+      // so CTA 0 clears them for iteration it + 2; its clearing is released
+      // with its next arrival, before anyone can add into them.
       const int prev = set == 0 ? 2 : set - 1;
-      if (blockIdx.x == 0)
+      if (blockIdx.x == 0) {
         for (int k = threadIdx.x; k < kFixSet; k += blockDim.x) __stcg(a.fix + (size_t)prev * kFixSet + k, 0ull);
+        if (RGB) {
+          for (int k = threadIdx.x; k < kFixSet; k += blockDim.x) __stcg(a.fix_rgb + (size_t)prev * kFixSet + k, 0ull);
+          if (threadIdx.x < kFixGroups * 2) __stcg(a.rgb_res + (size_t)prev * kFixGroups * 2 + threadIdx.x, 0u);
+        }
+      }
       __syncthreads();
       prof_mark(a, it, 4);
       if (threadIdx.x == 0)
         s_solve_marks = (a.prof && blockIdx.x == 0 && it < kProfIters) ? a.prof + it * kProfSlots + 8 : nullptr;
       __syncwarp();
-      if (threadIdx.x < 96) ctl_step_fast(ctl, sums, L.min_count, ssolve);
+      if (threadIdx.x < 96) ctl_step_fast(ctl, sums, L.min_count, ssolve, RGB ? rsums : nullptr);
       __syncthreads();
       prof_mark(a, it, 5);
       set = set == 2 ? 0 : set + 1;
@@ -532,9 +703,54 @@ __global__ void __launch_bounds__(kThreads) k_icp_reduce(const double *part, int
   if (threadIdx.x < 29) out[threadIdx.x] = sums[threadIdx.x];
 }
 
+// Plain form of RGBStep, launch 1: correspondences, their count and sum of
+// diff^2 added into res[0..1] (zero on entry).
+__global__ void __launch_bounds__(kThreads) k_rgb_residual(IcpLevelArgs L, RgbLevelArgs R, PoseF p,
+                                                           unsigned *res) {
+  __shared__ unsigned s2[2];
+  if (threadIdx.x < 2) s2[threadIdx.x] = 0u;
+  __syncthreads();
+  unsigned cnt = 0u, ssq = 0u;
+  rgb_residual_pass(L, R, p, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, cnt, ssq);
+  block_sum2(cnt, ssq, s2);
+  if (threadIdx.x < 2) atomicAdd(res + threadIdx.x, s2[threadIdx.x]);
+}
+
+// Plain form of RGBStep, launch 2: per-CTA FP64 partials of the rows'
+// 29 terms, sigma from res.
+__global__ void __launch_bounds__(kThreads) k_rgb_partials(IcpLevelArgs L, RgbLevelArgs R, PoseF p,
+                                                           const unsigned *res, double *part, int stride) {
+  __shared__ float2 bsum[29];
+  __shared__ ff wpart[kWarps][33];
+  bool tiny;
+  const float sigma = rgb_sigma(__ldcg(res), __ldcg(res + 1), tiny);
+  float acc[29];
+  rgb_rows_pass(L, R, p, sigma, tiny, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, acc);
+  block_reduce29<kWarps>(acc, wpart, bsum);
+  if (threadIdx.x < 29)
+    part[(size_t)threadIdx.x * stride + blockIdx.x] = (double)bsum[threadIdx.x].x + (double)bsum[threadIdx.x].y;
+}
+
+// FindCorresp's pose-independent tests from an image and its derivatives
+// (the flag launch_derivatives makes beside them).
+__global__ void k_rgb_cand(sf_image img, sf_image dx, sf_image dy, sf_image cand) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= img.cols || y >= img.rows) return;
+  bool ok = x >= 5 && x < img.cols - 5 && y >= 5 && y < img.rows - 5 &&
+            (row_ptr<const short>(dx, y)[x] != 0 || row_ptr<const short>(dy, y)[x] != 0);
+  if (ok)
+    for (int u = y - 2; u < y + 2; ++u)
+      for (int v = x - 2; v < x + 2; ++v) ok = ok && row_ptr<const uint8_t>(img, u)[v] > 0;
+  row_ptr<uint8_t>(cand, y)[x] = ok ? 1 : 0;
+}
+
 }  // namespace
 
-constexpr size_t kBarrierBytes = 256 + sizeof(unsigned long long) * 3 * kFixSet;
+// arrival count (256 B), ICP accumulator sets, photometric accumulator
+// sets, photometric count / sum of diff^2 sets
+constexpr size_t kFixBytes = sizeof(unsigned long long) * 3 * kFixSet;
+constexpr size_t kBarrierBytes = 256 + 2 * kFixBytes + sizeof(unsigned) * 3 * kFixGroups * 2;
 
 cudaError_t icp_persistent_reset(const IcpWorkspace &w, cudaStream_t s) {
   return cudaMemsetAsync(w.barrier, 0, kBarrierBytes, s);
@@ -545,17 +761,24 @@ int icp_workspace_init(IcpWorkspace &w) {
   if (cudaGetDevice(&dev) != cudaSuccess) return SF_ERR_CUDA;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_icp_persistent, kPThreads, 0) !=
-      cudaSuccess)
+  int per_sm_rgb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_icp_persistent<false>, kPThreads, 0) !=
+          cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_rgb, k_icp_persistent<true>, kPThreads, 0) !=
+          cudaSuccess)
     return SF_ERR_CUDA;
-  if (per_sm < 1 || !coop) return SF_ERR_CUDA;
+  if (per_sm < 1 || per_sm_rgb < 1 || !coop) return SF_ERR_CUDA;
   w.max_blocks = sms * per_sm;
+  w.max_blocks_rgb = sms * per_sm_rgb;
   w.threads = kPThreads;
   if (cudaMalloc(&w.partials, sizeof(double) * 2 * 29 * (size_t)w.max_blocks) != cudaSuccess) return SF_ERR_CUDA;
-  if (cudaMalloc(&w.sums, sizeof(double) * 29) != cudaSuccess) return SF_ERR_CUDA;
+  if (cudaMalloc(&w.sums, sizeof(double) * 2 * 29) != cudaSuccess) return SF_ERR_CUDA;
   if (cudaMalloc(&w.barrier, kBarrierBytes) != cudaSuccess) return SF_ERR_CUDA;
   if (cudaMemset(w.barrier, 0, kBarrierBytes) != cudaSuccess) return SF_ERR_CUDA;
-  w.fix = reinterpret_cast<unsigned long long *>(reinterpret_cast<char *>(w.barrier) + 256);
+  char *base = reinterpret_cast<char *>(w.barrier);
+  w.fix = reinterpret_cast<unsigned long long *>(base + 256);
+  w.fix_rgb = reinterpret_cast<unsigned long long *>(base + 256 + kFixBytes);
+  w.rgb_res = reinterpret_cast<unsigned *>(base + 256 + 2 * kFixBytes);
   if (cudaMalloc(&w.ctl, sizeof(TrackCtl)) != cudaSuccess) return SF_ERR_CUDA;
   if (cudaMalloc(&w.prof, sizeof(unsigned long long) * kProfSlots * kProfIters) != cudaSuccess) return SF_ERR_CUDA;
   if (cudaMemset(w.prof, 0, sizeof(unsigned long long) * kProfSlots * kProfIters) != cudaSuccess) return SF_ERR_CUDA;
@@ -568,7 +791,41 @@ void icp_workspace_free(IcpWorkspace &w) {
   cudaFree(w.barrier);
   cudaFree(w.ctl);
   cudaFree(w.prof);
+  cudaFree(w.corr);
+  cudaFree(w.cand);
   w = IcpWorkspace();
+}
+
+int icp_workspace_rgb(IcpWorkspace &w, size_t pixels) {
+  if (pixels <= w.rgb_pixels) return SF_OK;
+  cudaFree(w.corr);
+  cudaFree(w.cand);
+  w.corr = nullptr;
+  w.cand = nullptr;
+  w.rgb_pixels = 0;
+  // candidate flags of every level: at most 4/3 of level 0, padded
+  if (cudaMalloc(&w.corr, sizeof(int2) * pixels) != cudaSuccess) return SF_ERR_CUDA;
+  if (cudaMalloc(&w.cand, pixels * 2) != cudaSuccess) return SF_ERR_CUDA;
+  w.rgb_pixels = pixels;
+  return SF_OK;
+}
+
+void launch_rgb_step(const IcpWorkspace &w, const IcpLevelArgs &L, const RgbLevelArgs &R, const m3 &Rc,
+                     const m3 &RcInv, f3 tc, const m3 &Rl, const m3 &RlInv, f3 tl, cudaStream_t s) {
+  PoseF p;
+  p.Rc = Rc; p.RcI = RcInv; p.tc = tc; p.Rl = Rl; p.RlI = RlInv; p.tl = tl;
+  const int nb = w.max_blocks;
+  cudaMemsetAsync(w.rgb_res, 0, 2 * sizeof(unsigned), s);
+  k_rgb_residual<<<nb, kThreads, 0, s>>>(L, R, p, w.rgb_res); note_launch();
+  k_rgb_partials<<<nb, kThreads, 0, s>>>(L, R, p, w.rgb_res, w.partials, w.max_blocks); note_launch();
+  k_icp_reduce<<<1, kThreads, 0, s>>>(w.partials, nb, w.max_blocks, w.sums + 29); note_launch();
+}
+
+void launch_rgb_cand(const sf_image &inext, const sf_image &dx, const sf_image &dy, const sf_image &cand,
+                     cudaStream_t s) {
+  const dim3 blk(32, 8);
+  const dim3 grd((inext.cols + 31) / 32, (inext.rows + 7) / 8);
+  k_rgb_cand<<<grd, blk, 0, s>>>(inext, dx, dy, cand); note_launch();
 }
 
 void launch_icp_step(const IcpWorkspace &w, const IcpLevelArgs &L, const m3 &Rc, f3 tc,
@@ -582,20 +839,25 @@ void launch_icp_step(const IcpWorkspace &w, const IcpLevelArgs &L, const m3 &Rc,
 
 cudaError_t launch_icp_persistent(const IcpWorkspace &w, const IcpLevelArgs *levels, int nlevels,
                                   float thresh, const double *last_pose, const int *skip_flag,
-                                  uint32_t *flags, cudaStream_t s) {
-  PersistentArgs a;
-  for (int l = 0; l < nlevels && l < kMaxLevels; ++l) a.lv[l] = levels[l];
+                                  uint32_t *flags, cudaStream_t s, const RgbLevelArgs *rgb) {
+  PersistentArgs a = {};
+  for (int l = 0; l < nlevels && l < kMaxLevels; ++l) {
+    a.lv[l] = levels[l];
+    if (rgb) a.rg[l] = rgb[l];
+  }
   a.levels = nlevels;
   a.thresh = thresh;
   a.arrivals = w.barrier;
   a.fix = w.fix;
+  a.fix_rgb = w.fix_rgb;
+  a.rgb_res = w.rgb_res;
   a.ctl = w.ctl;
   a.last_pose = last_pose;
   a.skip_flag = skip_flag;
   a.flags = flags;
   a.prof = w.profile ? w.prof : nullptr;
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(w.max_blocks);
+  cfg.gridDim = dim3(rgb ? w.max_blocks_rgb : w.max_blocks);
   cfg.blockDim = dim3(kPThreads);
   cfg.dynamicSmemBytes = 0;
   cfg.stream = s;
@@ -605,7 +867,8 @@ cudaError_t launch_icp_persistent(const IcpWorkspace &w, const IcpLevelArgs *lev
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   note_launch();
-  return cudaLaunchKernelEx(&cfg, k_icp_persistent, a);
+  return rgb ? cudaLaunchKernelEx(&cfg, k_icp_persistent<true>, a)
+             : cudaLaunchKernelEx(&cfg, k_icp_persistent<false>, a);
 }
 
 }  // namespace sf

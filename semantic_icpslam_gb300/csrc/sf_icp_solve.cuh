@@ -127,10 +127,20 @@ __device__ __forceinline__ void solve6_two_warps(const double *sums, double x[6]
 // inliers or a NaN error (next = last), 2 to stop on three rises in a row
 // (next = the candidate); *copy_cand asks for the current pose to become
 // the candidate first.
-__device__ __forceinline__ int ctl_decide(TrackCtl &c, const double *sums, int min_count, int *copy_cand) {
+__device__ __forceinline__ int ctl_decide(TrackCtl &c, const double *sums, int min_count, int *copy_cand,
+                                          const double *rsums) {
   int code = 0;
   *copy_cand = 0;
   c.iters_run++;
+  if (rsums) {  // RGBStep's error and count first (Tracking.cc:421-431)
+    const float r0 = (float)rsums[27], r1 = (float)rsums[28];
+    c.rgbError = sqrtf(r0) / r1;
+    c.rgbCount = (int)r1;
+    if (isnan(c.rgbError) || c.rgbCount < min_count) {
+      c.stop = 1;
+      return 1;
+    }
+  }
   float residual0 = (float)sums[27], residual1 = (float)sums[28];
   c.icpError = sqrtf(residual0) / residual1;
   c.icpCount = (int)residual1;
@@ -138,8 +148,8 @@ __device__ __forceinline__ int ctl_decide(TrackCtl &c, const double *sums, int m
     c.stop = 1;
     code = 1;
   } else {
-    const float rgbError = 0.f, wgt = 1e-4f;
-    float currError = rgbError * wgt + c.icpError;
+    const float wgt = 1e-4f;
+    float currError = c.rgbError * wgt + c.icpError;
     if (c.lastError < currError) {
       c.breakCount++;
       *copy_cand = (c.breakCount == 1);
@@ -163,11 +173,14 @@ __device__ __forceinline__ int ctl_decide(TrackCtl &c, const double *sums, int m
 // and 1 solve and build exp(-x) (rotation on warp 0, translation on warp
 // 1), so the three overlap; after named barrier 2, warp 0 applies the
 // decision (or the update).  Same contract and state transitions as
-// sf::ctl_step; warp 0 returns whether to go on.
-__device__ bool ctl_step_fast(TrackCtl &c, const double *sums, int min_count, IcpSolveSmem &s) {
+// sf::ctl_step; warp 0 returns whether to go on.  With the photometric
+// term, sums[0..26] already hold the combined system and rsums the RGB
+// sums (for its error and count).
+__device__ bool ctl_step_fast(TrackCtl &c, const double *sums, int min_count, IcpSolveSmem &s,
+                              const double *rsums = nullptr) {
   const int lane = threadIdx.x & 31;
   if (threadIdx.x >= 64) {  // warp 2
-    if (lane == 0) s.code = ctl_decide(c, sums, min_count, &s.copy_cand);
+    if (lane == 0) s.code = ctl_decide(c, sums, min_count, &s.copy_cand, rsums);
     asm volatile("bar.sync 2, 96;" ::: "memory");
     return false;
   }

@@ -44,17 +44,52 @@ struct IcpLevelArgs {
   int iters, min_count;
 };
 
+// Photometric term of one level (RGBStep, Tracking/Reduction.cu:387-642):
+// the next and last frames' intensities (uint8), the next frame's
+// derivative images (int16) and candidate flags (uint8, see
+// launch_derivatives), and the per-pixel correspondences of the current
+// iteration (int2 {u | v << 16, diff}, x = -1 when none).
+struct RgbLevelArgs {
+  sf_image inext, ilast, dx, dy, cand;
+  int2 *corr;
+};
+
 struct IcpWorkspace {
   double *partials = nullptr;  // [2][29][max_blocks]
-  double *sums = nullptr;      // [29]
+  double *sums = nullptr;      // [29] (photometric: [2][29], ICP then RGB)
   unsigned *barrier = nullptr; // persistent kernel: arrival count, then (at +256 B) fix
   unsigned long long *fix = nullptr;  // [3][8][29][4] fixed-point accumulators (sets, CTA groups)
+  unsigned long long *fix_rgb = nullptr;  // the same for the photometric sums
+  unsigned *rgb_res = nullptr;  // [3][8][2] correspondence count and sum of diff^2 (sets, groups)
   TrackCtl *ctl = nullptr;     // device copy of the tracking state
   int max_blocks = 0;          // co-resident CTAs of the persistent kernel
+  int max_blocks_rgb = 0;      // the same for the photometric form
   int threads = 0;
   unsigned long long *prof = nullptr;  // [64][8] phase clocks of CTA 0
   int profile = 0;                     // record phase clocks when set
+  // photometric scratch, grown on demand: correspondences of the largest
+  // level, and candidate flags of every level for callers that pass none
+  int2 *corr = nullptr;
+  uint8_t *cand = nullptr;
+  size_t rgb_pixels = 0;
 };
+
+// Grows the photometric scratch to `pixels` (level 0) pixels.
+int icp_workspace_rgb(IcpWorkspace &w, size_t pixels);
+
+// Photometric images (csrc/photometric.cu).  save (may be null) receives
+// each pixel's previous value first when *save_flag is nonzero.
+void launch_intensity(const sf_image &rgb, const sf_image &out, const sf_image *save, const int *save_flag,
+                      cudaStream_t s);
+void launch_pyrdown_u8(const sf_image &src, const sf_image &dst, const sf_image *save, const int *save_flag,
+                       cudaStream_t s);
+// Derivative images of every level in one launch; cand (may be null) gets
+// the per-pixel flag of FindCorresp's pose-independent tests.
+void launch_derivatives(const sf_image *img, const sf_image *dx, const sf_image *dy, const sf_image *cand,
+                        int levels, cudaStream_t s);
+void launch_intensity_pyramid(const sf_image &rgb, const sf_image *img, const sf_image *save,
+                              const int *save_flag, const sf_image *dx, const sf_image *dy,
+                              const sf_image *cand, int levels, cudaStream_t s);
 
 int icp_workspace_init(IcpWorkspace &w);
 void icp_workspace_free(IcpWorkspace &w);
@@ -64,6 +99,16 @@ void icp_workspace_free(IcpWorkspace &w);
 void launch_icp_step(const IcpWorkspace &w, const IcpLevelArgs &L, const m3 &Rc, f3 tc,
                      const m3 &Rl, const m3 &RlInv, f3 tl, cudaStream_t s);
 
+// Plain form of RGBStep: the correspondence pass (its count and sum of
+// diff^2 land in w.rgb_res[0..1]), then, with sigma computed from them on
+// the device, the 29 sums of the photometric rows in w.sums + 29.
+void launch_rgb_step(const IcpWorkspace &w, const IcpLevelArgs &L, const RgbLevelArgs &R, const m3 &Rc,
+                     const m3 &RcInv, f3 tc, const m3 &Rl, const m3 &RlInv, f3 tl, cudaStream_t s);
+// Candidate flags of FindCorresp's pose-independent tests from an
+// intensity image and its derivatives (callers that have none).
+void launch_rgb_cand(const sf_image &inext, const sf_image &dx, const sf_image &dy, const sf_image &cand,
+                     cudaStream_t s);
+
 // Zeroes the persistent kernel's barrier count and accumulators (one memset);
 // enqueue it before each launch_icp_persistent.
 cudaError_t icp_persistent_reset(const IcpWorkspace &w, cudaStream_t s);
@@ -71,9 +116,11 @@ cudaError_t icp_persistent_reset(const IcpWorkspace &w, cudaStream_t s);
 // Persistent form: every level and iteration of Tracker::ComputeSE3 in one
 // cooperative launch.  last_pose: device double[16]; result in *w.ctl.
 // skip_flag (device int, may be null): when nonzero the kernel does nothing.
+// rgb (may be null): per-level photometric inputs; then each iteration
+// adds RGBStep's rows (ComputeSE3 with icpOnly = false).
 cudaError_t launch_icp_persistent(const IcpWorkspace &w, const IcpLevelArgs *levels, int nlevels,
                                   float thresh, const double *last_pose, const int *skip_flag,
-                                  uint32_t *flags, cudaStream_t s);
+                                  uint32_t *flags, cudaStream_t s, const RgbLevelArgs *rgb = nullptr);
 
 // -------------------------------------------------------------- fusion
 struct FuseScratch {

@@ -160,6 +160,8 @@ struct TrackCtl {
   int breakCount, icpCount, iters_run;
   int stop;               // 0 running, 1 failed (rolled back), 2 diverged (candidate)
   int accepted;           // final decision (valid after finish)
+  float rgbError;         // photometric term (icpOnly = false), else 0
+  int rgbCount;
 };
 
 SF_HD void ctl_begin(TrackCtl &c, const double *last_pose) {
@@ -178,11 +180,26 @@ SF_HD void ctl_begin(TrackCtl &c, const double *last_pose) {
   c.iters_run = 0;
   c.stop = 0;
   c.accepted = 0;
+  c.rgbError = 0.f;
+  c.rgbCount = 0;
 }
 
-// One iteration given the 29 sums.  Returns false when the loop stops.
-SF_HD bool ctl_step(TrackCtl &c, const double *sums29, int min_count) {
+// One iteration given the 29 ICP sums and, with the photometric term
+// (icpOnly = false), the 29 RGB sums (Tracking.cc:400-499): the RGB error
+// and count are tested first, and the solve takes A_rgb w + A_icp,
+// b_rgb w + b_icp with w = 1e-4f.  Returns false when the loop stops.
+SF_HD bool ctl_step(TrackCtl &c, const double *sums29, int min_count, const double *rgb29 = nullptr) {
   c.iters_run++;
+  if (rgb29) {
+    const float r0 = (float)rgb29[27], r1 = (float)rgb29[28];
+    c.rgbError = sqrtf(r0) / r1;
+    c.rgbCount = (int)r1;
+    if (isnan(c.rgbError) || c.rgbCount < min_count) {
+      for (int k = 0; k < 16; ++k) c.next_pose[k] = c.last_pose[k];
+      c.stop = 1;
+      return false;
+    }
+  }
   float residual0 = (float)sums29[27], residual1 = (float)sums29[28];
   c.icpError = sqrtf(residual0) / residual1;
   c.icpCount = (int)residual1;
@@ -191,8 +208,8 @@ SF_HD bool ctl_step(TrackCtl &c, const double *sums29, int min_count) {
     c.stop = 1;
     return false;
   }
-  const float rgbError = 0.f, w = 1e-4f;
-  float currError = rgbError * w + c.icpError;
+  const float w = 1e-4f;
+  float currError = c.rgbError * w + c.icpError;
   if (c.lastError < currError) {
     c.breakCount++;
     if (c.breakCount == 1)
@@ -210,6 +227,12 @@ SF_HD bool ctl_step(TrackCtl &c, const double *sums29, int min_count) {
   c.lastError = currError;
   double A[36], b[6], x[6], dT[16], dInv[16];
   create_matrix(sums29, A, b);
+  if (rgb29) {
+    double Ar[36], br[6];
+    create_matrix(rgb29, Ar, br);
+    for (int k = 0; k < 36; ++k) A[k] = Ar[k] * (double)w + A[k];
+    for (int k = 0; k < 6; ++k) b[k] = br[k] * (double)w + b[k];
+  }
   ldlt_solve6(A, b, x);
   se3_exp(x, dT);
   mat4_mul(dT, c.delta, c.delta);

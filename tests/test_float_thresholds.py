@@ -9,10 +9,17 @@ monotone in z and agree trivially.
   Mapping/RenderScene.cu:402   z < 1e-3           ->  z < 0.001f
   Mapping/RenderScene.cu:73    pt3d.z < 2e-1      ->  z < 0.2f
 
+  Tracking/Reduction.cu:487    w < 1e-3           ->  w < 0.001f
+  Tracking/Reduction.cu:490    sigma < 1e-6       ->  sigma <= 1e-6f
+
 The ICP inlier tests of Tracking/Reduction.cu:253-255 compare norms,
-sqrtf(d) <= 0.1f and sqrtf(s) < 0.6f; the kernel compares the squared norms
-with the float thresholds that make the two forms agree (sqrtf is correctly
-rounded and monotone), checked the same way against numpy's float32 sqrt.
+sqrtf(d) <= 0.1f and sqrtf(s) < 0.6f, and the photometric correspondence
+test of :448 compares (double)sqrtf(d) < 0.1 (the float4 norm); the kernels
+compare the squared norms with the float thresholds that make the forms
+agree (sqrtf is correctly rounded and monotone), checked the same way
+against numpy's float32 sqrt.  The photometric row's gradient
+(float)((double)g / 9.0) equals the float quotient g / 9.0f for every short
+g (checked exhaustively).
 """
 import numpy as np
 import pytest
@@ -21,6 +28,7 @@ CASES = [
     (0.1, lambda d, t: d > t, lambda f: f >= np.float32(0.1)),
     (1e-3, lambda d, t: d < t, lambda f: f < np.float32(0.001)),
     (2e-1, lambda d, t: d < t, lambda f: f < np.float32(0.2)),
+    (1e-6, lambda d, t: d < t, lambda f: f <= np.float32(1e-6)),
 ]
 
 
@@ -44,6 +52,7 @@ def test_float_threshold_is_exact(t, ref, ours):
 SQRT_CASES = [
     (0.1, 0x3c23d70b, lambda r, t: r <= t, lambda d, T: d <= T),
     (0.6, 0x3eb851ec, lambda r, t: r < t, lambda d, T: d < T),
+    (0.1, 0x3c23d70a, lambda r, t: r.astype(np.float64) < 0.1, lambda d, T: d < T),
 ]
 
 
@@ -56,3 +65,8 @@ def test_squared_norm_threshold_is_exact(t, bits, ref, ours):
         a = ref(np.sqrt(d), np.float32(t))
         b = ours(d, T)
     assert np.array_equal(a, b)
+
+
+def test_gradient_over_nine_is_float_division():
+    g = np.arange(-32768, 32768, dtype=np.float32)
+    assert np.array_equal((g.astype(np.float64) / 9.0).astype(np.float32), g / np.float32(9.0))
