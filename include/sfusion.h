@@ -373,6 +373,9 @@ typedef struct {
   int zrange_cols;         /* z-range image (0: ceil(cols / 8))            */
   int zrange_rows;         /* z-range image (0: ceil(rows / 8))            */
   int use_graph;           /* 1: one CUDA graph per frame; 0: per launch  */
+  int rgb_term;            /* 1: ComputeSE3(icpOnly = false), the
+                              reference's default (Tracking.cc:170): RGBStep
+                              beside ICPStep every iteration; 0: ICP only   */
 } sf_system_config;
 
 typedef struct {
@@ -388,6 +391,8 @@ typedef struct {
   int allocated;           /* entries with ptr >= 0                        */
   uint32_t flags;          /* SF_FLAG_* overflow / timeout bits            */
   double pose[16];         /* camera->world pose after this frame          */
+  float rgb_error;         /* photometric error of the last iteration      */
+  int rgb_count;           /* photometric correspondences                  */
 } sf_frame_stats;
 
 int sf_system_create(sf_context *ctx, const sf_system_config *cfg,

@@ -203,7 +203,7 @@ class System:
 def system_config(cols, rows, K, voxel_size, trunc_dist, num_buckets, num_excess, num_sdf_blocks,
                   levels=3, iters=(10, 5, 4), min_count=(2000, 1000, 100), depth_scale=1000.0,
                   depth_cutoff=3.0, icp_thresh=1e-4, use_graph=1, depth_min=0.1, depth_max=3.0,
-                  zrange=(0, 0), max_rendering_blocks=260000):
+                  zrange=(0, 0), max_rendering_blocks=260000, rgb_term=0):
     cfg = SystemConfig()
     cfg.map = MapConfig(voxel_size, trunc_dist, depth_min, depth_max, num_buckets, num_excess, num_sdf_blocks,
                         max_rendering_blocks)
@@ -216,6 +216,7 @@ def system_config(cols, rows, K, voxel_size, trunc_dist, num_buckets, num_excess
     cfg.icp_thresh = icp_thresh
     cfg.zrange_cols, cfg.zrange_rows = zrange
     cfg.use_graph = use_graph
+    cfg.rgb_term = int(rgb_term)
     return cfg
 
 

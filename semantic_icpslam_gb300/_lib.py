@@ -66,14 +66,15 @@ class SystemConfig(C.Structure):
     _fields_ = [("map", MapConfig), ("cols", C.c_int), ("rows", C.c_int), ("levels", C.c_int),
                 ("K", Intrinsics), ("depth_scale", C.c_float), ("depth_cutoff", C.c_float),
                 ("iters", C.c_int * 4), ("min_count", C.c_int * 4), ("icp_thresh", C.c_float),
-                ("zrange_cols", C.c_int), ("zrange_rows", C.c_int), ("use_graph", C.c_int)]
+                ("zrange_cols", C.c_int), ("zrange_rows", C.c_int), ("use_graph", C.c_int), ("rgb_term", C.c_int)]
 
 
 class FrameStats(C.Structure):
     _fields_ = [("tracked", C.c_int), ("accepted", C.c_int), ("fail", C.c_int), ("iterations", C.c_int),
                 ("icp_error", C.c_float), ("icp_count", C.c_int), ("visible", C.c_uint32),
                 ("heap_counter", C.c_int), ("entry_ptr", C.c_int), ("allocated", C.c_int),
-                ("flags", C.c_uint32), ("pose", C.c_double * 16)]
+                ("flags", C.c_uint32), ("pose", C.c_double * 16), ("rgb_error", C.c_float),
+                ("rgb_count", C.c_int)]
 
 
 class AutotuneReport(C.Structure):

@@ -83,11 +83,14 @@ __global__ void k_sys_stats(const SysDev *s, const TrackCtl *ctl, DevMap m, cons
   st.accepted = s->accepted;
   if (s->first) {
     st.fail = 0; st.iterations = 0; st.icp_error = 0.f; st.icp_count = 0;
+    st.rgb_error = 0.f; st.rgb_count = 0;
   } else {
     st.fail = ctl->stop;
     st.iterations = ctl->iters_run;
     st.icp_error = ctl->icpError;
     st.icp_count = ctl->icpCount;
+    st.rgb_error = ctl->rgbError;
+    st.rgb_count = ctl->rgbCount;
   }
   st.visible = s->run ? *m.no_visible : 0u;
   st.heap_counter = *m.heap_counter;
@@ -129,6 +132,11 @@ struct sf_system {
   float *d_depth[kMaxLevels] = {};
   float4 *d_vmap[kMaxLevels] = {}, *d_nmap[kMaxLevels] = {};
   float4 *d_mv[kMaxLevels] = {}, *d_mn[kMaxLevels] = {};
+  // photometric term: this frame's and the last frame's intensity pyramids,
+  // this frame's derivative images and correspondence candidate flags
+  uint8_t *d_int[kMaxLevels] = {}, *d_int_last[kMaxLevels] = {}, *d_cand[kMaxLevels] = {};
+  int16_t *d_dx[kMaxLevels] = {}, *d_dy[kMaxLevels] = {};
+  int2 *d_corr = nullptr;  // per-iteration correspondences (level-0 size)
   float *d_zmin = nullptr, *d_zmax = nullptr;
   SysDev *d_sys = nullptr;
   sf_frame_stats *d_stats = nullptr;
@@ -180,7 +188,12 @@ int alloc_all(sf_system *s) {
     ok = A((void **)&s->d_depth[l], n * 4) && A((void **)&s->d_vmap[l], n * 16) &&
          A((void **)&s->d_nmap[l], n * 16) && A((void **)&s->d_mv[l], n * 16) &&
          A((void **)&s->d_mn[l], n * 16);
+    if (ok && s->cfg.rgb_term)
+      ok = A((void **)&s->d_int[l], n) && A((void **)&s->d_int_last[l], n) && A((void **)&s->d_cand[l], n) &&
+           A((void **)&s->d_dx[l], n * 2) && A((void **)&s->d_dy[l], n * 2) &&
+           cudaMemset(s->d_int[l], 0, n) == cudaSuccess && cudaMemset(s->d_int_last[l], 0, n) == cudaSuccess;
   }
+  if (ok && s->cfg.rgb_term) ok = A((void **)&s->d_corr, np * sizeof(int2));
   ok = ok && cudaMallocHost(&s->h_depth16, np * 2) == cudaSuccess &&
        cudaMallocHost(&s->h_rgb, np * 3) == cudaSuccess &&
        cudaMallocHost(&s->h_mask, np) == cudaSuccess &&
@@ -194,10 +207,12 @@ int alloc_all(sf_system *s) {
 
 void free_all(sf_system *s) {
   cudaFree(s->d_depth16); cudaFree(s->d_rgb); cudaFree(s->d_mask); cudaFree(s->d_raw);
-  cudaFree(s->d_zmin); cudaFree(s->d_zmax); cudaFree(s->d_sys); cudaFree(s->d_stats);
+  cudaFree(s->d_zmin); cudaFree(s->d_zmax); cudaFree(s->d_sys); cudaFree(s->d_stats); cudaFree(s->d_corr);
   for (int l = 0; l < kMaxLevels; ++l) {
     cudaFree(s->d_depth[l]); cudaFree(s->d_vmap[l]); cudaFree(s->d_nmap[l]);
     cudaFree(s->d_mv[l]); cudaFree(s->d_mn[l]);
+    cudaFree(s->d_int[l]); cudaFree(s->d_int_last[l]); cudaFree(s->d_cand[l]);
+    cudaFree(s->d_dx[l]); cudaFree(s->d_dy[l]);
   }
   if (s->h_depth16) cudaFreeHost(s->h_depth16);
   if (s->h_rgb) cudaFreeHost(s->h_rgb);
@@ -212,9 +227,51 @@ void free_all(sf_system *s) {
   if (s->cstream) cudaStreamDestroy(s->cstream);
 }
 
+// The frame's colour (and mask) upload on the copy stream; captured as an
+// external event wait in the frame graph.
+void wait_inputs(sf_system *s, cudaStream_t st) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(st, &cs);
+  cudaStreamWaitEvent(st, s->ev_inputs, cs == cudaStreamCaptureStatusActive ? cudaEventWaitExternal : 0);
+}
+
+// Frame::FillImages intensity part (Core/Frame.cc:74-84), with the
+// photometric term only: this frame's intensity pyramid, saving the one it
+// replaces as the last frame's when the previous frame was tracked
+// (SwapFrame, Tracking.cc:65-119; SysDev.run still holds that frame's
+// outcome here), then the derivative images and candidate flags.
+void enqueue_intensity(sf_system *s, cudaStream_t st) {
+  const int C = s->cfg.cols, R = s->cfg.rows;
+  sf_image im[kMaxLevels], sv[kMaxLevels], dx[kMaxLevels], dy[kMaxLevels], cd[kMaxLevels];
+  for (int l = 0; l < s->L; ++l) {
+    im[l] = img(s->d_int[l], C >> l, R >> l, 1);
+    sv[l] = img(s->d_int_last[l], C >> l, R >> l, 1);
+    dx[l] = img(s->d_dx[l], C >> l, R >> l, 2);
+    dy[l] = img(s->d_dy[l], C >> l, R >> l, 2);
+    cd[l] = img(s->d_cand[l], C >> l, R >> l, 1);
+  }
+  wait_inputs(s, st);
+  launch_intensity_pyramid(img(s->d_rgb, C, R, 3), im, sv, dev_field<int>(s->d_sys, offsetof(SysDev, run)), dx,
+                           dy, cd, s->L, st);
+}
+
+void rgb_levels(sf_system *s, RgbLevelArgs *rg) {
+  const int C = s->cfg.cols, R = s->cfg.rows;
+  for (int l = 0; l < s->L; ++l) {
+    const int c = C >> l, r = R >> l;
+    rg[l].inext = img(s->d_int[l], c, r, 1);
+    rg[l].ilast = img(s->d_int_last[l], c, r, 1);
+    rg[l].dx = img(s->d_dx[l], c, r, 2);
+    rg[l].dy = img(s->d_dy[l], c, r, 2);
+    rg[l].cand = img(s->d_cand[l], c, r, 1);
+    rg[l].corr = s->d_corr;
+  }
+}
+
 // Frame::FillImages depth part (Core/Frame.cc:68-92).
 void enqueue_pyramid(sf_system *s, cudaStream_t st) {
   const int C = s->cfg.cols, R = s->cfg.rows;
+  if (s->cfg.rgb_term) enqueue_intensity(s, st);
   launch_filter_depth(img(s->d_depth16, C, R, 2), img(s->d_raw, C, R, 4), img(s->d_depth[0], C, R, 4),
                       s->cfg.depth_scale, s->cfg.depth_cutoff, st);
   if (s->L >= 2) {
@@ -270,11 +327,9 @@ void enqueue_mapping(sf_system *s, const Cam *cam, const int *run, int num_detec
   mark(s, st, 3);
   launch_visibility(m, f, cam, &zmin, &zmax, run, flags, st);
   mark(s, st, 4);
-  // the frame's colour and mask, uploaded on the copy stream (captured as
-  // an external event wait in the frame graph)
-  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-  cudaStreamIsCapturing(st, &cs);
-  cudaStreamWaitEvent(st, s->ev_inputs, cs == cudaStreamCaptureStatusActive ? cudaEventWaitExternal : 0);
+  // the frame's colour and mask (already waited for by the intensity
+  // pyramid with the photometric term)
+  if (!s->cfg.rgb_term) wait_inputs(s, st);
   launch_integrate(m, depth, rgb, &nm0, &mask, num_detection, cam, true, num_detection > 0, run, st);
   if (num_detection > 0) launch_unify_neighbor(m, f, run, st);  // FuseMap.cu:1141-1160
   mark(s, st, 5);
@@ -298,9 +353,11 @@ cudaError_t enqueue_device_frame(sf_system *s, int num_detection, cudaStream_t s
   icp_levels(s, lv);
   cudaError_t e = icp_persistent_reset(w, st);
   if (e != cudaSuccess) return e;
+  RgbLevelArgs rg[kMaxLevels];
+  if (s->cfg.rgb_term) rgb_levels(s, rg);
   e = launch_icp_persistent(w, lv, s->L, s->cfg.icp_thresh, dev_field<double>(s->d_sys, offsetof(SysDev, last_pose)),
                             dev_field<int>(s->d_sys, offsetof(SysDev, state)),
-                            ctx_flags(s->ctx), st);
+                            ctx_flags(s->ctx), st, s->cfg.rgb_term ? rg : nullptr);
   if (e != cudaSuccess) return e;
   k_sys_post<<<1, 1, 0, st>>>(s->d_sys, w.ctl, s->tmpl, map_scratch(s->map)); note_launch();
   mark(s, st, 2);
@@ -327,8 +384,10 @@ int run_plain_frame(sf_system *s, int num_detection) {
   } else {
     IcpLevelArgs lv[kMaxLevels];
     icp_levels(s, lv);
+    RgbLevelArgs rg[kMaxLevels];
+    if (s->cfg.rgb_term) rgb_levels(s, rg);
     ctl_begin(s->ctl, s->last_pose);
-    double sums[29];
+    double sums[58];  // ICP, then RGB
     for (int l = s->L - 1; l >= 0 && !s->ctl.stop; --l) {
       for (int j = 0; j < lv[l].iters; ++j) {
         m3 Rc, Rci, Rl, Rli;
@@ -344,11 +403,15 @@ int run_plain_frame(sf_system *s, int num_detection) {
         };
         tofl(s->ctl.next_pose, Rc, Rci, tc);
         tofl(s->ctl.last_pose, Rl, Rli, tl);
+        const bool rgb = s->cfg.rgb_term != 0;
+        // RGBStep then ICPStep (Tracking.cc:400-447), each downloading its sums
+        if (rgb) launch_rgb_step(w, lv[l], rg[l], Rc, Rci, tc, Rl, Rli, tl, st);
         launch_icp_step(w, lv[l], Rc, tc, Rl, Rli, tl, st);
-        if (cudaMemcpyAsync(sums, w.sums, sizeof(sums), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        if (cudaMemcpyAsync(sums, w.sums, (rgb ? 58 : 29) * sizeof(double), cudaMemcpyDeviceToHost, st) !=
+                cudaSuccess ||
             cudaStreamSynchronize(st) != cudaSuccess)
           return SF_ERR_CUDA;
-        if (!ctl_step(s->ctl, sums, lv[l].min_count)) break;
+        if (!ctl_step(s->ctl, sums, lv[l].min_count, rgb ? sums + 29 : nullptr)) break;
       }
     }
     ctl_finish(s->ctl, s->cfg.icp_thresh);
@@ -457,7 +520,8 @@ int sf_system_create(sf_context *ctx, const sf_system_config *cfg, const double 
   *out = nullptr;
   if (cfg->cols <= 0 || cfg->rows <= 0 || cfg->levels < 1 || cfg->levels > kMaxLevels ||
       (cfg->cols >> (cfg->levels - 1)) < 2 || (cfg->rows >> (cfg->levels - 1)) < 2 ||
-      cfg->depth_scale <= 0 || cfg->K.fx <= 0 || cfg->K.fy <= 0)
+      cfg->depth_scale <= 0 || cfg->K.fx <= 0 || cfg->K.fy <= 0 || cfg->rgb_term < 0 || cfg->rgb_term > 1 ||
+      (cfg->rgb_term && ((size_t)cfg->cols >= 65536 || (size_t)cfg->rows >= 32768)))
     return SF_ERR_INVALID;
   sf_system *s = new (std::nothrow) sf_system();
   if (!s) return SF_ERR_INVALID;
