@@ -113,9 +113,9 @@ def make_frames(n, rank=0):
     return [syn.frame(i) for i in range(n)]
 
 
-def sys_cfg(sf, mode):
+def sys_cfg(sf, mode, rgb=0):
     return sf.system_config(cols=COLS, rows=ROWS, K=K, levels=LEVELS, iters=ITERS, min_count=MIN_COUNT,
-                            use_graph=mode, **MAP)
+                            use_graph=mode, rgb_term=rgb, **MAP)
 
 
 def use_corridor_config():
@@ -145,14 +145,14 @@ def launches(sf):
     return v.value
 
 
-def time_device_resident(sf, ctx, frames, steps, warmup, mode, barrier, timing=False, autotune=False):
+def time_device_resident(sf, ctx, frames, steps, warmup, mode, barrier, timing=False, autotune=False, rgb=0):
     """Frames/s with inputs already in HBM; CUDA events on the system stream.
     With autotune, sf_system_autotune runs half-way through the warm-up
     (its choice is recaptured in the graph before the timed frames)."""
     import torch
     dev = [(torch.from_numpy(d).cuda(), torch.from_numpy(c).cuda()) for d, c, _, _ in frames[:steps + warmup]]
     torch.cuda.synchronize()
-    s = sf.System(ctx, sys_cfg(sf, mode), init_pose=frames[0][3])
+    s = sf.System(ctx, sys_cfg(sf, mode, rgb), init_pose=frames[0][3])
     stage_ms = np.zeros(len(STAGES))
     stats = []
     if timing:
@@ -200,10 +200,10 @@ def pinned(a):
     return torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
 
 
-def time_e2e(sf, ctx, frames, steps, warmup, mode):
+def time_e2e(sf, ctx, frames, steps, warmup, mode, rgb=0):
     """Frames/s through sf_system_grab with host buffers in pinned memory
     (the H2D copies of each frame and the D2H of its stats inside)."""
-    s = sf.System(ctx, sys_cfg(sf, mode), init_pose=frames[0][3])
+    s = sf.System(ctx, sys_cfg(sf, mode, rgb), init_pose=frames[0][3])
     host = [(pinned(d), pinned(c)) for d, c, _, _ in frames[:warmup + steps]]
     for i in range(warmup):
         s.grab(*host[i])
@@ -330,10 +330,11 @@ def algorithmic_bytes(stats_list):
     return integ.mean(), ray.mean(), V.mean()
 
 
-def time_reference_cuda(frames, steps, warmup):
+def time_reference_cuda(frames, steps, warmup, rgb_term=False):
     """The reference's own CUDA launchers (oracle/_ref/gpu_c2/librefgpu.so,
     built by oracle/ref_shim/build_ref_gpu.py) in System::GrabImage's order,
-    ICP-only, host buffers in: frames/s over `steps` frames after `warmup`."""
+    ICP-only (or with the photometric term, the reference's default, when
+    rgb_term), host buffers in: frames/s over `steps` frames after `warmup`."""
     import ctypes as C
     lib_path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "oracle", "_ref", "gpu_c2", "librefgpu.so")
     if not os.path.exists(lib_path):
@@ -354,6 +355,12 @@ def time_reference_cuda(frames, steps, warmup):
     h = L.refgpu_create(COLS, ROWS, K4, 1000.0, 3.0, init.ctypes.data_as(C.POINTER(C.c_double)))
     if not h:
         return {"unavailable": "refgpu_create failed"}
+    if rgb_term:
+        if not hasattr(L, "refgpu_set_rgb"):
+            L.refgpu_destroy(h)
+            return {"unavailable": "the reference's CUDA build predates its photometric mode"}
+        L.refgpu_set_rgb.argtypes = [C.c_void_p, C.c_int]
+        L.refgpu_set_rgb(h, 1)
     pose = np.zeros(16, np.float64)
     n = min(len(frames), steps + warmup)
     tracked = 0
@@ -371,8 +378,9 @@ def time_reference_cuda(frames, steps, warmup):
     timed = n - warmup
     return {"value": round(timed / dt, 3), "unit": "frames/s", "steps": timed, "warmup": warmup,
             "tracked_frames": int(tracked), "max_translation_error_vs_ground_truth_m": round(err, 5),
-            "kind": "reference CUDA build (Tracking/*.cu, Mapping/*.cu for sm_103a), ICP-only ComputeSE3, "
-                    "host buffers in, the reference's per-launch synchronisation"}
+            "kind": "reference CUDA build (Tracking/*.cu, Mapping/*.cu for sm_103a), %s ComputeSE3, "
+                    "host buffers in, the reference's per-launch synchronisation"
+                    % ("RGB-D (icpOnly = false: RGBStep + ICPStep)" if rgb_term else "ICP-only")}
 
 
 def run_reference(args):
@@ -394,6 +402,9 @@ def run_reference(args):
                                        "the reference's own kernels)" % (n - 1)},
             "e2e": {"value": round(fps, 4), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     line["reference_cuda"] = time_reference_cuda(frames, min(args.steps, len(frames) - args.warmup), args.warmup)
+    if args.config == "c2":
+        line["reference_cuda_rgbd"] = time_reference_cuda(frames, min(args.steps, len(frames) - args.warmup),
+                                                          args.warmup, rgb_term=True)
     print(json.dumps(line), flush=True)
 
 
@@ -496,6 +507,18 @@ def main():
     out["e2e"] = {"value": round(args.steps / e2e_t, 3), "unit": "frames/s",
                   "h2d_bytes_per_step": COLS * ROWS * (2 + 3), "d2h_bytes_per_step": 208,
                   "tracked_frames": int(tracked)}
+    if args.config == "c2":
+        # the reference's default tracking mode: ComputeSE3(icpOnly = false)
+        r = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 1, barrier, rgb=1)
+        re2e, rtracked = time_e2e(sf, ctx, frames, args.steps, args.warmup, 1, rgb=1)
+        out["rgbd"] = {"value": round(args.steps / r["elapsed"], 3), "unit": "frames/s",
+                       "e2e": round(args.steps / re2e, 3), "tracked_frames": int(rtracked),
+                       "gpu_launches": int(r["launches"]),
+                       "mode": "ComputeSE3 with icpOnly = false (the reference's default): RGBStep beside ICPStep "
+                               "in every iteration, same frames"}
+        if not args.no_plain:
+            rp = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 0, barrier, rgb=1)
+            out["rgbd"]["plain"] = round(args.steps / rp["elapsed"], 3)
     out["pose_err_fp64_max"] = pose_error_fp64(sf, ctx, frames, 6)
     if args.config == "c2":
         out["reloc"] = time_reloc(sf, ctx, frames)

@@ -9,9 +9,10 @@
 //                          :65-173, 369-517) and SwapFrame on success
 //   Mapping::FuseColor, Mapping::RayTrace (Mapping/Mapping.cc:76-161) on
 //                          the last frame.
-// ComputeSE3 runs ICP-only (its icpOnly = true path): the reference's
-// default adds the photometric term, which this loop does not have.  The
-// host 6x6 solve, SE(3) update, divergence guard and acceptance gate are
+// ComputeSE3 runs ICP-only (its icpOnly = true path), or, after
+// refgpu_set_rgb(h, 1), with the photometric term (icpOnly = false, the
+// reference's default): the reference's RGBStep before ICPStep in every
+// iteration and the combined solve.  The host 6x6 solve, SE(3) update, divergence guard and acceptance gate are
 // semantic_icpslam_gb300/csrc/sf_solve.h's FP64 restatement of Eigen LDLT and
 // Sophus (the reference's Eigen/Sophus/OpenCV host code cannot be built
 // here).  Keypoints, keyframes and the viewer are not part of the loop.
@@ -93,6 +94,9 @@ struct RefSystem {
   // Tracker scratch (Tracking.cc:36-41)
   DeviceArray2D<float> sumSE3;
   DeviceArray<float> outSE3;
+  DeviceArray2D<int> sumRes;
+  DeviceArray<int> outRes;
+  int rgb = 0;
 
   DeviceMap dmap() const {  // Mapping::operator DeviceMap (Mapping.cc:363-377)
     DeviceMap m;
@@ -109,23 +113,35 @@ struct RefSystem {
 
   Intrinsics K(int level) const { return Intrinsics(fx, fy, cx, cy)(level); }
 
-  // Tracker::ComputeSE3(icpOnly = true) with the FP64 solve of sf_solve.h
+  // CreateMatrix<6,7>'s 27 sums (Reduction.cu:6-16) back from A, b, and
+  // the residual pair
+  static void to_sums(const double *A, const double *b, const float *residual, double *sums) {
+    int k = 0;
+    for (int r = 0; r < 6; ++r)
+      for (int q = r; q < 7; ++q) sums[k++] = q == 6 ? b[r] : A[r * 6 + q];
+    sums[27] = residual[0];
+    sums[28] = residual[1];
+  }
+
+  // Tracker::ComputeSE3(icpOnly = !rgb) with the FP64 solve of sf_solve.h
   bool compute_se3() {
     sf::TrackCtl c;
     sf::ctl_begin(c, last->pose);
-    float residual[2];
-    double A[36], b[6], sums[29];
+    float residual[2], rres[2];
+    double A[36], b[6], sums[29], rsums[29];
     for (int i = kLevels - 1; i >= 0; --i) {
       for (int j = 0; j < kIters[i]; ++j) {
+        if (rgb) {
+          RGBStep(next->image[i], last->image[i], next->vmap[i], last->vmap[i], next->dIdx[i], next->dIdy[i],
+                  rot(c.next_pose), rot_inv(c.next_pose), rot(last->pose), rot_inv(last->pose),
+                  trans(c.next_pose), trans(last->pose), K(i), sumSE3, outSE3, sumRes, outRes, rres, A, b);
+          to_sums(A, b, rres, rsums);
+        }
         ICPStep(next->vmap[i], last->vmap[i], next->nmap[i], last->nmap[i], rot(c.next_pose),
                 trans(c.next_pose), rot(last->pose), rot_inv(last->pose), trans(last->pose), K(i), sumSE3,
                 outSE3, residual, A, b);
-        int k = 0;  // back to CreateMatrix<6,7>'s 27 sums (Reduction.cu:6-16)
-        for (int r = 0; r < 6; ++r)
-          for (int q = r; q < 7; ++q) sums[k++] = q == 6 ? b[r] : A[r * 6 + q];
-        sums[27] = residual[0];
-        sums[28] = residual[1];
-        if (!sf::ctl_step(c, sums, kMinCount[i])) break;
+        to_sums(A, b, residual, sums);
+        if (!sf::ctl_step(c, sums, kMinCount[i], rgb ? rsums : nullptr)) break;
       }
       if (c.stop) break;
     }
@@ -163,6 +179,8 @@ extern "C" void *refgpu_create(int cols, int rows, const float *K, float depth_s
   s->labels.create(1);
   s->sumSE3.create(29, 96);
   s->outSE3.create(29);
+  s->sumRes.create(2, 96);
+  s->outRes.create(2);
   ResetMap(s->dmap());  // Mapping::Reset
   return s;
 }
@@ -219,3 +237,5 @@ extern "C" int refgpu_grab(void *h, const uint16_t *depth, const uint8_t *rgb, d
 }
 
 extern "C" void refgpu_destroy(void *h) { delete static_cast<RefSystem *>(h); }
+
+extern "C" void refgpu_set_rgb(void *h, int on) { static_cast<RefSystem *>(h)->rgb = on != 0; }
