@@ -297,6 +297,15 @@ int sf_AnalyzeMapSemantics(sf_context *ctx, sf_map *map, sf_image depth,
  * neighbour reads).  The first call allocates 4 bytes per voxel of the
  * block pool as the pass's output buffer. */
 int sf_UnifyNeighbor(sf_context *ctx, sf_map *map);
+/* Mapping::SemanticAnalysis(const Frame *) (Mapping/Mapping.cc:99-123), the
+ * localisation mode's label pass (System.cc:206-212): AnalyzeMapSemantics
+ * on the rendered depth, the z channel of the raycast vertex map `vmap`,
+ * with the raycast normals `nmap`. */
+int sf_SemanticAnalysis(sf_context *ctx, sf_map *map, sf_image vmap,
+                        sf_image color, sf_image nmap, sf_image mask,
+                        int num_detection, sf_mat3 Rview, sf_mat3 RviewInv,
+                        sf_float3 tview, float fx, float fy, float cx,
+                        float cy);
 
 /* -------------------------------------------------------------- raycast */
 /* CreateRenderingBlocks (RenderScene.h:20; RenderScene.cu:210-289).
@@ -432,6 +441,12 @@ typedef struct {
   int minb[16], tile_x[16], tile_y[16];
 } sf_autotune_report;
 int sf_system_autotune(sf_system *sys, int reps, sf_autotune_report *report);
+/* Tracker::mappingDisabled (Tracking.h:51, toggled by the viewer,
+ * GUI/Viewer.cc:151-156): enabled = 0 switches the loop to localisation,
+ * UpdateVisibility and RayTrace instead of FuseColor, and with detections
+ * the rendered-depth label pass of sf_SemanticAnalysis (System.cc:161-212);
+ * 1 switches back.  Takes effect on the next frame. */
+int sf_system_set_mapping(sf_system *sys, int enabled);
 
 int sf_system_set_timing(sf_system *sys, int enable);
 int sf_system_stage_ms(sf_system *sys, float ms[7]);

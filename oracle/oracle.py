@@ -95,6 +95,7 @@ def lib():
                 "sfo_system_destroy": (None, [vp]),
                 "sfo_system_grab": (C.c_int, [vp, U16P, U8P, U8P, C.c_int, F64P, F64P]),
                 "sfo_system_set_rgb": (None, [vp, C.c_int]),
+                "sfo_system_set_mapping": (None, [vp, C.c_int]),
                 "sfo_system_map": (vp, [vp]),
                 "sfo_system_vmap": (vp, [vp, C.c_int]),
                 "sfo_system_nmap": (vp, [vp, C.c_int]),
@@ -462,6 +463,10 @@ class System:
         if getattr(self, "h", None):
             lib().sfo_system_destroy(self.h)
             self.h = None
+
+    def set_mapping(self, enabled):
+        """Tracker::mappingDisabled = not enabled (localisation mode)."""
+        lib().sfo_system_set_mapping(self.h, int(bool(enabled)))
 
     def grab(self, depth_u16, rgb, mask=None, num_detection=0):
         d = np.ascontiguousarray(depth_u16, np.uint16)

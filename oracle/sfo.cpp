@@ -1834,6 +1834,7 @@ struct sfo_system {
   sfo_frame *next = &fa, *last = &fb;
   int state = 1;  // 1 = init, 0 = tracking (Tracking.cc:65-119)
   int rgb = 0;    // 1: ComputeSE3(icpOnly = false), the reference's default
+  int mapping = 1;  // 0: localisation mode (Tracker::mappingDisabled)
   double init_pose[16];
   std::vector<float> zmin, zmax;
   int zc, zr;
@@ -1902,14 +1903,17 @@ extern "C" sfo_system *sfo_system_create(const sfo_config *cfg, int cols, int ro
 }
 extern "C" void sfo_system_destroy(sfo_system *s) { sfo_map_destroy(s->map); delete s; }
 extern "C" void sfo_system_set_rgb(sfo_system *s, int on) { s->rgb = on != 0; }
+extern "C" void sfo_system_set_mapping(sfo_system *s, int on) { s->mapping = on != 0; }
 extern "C" sfo_map *sfo_system_map(sfo_system *s) { return s->map; }
 extern "C" const float *sfo_system_vmap(sfo_system *s, int l) { return s->last->vmap[l].data(); }
 extern "C" const float *sfo_system_nmap(sfo_system *s, int l) { return s->last->nmap[l].data(); }
 
 // System::GrabImage (Core/System.cc:131-270) with Tracker::GrabFrame /
-// Track / TrackFrame (Tracking.cc:65-173,246-280): icp-only tracking, no
-// keyframes / SURF / relocalisation (a lost frame is skipped and the next
-// frame is tracked against the same model).
+// Track / TrackFrame (Tracking.cc:65-173,246-280): icp-only tracking (or
+// the photometric term, sfo_system_set_rgb), no keyframes / SURF /
+// relocalisation (a lost frame is skipped and the next frame is tracked
+// against the same model).  num_detection > 0 stands for the semantic
+// mode's detections of this frame (gap_semantic = 1).
 extern "C" int sfo_system_grab(sfo_system *s, const uint16_t *depth, const uint8_t *rgb,
                                const uint8_t *mask, int num_detection, double *pose_out,
                                double *stats) {
@@ -1946,17 +1950,48 @@ extern "C" int sfo_system_grab(sfo_system *s, const uint16_t *depth, const uint8
     sfo_frame &f = *s->last;
     float R[9], RI[9], t[3];
     pose_to_gpu(f.pose, R, RI, t);
-    nvis = sfo_fuse(s->map, f.raw.data(), rgb, f.nmap[0].data(), mask, num_detection, s->cols,
-                    s->rows, R, RI, t, s->K[0], s->K[1], s->K[2], s->K[3], 1);
     // Mapping::RayTrace (Mapping.cc:142-161): raycast only if the z-range
     // pass produced rendering blocks; else vmap[0]/nmap[0] keep the
     // measured maps.
-    if (sfo_zrange(s->map, s->zmin.data(), s->zmax.data(), s->zc, s->zr, s->map->c.depth_max,
-                   s->map->c.depth_min, RI, t, s->K[0], s->K[1], s->K[2], s->K[3], nullptr, 0,
-                   nullptr)) {
-      sfo_raycast(s->map, f.vmap[0].data(), f.nmap[0].data(), s->cols, s->rows, s->zmin.data(),
-                  s->zmax.data(), s->zc, s->zr, R, RI, t, (float)(1.0 / (double)s->K[0]),
-                  (float)(1.0 / (double)s->K[1]), s->K[2], s->K[3]);
+    auto raytrace = [&]() {
+      if (sfo_zrange(s->map, s->zmin.data(), s->zmax.data(), s->zc, s->zr, s->map->c.depth_max,
+                     s->map->c.depth_min, RI, t, s->K[0], s->K[1], s->K[2], s->K[3], nullptr, 0, nullptr)) {
+        sfo_raycast(s->map, f.vmap[0].data(), f.nmap[0].data(), s->cols, s->rows, s->zmin.data(),
+                    s->zmax.data(), s->zc, s->zr, R, RI, t, (float)(1.0 / (double)s->K[0]),
+                    (float)(1.0 / (double)s->K[1]), s->K[2], s->K[3]);
+      }
+    };
+    if (s->mapping) {
+      // FuseColor on the frame as grabbed (Frame::FillImages leaves
+      // numDetection 0, Core/Frame.cc:86-91), RayTrace (System.cc:163-168)
+      nvis = sfo_fuse(s->map, f.raw.data(), rgb, f.nmap[0].data(), mask, 0, s->cols, s->rows, R, RI, t,
+                      s->K[0], s->K[1], s->K[2], s->K[3], 1);
+      raytrace();
+      if (num_detection > 0) {
+        // with detections, FuseColor again with the labels (its label pass
+        // reading the raycast normals now in nmap[0]) and RayTrace
+        // (System.cc:184-205)
+        nvis = sfo_fuse(s->map, f.raw.data(), rgb, f.nmap[0].data(), mask, num_detection, s->cols, s->rows,
+                        R, RI, t, s->K[0], s->K[1], s->K[2], s->K[3], 1);
+        raytrace();
+      }
+    } else {
+      // localisation: UpdateVisibility + RayTrace (System.cc:169-172)
+      nvis = sfo_visibility(s->map, R, RI, t, s->cols, s->rows, s->K[0], s->K[1], s->K[2], s->K[3],
+                            s->map->c.depth_max, s->map->c.depth_min);
+      raytrace();
+      if (num_detection > 0) {
+        // Mapping::SemanticAnalysis(f) (Mapping.cc:99-123, System.cc:206-212):
+        // AnalyzeMapSemantics on the rendered depth, vmap[0].z
+        std::vector<float> rdepth((size_t)s->cols * s->rows);
+        for (size_t i = 0; i < rdepth.size(); ++i) rdepth[i] = f.vmap[0][4 * i + 2];
+        if (sfo_visibility(s->map, R, RI, t, s->cols, s->rows, s->K[0], s->K[1], s->K[2], s->K[3],
+                           s->map->c.depth_max, s->map->c.depth_min) > 0) {
+          sfo_semantics(s->map, rdepth.data(), rgb, f.nmap[0].data(), mask, num_detection, s->cols, s->rows, RI, t,
+                        s->K[0], s->K[1], s->K[2], s->K[3], s->map->c.depth_max, s->map->c.depth_min);
+          sfo_unify_neighbor(s->map);
+        }
+      }
     }
   }
   if (pose_out) memcpy(pose_out, s->last->pose, sizeof(s->last->pose));

@@ -162,6 +162,10 @@ void sfo_system_destroy(sfo_system *s);
 // on != 0: track with the photometric term (ComputeSE3(icpOnly = false),
 // the reference's default, Tracking.cc:170).
 void sfo_system_set_rgb(sfo_system *s, int on);
+// on == 0: localisation mode (Tracker::mappingDisabled): UpdateVisibility
+// and RayTrace instead of FuseColor, labels by AnalyzeMapSemantics on the
+// rendered depth (System.cc:161-212).
+void sfo_system_set_mapping(sfo_system *s, int on);
 // Returns the tracking result (1 tracked / 0 lost); pose_out = the frame's
 // pose after tracking; stats[8] = {icpError, count, iters, fail, visible,
 // heapCounter, entryPtr, allocated}, with the photometric term

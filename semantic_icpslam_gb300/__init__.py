@@ -177,6 +177,11 @@ class System:
         cands = [(rep.minb[i], rep.tile_x[i], rep.tile_y[i], rep.ms[i]) for i in range(rep.candidates)]
         return cands, rep.chosen
 
+    def set_mapping(self, enabled):
+        """sf_system_set_mapping: False switches to localisation
+        (Tracker::mappingDisabled), True back to mapping."""
+        call("sf_system_set_mapping", self.h, int(bool(enabled)))
+
     def stats(self):
         st = FrameStats()
         call("sf_system_stats", self.h, C.byref(st))

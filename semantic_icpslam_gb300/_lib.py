@@ -142,6 +142,7 @@ SIGNATURES = {
     "sf_AnalyzeMapSemantics": [vp, vp, Image, Image, Image, Image, C.c_int, Mat3, Mat3, Float3]
                               + [C.c_float] * 6,
     "sf_UnifyNeighbor": [vp, vp],
+    "sf_SemanticAnalysis": [vp, vp, Image, Image, Image, Image, C.c_int, Mat3, Mat3, Float3] + [C.c_float] * 4,
     "sf_CreateRenderingBlocks": [vp, vp, Image, Image, C.c_float, C.c_float, vp, vp, Mat3, Float3, C.c_uint32]
                                 + [C.c_float] * 4 + [I32P],
     "sf_Raycast": [vp, vp, Image, Image, Image, Image, Mat3, Mat3, Float3] + [C.c_float] * 4,
@@ -155,6 +156,7 @@ SIGNATURES = {
     "sf_system_get_map": [vp, pvp],
     "sf_system_set_timing": [vp, C.c_int],
     "sf_system_autotune": [vp, C.c_int, C.POINTER(AutotuneReport)],
+    "sf_system_set_mapping": [vp, C.c_int],
     "sf_system_stage_ms": [vp, F32P],
     "sf_system_pose_device": [vp, C.POINTER(C.POINTER(C.c_double))],
     "sf_synth_create": [C.POINTER(SynthConfig), pvp],

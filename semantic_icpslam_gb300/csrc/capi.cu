@@ -34,6 +34,8 @@ struct sf_context {
   float *adj_part = nullptr;              // device [adj_cap][6] pose partials
   double *adj_pose = nullptr;             // device [6]
   int adj_cap = 0;
+  float *rdepth = nullptr;                // device rendered depth (sf_SemanticAnalysis)
+  size_t rdepth_px = 0;
 };
 
 struct sf_map {
@@ -143,6 +145,7 @@ int sf_context_destroy(sf_context *ctx) {
   cudaFree(ctx->reloc_scores);
   cudaFree(ctx->adj_part);
   cudaFree(ctx->adj_pose);
+  cudaFree(ctx->rdepth);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return SF_OK;
@@ -812,6 +815,27 @@ int sf_AnalyzeMapSemantics(sf_context *ctx, sf_map *m, sf_image depth, sf_image 
   SF_CHECK(cudaGetLastError());
   SF_CHECK(cudaStreamSynchronize(ctx->stream));
   return SF_OK;
+}
+
+int sf_SemanticAnalysis(sf_context *ctx, sf_map *m, sf_image vmap, sf_image color, sf_image nmap, sf_image mask,
+                        int num_detection, sf_mat3 Rview, sf_mat3 RviewInv, sf_float3 tview, float fx, float fy,
+                        float cx, float cy) {
+  if (!ctx || !m || !img_ok(vmap, 16) || !img_ok(color, 3) || !img_ok(nmap, 16)) return SF_ERR_INVALID;
+  const size_t px = (size_t)vmap.cols * vmap.rows;
+  if (px > ctx->rdepth_px) {
+    SF_CHECK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(ctx->rdepth);
+    ctx->rdepth = nullptr;
+    ctx->rdepth_px = 0;
+    SF_CHECK(cudaMalloc(&ctx->rdepth, px * sizeof(float)));
+    ctx->rdepth_px = px;
+  }
+  sf_image rd;
+  rd.data = ctx->rdepth; rd.step = (size_t)vmap.cols * sizeof(float); rd.cols = vmap.cols; rd.rows = vmap.rows;
+  launch_vmap_depth(vmap, rd, nullptr, ctx->stream);
+  SF_CHECK(cudaGetLastError());
+  return sf_AnalyzeMapSemantics(ctx, m, rd, color, nmap, mask, num_detection, Rview, RviewInv, tview, fx, fy, cx,
+                                cy, m->cfg.depth_max, m->cfg.depth_min);
 }
 
 int sf_UnifyNeighbor(sf_context *ctx, sf_map *m) {

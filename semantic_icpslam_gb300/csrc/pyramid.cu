@@ -373,6 +373,16 @@ __global__ void k_resize(sf_image vsrc, sf_image nsrc, sf_image vdst, sf_image n
 }
 
 // ------------------------------------------------------------- launchers
+// Mapping::SemanticAnalysis' rendered depth (Mapping.cc:99-111): the z of
+// the raycast vertex map, NaN where the ray found no surface.
+__global__ void k_vmap_depth(sf_image vmap, sf_image depth, const int *run_flag) {
+  if (run_flag && *run_flag == 0) return;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= depth.cols || y >= depth.rows) return;
+  row_ptr<float>(depth, y)[x] = row_ptr<const float4>(vmap, y)[x].z;
+}
+
 static inline dim3 grid2d(int cols, int rows, dim3 blk) {
   return dim3((cols + blk.x - 1) / blk.x, (rows + blk.y - 1) / blk.y);
 }
@@ -439,6 +449,11 @@ void launch_vmap(const sf_image &depth, const sf_image &vmap, float fx, float fy
 void launch_nmap(const sf_image &vmap, const sf_image &nmap, cudaStream_t s) {
   dim3 blk(32, 8);
   k_nmap<<<grid2d(vmap.cols, vmap.rows, blk), blk, 0, s>>>(vmap, nmap); note_launch();
+}
+
+void launch_vmap_depth(const sf_image &vmap, const sf_image &depth, const int *run_flag, cudaStream_t s) {
+  dim3 blk(32, 8);
+  k_vmap_depth<<<grid2d(depth.cols, depth.rows, blk), blk, 0, s>>>(vmap, depth, run_flag); note_launch();
 }
 
 void launch_resize(const sf_image &vsrc, const sf_image &nsrc, const sf_image &vdst,

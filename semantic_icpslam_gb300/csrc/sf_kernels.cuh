@@ -18,6 +18,8 @@ void launch_vnmap(const sf_image &depth, const sf_image &vmap, const sf_image &n
 void launch_vmap(const sf_image &depth, const sf_image &vmap, float fx, float fy, float cx,
                  float cy, float cutoff, cudaStream_t s);
 void launch_nmap(const sf_image &vmap, const sf_image &nmap, cudaStream_t s);
+// The z channel of a vertex map as a depth image (rendered depth).
+void launch_vmap_depth(const sf_image &vmap, const sf_image &depth, const int *run_flag, cudaStream_t s);
 void launch_resize(const sf_image &vsrc, const sf_image &nsrc, const sf_image &vdst,
                    const sf_image &ndst, cudaStream_t s);
 

@@ -137,6 +137,8 @@ struct sf_system {
   uint8_t *d_int[kMaxLevels] = {}, *d_int_last[kMaxLevels] = {}, *d_cand[kMaxLevels] = {};
   int16_t *d_dx[kMaxLevels] = {}, *d_dy[kMaxLevels] = {};
   int2 *d_corr = nullptr;  // per-iteration correspondences (level-0 size)
+  float *d_rdepth = nullptr;  // rendered depth (localisation mode's label pass)
+  int mapping = 1;            // 0: localisation mode (Tracker::mappingDisabled)
   float *d_zmin = nullptr, *d_zmax = nullptr;
   SysDev *d_sys = nullptr;
   sf_frame_stats *d_stats = nullptr;
@@ -152,6 +154,7 @@ struct sf_system {
   // graph
   cudaGraphExec_t gexec = nullptr;
   int graph_sem = -1;  // semantics flag the graph was captured with
+  int graph_mapping = -1;  // mapping flag the graph was captured with
   unsigned long long graph_kernels = 0;  // kernel launches recorded in the graph
   int num_detection_captured = 0;
   // stage timing (eager form only): events at the stage boundaries
@@ -179,7 +182,7 @@ int alloc_all(sf_system *s) {
   const size_t np = (size_t)C * R;
   auto A = [&](void **p, size_t bytes) { return cudaMalloc(p, bytes) == cudaSuccess; };
   bool ok = A((void **)&s->d_depth16, np * 2) && A((void **)&s->d_rgb, np * 3) &&
-            A((void **)&s->d_mask, np) && A((void **)&s->d_raw, np * 4) &&
+            A((void **)&s->d_mask, np) && A((void **)&s->d_raw, np * 4) && A((void **)&s->d_rdepth, np * 4) &&
             A((void **)&s->d_zmin, (size_t)s->zc * s->zr * 4) &&
             A((void **)&s->d_zmax, (size_t)s->zc * s->zr * 4) &&
             A((void **)&s->d_sys, sizeof(SysDev)) && A((void **)&s->d_stats, sizeof(sf_frame_stats));
@@ -206,7 +209,7 @@ int alloc_all(sf_system *s) {
 }
 
 void free_all(sf_system *s) {
-  cudaFree(s->d_depth16); cudaFree(s->d_rgb); cudaFree(s->d_mask); cudaFree(s->d_raw);
+  cudaFree(s->d_depth16); cudaFree(s->d_rgb); cudaFree(s->d_mask); cudaFree(s->d_raw); cudaFree(s->d_rdepth);
   cudaFree(s->d_zmin); cudaFree(s->d_zmax); cudaFree(s->d_sys); cudaFree(s->d_stats); cudaFree(s->d_corr);
   for (int l = 0; l < kMaxLevels; ++l) {
     cudaFree(s->d_depth[l]); cudaFree(s->d_vmap[l]); cudaFree(s->d_nmap[l]);
@@ -312,35 +315,93 @@ void icp_levels(sf_system *s, IcpLevelArgs *lv) {
   }
 }
 
-// Mapping::FuseColor + Mapping::RayTrace and the next frame's
-// Frame::ResizeImages, every launch gated by `run` (device) when given.
-void enqueue_mapping(sf_system *s, const Cam *cam, const int *run, int num_detection,
-                     cudaStream_t st) {
+// Mapping::FuseColor (FuseMapColor) and Mapping::RayTrace of the frame's
+// mapping stage.  `first` marks the stage boundaries and joins the colour
+// upload; `plain` downloads the visible count and skips the integration
+// when it is zero, as FuseMapColor does (FuseMap.cu:1116-1120).
+int fuse_and_raytrace(sf_system *s, const Cam *cam, const int *run, int num_detection, const sf_image &nmap,
+                      bool first, bool plain, cudaStream_t st) {
   const int C = s->cfg.cols, R = s->cfg.rows;
   DevMap &m = map_dev(s->map);
   FuseScratch &f = map_scratch(s->map);
   uint32_t *flags = ctx_flags(s->ctx);
-  sf_image depth = img(s->d_raw, C, R, 4), rgb = img(s->d_rgb, C, R, 3);
-  sf_image nm0 = img(s->d_nmap[0], C, R, 16), mask = img(s->d_mask, C, R, 1);
+  sf_image depth = img(s->d_raw, C, R, 4), rgb = img(s->d_rgb, C, R, 3), mask = img(s->d_mask, C, R, 1);
   sf_image zmin = img(s->d_zmin, s->zc, s->zr, 4), zmax = img(s->d_zmax, s->zc, s->zr, 4);
-  launch_alloc(m, f, depth, cam, run, flags, st, /*begin=*/run == nullptr);
-  mark(s, st, 3);
+  // the first pass of a device-driven frame starts its allocation epoch in
+  // k_sys_post
+  launch_alloc(m, f, depth, cam, run, flags, st, /*begin=*/!first || run == nullptr);
+  if (first) mark(s, st, 3);
   launch_visibility(m, f, cam, &zmin, &zmax, run, flags, st);
-  mark(s, st, 4);
-  // the frame's colour and mask (already waited for by the intensity
-  // pyramid with the photometric term)
-  if (!s->cfg.rgb_term) wait_inputs(s, st);
-  launch_integrate(m, depth, rgb, &nm0, &mask, num_detection, cam, true, num_detection > 0, run, st);
-  if (num_detection > 0) launch_unify_neighbor(m, f, run, st);  // FuseMap.cu:1141-1160
-  mark(s, st, 5);
+  if (first) {
+    mark(s, st, 4);
+    // the frame's colour and mask (already waited for by the intensity
+    // pyramid with the photometric term)
+    if (!s->cfg.rgb_term) wait_inputs(s, st);
+  }
+  bool integrate = true;
+  if (plain) {
+    uint32_t nvis = 0;
+    if (cudaMemcpyAsync(&nvis, m.no_visible, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return SF_ERR_CUDA;
+    integrate = nvis > 0;
+  }
+  if (integrate) {
+    launch_integrate(m, depth, rgb, &nmap, &mask, num_detection, cam, true, num_detection > 0, run, st);
+    if (num_detection > 0) launch_unify_neighbor(m, f, run, st);  // FuseMap.cu:1141-1160
+  }
+  if (first) mark(s, st, 5);
   sf_image fv = img(s->d_vmap[0], C, R, 16), fn = img(s->d_nmap[0], C, R, 16);
   launch_raycast(m, f, img(s->d_mv[0], C, R, 16), img(s->d_mn[0], C, R, 16), zmin, zmax, cam,
                  f.counters + 3, &fv, &fn, run, st, s->rc_tune);
-  mark(s, st, 6);
+  if (first) mark(s, st, 6);
+  return SF_OK;
+}
+
+// The mapping stage of System::GrabImage (Core/System.cc:161-212) and the
+// next frame's Frame::ResizeImages, every launch gated by `run` (device)
+// when given.  Mapping: FuseColor + RayTrace; with detections (the
+// semantic mode, gap_semantic = 1) FuseColor again with the labels, its
+// label pass reading the raycast normals, and RayTrace.  Localisation
+// (mapping disabled): UpdateVisibility + RayTrace; with detections
+// Mapping::SemanticAnalysis: AnalyzeMapSemantics on the rendered depth
+// (vmap[0].z, Mapping.cc:99-123).
+int enqueue_mapping(sf_system *s, const Cam *cam, const int *run, int num_detection, bool plain,
+                    cudaStream_t st) {
+  const int C = s->cfg.cols, R = s->cfg.rows;
+  DevMap &m = map_dev(s->map);
+  FuseScratch &f = map_scratch(s->map);
+  uint32_t *flags = ctx_flags(s->ctx);
+  const sf_image mn0 = img(s->d_mn[0], C, R, 16);
+  int e = SF_OK;
+  if (s->mapping) {
+    e = fuse_and_raytrace(s, cam, run, 0, img(s->d_nmap[0], C, R, 16), true, plain, st);
+    if (e == SF_OK && num_detection > 0) e = fuse_and_raytrace(s, cam, run, num_detection, mn0, false, plain, st);
+  } else {
+    sf_image zmin = img(s->d_zmin, s->zc, s->zr, 4), zmax = img(s->d_zmax, s->zc, s->zr, 4);
+    mark(s, st, 3);
+    launch_visibility(m, f, cam, &zmin, &zmax, run, flags, st);
+    mark(s, st, 4);
+    if (!s->cfg.rgb_term) wait_inputs(s, st);
+    mark(s, st, 5);
+    sf_image fv = img(s->d_vmap[0], C, R, 16), fn = img(s->d_nmap[0], C, R, 16);
+    launch_raycast(m, f, img(s->d_mv[0], C, R, 16), mn0, zmin, zmax, cam, f.counters + 3, &fv, &fn, run, st,
+                   s->rc_tune);
+    mark(s, st, 6);
+    if (num_detection > 0) {
+      const sf_image rd = img(s->d_rdepth, C, R, 4), rgb = img(s->d_rgb, C, R, 3), mask = img(s->d_mask, C, R, 1);
+      launch_vmap_depth(img(s->d_mv[0], C, R, 16), rd, run, st);
+      launch_visibility(m, f, cam, nullptr, nullptr, run, flags, st);
+      launch_integrate(m, rd, rgb, &mn0, &mask, num_detection, cam, false, true, run, st);
+      launch_unify_neighbor(m, f, run, st);
+    }
+  }
+  if (e != SF_OK) return e;
   for (int l = 1; l < s->L; ++l)
     launch_resize(img(s->d_mv[l - 1], C >> (l - 1), R >> (l - 1), 16),
                   img(s->d_mn[l - 1], C >> (l - 1), R >> (l - 1), 16),
                   img(s->d_mv[l], C >> l, R >> l, 16), img(s->d_mn[l], C >> l, R >> l, 16), st);
+  return SF_OK;
 }
 
 // Device-driven frame (eager and graph forms).
@@ -362,7 +423,7 @@ cudaError_t enqueue_device_frame(sf_system *s, int num_detection, cudaStream_t s
   k_sys_post<<<1, 1, 0, st>>>(s->d_sys, w.ctl, s->tmpl, map_scratch(s->map)); note_launch();
   mark(s, st, 2);
   enqueue_mapping(s, dev_field<Cam>(s->d_sys, offsetof(SysDev, cam)),
-                  dev_field<int>(s->d_sys, offsetof(SysDev, run)), num_detection, st);
+                  dev_field<int>(s->d_sys, offsetof(SysDev, run)), num_detection, false, st);
   k_sys_stats<<<1, 1, 0, st>>>(s->d_sys, w.ctl, map_dev(s->map), ctx_flags(s->ctx), s->d_stats); note_launch();
   mark(s, st, 7);
   return cudaGetLastError();
@@ -440,33 +501,8 @@ int run_plain_frame(sf_system *s, int num_detection) {
   if (cudaMemcpyAsync(w.ctl, &s->ctl, sizeof(TrackCtl), cudaMemcpyHostToDevice, st) != cudaSuccess)
     return SF_ERR_CUDA;
   if (tracked) {
-    DevMap &m = map_dev(s->map);
-    FuseScratch &f = map_scratch(s->map);
-    const int C = s->cfg.cols, R = s->cfg.rows;
-    uint32_t *flags = ctx_flags(s->ctx);
-    sf_image depth = img(s->d_raw, C, R, 4), rgb = img(s->d_rgb, C, R, 3);
-    sf_image nm0 = img(s->d_nmap[0], C, R, 16), mask = img(s->d_mask, C, R, 1);
-    sf_image zmin = img(s->d_zmin, s->zc, s->zr, 4), zmax = img(s->d_zmax, s->zc, s->zr, 4);
-    const Cam *cam = dev_field<Cam>(s->d_sys, offsetof(SysDev, cam));
-    launch_alloc(m, f, depth, cam, nullptr, flags, st);
-    launch_visibility(m, f, cam, &zmin, &zmax, nullptr, flags, st);
-    uint32_t nvis = 0;  // FuseMapColor downloads the visible count (FuseMap.cu:1116)
-    if (cudaMemcpyAsync(&nvis, m.no_visible, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess)
-      return SF_ERR_CUDA;
-    if (nvis > 0) {
-      cudaStreamWaitEvent(st, s->ev_inputs, 0);
-      launch_integrate(m, depth, rgb, &nm0, &mask, num_detection, cam, true, num_detection > 0,
-                       nullptr, st);
-      if (num_detection > 0) launch_unify_neighbor(m, f, nullptr, st);
-    }
-    sf_image fv = img(s->d_vmap[0], C, R, 16), fn = img(s->d_nmap[0], C, R, 16);
-    launch_raycast(m, f, img(s->d_mv[0], C, R, 16), img(s->d_mn[0], C, R, 16), zmin, zmax, cam,
-                   f.counters + 3, &fv, &fn, nullptr, st, s->rc_tune);
-    for (int l = 1; l < s->L; ++l)
-      launch_resize(img(s->d_mv[l - 1], C >> (l - 1), R >> (l - 1), 16),
-                    img(s->d_mn[l - 1], C >> (l - 1), R >> (l - 1), 16),
-                    img(s->d_mv[l], C >> l, R >> l, 16), img(s->d_mn[l], C >> l, R >> l, 16), st);
+    int e = enqueue_mapping(s, dev_field<Cam>(s->d_sys, offsetof(SysDev, cam)), nullptr, num_detection, true, st);
+    if (e != SF_OK) return e;
   }
   k_sys_stats<<<1, 1, 0, st>>>(s->d_sys, w.ctl, map_dev(s->map), ctx_flags(s->ctx), s->d_stats); note_launch();
   return cudaGetLastError() == cudaSuccess ? SF_OK : SF_ERR_CUDA;
@@ -484,7 +520,8 @@ int run_frame(sf_system *s, int num_detection) {
     return enqueue_device_frame(s, num_detection, st) == cudaSuccess ? SF_OK : SF_ERR_CUDA;
   }
   const int sem = num_detection > 0 ? 1 : 0;
-  if (!s->gexec || s->graph_sem != sem || (sem && s->num_detection_captured != num_detection)) {
+  if (!s->gexec || s->graph_sem != sem || s->graph_mapping != s->mapping ||
+      (sem && s->num_detection_captured != num_detection)) {
     if (s->gexec) { cudaGraphExecDestroy(s->gexec); s->gexec = nullptr; }
     cudaGraph_t g = nullptr;
     const unsigned long long before = launches_total();
@@ -503,6 +540,7 @@ int run_frame(sf_system *s, int num_detection) {
     cudaGraphDestroy(g);
     if (e != cudaSuccess) { s->gexec = nullptr; return SF_ERR_CUDA; }
     s->graph_sem = sem;
+    s->graph_mapping = s->mapping;
     s->num_detection_captured = num_detection;
   }
   if (cudaGraphLaunch(s->gexec, st) != cudaSuccess) return SF_ERR_CUDA;
@@ -617,6 +655,12 @@ int sf_system_grab_device(sf_system *s, const uint16_t *depth, const uint8_t *rg
       cudaMemcpyAsync(s->d_mask, mask, np, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
     return SF_ERR_CUDA;
   return run_frame(s, num_detection);
+}
+
+int sf_system_set_mapping(sf_system *s, int enabled) {
+  if (!s || (enabled != 0 && enabled != 1)) return SF_ERR_INVALID;
+  s->mapping = enabled;  // the frame graph is captured again on the next frame
+  return SF_OK;
 }
 
 int sf_system_autotune(sf_system *s, int reps, sf_autotune_report *report) {

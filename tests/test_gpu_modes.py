@@ -1,0 +1,183 @@
+"""The two other modes of System::GrabImage's mapping stage
+(Core/System.cc:161-212) on the GPU:
+
+* localisation (Tracker::mappingDisabled): UpdateVisibility + RayTrace
+  instead of FuseColor, and with detections Mapping::SemanticAnalysis, the
+  label pass on the rendered depth (vmap[0].z, Mapping.cc:99-123);
+* the semantic mode with detections: FuseColor, RayTrace, then FuseColor
+  again with the labels (its label pass reading the raycast normals) and
+  RayTrace.
+
+sf_SemanticAnalysis is bit-exact against the oracle on the same map state;
+the loops are checked against the oracle's loop in the same mode.
+"""
+import numpy as np
+import pytest
+
+from tests.helpers import C1, MAP_C1, cuda, map_to_host, positions, sequence
+
+pytestmark = pytest.mark.gpu
+
+TRAJ_TOL = 2e-4
+POSE_TOL = 1e-6
+FLIP_TOL = 1e-4
+LOOP_TOL = 2e-3
+
+
+@pytest.fixture(scope="module")
+def lib(built):
+    import torch
+    import semantic_icpslam_gb300 as sf
+    assert torch.cuda.is_available()
+    ctx = sf.Context()
+    yield sf, ctx
+    ctx.close()
+
+
+def _load(sf, ctx, gmap, entries, voxels):
+    a = gmap.arrays()
+    entries = np.ascontiguousarray(entries)
+    voxels = np.ascontiguousarray(voxels)
+    ctx.memcpy(a.hash_entries, entries.ctypes.data, entries.nbytes)
+    ctx.memcpy(a.voxel_blocks, voxels.ctypes.data, voxels.nbytes)
+    sf.call("sf_map_rebuild_index", ctx.h, gmap.h)
+
+
+def test_semantic_analysis_rendered_depth(lib):
+    """Mapping::SemanticAnalysis on one map state, GPU vs oracle: the
+    rendered depth of the oracle's raycast, visibility, the label pass and
+    UnifyNeighbor, every voxel byte."""
+    from oracle import oracle as O
+    sf, ctx = lib
+    K = C1["K"]
+    seq = sequence(C1["cols"], C1["rows"], K, 4, trajectory=0, label_flip=0.05, n_objects=10, seed=3)
+    om = O.Map(**MAP_C1)
+    for i in range(3):
+        d, rgb, mask, P = seq[i]
+        raw, filt = O.filter_depth(d, 1000.0, 3.0)
+        om.fuse(raw, rgb, O.nmap(O.vmap(filt, *K, 3.0)), mask, 10 if i else 0, P, K)
+    d, rgb, mask, P = seq[3]
+    ok, zmin, zmax, _, _ = om.zrange(P, K, 40, 30)
+    assert ok
+    vm, nm = om.raycast(P, K, C1["cols"], C1["rows"], zmin, zmax)
+    e = om.entries.copy()
+    nvox = int(e["ptr"].max()) + 512
+    gmap = sf.Map(**MAP_C1)
+    _load(sf, ctx, gmap, e, om.voxels[:nvox].copy())
+    R, RI, t = sf.pose_to_gpu(P)
+    dv, dc, dn, dm = cuda(vm), cuda(rgb), cuda(nm), cuda(mask)  # alive through the call
+    sf.call("sf_SemanticAnalysis", ctx.h, gmap.h, sf.image(dv), sf.image(dc), sf.image(dn), sf.image(dm), 10, R, RI,
+            t, *K)
+    ctx.sync()
+    om.visibility(P, K, C1["cols"], C1["rows"])
+    om.analyze_semantics(np.ascontiguousarray(vm[..., 2]), rgb, nm, mask, 10, P, K)
+    got = ctx.download(gmap.arrays().voxel_blocks, np.uint8, nvox * 16).reshape(nvox, 16)
+    want = om.voxels[:nvox].view(np.uint8).reshape(nvox, 16)
+    assert np.array_equal(got, want)
+    assert (want[:, 8] > 0).sum() > 100
+    gmap.close()
+
+
+def _system(sf, ctx, mode, seq):
+    cfg = sf.system_config(cols=C1["cols"], rows=C1["rows"], K=C1["K"], use_graph=mode, **MAP_C1)
+    return sf.System(ctx, cfg, init_pose=seq[0][3])
+
+
+def _maps(ctx, imgs):
+    return [ctx.download(im.data, np.float32, im.rows * im.cols * 4).reshape(im.rows, im.cols, 4) for im in imgs]
+
+
+def _measured(d, K):
+    from oracle import oracle as O
+    _, filt = O.filter_depth(d, 1000.0, 3.0)
+    deps = [filt]
+    for _ in range(2):
+        deps.append(O.pyrdown(deps[-1]))
+    vms = [O.vmap(deps[l], *[k / (1 << l) for k in K], 3.0) for l in range(3)]
+    return vms, [O.nmap(v) for v in vms]
+
+
+@pytest.mark.parametrize("mode", [1, 0])
+def test_localisation_mode(lib, mode):
+    """Three mapping frames, then localisation: the map is left as it was
+    (without detections) and tracking goes on against the raycast of the
+    fixed map; then mapping again.  Per frame, the GPU's ComputeSE3 equals
+    the oracle's on the same inputs (POSE_TOL), or, where the divergence
+    guard ended a level one iteration apart on rounding-level differences of
+    the error (at most twice), agrees to FLIP_TOL; the trajectory follows the
+    oracle's loop in the same modes within LOOP_TOL (three frames without
+    fusion leave the model further behind, which makes the discontinuous
+    divergence guard of ComputeSE3 more sensitive to rounding than in the
+    mapping-only loop) and ground truth within 5 cm."""
+    from oracle import oracle as O
+    sf, ctx = lib
+    K = C1["K"]
+    n = 9
+    seq = sequence(C1["cols"], C1["rows"], K, n, trajectory=0)
+    s = _system(sf, ctx, mode, seq)
+    osys = O.System(MAP_C1, C1["cols"], C1["rows"], K, init_pose=seq[0][3])
+    m = s.map()
+    before = None
+    prev = None
+    flips = 0
+    for i, (d, rgb, _, Pgt) in enumerate(seq):
+        if i > 0:
+            model = [s.model_maps(l) for l in range(3)]
+            mv, mn = _maps(ctx, [x[0] for x in model]), _maps(ctx, [x[1] for x in model])
+        if i == 3:
+            s.set_mapping(False)
+            osys.set_mapping(False)
+            e0, v0, _ = map_to_host(ctx, m)
+            before = (e0.copy(), v0.copy())
+        if i == 6:
+            e1, v1, _ = map_to_host(ctx, m)
+            assert np.array_equal(e1, before[0]), "hash table changed in localisation"
+            assert np.array_equal(v1.view(np.uint8), before[1].view(np.uint8)), "voxels changed in localisation"
+            s.set_mapping(True)
+            osys.set_mapping(True)
+        st = s.grab(d, rgb)
+        ok, P, _ = osys.grab(d, rgb)
+        pose = np.array(st.pose[:]).reshape(4, 4)
+        assert bool(st.tracked) == ok and st.flags == 0, "frame %d" % i
+        if i > 0:
+            vms, nms = _measured(d, K)
+            ok1, P1, ost = O.compute_se3(vms, nms, mv, mn, K, (10, 5, 4), (2000, 1000, 100), 1e-4, prev, prev)
+            assert ok1 == bool(st.accepted), "frame %d" % i
+            if int(ost[2]) == st.iterations:
+                assert np.abs(P1 - pose).max() < POSE_TOL, "frame %d ComputeSE3" % i
+            else:  # the divergence guard ended a level one iteration apart
+                flips += 1
+                assert abs(int(ost[2]) - st.iterations) == 1 and np.abs(P1 - pose).max() < FLIP_TOL, "frame %d" % i
+        assert np.abs(pose - P).max() < LOOP_TOL, "frame %d" % i
+        assert np.linalg.norm(pose[:3, 3] - Pgt[:3, 3]) < 0.05
+        prev = pose
+    assert flips <= 2
+    e2, _, _ = map_to_host(ctx, m)
+    assert (e2["ptr"] >= 0).sum() > (before[0]["ptr"] >= 0).sum()  # mapping resumed
+    s.close()
+
+
+@pytest.mark.parametrize("mode", [1, 0])
+def test_semantic_mode_fuses_twice(lib, mode):
+    """With detections every frame: FuseColor without and then with the
+    labels; the trajectory follows the oracle's loop, the voxels' weights
+    count each frame twice, as the reference's GrabImage does."""
+    from oracle import oracle as O
+    sf, ctx = lib
+    n = 5
+    seq = sequence(C1["cols"], C1["rows"], C1["K"], n, trajectory=0, label_flip=0.05, n_objects=10, seed=5)
+    s = _system(sf, ctx, mode, seq)
+    osys = O.System(MAP_C1, C1["cols"], C1["rows"], C1["K"], init_pose=seq[0][3])
+    for i, (d, rgb, mask, _) in enumerate(seq):
+        st = s.grab(d, rgb, mask, 10)
+        ok, P, _ = osys.grab(d, rgb, mask, 10)
+        pose = np.array(st.pose[:]).reshape(4, 4)
+        assert bool(st.tracked) == ok and st.flags == 0, "frame %d" % i
+        assert np.abs(pose - P).max() < TRAJ_TOL, "frame %d" % i
+    e, v, _ = map_to_host(ctx, s.map())
+    oe, ov = osys.entries(), osys.voxels()
+    a, b = positions(e[e["ptr"] >= 0]), positions(oe[oe["ptr"] >= 0])
+    assert len(a ^ b) <= 0.01 * len(b)
+    assert int(v["weight"].max()) == int(ov["weight"].max()) == 2 * n
+    assert (v["label"][v["weight"] > 0] > 0).sum() > 100
+    s.close()

@@ -87,7 +87,8 @@ def test_intensity_every_colour(lib):
     v = np.arange(1 << 24, dtype=np.uint32)
     rgb = np.stack([(v >> 16) & 255, (v >> 8) & 255, v & 255], -1).astype(np.uint8).reshape(4096, 4096, 3)
     out = empty((4096, 4096), torch.uint8)
-    sf.call("sf_ImageToIntensity", ctx.h, sf.image(cuda(rgb), 3), sf.image(out))
+    dc = cuda(rgb)  # alive through the call
+    sf.call("sf_ImageToIntensity", ctx.h, sf.image(dc, 3), sf.image(out))
     ctx.sync()
     assert np.array_equal(host(out), O.intensity(rgb))
 

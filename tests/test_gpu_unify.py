@@ -126,9 +126,10 @@ def test_unify_visible_count_edges(lib):
 
 
 def test_frame_graph_runs_unify(lib):
-    """The system loop with detections runs the pass (two launches more per
-    frame than without), in graph and plain form; the label state it leaves
-    is a fixed input the oracle's pass reproduces on the same layout."""
+    """The system loop with detections runs the pass (inside the second,
+    labelled FuseColor of the semantic mode), in graph and plain form; the
+    label state it leaves is a fixed input the oracle's pass reproduces on
+    the same layout."""
     from oracle import oracle as O
     sf, ctx = lib
     K = C1["K"]
@@ -163,5 +164,8 @@ def test_frame_graph_runs_unify(lib):
                 got = _voxel_bytes(ctx, m, nvox)
                 assert np.array_equal(got, om.voxels[:nvox].view(np.uint8).reshape(nvox, 16))
             s.close()
-    assert per_frame[(1, 10)] == per_frame[(1, 0)] + 2
-    assert per_frame[(0, 10)] == per_frame[(0, 0)] + 2
+    # with detections the frame graph runs FuseColor again with the labels
+    # (allocation 3 launches, visibility 2, integration 1, UnifyNeighbor 2)
+    # and RayTrace (1), System.cc:184-205.  (The plain form's count also
+    # follows the ICP iterations, which differ between the two maps.)
+    assert per_frame[(1, 10)] == per_frame[(1, 0)] + 9
