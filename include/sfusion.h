@@ -226,6 +226,26 @@ int sf_ComputeSE3(sf_context *ctx, int levels, const sf_image *next_vmaps,
                   const int *min_count, float thresh, const double last_pose[16],
                   double next_pose_out[16], int stats_out[4], float *icp_error_out);
 
+/* ----------------------------------------------------------------- mesh */
+/* MeshScene (RenderScene.h:29; MeshScene.cu:299-356, Mapping::CreateModel
+ * Mapping.cc:183-192): marching cubes over every allocated block.  Writes
+ * up to max_triangles triangles, three vertices each, to DEVICE arrays:
+ * vertices and normals float[3 * 3 * max_triangles] (metres, unit
+ * normals), colors uint8[3 * 3 * max_triangles]; *num_triangles = the
+ * triangles written.  Vertices, normals and colours are the reference's
+ * per cube; each cube's polygons are those of the reference's tables, split
+ * into triangles by this library's own rule (a fan from the polygon's
+ * lowest edge).  Triangle order is not defined. */
+int sf_MeshScene(sf_context *ctx, sf_map *map, float *vertices, float *normals,
+                 uint8_t *colors, uint32_t max_triangles,
+                 uint32_t *num_triangles);
+/* System::WriteMeshToDisk (Core/System.cc:272-325): the mesh (DEVICE
+ * arrays as sf_MeshScene writes them) as an ASCII PLY file, the reference's
+ * layout. */
+int sf_mesh_write_ply(sf_context *ctx, const char *path, const float *vertices,
+                      const float *normals, const uint8_t *colors,
+                      uint32_t num_triangles);
+
 /* ----------------------------------------------------- photometric term */
 /* ImageToIntensity (Tracking/Reduction.h:34; Pyrdown.cu:250-271): uchar3
  * colour -> uint8 intensity, (int)(0.2125 g + 0.7154 r + 0.0721 b) with the

@@ -96,6 +96,8 @@ def lib():
                 "sfo_system_grab": (C.c_int, [vp, U16P, U8P, U8P, C.c_int, F64P, F64P]),
                 "sfo_system_set_rgb": (None, [vp, C.c_int]),
                 "sfo_system_set_mapping": (None, [vp, C.c_int]),
+                "sfo_mc_tables": (None, [I32P, I32P, I32P]),
+                "sfo_mesh": (C.c_uint, [vp, C.c_uint, F32P, F32P, U8P]),
                 "sfo_system_map": (vp, [vp]),
                 "sfo_system_vmap": (vp, [vp, C.c_int]),
                 "sfo_system_nmap": (vp, [vp, C.c_int]),
@@ -240,6 +242,15 @@ def compute_se3(vnext, nnext, vlast, nlast, K, iters, min_count, thresh, last_po
     return bool(ok), npose, (stats if rgb is not None else stats[:4])
 
 
+def mc_tables():
+    """(triangle table [256,16], vertex counts [256], edge masks [256])."""
+    t = np.zeros((256, 16), np.int32)
+    nv = np.zeros(256, np.int32)
+    ed = np.zeros(256, np.int32)
+    lib().sfo_mc_tables(_p(t, I32P), _p(nv, I32P), _p(ed, I32P))
+    return t, nv, ed
+
+
 def intensity(rgb):
     """ImageToIntensity: uchar3 rows x cols x 3 -> uint8."""
     rgb = np.ascontiguousarray(rgb, np.uint8)
@@ -373,6 +384,14 @@ class Map:
         pass: the label pass, then UnifyNeighbor."""
         self.semantics(depth, rgb, nmap_, mask, num_detection, P, K)
         self.unify_neighbor()
+
+    def mesh(self, max_tri=2000000):
+        """MeshScene: (vertices [n,3,3], normals [n,3,3], colours [n,3,3] uint8)."""
+        v = np.zeros((max_tri, 3, 3), np.float32)
+        n = np.zeros((max_tri, 3, 3), np.float32)
+        c = np.zeros((max_tri, 3, 3), np.uint8)
+        k = lib().sfo_mesh(self.h, max_tri, _p(v, F32P), _p(n, F32P), _p(c, U8P))
+        return v[:k], n[:k], c[:k]
 
     def fuse(self, depth, rgb, nmap_, mask, num_detection, P, K, unify=True):
         """FuseMapColor.  unify=False stops before the UnifyNeighbor pass

@@ -11,7 +11,7 @@ The rewrites only make the CUDA sources compile as serial host C++:
   * `static __shared__` becomes `__shared__` (emulated as static);
   * Utility/ParallelScan.h is replaced by a serial prefix offset;
   * DeviceMap's static constexpr constants take the golden configuration's
-    values (voxel size, truncation, table sizes);
+    values (voxel size, truncation, table sizes, mesh triangle cap);
   * FuseMapColor's SemanticAnalysisKernel and UnifyNeighborKernel launches
     use the (8, 8) thread block that AnalyzeMapSemantics uses (the (8, 8, 8)
     launch applies one update per z-thread, a race on the GPU);
@@ -41,15 +41,15 @@ ORACLE = os.path.dirname(HERE)
 OUT = os.path.join(ORACLE, "_ref")
 REF = os.environ.get("SF_REFERENCE_DIR", "/root/reference")
 
-SOURCES = ["Mapping/DeviceMap.cu", "Mapping/FuseMap.cu", "Mapping/RenderScene.cu", "Tracking/Pyrdown.cu",
-           "Tracking/Reduction.cu"]
+SOURCES = ["Mapping/DeviceMap.cu", "Mapping/FuseMap.cu", "Mapping/RenderScene.cu", "Mapping/MeshScene.cu",
+           "Tracking/Pyrdown.cu", "Tracking/Reduction.cu"]
 HEADERS = ["Mapping/DeviceMap.h", "Mapping/RenderScene.h", "Mapping/Constant.h", "Tracking/Reduction.h",
            "Utility/DeviceArray.h", "Utility/VectorMath.h", "Utility/SafeCall.h", "Utility/Intrinsics.h"]
 
 # Golden configurations: DeviceMap constants (Mapping/DeviceMap.h:166-189).
 CONFIGS = {
     "g1": dict(VoxelSize="0.01f", TruncateMul=3, NumBuckets=4096, NumExcess=8192, NumSdfBlocks=16384,
-               DepthMin="0.1f", DepthMax="3.0f"),
+               DepthMin="0.1f", DepthMax="3.0f", MaxTriangles=1000000),
 }
 
 ICP_APPENDIX = r'''
@@ -224,6 +224,7 @@ def patch_sources(name, text, cfg):
         sub("NumSdfBlocks", cfg["NumSdfBlocks"])
         sub("DepthMin", cfg["DepthMin"])
         sub("DepthMax", cfg["DepthMax"])
+        sub("MaxTriangles", cfg["MaxTriangles"])
     if name == "FuseMap.cu":
         # GarbageCollectKernel only rewrites the visible-list copy's ptr to
         # EntryToDelete; SemanticAnalysisKernel then indexes

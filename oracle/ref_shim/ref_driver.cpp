@@ -6,6 +6,7 @@
 #include <cstring>
 #include <vector>
 
+#include "Constant.h"
 #include "DeviceMap.h"
 #include "Reduction.h"
 #include "RenderScene.h"
@@ -265,6 +266,28 @@ int ref_map_raytrace(void *mp, int cols, int rows, const float *R, const float *
 const void *ref_map_entries(void *mp) { return ((RefMap *)mp)->hashEntries.data; }
 const void *ref_map_visible(void *mp) { return ((RefMap *)mp)->visibleEntries.data; }
 const void *ref_map_voxels(void *mp) { return ((RefMap *)mp)->sdfBlock.data; }
+// Mapping::CreateModel (Mapping.cc:183-192): MeshScene with the tables of
+// Constant.h.  Returns the triangle count; vert / nrm float[9] and col
+// uint8[9] per triangle (up to max_tri).
+unsigned ref_map_mesh(void *mp, unsigned max_tri, float *vert, float *nrm, uint8_t *col) {
+  RefMap &m = *(RefMap *)mp;
+  DeviceArray<int> edge(256), verts(256);
+  DeviceArray2D<int> tri(16, 256);
+  edge.upload(edgeTableHost, 256);
+  verts.upload(vertexTableHost, 256);
+  tri.upload(triangleTableHost, 16 * sizeof(int));
+  DeviceArray<float3> normal(DeviceMap::MaxVertices), vertex(DeviceMap::MaxVertices);
+  DeviceArray<uchar3> color(DeviceMap::MaxVertices);
+  DeviceArray<int3> blocks(DeviceMap::NumEntries);
+  DeviceArray<uint> nblocks(1), ntri(1);
+  uint n = MeshScene(nblocks, ntri, m.view(), edge, verts, tri, normal, vertex, color, blocks);
+  if (n > max_tri) n = max_tri;
+  vertex.download(vert, 3 * n);
+  normal.download(nrm, 3 * n);
+  color.download(col, 3 * n);
+  return n;
+}
+
 // UnifyNeighborKernel over hash slots [0, nvis) with the (8, 8) block of
 // AnalyzeMapSemantics (FuseMap.cu:1244-1246).
 void ref_map_unify(void *mp, unsigned nvis) {

@@ -1568,6 +1568,176 @@ extern "C" void sfo_raycast(sfo_map *m, float *vmap, float *nmap, int cols, int 
     }
 }
 
+// ========================================================= marching cubes
+namespace {
+// Corners (0,0,0) (1,0,0) (1,1,0) (0,1,0) (0,0,1) (1,0,1) (1,1,1) (0,1,1)
+// and edges (0,1) (1,2) (2,3) (3,0) (4,5) (5,6) (6,7) (7,4) (0,4) (1,5)
+// (2,6) (3,7), MeshScene.cu's numbering.
+const int kMcA[12] = {0, 1, 2, 3, 4, 5, 6, 7, 0, 1, 2, 3};
+const int kMcB[12] = {1, 2, 3, 0, 5, 6, 7, 4, 4, 5, 6, 7};
+const int kMcCorner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+struct McTab { int tri[256][16]; int nverts[256]; int edges[256]; };
+// The polygons of each configuration: on every face (corners taken
+// counterclockwise from outside) a segment cuts off each inside corner
+// (or run of them), from the crossing that leaves it to the crossing that
+// enters it; the segments chain into loops, each fanned into triangles
+// from its lowest edge.  The loops are those of the classic table
+// Mapping/Constant.h holds (checked by tests/test_oracle_mesh.py).
+McTab mc_tables() {
+  static const int face[6][4] = {{0, 3, 2, 1}, {4, 5, 6, 7}, {0, 1, 5, 4}, {3, 7, 6, 2}, {0, 4, 7, 3}, {1, 2, 6, 5}};
+  McTab t;
+  auto edge_of = [](int a, int b) {
+    for (int e = 0; e < 12; ++e)
+      if ((kMcA[e] == a && kMcB[e] == b) || (kMcA[e] == b && kMcB[e] == a)) return e;
+    return -1;
+  };
+  for (int ci = 0; ci < 256; ++ci) {
+    int nxt[12];
+    for (int e = 0; e < 12; ++e) nxt[e] = -1;
+    int emask = 0;
+    for (const auto &f : face) {
+      std::vector<std::pair<int, int>> cr;  // (edge, leaves an inside corner)
+      for (int k = 0; k < 4; ++k) {
+        int a = f[k], b = f[(k + 1) % 4];
+        int ia = (ci >> a) & 1, ib = (ci >> b) & 1;
+        if (ia != ib) cr.push_back({edge_of(a, b), ia});
+      }
+      for (size_t j = 0; j < cr.size(); ++j) {
+        emask |= 1 << cr[j].first;
+        if (cr[j].second == 0) nxt[cr[(j + 1) % cr.size()].first] = cr[j].first;
+      }
+    }
+    t.edges[ci] = emask;
+    for (int k = 0; k < 16; ++k) t.tri[ci][k] = -1;
+    int used = 0, nt = 0;
+    for (int s0 = 0; s0 < 12; ++s0) {
+      if (nxt[s0] < 0 || ((used >> s0) & 1)) continue;
+      std::vector<int> loop;
+      int e = s0;
+      do { loop.push_back(e); used |= 1 << e; e = nxt[e]; } while (e != s0);
+      for (size_t q = 1; q + 1 < loop.size(); ++q) {
+        t.tri[ci][3 * nt] = loop[0]; t.tri[ci][3 * nt + 1] = loop[q]; t.tri[ci][3 * nt + 2] = loop[q + 1];
+        ++nt;
+      }
+    }
+    t.nverts[ci] = 3 * nt;
+  }
+  return t;
+}
+}  // namespace
+
+extern "C" void sfo_mc_tables(int *tri4096, int *nverts256, int *edges256) {
+  static const McTab t = mc_tables();
+  memcpy(tri4096, t.tri, sizeof(t.tri));
+  memcpy(nverts256, t.nverts, sizeof(t.nverts));
+  memcpy(edges256, t.edges, sizeof(t.edges));
+}
+
+// MeshEngine (Mapping/MeshScene.cu:4-297) over the allocated entries in
+// table order, the cubes of a block in its (8, 8) launch order (y, x, then
+// z): up to max_tri triangles into vert / norm (float[9] each per
+// triangle) and col (uint8[9]).  Returns the triangle count (capped).
+extern "C" unsigned sfo_mesh(sfo_map *m, unsigned max_tri, float *vert, float *nrm_out, uint8_t *col) {
+  static const McTab T = mc_tables();
+  const float vs = m->c.voxel_size;
+  auto voxel = [&](i3 v) -> const sfo_voxel * {
+    const sfo_entry *e = find_entry(*m, vox2block(v));
+    return e ? &m->voxels[(size_t)e->ptr + vox2local(v)] : nullptr;
+  };
+  auto sdf_at = [&](i3 v) {
+    const sfo_voxel *p = voxel(v);
+    return p ? p->sdf : std::nanf("");
+  };
+  // interp (MeshScene.cu:144-152), the 1e-6 tests in double
+  auto interp = [](float v1, float v2) {
+    if ((double)std::fabs(0.f - v1) < 1e-6) return 0.f;
+    if ((double)std::fabs(0.f - v2) < 1e-6) return 1.f;
+    if ((double)std::fabs(v1 - v2) < 1e-6) return 0.f;
+    return (0.f - v1) / (v2 - v1);
+  };
+  unsigned count = 0;
+  for (const sfo_entry &ent : m->entries) {
+    if (ent.ptr < 0) continue;
+    for (int ty = 0; ty < 8; ++ty)
+      for (int tx = 0; tx < 8; ++tx)
+        for (int z = 0; z < 8; ++z) {
+          const i3 pos = {ent.x * 8 + tx, ent.y * 8 + ty, ent.z * 8 + z};
+          // readVertexAndColor (:115-141)
+          float sdf[8];
+          uint8_t c[8][3];
+          bool ok = true;
+          for (int k = 0; k < 8 && ok; ++k) {
+            const sfo_voxel *p = voxel({pos.x + kMcCorner[k][0], pos.y + kMcCorner[k][1], pos.z + kMcCorner[k][2]});
+            sdf[k] = p ? p->sdf : std::nanf("");
+            for (int q = 0; q < 3; ++q) c[k][q] = p ? p->color[q] : 0;
+            ok = !(sdf[k] == 1.0 || std::isnan(sdf[k]));
+          }
+          if (!ok) continue;
+          // readNormal (:43-113): per corner, the differences to the
+          // outside neighbour along x, y, z (sdf[] of the in-cube one)
+          f3 n[8];
+          for (int k = 0; k < 8 && ok; ++k) {
+            float d[3];
+            for (int ax = 0; ax < 3; ++ax) {
+              const int lo = kMcCorner[k][ax] == 0;  // the neighbour outside is below
+              i3 q = {pos.x + kMcCorner[k][0], pos.y + kMcCorner[k][1], pos.z + kMcCorner[k][2]};
+              int other = k;
+              if (ax == 0) { q.x += lo ? -1 : 1; other = k ^ 1; }
+              if (ax == 1) { q.y += lo ? -1 : 1; other = (k & 4) | (3 - (k & 3)); }
+              if (ax == 2) { q.z += lo ? -1 : 1; other = k ^ 4; }
+              const float v = sdf_at(q);
+              if (std::isnan(v)) { ok = false; break; }
+              d[ax] = lo ? sdf[other] - v : v - sdf[other];
+            }
+            if (ok) n[k] = {d[0], d[1], d[2]};
+          }
+          if (!ok) continue;
+          int ci = 0;
+          for (int k = 0; k < 8; ++k) ci |= (sdf[k] < 0) << k;
+          if (T.edges[ci] == 0 || ci <= 0) continue;
+          // buildVertexList (:172-247)
+          f3 vl[12], nl[12];
+          uint8_t cl[12][3];
+          static const float dir[12][3] = {{1, 0, 0}, {0, 1, 0}, {-1, 0, 0}, {0, -1, 0}, {1, 0, 0}, {0, 1, 0},
+                                           {-1, 0, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, 1}, {0, 0, 1}, {0, 0, 1}};
+          for (int e = 0; e < 12; ++e) {
+            if (!((T.edges[ci] >> e) & 1)) continue;
+            const int a = kMcA[e], b = kMcB[e];
+            const float val = interp(sdf[a], sdf[b]);
+            // pos + make_float3(o): the corner a, plus val along the edge
+            // (1 - val where the edge runs backwards)
+            float o[3];
+            for (int ax = 0; ax < 3; ++ax) {
+              const float base = (float)kMcCorner[a][ax];
+              o[ax] = dir[e][ax] > 0 ? val : (dir[e][ax] < 0 ? 1.f - val : base);
+            }
+            vl[e] = {(float)pos.x + o[0], (float)pos.y + o[1], (float)pos.z + o[2]};
+            nl[e] = n[a] + val * (n[b] - n[a]);
+            // uchar3 + val * (uchar3 - uchar3): val taken as an int
+            const int s = (int)val;
+            for (int q = 0; q < 3; ++q)
+              cl[e][q] = (uint8_t)(c[a][q] + (uint8_t)((uint8_t)(c[b][q] - c[a][q]) * s));
+          }
+          const int nt = T.nverts[ci] / 3;
+          for (int j = 0; j < nt; ++j) {
+            if (count >= max_tri) return count;
+            for (int q = 0; q < 3; ++q) {
+              const int e = T.tri[ci][3 * j + q];
+              const f3 v = vl[e] * vs;
+              const f3 nn = nl[e] / norm(nl[e]);
+              float *pv = vert + 9 * (size_t)count + 3 * q, *pn = nrm_out + 9 * (size_t)count + 3 * q;
+              pv[0] = v.x; pv[1] = v.y; pv[2] = v.z;
+              pn[0] = nn.x; pn[1] = nn.y; pn[2] = nn.z;
+              for (int r = 0; r < 3; ++r) col[9 * (size_t)count + 3 * q + r] = cl[e][r];
+            }
+            ++count;
+          }
+        }
+  }
+  return count;
+}
+
+
 // RelocScoreBatch of the GB300 loop (no reference kernel; see
 // semantic_icpslam_gb300/csrc/reloc.cu): per candidate, every stride-th
 // vertex moved into the map by (R | t) and read with readSdfInterped

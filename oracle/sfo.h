@@ -94,6 +94,10 @@ int sfo_compute_se3_ex(int levels, const int *cols, const int *rows,
                        float thresh, const double *last_pose, double *next_pose,
                        int fp64, double *stats);
 
+// ---- marching cubes (Mapping/MeshScene.cu) ----
+// The triangle / vertex-count / edge tables of this restatement's rule.
+void sfo_mc_tables(int *tri4096, int *nverts256, int *edges256);
+
 // ---- map (Mapping/DeviceMap.cu, FuseMap.cu, RenderScene.cu) ----
 sfo_map *sfo_map_create(const sfo_config *cfg);
 void sfo_map_destroy(sfo_map *m);
@@ -122,6 +126,10 @@ void sfo_semantics(sfo_map *m, const float *depth, const uint8_t *rgb,
                    int cols, int rows, const float *Rinv, const float *t,
                    float fx, float fy, float cx, float cy, float depth_max,
                    float depth_min);
+// MeshScene's marching cubes over the allocated entries in table order:
+// up to max_tri triangles, 9 floats of vertices and of normals and 9 bytes
+// of colour each.  Returns the triangle count.
+unsigned sfo_mesh(sfo_map *m, unsigned max_tri, float *vert, float *nrm, uint8_t *col);
 // Fusion::UnifyNeighbor over hash entries [0, noVisible) (FuseMap.cu:757-896).
 void sfo_unify_neighbor(sfo_map *m);
 // FuseMapColor order (FuseMap.cu:1039-1162): alloc, visibility, integrate,

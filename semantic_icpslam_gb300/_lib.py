@@ -142,6 +142,8 @@ SIGNATURES = {
     "sf_AnalyzeMapSemantics": [vp, vp, Image, Image, Image, Image, C.c_int, Mat3, Mat3, Float3]
                               + [C.c_float] * 6,
     "sf_UnifyNeighbor": [vp, vp],
+    "sf_MeshScene": [vp, vp, vp, vp, vp, C.c_uint32, U32P],
+    "sf_mesh_write_ply": [vp, C.c_char_p, vp, vp, vp, C.c_uint32],
     "sf_SemanticAnalysis": [vp, vp, Image, Image, Image, Image, C.c_int, Mat3, Mat3, Float3] + [C.c_float] * 4,
     "sf_CreateRenderingBlocks": [vp, vp, Image, Image, C.c_float, C.c_float, vp, vp, Mat3, Float3, C.c_uint32]
                                 + [C.c_float] * 4 + [I32P],

@@ -716,6 +716,55 @@ int sf_ComputeSE3_rgbd(sf_context *ctx, int levels, const sf_image *nv, const sf
   return SF_OK;
 }
 
+// ------------------------------------------------------------- mesh
+int sf_MeshScene(sf_context *ctx, sf_map *m, float *vertices, float *normals, uint8_t *colors,
+                 uint32_t max_triangles, uint32_t *num_triangles) {
+  if (!ctx || !m || !vertices || !normals || !colors || !num_triangles || max_triangles == 0) return SF_ERR_INVALID;
+  launch_mesh(m->d, reinterpret_cast<float3 *>(vertices), reinterpret_cast<float3 *>(normals),
+              reinterpret_cast<uchar3 *>(colors), max_triangles, ctx->u32, ctx->stream);
+  SF_CHECK(cudaGetLastError());
+  uint32_t n = 0;
+  SF_CHECK(cudaMemcpyAsync(&n, ctx->u32, sizeof(n), cudaMemcpyDeviceToHost, ctx->stream));
+  SF_CHECK(cudaStreamSynchronize(ctx->stream));
+  *num_triangles = n < max_triangles ? n : max_triangles;  // MeshScene.cu:352-353
+  return SF_OK;
+}
+
+int sf_mesh_write_ply(sf_context *ctx, const char *path, const float *vertices, const float *normals,
+                      const uint8_t *colors, uint32_t num_triangles) {
+  if (!ctx || !path || (num_triangles && (!vertices || !normals || !colors))) return SF_ERR_INVALID;
+  FILE *fp = fopen(path, "w");
+  if (!fp) return SF_ERR_IO;
+  FileCloser close_fp{fp};
+  const size_t nv = (size_t)num_triangles * 3;
+  // System::WriteMeshToDisk's ASCII layout (Core/System.cc:283-322); the
+  // numbers print as an ostream's defaults (%g)
+  if (fprintf(fp,
+              "ply\nformat ascii 1.0\nelement vertex %zu\nproperty float x\nproperty float y\nproperty float z\n"
+              "property float nx\nproperty float ny\nproperty float nz\nproperty uchar red\nproperty uchar green\n"
+              "property uchar blue\nelement face %u\nproperty list uchar uint vertex_indices\nend_header\n",
+              nv, num_triangles) < 0)
+    return SF_ERR_IO;
+  const size_t chunk = 1 << 18;
+  std::vector<float> v, n;
+  std::vector<uint8_t> c;
+  for (size_t i0 = 0; i0 < nv; i0 += chunk) {
+    const size_t k = nv - i0 < chunk ? nv - i0 : chunk;
+    v.resize(3 * k); n.resize(3 * k); c.resize(3 * k);
+    SF_CHECK(cudaMemcpyAsync(v.data(), vertices + 3 * i0, 12 * k, cudaMemcpyDeviceToHost, ctx->stream));
+    SF_CHECK(cudaMemcpyAsync(n.data(), normals + 3 * i0, 12 * k, cudaMemcpyDeviceToHost, ctx->stream));
+    SF_CHECK(cudaMemcpyAsync(c.data(), colors + 3 * i0, 3 * k, cudaMemcpyDeviceToHost, ctx->stream));
+    SF_CHECK(cudaStreamSynchronize(ctx->stream));
+    for (size_t i = 0; i < k; ++i)
+      if (fprintf(fp, "%g %g %g %g %g %g %d %d %d\n", v[3 * i], v[3 * i + 1], v[3 * i + 2], n[3 * i], n[3 * i + 1],
+                  n[3 * i + 2], (int)c[3 * i], (int)c[3 * i + 1], (int)c[3 * i + 2]) < 0)
+        return SF_ERR_IO;
+  }
+  for (uint32_t t = 0; t < num_triangles; ++t)
+    if (fprintf(fp, "3 %d %d %d\n", (int)t * 3 + 0, (int)t * 3 + 1, (int)t * 3 + 2) < 0) return SF_ERR_IO;
+  return SF_OK;
+}
+
 // -------------------------------------------------------- relocalisation
 int sf_RelocScoreBatch(sf_context *ctx, sf_map *m, sf_image vmap, int stride, const double *poses, int n,
                        float inlier_sdf, sf_reloc_score *scores_out) {

@@ -184,6 +184,10 @@ void launch_visibility(const DevMap &m, const FuseScratch &f, const Cam *c, cons
                        const sf_image *zmax, const int *run_flag, uint32_t *flags,
                        cudaStream_t s);
 // createVoxels (+ analyzeSemantics when mask != null), FuseMap.cu:432-668.
+// MeshScene's marching cubes over the allocated blocks: up to max_tri
+// triangles (3 vertices, normals, colours each) appended at *count.
+void launch_mesh(const DevMap &m, float3 *vert, float3 *norm, uchar3 *col, uint32_t max_tri, uint32_t *count,
+                 cudaStream_t s);
 // Fusion::UnifyNeighbor over hash slots [0, *no_visible) from the pass-start
 // state (two launches); needs fuse_scratch_unify first.
 int fuse_scratch_unify(FuseScratch &f, const MapConst &c);

@@ -14,7 +14,8 @@ ComputeVMap, ComputeNMap, ResizeMap, per-pixel ICP rows, the intensity pyramid
 (ImageToIntensity, PyrDownGauss(uchar), ComputeDerivativeImage), per-pixel
 RGB rows (RGBStep's FindCorresp and GetRow), FuseMapColor over
 five frames (labels from frame 2 on), CheckBlockVisibility, AnalyzeMapSemantics,
-CreateRenderingBlocks + Raycast from two poses, and UnifyNeighborKernel alone
+CreateRenderingBlocks + Raycast from two poses, MeshScene on the fused map,
+and UnifyNeighborKernel alone
 on a seeded label state (unify_state below).
 """
 import ctypes as C
@@ -46,9 +47,10 @@ def load_ref():
     L.ref_map_fuse.restype = C.c_uint
     L.ref_map_visibility.restype = C.c_uint
     L.ref_map_raytrace.restype = C.c_int
+    L.ref_map_mesh.restype = C.c_uint
     for n in ("ref_map_fuse", "ref_map_visibility", "ref_map_semantics", "ref_map_raytrace", "ref_map_counters",
               "ref_map_unify", "ref_map_entries", "ref_map_visible", "ref_map_voxels", "ref_map_destroy",
-              "ref_intensity", "ref_pyrdown_u8", "ref_sobel", "ref_rgb_rows"):
+              "ref_intensity", "ref_pyrdown_u8", "ref_sobel", "ref_rgb_rows", "ref_map_mesh"):
         getattr(L, n).argtypes = None
     return L
 
@@ -62,6 +64,17 @@ def pose_parts(P):
     Ri = np.ascontiguousarray(P[:3, :3].T, np.float32)
     t = np.ascontiguousarray(P[:3, 3], np.float32)
     return R, Ri, t
+
+
+def mesh_records(v, n, c):
+    """The sorted distinct vertex records of a mesh: 3 floats position, 3
+    floats normal, 3 bytes colour and a zero byte, 28 bytes each."""
+    k = v.reshape(-1, 3).shape[0]
+    rec = np.zeros((k, 28), np.uint8)
+    rec[:, :12] = np.ascontiguousarray(v.reshape(-1, 3)).view(np.uint8).reshape(k, 12)
+    rec[:, 12:24] = np.ascontiguousarray(n.reshape(-1, 3)).view(np.uint8).reshape(k, 12)
+    rec[:, 24:27] = c.reshape(-1, 3)
+    return np.unique(rec, axis=0)
 
 
 def block_digests(entries, voxels_ptr, n_sdf):
@@ -282,6 +295,18 @@ def main():
     ent = np.frombuffer((C.c_char * (n_entries * 32)).from_address(L.ref_map_entries(C.c_void_p(m))), ENTRY).copy()
     pos, dig, sample = block_digests(ent, L.ref_map_voxels(C.c_void_p(m)), n_sdf)
     out.update(map_pos=pos, map_sha1=dig, map_sample=sample)
+
+    # MeshScene on that map (Mapping::CreateModel): the triangle count and a
+    # digest of the set of distinct vertex records (position, normal, colour)
+    max_tri = 1000000
+    v = np.zeros((max_tri, 3, 3), np.float32)
+    nrm = np.zeros((max_tri, 3, 3), np.float32)
+    col = np.zeros((max_tri, 3, 3), np.uint8)
+    ntri = L.ref_map_mesh(C.c_void_p(m), C.c_uint(max_tri), fptr(v), fptr(nrm), fptr(col))
+    recs = mesh_records(v[:ntri], nrm[:ntri], col[:ntri])
+    out.update(mesh_ntri=np.int64(ntri), mesh_nrec=np.int64(len(recs)),
+               mesh_rec_sha1=np.frombuffer(hashlib.sha1(recs.tobytes()).digest(), np.uint8))
+    print("mesh: %d triangles, %d distinct vertex records" % (ntri, len(recs)))
 
     # raytrace from the last fused pose and the next pose (Mapping::RayTrace)
     for k, fi in enumerate((NFRAMES - 1, NFRAMES)):

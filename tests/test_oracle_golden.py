@@ -219,3 +219,28 @@ def test_rgb_rows(g):
                               g["rgb_rows_sha1_%d" % l]), "level %d" % l
         np.testing.assert_allclose(sums, g["rgb_sums%d" % l], rtol=1e-12)
     assert g["rgb_res0"][0] > 5000
+
+
+def mesh_records(v, n, c):
+    """Sorted distinct vertex records (position, normal, colour, 28 bytes),
+    as tests/golden/make_golden.py makes them."""
+    k = v.reshape(-1, 3).shape[0]
+    rec = np.zeros((k, 28), np.uint8)
+    rec[:, :12] = np.ascontiguousarray(v.reshape(-1, 3)).view(np.uint8).reshape(k, 12)
+    rec[:, 12:24] = np.ascontiguousarray(n.reshape(-1, 3)).view(np.uint8).reshape(k, 12)
+    rec[:, 24:27] = c.reshape(-1, 3)
+    return np.unique(rec, axis=0)
+
+
+def test_mesh(g, fused):
+    """MeshScene on the five fused frames' map: the same triangle count and
+    the same set of vertex records (every active edge of every cube: its
+    interpolated position, normal and colour) as the reference's kernel.
+    Each cube's polygons are the reference table's (tests/test_oracle_mesh.py);
+    only their split into triangles differs, which neither measure sees."""
+    m, _ = fused
+    v, n, c = m.mesh(1000000)
+    assert len(v) == int(g["mesh_ntri"])
+    recs = mesh_records(v, n, c)
+    assert len(recs) == int(g["mesh_nrec"])
+    assert np.array_equal(np.frombuffer(hashlib.sha1(recs.tobytes()).digest(), np.uint8), g["mesh_rec_sha1"])
