@@ -424,6 +424,8 @@ def main():
                     help="run sf_system_autotune during the warm-up of the headline form and keep its choice")
     ap.add_argument("--quick", action="store_true",
                     help="only the CUDA-graph timing (for profiler runs)")
+    ap.add_argument("--rgbd", action="store_true",
+                    help="with --quick: time the RGB-D tracking mode (ComputeSE3 with icpOnly = false) instead")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -449,7 +451,8 @@ def main():
     frames = make_frames(n, rank)
 
     # headline: CUDA graph, inputs in HBM
-    g = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 1, barrier, autotune=args.autotune)
+    g = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 1, barrier, autotune=args.autotune,
+                             rgb=1 if (args.quick and args.rgbd) else 0)
     elapsed = g["elapsed"]
     if ws > 1:
         import torch.distributed as dist
@@ -511,7 +514,9 @@ def main():
         # the reference's default tracking mode: ComputeSE3(icpOnly = false)
         r = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 1, barrier, rgb=1)
         re2e, rtracked = time_e2e(sf, ctx, frames, args.steps, args.warmup, 1, rgb=1)
+        rt = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 2, barrier, timing=True, rgb=1)
         out["rgbd"] = {"value": round(args.steps / r["elapsed"], 3), "unit": "frames/s",
+                       "stages_ms": dict(zip(STAGES, [round(float(x), 5) for x in rt["stage_ms"]])),
                        "e2e": round(args.steps / re2e, 3), "tracked_frames": int(rtracked),
                        "gpu_launches": int(r["launches"]),
                        "mode": "ComputeSE3 with icpOnly = false (the reference's default): RGBStep beside ICPStep "

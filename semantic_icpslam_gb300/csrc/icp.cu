@@ -209,16 +209,36 @@ __device__ __forceinline__ void icp_accumulate(const IcpLevelArgs &L, const Pose
 }
 
 // ------------------------------------------------------ photometric term
+// Pixel (x, y) of index i: i / cols through the float reciprocal (exact
+// after the remainder correction for i < 2^24), as icp_accumulate does.
+__device__ __forceinline__ void pixel_xy(int i, int cols, float inv_cols, bool small, int &x, int &y) {
+  if (small) {
+    y = (int)((float)i * inv_cols);
+    x = i - y * cols;
+    if (x < 0) { --y; x += cols; }
+    if (x >= cols) { ++y; x -= cols; }
+  } else {
+    y = i / cols;
+    x = i - y * cols;
+  }
+}
+
+// A pixel's correspondence for the iteration: the last frame's vertex in
+// the current camera (the `point` of GetRow) and the intensity difference,
+// or w = kNoCorr.
+constexpr int kNoCorr = (int)0x80000000;
+
 // RGBReduction::FindCorresp (Reduction.cu:412-463) for a pixel whose
 // pose-independent tests passed (its candidate flag): the current vertex
 // through the current and last poses to the last frame's pixel (u, v) --
 // `+ 0.5` is double and the sum reaches __float2int_rd as a float; the
 // double sum is exact, so that is the float sum rounded once -- then the
 // two vertices' float4 distance below 0.1 and a nonzero last intensity.
-// Returns {u | v << 16, diff}, or x = -1.
-__device__ __forceinline__ int2 rgb_find(const IcpLevelArgs &L, const RgbLevelArgs &R, const PoseF &p, int x,
-                                         int y) {
-  const int2 none = make_int2(-1, 0);
+// GetRow's pose-dependent point (Reduction.cu:497) is made here from the
+// vertex just gathered.
+__device__ __forceinline__ float4 rgb_find(const IcpLevelArgs &L, const RgbLevelArgs &R, const PoseF &p, int x,
+                                           int y) {
+  const float4 none = make_float4(0.f, 0.f, 0.f, __int_as_float(kNoCorr));
   const float4 vc = __ldg(row_ptr<const float4>(L.vc, y) + x);
   if (isnan(vc.x)) return none;
   const f3 vg = mul(p.Rc, xyz(vc)) + p.tc;
@@ -235,22 +255,21 @@ __device__ __forceinline__ int2 rgb_find(const IcpLevelArgs &L, const RgbLevelAr
   const int il = __ldg(row_ptr<const uint8_t>(R.ilast, v) + u);
   if (il == 0) return none;
   const int in = __ldg(row_ptr<const uint8_t>(R.inext, y) + x);
-  return make_int2(u | (v << 16), in - il);
+  const f3 point = mul(p.RcI, (mul(p.Rl, xyz(vl)) + p.tl) - p.tc);
+  return make_float4(point.x, point.y, point.z, __int_as_float(in - il));
 }
 
-// RGBReduction::GetRow (Reduction.cu:483-517): w = 1 / (sigma + |diff|)
-// (1 when that is below 1e-3, or when sigma < 1e-6), the last vertex in the
-// current camera, the gradient / 9 (the float quotient equals the
-// reference's double one for every short), and the row [w left,
-// w (point x left), -w diff].
-__device__ __forceinline__ void rgb_row(const IcpLevelArgs &L, const RgbLevelArgs &R, const PoseF &p,
-                                        float sigma, bool sigma_tiny, int x, int y, int2 c, float row[7]) {
-  const int u = c.x & 0xffff, v = c.x >> 16, diff = c.y;
+// RGBReduction::GetRow (Reduction.cu:483-517) from a correspondence: w =
+// 1 / (sigma + |diff|) (1 when that is below 1e-3, or when sigma < 1e-6),
+// the gradient / 9 (the float quotient equals the reference's double one
+// for every short), and the row [w left, w (point x left), -w diff].
+__device__ __forceinline__ void rgb_row(const IcpLevelArgs &L, const RgbLevelArgs &R, float sigma, bool sigma_tiny,
+                                        int x, int y, float4 c, float row[7]) {
+  const int diff = __float_as_int(c.w);
   float w = sigma + (float)abs(diff);
   w = w < 0.001f ? 1.0f : __fdiv_rn(1.0f, w);  // (double)w < 1e-3 iff w < 0.001f
   if (sigma_tiny) w = 1.0f;
-  const float4 vl = __ldg(row_ptr<const float4>(L.vl, v) + u);
-  const f3 point = mul(p.RcI, (mul(p.Rl, xyz(vl)) + p.tl) - p.tc);
+  const f3 point = mk3(c.x, c.y, c.z);
   const float gx = __fdiv_rn((float)__ldg(row_ptr<const short>(R.dx, y) + x), 9.0f);
   const float gy = __fdiv_rn((float)__ldg(row_ptr<const short>(R.dy, y) + x), 9.0f);
   const float invz = __fdiv_rn(1.0f, point.z);
@@ -280,31 +299,38 @@ __device__ __forceinline__ float rgb_sigma(unsigned cnt, unsigned ssq, bool &tin
 __device__ __forceinline__ void rgb_residual_pass(const IcpLevelArgs &L, const RgbLevelArgs &R, const PoseF &p,
                                                   int gtid, int gstride, unsigned &cnt, unsigned &ssq) {
   const int cols = L.vc.cols, N = cols * L.vc.rows;
+  const float inv_cols = 1.0f / (float)cols;
+  const bool small = N < (1 << 24) - gstride;
   for (int i = gtid; i < N; i += gstride) {
-    const int y = i / cols, x = i - y * cols;
-    int2 c = make_int2(-1, 0);
+    int x, y;
+    pixel_xy(i, cols, inv_cols, small, x, y);
+    float4 c = make_float4(0.f, 0.f, 0.f, __int_as_float(kNoCorr));
     if (__ldg(row_ptr<const uint8_t>(R.cand, y) + x)) c = rgb_find(L, R, p, x, y);
     __stcg(R.corr + i, c);
-    if (c.x >= 0) {
+    const int d = __float_as_int(c.w);
+    if (d != kNoCorr) {
       cnt += 1u;
-      ssq += (unsigned)(c.y * c.y);
+      ssq += (unsigned)(d * d);
     }
   }
 }
 
 // RgbStepKernel's pass (Reduction.cu:519-551): the 29 terms of this
 // thread's pixels' rows.
-__device__ __forceinline__ void rgb_rows_pass(const IcpLevelArgs &L, const RgbLevelArgs &R, const PoseF &p,
-                                              float sigma, bool tiny, int gtid, int gstride, float acc[29]) {
+__device__ __forceinline__ void rgb_rows_pass(const IcpLevelArgs &L, const RgbLevelArgs &R, float sigma, bool tiny,
+                                              int gtid, int gstride, float acc[29]) {
 #pragma unroll
   for (int k = 0; k < 29; ++k) acc[k] = 0.f;
   const int cols = L.vc.cols, N = cols * L.vc.rows;
+  const float inv_cols = 1.0f / (float)cols;
+  const bool small = N < (1 << 24) - gstride;
   for (int i = gtid; i < N; i += gstride) {
-    const int2 c = __ldcg(R.corr + i);
-    if (c.x < 0) continue;
-    const int y = i / cols, x = i - y * cols;
+    const float4 c = __ldcg(R.corr + i);
+    if (__float_as_int(c.w) == kNoCorr) continue;
+    int x, y;
+    pixel_xy(i, cols, inv_cols, small, x, y);
     float row[7];
-    rgb_row(L, R, p, sigma, tiny, x, y, c, row);
+    rgb_row(L, R, sigma, tiny, x, y, c, row);
     icp_add_row(acc, row);
   }
 }
@@ -641,7 +667,7 @@ __global__ void __launch_bounds__(kPThreads, 1) k_icp_persistent(PersistentArgs 
         __syncthreads();
         bool tiny;
         const float sigma = rgb_sigma(s2[0], s2[1], tiny);
-        rgb_rows_pass(L, a.rg[l], pose, sigma, tiny, gtid, gstride, acc);
+        rgb_rows_pass(L, a.rg[l], sigma, tiny, gtid, gstride, acc);
         block_reduce29<kPWarps>(acc, wpart, bsum);
         if (threadIdx.x < 29) fix_add(fxr + (group * 29 + threadIdx.x) * kFixSlots, bsum[threadIdx.x]);
         grid_barrier(a, nb, 2 * it + 1);
@@ -725,7 +751,7 @@ __global__ void __launch_bounds__(kThreads) k_rgb_partials(IcpLevelArgs L, RgbLe
   bool tiny;
   const float sigma = rgb_sigma(__ldcg(res), __ldcg(res + 1), tiny);
   float acc[29];
-  rgb_rows_pass(L, R, p, sigma, tiny, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, acc);
+  rgb_rows_pass(L, R, sigma, tiny, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, acc);
   block_reduce29<kWarps>(acc, wpart, bsum);
   if (threadIdx.x < 29)
     part[(size_t)threadIdx.x * stride + blockIdx.x] = (double)bsum[threadIdx.x].x + (double)bsum[threadIdx.x].y;
@@ -804,7 +830,7 @@ int icp_workspace_rgb(IcpWorkspace &w, size_t pixels) {
   w.cand = nullptr;
   w.rgb_pixels = 0;
   // candidate flags of every level: at most 4/3 of level 0, padded
-  if (cudaMalloc(&w.corr, sizeof(int2) * pixels) != cudaSuccess) return SF_ERR_CUDA;
+  if (cudaMalloc(&w.corr, sizeof(float4) * pixels) != cudaSuccess) return SF_ERR_CUDA;
   if (cudaMalloc(&w.cand, pixels * 2) != cudaSuccess) return SF_ERR_CUDA;
   w.rgb_pixels = pixels;
   return SF_OK;

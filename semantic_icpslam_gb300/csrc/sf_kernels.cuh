@@ -50,10 +50,11 @@ struct IcpLevelArgs {
 // the next and last frames' intensities (uint8), the next frame's
 // derivative images (int16) and candidate flags (uint8, see
 // launch_derivatives), and the per-pixel correspondences of the current
-// iteration (int2 {u | v << 16, diff}, x = -1 when none).
+// iteration (float4: the last frame's vertex in the current camera, and
+// the intensity difference as int bits, INT_MIN when none).
 struct RgbLevelArgs {
   sf_image inext, ilast, dx, dy, cand;
-  int2 *corr;
+  float4 *corr;
 };
 
 struct IcpWorkspace {
@@ -71,7 +72,7 @@ struct IcpWorkspace {
   int profile = 0;                     // record phase clocks when set
   // photometric scratch, grown on demand: correspondences of the largest
   // level, and candidate flags of every level for callers that pass none
-  int2 *corr = nullptr;
+  float4 *corr = nullptr;
   uint8_t *cand = nullptr;
   size_t rgb_pixels = 0;
 };

@@ -136,7 +136,7 @@ struct sf_system {
   // this frame's derivative images and correspondence candidate flags
   uint8_t *d_int[kMaxLevels] = {}, *d_int_last[kMaxLevels] = {}, *d_cand[kMaxLevels] = {};
   int16_t *d_dx[kMaxLevels] = {}, *d_dy[kMaxLevels] = {};
-  int2 *d_corr = nullptr;  // per-iteration correspondences (level-0 size)
+  float4 *d_corr = nullptr;  // per-iteration correspondences (level-0 size)
   float *d_rdepth = nullptr;  // rendered depth (localisation mode's label pass)
   int mapping = 1;            // 0: localisation mode (Tracker::mappingDisabled)
   float *d_zmin = nullptr, *d_zmax = nullptr;
@@ -164,6 +164,10 @@ struct sf_system {
   // overlapping the pyramid and ICP; integration waits for ev_inputs
   cudaStream_t cstream = nullptr;
   cudaEvent_t ev_inputs = nullptr, ev_prev = nullptr;
+  // the photometric term's intensity pyramid runs on its own stream beside
+  // the depth pyramid (fork / join events)
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   // raycast launch shape (sf_system_autotune)
   RaycastTune rc_tune;
   long long frames = 0;  // frames run (any form)
@@ -196,13 +200,16 @@ int alloc_all(sf_system *s) {
            A((void **)&s->d_dx[l], n * 2) && A((void **)&s->d_dy[l], n * 2) &&
            cudaMemset(s->d_int[l], 0, n) == cudaSuccess && cudaMemset(s->d_int_last[l], 0, n) == cudaSuccess;
   }
-  if (ok && s->cfg.rgb_term) ok = A((void **)&s->d_corr, np * sizeof(int2));
+  if (ok && s->cfg.rgb_term) ok = A((void **)&s->d_corr, np * sizeof(float4));
   ok = ok && cudaMallocHost(&s->h_depth16, np * 2) == cudaSuccess &&
        cudaMallocHost(&s->h_rgb, np * 3) == cudaSuccess &&
        cudaMallocHost(&s->h_mask, np) == cudaSuccess &&
        cudaMallocHost(&s->h_stats, sizeof(sf_frame_stats)) == cudaSuccess;
   if (ok) ok = cudaMemset(s->d_mask, 0, np) == cudaSuccess;
   ok = ok && cudaStreamCreateWithFlags(&s->cstream, cudaStreamNonBlocking) == cudaSuccess &&
+       cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) == cudaSuccess &&
+       cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming) == cudaSuccess &&
+       cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming) == cudaSuccess &&
        cudaEventCreateWithFlags(&s->ev_inputs, cudaEventDisableTiming) == cudaSuccess &&
        cudaEventCreateWithFlags(&s->ev_prev, cudaEventDisableTiming) == cudaSuccess;
   return ok ? SF_OK : SF_ERR_CUDA;
@@ -228,6 +235,10 @@ void free_all(sf_system *s) {
   if (s->ev_inputs) cudaEventDestroy(s->ev_inputs);
   if (s->ev_prev) cudaEventDestroy(s->ev_prev);
   if (s->cstream) cudaStreamDestroy(s->cstream);
+  if (s->side) cudaStreamSynchronize(s->side);
+  if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+  if (s->ev_join) cudaEventDestroy(s->ev_join);
+  if (s->side) cudaStreamDestroy(s->side);
 }
 
 // The frame's colour (and mask) upload on the copy stream; captured as an
@@ -271,10 +282,26 @@ void rgb_levels(sf_system *s, RgbLevelArgs *rg) {
   }
 }
 
-// Frame::FillImages depth part (Core/Frame.cc:68-92).
+// Frame::FillImages (Core/Frame.cc:68-92): the depth pyramid, and with the
+// photometric term the intensity pyramid forked onto the side stream so
+// that the two run side by side (joined before this returns).
+void enqueue_depth_pyramid(sf_system *s, cudaStream_t st);
 void enqueue_pyramid(sf_system *s, cudaStream_t st) {
+  if (!s->cfg.rgb_term) {
+    enqueue_depth_pyramid(s, st);
+    return;
+  }
+  cudaEventRecord(s->ev_fork, st);
+  cudaStreamWaitEvent(s->side, s->ev_fork, 0);
+  enqueue_intensity(s, s->side);
+  cudaEventRecord(s->ev_join, s->side);
+  enqueue_depth_pyramid(s, st);
+  cudaStreamWaitEvent(st, s->ev_join, 0);
+}
+
+// Frame::FillImages depth part.
+void enqueue_depth_pyramid(sf_system *s, cudaStream_t st) {
   const int C = s->cfg.cols, R = s->cfg.rows;
-  if (s->cfg.rgb_term) enqueue_intensity(s, st);
   launch_filter_depth(img(s->d_depth16, C, R, 2), img(s->d_raw, C, R, 4), img(s->d_depth[0], C, R, 4),
                       s->cfg.depth_scale, s->cfg.depth_cutoff, st);
   if (s->L >= 2) {
