@@ -145,12 +145,14 @@ def launches(sf):
     return v.value
 
 
-def time_device_resident(sf, ctx, frames, steps, warmup, mode, barrier, timing=False, autotune=False, rgb=0):
+def time_device_resident(sf, ctx, frames, steps, warmup, mode, barrier, timing=False, autotune=False, rgb=0,
+                         ndet=0):
     """Frames/s with inputs already in HBM; CUDA events on the system stream.
     With autotune, sf_system_autotune runs half-way through the warm-up
     (its choice is recaptured in the graph before the timed frames)."""
     import torch
-    dev = [(torch.from_numpy(d).cuda(), torch.from_numpy(c).cuda()) for d, c, _, _ in frames[:steps + warmup]]
+    dev = [(torch.from_numpy(d).cuda(), torch.from_numpy(c).cuda(), torch.from_numpy(m).cuda())
+           for d, c, m, _ in frames[:steps + warmup]]
     torch.cuda.synchronize()
     s = sf.System(ctx, sys_cfg(sf, mode, rgb), init_pose=frames[0][3])
     stage_ms = np.zeros(len(STAGES))
@@ -159,7 +161,7 @@ def time_device_resident(sf, ctx, frames, steps, warmup, mode, barrier, timing=F
         sf.call("sf_system_set_timing", s.h, 1)
     tune = None
     for i in range(warmup):
-        s.grab_device(dev[i][0].data_ptr(), dev[i][1].data_ptr())
+        s.grab_device(dev[i][0].data_ptr(), dev[i][1].data_ptr(), dev[i][2].data_ptr() if ndet else None, ndet)
         if autotune and i == warmup // 2:
             cands, chosen = s.autotune(reps=10)
             tune = {"chosen": {"ctas_per_sm": cands[chosen][0], "tile": [cands[chosen][1], cands[chosen][2]]},
@@ -175,7 +177,7 @@ def time_device_resident(sf, ctx, frames, steps, warmup, mode, barrier, timing=F
     import ctypes as C
     ms = (C.c_float * 7)()
     for i in range(warmup, warmup + steps):
-        s.grab_device(dev[i][0].data_ptr(), dev[i][1].data_ptr())
+        s.grab_device(dev[i][0].data_ptr(), dev[i][1].data_ptr(), dev[i][2].data_ptr() if ndet else None, ndet)
         if timing:
             sf.call("sf_system_stage_ms", s.h, ms)
             stage_ms += np.array(ms[:])
@@ -192,6 +194,34 @@ def time_device_resident(sf, ctx, frames, steps, warmup, mode, barrier, timing=F
     del dev
     return dict(elapsed=elapsed, launches=n_launch, clocks=clocks, stage_ms=stage_ms / max(steps, 1),
                 stats=stats, last=last, autotune=tune)
+
+
+def time_mesh(sf, ctx, frames, n, reps=3):
+    """sf_MeshScene over the map of the whole sequence (Mapping::CreateModel):
+    milliseconds per call (CUDA events on the context stream, mean of reps
+    after one warm-up) and triangles."""
+    import ctypes as C
+    import torch
+    s = sf.System(ctx, sys_cfg(sf, 1), init_pose=frames[0][3])
+    for i in range(n):
+        s.grab(frames[i][0], frames[i][1])
+    m = s.map()
+    cap = 8000000
+    v = torch.empty((cap, 9), dtype=torch.float32, device="cuda")
+    nn = torch.empty((cap, 9), dtype=torch.float32, device="cuda")
+    c = torch.empty((cap, 9), dtype=torch.uint8, device="cuda")
+    k = C.c_uint32()
+    sf.call("sf_MeshScene", ctx.h, m.h, v.data_ptr(), nn.data_ptr(), c.data_ptr(), cap, C.byref(k))
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        sf.call("sf_MeshScene", ctx.h, m.h, v.data_ptr(), nn.data_ptr(), c.data_ptr(), cap, C.byref(k))
+    e1.record(stream)
+    e1.synchronize()
+    blocks = int(m.counters(ctx)[3])
+    s.close()
+    return {"ms": round(e0.elapsed_time(e1) / reps, 3), "triangles": int(k.value), "blocks": blocks}
 
 
 def pinned(a):
@@ -524,6 +554,18 @@ def main():
         if not args.no_plain:
             rp = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 0, barrier, rgb=1)
             out["rgbd"]["plain"] = round(args.steps / rp["elapsed"], 3)
+    if args.config == "c2":
+        # the semantic mode (System.cc:184-205): the same room with ten
+        # labelled objects and 5% label flips, detections every frame
+        import semantic_icpslam_gb300 as sfm
+        syn = sfm.Synth(COLS, ROWS, K, n_objects=10, label_flip=0.05, **SEQ)
+        lframes = [syn.frame(i) for i in range(n)]
+        lab = time_device_resident(sf, ctx, lframes, args.steps, args.warmup, 1, barrier, ndet=10)
+        out["labels"] = {"value": round(args.steps / lab["elapsed"], 3), "unit": "frames/s",
+                         "gpu_launches": int(lab["launches"]),
+                         "mode": "detections every frame (10 objects, 5% label flips): FuseColor, RayTrace, "
+                                 "FuseColor with the labels (label pass + UnifyNeighbor), RayTrace"}
+        out["mesh"] = time_mesh(sf, ctx, frames, args.steps + args.warmup)
     out["pose_err_fp64_max"] = pose_error_fp64(sf, ctx, frames, 6)
     if args.config == "c2":
         out["reloc"] = time_reloc(sf, ctx, frames)

@@ -641,14 +641,43 @@ struct NeighborTable {
   }
 };
 
-__device__ __forceinline__ void unify_column(const DevMap &m, uint32_t *out, int4 h, int tx, int ty) {
+// A block's neighbourhood for the pass: its voxels and the ones whose
+// float positions (pos +- VoxelSize) / VoxelSize can floor to -- offsets
+// -2..+1 from a block voxel, so cells -2..8 per axis (11^3) -- each as
+// {weight > 0, label, count} (0: no neighbour value: a missing block or
+// weight 0), staged in shared memory by the whole CTA with every load in
+// flight; the columns' 26-neighbour walks then read shared memory.
+constexpr int kUnifyHalo = 11;
+constexpr int kUnifyCells = kUnifyHalo * kUnifyHalo * kUnifyHalo;
+
+__device__ __forceinline__ uint32_t unify_cell_value(const DevMap &m, int ptr, i3 v) {
+  if (ptr < 0) return 0u;
+  const uint32_t *w = (const uint32_t *)(m.voxels + ptr + vox2local(v));
+  if ((__ldg(w + 1) & 0xffu) == 0u) return 0u;  // weight 0: label -1
+  return 0x10000u | (__ldg(w + 2) & 0xffffu);    // valid | count << 8 | label
+}
+
+__device__ __forceinline__ void unify_block(const DevMap &m, uint32_t *out, int4 h, uint32_t *cells,
+                                            int *bptr) {
+  const int tx = threadIdx.x & 7, ty = threadIdx.x >> 3;
+  const int bx = (int)((uint32_t)h.x * 8u), by = (int)((uint32_t)h.y * 8u), bz = (int)((uint32_t)h.z * 8u);
+  const int ox = bx - 2, oy = by - 2, oz = bz - 2;  // the neighbourhood's first cell
+  // the 27 blocks around this one (cells -2..-1 in block -1, 8 in block +1)
+  if (threadIdx.x < 27) {
+    const int dx = threadIdx.x % 3 - 1, dy = (threadIdx.x / 3) % 3 - 1, dz = threadIdx.x / 9 - 1;
+    bptr[threadIdx.x] = (dx | dy | dz) == 0 ? h.w : find_block(m, mk_i3(h.x + dx, h.y + dy, h.z + dz));
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < kUnifyCells; c += blockDim.x) {
+    const int ix = c % kUnifyHalo, iy = (c / kUnifyHalo) % kUnifyHalo, iz = c / (kUnifyHalo * kUnifyHalo);
+    const int sx = ix < 2 ? 0 : (ix < 10 ? 1 : 2), sy = iy < 2 ? 0 : (iy < 10 ? 1 : 2), sz = iz < 2 ? 0 : (iz < 10 ? 1 : 2);
+    cells[c] = unify_cell_value(m, bptr[sx + 3 * sy + 9 * sz], mk_i3(ox + ix, oy + iy, oz + iz));
+  }
+  __syncthreads();
   const float vs = m.c.voxel_size;
   const float step = vs * (float)1;  // VoxelSize * r, r = 1
-  const int bx = (int)((uint32_t)h.x * 8u), by = (int)((uint32_t)h.y * 8u), bz = (int)((uint32_t)h.z * 8u);
   const AxisCands cx((float)(bx + tx) * vs, step, vs), cy((float)(by + ty) * vs, step, vs);
   NeighborTable t;
-  i3 cache_pos = mk_i3(h.x, h.y, h.z);
-  int cache_ptr = h.w;
   for (int i = 0; i < 8; ++i) {
     const int idx = h.w + i * 64 + ty * 8 + tx;
     const uint32_t *cw = (const uint32_t *)(m.voxels + idx);
@@ -659,22 +688,17 @@ __device__ __forceinline__ void unify_column(const DevMap &m, uint32_t *out, int
       const AxisCands cz((float)(bz + i) * vs, step, vs);
       for (int k = 0; k < 26; ++k) {
         const unsigned o = kUnifyOrder[k];
-        const i3 v = mk_i3(cx.at(o & 3u), cy.at((o >> 2) & 3u), cz.at((o >> 4) & 3u));
-        const i3 b = vox2block(v);
-        int ptr;
-        if (b.x == cache_pos.x && b.y == cache_pos.y && b.z == cache_pos.z) {
-          ptr = cache_ptr;
-        } else {
-          ptr = find_block(m, b);
-          cache_pos = b;
-          cache_ptr = ptr;
+        const int vx = cx.at(o & 3u), vy = cy.at((o >> 2) & 3u), vz = cz.at((o >> 4) & 3u);
+        const unsigned qx = (unsigned)(vx - ox), qy = (unsigned)(vy - oy), qz = (unsigned)(vz - oz);
+        uint32_t cv;
+        if (qx < (unsigned)kUnifyHalo && qy < (unsigned)kUnifyHalo && qz < (unsigned)kUnifyHalo) {
+          cv = cells[(qz * kUnifyHalo + qy) * kUnifyHalo + qx];
+        } else {  // outside the staged cells (not reached for |coordinates| < 2^21): the table
+          const i3 v = mk_i3(vx, vy, vz);
+          cv = unify_cell_value(m, find_block(m, vox2block(v)), v);
         }
-        if (ptr < 0) continue;
-        const uint32_t *nw = (const uint32_t *)(m.voxels + ptr + vox2local(v));
-        if ((__ldg(nw + 1) & 0xffu) == 0u) continue;  // weight 0: label -1
-        const uint32_t n2 = __ldg(nw + 2);
-        const int lab = (int)(n2 & 0xffu), cnt = (int)((n2 >> 8) & 0xffu);
-        t.add(lab, cnt);
+        if (cv == 0u) continue;
+        t.add((int)(cv & 0xffu), (int)((cv >> 8) & 0xffu));
       }
       int nei_label = -1, nei_count = 0, nei_lc = 0;
       t.pick(t.l0, t.c0, t.lc0, nei_label, nei_count, nei_lc);
@@ -692,6 +716,7 @@ __device__ __forceinline__ void unify_column(const DevMap &m, uint32_t *out, int
     }
     out[idx] = res;
   }
+  __syncthreads();  // before the cells are restaged
 }
 
 __global__ void __launch_bounds__(kUnifyThreads) k_unify_compute(DevMap m, uint32_t *out, const int *run_flag) {
@@ -699,7 +724,8 @@ __global__ void __launch_bounds__(kUnifyThreads) k_unify_compute(DevMap m, uint3
   const unsigned n = min(*m.no_visible, m.c.num_entries);
   __shared__ int4 s_head[kUnifyThreads];
   __shared__ int s_cnt;
-  const int tx = threadIdx.x & 7, ty = threadIdx.x >> 3;
+  __shared__ uint32_t s_cells[kUnifyCells];
+  __shared__ int s_bptr[27];
   for (unsigned base = blockIdx.x * kUnifyThreads; base < n; base += gridDim.x * kUnifyThreads) {
     const unsigned e = base + threadIdx.x;
     const int4 h = e < n ? entry_head(m.entries + e) : make_int4(0, 0, 0, -1);
@@ -708,7 +734,7 @@ __global__ void __launch_bounds__(kUnifyThreads) k_unify_compute(DevMap m, uint3
     if (h.w != -1) s_head[atomicAdd(&s_cnt, 1)] = h;  // entries are independent: order free
     __syncthreads();
     const int cnt = s_cnt;
-    for (int k = 0; k < cnt; ++k) unify_column(m, out, s_head[k], tx, ty);
+    for (int k = 0; k < cnt; ++k) unify_block(m, out, s_head[k], s_cells, s_bptr);
     __syncthreads();
   }
 }
