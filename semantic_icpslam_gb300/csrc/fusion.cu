@@ -585,9 +585,9 @@ constexpr int kUnifyThreads = 64;
 
 // UnifyNeighbor's 26 offsets in its order (FuseMap.cu:834-887), as
 // (dx + 1) | (dy + 1) << 2 | (dz + 1) << 4.
-__constant__ uint8_t kUnifyOrder[26] = {
-    0x16, 0x1a, 0x12, 0x26, 0x06, 0x2a, 0x0a, 0x22, 0x02, 0x14, 0x18, 0x10, 0x24,
-    0x04, 0x28, 0x08, 0x20, 0x00, 0x19, 0x29, 0x09, 0x11, 0x21, 0x01, 0x25, 0x05};
+__device__ __forceinline__ constexpr unsigned unify_order(int k) {
+  return k == 0 ? 0x16u : k == 1 ? 0x1au : k == 2 ? 0x12u : k == 3 ? 0x26u : k == 4 ? 0x06u : k == 5 ? 0x2au : k == 6 ? 0x0au : k == 7 ? 0x22u : k == 8 ? 0x02u : k == 9 ? 0x14u : k == 10 ? 0x18u : k == 11 ? 0x10u : k == 12 ? 0x24u : k == 13 ? 0x04u : k == 14 ? 0x28u : k == 15 ? 0x08u : k == 16 ? 0x20u : k == 17 ? 0x00u : k == 18 ? 0x19u : k == 19 ? 0x29u : k == 20 ? 0x09u : k == 21 ? 0x11u : k == 22 ? 0x21u : k == 23 ? 0x01u : k == 24 ? 0x25u : 0x05u;
+}
 
 // make_int3(float) on one axis: floor (VectorMath.h:36-42).
 __device__ __forceinline__ int floor1i(float a) {
@@ -652,9 +652,9 @@ constexpr int kUnifyCells = kUnifyHalo * kUnifyHalo * kUnifyHalo;
 
 __device__ __forceinline__ uint32_t unify_cell_value(const DevMap &m, int ptr, i3 v) {
   if (ptr < 0) return 0u;
-  const uint32_t *w = (const uint32_t *)(m.voxels + ptr + vox2local(v));
-  if ((__ldg(w + 1) & 0xffu) == 0u) return 0u;  // weight 0: label -1
-  return 0x10000u | (__ldg(w + 2) & 0xffffu);    // valid | count << 8 | label
+  const uint4 w = __ldg((const uint4 *)(m.voxels + ptr + vox2local(v)));
+  if ((w.y & 0xffu) == 0u) return 0u;  // weight 0: label -1
+  return 0x10000u | (w.z & 0xffffu);   // valid | count << 8 | label
 }
 
 __device__ __forceinline__ void unify_block(const DevMap &m, uint32_t *out, int4 h, uint32_t *cells,
@@ -668,38 +668,77 @@ __device__ __forceinline__ void unify_block(const DevMap &m, uint32_t *out, int4
     bptr[threadIdx.x] = (dx | dy | dz) == 0 ? h.w : find_block(m, mk_i3(h.x + dx, h.y + dy, h.z + dz));
   }
   __syncthreads();
-  for (int c = threadIdx.x; c < kUnifyCells; c += blockDim.x) {
-    const int ix = c % kUnifyHalo, iy = (c / kUnifyHalo) % kUnifyHalo, iz = c / (kUnifyHalo * kUnifyHalo);
-    const int sx = ix < 2 ? 0 : (ix < 10 ? 1 : 2), sy = iy < 2 ? 0 : (iy < 10 ? 1 : 2), sz = iz < 2 ? 0 : (iz < 10 ? 1 : 2);
-    cells[c] = unify_cell_value(m, bptr[sx + 3 * sy + 9 * sz], mk_i3(ox + ix, oy + iy, oz + iz));
+  // four cells per thread per round, their loads issued together
+  constexpr int kRound = 4 * kUnifyThreads;
+  for (int c0 = 0; c0 < kUnifyCells; c0 += kRound) {
+    uint4 w[4];
+    int cell[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int c = c0 + q * kUnifyThreads + threadIdx.x;
+      cell[q] = -1;
+      w[q] = make_uint4(0u, 0u, 0u, 0u);
+      if (c < kUnifyCells) {
+        const int ix = c % kUnifyHalo, iy = (c / kUnifyHalo) % kUnifyHalo, iz = c / (kUnifyHalo * kUnifyHalo);
+        const int sx = ix < 2 ? 0 : (ix < 10 ? 1 : 2), sy = iy < 2 ? 0 : (iy < 10 ? 1 : 2);
+        const int sz = iz < 2 ? 0 : (iz < 10 ? 1 : 2);
+        const int ptr = bptr[sx + 3 * sy + 9 * sz];
+        cell[q] = c;
+        if (ptr >= 0) {
+          w[q] = __ldg((const uint4 *)(m.voxels + ptr + vox2local(mk_i3(ox + ix, oy + iy, oz + iz))));
+          w[q].x = 1u;  // found
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (cell[q] >= 0)
+        cells[cell[q]] = (w[q].x == 0u || (w[q].y & 0xffu) == 0u) ? 0u : (0x10000u | (w[q].z & 0xffffu));
   }
   __syncthreads();
   const float vs = m.c.voxel_size;
   const float step = vs * (float)1;  // VoxelSize * r, r = 1
   const AxisCands cx((float)(bx + tx) * vs, step, vs), cy((float)(by + ty) * vs, step, vs);
   NeighborTable t;
+  // the column's own label word, each loaded one voxel ahead (its weight
+  // is in the staged cells: valid = weight > 0)
+  const uint32_t *own = (const uint32_t *)(m.voxels + h.w + ty * 8 + tx) + 2;
+  uint32_t next = __ldg(own);
+#pragma unroll 1
   for (int i = 0; i < 8; ++i) {
     const int idx = h.w + i * 64 + ty * 8 + tx;
-    const uint32_t *cw = (const uint32_t *)(m.voxels + idx);
-    const uint32_t w1 = __ldg(cw + 1), w2 = __ldg(cw + 2);
+    const uint32_t w2 = next;
+    if (i < 7) next = __ldg(own + (i + 1) * 64 * 4);
     uint32_t res = w2;
-    if ((w1 & 0xffu) != 0u) {
+    if (cells[((i + 2) * kUnifyHalo + ty + 2) * kUnifyHalo + tx + 2] != 0u) {
       const int cur_label = (int)(w2 & 0xffu);
       const AxisCands cz((float)(bz + i) * vs, step, vs);
+      // the 26 neighbour values first (independent shared-memory reads, all
+      // in flight), then the table updates in UnifyNeighbor's order
+      uint32_t nv[26];
+      bool outside = false;
+#pragma unroll
       for (int k = 0; k < 26; ++k) {
-        const unsigned o = kUnifyOrder[k];
-        const int vx = cx.at(o & 3u), vy = cy.at((o >> 2) & 3u), vz = cz.at((o >> 4) & 3u);
-        const unsigned qx = (unsigned)(vx - ox), qy = (unsigned)(vy - oy), qz = (unsigned)(vz - oz);
-        uint32_t cv;
-        if (qx < (unsigned)kUnifyHalo && qy < (unsigned)kUnifyHalo && qz < (unsigned)kUnifyHalo) {
-          cv = cells[(qz * kUnifyHalo + qy) * kUnifyHalo + qx];
-        } else {  // outside the staged cells (not reached for |coordinates| < 2^21): the table
-          const i3 v = mk_i3(vx, vy, vz);
-          cv = unify_cell_value(m, find_block(m, vox2block(v)), v);
-        }
-        if (cv == 0u) continue;
-        t.add((int)(cv & 0xffu), (int)((cv >> 8) & 0xffu));
+        const unsigned o = unify_order(k);
+        const unsigned qx = (unsigned)(cx.at(o & 3u) - ox), qy = (unsigned)(cy.at((o >> 2) & 3u) - oy);
+        const unsigned qz = (unsigned)(cz.at((o >> 4) & 3u) - oz);
+        const bool in = qx < (unsigned)kUnifyHalo && qy < (unsigned)kUnifyHalo && qz < (unsigned)kUnifyHalo;
+        outside |= !in;
+        nv[k] = in ? cells[(qz * kUnifyHalo + qy) * kUnifyHalo + qx] : 0u;
       }
+      if (outside) {  // a position outside the staged cells (not reached for |coordinates| < 2^21): the table
+#pragma unroll
+        for (int k = 0; k < 26; ++k) {
+          const unsigned o = unify_order(k);
+          const i3 v = mk_i3(cx.at(o & 3u), cy.at((o >> 2) & 3u), cz.at((o >> 4) & 3u));
+          const unsigned qx = (unsigned)(v.x - ox), qy = (unsigned)(v.y - oy), qz = (unsigned)(v.z - oz);
+          if (!(qx < (unsigned)kUnifyHalo && qy < (unsigned)kUnifyHalo && qz < (unsigned)kUnifyHalo))
+            nv[k] = unify_cell_value(m, find_block(m, vox2block(v)), v);
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 26; ++k)
+        if (nv[k] != 0u) t.add((int)(nv[k] & 0xffu), (int)((nv[k] >> 8) & 0xffu));
       int nei_label = -1, nei_count = 0, nei_lc = 0;
       t.pick(t.l0, t.c0, t.lc0, nei_label, nei_count, nei_lc);
       t.pick(t.l1, t.c1, t.lc1, nei_label, nei_count, nei_lc);
@@ -719,28 +758,33 @@ __device__ __forceinline__ void unify_block(const DevMap &m, uint32_t *out, int4
   __syncthreads();  // before the cells are restaged
 }
 
-__global__ void __launch_bounds__(kUnifyThreads) k_unify_compute(DevMap m, uint32_t *out, const int *run_flag) {
+// The allocated entries among hash slots [0, visible count), in any order
+// (each block's pass is independent): list[0..*count).
+__global__ void k_unify_list(DevMap m, int *list, unsigned *count, const int *run_flag) {
   if (run_flag && *run_flag == 0) return;
   const unsigned n = min(*m.no_visible, m.c.num_entries);
-  __shared__ int4 s_head[kUnifyThreads];
-  __shared__ int s_cnt;
-  __shared__ uint32_t s_cells[kUnifyCells];
-  __shared__ int s_bptr[27];
-  for (unsigned base = blockIdx.x * kUnifyThreads; base < n; base += gridDim.x * kUnifyThreads) {
+  for (unsigned base = blockIdx.x * blockDim.x; base < n; base += grid_stride()) {
     const unsigned e = base + threadIdx.x;
-    const int4 h = e < n ? entry_head(m.entries + e) : make_int4(0, 0, 0, -1);
-    if (threadIdx.x == 0) s_cnt = 0;
-    __syncthreads();
-    if (h.w != -1) s_head[atomicAdd(&s_cnt, 1)] = h;  // entries are independent: order free
-    __syncthreads();
-    const int cnt = s_cnt;
-    for (int k = 0; k < cnt; ++k) unify_block(m, out, s_head[k], s_cells, s_bptr);
-    __syncthreads();
+    const bool occ = e < n && __ldcg(&m.entries[e].ptr) >= 0;
+    const unsigned slot = warp_append(count, occ);
+    if (occ) list[slot] = (int)e;
   }
 }
 
-__global__ void k_unify_apply(DevMap m, const uint32_t *out, const int *run_flag) {
+// One CTA per listed block.
+__global__ void __launch_bounds__(kUnifyThreads) k_unify_compute(DevMap m, uint32_t *out, const int *list,
+                                                                  const unsigned *count, const int *run_flag) {
   if (run_flag && *run_flag == 0) return;
+  __shared__ uint32_t s_cells[kUnifyCells];
+  __shared__ int s_bptr[27];
+  const unsigned n = __ldcg(count);
+  for (unsigned j = blockIdx.x; j < n; j += gridDim.x)
+    unify_block(m, out, entry_head(m.entries + __ldcg(list + j)), s_cells, s_bptr);
+}
+
+__global__ void k_unify_apply(DevMap m, const uint32_t *out, unsigned *list_count, const int *run_flag) {
+  if (run_flag && *run_flag == 0) return;
+  if (grid_tid() == 0) *list_count = 0u;  // the compute pass has read it; zero for the next pass
   const unsigned n = min(*m.no_visible, m.c.num_entries);
   const unsigned lane = threadIdx.x & 31u;
   const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -912,14 +956,22 @@ void launch_visibility(const DevMap &m, const FuseScratch &f, const Cam *c, cons
 }
 
 void launch_unify_neighbor(const DevMap &m, const FuseScratch &f, const int *run_flag, cudaStream_t s) {
-  k_unify_compute<<<sm_count() * 16, kUnifyThreads, 0, s>>>(m, f.unify_out, run_flag); note_launch();
-  k_unify_apply<<<sm_count() * 4, 256, 0, s>>>(m, f.unify_out, run_flag); note_launch();
+  k_unify_list<<<sm_count() * 4, 256, 0, s>>>(m, f.unify_list, f.unify_count, run_flag); note_launch();
+  k_unify_compute<<<sm_count() * 16, kUnifyThreads, 0, s>>>(m, f.unify_out, f.unify_list, f.unify_count,
+                                                             run_flag); note_launch();
+  k_unify_apply<<<sm_count() * 4, 256, 0, s>>>(m, f.unify_out, f.unify_count, run_flag); note_launch();
 }
 
 int fuse_scratch_unify(FuseScratch &f, const MapConst &c) {
   if (f.unify_out) return SF_OK;
-  const size_t bytes = sizeof(uint32_t) * 512 * (size_t)c.num_sdf_blocks;
-  return cudaMalloc(&f.unify_out, bytes) == cudaSuccess ? SF_OK : SF_ERR_CUDA;
+  const size_t words = 512 * (size_t)c.num_sdf_blocks;
+  // the new label words, then the block list and its count
+  if (cudaMalloc(&f.unify_out, sizeof(uint32_t) * (words + c.num_sdf_blocks + 1)) != cudaSuccess) return SF_ERR_CUDA;
+  f.unify_list = reinterpret_cast<int *>(f.unify_out + words);
+  f.unify_count = reinterpret_cast<unsigned *>(f.unify_out + words + c.num_sdf_blocks);
+  // zero before first use (the apply pass zeroes it for the next pass)
+  if (cudaMemset(f.unify_count, 0, sizeof(unsigned)) != cudaSuccess) return SF_ERR_CUDA;
+  return cudaDeviceSynchronize() == cudaSuccess ? SF_OK : SF_ERR_CUDA;
 }
 
 void launch_integrate(const DevMap &m, const sf_image &depth, const sf_image &rgb,

@@ -146,6 +146,8 @@ struct FuseScratch {
   // UnifyNeighbor's new {label, count, label_2, count_2} words, indexed like
   // the voxel array; allocated on the first pass with labels.
   uint32_t *unify_out = nullptr;          // [num_sdf_blocks * 512]
+  int *unify_list = nullptr;              // [num_sdf_blocks] blocks of the pass (inside unify_out's allocation)
+  unsigned *unify_count = nullptr;        // [1]
 };
 
 // Start of a frame's allocation pass: clears the per-frame counters and
@@ -190,7 +192,8 @@ void launch_visibility(const DevMap &m, const FuseScratch &f, const Cam *c, cons
 void launch_mesh(const DevMap &m, float3 *vert, float3 *norm, uchar3 *col, uint32_t max_tri, uint32_t *count,
                  cudaStream_t s);
 // Fusion::UnifyNeighbor over hash slots [0, *no_visible) from the pass-start
-// state (two launches); needs fuse_scratch_unify first.
+// state (three launches: the block list, the pass, the copy back); needs
+// fuse_scratch_unify first.
 int fuse_scratch_unify(FuseScratch &f, const MapConst &c);
 void launch_unify_neighbor(const DevMap &m, const FuseScratch &f, const int *run_flag, cudaStream_t s);
 void launch_integrate(const DevMap &m, const sf_image &depth, const sf_image &rgb,
