@@ -168,6 +168,15 @@ struct sf_system {
   // the depth pyramid (fork / join events)
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // A device-driven frame with mapping takes its stats before the final
+  // RayTrace (which changes none of them); the graph form also copies them
+  // to h_stats there and records ev_stats, so sf_system_grab returns while
+  // the raycast and ResizeMap still run and the next frame's uploads and
+  // launch overlap them.
+  cudaEvent_t ev_stats = nullptr;
+  bool capturing = false;    // enqueue_device_frame is being captured
+  bool stats_taken = false;  // this frame's enqueue took the stats early
+  bool graph_early = false;  // the frame graph records ev_stats
   // raycast launch shape (sf_system_autotune)
   RaycastTune rc_tune;
   long long frames = 0;  // frames run (any form)
@@ -211,7 +220,8 @@ int alloc_all(sf_system *s) {
        cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming) == cudaSuccess &&
        cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming) == cudaSuccess &&
        cudaEventCreateWithFlags(&s->ev_inputs, cudaEventDisableTiming) == cudaSuccess &&
-       cudaEventCreateWithFlags(&s->ev_prev, cudaEventDisableTiming) == cudaSuccess;
+       cudaEventCreateWithFlags(&s->ev_prev, cudaEventDisableTiming) == cudaSuccess &&
+       cudaEventCreateWithFlags(&s->ev_stats, cudaEventDisableTiming) == cudaSuccess;
   return ok ? SF_OK : SF_ERR_CUDA;
 }
 
@@ -234,6 +244,7 @@ void free_all(sf_system *s) {
   if (s->cstream) cudaStreamSynchronize(s->cstream);
   if (s->ev_inputs) cudaEventDestroy(s->ev_inputs);
   if (s->ev_prev) cudaEventDestroy(s->ev_prev);
+  if (s->ev_stats) cudaEventDestroy(s->ev_stats);
   if (s->cstream) cudaStreamDestroy(s->cstream);
   if (s->side) cudaStreamSynchronize(s->side);
   if (s->ev_fork) cudaEventDestroy(s->ev_fork);
@@ -342,12 +353,24 @@ void icp_levels(sf_system *s, IcpLevelArgs *lv) {
   }
 }
 
+// The frame's stats (k_sys_stats); in a captured frame also their copy to
+// h_stats and ev_stats.
+cudaError_t enqueue_stats(sf_system *s, cudaStream_t st) {
+  k_sys_stats<<<1, 1, 0, st>>>(s->d_sys, ctx_icp(s->ctx).ctl, map_dev(s->map), ctx_flags(s->ctx), s->d_stats);
+  note_launch();
+  if (!s->capturing) return cudaGetLastError();
+  cudaError_t e = cudaMemcpyAsync(s->h_stats, s->d_stats, sizeof(sf_frame_stats), cudaMemcpyDeviceToHost, st);
+  return e != cudaSuccess ? e : cudaEventRecordWithFlags(s->ev_stats, st, cudaEventRecordExternal);
+}
+
 // Mapping::FuseColor (FuseMapColor) and Mapping::RayTrace of the frame's
 // mapping stage.  `first` marks the stage boundaries and joins the colour
 // upload; `plain` downloads the visible count and skips the integration
-// when it is zero, as FuseMapColor does (FuseMap.cu:1116-1120).
+// when it is zero, as FuseMapColor does (FuseMap.cu:1116-1120).  `last`:
+// the frame's final pass, whose raycast a device-driven frame's stats
+// precede.
 int fuse_and_raytrace(sf_system *s, const Cam *cam, const int *run, int num_detection, const sf_image &nmap,
-                      bool first, bool plain, cudaStream_t st) {
+                      bool first, bool last, bool plain, cudaStream_t st) {
   const int C = s->cfg.cols, R = s->cfg.rows;
   DevMap &m = map_dev(s->map);
   FuseScratch &f = map_scratch(s->map);
@@ -378,6 +401,10 @@ int fuse_and_raytrace(sf_system *s, const Cam *cam, const int *run, int num_dete
     if (num_detection > 0) launch_unify_neighbor(m, f, run, st);  // FuseMap.cu:1141-1160
   }
   if (first) mark(s, st, 5);
+  if (last && !plain) {
+    if (enqueue_stats(s, st) != cudaSuccess) return SF_ERR_CUDA;
+    s->stats_taken = true;
+  }
   sf_image fv = img(s->d_vmap[0], C, R, 16), fn = img(s->d_nmap[0], C, R, 16);
   launch_raycast(m, f, img(s->d_mv[0], C, R, 16), img(s->d_mn[0], C, R, 16), zmin, zmax, cam,
                  f.counters + 3, &fv, &fn, run, st, s->rc_tune);
@@ -402,8 +429,9 @@ int enqueue_mapping(sf_system *s, const Cam *cam, const int *run, int num_detect
   const sf_image mn0 = img(s->d_mn[0], C, R, 16);
   int e = SF_OK;
   if (s->mapping) {
-    e = fuse_and_raytrace(s, cam, run, 0, img(s->d_nmap[0], C, R, 16), true, plain, st);
-    if (e == SF_OK && num_detection > 0) e = fuse_and_raytrace(s, cam, run, num_detection, mn0, false, plain, st);
+    e = fuse_and_raytrace(s, cam, run, 0, img(s->d_nmap[0], C, R, 16), true, num_detection == 0, plain, st);
+    if (e == SF_OK && num_detection > 0)
+      e = fuse_and_raytrace(s, cam, run, num_detection, mn0, false, true, plain, st);
   } else {
     sf_image zmin = img(s->d_zmin, s->zc, s->zr, 4), zmax = img(s->d_zmax, s->zc, s->zr, 4);
     mark(s, st, 3);
@@ -449,9 +477,14 @@ cudaError_t enqueue_device_frame(sf_system *s, int num_detection, cudaStream_t s
   if (e != cudaSuccess) return e;
   k_sys_post<<<1, 1, 0, st>>>(s->d_sys, w.ctl, s->tmpl, map_scratch(s->map)); note_launch();
   mark(s, st, 2);
-  enqueue_mapping(s, dev_field<Cam>(s->d_sys, offsetof(SysDev, cam)),
-                  dev_field<int>(s->d_sys, offsetof(SysDev, run)), num_detection, false, st);
-  k_sys_stats<<<1, 1, 0, st>>>(s->d_sys, w.ctl, map_dev(s->map), ctx_flags(s->ctx), s->d_stats); note_launch();
+  s->stats_taken = false;
+  if (enqueue_mapping(s, dev_field<Cam>(s->d_sys, offsetof(SysDev, cam)),
+                      dev_field<int>(s->d_sys, offsetof(SysDev, run)), num_detection, false, st) != SF_OK)
+    return cudaErrorUnknown;
+  if (!s->stats_taken) {
+    e = enqueue_stats(s, st);
+    if (e != cudaSuccess) return e;
+  }
   mark(s, st, 7);
   return cudaGetLastError();
 }
@@ -553,7 +586,10 @@ int run_frame(sf_system *s, int num_detection) {
     cudaGraph_t g = nullptr;
     const unsigned long long before = launches_total();
     if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return SF_ERR_CUDA;
+    s->capturing = true;
+    s->graph_early = false;
     cudaError_t e = enqueue_device_frame(s, num_detection, st);
+    s->capturing = false;
     cudaError_t e2 = cudaStreamEndCapture(st, &g);
     // captured launches are recorded, not run: count them per replay instead
     s->graph_kernels = launches_total() - before;
@@ -568,6 +604,7 @@ int run_frame(sf_system *s, int num_detection) {
     if (e != cudaSuccess) { s->gexec = nullptr; return SF_ERR_CUDA; }
     s->graph_sem = sem;
     s->graph_mapping = s->mapping;
+    s->graph_early = true;  // every captured frame copies its stats and records ev_stats
     s->num_detection_captured = num_detection;
   }
   if (cudaGraphLaunch(s->gexec, st) != cudaSuccess) return SF_ERR_CUDA;
@@ -659,10 +696,13 @@ int sf_system_grab(sf_system *s, const uint16_t *depth, const uint8_t *rgb, cons
   if (cudaEventRecord(s->ev_inputs, s->cstream) != cudaSuccess) return SF_ERR_CUDA;
   int r = run_frame(s, num_detection);
   if (r) return r;
-  if (cudaMemcpyAsync(s->h_stats, s->d_stats, sizeof(sf_frame_stats), cudaMemcpyDeviceToHost, st) !=
-          cudaSuccess ||
-      cudaStreamSynchronize(st) != cudaSuccess)
+  if (s->cfg.use_graph == 1 && s->graph_early) {  // the graph copied them before its final raycast
+    if (cudaEventSynchronize(s->ev_stats) != cudaSuccess) return SF_ERR_CUDA;
+  } else if (cudaMemcpyAsync(s->h_stats, s->d_stats, sizeof(sf_frame_stats), cudaMemcpyDeviceToHost, st) !=
+                 cudaSuccess ||
+             cudaStreamSynchronize(st) != cudaSuccess) {
     return SF_ERR_CUDA;
+  }
   if (stats) *stats = *s->h_stats;
   return SF_OK;
 }
