@@ -76,8 +76,10 @@ __global__ void k_sys_post(SysDev *s, const TrackCtl *ctl, Cam tmpl, FuseScratch
   s->cam = c;
 }
 
+// `host_out` (pinned host memory, or null) receives a copy: a store from
+// the kernel costs the frame less than a copy node.
 __global__ void k_sys_stats(const SysDev *s, const TrackCtl *ctl, DevMap m, const uint32_t *flags,
-                            sf_frame_stats *out) {
+                            sf_frame_stats *out, sf_frame_stats *host_out) {
   sf_frame_stats st;
   st.tracked = s->run;
   st.accepted = s->accepted;
@@ -99,6 +101,7 @@ __global__ void k_sys_stats(const SysDev *s, const TrackCtl *ctl, DevMap m, cons
   st.flags = *flags;
   for (int k = 0; k < 16; ++k) st.pose[k] = s->last_pose[k];
   *out = st;
+  if (host_out) *host_out = st;
 }
 
 template <class T>
@@ -353,14 +356,14 @@ void icp_levels(sf_system *s, IcpLevelArgs *lv) {
   }
 }
 
-// The frame's stats (k_sys_stats); in a captured frame also their copy to
-// h_stats and ev_stats.
+// The frame's stats (k_sys_stats); in a captured frame also written to
+// h_stats (pinned, device-accessible) and followed by ev_stats.
 cudaError_t enqueue_stats(sf_system *s, cudaStream_t st) {
-  k_sys_stats<<<1, 1, 0, st>>>(s->d_sys, ctx_icp(s->ctx).ctl, map_dev(s->map), ctx_flags(s->ctx), s->d_stats);
+  k_sys_stats<<<1, 1, 0, st>>>(s->d_sys, ctx_icp(s->ctx).ctl, map_dev(s->map), ctx_flags(s->ctx), s->d_stats,
+                               s->capturing ? s->h_stats : nullptr);
   note_launch();
   if (!s->capturing) return cudaGetLastError();
-  cudaError_t e = cudaMemcpyAsync(s->h_stats, s->d_stats, sizeof(sf_frame_stats), cudaMemcpyDeviceToHost, st);
-  return e != cudaSuccess ? e : cudaEventRecordWithFlags(s->ev_stats, st, cudaEventRecordExternal);
+  return cudaEventRecordWithFlags(s->ev_stats, st, cudaEventRecordExternal);
 }
 
 // Mapping::FuseColor (FuseMapColor) and Mapping::RayTrace of the frame's
@@ -564,7 +567,8 @@ int run_plain_frame(sf_system *s, int num_detection) {
     int e = enqueue_mapping(s, dev_field<Cam>(s->d_sys, offsetof(SysDev, cam)), nullptr, num_detection, true, st);
     if (e != SF_OK) return e;
   }
-  k_sys_stats<<<1, 1, 0, st>>>(s->d_sys, w.ctl, map_dev(s->map), ctx_flags(s->ctx), s->d_stats); note_launch();
+  k_sys_stats<<<1, 1, 0, st>>>(s->d_sys, w.ctl, map_dev(s->map), ctx_flags(s->ctx), s->d_stats, nullptr);
+  note_launch();
   return cudaGetLastError() == cudaSuccess ? SF_OK : SF_ERR_CUDA;
 }
 
