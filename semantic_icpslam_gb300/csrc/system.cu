@@ -76,10 +76,11 @@ __global__ void k_sys_post(SysDev *s, const TrackCtl *ctl, Cam tmpl, FuseScratch
   s->cam = c;
 }
 
-// `host_out` (pinned host memory, or null) receives a copy: a store from
-// the kernel costs the frame less than a copy node.
+// `host_out` (pinned host memory, or null) receives a copy, and then
+// *host_ready = 1 (stores from the kernel cost the frame less than a copy
+// node and an event).
 __global__ void k_sys_stats(const SysDev *s, const TrackCtl *ctl, DevMap m, const uint32_t *flags,
-                            sf_frame_stats *out, sf_frame_stats *host_out) {
+                            sf_frame_stats *out, sf_frame_stats *host_out, uint32_t *host_ready) {
   sf_frame_stats st;
   st.tracked = s->run;
   st.accepted = s->accepted;
@@ -101,7 +102,11 @@ __global__ void k_sys_stats(const SysDev *s, const TrackCtl *ctl, DevMap m, cons
   st.flags = *flags;
   for (int k = 0; k < 16; ++k) st.pose[k] = s->last_pose[k];
   *out = st;
-  if (host_out) *host_out = st;
+  if (host_out) {
+    *host_out = st;
+    __threadfence_system();  // the stats before the flag, as the host sees them
+    *(volatile uint32_t *)host_ready = 1u;
+  }
 }
 
 template <class T>
@@ -172,14 +177,14 @@ struct sf_system {
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   // A device-driven frame with mapping takes its stats before the final
-  // RayTrace (which changes none of them); the graph form also copies them
-  // to h_stats there and records ev_stats, so sf_system_grab returns while
-  // the raycast and ResizeMap still run and the next frame's uploads and
-  // launch overlap them.
-  cudaEvent_t ev_stats = nullptr;
+  // RayTrace (which changes none of them); the graph form also writes them
+  // to h_stats there and then sets *h_ready, so sf_system_grab returns
+  // while the raycast and ResizeMap still run and the next frame's uploads
+  // and launch overlap them.
+  uint32_t *h_ready = nullptr;  // pinned; zeroed before each graph launch
   bool capturing = false;    // enqueue_device_frame is being captured
   bool stats_taken = false;  // this frame's enqueue took the stats early
-  bool graph_early = false;  // the frame graph records ev_stats
+  bool graph_early = false;  // the frame graph writes h_stats and h_ready
   // raycast launch shape (sf_system_autotune)
   RaycastTune rc_tune;
   long long frames = 0;  // frames run (any form)
@@ -216,15 +221,15 @@ int alloc_all(sf_system *s) {
   ok = ok && cudaMallocHost(&s->h_depth16, np * 2) == cudaSuccess &&
        cudaMallocHost(&s->h_rgb, np * 3) == cudaSuccess &&
        cudaMallocHost(&s->h_mask, np) == cudaSuccess &&
-       cudaMallocHost(&s->h_stats, sizeof(sf_frame_stats)) == cudaSuccess;
+       cudaMallocHost(&s->h_stats, sizeof(sf_frame_stats)) == cudaSuccess &&
+       cudaMallocHost(&s->h_ready, sizeof(uint32_t)) == cudaSuccess;
   if (ok) ok = cudaMemset(s->d_mask, 0, np) == cudaSuccess;
   ok = ok && cudaStreamCreateWithFlags(&s->cstream, cudaStreamNonBlocking) == cudaSuccess &&
        cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) == cudaSuccess &&
        cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming) == cudaSuccess &&
        cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming) == cudaSuccess &&
        cudaEventCreateWithFlags(&s->ev_inputs, cudaEventDisableTiming) == cudaSuccess &&
-       cudaEventCreateWithFlags(&s->ev_prev, cudaEventDisableTiming) == cudaSuccess &&
-       cudaEventCreateWithFlags(&s->ev_stats, cudaEventDisableTiming) == cudaSuccess;
+       cudaEventCreateWithFlags(&s->ev_prev, cudaEventDisableTiming) == cudaSuccess;
   return ok ? SF_OK : SF_ERR_CUDA;
 }
 
@@ -241,13 +246,13 @@ void free_all(sf_system *s) {
   if (s->h_rgb) cudaFreeHost(s->h_rgb);
   if (s->h_mask) cudaFreeHost(s->h_mask);
   if (s->h_stats) cudaFreeHost(s->h_stats);
+  if (s->h_ready) cudaFreeHost(s->h_ready);
   if (s->gexec) cudaGraphExecDestroy(s->gexec);
   for (auto &e : s->ev)
     if (e) cudaEventDestroy(e);
   if (s->cstream) cudaStreamSynchronize(s->cstream);
   if (s->ev_inputs) cudaEventDestroy(s->ev_inputs);
   if (s->ev_prev) cudaEventDestroy(s->ev_prev);
-  if (s->ev_stats) cudaEventDestroy(s->ev_stats);
   if (s->cstream) cudaStreamDestroy(s->cstream);
   if (s->side) cudaStreamSynchronize(s->side);
   if (s->ev_fork) cudaEventDestroy(s->ev_fork);
@@ -357,13 +362,12 @@ void icp_levels(sf_system *s, IcpLevelArgs *lv) {
 }
 
 // The frame's stats (k_sys_stats); in a captured frame also written to
-// h_stats (pinned, device-accessible) and followed by ev_stats.
+// h_stats (pinned, device-accessible) and flagged in h_ready.
 cudaError_t enqueue_stats(sf_system *s, cudaStream_t st) {
   k_sys_stats<<<1, 1, 0, st>>>(s->d_sys, ctx_icp(s->ctx).ctl, map_dev(s->map), ctx_flags(s->ctx), s->d_stats,
-                               s->capturing ? s->h_stats : nullptr);
+                               s->capturing ? s->h_stats : nullptr, s->h_ready);
   note_launch();
-  if (!s->capturing) return cudaGetLastError();
-  return cudaEventRecordWithFlags(s->ev_stats, st, cudaEventRecordExternal);
+  return cudaGetLastError();
 }
 
 // Mapping::FuseColor (FuseMapColor) and Mapping::RayTrace of the frame's
@@ -567,7 +571,7 @@ int run_plain_frame(sf_system *s, int num_detection) {
     int e = enqueue_mapping(s, dev_field<Cam>(s->d_sys, offsetof(SysDev, cam)), nullptr, num_detection, true, st);
     if (e != SF_OK) return e;
   }
-  k_sys_stats<<<1, 1, 0, st>>>(s->d_sys, w.ctl, map_dev(s->map), ctx_flags(s->ctx), s->d_stats, nullptr);
+  k_sys_stats<<<1, 1, 0, st>>>(s->d_sys, w.ctl, map_dev(s->map), ctx_flags(s->ctx), s->d_stats, nullptr, nullptr);
   note_launch();
   return cudaGetLastError() == cudaSuccess ? SF_OK : SF_ERR_CUDA;
 }
@@ -608,9 +612,10 @@ int run_frame(sf_system *s, int num_detection) {
     if (e != cudaSuccess) { s->gexec = nullptr; return SF_ERR_CUDA; }
     s->graph_sem = sem;
     s->graph_mapping = s->mapping;
-    s->graph_early = true;  // every captured frame copies its stats and records ev_stats
+    s->graph_early = true;  // every captured frame writes h_stats and h_ready
     s->num_detection_captured = num_detection;
   }
+  __atomic_store_n(s->h_ready, 0u, __ATOMIC_RELAXED);  // the previous replay's write has landed
   if (cudaGraphLaunch(s->gexec, st) != cudaSuccess) return SF_ERR_CUDA;
   note_launch(s->graph_kernels);
   return SF_OK;
@@ -700,8 +705,14 @@ int sf_system_grab(sf_system *s, const uint16_t *depth, const uint8_t *rgb, cons
   if (cudaEventRecord(s->ev_inputs, s->cstream) != cudaSuccess) return SF_ERR_CUDA;
   int r = run_frame(s, num_detection);
   if (r) return r;
-  if (s->cfg.use_graph == 1 && s->graph_early) {  // the graph copied them before its final raycast
-    if (cudaEventSynchronize(s->ev_stats) != cudaSuccess) return SF_ERR_CUDA;
+  if (s->cfg.use_graph == 1 && s->graph_early) {
+    // the graph wrote them before its final raycast; the wait ends with the
+    // flag, or with the stream (done, or failed)
+    while (__atomic_load_n(s->h_ready, __ATOMIC_ACQUIRE) == 0u) {
+      const cudaError_t q = cudaStreamQuery(st);
+      if (q == cudaErrorNotReady) continue;
+      if (q != cudaSuccess || __atomic_load_n(s->h_ready, __ATOMIC_ACQUIRE) == 0u) return SF_ERR_CUDA;
+    }
   } else if (cudaMemcpyAsync(s->h_stats, s->d_stats, sizeof(sf_frame_stats), cudaMemcpyDeviceToHost, st) !=
                  cudaSuccess ||
              cudaStreamSynchronize(st) != cudaSuccess) {
