@@ -145,6 +145,14 @@ def launches(sf):
     return v.value
 
 
+def label_frames(n):
+    """The room with ten labelled objects and 5% label flips (the semantic
+    mode's workload)."""
+    import semantic_icpslam_gb300 as sfm
+    syn = sfm.Synth(COLS, ROWS, K, n_objects=10, label_flip=0.05, **SEQ)
+    return [syn.frame(i) for i in range(n)]
+
+
 def time_device_resident(sf, ctx, frames, steps, warmup, mode, barrier, timing=False, autotune=False, rgb=0,
                          ndet=0):
     """Frames/s with inputs already in HBM; CUDA events on the system stream.
@@ -456,6 +464,8 @@ def main():
                     help="only the CUDA-graph timing (for profiler runs)")
     ap.add_argument("--rgbd", action="store_true",
                     help="with --quick: time the RGB-D tracking mode (ComputeSE3 with icpOnly = false) instead")
+    ap.add_argument("--labels", action="store_true",
+                    help="with --quick: time the semantic mode (detections every frame) instead")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -479,6 +489,12 @@ def main():
     n = args.steps + args.warmup
     MAP["num_sdf_blocks"] = 1 << args.map_blocks
     frames = make_frames(n, rank)
+    if args.quick and args.labels:  # for profiler runs of the semantic mode's kernels
+        g = time_device_resident(sf, ctx, label_frames(n), args.steps, args.warmup, 1, barrier, ndet=10)
+        ctx.close()
+        if rank == 0:
+            print(json.dumps({"labels": round(args.steps / g["elapsed"], 3), "unit": "frames/s"}), flush=True)
+        return
 
     # headline: CUDA graph, inputs in HBM
     g = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 1, barrier, autotune=args.autotune,
@@ -557,10 +573,7 @@ def main():
     if args.config == "c2":
         # the semantic mode (System.cc:184-205): the same room with ten
         # labelled objects and 5% label flips, detections every frame
-        import semantic_icpslam_gb300 as sfm
-        syn = sfm.Synth(COLS, ROWS, K, n_objects=10, label_flip=0.05, **SEQ)
-        lframes = [syn.frame(i) for i in range(n)]
-        lab = time_device_resident(sf, ctx, lframes, args.steps, args.warmup, 1, barrier, ndet=10)
+        lab = time_device_resident(sf, ctx, label_frames(n), args.steps, args.warmup, 1, barrier, ndet=10)
         out["labels"] = {"value": round(args.steps / lab["elapsed"], 3), "unit": "frames/s",
                          "gpu_launches": int(lab["launches"]),
                          "mode": "detections every frame (10 objects, 5% label flips): FuseColor, RayTrace, "
