@@ -429,7 +429,10 @@ int sf_system_create(sf_context *ctx, const sf_system_config *cfg,
 int sf_system_destroy(sf_system *sys);
 /* One frame from HOST buffers: depth uint16[rows*cols], rgb uint8[rows*cols*3],
  * mask uint8[rows*cols] (may be NULL).  Copies in, runs the frame, copies
- * the stats (pose included) out; returns when the frame is done. */
+ * the stats (pose included) out.  Returns when the stats are final: in the
+ * graph form (use_graph = 1) the frame's last raycast and ResizeMap may still
+ * run on the context's stream, and work ordered on that stream (the next
+ * frame, sf_memcpy, sf_context_sync) comes after them. */
 int sf_system_grab(sf_system *sys, const uint16_t *depth, const uint8_t *rgb,
                    const uint8_t *mask, int num_detection, sf_frame_stats *stats);
 /* One frame from DEVICE buffers (already resident); asynchronous on the

@@ -124,3 +124,30 @@ def test_first_frame_is_identity_tracked(lib):
     assert st.tracked == 1 and st.iterations == 0 and st.visible > 0
     assert np.array_equal(np.array(st.pose[:]).reshape(4, 4), seq[0][3])
     s.close()
+
+
+@pytest.mark.parametrize("ndet", [0, 10])
+def test_graph_grab_stats_before_raycast(lib, ndet):
+    """The graph form's sf_system_grab returns the stats it wrote before the
+    frame's final raycast: each frame they equal the stats read after the
+    whole frame (sf_system_stats), and the model maps read afterwards are the
+    finished raycast's (the eager form's, bit for bit)."""
+    sf, ctx = lib
+    seq = sequence(C1["cols"], C1["rows"], C1["K"], 4, trajectory=0, label_flip=0.05, n_objects=10, seed=4)
+    runs = {}
+    for mode in (1, 2):
+        cfg = sf.system_config(cols=C1["cols"], rows=C1["rows"], K=C1["K"], use_graph=mode, **MAP_C1)
+        s = sf.System(ctx, cfg, init_pose=seq[0][3])
+        out = []
+        for d, rgb, mask, _ in seq:
+            st = s.grab(d, rgb, mask if ndet else None, ndet)
+            fin = s.stats()
+            assert bytes(st) == bytes(fin)
+            v, n = s.model_maps(0)
+            out.append((np.array(st.pose[:]), _maps(ctx, [v])[0], _maps(ctx, [n])[0]))
+        runs[mode] = out
+        s.close()
+    for (p1, v1, n1), (p2, v2, n2) in zip(runs[1], runs[2]):
+        assert np.array_equal(p1, p2)
+        assert np.array_equal(v1.view(np.uint8), v2.view(np.uint8))
+        assert np.array_equal(n1.view(np.uint8), n2.view(np.uint8))
