@@ -200,7 +200,13 @@ int sf_ICPStep(sf_context *ctx, sf_image next_vmap, sf_image last_vmap,
  * exits.  Images of more than SF_ICP_STATIC_MAX_PIXELS pixels return
  * SF_ERR_TOO_LARGE before any GPU work.
  * The first call on each device looks up the array's device address.
- * Make that first call before any stream capture.
+ * Under CUDA's lazy module loading (the default since CUDA 12) that first
+ * call, or any earlier first use of this library's kernels, also loads the
+ * library's device image, which allocates device memory for its code and
+ * this array once and may synchronise the device.  A caller that can allow
+ * neither in its loop makes one warm-up call at initialisation (or sets
+ * CUDA_MODULE_LOADING=EAGER); later calls allocate nothing.  Make that
+ * first call before any stream capture.
  * All calls share the one array, so calls that overlap on the GPU (other
  * streams, other host threads) race and give wrong sums.  The call
  * synchronises `stream` before it returns. */

@@ -933,7 +933,10 @@ int icp_static_scratch(double **out) {
   std::lock_guard<std::mutex> lock(g_icp_static_mu);
   if (!g_icp_static_addr[dev]) {
     double *p = nullptr;
-    if (cudaGetSymbolAddress((void **)&p, g_icp_static) != cudaSuccess || !p) return SF_ERR_CUDA;
+    if (cudaGetSymbolAddress((void **)&p, g_icp_static) != cudaSuccess || !p) {
+      cudaGetLastError();  // leave no error of this lookup pending for the caller's next CUDA call
+      return SF_ERR_CUDA;
+    }
     g_icp_static_addr[dev] = p;
   }
   *out = g_icp_static_addr[dev];
@@ -973,9 +976,26 @@ extern "C" int sf_ICPStep_static(void *stream, sf_image next_vmap, sf_image last
   p.Rl = to_m3(Rlast); p.RlI = to_m3(RlastInv); p.tl = to_f3(tlast);
   const int nb = (int)((pixels + kStaticPixPerCta - 1) / kStaticPixPerCta);
   double *sums_dev = scratch + kStaticSumsOffset;
-  k_icp_partials<<<nb, kThreads, 0, s>>>(L, p, scratch, kStaticMaxCtas); note_launch();
-  k_icp_reduce<<<1, kThreads, 0, s>>>(scratch, nb, kStaticMaxCtas, sums_dev); note_launch();
-  if (cudaGetLastError() != cudaSuccess) return SF_ERR_CUDA;
+  // Each launch's own status: cudaLaunchKernelEx returns it directly, so an
+  // unrelated error the caller's earlier work left pending is neither
+  // reported nor cleared here.  A failed launch's error is cleared before
+  // returning, so it does not leak into the caller's next CUDA call.
+  cudaLaunchConfig_t lc = {};
+  lc.blockDim = dim3(kThreads);
+  lc.stream = s;
+  lc.gridDim = dim3(nb);
+  if (cudaLaunchKernelEx(&lc, k_icp_partials, L, p, scratch, kStaticMaxCtas) != cudaSuccess) {
+    cudaGetLastError();
+    return SF_ERR_CUDA;
+  }
+  note_launch();
+  lc.gridDim = dim3(1);
+  if (cudaLaunchKernelEx(&lc, k_icp_reduce, (const double *)scratch, nb, kStaticMaxCtas, sums_dev) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return SF_ERR_CUDA;
+  }
+  note_launch();
   double sums[29];
   if (cudaMemcpyAsync(sums, sums_dev, sizeof(sums), cudaMemcpyDeviceToHost, s) != cudaSuccess)
     return SF_ERR_CUDA;

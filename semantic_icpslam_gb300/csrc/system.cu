@@ -77,10 +77,13 @@ __global__ void k_sys_post(SysDev *s, const TrackCtl *ctl, Cam tmpl, FuseScratch
 }
 
 // `host_out` (pinned host memory, or null) receives a copy, and then
-// *host_ready = 1 (stores from the kernel cost the frame less than a copy
-// node and an event).
+// *host_ready the frame's sequence number, *seq + 1, which *seq keeps
+// (stores from the kernel cost the frame less than a copy node and an
+// event).  A reader waits for its own frame's number, so a flag left by an
+// earlier frame that nobody waited for cannot stand in for it.
 __global__ void k_sys_stats(const SysDev *s, const TrackCtl *ctl, DevMap m, const uint32_t *flags,
-                            sf_frame_stats *out, sf_frame_stats *host_out, uint32_t *host_ready) {
+                            sf_frame_stats *out, sf_frame_stats *host_out, uint32_t *host_ready,
+                            uint32_t *seq) {
   sf_frame_stats st;
   st.tracked = s->run;
   st.accepted = s->accepted;
@@ -103,9 +106,11 @@ __global__ void k_sys_stats(const SysDev *s, const TrackCtl *ctl, DevMap m, cons
   for (int k = 0; k < 16; ++k) st.pose[k] = s->last_pose[k];
   *out = st;
   if (host_out) {
+    const uint32_t q = *seq + 1u;
+    *seq = q;
     *host_out = st;
     __threadfence_system();  // the stats before the flag, as the host sees them
-    *(volatile uint32_t *)host_ready = 1u;
+    *(volatile uint32_t *)host_ready = q;
   }
 }
 
@@ -181,7 +186,9 @@ struct sf_system {
   // to h_stats there and then sets *h_ready, so sf_system_grab returns
   // while the raycast and ResizeMap still run and the next frame's uploads
   // and launch overlap them.
-  uint32_t *h_ready = nullptr;  // pinned; zeroed before each graph launch
+  uint32_t *h_ready = nullptr;  // pinned; the sequence number of the last frame that wrote h_stats
+  uint32_t *d_seq = nullptr;    // device: graph frames run so far (k_sys_stats counts them)
+  uint32_t graph_seq = 0;       // host: graph frames launched so far
   bool capturing = false;    // enqueue_device_frame is being captured
   bool stats_taken = false;  // this frame's enqueue took the stats early
   bool graph_early = false;  // the frame graph writes h_stats and h_ready
@@ -206,7 +213,8 @@ int alloc_all(sf_system *s) {
             A((void **)&s->d_mask, np) && A((void **)&s->d_raw, np * 4) && A((void **)&s->d_rdepth, np * 4) &&
             A((void **)&s->d_zmin, (size_t)s->zc * s->zr * 4) &&
             A((void **)&s->d_zmax, (size_t)s->zc * s->zr * 4) &&
-            A((void **)&s->d_sys, sizeof(SysDev)) && A((void **)&s->d_stats, sizeof(sf_frame_stats));
+            A((void **)&s->d_sys, sizeof(SysDev)) && A((void **)&s->d_stats, sizeof(sf_frame_stats)) &&
+            A((void **)&s->d_seq, sizeof(uint32_t)) && cudaMemset(s->d_seq, 0, sizeof(uint32_t)) == cudaSuccess;
   for (int l = 0; ok && l < s->L; ++l) {
     const size_t n = (size_t)(C >> l) * (R >> l);
     ok = A((void **)&s->d_depth[l], n * 4) && A((void **)&s->d_vmap[l], n * 16) &&
@@ -224,6 +232,7 @@ int alloc_all(sf_system *s) {
        cudaMallocHost(&s->h_stats, sizeof(sf_frame_stats)) == cudaSuccess &&
        cudaMallocHost(&s->h_ready, sizeof(uint32_t)) == cudaSuccess;
   if (ok) ok = cudaMemset(s->d_mask, 0, np) == cudaSuccess;
+  if (ok) *s->h_ready = 0u;
   ok = ok && cudaStreamCreateWithFlags(&s->cstream, cudaStreamNonBlocking) == cudaSuccess &&
        cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) == cudaSuccess &&
        cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming) == cudaSuccess &&
@@ -236,6 +245,7 @@ int alloc_all(sf_system *s) {
 void free_all(sf_system *s) {
   cudaFree(s->d_depth16); cudaFree(s->d_rgb); cudaFree(s->d_mask); cudaFree(s->d_raw); cudaFree(s->d_rdepth);
   cudaFree(s->d_zmin); cudaFree(s->d_zmax); cudaFree(s->d_sys); cudaFree(s->d_stats); cudaFree(s->d_corr);
+  cudaFree(s->d_seq);
   for (int l = 0; l < kMaxLevels; ++l) {
     cudaFree(s->d_depth[l]); cudaFree(s->d_vmap[l]); cudaFree(s->d_nmap[l]);
     cudaFree(s->d_mv[l]); cudaFree(s->d_mn[l]);
@@ -365,7 +375,7 @@ void icp_levels(sf_system *s, IcpLevelArgs *lv) {
 // h_stats (pinned, device-accessible) and flagged in h_ready.
 cudaError_t enqueue_stats(sf_system *s, cudaStream_t st) {
   k_sys_stats<<<1, 1, 0, st>>>(s->d_sys, ctx_icp(s->ctx).ctl, map_dev(s->map), ctx_flags(s->ctx), s->d_stats,
-                               s->capturing ? s->h_stats : nullptr, s->h_ready);
+                               s->capturing ? s->h_stats : nullptr, s->h_ready, s->d_seq);
   note_launch();
   return cudaGetLastError();
 }
@@ -571,7 +581,8 @@ int run_plain_frame(sf_system *s, int num_detection) {
     int e = enqueue_mapping(s, dev_field<Cam>(s->d_sys, offsetof(SysDev, cam)), nullptr, num_detection, true, st);
     if (e != SF_OK) return e;
   }
-  k_sys_stats<<<1, 1, 0, st>>>(s->d_sys, w.ctl, map_dev(s->map), ctx_flags(s->ctx), s->d_stats, nullptr, nullptr);
+  k_sys_stats<<<1, 1, 0, st>>>(s->d_sys, w.ctl, map_dev(s->map), ctx_flags(s->ctx), s->d_stats, nullptr, nullptr,
+                               nullptr);
   note_launch();
   return cudaGetLastError() == cudaSuccess ? SF_OK : SF_ERR_CUDA;
 }
@@ -615,8 +626,8 @@ int run_frame(sf_system *s, int num_detection) {
     s->graph_early = true;  // every captured frame writes h_stats and h_ready
     s->num_detection_captured = num_detection;
   }
-  __atomic_store_n(s->h_ready, 0u, __ATOMIC_RELAXED);  // the previous replay's write has landed
   if (cudaGraphLaunch(s->gexec, st) != cudaSuccess) return SF_ERR_CUDA;
+  ++s->graph_seq;  // this replay's k_sys_stats writes this number to h_ready
   note_launch(s->graph_kernels);
   return SF_OK;
 }
@@ -706,12 +717,15 @@ int sf_system_grab(sf_system *s, const uint16_t *depth, const uint8_t *rgb, cons
   int r = run_frame(s, num_detection);
   if (r) return r;
   if (s->cfg.use_graph == 1 && s->graph_early) {
-    // the graph wrote them before its final raycast; the wait ends with the
-    // flag, or with the stream (done, or failed)
-    while (__atomic_load_n(s->h_ready, __ATOMIC_ACQUIRE) == 0u) {
+    // the graph wrote them before its final raycast; the wait ends with this
+    // frame's sequence number in the flag (an earlier frame's number, left
+    // by a replay that sf_system_grab_device launched and nobody waited for,
+    // does not end it), or with the stream (done, or failed)
+    const uint32_t want = s->graph_seq;
+    while (__atomic_load_n(s->h_ready, __ATOMIC_ACQUIRE) != want) {
       const cudaError_t q = cudaStreamQuery(st);
       if (q == cudaErrorNotReady) continue;
-      if (q != cudaSuccess || __atomic_load_n(s->h_ready, __ATOMIC_ACQUIRE) == 0u) return SF_ERR_CUDA;
+      if (q != cudaSuccess || __atomic_load_n(s->h_ready, __ATOMIC_ACQUIRE) != want) return SF_ERR_CUDA;
     }
   } else if (cudaMemcpyAsync(s->h_stats, s->d_stats, sizeof(sf_frame_stats), cudaMemcpyDeviceToHost, st) !=
                  cudaSuccess ||

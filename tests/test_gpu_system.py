@@ -151,3 +151,33 @@ def test_graph_grab_stats_before_raycast(lib, ndet):
         assert np.array_equal(p1, p2)
         assert np.array_equal(v1.view(np.uint8), v2.view(np.uint8))
         assert np.array_equal(n1.view(np.uint8), n2.view(np.uint8))
+
+
+def test_graph_grab_after_grab_device(lib):
+    """sf_system_grab after frames that sf_system_grab_device launched and
+    nobody waited for returns its own frame's stats: the pose and counters
+    of every grabbed frame equal the eager form's for the same frame."""
+    import torch
+    sf, ctx = lib
+    n = 7
+    seq = sequence(C1["cols"], C1["rows"], C1["K"], n, trajectory=0)
+    cfg = lambda mode: sf.system_config(cols=C1["cols"], rows=C1["rows"], K=C1["K"], use_graph=mode, **MAP_C1)
+    e = sf.System(ctx, cfg(2), init_pose=seq[0][3])
+    want = []
+    for d, rgb, _, _ in seq:
+        e.grab(d, rgb)
+        want.append(e.stats())
+    e.close()
+    g = sf.System(ctx, cfg(1), init_pose=seq[0][3])
+    dev = [(cuda(d), cuda(rgb)) for d, rgb, _, _ in seq]
+    torch.cuda.synchronize()
+    for i in range(n):
+        if i % 3 == 2:  # grab with host buffers right behind unwaited device-buffer frames
+            st = g.grab(seq[i][0], seq[i][1])
+            w = want[i]
+            assert np.array_equal(np.array(st.pose[:]), np.array(w.pose[:])), "frame %d" % i
+            assert (st.tracked, st.visible, st.iterations, st.allocated) == \
+                (w.tracked, w.visible, w.iterations, w.allocated), "frame %d" % i
+        else:
+            g.grab_device(dev[i][0].data_ptr(), dev[i][1].data_ptr(), None, 0)
+    g.close()

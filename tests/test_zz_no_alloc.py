@@ -9,8 +9,8 @@ sf_ICPStep_static takes a stream plus the same inputs and host outputs as
 sf_ICPStep, and keeps its scratch in a fixed array inside the library's
 device image.
 
-Its results must match sf_ICPStep on the same inputs, for two calls in a
-row.  The second call reuses the array the first call left behind.  The
+Its results must match sf_ICPStep on the same inputs, for three calls in a
+row.  Each later call reuses the array the call before left behind.  The
 match count must be exact.  The sums may differ only by summation order:
 the two calls split the pixels over different numbers of CTAs.  The
 tolerance is the one the ICP parity tests use.
@@ -83,7 +83,7 @@ def test_static_icp_step_matches_context_step(lib):
     Pc[:3, 3] = 0.5 * (P0[:3, 3] + P1[:3, 3])
     stream = torch.cuda.Stream()
     K = C1["K"]
-    calls = [(0, Pc), (1, P1)]  # two calls in a row, different sizes and poses
+    calls = [(0, Pc), (1, P1), (0, P1)]  # calls in a row, different sizes and poses
     free = []
     for level, P in calls:
         div = float(1 << level)
@@ -93,8 +93,9 @@ def test_static_icp_step_matches_context_step(lib):
         got = _step(sf, "sf_ICPStep_static", C.c_void_p(stream.cuda_stream), ims, P, P0, Kl)
         _same(got, want)
         free.append(torch.cuda.mem_get_info()[0])
-    # the second call allocated nothing on the device
-    assert free[1] >= free[0]
+    # the calls after the first allocated nothing on the device (the first
+    # may load the library's device image under lazy module loading)
+    assert free[1] >= free[0] and free[2] >= free[0]
     del keep0, keep1
 
 
