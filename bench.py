@@ -108,8 +108,8 @@ def dist_env():
 
 
 def make_frames(n, rank=0):
-    import semantic_icpslam_gb300 as sf
-    syn = sf.Synth(COLS, ROWS, K, **SEQ)
+    from synth import Synth  # host-only generator library: loads none of the product's code
+    syn = Synth(COLS, ROWS, K, **SEQ)
     return [syn.frame(i) for i in range(n)]
 
 
@@ -148,8 +148,8 @@ def launches(sf):
 def label_frames(n):
     """The room with ten labelled objects and 5% label flips (the semantic
     mode's workload)."""
-    import semantic_icpslam_gb300 as sfm
-    syn = sfm.Synth(COLS, ROWS, K, n_objects=10, label_flip=0.05, **SEQ)
+    from synth import Synth
+    syn = Synth(COLS, ROWS, K, n_objects=10, label_flip=0.05, **SEQ)
     return [syn.frame(i) for i in range(n)]
 
 

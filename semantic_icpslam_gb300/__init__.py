@@ -12,10 +12,10 @@ import weakref
 import numpy as np
 
 from . import _lib
-from ._lib import (FrameStats, Image, Intrinsics, MapConfig, Mat3, Float3, SfError, SynthConfig,
+from ._lib import (FrameStats, Image, Intrinsics, MapConfig, Mat3, Float3, SfError,
                    SystemConfig, call, load)
 
-__all__ = ["Context", "Map", "System", "Synth", "image", "pose_to_gpu", "mat3", "float3",
+__all__ = ["Context", "Map", "System", "image", "pose_to_gpu", "mat3", "float3",
            "SfError", "load", "DEFAULT_C1", "DEFAULT_C2"]
 
 
@@ -223,43 +223,6 @@ def system_config(cols, rows, K, voxel_size, trunc_dist, num_buckets, num_excess
     cfg.use_graph = use_graph
     cfg.rgb_term = int(rgb_term)
     return cfg
-
-
-class Synth:
-    """Seeded synthetic RGB-D sequence (include/sf_synth.h)."""
-
-    ROOM, CORRIDOR = 0, 1
-    CIRCLE, SPLINE, FORWARD = 0, 1, 2
-
-    def __init__(self, cols, rows, K, scene=0, trajectory=0, seed=1, dropout=0.0, label_flip=0.0,
-                 n_objects=0, noise=1.0, depth_scale=1000.0):
-        self.cfg = SynthConfig(scene, trajectory, cols, rows, K[0], K[1], K[2], K[3], depth_scale, dropout,
-                               label_flip, n_objects, noise, seed)
-        h = C.c_void_p()
-        call("sf_synth_create", C.byref(self.cfg), C.byref(h))
-        self.h = h
-        self.cols, self.rows = cols, rows
-
-    def close(self):
-        if getattr(self, "h", None):
-            load().sf_synth_destroy(self.h)
-            self.h = None
-
-    __del__ = close
-
-    def frame(self, i):
-        d = np.zeros((self.rows, self.cols), np.uint16)
-        rgb = np.zeros((self.rows, self.cols, 3), np.uint8)
-        m = np.zeros((self.rows, self.cols), np.uint8)
-        P = np.zeros(16, np.float64)
-        call("sf_synth_frame", self.h, i, d.ctypes.data, rgb.ctypes.data, m.ctypes.data,
-             P.ctypes.data_as(_lib.F64P))
-        return d, rgb, m, P.reshape(4, 4)
-
-    def pose(self, i):
-        P = np.zeros(16, np.float64)
-        call("sf_synth_pose", self.h, i, P.ctypes.data_as(_lib.F64P))
-        return P.reshape(4, 4)
 
 
 # Workloads: a 320x240 / 10 mm room sequence and a 640x480 / 5 mm room

@@ -82,13 +82,6 @@ class AutotuneReport(C.Structure):
                 ("tile_x", C.c_int * 16), ("tile_y", C.c_int * 16)]
 
 
-class SynthConfig(C.Structure):
-    _fields_ = [("scene", C.c_int), ("trajectory", C.c_int), ("cols", C.c_int), ("rows", C.c_int),
-                ("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float), ("cy", C.c_float),
-                ("depth_scale", C.c_float), ("dropout", C.c_float), ("label_flip", C.c_float),
-                ("n_objects", C.c_int), ("noise", C.c_float), ("seed", C.c_uint64)]
-
-
 vp = C.c_void_p
 pvp = C.POINTER(C.c_void_p)
 U32P = C.POINTER(C.c_uint32)
@@ -161,10 +154,6 @@ SIGNATURES = {
     "sf_system_set_mapping": [vp, C.c_int],
     "sf_system_stage_ms": [vp, F32P],
     "sf_system_pose_device": [vp, C.POINTER(C.POINTER(C.c_double))],
-    "sf_synth_create": [C.POINTER(SynthConfig), pvp],
-    "sf_synth_destroy": [vp],
-    "sf_synth_pose": [vp, C.c_int, F64P],
-    "sf_synth_frame": [vp, C.c_int, vp, vp, vp, F64P],
 }
 
 _lib = None

@@ -17,6 +17,8 @@ def built():
     """Builds the oracle and the CUDA library once per session."""
     from oracle import build as obuild
     from semantic_icpslam_gb300 import build as pbuild
+    import synth
     obuild.build()
     pbuild.build()
+    synth.build()
     return True

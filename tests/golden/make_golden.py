@@ -156,13 +156,13 @@ UNIFY_NVIS = (2048, 4096 + 8192)  # half the bucket slots; every slot
 
 
 def main():
-    import semantic_icpslam_gb300 as sf
+    from synth import Synth
     L = load_ref()
     consts = np.zeros(8, np.float64)
     L.ref_constants(fptr(consts))
     n_sdf = int(consts[4])
     n_entries = int(consts[2] + consts[3])
-    syn = sf.Synth(COLS, ROWS, K, scene=0, trajectory=1, seed=7, dropout=0.02, label_flip=0.05, n_objects=10)
+    syn = Synth(COLS, ROWS, K, scene=0, trajectory=1, seed=7, dropout=0.02, label_flip=0.05, n_objects=10)
     frames = [syn.frame(i) for i in range(NFRAMES + 1)]
     out = {"K": np.array(K, np.float32), "consts": consts}
     for i, (d, rgb, mask, P) in enumerate(frames):

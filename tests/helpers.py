@@ -14,7 +14,7 @@ MAP_C2 = dict(voxel_size=0.005, trunc_dist=0.04, num_buckets=1 << 20, num_excess
 def sequence(cols, rows, K, n, scene=0, trajectory=0, seed=1, dropout=0.0, label_flip=0.0, noise=1.0,
              n_objects=0):
     """Frames (depth u16, rgb, mask, gt pose) of a seeded synthetic sequence."""
-    from semantic_icpslam_gb300 import Synth
+    from synth import Synth
     s = Synth(cols, rows, K, scene=scene, trajectory=trajectory, seed=seed, dropout=dropout,
               label_flip=label_flip, noise=noise, n_objects=n_objects)
     return [s.frame(i) for i in range(n)]
