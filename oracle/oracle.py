@@ -77,6 +77,8 @@ def lib():
                 "sfo_alloc": (None, [vp, F32P, C.c_int, C.c_int, F32P, F32P] + [C.c_float] * 4),
                 "sfo_visibility": (C.c_uint, [vp, F32P, F32P, F32P, C.c_int, C.c_int] + [C.c_float] * 6),
                 "sfo_integrate": (None, [vp, F32P, U8P, C.c_int, C.c_int, F32P, F32P] + [C.c_float] * 6),
+                "sfo_integrate_f64": (None, [vp, F32P, C.c_int, C.c_int, F32P, F32P, F64P] + [C.c_float] * 6),
+                "sfo_tsdf_f64_error": (None, [vp, F64P]),
                 "sfo_semantics": (None, [vp, F32P, U8P, F32P, U8P, C.c_int, C.c_int, C.c_int, F32P, F32P] + [C.c_float] * 6),
                 "sfo_unify_neighbor": (None, [vp]),
                 "sfo_map_set_no_visible": (None, [vp, C.c_uint]),
@@ -361,6 +363,24 @@ class Map:
         _, RI, t = pose_to_gpu(P)
         lib().sfo_integrate(self.h, _p(depth, F32P), _p(rgb, U8P), cols, rows, _p(RI, F32P), _p(t, F32P),
                             *map(float, K), self.cfg.depth_max, self.cfg.depth_min)
+
+    def integrate_f64(self, depth, P, K):
+        """The FP64 shadow of this frame's TSDF update (measurement only):
+        call after visibility() and before integrate() of the same frame.
+        P: the FP64 camera->world pose the FP32 rotation is taken from."""
+        depth = _f32(depth)
+        rows, cols = depth.shape
+        _, RI, t = pose_to_gpu(P)
+        P64 = np.ascontiguousarray(P, np.float64)
+        lib().sfo_integrate_f64(self.h, _p(depth, F32P), cols, rows, _p(RI, F32P), _p(t, F32P), _p(P64, F64P),
+                                *map(float, K), self.cfg.depth_max, self.cfg.depth_min)
+
+    def tsdf_f64_error(self):
+        """(max |tsdf32 - tsdf64|, RMS, voxels) over the voxels the FP64
+        shadow covers."""
+        out = np.zeros(3, np.float64)
+        lib().sfo_tsdf_f64_error(self.h, _p(out, F64P))
+        return float(out[0]), float(out[1]), int(out[2])
 
     def semantics(self, depth, rgb, nmap_, mask, num_detection, P, K):
         depth, nmap_ = _f32(depth), _f32(nmap_)

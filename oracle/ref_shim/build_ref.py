@@ -38,6 +38,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
+ROOT = os.path.dirname(ORACLE)
 OUT = os.path.join(ORACLE, "_ref")
 REF = os.environ.get("SF_REFERENCE_DIR", "/root/reference")
 
@@ -46,10 +47,17 @@ SOURCES = ["Mapping/DeviceMap.cu", "Mapping/FuseMap.cu", "Mapping/RenderScene.cu
 HEADERS = ["Mapping/DeviceMap.h", "Mapping/RenderScene.h", "Mapping/Constant.h", "Tracking/Reduction.h",
            "Utility/DeviceArray.h", "Utility/VectorMath.h", "Utility/SafeCall.h", "Utility/Intrinsics.h"]
 
-# Golden configurations: DeviceMap constants (Mapping/DeviceMap.h:166-189).
+# Configurations: DeviceMap constants (Mapping/DeviceMap.h:166-189).
+#  * g1: the golden fixtures' 128x96 / 10 mm map, serial launches;
+#  * c2: the benchmark's 640x480 map (5 mm voxels, 4 cm truncation, 2^20
+#    buckets, 2^18 excess entries, 2^19 heap blocks), OpenMP over each
+#    launch's blocks, linked with the loop driver ref_cpu_driver.cpp: the
+#    reference's own loop on the host cores (the CPU baseline).
 CONFIGS = {
     "g1": dict(VoxelSize="0.01f", TruncateMul=3, NumBuckets=4096, NumExcess=8192, NumSdfBlocks=16384,
                DepthMin="0.1f", DepthMax="3.0f", MaxTriangles=1000000),
+    "c2": dict(VoxelSize="0.005f", TruncateMul=8, NumBuckets=1048576, NumExcess=262144, NumSdfBlocks=524288,
+               DepthMin="0.1f", DepthMax="3.0f", MaxTriangles=1000000, omp=True, driver="ref_cpu_driver.cpp"),
 }
 
 ICP_APPENDIX = r'''
@@ -77,6 +85,48 @@ extern "C" void ref_icp_rows_impl(const float *vc, const float *vl, const float 
   icp.fx = fx; icp.fy = fy; icp.cx = cx; icp.cy = cy;
   icp.angleThresh = 0.6; icp.distThresh = 0.1;  // as ICPStep sets them
   for (int i = 0; i < cols * rows; ++i) icp.getRow(i, out29 + 29 * (size_t)i);
+}
+
+// ---- appended by oracle/ref_shim/build_ref.py: ICP sums over every pixel ----
+// ICPStep's 29 sums: ICPReduce::getRow for every pixel, summed in FP64 per
+// host thread and then over the threads (the reference reduces the rows
+// with warp shuffles and a block tree, which have no serial form).
+extern "C" void ref_icp_sums_impl(const float *vc, const float *vl, const float *nc, const float *nl,
+                                  int cols, int rows, const float *Rc, const float *tc, const float *Rl,
+                                  const float *RlInv, const float *tl, float fx, float fy, float cx,
+                                  float cy, double *sums29) {
+  ICPReduce icp;
+  auto m3 = [](const float *R) {
+    Matrix3f M;
+    M.rowx = make_float3(R[0], R[1], R[2]);
+    M.rowy = make_float3(R[3], R[4], R[5]);
+    M.rowz = make_float3(R[6], R[7], R[8]);
+    return M;
+  };
+  icp.Rcurr = m3(Rc); icp.Rlast = m3(Rl); icp.RlastInv = m3(RlInv);
+  icp.tcurr = make_float3(tc[0], tc[1], tc[2]);
+  icp.tlast = make_float3(tl[0], tl[1], tl[2]);
+  icp.VMapCurr.data = (float4 *)vc; icp.VMapCurr.step = sizeof(float4) * cols;
+  icp.VMapLast.data = (float4 *)vl; icp.VMapLast.step = sizeof(float4) * cols;
+  icp.NMapCurr.data = (float4 *)nc; icp.NMapCurr.step = sizeof(float4) * cols;
+  icp.NMapLast.data = (float4 *)nl; icp.NMapLast.step = sizeof(float4) * cols;
+  icp.cols = cols; icp.rows = rows; icp.N = cols * rows;
+  icp.fx = fx; icp.fy = fy; icp.cx = cx; icp.cy = cy;
+  icp.angleThresh = 0.6; icp.distThresh = 0.1;  // as ICPStep sets them
+  double tot[29] = {0};
+#pragma omp parallel
+  {
+    double part[29] = {0};
+    float row[29];
+#pragma omp for schedule(static)
+    for (int i = 0; i < cols * rows; ++i) {
+      icp.getRow(i, row);
+      for (int k = 0; k < 29; ++k) part[k] += row[k];
+    }
+#pragma omp critical
+    for (int k = 0; k < 29; ++k) tot[k] += part[k];
+  }
+  for (int k = 0; k < 29; ++k) sums29[k] = tot[k];
 }
 
 // ---- appended by oracle/ref_shim/build_ref.py: per-pixel RGB rows ----
@@ -255,20 +305,14 @@ def patch_sources(name, text, cfg):
     return text
 
 
-def build(cfg_name="g1", force=False, verbose=False):
+def prepare(cfg_name="g1"):
+    """Writes the rewritten copies of the reference sources into
+    oracle/_ref/<cfg>/src (needs the reference tree)."""
     if not os.path.isdir(REF):
         raise FileNotFoundError("reference sources not found at %s" % REF)
     cfg = CONFIGS[cfg_name]
-    dst = os.path.join(OUT, cfg_name)
-    src_dir = os.path.join(dst, "src")
-    lib = os.path.join(dst, "libref.so")
-    driver = os.path.join(HERE, "ref_driver.cpp")
-    if not force and os.path.exists(lib) and os.path.getmtime(lib) > max(
-            os.path.getmtime(__file__), os.path.getmtime(driver),
-            os.path.getmtime(os.path.join(HERE, "include", "cuda_runtime.h"))):
-        return lib
+    src_dir = os.path.join(OUT, cfg_name, "src")
     os.makedirs(src_dir, exist_ok=True)
-    objs = []
     for rel in HEADERS + SOURCES:
         name = os.path.basename(rel)
         text = open(os.path.join(REF, rel)).read()
@@ -276,8 +320,41 @@ def build(cfg_name="g1", force=False, verbose=False):
         out_name = name[:-3] + ".cpp" if name.endswith(".cu") else name
         with open(os.path.join(src_dir, out_name), "w") as f:
             f.write(text)
+    with open(os.path.join(src_dir, ".prepared"), "w") as f:
+        f.write(_recipe_stamp())
+    return src_dir
+
+
+def _recipe_stamp():
+    return "%.6f" % os.path.getmtime(__file__)
+
+
+def build(cfg_name="g1", force=False, verbose=False):
+    """Compiles oracle/_ref/<cfg>/libref.so from the prepared copies,
+    preparing them first where the reference tree is present.  On a machine
+    without the reference tree (the GPU machine) it compiles copies prepared
+    elsewhere, and raises FileNotFoundError when there are none."""
+    cfg = CONFIGS[cfg_name]
+    dst = os.path.join(OUT, cfg_name)
+    src_dir = os.path.join(dst, "src")
+    lib = os.path.join(dst, "libref.so")
+    driver = os.path.join(HERE, cfg.get("driver", "ref_driver.cpp"))
+    deps = [driver, os.path.join(HERE, "include", "cuda_runtime.h"), os.path.join(HERE, "include", "ParallelScan.h"),
+            os.path.join(HERE, "ref_loop.h"), os.path.join(ROOT, "semantic_icpslam_gb300", "csrc", "sf_solve.h")]
+    stamp = os.path.join(src_dir, ".prepared")
+    if os.path.isdir(REF):
+        if force or not os.path.exists(stamp) or open(stamp).read() != _recipe_stamp():
+            prepare(cfg_name)
+    elif not os.path.exists(stamp):
+        raise FileNotFoundError("reference sources not found at %s and no prepared copies" % REF)
+    deps.append(stamp)
+    if not force and os.path.exists(lib) and os.path.getmtime(lib) > max(os.path.getmtime(d) for d in deps):
+        return lib
+    objs = []
     flags = ["-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-w",
              "-I", os.path.join(HERE, "include"), "-I", src_dir]
+    if cfg.get("omp"):
+        flags += ["-fopenmp", "-DSHIM_OMP", "-I", HERE, "-I", os.path.join(ROOT, "semantic_icpslam_gb300", "csrc")]
     units = [os.path.join(src_dir, os.path.basename(r)[:-3] + ".cpp") for r in SOURCES] + [driver]
     procs = []
     for u in units:
@@ -291,12 +368,23 @@ def build(cfg_name="g1", force=False, verbose=False):
         out, _ = p.communicate()
         if p.returncode != 0:
             raise RuntimeError("compile failed: %s\n%s" % (" ".join(cmd), out[-4000:]))
-    subprocess.check_call(["g++", "-shared", "-o", lib] + objs)
+    subprocess.check_call(["g++", "-shared", "-o", lib + ".tmp"] + objs + (["-fopenmp"] if cfg.get("omp") else []))
+    os.replace(lib + ".tmp", lib)
     return lib
 
 
+def build_all(force=False, verbose=False):
+    """Every configuration that can be built here; returns {name: path or
+    the reason it was skipped}."""
+    out = {}
+    for name in CONFIGS:
+        try:
+            out[name] = build(name, force=force, verbose=verbose)
+        except (FileNotFoundError, RuntimeError, subprocess.CalledProcessError) as e:
+            out[name] = "skipped: %s" % str(e).splitlines()[0]
+    return out
+
+
 if __name__ == "__main__":
-    try:
-        print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
-    except FileNotFoundError as e:
-        print("skipped:", e)
+    for k, v in build_all(force="--force" in sys.argv, verbose="-v" in sys.argv).items():
+        print(k, v)

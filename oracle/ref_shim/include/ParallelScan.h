@@ -7,7 +7,11 @@
 template <int threadBlock>
 inline int ComputeOffset(unsigned int element, unsigned int *sum) {
   if (element == 0) return -1;
+#ifdef SHIM_OMP  // blocks on several host threads: the same offsets, in racing order
+  return (int)__atomic_fetch_add(sum, element, __ATOMIC_RELAXED);
+#else
   unsigned int o = *sum;
   *sum = o + element;
   return (int)o;
+#endif
 }

@@ -1,11 +1,22 @@
 // CUDA emulation header for compiling the reference's device code as host
 // C++ (test infrastructure only: it pins the oracle against the reference's
-// own kernels).  Kernels run serially, one emulated thread at a time, over
-// the launch grid; "device" memory is host memory; atomics are plain
-// read-modify-writes.  Block-level primitives (__syncthreads, warp shuffles)
-// are not emulated: the recipe only runs kernels whose result is defined
-// without them, and replaces Utility/ParallelScan.h with a serial prefix
-// offset.
+// own kernels, and times that code on the host cores as the CPU baseline).
+// "Device" memory is host memory.  Block-level primitives (__syncthreads,
+// warp shuffles) are not emulated: the recipe only runs kernels whose result
+// is defined without them, and replaces Utility/ParallelScan.h with a
+// prefix offset handed out one thread at a time.
+//
+// Two launch modes:
+//  * serial (default): every (block, thread) of the grid in order, one
+//    emulated thread at a time; atomics are plain read-modify-writes.  The
+//    golden fixtures come from this mode, so allocation and list orders are
+//    those of one thread.
+//  * SHIM_OMP: an OpenMP parallel loop over the grid's blocks, each block's
+//    threads in order on one host thread (block-shared variables are
+//    per-host-thread statics); atomics are real atomics.  Results are then
+//    as racy as on the GPU (list orders, the bucket lock's skipped
+//    allocations), which is the reference's own behaviour; this mode times
+//    the reference's code on the host cores.
 #ifndef REF_SHIM_CUDA_RUNTIME_H_
 #define REF_SHIM_CUDA_RUNTIME_H_
 
@@ -24,7 +35,11 @@
 #define __global__
 #define __forceinline__ inline
 #define __inline__ inline
+#ifdef SHIM_OMP
+#define __shared__ static thread_local
+#else
 #define __shared__ static
+#endif
 #define __constant__
 #define __launch_bounds__(...)
 #define __align__(n) alignas(n)
@@ -110,6 +125,44 @@ inline float max(float a, float b) { return std::fmax(a, b); }
 inline double min(double a, double b) { return std::fmin(a, b); }
 inline double max(double a, double b) { return std::fmax(a, b); }
 
+#ifdef SHIM_OMP
+// real atomics (blocks run concurrently on the host threads)
+inline int atomicAdd(int *p, int v) { return __atomic_fetch_add(p, v, __ATOMIC_RELAXED); }
+inline unsigned atomicAdd(unsigned *p, unsigned v) { return __atomic_fetch_add(p, v, __ATOMIC_RELAXED); }
+inline float atomicAdd(float *p, float v) {
+  unsigned *u = (unsigned *)p;
+  unsigned o = __atomic_load_n(u, __ATOMIC_RELAXED), n;
+  do {
+    float f;
+    memcpy(&f, &o, 4);
+    f += v;
+    memcpy(&n, &f, 4);
+  } while (!__atomic_compare_exchange_n(u, &o, n, false, __ATOMIC_RELAXED, __ATOMIC_RELAXED));
+  float r;
+  memcpy(&r, &o, 4);
+  return r;
+}
+inline int atomicSub(int *p, int v) { return __atomic_fetch_sub(p, v, __ATOMIC_RELAXED); }
+inline unsigned atomicSub(unsigned *p, unsigned v) { return __atomic_fetch_sub(p, v, __ATOMIC_RELAXED); }
+inline int atomicExch(int *p, int v) { return __atomic_exchange_n(p, v, __ATOMIC_ACQ_REL); }
+inline unsigned atomicExch(unsigned *p, unsigned v) { return __atomic_exchange_n(p, v, __ATOMIC_ACQ_REL); }
+inline int atomicCAS(int *p, int c, int v) {
+  __atomic_compare_exchange_n(p, &c, v, false, __ATOMIC_ACQ_REL, __ATOMIC_RELAXED);
+  return c;  // the old value on success and failure alike
+}
+inline int atomicMin(int *p, int v) {
+  int o = __atomic_load_n(p, __ATOMIC_RELAXED);
+  while (v < o && !__atomic_compare_exchange_n(p, &o, v, false, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) {
+  }
+  return o;
+}
+inline int atomicMax(int *p, int v) {
+  int o = __atomic_load_n(p, __ATOMIC_RELAXED);
+  while (v > o && !__atomic_compare_exchange_n(p, &o, v, false, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) {
+  }
+  return o;
+}
+#else
 // serial atomics (one emulated thread at a time)
 inline int atomicAdd(int *p, int v) { int o = *p; *p = o + v; return o; }
 inline unsigned atomicAdd(unsigned *p, unsigned v) { unsigned o = *p; *p = o + v; return o; }
@@ -121,6 +174,7 @@ inline unsigned atomicExch(unsigned *p, unsigned v) { unsigned o = *p; *p = v; r
 inline int atomicCAS(int *p, int c, int v) { int o = *p; if (o == c) *p = v; return o; }
 inline int atomicMin(int *p, int v) { int o = *p; if (v < o) *p = v; return o; }
 inline int atomicMax(int *p, int v) { int o = *p; if (v > o) *p = v; return o; }
+#endif
 
 // ------------------------------------------------------------ runtime API
 typedef int cudaError_t;
@@ -162,9 +216,26 @@ inline cudaError_t cudaMemset2D(void *d, size_t dp, int v, size_t w, size_t h) {
 }
 inline cudaError_t cudaMemGetInfo(size_t *f, size_t *t) { *f = *t = 0; return cudaSuccess; }
 
-// Serial launch: every (block, thread) of the grid in order.
+// Launch: every (block, thread) of the grid, blocks in order (serial) or
+// spread over the host threads (SHIM_OMP), each block's threads in order.
 template <class F>
 inline void shim_launch(dim3 grid, dim3 block, F &&f) {
+#ifdef SHIM_OMP
+  const long long nb = (long long)grid.x * grid.y * grid.z;
+#pragma omp parallel for schedule(dynamic, 4)
+  for (long long b = 0; b < nb; ++b) {
+    gridDim = grid;
+    blockDim = block;
+    blockIdx = {(unsigned)(b % grid.x), (unsigned)((b / grid.x) % grid.y), (unsigned)(b / ((long long)grid.x * grid.y))};
+    for (unsigned tz = 0; tz < block.z; ++tz)
+      for (unsigned ty = 0; ty < block.y; ++ty)
+        for (unsigned tx = 0; tx < block.x; ++tx) {
+          threadIdx = {tx, ty, tz};
+          f();
+        }
+  }
+  return;
+#endif
   gridDim = grid;
   blockDim = block;
   for (unsigned bz = 0; bz < grid.z; ++bz)

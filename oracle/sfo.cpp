@@ -21,6 +21,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <limits>
+#include <memory>
+#include <mutex>
 #include <vector>
 
 namespace {
@@ -1134,6 +1136,99 @@ extern "C" void sfo_integrate(sfo_map *m, const float *depth, const uint8_t *rgb
           }
         }
   }
+}
+
+// FP64 shadow of the TSDF (measurement only, not a reference kernel): for
+// the voxels createVoxels updates this frame (the same gates, decided in
+// FP32 as the reference decides them), the new TSDF in double: the voxel's
+// camera depth from the FP64 pose and the voxel centre in double, and the
+// running average in double.  Called before sfo_integrate of the same frame
+// (it reads the pre-update weight).  The shadow is per heap block, made on
+// first touch; sfo_tsdf_f64_error compares it with the FP32 voxels.
+struct sfo_f64_shadow {
+  std::vector<std::unique_ptr<double[]>> blocks;
+};
+static sfo_f64_shadow &f64_shadow(sfo_map *m) {
+  static std::mutex mu;
+  static std::vector<std::pair<sfo_map *, std::unique_ptr<sfo_f64_shadow>>> all;
+  std::lock_guard<std::mutex> lock(mu);
+  for (auto &e : all)
+    if (e.first == m) return *e.second;
+  all.emplace_back(m, std::unique_ptr<sfo_f64_shadow>(new sfo_f64_shadow()));
+  all.back().second->blocks.resize(m->c.num_sdf_blocks);
+  return *all.back().second;
+}
+
+extern "C" void sfo_integrate_f64(sfo_map *m, const float *depth, int cols, int rows, const float *Rinv,
+                                  const float *t, const double *P64, float fx, float fy, float cx, float cy,
+                                  float depth_max, float depth_min) {
+  Cam c{{}, m3_from(Rinv), f3_from(t), fx, fy, cx, cy, cols, rows, depth_min, depth_max};
+  const float thresh = m->c.trunc_dist;
+  sfo_f64_shadow &sh = f64_shadow(m);
+  // the visible blocks' shadows, made serially before the parallel pass
+  for (unsigned b = 0; b < m->noVisible; ++b) {
+    const sfo_entry &entry = m->visible[b];
+    if (entry.ptr < 0) continue;
+    auto &blk = sh.blocks[(size_t)entry.ptr / 512];
+    if (!blk) {
+      blk.reset(new double[512]);
+      for (int k = 0; k < 512; ++k) blk[k] = 0.0;
+    }
+  }
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int b = 0; b < (int)m->noVisible; ++b) {
+    const sfo_entry &entry = m->visible[b];
+    if (entry.ptr == -1) continue;
+    i3 blk = {entry.x, entry.y, entry.z};
+    double *s64 = sh.blocks[(size_t)entry.ptr / 512].get();
+    for (int lz = 0; lz < 8; ++lz)
+      for (int ly = 0; ly < 8; ++ly)
+        for (int lx = 0; lx < 8; ++lx) {
+          f3 pos;
+          int u, v;
+          if (!voxel_pixel(c, *m, blk, lx, ly, lz, pos, u, v)) continue;
+          float dp = depth[v * cols + u];
+          if (std::isnan(dp) || dp > c.dmax || dp < c.dmin) continue;
+          float sdf = dp - pos.z;
+          if (!(sdf >= -thresh)) continue;
+          // camera depth of the voxel centre in double: z = row 2 of R^T (w - t)
+          const double vs = (double)m->c.voxel_size;
+          const double wx = (double)(blk.x * 8 + lx) * vs, wy = (double)(blk.y * 8 + ly) * vs,
+                       wz = (double)(blk.z * 8 + lz) * vs;
+          const double dx = wx - P64[3], dy = wy - P64[7], dz = wz - P64[11];
+          const double z64 = P64[2] * dx + P64[6] * dy + P64[10] * dz;
+          double sd = (double)dp - z64;
+          sd = std::fmin(1.0, sd / (double)thresh);
+          const size_t li = (size_t)(lz * 64 + ly * 8 + lx);
+          const sfo_voxel &prev = m->voxels[(size_t)entry.ptr + li];
+          if (prev.weight == 0)
+            s64[li] = sd;
+          else
+            s64[li] = (s64[li] * (double)prev.weight + sd) / (double)(prev.weight + 1);
+        }
+  }
+}
+
+// out[0] = max |tsdf32 - tsdf64|, out[1] = RMS, out[2] = voxels compared
+// (every voxel of a shadowed block with weight > 0).  The TSDF is the
+// voxel's normalised distance in [-1, 1].
+extern "C" void sfo_tsdf_f64_error(sfo_map *m, double *out) {
+  sfo_f64_shadow &sh = f64_shadow(m);
+  double mx = 0.0, ss = 0.0, n = 0.0;
+  for (size_t b = 0; b < sh.blocks.size(); ++b) {
+    if (!sh.blocks[b]) continue;
+    for (int k = 0; k < 512; ++k) {
+      const sfo_voxel &v = m->voxels[b * 512 + k];
+      if (v.weight == 0) continue;
+      const double e = std::fabs((double)v.sdf - sh.blocks[b][k]);
+      mx = std::max(mx, e);
+      ss += e * e;
+      n += 1.0;
+    }
+  }
+  out[0] = mx;
+  out[1] = n > 0 ? std::sqrt(ss / n) : 0.0;
+  out[2] = n;
 }
 
 // Fusion::analyzeSemantics, FuseMap.cu:509-668, one update per voxel (the
