@@ -6,17 +6,25 @@ Perlin RGB, depth noise 0.0012 + 0.0019 (z - 0.4)^2 m), 5 mm voxels, 2^20
 buckets, 4 cm truncation, 3-level ICP with 10/5/4 iterations.  One step is
 one frame through System::GrabImage's order: pyramid -> ICP (all levels and
 iterations) -> allocation -> visibility -> integration -> raycast -> resize.
+Frames 0..W-1 warm the loop up; frames W..W+K-1 are timed.
 
-`value`: CUDA-graph form, inputs resident in HBM (a new frame per step from
-a sequence larger than L2), CUDA events on the system's stream.
+`value`: CUDA-graph form, inputs resident in HBM, one CUDA-event pair per
+step on the system's stream; L2 is flushed (a 256 MiB write) before every
+timed step, outside the timed intervals.
 `plain`: the same kernels launched one by one, host-driven (ICP sums
 downloaded and solved on the host every iteration, as the reference does).
 `e2e`: CUDA-graph form through the public host-buffer API (sf_system_grab:
-host -> pinned -> device copies and the stats read-back inside the timed
-region).
-`--impl reference`: the reference's CPU implementation of the loop (the
-oracle restatement, which reproduces the reference's own kernels bit for
-bit), timed on the host cores over a bounded sample of the same workload.
+pinned host -> device copies and the stats read-back inside the timed
+region; each step timed on the host clock up to the context's
+synchronisation, L2 flushed between steps).
+`errors`: per timed frame, the loop's pose against the FP64 oracle's
+ComputeSE3 on the same inputs, sf_ICPStep's J^T J / J^T r against FP64 sums,
+and, over the whole sequence, the TSDF against an FP64 shadow of the
+integration and the device map against the FP32 oracle map.
+`--impl reference`: the reference's own device code compiled as host
+C++/OpenMP at these constants (oracle/_ref/c2), driven in GrabImage's order,
+timed on the host cores over the same frames; beside it the reference's CUDA
+build on the GPU.
 """
 import argparse
 import json
@@ -113,6 +121,31 @@ def make_frames(n, rank=0):
     return [syn.frame(i) for i in range(n)]
 
 
+def bench_config():
+    """The `config` of both arms' lines (the same dict, so the two arms'
+    configurations compare equal)."""
+    return {"workload": WORKLOAD, "global_batch": "1 frame per GPU per step",
+            "parallelism": "replicas (one independent sequence per GPU)",
+            "l2": "flushed before every timed step (a %d MiB write on the timed stream, outside the timed "
+                  "intervals); each step reads a new frame" % (FLUSH_BYTES >> 20)}
+
+
+FLUSH_BYTES = 256 << 20
+
+
+class L2Flush:
+    """Writes a buffer larger than L2 on a stream (between timed steps)."""
+
+    def __init__(self):
+        import torch
+        self.buf = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+
+    def __call__(self, stream):
+        import torch
+        with torch.cuda.stream(stream):
+            self.buf.fill_(1)
+
+
 def sys_cfg(sf, mode, rgb=0):
     return sf.system_config(cols=COLS, rows=ROWS, K=K, levels=LEVELS, iters=ITERS, min_count=MIN_COUNT,
                             use_graph=mode, rgb_term=rgb, **MAP)
@@ -154,10 +187,13 @@ def label_frames(n):
 
 
 def time_device_resident(sf, ctx, frames, steps, warmup, mode, barrier, timing=False, autotune=False, rgb=0,
-                         ndet=0):
-    """Frames/s with inputs already in HBM; CUDA events on the system stream.
-    With autotune, sf_system_autotune runs half-way through the warm-up
-    (its choice is recaptured in the graph before the timed frames)."""
+                         ndet=0, flush=None):
+    """Frames/s with inputs already in HBM: one CUDA-event pair per timed
+    step on the system stream, L2 flushed before each step outside the
+    pair.  With autotune, sf_system_autotune runs half-way through the
+    warm-up (its choice is recaptured in the graph before the timed
+    frames)."""
+    import ctypes as C
     import torch
     dev = [(torch.from_numpy(d).cuda(), torch.from_numpy(c).cuda(), torch.from_numpy(m).cuda())
            for d, c, m, _ in frames[:steps + warmup]]
@@ -176,26 +212,27 @@ def time_device_resident(sf, ctx, frames, steps, warmup, mode, barrier, timing=F
                     "raycast_ms": {"%dx%d/%d" % (x, y, m): round(ms, 4) for m, x, y, ms in cands}}
     ctx.sync()
     stream = torch.cuda.ExternalStream(ctx.stream)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     barrier()
     torch.cuda.synchronize()
     l0 = launches(sf)
     sampler = ClockSampler(torch.cuda.current_device()) if not timing else None
-    e0.record(stream)
-    import ctypes as C
     ms = (C.c_float * 7)()
-    for i in range(warmup, warmup + steps):
+    for k, i in enumerate(range(warmup, warmup + steps)):
+        if flush is not None:
+            flush(stream)
+        ev[k][0].record(stream)
         s.grab_device(dev[i][0].data_ptr(), dev[i][1].data_ptr(), dev[i][2].data_ptr() if ndet else None, ndet)
+        ev[k][1].record(stream)
         if timing:
             sf.call("sf_system_stage_ms", s.h, ms)
             stage_ms += np.array(ms[:])
             stats.append(s.stats())
-    e1.record(stream)
-    e1.synchronize()
+    ev[-1][1].synchronize()
     clocks = sampler.stop() if sampler else None
     torch.cuda.synchronize()
     barrier()
-    elapsed = e0.elapsed_time(e1) / 1e3
+    elapsed = sum(a.elapsed_time(b) for a, b in ev) / 1e3
     n_launch = launches(sf) - l0
     last = s.stats()
     s.close()
@@ -238,67 +275,244 @@ def pinned(a):
     return torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
 
 
-def time_e2e(sf, ctx, frames, steps, warmup, mode, rgb=0):
-    """Frames/s through sf_system_grab with host buffers in pinned memory
-    (the H2D copies of each frame and the D2H of its stats inside)."""
+def time_e2e(sf, ctx, frames, steps, warmup, mode, rgb=0, flush=None):
+    """Frames/s through sf_system_grab with host buffers in pinned memory:
+    each step from the call to the context's synchronisation (the H2D
+    copies of the frame, the whole frame, the D2H of its stats), on the
+    host clock; L2 flushed between steps outside the timed intervals."""
+    import torch
     s = sf.System(ctx, sys_cfg(sf, mode, rgb), init_pose=frames[0][3])
     host = [(pinned(d), pinned(c)) for d, c, _, _ in frames[:warmup + steps]]
     for i in range(warmup):
         s.grab(*host[i])
     ctx.sync()
-    t0 = time.perf_counter()
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    total = 0.0
     tracked = 0
     for i in range(warmup, warmup + steps):
+        if flush is not None:
+            flush(stream)
+            ctx.sync()
+        t0 = time.perf_counter()
         st = s.grab(*host[i])
+        ctx.sync()
+        total += time.perf_counter() - t0
         tracked += st.tracked
-    t1 = time.perf_counter()
     s.close()
-    return (t1 - t0), tracked
+    return total, tracked
 
 
-def pose_error_fp64(sf, ctx, frames, n):
-    """Per frame: the GPU's ComputeSE3 pose vs the FP64 oracle's on the same
-    inputs (the frame's measured pyramid, the model maps the GPU raycast for
-    the previous frame, the previous pose).  Max over frames 1..n-1."""
+class _DevBuf:
+    """A device allocation of this library seen as a torch tensor (bytes)."""
+
+    def __init__(self, ptr, nbytes):
+        self.__cuda_array_interface__ = {"shape": (nbytes,), "typestr": "|u1", "data": (ptr, False),
+                                         "version": 3, "strides": None}
+
+
+def _dev_bytes(ptr, nbytes):
+    import torch
+    return torch.as_tensor(_DevBuf(ptr, nbytes), device="cuda")
+
+
+def _icp_bytes(iterations):
+    """ICP algorithmic bytes of one frame: 64 B per pixel per iteration
+    (current vertex + normal, gathered model vertex + normal), iterations
+    split over the levels coarse to fine as ComputeSE3 runs them (a stop
+    ends every level)."""
+    left, b = int(iterations), 0
+    for l in range(LEVELS - 1, -1, -1):
+        k = min(left, ITERS[l])
+        b += 64 * (COLS >> l) * (ROWS >> l) * k
+        left -= k
+    return b
+
+
+def stage_bytes(stats_list):
+    """Mean algorithmic bytes per frame of the stages with a byte model
+    (per-unit figures: pyramid 2WH + 4WH + 4P + 32P; ICP 64 B per pixel per
+    iteration; integration V*512*32 + 8WH; raycast 32V + V*512*8 + 32WH;
+    resize 32*(L1+L2 pixels)*5)."""
+    V = np.array([st.visible for st in stats_list], np.float64)
+    it = np.array([st.iterations for st in stats_list], np.float64)
+    wh = COLS * ROWS
+    P = sum((COLS >> l) * (ROWS >> l) for l in range(LEVELS))
+    return {"pyramid": 6 * wh + 36 * P,
+            "icp": float(np.mean([_icp_bytes(i) for i in it])),
+            "integrate": float((V * 512 * 32 + 8 * wh).mean()),
+            "raycast": float((32 * V + V * 512 * 8 + 32 * wh).mean()),
+            "resize_stats": 32 * 5 * sum((COLS >> l) * (ROWS >> l) for l in range(1, LEVELS))}, V
+
+
+def l2_copy_peak():
+    """L2-resident copy bandwidth (GB/s, read + write bytes): a 24 MiB
+    buffer copied back and forth 400 times after a warm-up; CUDA events."""
+    import torch
+    n = 24 << 20
+    a = torch.empty(n, dtype=torch.uint8, device="cuda")
+    b = torch.empty(n, dtype=torch.uint8, device="cuda")
+    a.fill_(1)
+    for _ in range(20):
+        b.copy_(a)
+        a.copy_(b)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(200):
+        b.copy_(a)
+        a.copy_(b)
+    e1.record()
+    e1.synchronize()
+    return 2 * n * 400 / (e0.elapsed_time(e1) * 1e-3) / 1e9
+
+
+def error_pass(sf, ctx, frames, steps, warmup):
+    """Accuracy of the loop against the FP64 oracle, over frames 0..W+K-1 in
+    the eager form (equal to the graph form bit for bit):
+      * pose: for every timed frame, the loop's ComputeSE3 pose against the
+        FP64 oracle's ComputeSE3 on the same inputs (the frame's measured
+        pyramid, the model maps the loop raycast for the previous frame,
+        the previous pose), max abs element of the 4x4 difference;
+      * J^T J / J^T r: for every timed frame, sf_ICPStep at the frame's
+        final pose (level 0) against the oracle's FP64 rows and sums,
+        relative to the largest diagonal entry / the largest |b|;
+      * TSDF: the oracle replays the mapping of every tracked frame with the
+        loop's poses, with an FP64 shadow of each TSDF update (same voxels,
+        distance and running average in double); max and RMS of
+        |tsdf32 - tsdf64| at the end, and whether the device map equals the
+        oracle's FP32 map voxel for voxel (per block position)."""
+    import ctypes as C
     import torch
     from oracle import oracle as O
-    s = sf.System(ctx, sys_cfg(sf, 1), init_pose=frames[0][3])
-    worst, prev = 0.0, None
-    for i in range(n):
+    s = sf.System(ctx, sys_cfg(sf, 2), init_pose=frames[0][3])
+    om = O.Map(**MAP)
+    pose_err, jtj_err, jtr_err, mism = [], [], [], 0
+    prev = None
+    dl = lambda im: ctx.download(im.data, np.float32, im.rows * im.cols * 4).reshape(im.rows, im.cols, 4)
+    Kf = lambda l: tuple(k / float(1 << l) for k in K)
+    for i in range(warmup + steps):
         d, rgb, _, _ = frames[i]
-        if i > 0:
-            mv, mn = [], []
-            for l in range(LEVELS):
-                v, nm = s.model_maps(l)
-                mv.append(ctx.download(v.data, np.float32, v.rows * v.cols * 4).reshape(v.rows, v.cols, 4))
-                mn.append(ctx.download(nm.data, np.float32, nm.rows * nm.cols * 4).reshape(nm.rows, nm.cols, 4))
+        timed = i >= warmup and i > 0
+        if timed:
+            mv, mn = zip(*[tuple(map(dl, s.model_maps(l))) for l in range(LEVELS)])
         st = s.grab(d, rgb)
-        pose = np.array(st.pose[:]).reshape(4, 4)
-        if i > 0:
-            vs, ns = [], []
-            for l in range(LEVELS):
-                v, nm, _ = s.frame_maps(l)
-                vs.append(ctx.download(v.data, np.float32, v.rows * v.cols * 4).reshape(v.rows, v.cols, 4))
-                ns.append(ctx.download(nm.data, np.float32, nm.rows * nm.cols * 4).reshape(nm.rows, nm.cols, 4))
-            ok, P64, _ = O.compute_se3(vs, ns, mv, mn, K, ITERS, MIN_COUNT, 1e-4, prev, prev, fp64=True)
+        P = np.array(st.pose[:]).reshape(4, 4)
+        if timed:
+            fm = [s.frame_maps(l) for l in range(LEVELS)]
+            vs, ns = [dl(f[0]) for f in fm], [dl(f[1]) for f in fm]
+            ok, P64, _ = O.compute_se3(vs, ns, list(mv), list(mn), K, ITERS, MIN_COUNT, 1e-4, prev, prev,
+                                       fp64=True)
             if ok == bool(st.accepted):
-                worst = max(worst, float(np.abs(P64 - pose).max()))
+                pose_err.append(float(np.abs(P64 - P).max()))
             else:
-                worst = float("inf")
-        prev = pose
+                mism += 1
+            # J^T J / J^T r at the final pose, level 0
+            mv0, mn0 = torch.from_numpy(mv[0]).cuda(), torch.from_numpy(mn[0]).cuda()
+            Rc, _, tc = sf.pose_to_gpu(P)
+            Rl, RlI, tl = sf.pose_to_gpu(prev)
+            res, A, b = (C.c_float * 2)(), (C.c_double * 36)(), (C.c_double * 6)()
+            sf.call("sf_ICPStep", ctx.h, fm[0][0], sf.image(mv0), fm[0][1], sf.image(mn0), Rc, tc, Rl, RlI, tl,
+                    sf.Intrinsics(*Kf(0)), res, A, b)
+            s64 = O.icp_sums(vs[0], mv[0], ns[0], mn[0], P, prev, Kf(0), fp64=True)
+            A64, b64 = O.create_matrix(s64)
+            A32, b32 = np.array(A[:]).reshape(6, 6), np.array(b[:])
+            jtj_err.append(float(np.abs(A32 - A64).max() / np.abs(np.diag(A64)).max()))
+            jtr_err.append(float(np.abs(b32 - b64).max() / max(np.abs(b64).max(), 1e-30)))
+            del mv0, mn0
+        if st.tracked:  # the oracle maps the frame as the loop did, with an FP64 shadow
+            raw, _ = O.filter_depth(d, 1000.0, 3.0)
+            om.alloc(raw, P, K)
+            if om.visibility(P, K, COLS, ROWS):
+                om.integrate_f64(raw, P, K)
+                om.integrate(raw, rgb, P, K)
+        prev = P
+    tsdf_max, tsdf_rms, nvox = om.tsdf_f64_error()
+    # the device map against the oracle's FP32 map, per block position
+    from oracle.oracle import ENTRY_DTYPE, VOXEL_DTYPE
+    m = s.map()
+    a = m.arrays()
+    ne = MAP["num_buckets"] + MAP["num_excess"]
+    ge = ctx.download(a.hash_entries, ENTRY_DTYPE, ne)
+    oe = np.array(om.entries)
+    gsel, osel = ge[ge["ptr"] >= 0], oe[oe["ptr"] >= 0]
+    key = lambda e: (e["x"].astype(np.int64) << 42) ^ ((e["y"].astype(np.int64) & 0x1fffff) << 21) ^ \
+        (e["z"].astype(np.int64) & 0x1fffff)
+    gk, ok_ = key(gsel), key(osel)
+    same_set = np.array_equal(np.sort(gk), np.sort(ok_))
+    map_equal = False
+    if same_set:
+        gsel, osel = gsel[np.argsort(gk)], osel[np.argsort(ok_)]
+        vox = _dev_bytes(a.voxel_blocks, MAP["num_sdf_blocks"] * 512 * 16).view(-1, 512 * 16)
+        gblk = vox[torch.from_numpy((gsel["ptr"] // 512).astype(np.int64)).cuda()].cpu().numpy()
+        ov = om.voxels.view(np.uint8).reshape(-1, 512 * 16)
+        oblk = ov[(osel["ptr"] // 512).astype(np.int64)]
+        map_equal = bool(np.array_equal(gblk, oblk))
+        del vox
     s.close()
-    return worst
+    n_t = len(pose_err) + mism
+    return {"frames": "timed frames %d..%d (pose, J^T J: %d compared); TSDF over frames 0..%d"
+                      % (warmup, warmup + steps - 1, n_t, warmup + steps - 1),
+            "pose_max": max(pose_err) if pose_err else None, "pose_mean": float(np.mean(pose_err)) if pose_err else None,
+            "acceptance_mismatch": mism,
+            "jtj_rel_max": max(jtj_err) if jtj_err else None, "jtr_rel_max": max(jtr_err) if jtr_err else None,
+            "tsdf_max": tsdf_max, "tsdf_rms": tsdf_rms, "tsdf_voxels": nvox,
+            "map_blocks": int(len(gsel)), "map_block_set_equal_fp32_oracle": bool(same_set),
+            "map_voxels_equal_fp32_oracle": map_equal}
 
 
-def cpu_reference(frames, n):
-    """The oracle loop (C++/OpenMP) over frames 0..n-1; frames/s of 1..n-1."""
-    from oracle import oracle as O
-    s = O.System(dict(MAP), COLS, ROWS, K, iters=ITERS, init_pose=frames[0][3])
-    s.grab(frames[0][0], frames[0][1])
-    t0 = time.perf_counter()
-    for i in range(1, n):
-        s.grab(frames[i][0], frames[i][1])
-    return (n - 1) / (time.perf_counter() - t0)
+def _ref_cpu_lib():
+    import ctypes as C
+    path = os.path.join(ROOT, "oracle", "_ref", "c2", "libref.so")
+    if not os.path.exists(path):
+        return None
+    L = C.CDLL(path)
+    L.refcpu_create.restype = C.c_void_p
+    L.refcpu_create.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_float), C.c_float, C.c_float,
+                                C.POINTER(C.c_double)]
+    L.refcpu_grab.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]
+    L.refcpu_destroy.argtypes = [C.c_void_p]
+    L.refcpu_threads.restype = C.c_int
+    return L
+
+
+def time_reference_cpu(frames, steps, warmup, budget_s=None):
+    """The reference's CPU implementation of the loop over frames
+    0..warmup+steps-1, frames warmup.. timed (host clock per frame).  The
+    reference's own device code compiled as host C++/OpenMP at the 640x480
+    constants (oracle/_ref/c2/libref.so) when present and the workload is
+    the 640x480 room; else the oracle port of the loop (C++/OpenMP).
+    budget_s bounds the timed frames' total time (at least two frames)."""
+    import ctypes as C
+    L = _ref_cpu_lib() if (COLS, ROWS) == (640, 480) else None
+    pose = np.zeros(16, np.float64)
+    if L is not None:
+        init = np.ascontiguousarray(frames[0][3], np.float64)
+        h = L.refcpu_create(COLS, ROWS, (C.c_float * 4)(*K), 1000.0, 3.0, init.ctypes.data_as(C.POINTER(C.c_double)))
+        grab = lambda d, c: L.refcpu_grab(h, np.ascontiguousarray(d).ctypes.data, np.ascontiguousarray(c).ctypes.data,
+                                          pose.ctypes.data_as(C.POINTER(C.c_double)))
+        kind, cores = "reference", int(L.refcpu_threads())
+        what = ("the reference's Tracking/*.cu and Mapping/*.cu compiled as host C++ (CUDA emulation header, "
+                "OpenMP over each launch's blocks) at the 640x480 constants, driven in GrabImage's order, "
+                "ICP-only ComputeSE3 (getRow per pixel, FP64 sums per thread)")
+    else:
+        from oracle import oracle as O
+        so = O.System(dict(MAP), COLS, ROWS, K, levels=LEVELS, iters=ITERS, min_count=MIN_COUNT,
+                      init_pose=frames[0][3])
+        grab = lambda d, c: so.grab(d, c)[0]
+        kind, cores = "port", omp_threads()
+        what = "the oracle loop (the reference's algorithm restated in C++/OpenMP, pinned to its kernels)"
+    for i in range(warmup):
+        grab(frames[i][0], frames[i][1])
+    total, n, tracked = 0.0, 0, 0
+    for i in range(warmup, warmup + steps):
+        t0 = time.perf_counter()
+        tracked += int(bool(grab(frames[i][0], frames[i][1])))
+        total += time.perf_counter() - t0
+        n += 1
+        if budget_s is not None and n >= 2 and total >= budget_s:
+            break
+    if L is not None:
+        L.refcpu_destroy(h)
+    return {"fps": n / total, "frames": n, "kind": kind, "cores": cores, "what": what, "tracked": tracked}
 
 
 def omp_threads():
@@ -345,36 +559,34 @@ def time_reloc(sf, ctx, frames, n=256, reps=10, seed=5):
             "note": "one launch per call; sigma 5 cm / 5 deg candidates around the tracked pose of frame %d" % k}
 
 
-def load_traffic(kernel):
-    """dram__bytes_read.sum + dram__bytes_write.sum of one launch of the kernel
-    on this workload, from the committed ncu summary (null if absent)."""
-    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", "roofline_traffic_640x480.json")
+def load_traffic(kernel, first, count):
+    """Mean dram__bytes_read.sum + dram__bytes_write.sum per launch of the
+    kernel over frames first..first+count-1 of this workload, from the
+    committed ncu capture of the same frames (None when the capture does not
+    cover them)."""
+    path = os.path.join(ROOT, "profiles", "roofline_traffic_640x480.json")
     try:
         with open(path) as f:
-            return int(json.load(f)["kernels"]["k_" + kernel]["dram_bytes"])
-    except (OSError, KeyError, ValueError):
+            per = json.load(f)["kernels"][kernel]["per_frame_dram_bytes"]
+        vals = [per[str(i)] for i in range(first, first + count)]
+        return float(np.mean(vals))
+    except (OSError, KeyError, ValueError, TypeError):
         return None
 
 
-def algorithmic_bytes(stats_list):
-    """Compulsory bytes per frame of the integration and raycast stages
-    (per-unit figures in the design doc): integration V*512*32 + 8WH (voxel
-    read+write, depth + rgb gathers); raycast 32*V + V*512*8 + 32WH (entry
-    reads, (sdf, weight) of each visible block, vertex + normal maps out)."""
-    V = np.array([st.visible for st in stats_list], np.float64)
-    wh = COLS * ROWS
-    integ = V * 512 * 32 + 8 * wh
-    ray = 32 * V + V * 512 * 8 + 32 * wh
-    return integ.mean(), ray.mean(), V.mean()
+STAGE_KERNEL = {"pyramid": "k_pyramid_levels_3", "icp": "k_icp_persistent", "integrate": "k_integrate",
+                "raycast": "k_raycast", "resize_stats": "k_resize"}
 
 
-def time_reference_cuda(frames, steps, warmup, rgb_term=False):
+def time_reference_cuda(frames, steps, warmup, rgb_term=False, flush=None):
     """The reference's own CUDA launchers (oracle/_ref/gpu_c2/librefgpu.so,
     built by oracle/ref_shim/build_ref_gpu.py) in System::GrabImage's order,
     ICP-only (or with the photometric term, the reference's default, when
-    rgb_term), host buffers in: frames/s over `steps` frames after `warmup`."""
+    rgb_term), host buffers in: frames/s over `steps` frames after `warmup`,
+    each frame timed on the host clock up to the device's synchronisation,
+    L2 flushed between frames outside the timed intervals."""
     import ctypes as C
-    lib_path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "oracle", "_ref", "gpu_c2", "librefgpu.so")
+    lib_path = os.path.join(ROOT, "oracle", "_ref", "gpu_c2", "librefgpu.so")
     if not os.path.exists(lib_path):
         return {"unavailable": "the reference's CUDA build is not present (oracle/_ref/gpu_c2 not prepared)"}
     try:
@@ -401,48 +613,58 @@ def time_reference_cuda(frames, steps, warmup, rgb_term=False):
         L.refgpu_set_rgb(h, 1)
     pose = np.zeros(16, np.float64)
     n = min(len(frames), steps + warmup)
-    tracked = 0
-    err = 0.0
+    host = [(pinned(frames[i][0]), pinned(frames[i][1])) for i in range(n)]
+    stream = torch.cuda.current_stream()
+    tracked, err, dt = 0, 0.0, 0.0
     for i in range(n):
-        if i == warmup:
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-        d, rgb = np.ascontiguousarray(frames[i][0]), np.ascontiguousarray(frames[i][1])
-        tracked += L.refgpu_grab(h, d.ctypes.data, rgb.ctypes.data, pose.ctypes.data_as(C.POINTER(C.c_double)))
-        err = max(err, float(np.abs(pose.reshape(4, 4)[:3, 3] - frames[i][3][:3, 3]).max()))
-    torch.cuda.synchronize()
-    dt = time.perf_counter() - t0
+        if i >= warmup and flush is not None:
+            flush(stream)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d, rgb = host[i]
+        tr = L.refgpu_grab(h, d.ctypes.data, rgb.ctypes.data, pose.ctypes.data_as(C.POINTER(C.c_double)))
+        torch.cuda.synchronize()
+        if i >= warmup:
+            dt += time.perf_counter() - t0
+            tracked += tr
+            err = max(err, float(np.abs(pose.reshape(4, 4)[:3, 3] - frames[i][3][:3, 3]).max()))
     L.refgpu_destroy(h)
     timed = n - warmup
     return {"value": round(timed / dt, 3), "unit": "frames/s", "steps": timed, "warmup": warmup,
             "tracked_frames": int(tracked), "max_translation_error_vs_ground_truth_m": round(err, 5),
             "kind": "reference CUDA build (Tracking/*.cu, Mapping/*.cu for sm_103a), %s ComputeSE3, "
-                    "host buffers in, the reference's per-launch synchronisation"
-                    % ("RGB-D (icpOnly = false: RGBStep + ICPStep)" if rgb_term else "ICP-only")}
+                    "pinned host buffers in, the reference's per-launch synchronisation; the same timed frames and "
+                    "L2 flush as e2e" % ("RGB-D (icpOnly = false: RGBStep + ICPStep)" if rgb_term else "ICP-only")}
 
 
 def run_reference(args):
+    """The reference arm: the reference's CPU implementation of the loop on
+    the host cores, over the same frames, steps and warm-up as the GPU arm
+    (rank 0 only); its CUDA build beside it."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    n = max(4, min(12, args.steps + 1))
-    frames = make_frames(max(n, min(args.steps + args.warmup, 300)))
-    threads = omp_threads()
-    fps = cpu_reference(frames[:n], n)
+    n = args.steps + args.warmup
+    frames = make_frames(n)
+    r = time_reference_cpu(frames, args.steps, args.warmup)
+    fps = r["fps"]
     line = {"impl": "reference", "metric": METRIC, "value": round(fps, 4), "unit": "frames/s", "n_gpus": args.gpus,
-            "steps": n - 1, "warmup": 1, "ms_per_step": round(1000.0 / fps, 3), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 6x6 solve)",
-            "data": "synthetic: " + WORKLOAD,
-            "config": {"workload": WORKLOAD, "sample": "frames 1..%d of the sequence" % (n - 1)},
-            "cpu_baseline": {"value": round(fps, 4), "unit": "frames/s", "cores": threads, "kind": "port",
-                             "sample": "frames 1..%d of the 640x480 sequence through the oracle loop "
-                                       "(the reference's algorithm restated in C++/OpenMP, pinned bit-exact to "
-                                       "the reference's own kernels)" % (n - 1)},
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000.0 / fps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 6x6 solve)",
+            "data": "synthetic: " + WORKLOAD, "config": bench_config(),
+            "cpu_baseline": {"value": round(fps, 4), "unit": "frames/s", "cores": r["cores"], "kind": r["kind"],
+                             "sample": "frames %d..%d of the sequence after %d warm-up frames: %s"
+                                       % (args.warmup, args.warmup + r["frames"] - 1, args.warmup, r["what"])},
+            "tracked_frames": r["tracked"],
             "e2e": {"value": round(fps, 4), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    line["reference_cuda"] = time_reference_cuda(frames, min(args.steps, len(frames) - args.warmup), args.warmup)
+    try:
+        flush = L2Flush()
+    except Exception:
+        flush = None
+    line["reference_cuda"] = time_reference_cuda(frames, args.steps, args.warmup, flush=flush)
     if args.config == "c2":
-        line["reference_cuda_rgbd"] = time_reference_cuda(frames, min(args.steps, len(frames) - args.warmup),
-                                                          args.warmup, rgb_term=True)
+        line["reference_cuda_rgbd"] = time_reference_cuda(frames, args.steps, args.warmup, rgb_term=True,
+                                                          flush=flush)
     print(json.dumps(line), flush=True)
 
 
@@ -454,6 +676,7 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-errors", action="store_true", help="skip the accuracy pass against the FP64 oracle")
     ap.add_argument("--map-blocks", type=int, default=19,
                     help="log2 of the voxel-block heap (2^19 blocks = 4 GB of voxels)")
     ap.add_argument("--config", default="c2", choices=["c2", "c3"],
@@ -468,10 +691,10 @@ def main():
                     help="with --quick: time the semantic mode (detections every frame) instead")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    if args.impl == "reference":
-        return run_reference(args)
     if args.config == "c3":
         use_corridor_config()
+    if args.impl == "reference":
+        return run_reference(args)
 
     import torch
     ws, rank, local = dist_env()
@@ -486,11 +709,12 @@ def main():
     import semantic_icpslam_gb300 as sf
     sf.load()
     ctx = sf.Context()
+    flush = L2Flush()
     n = args.steps + args.warmup
     MAP["num_sdf_blocks"] = 1 << args.map_blocks
     frames = make_frames(n, rank)
     if args.quick and args.labels:  # for profiler runs of the semantic mode's kernels
-        g = time_device_resident(sf, ctx, label_frames(n), args.steps, args.warmup, 1, barrier, ndet=10)
+        g = time_device_resident(sf, ctx, label_frames(n), args.steps, args.warmup, 1, barrier, ndet=10, flush=flush)
         ctx.close()
         if rank == 0:
             print(json.dumps({"labels": round(args.steps / g["elapsed"], 3), "unit": "frames/s"}), flush=True)
@@ -498,7 +722,7 @@ def main():
 
     # headline: CUDA graph, inputs in HBM
     g = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 1, barrier, autotune=args.autotune,
-                             rgb=1 if (args.quick and args.rgbd) else 0)
+                             rgb=1 if (args.quick and args.rgbd) else 0, flush=flush)
     elapsed = g["elapsed"]
     if ws > 1:
         import torch.distributed as dist
@@ -509,11 +733,7 @@ def main():
     out = {"metric": METRIC, "value": round(fps, 3), "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(1000.0 * elapsed / args.steps, 4), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 6x6 solve)",
-           "data": "synthetic: " + WORKLOAD,
-           "config": {"workload": WORKLOAD, "global_batch": "1 frame per GPU per step", "parallelism":
-                      "replicas (%d independent sequences)" % ws,
-                      "l2": "inputs larger than L2: a new frame per step from a %d-frame sequence resident in HBM "
-                            "(%.0f MB); map state carried across frames as in the loop" % (n, n * COLS * ROWS * 5 / 1e6)},
+           "data": "synthetic: " + WORKLOAD, "config": bench_config(),
            "gpu_launches": int(g["launches"]), "clocks": g["clocks"]}
     if g["autotune"]:
         out["autotune"] = g["autotune"]
@@ -523,44 +743,49 @@ def main():
         if rank == 0:
             print(json.dumps(out), flush=True)
         return
-    # per-stage timing pass (eager device-driven form, same kernels)
-    tp = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 2, barrier, timing=True)
-    integ_b, ray_b, V = algorithmic_bytes(tp["stats"])
+    # per-stage timing pass (eager device-driven form, same kernels, same frames)
+    tp = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 2, barrier, timing=True, flush=flush)
+    sbytes, V = stage_bytes(tp["stats"])
     peak, peak_kind = load_peaks()
+    l2_peak = l2_copy_peak()
     st_ms = dict(zip(STAGES, [round(float(x), 5) for x in tp["stage_ms"]]))
-    dom = max(("integrate", "raycast"), key=lambda k: st_ms[k])
     kern = {}
-    for name, b in (("integrate", integ_b), ("raycast", ray_b)):
+    for name, b in sbytes.items():
         gbs = b / (st_ms[name] * 1e-3) / 1e9
-        kern[name] = {"ms": st_ms[name], "algorithmic_bytes": int(b), "achieved_gbs": round(gbs, 1),
-                      "frac_of_%s_hbm" % peak_kind: round(gbs / peak, 4)}
+        kern[name] = {"kernel": STAGE_KERNEL[name], "ms": st_ms[name], "algorithmic_bytes": int(b),
+                      "achieved_gbs": round(gbs, 1), "frac_of_%s_hbm" % peak_kind: round(gbs / peak, 4)}
+    dom = max(sbytes, key=lambda k: st_ms[k])  # the frame's dominant kernel
     out["stages_ms"] = st_ms
     out["kernels"] = kern
-    out["visible_blocks_mean"] = round(V, 1)
+    out["visible_blocks_mean"] = round(float(V.mean()), 1)
     d = kern[dom]
-    traffic = load_traffic(dom) if args.config == "c2" else None
-    out["roofline"] = {"kernel": dom, "bound": "hbm", "achieved": d["achieved_gbs"], "peak": peak, "unit": "GB/s",
-                       "frac": d["frac_of_%s_hbm" % peak_kind], "peak_source": peak_kind,
+    traffic = load_traffic(STAGE_KERNEL[dom], args.warmup, args.steps) if args.config == "c2" else None
+    out["roofline"] = {"kernel": STAGE_KERNEL[dom], "bound": "hbm", "achieved": d["achieved_gbs"], "peak": peak,
+                       "unit": "GB/s", "frac": d["frac_of_%s_hbm" % peak_kind], "peak_source": peak_kind,
                        "traffic": traffic, "algorithmic_bytes": d["algorithmic_bytes"],
-                       "traffic_source": "profiles/roofline_traffic_640x480.json (ncu dram bytes, one launch)"
-                       if traffic else None}
+                       "traffic_source": ("profiles/roofline_traffic_640x480.json: ncu dram bytes per launch, mean "
+                                          "over the same frames %d..%d" % (args.warmup, n - 1)) if traffic else
+                       "no ncu capture of these frames",
+                       "l2": {"peak_gbs": round(l2_peak, 1), "frac": round(d["achieved_gbs"] / l2_peak, 4),
+                              "peak_source": "measured live: L2-resident 24 MiB copies (read + write bytes)"}}
 
     if not args.no_plain:
-        p = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 0, barrier)
+        p = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 0, barrier, flush=flush)
         out["plain"] = {"value": round(args.steps / p["elapsed"], 3),
                         "ms_per_step": round(1000.0 * p["elapsed"] / args.steps, 4),
                         "gpu_launches": int(p["launches"]), "frames": "the same frames as value"}
         out["graph_over_plain"] = round(out["value"] / out["plain"]["value"], 3)
 
-    e2e_t, tracked = time_e2e(sf, ctx, frames, args.steps, args.warmup, 1)
+    e2e_t, tracked = time_e2e(sf, ctx, frames, args.steps, args.warmup, 1, flush=flush)
     out["e2e"] = {"value": round(args.steps / e2e_t, 3), "unit": "frames/s",
                   "h2d_bytes_per_step": COLS * ROWS * (2 + 3), "d2h_bytes_per_step": 208,
                   "tracked_frames": int(tracked)}
     if args.config == "c2":
         # the reference's default tracking mode: ComputeSE3(icpOnly = false)
-        r = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 1, barrier, rgb=1)
-        re2e, rtracked = time_e2e(sf, ctx, frames, args.steps, args.warmup, 1, rgb=1)
-        rt = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 2, barrier, timing=True, rgb=1)
+        r = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 1, barrier, rgb=1, flush=flush)
+        re2e, rtracked = time_e2e(sf, ctx, frames, args.steps, args.warmup, 1, rgb=1, flush=flush)
+        rt = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 2, barrier, timing=True, rgb=1,
+                                  flush=flush)
         out["rgbd"] = {"value": round(args.steps / r["elapsed"], 3), "unit": "frames/s",
                        "stages_ms": dict(zip(STAGES, [round(float(x), 5) for x in rt["stage_ms"]])),
                        "e2e": round(args.steps / re2e, 3), "tracked_frames": int(rtracked),
@@ -568,26 +793,27 @@ def main():
                        "mode": "ComputeSE3 with icpOnly = false (the reference's default): RGBStep beside ICPStep "
                                "in every iteration, same frames"}
         if not args.no_plain:
-            rp = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 0, barrier, rgb=1)
+            rp = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 0, barrier, rgb=1, flush=flush)
             out["rgbd"]["plain"] = round(args.steps / rp["elapsed"], 3)
-    if args.config == "c2":
         # the semantic mode (System.cc:184-205): the same room with ten
         # labelled objects and 5% label flips, detections every frame
-        lab = time_device_resident(sf, ctx, label_frames(n), args.steps, args.warmup, 1, barrier, ndet=10)
+        lab = time_device_resident(sf, ctx, label_frames(n), args.steps, args.warmup, 1, barrier, ndet=10,
+                                   flush=flush)
         out["labels"] = {"value": round(args.steps / lab["elapsed"], 3), "unit": "frames/s",
                          "gpu_launches": int(lab["launches"]),
                          "mode": "detections every frame (10 objects, 5% label flips): FuseColor, RayTrace, "
                                  "FuseColor with the labels (label pass + UnifyNeighbor), RayTrace"}
         out["mesh"] = time_mesh(sf, ctx, frames, args.steps + args.warmup)
-    out["pose_err_fp64_max"] = pose_error_fp64(sf, ctx, frames, 6)
+    if not args.no_errors:
+        out["errors"] = error_pass(sf, ctx, frames, args.steps, args.warmup)
     if args.config == "c2":
         out["reloc"] = time_reloc(sf, ctx, frames)
-    if rank == 0 and not args.no_cpu and args.config == "c2":
-        ncpu = 6
-        fps_cpu = cpu_reference(frames, ncpu)
-        out["cpu_baseline"] = {"value": round(fps_cpu, 4), "unit": "frames/s", "cores": omp_threads(),
-                               "kind": "port", "sample": "frames 1..%d of the same sequence through the oracle "
-                                                         "loop (C++/OpenMP)" % (ncpu - 1)}
+    if rank == 0 and not args.no_cpu:
+        r = time_reference_cpu(frames, args.steps, args.warmup, budget_s=10.0)
+        out["cpu_baseline"] = {"value": round(r["fps"], 4), "unit": "frames/s", "cores": r["cores"],
+                               "kind": r["kind"],
+                               "sample": "frames %d..%d after %d warm-up frames (bounded to ~10 s): %s"
+                                         % (args.warmup, args.warmup + r["frames"] - 1, args.warmup, r["what"])}
     ctx.close()
     if rank == 0:
         print(json.dumps(out), flush=True)

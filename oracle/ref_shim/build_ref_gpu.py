@@ -15,8 +15,8 @@ oracle/_ref/gpu_c2/src (git-ignored) with two edits:
     out of bounds.  The change alters no lookup result.
 
 build() (on any machine with nvcc, the GPU machine included) compiles those
-copies for sm_103a with oracle/ref_shim/ref_gpu_driver.cu into
-oracle/_ref/gpu_c2/librefgpu.so.  Nothing here is shipped or imported by
+copies for sm_103a with oracle/ref_shim/ref_gpu_driver.cu (the loop of
+ref_loop.h) into oracle/_ref/gpu_c2/librefgpu.so.  Nothing here is shipped or imported by
 the product.
 """
 import os
@@ -80,7 +80,8 @@ def build(force=False, verbose=False):
             return None
     driver = os.path.join(HERE, "ref_gpu_driver.cu")
     srcs = [os.path.join(SRC, os.path.basename(s)) for s in SOURCES] + [driver]
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) > max(os.path.getmtime(s) for s in srcs):
+    deps = srcs + [os.path.join(HERE, "ref_loop.h"), os.path.join(ROOT, "semantic_icpslam_gb300", "csrc", "sf_solve.h")]
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) > max(os.path.getmtime(s) for s in deps):
         return LIB
     nvcc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
     nvcc = nvcc if os.path.exists(nvcc) else "nvcc"

@@ -3,6 +3,8 @@
 // driven in System::GrabImage's order by ref_loop.h: the reference's own
 // loop on the host cores, the benchmark's CPU baseline.  ICP-only tracking.
 // Test and benchmark infrastructure, never shipped.
+#include <omp.h>
+
 #include "ref_loop.h"
 
 thread_local uint3 threadIdx;
@@ -19,3 +21,5 @@ extern "C" int refcpu_grab(void *h, const uint16_t *depth, const uint8_t *rgb, d
   return refloop_grab(h, depth, rgb, pose_out);
 }
 extern "C" void refcpu_destroy(void *h) { refloop_destroy(h); }
+// Host threads the OpenMP launches use.
+extern "C" int refcpu_threads() { return omp_get_max_threads(); }
