@@ -371,7 +371,12 @@ def error_pass(sf, ctx, frames, steps, warmup):
       * pose: for every timed frame, the loop's ComputeSE3 pose against the
         FP64 oracle's ComputeSE3 on the same inputs (the frame's measured
         pyramid, the model maps the loop raycast for the previous frame,
-        the previous pose), max abs element of the 4x4 difference;
+        the previous pose), max abs element of the 4x4 difference; beside
+        it the FP32 oracle's (the reference's arithmetic) on the same
+        inputs, against the loop and against FP64, and the largest error
+        over the frames where FP64 runs as many iterations as the loop
+        (ComputeSE3's divergence guard is discontinuous in the error, so a
+        rounding-level difference can end a level one iteration earlier);
       * J^T J / J^T r: for every timed frame, sf_ICPStep at the frame's
         final pose (level 0) against the oracle's FP64 rows and sums,
         relative to the largest diagonal entry / the largest |b|;
@@ -386,6 +391,7 @@ def error_pass(sf, ctx, frames, steps, warmup):
     s = sf.System(ctx, sys_cfg(sf, 2), init_pose=frames[0][3])
     om = O.Map(**MAP)
     pose_err, jtj_err, jtr_err, mism = [], [], [], 0
+    e32, ref32, worst, same_it = [], [], None, []
     prev = None
     dl = lambda im: ctx.download(im.data, np.float32, im.rows * im.cols * 4).reshape(im.rows, im.cols, 4)
     Kf = lambda l: tuple(k / float(1 << l) for k in K)
@@ -399,10 +405,21 @@ def error_pass(sf, ctx, frames, steps, warmup):
         if timed:
             fm = [s.frame_maps(l) for l in range(LEVELS)]
             vs, ns = [dl(f[0]) for f in fm], [dl(f[1]) for f in fm]
-            ok, P64, _ = O.compute_se3(vs, ns, list(mv), list(mn), K, ITERS, MIN_COUNT, 1e-4, prev, prev,
-                                       fp64=True)
+            ok, P64, s64st = O.compute_se3(vs, ns, list(mv), list(mn), K, ITERS, MIN_COUNT, 1e-4, prev, prev,
+                                           fp64=True)
+            ok32, P32, s32st = O.compute_se3(vs, ns, list(mv), list(mn), K, ITERS, MIN_COUNT, 1e-4, prev, prev,
+                                             fp64=False)
             if ok == bool(st.accepted):
-                pose_err.append(float(np.abs(P64 - P).max()))
+                e = float(np.abs(P64 - P).max())
+                pose_err.append(e)
+                if int(s64st[2]) == int(st.iterations):
+                    same_it.append(e)
+                e32.append(float(np.abs(P32 - P).max()))
+                ref32.append(float(np.abs(P32 - P64).max()))
+                if e >= max(pose_err):
+                    worst = {"frame": i, "err": e, "iterations": int(st.iterations),
+                             "iterations_fp64": int(s64st[2]), "iterations_fp32_oracle": int(s32st[2]),
+                             "fp32_oracle_vs_fp64": ref32[-1]}
             else:
                 mism += 1
             # J^T J / J^T r at the final pose, level 0
@@ -415,8 +432,12 @@ def error_pass(sf, ctx, frames, steps, warmup):
             s64 = O.icp_sums(vs[0], mv[0], ns[0], mn[0], P, prev, Kf(0), fp64=True)
             A64, b64 = O.create_matrix(s64)
             A32, b32 = np.array(A[:]).reshape(6, 6), np.array(b[:])
-            jtj_err.append(float(np.abs(A32 - A64).max() / np.abs(np.diag(A64)).max()))
-            jtr_err.append(float(np.abs(b32 - b64).max() / max(np.abs(b64).max(), 1e-30)))
+            # J^T J relative to its largest diagonal entry; J^T r relative to
+            # its natural scale sqrt(max diag(J^T J) * sum r^2) (J^T r itself
+            # is near zero at a converged pose)
+            dmax = np.abs(np.diag(A64)).max()
+            jtj_err.append(float(np.abs(A32 - A64).max() / dmax))
+            jtr_err.append(float(np.abs(b32 - b64).max() / np.sqrt(dmax * max(s64[27], 1e-30))))
             del mv0, mn0
         if st.tracked:  # the oracle maps the frame as the loop did, with an FP64 shadow
             raw, _ = O.filter_depth(d, 1000.0, 3.0)
@@ -452,6 +473,11 @@ def error_pass(sf, ctx, frames, steps, warmup):
     return {"frames": "timed frames %d..%d (pose, J^T J: %d compared); TSDF over frames 0..%d"
                       % (warmup, warmup + steps - 1, n_t, warmup + steps - 1),
             "pose_max": max(pose_err) if pose_err else None, "pose_mean": float(np.mean(pose_err)) if pose_err else None,
+            "pose_worst": worst,
+            "pose_max_same_iterations": max(same_it) if same_it else None,
+            "frames_same_iterations": len(same_it),
+            "pose_vs_fp32_oracle_max": max(e32) if e32 else None,
+            "fp32_oracle_vs_fp64_max": max(ref32) if ref32 else None,
             "acceptance_mismatch": mism,
             "jtj_rel_max": max(jtj_err) if jtj_err else None, "jtr_rel_max": max(jtr_err) if jtr_err else None,
             "tsdf_max": tsdf_max, "tsdf_rms": tsdf_rms, "tsdf_voxels": nvox,
