@@ -27,6 +27,7 @@ timed on the host cores over the same frames; beside it the reference's CUDA
 build on the GPU.
 """
 import argparse
+import ctypes as C
 import json
 import os
 import subprocess
@@ -545,6 +546,52 @@ def omp_threads():
     return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
 
 
+def time_validate(sf, ctx, frames, n=256, reps=3, seed=5):
+    """Tracker::ValidatePose over n candidate poses (the true pose and seeded
+    5 cm / 5 deg perturbations) against one 640x480 frame
+    (sf_ValidatePoseBatch: visibility, raycast, resize and ComputeSE3 with
+    ITERATIONS_RELOC {3, 3, 2} for every candidate), after the sequence's
+    first frames are fused.  Milliseconds per call through the C ABI (host
+    poses in, host results out), mean of reps after one warm-up."""
+    s = sf.System(ctx, sys_cfg(sf, 2), init_pose=frames[0][3])
+    k = min(8, len(frames) - 2)
+    for i in range(k):
+        s.grab(frames[i][0], frames[i][1])
+    m = s.map()
+    s.grab(frames[k][0], frames[k][1])  # frame k's pyramid: the frame to relocalise
+    nxt = [s.frame_maps(l)[:2] for l in range(LEVELS)]
+    P = np.array(s.stats().pose[:], np.float64).reshape(4, 4)
+    rng = np.random.default_rng(seed)
+    cand = [P]
+    for _ in range(n - 1):
+        w = rng.normal(0, np.deg2rad(5.0), 3)
+        th = np.linalg.norm(w)
+        Kx = np.array([[0, -w[2], w[1]], [w[2], 0, -w[0]], [-w[1], w[0], 0]]) / max(th, 1e-12)
+        Q = P.copy()
+        Q[:3, :3] = (np.eye(3) + np.sin(th) * Kx + (1 - np.cos(th)) * Kx @ Kx) @ P[:3, :3]
+        Q[:3, 3] += rng.normal(0, 0.05, 3)
+        cand.append(Q)
+    cand = np.array(cand)
+    # LastFrame's maps: the model maps the loop ray traced for frame k - 1
+    # (now overwritten by frame k's); frame k's raycast stands in for them
+    lv = [v for v, _ in [s.model_maps(l) for l in range(LEVELS)]]
+    ln = [n_ for _, n_ in [s.model_maps(l) for l in range(LEVELS)]]
+    args = (ctx, m, [v for v, _ in nxt], [n_ for _, n_ in nxt], lv, ln, K, cand, (3, 3, 2)[:LEVELS],
+            MIN_COUNT[:LEVELS], 1e-3, 512)
+    out, chosen = sf.validate_pose_batch(*args)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        out, chosen = sf.validate_pose_batch(*args)
+    ms = (time.perf_counter() - t0) * 1e3 / reps
+    s.close()
+    return {"candidates": n, "pixels": int(COLS * ROWS), "ms_per_call": round(ms, 3),
+            "evaluated": int(sum(c.evaluated for c in out)), "accepted": int(sum(c.accepted for c in out)),
+            "chosen": int(chosen), "true_pose_accepted": bool(out[0].accepted),
+            "note": "Tracker::ValidatePose per candidate (UpdateVisibility, RayTrace, ResizeImages, ComputeSE3 "
+                    "{3, 3, 2}) for all candidates in one call; sigma 5 cm / 5 deg around the tracked pose of "
+                    "frame %d" % k}
+
+
 def time_reloc(sf, ctx, frames, n=256, reps=10, seed=5):
     """RelocScoreBatch on the workload: n candidate poses (the true pose and
     seeded 5 cm / 5 deg perturbations) scored against one 640x480 frame in one
@@ -804,7 +851,8 @@ def main():
 
     e2e_t, tracked = time_e2e(sf, ctx, frames, args.steps, args.warmup, 1, flush=flush)
     out["e2e"] = {"value": round(args.steps / e2e_t, 3), "unit": "frames/s",
-                  "h2d_bytes_per_step": COLS * ROWS * (2 + 3), "d2h_bytes_per_step": 208,
+                  "h2d_bytes_per_step": COLS * ROWS * (2 + 3),
+                  "d2h_bytes_per_step": C.sizeof(sf._lib.FrameStats),
                   "tracked_frames": int(tracked)}
     if args.config == "c2":
         # the reference's default tracking mode: ComputeSE3(icpOnly = false)
@@ -833,7 +881,8 @@ def main():
     if not args.no_errors:
         out["errors"] = error_pass(sf, ctx, frames, args.steps, args.warmup)
     if args.config == "c2":
-        out["reloc"] = time_reloc(sf, ctx, frames)
+        out["validate_pose"] = time_validate(sf, ctx, frames)
+        out["reloc_score"] = time_reloc(sf, ctx, frames)
     if rank == 0 and not args.no_cpu:
         r = time_reference_cpu(frames, args.steps, args.warmup, budget_s=10.0)
         out["cpu_baseline"] = {"value": round(r["fps"], 4), "unit": "frames/s", "cores": r["cores"],

@@ -389,6 +389,45 @@ int sf_RelocScoreBatch(sf_context *ctx, sf_map *map, sf_image vmap, int stride,
                        const double *poses, int n, float inlier_sdf,
                        sf_reloc_score *scores_out);
 
+/* Tracker::ValidatePose (Tracking/Tracking.cc:750-790) for n candidate
+ * poses against one frame, batched into a few launches over all candidates.
+ * For each candidate (host double[16], camera -> world): UpdateVisibility
+ * at the pose (`visible`); when visible >= min_visible (512 in the
+ * reference), RayTrace into the candidate's own model maps (`rendered`;
+ * a candidate that draws nothing tracks, as in the reference, against the
+ * maps of the closest earlier candidate that drew, else last_vmaps /
+ * last_nmaps), ResizeMap, and ComputeSE3(icpOnly = true, iters, thresh)
+ * from the pose (ITERATIONS_RELOC {3, 3, 2} and THRESH_ICP_RELOC 1e-3 in
+ * the reference, Tracking.h:111,119) against the frame's next_vmaps /
+ * next_nmaps (`levels` images each, level 0 first; float4).  out (host
+ * [n]) gets each candidate's result; *chosen (may be NULL) the candidate
+ * ValidatePose keeps, or -1: the first accepted one in candidate order
+ * (the reference's cv::sortIdx of its N x 1 error matrix sorts each row,
+ * so its index 0 always names the first).  The reference then runs the
+ * full ComputeSE3 from that candidate's pose (not its refined pose).  The
+ * map is read, not changed; its block-pointer window is rebuilt.
+ * 1 <= n <= 65535; the call allocates its workspace on first use (about
+ * 13 MB per candidate at 640x480) and synchronises the context stream. */
+typedef struct {
+  uint32_t visible;   /* UpdateVisibility's count at the candidate pose   */
+  int rendered;       /* RayTrace drew this candidate's own model maps    */
+  int evaluated;      /* visible >= min_visible: ComputeSE3 ran           */
+  int accepted;       /* ComputeSE3 accepted the refined pose             */
+  int fail;           /* 0 ok, 1 ICP count/NaN failure, 2 diverged        */
+  int iterations;     /* ICP iterations run                               */
+  float icp_error;    /* lastIcpError: sqrt(sum r^2) / count              */
+  int icp_count;
+  double pose[16];    /* NextFrame->pose after ComputeSE3 (the candidate
+                         itself when rejected or not evaluated)           */
+} sf_reloc_candidate;
+int sf_ValidatePoseBatch(sf_context *ctx, sf_map *map, int levels,
+                         const sf_image *next_vmaps, const sf_image *next_nmaps,
+                         const sf_image *last_vmaps, const sf_image *last_nmaps,
+                         sf_intrinsics K0, const double *poses, int n,
+                         const int *iters, const int *min_count, float thresh,
+                         uint32_t min_visible, sf_reloc_candidate *out,
+                         int *chosen);
+
 /* ------------------------------------------------------- whole frame loop */
 /* System::GrabImage (Core/System.cc:131-270) with Tracker::GrabFrame /
  * Track / ComputeSE3(icpOnly) (Tracking/Tracking.cc:65-173,246-280,369-517),
@@ -428,6 +467,10 @@ typedef struct {
   double pose[16];         /* camera->world pose after this frame          */
   float rgb_error;         /* photometric error of the last iteration      */
   int rgb_count;           /* photometric correspondences                  */
+  int state;               /* Tracker state of the NEXT frame: 1 initialise,
+                              0 track, -1 lost (Tracking.cc:65-119)        */
+  int missed;              /* Tracker::noMissedFrames                      */
+  int relocalised;         /* this frame was relocalised (Relocalise)      */
 } sf_frame_stats;
 
 int sf_system_create(sf_context *ctx, const sf_system_config *cfg,
@@ -446,6 +489,19 @@ int sf_system_grab(sf_system *sys, const uint16_t *depth, const uint8_t *rgb,
 int sf_system_grab_device(sf_system *sys, const uint16_t *depth, const uint8_t *rgb,
                           const uint8_t *mask, int num_detection);
 int sf_system_stats(sf_system *sys, sf_frame_stats *stats);
+/* Relocalisation candidates (Tracker::Relocalise, Tracking/Tracking.cc
+ * :107-116, 560-790): host double[n][16] camera -> world poses, copied.
+ * Track() counts frames in a row whose ComputeSE3 fails; after ten the
+ * tracker is lost (stats.state == -1).  Every later frame that starts lost
+ * and finds candidates registered runs Relocalise's validation as
+ * sf_ValidatePoseBatch does, then the final ComputeSE3 from the candidate
+ * it keeps; accepted, the frame is tracked and mapped (stats.relocalised).
+ * The candidates stand in for the poses the reference estimates from SURF
+ * matches, which are outside this loop.  Such frames run host-driven in
+ * every form.  n = 0 clears the candidates (lost frames are then skipped).
+ * With candidates registered, sf_system_grab_device reads the tracker state
+ * back before each frame (a stream synchronisation). */
+int sf_system_set_reloc_candidates(sf_system *sys, const double *poses, int n);
 /* Device views of the model maps (the last frame's raycast prediction,
  * level l) and of the current frame's measured maps. */
 int sf_system_model_maps(sf_system *sys, int level, sf_image *vmap, sf_image *nmap);

@@ -77,6 +77,9 @@ def lib():
                 "sfo_alloc": (None, [vp, F32P, C.c_int, C.c_int, F32P, F32P] + [C.c_float] * 4),
                 "sfo_visibility": (C.c_uint, [vp, F32P, F32P, F32P, C.c_int, C.c_int] + [C.c_float] * 6),
                 "sfo_integrate": (None, [vp, F32P, U8P, C.c_int, C.c_int, F32P, F32P] + [C.c_float] * 6),
+                "sfo_validate_pose_batch": (C.c_int, [vp, C.c_int, C.c_int, C.c_int] + [vp] * 4
+                                            + [F32P, F64P, C.c_int, I32P, I32P, C.c_float, C.c_uint, F64P]),
+                "sfo_system_set_reloc": (None, [vp, F64P, C.c_int]),
                 "sfo_integrate_f64": (None, [vp, F32P, C.c_int, C.c_int, F32P, F32P, F64P] + [C.c_float] * 6),
                 "sfo_tsdf_f64_error": (None, [vp, F64P]),
                 "sfo_semantics": (None, [vp, F32P, U8P, F32P, U8P, C.c_int, C.c_int, C.c_int, F32P, F32P] + [C.c_float] * 6),
@@ -242,6 +245,26 @@ def compute_se3(vnext, nnext, vlast, nlast, K, iters, min_count, thresh, last_po
                                   _p(Kf, F32P), _p(it, I32P), _p(mc, I32P), thresh, _p(lp, F64P),
                                   _p(npose, F64P), int(fp64), _p(stats, F64P))
     return bool(ok), npose, (stats if rgb is not None else stats[:4])
+
+
+def validate_pose_batch(m, vnext, nnext, vlast, nlast, K, poses, iters=(3, 3, 2), min_count=(2000, 1000, 100),
+                        thresh=1e-3, min_visible=512):
+    """Tracker::ValidatePose over n candidates (sfo_validate_pose_batch).
+    Returns (n x 24 array of per-candidate results, chosen index or -1)."""
+    L = len(vnext)
+    keep = [_f32(a) for a in list(vnext) + list(nnext) + list(vlast) + list(nlast)]
+    arr = lambda k: (C.c_void_p * L)(*[a.ctypes.data for a in keep[k * L:(k + 1) * L]])
+    rows, cols = keep[0].shape[:2]
+    P = np.ascontiguousarray(np.asarray(poses, np.float64).reshape(-1, 16))
+    n = P.shape[0]
+    Kf = np.asarray(K, np.float32)
+    it = np.asarray([iters[l] if l < len(iters) else 0 for l in range(L)], np.int32)
+    mc = np.asarray([min_count[l] if l < len(min_count) else 0 for l in range(L)], np.int32)
+    out = np.zeros((n, 24), np.float64)
+    chosen = lib().sfo_validate_pose_batch(m.h, L, cols, rows, arr(0), arr(1), arr(2), arr(3), _p(Kf, F32P),
+                                           _p(P, F64P), n, _p(it, I32P), _p(mc, I32P), float(thresh),
+                                           int(min_visible), _p(out, F64P))
+    return out, int(chosen)
 
 
 def mc_tables():
@@ -503,6 +526,12 @@ class System:
             lib().sfo_system_destroy(self.h)
             self.h = None
 
+    def set_reloc(self, poses):
+        """Relocalisation candidates (n x 4 x 4 camera->world) for lost frames."""
+        P = np.ascontiguousarray(np.asarray(poses, np.float64).reshape(-1, 16))
+        self._reloc = P
+        lib().sfo_system_set_reloc(self.h, _p(P, F64P), int(P.shape[0]))
+
     def set_mapping(self, enabled):
         """Tracker::mappingDisabled = not enabled (localisation mode)."""
         lib().sfo_system_set_mapping(self.h, int(bool(enabled)))
@@ -512,7 +541,7 @@ class System:
         rgb = np.ascontiguousarray(rgb, np.uint8)
         m = np.zeros(d.shape, np.uint8) if mask is None else np.ascontiguousarray(mask, np.uint8)
         pose = np.zeros(16, np.float64)
-        stats = np.zeros(10, np.float64)
+        stats = np.zeros(13, np.float64)
         ok = lib().sfo_system_grab(self.h, _p(d, U16P), _p(rgb, U8P), _p(m, U8P), num_detection,
                                    _p(pose, F64P), _p(stats, F64P))
         return bool(ok), pose.reshape(4, 4), stats

@@ -2082,6 +2082,72 @@ extern "C" double sfo_raycast_smooth_f64(sfo_map *m, const float *gv, const floa
   return L;
 }
 
+// Tracker::ValidatePose (Tracking.cc:750-790) over n candidates, one after
+// another as the reference runs them.  LastFrame's maps start as the
+// caller's last maps (all levels); a candidate with at least min_visible
+// visible blocks ray traces into level 0 when CreateRenderingBlocks finds a
+// block (else level 0 keeps what the previous candidate left), ResizeImages
+// remakes the levels below, and ComputeSE3(icpOnly = true, iters, thresh)
+// runs from the candidate.  out per candidate, 24 doubles: visible,
+// rendered, evaluated, accepted, fail code (ComputeSE3's: 1 count / NaN,
+// 2 rejected or diverged, 0 accepted), iterations, icp error, icp count,
+// then the pose after ComputeSE3 (16).  Returns the first accepted
+// candidate, the one ValidatePose keeps, or -1.
+extern "C" int sfo_validate_pose_batch(sfo_map *m, int levels, int cols, int rows, const float *const *nv,
+                                       const float *const *nn, const float *const *lv, const float *const *ln,
+                                       const float *K, const double *poses, int n, const int *iters,
+                                       const int *min_count, float thresh, unsigned min_visible, double *out) {
+  std::vector<std::vector<float>> wv(levels), wn(levels);
+  std::vector<int> cs(levels), rs(levels);
+  std::vector<const float *> pv(levels), pn(levels);
+  for (int l = 0; l < levels; ++l) {
+    cs[l] = cols >> l;
+    rs[l] = rows >> l;
+    const size_t e = 4 * (size_t)cs[l] * rs[l];
+    wv[l].assign(lv[l], lv[l] + e);
+    wn[l].assign(ln[l], ln[l] + e);
+    pv[l] = wv[l].data();
+    pn[l] = wn[l].data();
+  }
+  const int zc = (cols + 7) / 8, zr = (rows + 7) / 8;
+  std::vector<float> zmin((size_t)zc * zr), zmax((size_t)zc * zr);
+  const float invfx = (float)(1.0 / (double)K[0]), invfy = (float)(1.0 / (double)K[1]);
+  int chosen = -1;
+  for (int c = 0; c < n; ++c) {
+    const double *P = poses + 16 * (size_t)c;
+    double *o = out + 24 * (size_t)c;
+    for (int k = 0; k < 24; ++k) o[k] = 0.0;
+    for (int k = 0; k < 16; ++k) o[8 + k] = P[k];
+    float R[9], RI[9], t[3];
+    pose_to_gpu(P, R, RI, t);
+    const unsigned no = sfo_visibility(m, R, RI, t, cols, rows, K[0], K[1], K[2], K[3], m->c.depth_max,
+                                       m->c.depth_min);
+    o[0] = no;
+    if (no < min_visible) continue;
+    o[2] = 1;
+    const int drew = sfo_zrange(m, zmin.data(), zmax.data(), zc, zr, m->c.depth_max, m->c.depth_min, RI, t, K[0],
+                                K[1], K[2], K[3], nullptr, 0, nullptr);
+    if (drew)
+      sfo_raycast(m, wv[0].data(), wn[0].data(), cols, rows, zmin.data(), zmax.data(), zc, zr, R, RI, t, invfx,
+                  invfy, K[2], K[3]);
+    o[1] = drew ? 1 : 0;
+    for (int l = 1; l < levels; ++l)
+      sfo_resize(wv[l - 1].data(), wn[l - 1].data(), cs[l - 1], rs[l - 1], wv[l].data(), wn[l].data(), cs[l], rs[l]);
+    double np[16], st[6] = {0, 0, 0, 0, 0, 0};
+    memcpy(np, P, sizeof(np));
+    const int ok = sfo_compute_se3_ex(levels, cs.data(), rs.data(), nv, nn, pv.data(), pn.data(), nullptr, nullptr,
+                                      nullptr, nullptr, K, iters, min_count, thresh, P, np, 0, st);
+    o[3] = ok;
+    o[4] = st[3];
+    o[5] = st[2];
+    o[6] = st[0];
+    o[7] = st[1];
+    for (int k = 0; k < 16; ++k) o[8 + k] = np[k];
+    if (ok && chosen < 0) chosen = c;
+  }
+  return chosen;
+}
+
 // =============================================================== whole loop
 struct sfo_frame {
   std::vector<float> raw;
@@ -2097,7 +2163,10 @@ struct sfo_system {
   std::vector<int> iters, min_count;
   sfo_frame fa, fb;
   sfo_frame *next = &fa, *last = &fb;
-  int state = 1;  // 1 = init, 0 = tracking (Tracking.cc:65-119)
+  int state = 1;  // the next frame's state: 1 init, 0 tracking, -1 lost (Tracking.cc:65-119)
+  int prev_state = 0;  // the state the last frame ran in
+  int missed = 0;      // Tracker::noMissedFrames
+  std::vector<double> reloc;  // relocalisation candidates, n x 16
   int rgb = 0;    // 1: ComputeSE3(icpOnly = false), the reference's default
   int mapping = 1;  // 0: localisation mode (Tracker::mappingDisabled)
   double init_pose[16];
@@ -2168,6 +2237,9 @@ extern "C" sfo_system *sfo_system_create(const sfo_config *cfg, int cols, int ro
 }
 extern "C" void sfo_system_destroy(sfo_system *s) { sfo_map_destroy(s->map); delete s; }
 extern "C" void sfo_system_set_rgb(sfo_system *s, int on) { s->rgb = on != 0; }
+extern "C" void sfo_system_set_reloc(sfo_system *s, const double *poses, int n) {
+  s->reloc.assign(poses, poses + 16 * (size_t)n);
+}
 extern "C" void sfo_system_set_mapping(sfo_system *s, int on) { s->mapping = on != 0; }
 extern "C" sfo_map *sfo_system_map(sfo_system *s) { return s->map; }
 extern "C" const float *sfo_system_vmap(sfo_system *s, int l) { return s->last->vmap[l].data(); }
@@ -2175,22 +2247,64 @@ extern "C" const float *sfo_system_nmap(sfo_system *s, int l) { return s->last->
 
 // System::GrabImage (Core/System.cc:131-270) with Tracker::GrabFrame /
 // Track / TrackFrame (Tracking.cc:65-173,246-280): icp-only tracking (or
-// the photometric term, sfo_system_set_rgb), no keyframes / SURF /
-// relocalisation (a lost frame is skipped and the next frame is tracked
-// against the same model).  num_detection > 0 stands for the semantic
-// mode's detections of this frame (gap_semantic = 1).
+// the photometric term, sfo_system_set_rgb), no keyframes or SURF.  A
+// missed frame is skipped and the next frame is tracked against the same
+// model; after ten misses in a row the tracker is lost, and a lost frame
+// relocalises against the candidates of sfo_system_set_reloc (Relocalise's
+// ValidatePose and final ComputeSE3, Tracking.cc:107-116, 750-790; the
+// candidates stand in for its SURF pose estimates).  num_detection > 0
+// stands for the semantic mode's detections of this frame (gap_semantic =
+// 1).
 extern "C" int sfo_system_grab(sfo_system *s, const uint16_t *depth, const uint8_t *rgb,
                                const uint8_t *mask, int num_detection, double *pose_out,
                                double *stats) {
   resize_images(s, *s->last);
   fill_images(s, *s->next, depth);
   if (s->rgb) fill_intensity(s, *s->next, rgb);
-  int tracked = 1;
   double st[6] = {0, 0, 0, 0, 0, 0};
-  if (s->state == 1) {
+  const int state = s->state;
+  int ok = 0, relocalised = 0;
+  if (state == 1) {
     memcpy(s->next->pose, s->init_pose, sizeof(s->init_pose));
-    std::swap(s->next, s->last);
-    s->state = 0;
+    ok = 1;
+  } else if (state == -1) {
+    const int n = (int)(s->reloc.size() / 16);
+    if (n > 0) {
+      std::vector<int> it(s->levels), mc(s->levels);
+      std::vector<const float *> vn(s->levels), nn(s->levels), vl(s->levels), nl(s->levels);
+      for (int l = 0; l < s->levels; ++l) {
+        it[l] = l < 3 ? (l < 2 ? 3 : 2) : 0;  // ITERATIONS_RELOC {3, 3, 2} (Tracking.h:111)
+        mc[l] = s->min_count[l];
+        vn[l] = s->next->vmap[l].data(); nn[l] = s->next->nmap[l].data();
+        vl[l] = s->last->vmap[l].data(); nl[l] = s->last->nmap[l].data();
+      }
+      std::vector<double> out(24 * (size_t)n);
+      const int chosen = sfo_validate_pose_batch(s->map, s->levels, s->cols, s->rows, vn.data(), nn.data(), vl.data(),
+                                                 nl.data(), s->K, s->reloc.data(), n, it.data(), mc.data(), 1e-3f,
+                                                 512u, out.data());
+      if (chosen >= 0) {
+        // LastFrame->pose = the kept candidate; UpdateVisibility, RayTrace,
+        // ResizeImages there; ComputeSE3 from it (Tracking.cc:780-789)
+        sfo_frame &l = *s->last;
+        memcpy(l.pose, s->reloc.data() + 16 * (size_t)chosen, sizeof(l.pose));
+        float R[9], RI[9], t[3];
+        pose_to_gpu(l.pose, R, RI, t);
+        sfo_visibility(s->map, R, RI, t, s->cols, s->rows, s->K[0], s->K[1], s->K[2], s->K[3], s->map->c.depth_max,
+                       s->map->c.depth_min);
+        if (sfo_zrange(s->map, s->zmin.data(), s->zmax.data(), s->zc, s->zr, s->map->c.depth_max, s->map->c.depth_min,
+                       RI, t, s->K[0], s->K[1], s->K[2], s->K[3], nullptr, 0, nullptr))
+          sfo_raycast(s->map, l.vmap[0].data(), l.nmap[0].data(), s->cols, s->rows, s->zmin.data(), s->zmax.data(),
+                      s->zc, s->zr, R, RI, t, (float)(1.0 / (double)s->K[0]), (float)(1.0 / (double)s->K[1]),
+                      s->K[2], s->K[3]);
+        resize_images(s, l);
+        memcpy(s->next->pose, l.pose, sizeof(l.pose));
+        std::vector<int> cols(s->levels), rows(s->levels);
+        for (int k = 0; k < s->levels; ++k) { cols[k] = s->cols >> k; rows[k] = s->rows >> k; }
+        ok = sfo_compute_se3_ex(s->levels, cols.data(), rows.data(), vn.data(), nn.data(), vl.data(), nl.data(),
+                                nullptr, nullptr, nullptr, nullptr, s->K, s->iters.data(), s->min_count.data(),
+                                s->icp_thresh, l.pose, s->next->pose, 0, st);
+      }
+    }
   } else {
     memcpy(s->next->pose, s->last->pose, sizeof(s->last->pose));
     std::vector<int> cols(s->levels), rows(s->levels);
@@ -2204,12 +2318,30 @@ extern "C" int sfo_system_grab(sfo_system *s, const uint16_t *depth, const uint8
       in[l] = s->next->image[l].data(); il[l] = s->last->image[l].data();
       gx[l] = s->next->dIdx[l].data(); gy[l] = s->next->dIdy[l].data();
     }
-    tracked = sfo_compute_se3_ex(s->levels, cols.data(), rows.data(), vn.data(), nn.data(), vl.data(),
-                                 nl.data(), s->rgb ? in.data() : nullptr, il.data(), gx.data(), gy.data(), s->K,
-                                 s->iters.data(), s->min_count.data(), s->icp_thresh, s->last->pose,
-                                 s->next->pose, 0, st);
-    if (tracked) std::swap(s->next, s->last);
+    ok = sfo_compute_se3_ex(s->levels, cols.data(), rows.data(), vn.data(), nn.data(), vl.data(),
+                            nl.data(), s->rgb ? in.data() : nullptr, il.data(), gx.data(), gy.data(), s->K,
+                            s->iters.data(), s->min_count.data(), s->icp_thresh, s->last->pose,
+                            s->next->pose, 0, st);
   }
+  // Track()'s state machine (Tracking.cc:65-119)
+  int tracked = 0, next_state = 0;
+  if (state == 1) {
+    tracked = 1;
+  } else if (state == 0) {
+    if (ok) {
+      s->missed = 0;
+      tracked = s->prev_state != -1;
+    } else if (++s->missed > 9) {
+      next_state = -1;
+    }
+  } else {
+    tracked = ok;
+    next_state = ok ? 0 : -1;
+    relocalised = ok;
+  }
+  s->prev_state = state;
+  s->state = next_state;
+  if (tracked) std::swap(s->next, s->last);
   unsigned nvis = 0;
   if (tracked) {
     sfo_frame &f = *s->last;
@@ -2266,6 +2398,7 @@ extern "C" int sfo_system_grab(sfo_system *s, const uint16_t *depth, const uint8
     stats[0] = st[0]; stats[1] = st[1]; stats[2] = st[2]; stats[3] = st[3];
     stats[4] = nvis; stats[5] = c[0]; stats[6] = c[1]; stats[7] = c[3];
     if (s->rgb) { stats[8] = st[4]; stats[9] = st[5]; }
+    stats[10] = s->state; stats[11] = s->missed; stats[12] = relocalised;
   }
   return tracked;
 }

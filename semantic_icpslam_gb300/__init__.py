@@ -165,6 +165,12 @@ class System:
              num_detection, C.byref(st))
         return st
 
+    def set_reloc_candidates(self, poses):
+        """sf_system_set_reloc_candidates: candidate camera->world poses
+        (n x 4 x 4) tried by every frame that starts lost."""
+        P = np.ascontiguousarray(np.asarray(poses, np.float64).reshape(-1, 16))
+        call("sf_system_set_reloc_candidates", self.h, P.ctypes.data_as(_lib.F64P), int(P.shape[0]))
+
     def grab_device(self, depth_ptr, rgb_ptr, mask_ptr=None, num_detection=0):
         call("sf_system_grab_device", self.h, depth_ptr, rgb_ptr, mask_ptr, num_detection)
 
@@ -223,6 +229,25 @@ def system_config(cols, rows, K, voxel_size, trunc_dist, num_buckets, num_excess
     cfg.use_graph = use_graph
     cfg.rgb_term = int(rgb_term)
     return cfg
+
+
+def validate_pose_batch(ctx, m, next_vmaps, next_nmaps, last_vmaps, last_nmaps, K, poses, iters=(3, 3, 2),
+                        min_count=(2000, 1000, 100), thresh=1e-3, min_visible=512):
+    """sf_ValidatePoseBatch (Tracker::ValidatePose over n candidates).
+    Image lists are sf_image per level (level 0 first); poses n x 4 x 4.
+    Returns (list of RelocCandidate, chosen index or -1)."""
+    L = len(next_vmaps)
+    P = np.ascontiguousarray(np.asarray(poses, np.float64).reshape(-1, 16))
+    n = P.shape[0]
+    arr = lambda ims: (Image * L)(*ims)
+    it = (C.c_int * L)(*[int(iters[l]) if l < len(iters) else 0 for l in range(L)])
+    mc = (C.c_int * L)(*[int(min_count[l]) if l < len(min_count) else 0 for l in range(L)])
+    out = (_lib.RelocCandidate * n)()
+    chosen = C.c_int(-1)
+    call("sf_ValidatePoseBatch", ctx.h, m.h, L, arr(next_vmaps), arr(next_nmaps), arr(last_vmaps), arr(last_nmaps),
+         Intrinsics(*K), P.ctypes.data_as(_lib.F64P), n, it, mc, float(thresh), int(min_visible), out,
+         C.byref(chosen))
+    return list(out), chosen.value
 
 
 # Workloads: a 320x240 / 10 mm room sequence and a 640x480 / 5 mm room

@@ -74,7 +74,13 @@ class FrameStats(C.Structure):
                 ("icp_error", C.c_float), ("icp_count", C.c_int), ("visible", C.c_uint32),
                 ("heap_counter", C.c_int), ("entry_ptr", C.c_int), ("allocated", C.c_int),
                 ("flags", C.c_uint32), ("pose", C.c_double * 16), ("rgb_error", C.c_float),
-                ("rgb_count", C.c_int)]
+                ("rgb_count", C.c_int), ("state", C.c_int), ("missed", C.c_int), ("relocalised", C.c_int)]
+
+
+class RelocCandidate(C.Structure):
+    _fields_ = [("visible", C.c_uint32), ("rendered", C.c_int), ("evaluated", C.c_int), ("accepted", C.c_int),
+                ("fail", C.c_int), ("iterations", C.c_int), ("icp_error", C.c_float), ("icp_count", C.c_int),
+                ("pose", C.c_double * 16)]
 
 
 class AutotuneReport(C.Structure):
@@ -127,6 +133,10 @@ SIGNATURES = {
                                                                     I32P, F32P],
     "sf_RaycastAdjoint": [vp, vp, Image, Image, Mat3, Mat3, Float3] + [C.c_float] * 4 + [Image, Image, vp, F64P],
     "sf_RelocScoreBatch": [vp, vp, Image, C.c_int, F64P, C.c_int, C.c_float, C.POINTER(RelocScore)],
+    "sf_ValidatePoseBatch": [vp, vp, C.c_int] + [C.POINTER(Image)] * 4 + [Intrinsics, F64P, C.c_int, I32P, I32P,
+                                                                         C.c_float, C.c_uint32,
+                                                                         C.POINTER(RelocCandidate), I32P],
+    "sf_system_set_reloc_candidates": [vp, F64P, C.c_int],
     "sf_ComputeSE3": [vp, C.c_int, C.POINTER(Image), C.POINTER(Image), C.POINTER(Image), C.POINTER(Image),
                       Intrinsics, I32P, I32P, C.c_float, F64P, F64P, I32P, F32P],
     "sf_CheckBlockVisibility": [vp, vp, Mat3, Mat3, Float3, C.c_int, C.c_int] + [C.c_float] * 6 + [U32P],

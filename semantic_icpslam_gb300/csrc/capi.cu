@@ -36,6 +36,7 @@ struct sf_context {
   int adj_cap = 0;
   float *rdepth = nullptr;                // device rendered depth (sf_SemanticAnalysis)
   size_t rdepth_px = 0;
+  VpWorkspace *vp = nullptr;              // sf_ValidatePoseBatch's workspace
 };
 
 struct sf_map {
@@ -146,6 +147,7 @@ int sf_context_destroy(sf_context *ctx) {
   cudaFree(ctx->adj_part);
   cudaFree(ctx->adj_pose);
   cudaFree(ctx->rdepth);
+  vp_workspace_free(ctx->vp);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return SF_OK;
@@ -993,4 +995,5 @@ DevMap &map_dev(sf_map *m) { return m->d; }
 FuseScratch &map_scratch(sf_map *m) { return m->scratch; }
 int map_ensure_scratch(sf_map *m, int pixels) { return ensure_scratch(m, pixels); }
 const sf_map_config &map_cfg(sf_map *m) { return m->cfg; }
+VpWorkspace *&ctx_vp(sf_context *c) { return c->vp; }
 }  // namespace sf

@@ -492,6 +492,44 @@ __global__ void k_vis_start(DevMap m, FuseScratch f, const Cam *cam, unsigned *r
   }
 }
 
+// UpdateVisibility + CreateRenderingBlocks' z-range for n candidate
+// cameras (Tracker::ValidatePose, Tracking.cc:756-762): grid.y is the
+// candidate, grid.x strides over the allocated-entry index.  The count is
+// CheckBlockVisibility's (FuseMap.cu:991-1037); the z-range tiles are
+// Projection + fillBlocks' (RenderScene.cu:54-190), laid into the
+// candidate's zr-row slice of the tall z-range images.
+__global__ void k_vp_visibility(DevMap m, const Cam *cams, sf_image zmin, sf_image zmax, int zr, unsigned *vis,
+                                unsigned *rendered) {
+  const int c = blockIdx.y;
+  const Cam cam = cams[c];
+  sf_image zn = zmin, zx = zmax;
+  zn.data = (char *)zmin.data + (size_t)c * zr * zmin.step;
+  zx.data = (char *)zmax.data + (size_t)c * zr * zmax.step;
+  zn.rows = zx.rows = zr;
+  const unsigned n = (unsigned)*m.alloc_count;
+  unsigned cnt = 0;
+  bool drew = false;
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int4 h = entry_head(m.entries + m.alloc_list[k]);
+    if (h.w == -1) continue;
+    i3 pos; pos.x = h.x; pos.y = h.y; pos.z = h.z;
+    if (!block_visible(cam, m.c.block_width, pos)) continue;
+    ++cnt;
+    sf_rendering_block b;
+    if (project_block(pos, m.c.voxel_size, cam.Rinv, cam.t, cam.fx, cam.fy, cam.cx, cam.cy, zn.cols, zr,
+                      m.c.depth_max, m.c.depth_min, b)) {
+      fill_block_tiles(b, zn, zx);
+      drew = true;
+    }
+  }
+  cnt = __reduce_add_sync(0xffffffffu, cnt);
+  drew = __any_sync(0xffffffffu, drew);
+  if ((threadIdx.x & 31) == 0) {
+    if (cnt) atomicAdd(vis + c, cnt);
+    if (drew && rendered[c] == 0u) atomicExch(rendered + c, 1u);
+  }
+}
+
 // -------------------------------------------------------------- integrate
 union VoxelU {
   uint4 u;
@@ -953,6 +991,11 @@ void launch_visibility(const DevMap &m, const FuseScratch &f, const Cam *c, cons
   k_vis_start<<<sm_count() * 8, 256, 0, s>>>(m, f, c, rendered, zn, zx, do_z ? 1 : 0, run_flag); note_launch();
   k_visibility<<<sm_count() * 4, 256, 0, s>>>(m, f, c, zn, zx, do_z ? 1 : 0, rendered, run_flag,
                                               flags); note_launch();
+}
+
+void launch_vp_visibility(const DevMap &m, const Cam *cams, int n, const sf_image &zmin, const sf_image &zmax,
+                          int zr, unsigned *vis, unsigned *rendered, cudaStream_t s) {
+  k_vp_visibility<<<dim3(64, n), 256, 0, s>>>(m, cams, zmin, zmax, zr, vis, rendered); note_launch();
 }
 
 void launch_unify_neighbor(const DevMap &m, const FuseScratch &f, const int *run_flag, cudaStream_t s) {

@@ -771,6 +771,95 @@ __global__ void k_rgb_cand(sf_image img, sf_image dx, sf_image dy, sf_image cand
   row_ptr<uint8_t>(cand, y)[x] = ok ? 1 : 0;
 }
 
+// ------------------------------------- ValidatePose batch: ComputeSE3 part
+// ComputeSE3(icpOnly = true, ITERATIONS_RELOC, THRESH_ICP_RELOC) of n
+// candidates side by side (Tracker::ValidatePose, Tracking.cc:763-765).
+// Each iteration is two launches: every candidate still running gets nb
+// CTAs over the level's pixels (one FP64 partial per CTA and sum), then one
+// 96-thread CTA that sums its partials in a fixed order and runs the
+// persistent kernel's solve and stop logic (ctl_step_fast) on them.  The
+// candidate's state stays in ctl[c] between launches.
+struct VpArgs {
+  IcpLevelArgs L;  // vc, nc: the frame; vl, nl: tall model maps (or the fallback)
+  sf_image fv, fn;
+  int rows;
+  const int *src;
+  const TrackCtl *ctl;
+  double *part;
+  int stride;
+};
+
+__global__ void __launch_bounds__(kThreads) k_vp_partials(VpArgs a) {
+  const int c = blockIdx.y;
+  const int src = a.src[c];
+  if (src == -2 || a.ctl[c].stop) return;  // uniform over the CTA
+  __shared__ PoseF pose;
+  __shared__ float2 bsum[29];
+  __shared__ ff wpart[kWarps][33];
+  if (threadIdx.x < 32) pose_to_float_warp(a.ctl[c].next_pose, a.ctl[c].last_pose, pose);
+  __syncthreads();
+  IcpLevelArgs L = a.L;
+  if (src >= 0) {
+    L.vl.data = (char *)a.L.vl.data + (size_t)src * a.rows * a.L.vl.step;
+    L.nl.data = (char *)a.L.nl.data + (size_t)src * a.rows * a.L.nl.step;
+  } else {
+    L.vl = a.fv;
+    L.nl = a.fn;
+  }
+  L.vl.rows = L.nl.rows = a.rows;
+  float acc[29];
+  icp_accumulate(L, pose, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, acc);
+  block_reduce29<kWarps>(acc, wpart, bsum);
+  if (threadIdx.x < 29)
+    a.part[((size_t)c * 29 + threadIdx.x) * a.stride + blockIdx.x] =
+        (double)bsum[threadIdx.x].x + (double)bsum[threadIdx.x].y;
+}
+
+__global__ void __launch_bounds__(96) k_vp_step(const double *part, int nb, int stride, const int *src,
+                                                TrackCtl *ctl_g, int min_count) {
+  const int c = blockIdx.x;
+  if (src[c] == -2) return;
+  __shared__ TrackCtl ctl;
+  __shared__ IcpSolveSmem ssolve;
+  __shared__ double sums[29];
+  if (threadIdx.x == 0) {
+    ctl = ctl_g[c];
+    s_solve_marks = nullptr;
+  }
+  __syncthreads();
+  if (ctl.stop) return;  // uniform
+  if (threadIdx.x < 29) {
+    // four interleaved chains, joined in a fixed order
+    const double *p = part + ((size_t)c * 29 + threadIdx.x) * stride;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    int b = 0;
+    for (; b + 4 <= nb; b += 4) {
+      a0 += __ldcg(p + b);
+      a1 += __ldcg(p + b + 1);
+      a2 += __ldcg(p + b + 2);
+      a3 += __ldcg(p + b + 3);
+    }
+    for (; b < nb; ++b) a0 += __ldcg(p + b);
+    sums[threadIdx.x] = (a0 + a1) + (a2 + a3);
+  }
+  __syncthreads();
+  ctl_step_fast(ctl, sums, min_count, ssolve, nullptr);
+  __syncthreads();
+  if (threadIdx.x == 0) ctl_g[c] = ctl;
+}
+
+__global__ void __launch_bounds__(32) k_vp_finish(TrackCtl *ctl_g, const int *src, float thresh) {
+  const int c = blockIdx.x;
+  if (src[c] == -2) return;
+  __shared__ TrackCtl ctl;
+  __shared__ IcpSolveSmem ssolve;
+  if (threadIdx.x == 0) ctl = ctl_g[c];
+  __syncwarp();
+  ctl_finish_fast(ctl, thresh, ssolve);
+  __syncwarp();
+  if (threadIdx.x == 0) ctl_g[c] = ctl;
+}
+
 }  // namespace
 
 // arrival count (256 B), ICP accumulator sets, photometric accumulator
@@ -852,6 +941,31 @@ void launch_rgb_cand(const sf_image &inext, const sf_image &dx, const sf_image &
   const dim3 blk(32, 8);
   const dim3 grd((inext.cols + 31) / 32, (inext.rows + 7) / 8);
   k_rgb_cand<<<grd, blk, 0, s>>>(inext, dx, dy, cand); note_launch();
+}
+
+int vp_icp_blocks(int pixels) {
+  const int per = kThreads * 4;
+  return (pixels + per - 1) / per;
+}
+
+void launch_vp_icp_iteration(const VpLevel &V, const int *src, TrackCtl *ctl, double *part, int nb, int stride,
+                             int n, cudaStream_t s) {
+  VpArgs a;
+  a.L.vc = V.vc; a.L.nc = V.nc; a.L.vl = V.mv; a.L.nl = V.mn;
+  a.L.fx = V.fx; a.L.fy = V.fy; a.L.cx = V.cx; a.L.cy = V.cy;
+  a.L.iters = 1; a.L.min_count = V.min_count;
+  a.fv = V.fv; a.fn = V.fn;
+  a.rows = V.rows;
+  a.src = src;
+  a.ctl = ctl;
+  a.part = part;
+  a.stride = stride;
+  k_vp_partials<<<dim3(nb, n), kThreads, 0, s>>>(a); note_launch();
+  k_vp_step<<<n, 96, 0, s>>>(part, nb, stride, src, ctl, V.min_count); note_launch();
+}
+
+void launch_vp_icp_finish(TrackCtl *ctl, const int *src, float thresh, int n, cudaStream_t s) {
+  k_vp_finish<<<n, 32, 0, s>>>(ctl, src, thresh); note_launch();
 }
 
 void launch_icp_step(const IcpWorkspace &w, const IcpLevelArgs &L, const m3 &Rc, f3 tc,

@@ -339,10 +339,8 @@ __global__ void k_nmap(sf_image vmap, sf_image nmap) {
 // ResizeMapKernel (Pyrdown.cu:318-346): 2x2 mean, any NaN -> NaN; normals
 // normalised as float4 (w included in the norm, VectorMath.h:328-346).
 // Guarded on the destination size (the reference guards on the source).
-__global__ void k_resize(sf_image vsrc, sf_image nsrc, sf_image vdst, sf_image ndst) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  if (x >= vdst.cols || y >= vdst.rows) return;
+__device__ __forceinline__ void resize_px(const sf_image &vsrc, const sf_image &nsrc, const sf_image &vdst,
+                                          const sf_image &ndst, int x, int y) {
   const float4 *v0 = row_ptr<const float4>(vsrc, 2 * y) + 2 * x;
   const float4 *v1 = row_ptr<const float4>(vsrc, 2 * y + 1) + 2 * x;
   const float4 *n0 = row_ptr<const float4>(nsrc, 2 * y) + 2 * x;
@@ -370,6 +368,33 @@ __global__ void k_resize(sf_image vsrc, sf_image nsrc, sf_image vdst, sf_image n
     out = make_float4(s0 / len, s1 / len, s2 / len, s3 / len);
   }
   row_ptr<float4>(ndst, y)[x] = out;
+}
+
+__global__ void k_resize(sf_image vsrc, sf_image nsrc, sf_image vdst, sf_image ndst) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= vdst.cols || y >= vdst.rows) return;
+  resize_px(vsrc, nsrc, vdst, ndst, x, y);
+}
+
+// Frame::ResizeImages of n stacked candidates (Tracker::ValidatePose,
+// Tracking.cc:762): grid.z is the candidate; those with src[c] != c (not
+// drawn this call) are left alone.
+__global__ void k_resize_batch(sf_image vsrc, sf_image nsrc, sf_image vdst, sf_image ndst, int src_rows,
+                               int dst_rows, const int *src) {
+  const int k = blockIdx.z;
+  if (src[k] != k) return;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= vdst.cols || y >= dst_rows) return;
+  sf_image vs = vsrc, ns = nsrc, vd = vdst, nd = ndst;
+  vs.data = (char *)vsrc.data + (size_t)k * src_rows * vsrc.step;
+  ns.data = (char *)nsrc.data + (size_t)k * src_rows * nsrc.step;
+  vd.data = (char *)vdst.data + (size_t)k * dst_rows * vdst.step;
+  nd.data = (char *)ndst.data + (size_t)k * dst_rows * ndst.step;
+  vs.rows = ns.rows = src_rows;
+  vd.rows = nd.rows = dst_rows;
+  resize_px(vs, ns, vd, nd, x, y);
 }
 
 // ------------------------------------------------------------- launchers
@@ -460,6 +485,14 @@ void launch_resize(const sf_image &vsrc, const sf_image &nsrc, const sf_image &v
                    const sf_image &ndst, cudaStream_t s) {
   dim3 blk(32, 8);
   k_resize<<<grid2d(vdst.cols, vdst.rows, blk), blk, 0, s>>>(vsrc, nsrc, vdst, ndst); note_launch();
+}
+
+void launch_resize_batch(const sf_image &vsrc, const sf_image &nsrc, const sf_image &vdst, const sf_image &ndst,
+                         int src_rows, int dst_rows, int n, const int *src, cudaStream_t s) {
+  dim3 blk(32, 8);
+  dim3 grd = grid2d(vdst.cols, dst_rows, blk);
+  grd.z = n;
+  k_resize_batch<<<grd, blk, 0, s>>>(vsrc, nsrc, vdst, ndst, src_rows, dst_rows, src); note_launch();
 }
 
 }  // namespace sf

@@ -339,6 +339,53 @@ __device__ __forceinline__ void march_ray(const RayCtx &r, const Cam &c, float v
   ms.behind = behind;
 }
 
+__device__ __forceinline__ RayCtx ray_ctx(const DevMap &m, const FuseScratch &f) {
+  RayCtx r;
+  r.voxels = m.voxels;
+  r.cells = f.win_cells;
+  for (int k = 0; k < 6; ++k) r.win[k] = f.win[k];
+  r.entries = m.entries;
+  r.num_buckets = m.c.num_buckets;
+  r.num_excess = m.c.num_excess;
+  return r;
+}
+
+// One pixel of Rendering::operator() (RenderScene.cu:380-488): the z-range
+// test, the march, the two refinement steps, the normal, and the write.
+__device__ __forceinline__ void raycast_pixel(const RayCtx &r, const Cam &c, const MapConst &mc,
+                                              const sf_image &zmin, const sf_image &zmax, int x, int y,
+                                              const sf_image &vmap, const sf_image &nmap) {
+  float4 vout = nan4(), nout = nan4();
+  const int lx = (int)floorf((float)x / 8.0f), ly = (int)floorf((float)y / 8.0f);
+  const float zx = __ldg(row_ptr<const float>(zmin, ly) + lx);
+  const float zy = __ldg(row_ptr<const float>(zmax, ly) + lx);
+  // (double)z < 1e-3 of the reference: no float lies in [1e-3, 0.001f), so
+  // for a float z that is exactly z < 0.001f
+  if (!(zy < 0.001f || zx < 0.001f || isnan(zx) || isnan(zy))) {
+    MarchState ms;
+    march_ray(r, c, mc.voxel_size_inv, x, y, zx, zy, ms);
+    f3 result = ms.result;
+    const f3 dir = ms.dir;
+    float sdf = ms.sdf;
+    const bool behind = ms.behind;
+    if (!behind && sdf <= 0.0f) {
+      float step = sdf * mc.step_scale;
+      result = result + step * dir;
+      sdf = read_sdf_interp(r, result).sdf;
+      step = sdf * mc.step_scale;
+      result = result + step * dir;
+      const NormalOut no = read_normal(r, result, c.Rinv);
+      if (no.ok) {
+        const f3 q = mul(c.Rinv, result * mc.voxel_size - c.t);
+        vout = make_float4(q.x, q.y, q.z, 1.0f);
+        nout = make_float4(no.n.x, no.n.y, no.n.z, 1.0f);
+      }
+    }
+  }
+  row_ptr<float4>(vmap, y)[x] = vout;
+  row_ptr<float4>(nmap, y)[x] = nout;
+}
+
 // Rendering::operator() (RenderScene.cu:380-488).  The march reads kSpec
 // samples ahead at once, at the positions a run of 1-voxel steps would
 // reach (the same float additions), then replays the reference's loop over
@@ -366,42 +413,31 @@ __global__ void __launch_bounds__(128, MINB) k_raycast(DevMap m, FuseScratch f, 
     return;
   }
   const Cam c = *cam;
-  RayCtx r;
-  r.voxels = m.voxels;
-  r.cells = f.win_cells;
-  for (int k = 0; k < 6; ++k) r.win[k] = f.win[k];
-  r.entries = m.entries;
-  r.num_buckets = m.c.num_buckets;
-  r.num_excess = m.c.num_excess;
-  float4 vout = nan4(), nout = nan4();
-  const int lx = (int)floorf((float)x / 8.0f), ly = (int)floorf((float)y / 8.0f);
-  const float zx = __ldg(row_ptr<const float>(zmin, ly) + lx);
-  const float zy = __ldg(row_ptr<const float>(zmax, ly) + lx);
-  // (double)z < 1e-3 of the reference: no float lies in [1e-3, 0.001f), so
-  // for a float z that is exactly z < 0.001f
-  if (!(zy < 0.001f || zx < 0.001f || isnan(zx) || isnan(zy))) {
-    MarchState ms;
-    march_ray(r, c, m.c.voxel_size_inv, x, y, zx, zy, ms);
-    f3 result = ms.result;
-    const f3 dir = ms.dir;
-    float sdf = ms.sdf;
-    const bool behind = ms.behind;
-    if (!behind && sdf <= 0.0f) {
-      float step = sdf * m.c.step_scale;
-      result = result + step * dir;
-      sdf = read_sdf_interp(r, result).sdf;
-      step = sdf * m.c.step_scale;
-      result = result + step * dir;
-      const NormalOut no = read_normal(r, result, c.Rinv);
-      if (no.ok) {
-        const f3 q = mul(c.Rinv, result * m.c.voxel_size - c.t);
-        vout = make_float4(q.x, q.y, q.z, 1.0f);
-        nout = make_float4(no.n.x, no.n.y, no.n.z, 1.0f);
-      }
-    }
-  }
-  row_ptr<float4>(vmap, y)[x] = vout;
-  row_ptr<float4>(nmap, y)[x] = nout;
+  raycast_pixel(ray_ctx(m, f), c, m.c, zmin, zmax, x, y, vmap, nmap);
+}
+
+// Tracker::ValidatePose's RayTrace of n candidates in one launch
+// (Tracking.cc:759-761): grid.z is the candidate; a candidate draws into
+// its `rows`-row slice of the tall model maps from its zr-row slice of the
+// tall z-range images, and only when src[c] == c (its visible count
+// reached the threshold and a block projected).
+__global__ void __launch_bounds__(128, 8) k_raycast_batch(DevMap m, FuseScratch f, sf_image vmap, sf_image nmap,
+                                                          int rows, sf_image zmin, sf_image zmax, int zr,
+                                                          const Cam *cams, const int *src) {
+  const int k = blockIdx.z;
+  if (src[k] != k) return;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= vmap.cols || y >= rows) return;
+  sf_image v = vmap, n = nmap, zn = zmin, zx = zmax;
+  v.data = (char *)vmap.data + (size_t)k * rows * vmap.step;
+  n.data = (char *)nmap.data + (size_t)k * rows * nmap.step;
+  zn.data = (char *)zmin.data + (size_t)k * zr * zmin.step;
+  zx.data = (char *)zmax.data + (size_t)k * zr * zmax.step;
+  v.rows = n.rows = rows;
+  zn.rows = zx.rows = zr;
+  const Cam c = cams[k];
+  raycast_pixel(ray_ctx(m, f), c, m.c, zn, zx, x, y, v, n);
 }
 
 // RaycastAdjoint: gradient of the raycast's vertex and normal maps with
@@ -578,7 +614,63 @@ __global__ void k_window_build_fill(DevMap m, FuseScratch f) {
   }
 }
 
+// Window over the bounding box of every allocated block: box[0..2] min,
+// box[3..5] max block coordinates.
+__global__ void k_window_box_init(int *box) {
+  if (threadIdx.x < 3) box[threadIdx.x] = 0x7fffffff;
+  else if (threadIdx.x < 6) box[threadIdx.x] = (int)0x80000000;
+}
+__global__ void k_window_box_reduce(DevMap m, int *box) {
+  const unsigned n = (unsigned)*m.alloc_count;
+  int lo[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, hi[3] = {(int)0x80000000, (int)0x80000000, (int)0x80000000};
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int4 h = entry_head(m.entries + m.alloc_list[k]);
+    if (h.w < 0) continue;
+    const int p[3] = {h.x, h.y, h.z};
+    for (int d = 0; d < 3; ++d) { lo[d] = min(lo[d], p[d]); hi[d] = max(hi[d], p[d]); }
+  }
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = __reduce_min_sync(0xffffffffu, lo[d]);
+    hi[d] = __reduce_max_sync(0xffffffffu, hi[d]);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    for (int d = 0; d < 3; ++d) {
+      atomicMin(box + d, lo[d]);
+      atomicMax(box + 3 + d, hi[d]);
+    }
+  }
+}
+__global__ void k_window_box_setup(FuseScratch f, const int *box) {
+  long long total = 1;
+  int n[3];
+  for (int d = 0; d < 3; ++d) {
+    n[d] = box[3 + d] >= box[d] ? box[3 + d] - box[d] + 1 : 0;
+    total *= n[d];
+  }
+  if (total <= 0 || total > (long long)f.win_cap) n[0] = n[1] = n[2] = 0;
+  for (int d = 0; d < 3; ++d) {
+    f.win[d] = n[0] ? box[d] : 0;
+    f.win[3 + d] = n[d];
+  }
+}
+
 }  // namespace
+
+void launch_window_alloc_box(const DevMap &m, const FuseScratch &f, int *box, cudaStream_t s) {
+  k_window_box_init<<<1, 32, 0, s>>>(box); note_launch();
+  k_window_box_reduce<<<256, 256, 0, s>>>(m, box); note_launch();
+  k_window_box_setup<<<1, 1, 0, s>>>(f, box); note_launch();
+  k_window_build_clear<<<256, 256, 0, s>>>(f); note_launch();
+  k_window_build_fill<<<256, 256, 0, s>>>(m, f); note_launch();
+}
+
+void launch_raycast_batch(const DevMap &m, const FuseScratch &f, const sf_image &vmap, const sf_image &nmap,
+                          int rows, const sf_image &zmin, const sf_image &zmax, int zr, const Cam *cams, int n,
+                          const int *src, cudaStream_t s) {
+  const dim3 blk(8, 16);
+  const dim3 grd((vmap.cols + 7) / 8, (rows + 15) / 16, n);
+  k_raycast_batch<<<grd, blk, 0, s>>>(m, f, vmap, nmap, rows, zmin, zmax, zr, cams, src); note_launch();
+}
 
 void launch_rendering_blocks(const DevMap &m, uint32_t nvis, const sf_image &zmin,
                              sf_rendering_block *list, uint32_t *count, const Cam *c,

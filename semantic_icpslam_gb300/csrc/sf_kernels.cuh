@@ -242,6 +242,48 @@ void launch_window_build(const DevMap &m, const FuseScratch &f, const Cam *c, cu
 void launch_reloc_score(const DevMap &m, const sf_image &vmap, int stride, const float *poses, int n,
                         float inlier_sdf, sf_reloc_score *out, cudaStream_t s);
 
+// Tracker::ValidatePose (Tracking.cc:750-790) batched over n candidate
+// poses (csrc/validate.cu).  The candidates' model maps and z-range images
+// are stacked: candidate c's image of h rows is rows [c h, c h + h) of one
+// tall image.  cams: n device cameras (Frame::GpuRotation of each pose).
+//
+// UpdateVisibility + CreateRenderingBlocks' z-range per candidate:
+// vis[c] (zero on entry) gets the visible-block count, rendered[c] (zero
+// on entry) is set when a block projected; zmin / zmax hold 100 / 0 on
+// entry (launch_zrange_init on the tall images).
+void launch_vp_visibility(const DevMap &m, const Cam *cams, int n, const sf_image &zmin, const sf_image &zmax,
+                          int zr, unsigned *vis, unsigned *rendered, cudaStream_t s);
+// Block-pointer window over the bounding box of every allocated block
+// (box: device int[8] scratch), so the candidates' raycasts share one.
+void launch_window_alloc_box(const DevMap &m, const FuseScratch &f, int *box, cudaStream_t s);
+// Raycast of every candidate whose src[c] == c (drawn) into its rows of
+// the tall level-0 model maps.
+void launch_raycast_batch(const DevMap &m, const FuseScratch &f, const sf_image &vmap, const sf_image &nmap,
+                          int rows, const sf_image &zmin, const sf_image &zmax, int zr, const Cam *cams, int n,
+                          const int *src, cudaStream_t s);
+// ResizeMap of every drawn candidate (src[c] == c) from its src_rows-row
+// slice of the tall source maps into its dst_rows-row slice of the tall
+// destination maps.
+void launch_resize_batch(const sf_image &vsrc, const sf_image &nsrc, const sf_image &vdst, const sf_image &ndst,
+                         int src_rows, int dst_rows, int n, const int *src, cudaStream_t s);
+// One ComputeSE3 iteration of every evaluated candidate (src[c] != -2,
+// ctl[c].stop == 0) at one level: mv / mn are the tall model maps of this
+// level (candidate src[c]'s slice of `rows` rows), fv / fn the fallback
+// model maps (src[c] == -1); vc / nc the frame's maps.
+struct VpWorkspace;
+void vp_workspace_free(VpWorkspace *w);
+struct VpLevel {
+  sf_image vc, nc, mv, mn, fv, fn;
+  int rows;
+  float fx, fy, cx, cy;
+  int min_count;
+};
+int vp_icp_blocks(int pixels);  // CTAs per candidate of launch_vp_icp_partials
+void launch_vp_icp_iteration(const VpLevel &L, const int *src, TrackCtl *ctl, double *part, int nb, int stride,
+                             int n, cudaStream_t s);
+// ComputeSE3's acceptance gate of every evaluated candidate.
+void launch_vp_icp_finish(TrackCtl *ctl, const int *src, float thresh, int n, cudaStream_t s);
+
 // Converts host map config into device constants (DeviceMap.h:166-189).
 MapConst make_map_const(const sf_map_config &cfg);
 

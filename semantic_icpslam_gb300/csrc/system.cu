@@ -20,6 +20,7 @@
 #include <cstddef>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "sf_kernels.cuh"
 
@@ -34,13 +35,42 @@ const sf_map_config &map_cfg(sf_map *m);
 
 struct SysDev {
   double last_pose[16];
-  int state;     // 1 = initialise on the next frame (ICP skipped), 0 = tracking
-  int run;       // this frame is tracked: mapping runs
+  int state;       // state of the next frame: 1 initialise, 0 track, -1 lost (relocalise); ICP runs only in 0
+  int run;         // this frame is tracked: mapping runs
   int accepted;
-  int first;     // this frame was the initialisation frame
-  int pad_;
-  Cam cam;       // camera of this frame's mapping pass
+  int first;       // this frame was the initialisation frame
+  int prev_state;  // state this frame ran in (Tracker::lastState once the frame is done)
+  int missed;      // Tracker::noMissedFrames
+  int relocalised; // this frame was relocalised
+  int icp_ran;     // a ComputeSE3 ran this frame (its stats are reported)
+  Cam cam;         // camera of this frame's mapping pass
 };
+
+// Tracker::Track's state machine (Tracking.cc:65-119) after one frame's
+// attempt.  st: the state the frame ran in (1 initialise, 0 track, -1
+// relocalise); prev: the state the previous frame ran in; ok: the
+// attempt's result (ComputeSE3's acceptance in state 0, Relocalise's in
+// state -1).  Returns whether the frame is tracked (SwapFrame, then the
+// mapping stage), and sets the next frame's state and the missed-frame
+// count: ten misses in a row make the tracker lost, and the first frame
+// tracked after a relocalisation is not swapped (Track returns false).
+SF_HD int track_transition(int st, int prev, int ok, int &next, int &missed) {
+  if (st == 1) {
+    next = 0;
+    return 1;
+  }
+  if (st == 0) {
+    next = 0;
+    if (ok) {
+      missed = 0;
+      return prev != -1 ? 1 : 0;
+    }
+    if (++missed > 9) next = -1;
+    return 0;
+  }
+  next = ok ? 0 : -1;
+  return ok ? 1 : 0;
+}
 
 namespace {
 
@@ -48,20 +78,22 @@ namespace {
 // (Frame::GpuRotation / GpuInvRotation / GpuTranslation, Frame.cc:626-645);
 // when the frame is tracked, also the start of its allocation pass
 // (alloc_frame_begin), which would otherwise be a launch of its own.
+// A lost frame (state -1) relocalises only in the host-driven path of
+// sf_system_grab with candidates registered; here it stays lost.
 __global__ void k_sys_post(SysDev *s, const TrackCtl *ctl, Cam tmpl, FuseScratch f) {
-  int tracked;
-  if (s->state == 1) {
-    tracked = 1;
-    s->first = 1;
-    s->accepted = 1;
-    s->state = 0;
-  } else {
-    s->first = 0;
-    tracked = ctl->accepted;
-    s->accepted = ctl->accepted;
-    if (tracked)
-      for (int k = 0; k < 16; ++k) s->last_pose[k] = ctl->next_pose[k];
-  }
+  const int st = s->state;
+  const int ok = st == 0 ? ctl->accepted : 0;
+  int next, missed = s->missed;
+  const int tracked = track_transition(st, s->prev_state, ok, next, missed);
+  s->first = st == 1 ? 1 : 0;
+  s->accepted = st == 1 ? 1 : ok;
+  if (st == 0 && tracked)
+    for (int k = 0; k < 16; ++k) s->last_pose[k] = ctl->next_pose[k];
+  s->prev_state = st;
+  s->state = next;
+  s->missed = missed;
+  s->relocalised = 0;
+  s->icp_ran = st == 0 ? 1 : 0;
   s->run = tracked;
   if (tracked) alloc_frame_begin(f);
   const double *P = s->last_pose;
@@ -87,7 +119,10 @@ __global__ void k_sys_stats(const SysDev *s, const TrackCtl *ctl, DevMap m, cons
   sf_frame_stats st;
   st.tracked = s->run;
   st.accepted = s->accepted;
-  if (s->first) {
+  st.state = s->state;
+  st.missed = s->missed;
+  st.relocalised = s->relocalised;
+  if (!s->icp_ran) {  // no ComputeSE3 ran this frame
     st.fail = 0; st.iterations = 0; st.icp_error = 0.f; st.icp_count = 0;
     st.rgb_error = 0.f; st.rgb_count = 0;
   } else {
@@ -161,8 +196,16 @@ struct sf_system {
   sf_frame_stats *h_stats = nullptr;
   // plain-form host state
   double last_pose[16];
-  int state = 1;
+  int state = 1;        // the next frame's state (Tracker::state), as SysDev::state
+  int prev_state = 0;   // the state the last frame ran in
+  int missed = 0;       // Tracker::noMissedFrames
   TrackCtl ctl;
+  // relocalisation: the caller's candidate poses (n x 16, camera -> world),
+  // tried by every frame that starts lost; the device forms' next state as
+  // last read back (-2 = unknown)
+  std::vector<double> reloc;
+  int dev_state = -2;
+  bool host_driven = false;  // this frame ran host-driven (its stats are copied, not flagged)
   Cam tmpl;
   // graph
   cudaGraphExec_t gexec = nullptr;
@@ -511,14 +554,14 @@ int run_plain_frame(sf_system *s, int num_detection) {
   cudaStream_t st = ctx_stream(s->ctx);
   IcpWorkspace &w = ctx_icp(s->ctx);
   enqueue_pyramid(s, st);
-  int tracked;
-  bool first = false;
-  if (s->state == 1) {
-    tracked = 1;
-    first = true;
-    s->state = 0;
+  const int state = s->state;
+  int ok = 0;
+  if (state == 1) {
     ctl_begin(s->ctl, s->last_pose);
     s->ctl.accepted = 1;
+    ok = 1;
+  } else if (state == -1) {
+    // lost, and no candidates to relocalise against: the frame is skipped
   } else {
     IcpLevelArgs lv[kMaxLevels];
     icp_levels(s, lv);
@@ -553,17 +596,24 @@ int run_plain_frame(sf_system *s, int num_detection) {
       }
     }
     ctl_finish(s->ctl, s->cfg.icp_thresh);
-    tracked = s->ctl.accepted;
-    if (tracked) memcpy(s->last_pose, s->ctl.next_pose, sizeof(s->last_pose));
+    ok = s->ctl.accepted;
   }
+  int next = 0;
+  const int tracked = track_transition(state, s->prev_state, ok, next, s->missed);
+  if (state == 0 && tracked) memcpy(s->last_pose, s->ctl.next_pose, sizeof(s->last_pose));
+  s->prev_state = state;
+  s->state = next;
   // host -> device state (camera, pose, decision) for the mapping pass
   SysDev sd;
   memset(&sd, 0, sizeof(sd));
   memcpy(sd.last_pose, s->last_pose, sizeof(sd.last_pose));
-  sd.state = 0;
+  sd.state = next;
+  sd.prev_state = state;
+  sd.missed = s->missed;
   sd.run = tracked;
-  sd.accepted = s->ctl.accepted;
-  sd.first = first ? 1 : 0;
+  sd.accepted = ok;
+  sd.first = state == 1 ? 1 : 0;
+  sd.icp_ran = state == 0 ? 1 : 0;
   const double *P = s->last_pose;
   sd.cam = s->tmpl;
   sd.cam.R.rx = {(float)P[0], (float)P[1], (float)P[2]};
@@ -587,13 +637,160 @@ int run_plain_frame(sf_system *s, int num_detection) {
   return cudaGetLastError() == cudaSuccess ? SF_OK : SF_ERR_CUDA;
 }
 
+// ValidatePose's constants (Tracking.h:111,119; Tracking.cc:758):
+// ITERATIONS_RELOC per level (level 0 first; levels beyond the reference's
+// three run none), THRESH_ICP_RELOC, and the visible-block floor.
+constexpr int kRelocIters[kMaxLevels] = {3, 3, 2, 0};
+constexpr float kRelocThresh = 1e-3f;
+constexpr uint32_t kRelocMinVisible = 512;
+
+void set_cam(Cam &c, const Cam &tmpl, const double *P) {
+  c = tmpl;
+  c.R.rx = {(float)P[0], (float)P[1], (float)P[2]};
+  c.R.ry = {(float)P[4], (float)P[5], (float)P[6]};
+  c.R.rz = {(float)P[8], (float)P[9], (float)P[10]};
+  c.Rinv.rx = {(float)P[0], (float)P[4], (float)P[8]};
+  c.Rinv.ry = {(float)P[1], (float)P[5], (float)P[9]};
+  c.Rinv.rz = {(float)P[2], (float)P[6], (float)P[10]};
+  c.t = {(float)P[3], (float)P[7], (float)P[11]};
+}
+
+// A frame that starts lost, with candidate poses registered: Track()'s
+// state -1, Tracker::Relocalise's validation and final refinement
+// (Tracking.cc:107-116, 750-790), host-driven in every form.  The caller's
+// candidates stand in for the poses Relocalise estimates from SURF matches
+// (keypoint matching is outside this loop).  ValidatePose runs as one
+// batched call; the pose it keeps becomes LastFrame's pose (whether or not
+// the final ComputeSE3 then accepts), LastFrame's model maps are ray traced
+// and resized there, and ComputeSE3(icpOnly = true) with the loop's
+// iterations and threshold refines it.  Accepted, the frame is tracked and
+// mapped like any other.
+int run_reloc_frame(sf_system *s, int num_detection) {
+  cudaStream_t st = ctx_stream(s->ctx);
+  IcpWorkspace &w = ctx_icp(s->ctx);
+  const int C = s->cfg.cols, R = s->cfg.rows, L = s->L;
+  const bool plain = s->cfg.use_graph == 0;
+  DevMap &m = map_dev(s->map);
+  FuseScratch &f = map_scratch(s->map);
+  s->host_driven = true;
+  SysDev sd;
+  if (plain) {
+    memset(&sd, 0, sizeof(sd));
+    memcpy(sd.last_pose, s->last_pose, sizeof(sd.last_pose));
+    sd.prev_state = s->prev_state;
+    sd.missed = s->missed;
+  } else if (cudaMemcpyAsync(&sd, s->d_sys, sizeof(sd), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+             cudaStreamSynchronize(st) != cudaSuccess) {
+    return SF_ERR_CUDA;
+  }
+  enqueue_pyramid(s, st);
+  sf_image nv[kMaxLevels], nn[kMaxLevels], lv[kMaxLevels], ln[kMaxLevels];
+  int iters[kMaxLevels], minc[kMaxLevels];
+  for (int l = 0; l < L; ++l) {
+    nv[l] = img(s->d_vmap[l], C >> l, R >> l, 16);
+    nn[l] = img(s->d_nmap[l], C >> l, R >> l, 16);
+    lv[l] = img(s->d_mv[l], C >> l, R >> l, 16);
+    ln[l] = img(s->d_mn[l], C >> l, R >> l, 16);
+    iters[l] = kRelocIters[l];
+    minc[l] = s->cfg.min_count[l];
+  }
+  const int n = (int)(s->reloc.size() / 16);
+  std::vector<sf_reloc_candidate> out((size_t)n);
+  int chosen = -1;
+  int e = sf_ValidatePoseBatch(s->ctx, s->map, L, nv, nn, lv, ln, s->cfg.K, s->reloc.data(), n, iters, minc,
+                               kRelocThresh, kRelocMinVisible, out.data(), &chosen);
+  if (e != SF_OK) return e;
+  const Cam *cam = dev_field<Cam>(s->d_sys, offsetof(SysDev, cam));
+  int ok = 0;
+  TrackCtl &ctl = s->ctl;
+  if (chosen >= 0) {
+    // LastFrame->pose = the kept candidate; UpdateVisibility, RayTrace and
+    // ResizeImages there (Tracking.cc:780-785)
+    memcpy(sd.last_pose, s->reloc.data() + 16 * (size_t)chosen, sizeof(sd.last_pose));
+    set_cam(sd.cam, s->tmpl, sd.last_pose);
+    if (cudaMemcpyAsync(s->d_sys, &sd, sizeof(sd), cudaMemcpyHostToDevice, st) != cudaSuccess) return SF_ERR_CUDA;
+    const sf_image zmin = img(s->d_zmin, s->zc, s->zr, 4), zmax = img(s->d_zmax, s->zc, s->zr, 4);
+    launch_visibility(m, f, cam, &zmin, &zmax, nullptr, ctx_flags(s->ctx), st);
+    launch_raycast(m, f, lv[0], ln[0], zmin, zmax, cam, f.counters + 3, nullptr, nullptr, nullptr, st, s->rc_tune);
+    for (int l = 1; l < L; ++l) launch_resize(lv[l - 1], ln[l - 1], lv[l], ln[l], st);
+    // ComputeSE3(true, ITERATIONS_SE3, THRESH_ICP_SE3) from it (Tracking.cc:789)
+    IcpLevelArgs il[kMaxLevels];
+    icp_levels(s, il);
+    if (icp_persistent_reset(w, st) != cudaSuccess ||
+        launch_icp_persistent(w, il, L, s->cfg.icp_thresh, dev_field<double>(s->d_sys, offsetof(SysDev, last_pose)),
+                              nullptr, ctx_flags(s->ctx), st) != cudaSuccess ||
+        cudaMemcpyAsync(&ctl, w.ctl, sizeof(TrackCtl), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return SF_ERR_CUDA;
+    ok = ctl.accepted;
+  }
+  int next = -1, missed = sd.missed;
+  const int tracked = track_transition(-1, sd.prev_state, ok, next, missed);
+  if (tracked) memcpy(sd.last_pose, ctl.next_pose, sizeof(sd.last_pose));
+  sd.state = next;
+  sd.prev_state = -1;
+  sd.missed = missed;
+  sd.run = tracked;
+  sd.accepted = ok;
+  sd.first = 0;
+  sd.relocalised = tracked;
+  sd.icp_ran = chosen >= 0 ? 1 : 0;
+  set_cam(sd.cam, s->tmpl, sd.last_pose);
+  if (cudaMemcpyAsync(s->d_sys, &sd, sizeof(sd), cudaMemcpyHostToDevice, st) != cudaSuccess) return SF_ERR_CUDA;
+  if (plain) {
+    memcpy(s->last_pose, sd.last_pose, sizeof(s->last_pose));
+    s->state = next;
+    s->prev_state = -1;
+    s->missed = missed;
+  } else {
+    s->dev_state = next;
+  }
+  if (tracked) {
+    e = enqueue_mapping(s, cam, nullptr, num_detection, true, st);
+    if (e != SF_OK) return e;
+  } else if (!s->cfg.rgb_term) {
+    wait_inputs(s, st);  // the colour upload is not left behind the frame
+  }
+  k_sys_stats<<<1, 1, 0, st>>>(s->d_sys, w.ctl, m, ctx_flags(s->ctx), s->d_stats, nullptr, nullptr, nullptr);
+  note_launch();
+  return cudaGetLastError() == cudaSuccess ? SF_OK : SF_ERR_CUDA;
+}
+
+// The state the next frame starts in, when candidates are registered: the
+// plain form keeps it on the host; the device forms read it back when the
+// last frame's stats did not bring it.
+int upcoming_state(sf_system *s, int *state) {
+  if (s->cfg.use_graph == 0) {
+    *state = s->state;
+    return SF_OK;
+  }
+  if (s->dev_state == -2) {
+    int v = 0;
+    if (cudaMemcpyAsync(&v, dev_field<int>(s->d_sys, offsetof(SysDev, state)), sizeof(int), cudaMemcpyDeviceToHost,
+                        ctx_stream(s->ctx)) != cudaSuccess ||
+        cudaStreamSynchronize(ctx_stream(s->ctx)) != cudaSuccess)
+      return SF_ERR_CUDA;
+    s->dev_state = v;
+  }
+  *state = s->dev_state;
+  return SF_OK;
+}
+
 int run_frame(sf_system *s, int num_detection) {
   cudaStream_t st = ctx_stream(s->ctx);
   ++s->frames;
+  s->host_driven = false;
   if (num_detection > 0) {  // UnifyNeighbor's output buffer, before any capture
     int e = fuse_scratch_unify(map_scratch(s->map), map_dev(s->map).c);
     if (e != SF_OK) return e;
   }
+  if (!s->reloc.empty()) {
+    int state = 0;
+    int e = upcoming_state(s, &state);
+    if (e != SF_OK) return e;
+    if (state == -1) return run_reloc_frame(s, num_detection);
+  }
+  s->dev_state = -2;  // a device-form frame decides the next state on the device
   if (s->cfg.use_graph == 0) return run_plain_frame(s, num_detection);
   if (s->cfg.use_graph == 2) {  // eager device-driven
     return enqueue_device_frame(s, num_detection, st) == cudaSuccess ? SF_OK : SF_ERR_CUDA;
@@ -716,7 +913,7 @@ int sf_system_grab(sf_system *s, const uint16_t *depth, const uint8_t *rgb, cons
   if (cudaEventRecord(s->ev_inputs, s->cstream) != cudaSuccess) return SF_ERR_CUDA;
   int r = run_frame(s, num_detection);
   if (r) return r;
-  if (s->cfg.use_graph == 1 && s->graph_early) {
+  if (s->cfg.use_graph == 1 && s->graph_early && !s->host_driven) {
     // the graph wrote them before its final raycast; the wait ends with this
     // frame's sequence number in the flag (an earlier frame's number, left
     // by a replay that sf_system_grab_device launched and nobody waited for,
@@ -732,6 +929,7 @@ int sf_system_grab(sf_system *s, const uint16_t *depth, const uint8_t *rgb, cons
              cudaStreamSynchronize(st) != cudaSuccess) {
     return SF_ERR_CUDA;
   }
+  if (s->cfg.use_graph != 0) s->dev_state = s->h_stats->state;
   if (stats) *stats = *s->h_stats;
   return SF_OK;
 }
@@ -751,6 +949,13 @@ int sf_system_grab_device(sf_system *s, const uint16_t *depth, const uint8_t *rg
       cudaMemcpyAsync(s->d_mask, mask, np, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
     return SF_ERR_CUDA;
   return run_frame(s, num_detection);
+}
+
+int sf_system_set_reloc_candidates(sf_system *s, const double *poses, int n) {
+  if (!s || n < 0 || n > 65535 || (n > 0 && !poses)) return SF_ERR_INVALID;
+  s->reloc.assign(poses, poses + 16 * (size_t)n);
+  s->dev_state = -2;
+  return SF_OK;
 }
 
 int sf_system_set_mapping(sf_system *s, int enabled) {

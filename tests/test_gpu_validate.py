@@ -1,0 +1,247 @@
+"""Relocalisation with the reference's semantics: Tracker::ValidatePose
+(Tracking/Tracking.cc:750-790) batched over candidate poses
+(sf_ValidatePoseBatch), and the loop's lost state (Tracking.cc:65-119)
+relocalising against registered candidates.
+
+The batch is compared with the oracle's sequential restatement on the same
+map, frame and candidates: visible counts, which candidates draw and are
+evaluated, and acceptance exactly; iterations and inlier counts exactly
+where the two agree on the discrete decisions; refined poses within 1e-5
+(FP32 per-pixel rows, sums and solves ordered differently).  The chosen
+candidate is the first accepted one in both.  At the C5 size (256
+candidates against one 640x480 frame) a subset is checked against the
+oracle and the whole batch for determinism.  The loop test drives a
+sequence into the lost state with blank frames and checks that every
+form relocalises like the oracle's loop.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from tests.helpers import C1, C2, MAP_C1, MAP_C2, cuda, empty, host, sequence
+from tests.test_gpu_reloc import candidates
+
+pytestmark = pytest.mark.gpu
+
+POSE_TOL = 1e-5
+
+
+def _pyramid(sf, ctx, d, K, levels=3):
+    import torch
+    dd = cuda(d)
+    raw = empty(d.shape, torch.float32)
+    shp = lambda l: (d.shape[0] >> l, d.shape[1] >> l)
+    depths = [empty(shp(l), torch.float32) for l in range(levels)]
+    vms = [empty(shp(l) + (4,), torch.float32) for l in range(levels)]
+    nms = [empty(shp(l) + (4,), torch.float32) for l in range(levels)]
+    arr = lambda ts: (sf.Image * levels)(*[sf.image(t) for t in ts])
+    sf.call("sf_BuildPyramid", ctx.h, sf.image(dd), sf.image(raw), arr(depths), arr(vms), arr(nms), levels,
+            sf.Intrinsics(*K), 1000.0, 3.0)
+    ctx.sync()
+    return vms, nms, (dd, raw, depths)
+
+
+def _scene(sf, ctx, cfg, mapkw, nframes, seed):
+    """A map fused from nframes of a sequence at their true poses (device
+    and oracle, bit-identical), the next frame's pyramid (device tensors
+    and host copies), and the last fused frame's ray traced model maps
+    (levels resized) as LastFrame's maps."""
+    from oracle import oracle as O
+    from tests.test_gpu_fusion import _frame_inputs
+    import torch
+    K = cfg["K"]
+    seq = sequence(cfg["cols"], cfg["rows"], K, nframes + 1, trajectory=1, dropout=0.02, seed=seed)
+    gmap, omap = sf.Map(**mapkw), O.Map(**mapkw)
+    for d, rgb, mask, P in seq[:nframes]:
+        f = _frame_inputs(sf, ctx, d, rgb, mask, K)
+        R, RI, t = sf.pose_to_gpu(P)
+        nvis = C.c_uint32()
+        sf.call("sf_FuseMapColor", ctx.h, gmap.h, sf.image(f["raw"]), sf.image(f["rgb"]), sf.image(f["nmap"]),
+                sf.image(f["mask"]), 0, R, RI, t, *K, 3.0, 0.1, C.byref(nvis))
+        omap.fuse(f["raw_h"], rgb, f["nmap_h"], None, 0, P, K)
+    ctx.sync()
+    # LastFrame's maps: the oracle's raycast at the last fused pose, resized
+    Plast = seq[nframes - 1][3]
+    zc, zr = (cfg["cols"] + 7) // 8, (cfg["rows"] + 7) // 8
+    omap.visibility(Plast, K, cfg["cols"], cfg["rows"])
+    _, zmin, zmax, _, _ = omap.zrange(Plast, K, zc, zr)
+    v0, n0 = omap.raycast(Plast, K, cfg["cols"], cfg["rows"], zmin, zmax)
+    lv, ln = [v0], [n0]
+    for l in range(1, 3):
+        v, n = O.resize(lv[-1], ln[-1])
+        lv.append(v)
+        ln.append(n)
+    d, rgb, mask, P = seq[nframes]
+    vms, nms, keep = _pyramid(sf, ctx, d, K)
+    hv = [host(t) for t in vms]
+    hn = [host(t) for t in nms]
+    glv = [cuda(a) for a in lv]
+    gln = [cuda(a) for a in ln]
+    return dict(gmap=gmap, omap=omap, K=K, P=P, vms=vms, nms=nms, hv=hv, hn=hn, lv=lv, ln=ln, glv=glv, gln=gln,
+                keep=keep)
+
+
+def _run_both(sf, sc, cand):
+    from oracle import oracle as O
+    im = lambda ts: [sf.image(t) for t in ts]
+    g, gch = sf.validate_pose_batch(sc["ctx"], sc["gmap"], im(sc["vms"]), im(sc["nms"]), im(sc["glv"]), im(sc["gln"]),
+                                    sc["K"], cand)
+    o, och = O.validate_pose_batch(sc["omap"], sc["hv"], sc["hn"], sc["lv"], sc["ln"], sc["K"], cand)
+    return g, gch, o, och
+
+
+def _compare(g, o):
+    """Per-candidate agreement; returns the number of candidates whose
+    discrete ComputeSE3 decisions (iterations) differ."""
+    flips = 0
+    for k, (a, b) in enumerate(zip(g, o)):
+        assert a.visible == int(b[0]), "candidate %d visible %d vs %d" % (k, a.visible, b[0])
+        assert a.evaluated == int(b[2]), "candidate %d evaluated" % k
+        if not a.evaluated:
+            continue
+        assert a.rendered == int(b[1]), "candidate %d rendered" % k
+        assert a.accepted == int(b[3]), "candidate %d accepted %d vs %d" % (k, a.accepted, b[3])
+        if a.iterations != int(b[5]):
+            flips += 1
+            continue
+        assert abs(a.icp_count - int(b[7])) <= 2, "candidate %d count %d vs %d" % (k, a.icp_count, b[7])
+        pa = np.array(a.pose[:]).reshape(4, 4)
+        pb = b[8:].reshape(4, 4)
+        assert np.abs(pa - pb).max() < POSE_TOL, "candidate %d pose %g" % (k, np.abs(pa - pb).max())
+    return flips
+
+
+@pytest.fixture(scope="module")
+def c1(built):
+    import torch
+    import semantic_icpslam_gb300 as sf
+    assert torch.cuda.is_available()
+    ctx = sf.Context()
+    sc = _scene(sf, ctx, C1, MAP_C1, 4, seed=3)
+    sc["ctx"] = ctx
+    yield sf, sc
+    ctx.close()
+
+
+def test_validate_pose_batch_matches_oracle(c1):
+    sf, sc = c1
+    P = sc["P"]
+    cand = list(candidates(P, 22, seed=21))
+    far = P.copy()
+    far[:3, 3] += 20.0  # sees nothing: not evaluated
+    cand.insert(5, far)
+    cand.append(P.copy())
+    cand = np.array(cand)
+    g, gch, o, och = _run_both(sf, sc, cand)
+    assert not g[5].evaluated and g[5].visible < 512
+    assert g[0].evaluated and g[0].accepted
+    assert np.abs(np.array(g[0].pose[:]).reshape(4, 4) - P)[:3, 3].max() < 0.02
+    flips = _compare(g, o)
+    assert flips <= 1
+    assert gch == och
+    assert sum(c.accepted for c in g) >= 2
+
+
+def test_validate_pose_batch_min_visible_and_repeat(c1):
+    """A visible-count floor above every candidate's count evaluates none;
+    the same call twice gives the same results bit for bit."""
+    sf, sc = c1
+    cand = candidates(sc["P"], 9, seed=5)
+    im = lambda ts: [sf.image(t) for t in ts]
+    args = (sc["ctx"], sc["gmap"], im(sc["vms"]), im(sc["nms"]), im(sc["glv"]), im(sc["gln"]), sc["K"], cand)
+    a, ach = sf.validate_pose_batch(*args)
+    b, bch = sf.validate_pose_batch(*args)
+    assert ach == bch
+    assert [bytes(x) for x in a] == [bytes(x) for x in b]
+    none, nch = sf.validate_pose_batch(*args, min_visible=1 << 30)
+    assert nch == -1 and not any(c.evaluated for c in none)
+
+
+def test_validate_pose_batch_rejects_bad_arguments(c1):
+    sf, sc = c1
+    im = lambda ts: [sf.image(t) for t in ts]
+    with pytest.raises(sf.SfError):
+        sf.validate_pose_batch(sc["ctx"], sc["gmap"], im(sc["vms"]), im(sc["nms"]), im(sc["glv"][:1]) * 3,
+                               im(sc["gln"]), sc["K"], sc["P"][None])
+
+
+def test_validate_pose_batch_c5_256_candidates(built):
+    """256 candidates (sigma 5 cm / 5 deg) against one 640x480 frame: a
+    subset agrees with the oracle, the batch is deterministic, and the
+    true pose is evaluated and accepted close to the ground truth."""
+    import torch
+    import semantic_icpslam_gb300 as sf
+    ctx = sf.Context()
+    try:
+        sc = _scene(sf, ctx, C2, MAP_C2, 3, seed=2)
+        sc["ctx"] = ctx
+        P = sc["P"]
+        cand = candidates(P, 256, seed=7)
+        im = lambda ts: [sf.image(t) for t in ts]
+        args = (ctx, sc["gmap"], im(sc["vms"]), im(sc["nms"]), im(sc["glv"]), im(sc["gln"]), sc["K"], cand)
+        g, gch = sf.validate_pose_batch(*args)
+        g2, gch2 = sf.validate_pose_batch(*args)
+        assert gch == gch2 and [bytes(x) for x in g] == [bytes(x) for x in g2]
+        assert g[0].accepted and np.abs(np.array(g[0].pose[:]).reshape(4, 4) - P)[:3, 3].max() < 0.02
+        assert gch == next(i for i, c in enumerate(g) if c.accepted)
+        # the oracle on candidates that drew their own maps (their results
+        # do not depend on earlier candidates)
+        from oracle import oracle as O
+        pick = [k for k, c in enumerate(g) if c.rendered][:6]
+        o, _ = O.validate_pose_batch(sc["omap"], sc["hv"], sc["hn"], sc["lv"], sc["ln"], sc["K"], cand[pick])
+        assert _compare([g[k] for k in pick], o) <= 1
+    finally:
+        ctx.close()
+
+
+def _drive(sf, ctx, mode, seq, blanks, cand, O=None):
+    """The sequence's first frames, `blanks` blank frames (ICP fails: the
+    tracker gets lost after ten), then the rest with candidates registered."""
+    K = C1["K"]
+    rows, cols = seq[0][0].shape
+    out = []
+    if O is None:
+        cfg = sf.system_config(cols=cols, rows=rows, K=K, use_graph=mode, **MAP_C1)
+        s = sf.System(ctx, cfg, init_pose=seq[0][3])
+        grab = lambda d, c: s.grab(d, c)
+        res = lambda st: (int(st.tracked), int(st.state), int(st.missed), int(st.relocalised),
+                          np.array(st.pose[:]).reshape(4, 4))
+        setc = s.set_reloc_candidates
+    else:
+        s = O.System(dict(MAP_C1), cols, rows, K, init_pose=seq[0][3])
+        grab = lambda d, c: s.grab(d, c)
+        res = lambda r: (int(r[0]), int(r[2][10]), int(r[2][11]), int(r[2][12]), r[1])
+        setc = s.set_reloc
+    blank = (np.zeros((rows, cols), np.uint16), np.zeros((rows, cols, 3), np.uint8))
+    for d, rgb, _, _ in seq[:4]:
+        out.append(res(grab(d, rgb)))
+    for _ in range(blanks):
+        out.append(res(grab(*blank)))
+    setc(cand)
+    for d, rgb, _, _ in seq[4:]:
+        out.append(res(grab(d, rgb)))
+    if O is None:
+        s.close()
+    return out
+
+
+@pytest.mark.parametrize("mode", [0, 2, 1])
+def test_loop_relocalises_like_oracle(built, mode):
+    import torch
+    import semantic_icpslam_gb300 as sf
+    from oracle import oracle as O
+    ctx = sf.Context()
+    try:
+        seq = sequence(C1["cols"], C1["rows"], C1["K"], 8, trajectory=0)
+        cand = candidates(seq[4][3], 6, seed=9)[::-1]  # the true pose last
+        g = _drive(sf, ctx, mode, seq, 11, cand)
+        o = _drive(sf, ctx, mode, seq, 11, cand, O=O)
+        for i, (a, b) in enumerate(zip(g, o)):
+            assert a[:4] == b[:4], "frame %d: %s vs %s" % (i, a[:4], b[:4])
+            assert np.abs(a[4] - b[4]).max() < 2e-4, "frame %d pose" % i
+        states = [a[1] for a in g]
+        assert -1 in states and any(a[3] for a in g)  # lost, then relocalised
+        assert np.abs(g[-1][4] - seq[-1][3])[:3, 3].max() < 0.03
+    finally:
+        ctx.close()
