@@ -115,6 +115,17 @@ int sf_kernel_launches(uint64_t *out);
  * iteration start into slot 6, and clocks inside the solve into slots
  * 8-13; out (may be NULL, else 64 * 16 values) receives them. */
 int sf_icp_profile(sf_context *ctx, int enable, uint64_t *out);
+/* Bounds of the persistent ICP kernel's grid barriers (a diagnostic hook
+ * for testing failure detection; no counterpart in the reference).  Each
+ * barrier polls an arrival count at most poll_limit times (0 restores the
+ * default, 2^22, about a second) and waits for extra_arrivals arrivals
+ * beyond the grid's (0 by default; a test sets it so that no wait can end).
+ * A barrier that gives up records SF_FLAG_BARRIER_TIMEOUT, every CTA leaves
+ * its iterations, the tracking fails, and sf_ComputeSE3 /
+ * sf_ComputeSE3_rgbd return SF_ERR_TIMEOUT (sf_system_grab too, with the
+ * frame's stats.fail = 3); the context stays usable.  Takes effect for
+ * later launches (a frame graph captured before keeps its bounds). */
+int sf_icp_barrier_limits(sf_context *ctx, uint32_t poll_limit, uint32_t extra_arrivals);
 /* Copies `bytes` between any two host/device pointers (unified addressing)
  * on the context stream and waits for it. */
 int sf_memcpy(sf_context *ctx, void *dst, const void *src, size_t bytes);
@@ -455,7 +466,9 @@ typedef struct {
 typedef struct {
   int tracked;             /* Track() result for this frame                */
   int accepted;            /* ComputeSE3 acceptance (1 on the first frame) */
-  int fail;                /* 0 ok, 1 ICP count/NaN failure, 2 diverged    */
+  int fail;                /* 0 ok, 1 ICP count/NaN failure, 2 diverged,
+                              3 a bounded device wait gave up (the grab
+                              returns SF_ERR_TIMEOUT)                      */
   int iterations;          /* ICP iterations run                           */
   float icp_error;         /* sqrt(sum r^2) / count of the last iteration  */
   int icp_count;

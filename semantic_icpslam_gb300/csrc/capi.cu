@@ -172,6 +172,13 @@ int sf_context_flags(sf_context *ctx, uint32_t *flags_out) {
   return SF_OK;
 }
 
+int sf_icp_barrier_limits(sf_context *ctx, uint32_t poll_limit, uint32_t extra_arrivals) {
+  if (!ctx || extra_arrivals > 65536) return SF_ERR_INVALID;
+  ctx->icp.barrier_poll_limit = poll_limit ? poll_limit : (1u << 22);
+  ctx->icp.barrier_extra = extra_arrivals;
+  return SF_OK;
+}
+
 int sf_icp_profile(sf_context *ctx, int enable, uint64_t *out) {
   if (!ctx) return SF_ERR_INVALID;
   ctx->icp.profile = enable ? 1 : 0;
@@ -588,7 +595,7 @@ int sf_ComputeSE3(sf_context *ctx, int levels, const sf_image *nv, const sf_imag
     stats_out[3] = c.icpCount;
   }
   if (icp_error_out) *icp_error_out = c.icpError;
-  return SF_OK;
+  return c.timeout ? SF_ERR_TIMEOUT : SF_OK;
 }
 
 // ------------------------------------------------------ photometric term
@@ -715,7 +722,7 @@ int sf_ComputeSE3_rgbd(sf_context *ctx, int levels, const sf_image *nv, const sf
     errors_out[0] = c.icpError;
     errors_out[1] = c.rgbError;
   }
-  return SF_OK;
+  return c.timeout ? SF_ERR_TIMEOUT : SF_OK;
 }
 
 // ------------------------------------------------------------- mesh

@@ -538,6 +538,9 @@ struct PersistentArgs {
   const int *skip_flag;  // nonzero: the kernel does nothing
   uint32_t *flags;
   unsigned long long *prof;  // optional per-iteration phase clocks of CTA 0
+  unsigned poll_limit;       // polls before a grid barrier gives up
+  unsigned extra_arrivals;   // arrivals a barrier waits for beyond the grid (0; a test sets it to make
+                             // every wait run out)
 };
 
 // Phase clock of CTA 0 (SM cycles): 0 iteration start, 1 pixels
@@ -558,19 +561,23 @@ __device__ __forceinline__ void prof_mark(const PersistentArgs &a, int it, int k
 // count only grows, so the barrier is open once it reaches nb * (k + 1).
 // Thread 0 releases the CTA's accumulator adds (and the stores its threads
 // made before the __syncthreads) with its arrival and acquires everyone
-// else's with the poll that sees the count.  A wait that runs past 2^22
-// polls records SF_FLAG_BARRIER_TIMEOUT and goes on.
-__device__ __forceinline__ void grid_barrier(const PersistentArgs &a, int nb, int k) {
+// else's with the poll that sees the count.  A wait that runs past
+// a.poll_limit polls (2^22 unless a test lowers it) records
+// SF_FLAG_BARRIER_TIMEOUT and sets *abort (shared), after which the CTA
+// leaves its iterations with the tracking failed; the host reports
+// SF_ERR_TIMEOUT and the context stays usable.
+__device__ __forceinline__ void grid_barrier(const PersistentArgs &a, int nb, int k, int *abort) {
   __syncthreads();
   if (threadIdx.x == 0) {
     asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(a.arrivals) : "memory");
-    const unsigned target = (unsigned)nb * (unsigned)(k + 1);
+    const unsigned target = ((unsigned)nb + a.extra_arrivals) * (unsigned)(k + 1);
     unsigned polls = 0, seen;
     for (;;) {
       asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(seen) : "l"(a.arrivals) : "memory");
       if ((int)(seen - target) >= 0) break;
-      if (++polls > (1u << 22)) {
+      if (++polls > a.poll_limit) {
         atomicOr(a.flags, SF_FLAG_BARRIER_TIMEOUT);
+        *abort = 1;
         break;
       }
       __nanosleep(32);
@@ -617,10 +624,12 @@ __global__ void __launch_bounds__(kPThreads, 1) k_icp_persistent(PersistentArgs 
   __shared__ unsigned s2[2];
   __shared__ ff wpart[kPWarps][33];
   __shared__ unsigned long long sfix[kFixGroups * 29][kFixSlots];
+  __shared__ int abort_wait;  // a grid barrier gave up
   if (a.skip_flag && *a.skip_flag != 0) return;  // uniform across the grid
   if (threadIdx.x == 0) {
     ctl_begin(ctl, a.last_pose);
     s_solve_marks = nullptr;
+    abort_wait = 0;
   }
   __syncthreads();
   const int nb = gridDim.x;
@@ -652,7 +661,8 @@ __global__ void __launch_bounds__(kPThreads, 1) k_icp_persistent(PersistentArgs 
         if (threadIdx.x < 2) atomicAdd(rres + group * 2 + threadIdx.x, s2[threadIdx.x]);
       }
       prof_mark(a, it, 2);
-      grid_barrier(a, nb, RGB ? 2 * it : it);
+      grid_barrier(a, nb, RGB ? 2 * it : it, &abort_wait);
+      if (abort_wait) break;  // uniform: read after the barrier's __syncthreads
       prof_mark(a, it, 3);
       unsigned long long *fxr = a.fix_rgb + (size_t)set * kFixSet;
       if (RGB) {
@@ -670,7 +680,8 @@ __global__ void __launch_bounds__(kPThreads, 1) k_icp_persistent(PersistentArgs 
         rgb_rows_pass(L, a.rg[l], sigma, tiny, gtid, gstride, acc);
         block_reduce29<kPWarps>(acc, wpart, bsum);
         if (threadIdx.x < 29) fix_add(fxr + (group * 29 + threadIdx.x) * kFixSlots, bsum[threadIdx.x]);
-        grid_barrier(a, nb, 2 * it + 1);
+        grid_barrier(a, nb, 2 * it + 1, &abort_wait);
+        if (abort_wait) break;
       }
       read_fix_set(fx, sfix, sums, RGB);
       if (RGB) {
@@ -700,9 +711,16 @@ __global__ void __launch_bounds__(kPThreads, 1) k_icp_persistent(PersistentArgs 
       set = set == 2 ? 0 : set + 1;
       if (ctl.stop) break;
     }
-    if (ctl.stop) break;
+    if (ctl.stop || abort_wait) break;
   }
-  if (threadIdx.x == 0) s_solve_marks = nullptr;
+  if (threadIdx.x == 0) {
+    s_solve_marks = nullptr;
+    if (abort_wait) {  // a barrier gave up: the tracking failed
+      ctl.stop = 1;
+      ctl.timeout = 1;
+    }
+  }
+  __syncthreads();
   __syncwarp();
   if (threadIdx.x < 32) ctl_finish_fast(ctl, a.thresh, ssolve);
   __syncthreads();
@@ -996,6 +1014,8 @@ cudaError_t launch_icp_persistent(const IcpWorkspace &w, const IcpLevelArgs *lev
   a.skip_flag = skip_flag;
   a.flags = flags;
   a.prof = w.profile ? w.prof : nullptr;
+  a.poll_limit = w.barrier_poll_limit;
+  a.extra_arrivals = w.barrier_extra;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(rgb ? w.max_blocks_rgb : w.max_blocks);
   cfg.blockDim = dim3(kPThreads);

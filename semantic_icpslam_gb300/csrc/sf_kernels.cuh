@@ -70,6 +70,9 @@ struct IcpWorkspace {
   int threads = 0;
   unsigned long long *prof = nullptr;  // [64][8] phase clocks of CTA 0
   int profile = 0;                     // record phase clocks when set
+  // grid barrier bounds of the persistent kernel (sf_icp_barrier_limits)
+  unsigned barrier_poll_limit = 1u << 22;
+  unsigned barrier_extra = 0;
   // photometric scratch, grown on demand: correspondences of the largest
   // level, and candidate flags of every level for callers that pass none
   float4 *corr = nullptr;

@@ -162,6 +162,7 @@ struct TrackCtl {
   int accepted;           // final decision (valid after finish)
   float rgbError;         // photometric term (icpOnly = false), else 0
   int rgbCount;
+  int timeout;            // a bounded device wait gave up (the persistent kernel), stop = 1
 };
 
 SF_HD void ctl_begin(TrackCtl &c, const double *last_pose) {
@@ -181,6 +182,7 @@ SF_HD void ctl_begin(TrackCtl &c, const double *last_pose) {
   c.stop = 0;
   c.accepted = 0;
   c.rgbError = 0.f;
+  c.timeout = 0;
   c.rgbCount = 0;
 }
 

@@ -126,7 +126,7 @@ __global__ void k_sys_stats(const SysDev *s, const TrackCtl *ctl, DevMap m, cons
     st.fail = 0; st.iterations = 0; st.icp_error = 0.f; st.icp_count = 0;
     st.rgb_error = 0.f; st.rgb_count = 0;
   } else {
-    st.fail = ctl->stop;
+    st.fail = ctl->timeout ? 3 : ctl->stop;
     st.iterations = ctl->iters_run;
     st.icp_error = ctl->icpError;
     st.icp_count = ctl->icpCount;
@@ -931,7 +931,7 @@ int sf_system_grab(sf_system *s, const uint16_t *depth, const uint8_t *rgb, cons
   }
   if (s->cfg.use_graph != 0) s->dev_state = s->h_stats->state;
   if (stats) *stats = *s->h_stats;
-  return SF_OK;
+  return s->h_stats->fail == 3 ? SF_ERR_TIMEOUT : SF_OK;
 }
 
 int sf_system_grab_device(sf_system *s, const uint16_t *depth, const uint8_t *rgb,
