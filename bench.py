@@ -132,6 +132,7 @@ def bench_config():
 
 
 FLUSH_BYTES = 256 << 20
+AUTOTUNE = True  # every timed form takes the tuned launch shapes of its configuration (--no-autotune: defaults)
 
 
 class L2Flush:
@@ -187,7 +188,7 @@ def label_frames(n):
     return [syn.frame(i) for i in range(n)]
 
 
-def time_device_resident(sf, ctx, frames, steps, warmup, mode, barrier, timing=False, autotune=False, rgb=0,
+def time_device_resident(sf, ctx, frames, steps, warmup, mode, barrier, timing=False, autotune=None, rgb=0,
                          ndet=0, flush=None):
     """Frames/s with inputs already in HBM: one CUDA-event pair per timed
     step on the system stream, L2 flushed before each step outside the
@@ -205,12 +206,13 @@ def time_device_resident(sf, ctx, frames, steps, warmup, mode, barrier, timing=F
     if timing:
         sf.call("sf_system_set_timing", s.h, 1)
     tune = None
+    autotune = AUTOTUNE if autotune is None else autotune
     for i in range(warmup):
         s.grab_device(dev[i][0].data_ptr(), dev[i][1].data_ptr(), dev[i][2].data_ptr() if ndet else None, ndet)
         if autotune and i == warmup // 2:
-            cands, chosen = s.autotune(reps=10)
-            tune = {"chosen": {"ctas_per_sm": cands[chosen][0], "tile": [cands[chosen][1], cands[chosen][2]]},
-                    "raycast_ms": {"%dx%d/%d" % (x, y, m): round(ms, 4) for m, x, y, ms in cands}}
+            from semantic_icpslam_gb300 import tune as T
+            entry, cached = T.tuned(s, reps=10)
+            tune = dict(entry, cached=cached, cache=T.cache_path())
     ctx.sync()
     stream = torch.cuda.ExternalStream(ctx.stream)
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
@@ -286,6 +288,9 @@ def time_e2e(sf, ctx, frames, steps, warmup, mode, rgb=0, flush=None):
     host = [(pinned(d), pinned(c)) for d, c, _, _ in frames[:warmup + steps]]
     for i in range(warmup):
         s.grab(*host[i])
+        if AUTOTUNE and i == warmup // 2:
+            from semantic_icpslam_gb300 import tune as T
+            T.tuned(s, reps=10)
     ctx.sync()
     stream = torch.cuda.ExternalStream(ctx.stream)
     total = 0.0
@@ -754,8 +759,9 @@ def main():
                     help="log2 of the voxel-block heap (2^19 blocks = 4 GB of voxels)")
     ap.add_argument("--config", default="c2", choices=["c2", "c3"],
                     help="c2: the 640x480 room sequence (the headline); c3: the 1280x720 corridor stress run")
-    ap.add_argument("--autotune", action="store_true",
-                    help="run sf_system_autotune during the warm-up of the headline form and keep its choice")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default launch shapes (by default the headline form takes the tuned shapes of "
+                         "its configuration during the warm-up: cached, else timed by sf_system_autotune)")
     ap.add_argument("--quick", action="store_true",
                     help="only the CUDA-graph timing (for profiler runs)")
     ap.add_argument("--rgbd", action="store_true",
@@ -794,7 +800,9 @@ def main():
         return
 
     # headline: CUDA graph, inputs in HBM
-    g = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 1, barrier, autotune=args.autotune,
+    global AUTOTUNE
+    AUTOTUNE = not args.no_autotune
+    g = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 1, barrier,
                              rgb=1 if (args.quick and args.rgbd) else 0, flush=flush)
     elapsed = g["elapsed"]
     if ws > 1:

@@ -537,8 +537,29 @@ typedef struct {
   int chosen;
   float ms[16];
   int minb[16], tile_x[16], tile_y[16];
+  /* the integration's grid: CTAs per SM 2, 4, 8, 16, timed by rerunning
+   * the last frame's integration from the visible voxels as they stand
+   * (saved before and restored after each run, so the map is unchanged;
+   * a workspace of 8 KiB per visible block is allocated for the call);
+   * integrate_chosen = -1 when no block was visible */
+  int integrate_candidates;
+  int integrate_chosen;
+  float integrate_ms[8];
+  int integrate_ctas[8];
 } sf_autotune_report;
 int sf_system_autotune(sf_system *sys, int reps, sf_autotune_report *report);
+/* The frame's launch shapes: the raycast's (index of its candidate,
+ * 0..5: registers for 8 or 6 CTAs per SM x tiles 8x16, 16x8, 32x4) and the
+ * integration's CTAs per SM (1..64).  Every shape computes the same maps.
+ * sf_system_autotune picks them on the device at hand; a caller that cached
+ * a choice for a configuration sets it back with sf_system_set_tune (the
+ * frame graph is captured again on the next frame). */
+typedef struct {
+  int raycast;
+  int integrate_ctas_per_sm;
+} sf_frame_tune;
+int sf_system_get_tune(sf_system *sys, sf_frame_tune *tune);
+int sf_system_set_tune(sf_system *sys, const sf_frame_tune *tune);
 /* Tracker::mappingDisabled (Tracking.h:51, toggled by the viewer,
  * GUI/Viewer.cc:151-156): enabled = 0 switches the loop to localisation,
  * UpdateVisibility and RayTrace instead of FuseColor, and with detections

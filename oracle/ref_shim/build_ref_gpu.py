@@ -32,6 +32,10 @@ ROOT = os.path.dirname(ORACLE)
 OUT = os.path.join(ORACLE, "_ref", "gpu_c2")
 SRC = os.path.join(OUT, "src")
 LIB = os.path.join(OUT, "librefgpu.so")
+# The same sources built with FMA contraction off (-fmad=false): every float
+# operation rounds once, as the CPU oracle computes it
+OUT_NOFMA = os.path.join(ORACLE, "_ref", "gpu_c2_nofma")
+LIB_NOFMA = os.path.join(OUT_NOFMA, "librefgpu.so")
 REF = os.environ.get("SF_REFERENCE_DIR", "/root/reference")
 
 SOURCES = ["Mapping/DeviceMap.cu", "Mapping/FuseMap.cu", "Mapping/RenderScene.cu", "Tracking/Pyrdown.cu",
@@ -72,7 +76,9 @@ def prepare():
 
 
 def build(force=False, verbose=False):
-    """Compiles the prepared copies and the driver into librefgpu.so."""
+    """Compiles the prepared copies and the driver into librefgpu.so, as
+    the reference builds them (FMA contraction on) and with contraction
+    off (gpu_c2_nofma), both variants in parallel."""
     if not os.path.isdir(SRC):
         if os.path.isdir(REF):
             prepare()
@@ -81,13 +87,15 @@ def build(force=False, verbose=False):
     driver = os.path.join(HERE, "ref_gpu_driver.cu")
     srcs = [os.path.join(SRC, os.path.basename(s)) for s in SOURCES] + [driver]
     deps = srcs + [os.path.join(HERE, "ref_loop.h"), os.path.join(ROOT, "semantic_icpslam_gb300", "csrc", "sf_solve.h")]
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) > max(os.path.getmtime(s) for s in deps):
+    newest = max(os.path.getmtime(s) for s in deps)
+    todo = [(out, lib, extra) for out, lib, extra in ((OUT, LIB, []), (OUT_NOFMA, LIB_NOFMA, ["-fmad=false"]))
+            if force or not os.path.exists(lib) or os.path.getmtime(lib) <= newest]
+    if not todo:
         return LIB
     nvcc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
     nvcc = nvcc if os.path.exists(nvcc) else "nvcc"
     flags = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-rdc=true", "-Xcompiler", "-fPIC", "-w",
              "-I", SRC, "-I", os.path.join(ROOT, "semantic_icpslam_gb300", "csrc")]
-    objs = [os.path.join(OUT, os.path.basename(s) + ".o") for s in srcs]
 
     def run(cmd):
         if verbose:
@@ -96,10 +104,18 @@ def build(force=False, verbose=False):
         if r.returncode != 0:
             raise RuntimeError("reference CUDA build failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
 
-    with ThreadPoolExecutor(max_workers=len(srcs)) as ex:
-        list(ex.map(run, [[nvcc] + flags + ["-c", s, "-o", o] for s, o in zip(srcs, objs)]))
-    run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-rdc=true", "-shared", "-o", LIB + ".tmp"] + objs)
-    os.replace(LIB + ".tmp", LIB)
+    cmds, links = [], []
+    for out, lib, extra in todo:
+        os.makedirs(out, exist_ok=True)
+        objs = [os.path.join(out, os.path.basename(s) + ".o") for s in srcs]
+        cmds += [[nvcc] + flags + extra + ["-c", s, "-o", o] for s, o in zip(srcs, objs)]
+        links.append((lib, [nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-rdc=true", "-shared", "-o",
+                            lib + ".tmp"] + objs))
+    with ThreadPoolExecutor(max_workers=len(cmds)) as ex:
+        list(ex.map(run, cmds))
+    for lib, cmd in links:
+        run(cmd)
+        os.replace(lib + ".tmp", lib)
     return LIB
 
 

@@ -15,3 +15,4 @@ extern "C" int refgpu_grab(void *h, const uint16_t *depth, const uint8_t *rgb, d
 }
 extern "C" void refgpu_destroy(void *h) { refloop_destroy(h); }
 extern "C" void refgpu_set_rgb(void *h, int on) { refloop_set_rgb(h, on); }
+extern "C" void refgpu_map_arrays(void *h, void **out6, long long *sizes2) { refloop_map_arrays(h, out6, sizes2); }

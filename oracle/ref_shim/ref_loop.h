@@ -270,6 +270,21 @@ inline int refloop_grab(void *h, const uint16_t *depth, const uint8_t *rgb, doub
 
 inline void refloop_destroy(void *h) { delete static_cast<RefSystem *>(h); }
 
+// The map's arrays (device pointers in the CUDA build): hashEntries,
+// sdfBlock (voxels), visibleEntries, noVisibleEntries, heapCounter,
+// hashCounter (entryPtr); and the sizes NumEntries, NumSdfBlocks.
+inline void refloop_map_arrays(void *h, void **out6, long long *sizes2) {
+  RefSystem &s = *static_cast<RefSystem *>(h);
+  out6[0] = s.hashEntries.data;
+  out6[1] = s.sdfBlock.data;
+  out6[2] = s.visibleEntries.data;
+  out6[3] = s.noVisibleEntries.data;
+  out6[4] = s.heapCounter.data;
+  out6[5] = s.hashCounter.data;
+  sizes2[0] = DeviceMap::NumEntries;
+  sizes2[1] = DeviceMap::NumSdfBlocks;
+}
+
 inline void refloop_set_rgb(void *h, int on) { static_cast<RefSystem *>(h)->rgb = on != 0; }
 
 #endif  // REF_LOOP_H_

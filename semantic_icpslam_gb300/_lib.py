@@ -85,7 +85,12 @@ class RelocCandidate(C.Structure):
 
 class AutotuneReport(C.Structure):
     _fields_ = [("candidates", C.c_int), ("chosen", C.c_int), ("ms", C.c_float * 16), ("minb", C.c_int * 16),
-                ("tile_x", C.c_int * 16), ("tile_y", C.c_int * 16)]
+                ("tile_x", C.c_int * 16), ("tile_y", C.c_int * 16), ("integrate_candidates", C.c_int),
+                ("integrate_chosen", C.c_int), ("integrate_ms", C.c_float * 8), ("integrate_ctas", C.c_int * 8)]
+
+
+class FrameTune(C.Structure):
+    _fields_ = [("raycast", C.c_int), ("integrate_ctas_per_sm", C.c_int)]
 
 
 vp = C.c_void_p
@@ -162,6 +167,8 @@ SIGNATURES = {
     "sf_system_get_map": [vp, pvp],
     "sf_system_set_timing": [vp, C.c_int],
     "sf_system_autotune": [vp, C.c_int, C.POINTER(AutotuneReport)],
+    "sf_system_get_tune": [vp, C.POINTER(FrameTune)],
+    "sf_system_set_tune": [vp, C.POINTER(FrameTune)],
     "sf_system_set_mapping": [vp, C.c_int],
     "sf_system_stage_ms": [vp, F32P],
     "sf_system_pose_device": [vp, C.POINTER(C.POINTER(C.c_double))],

@@ -1019,12 +1019,32 @@ int fuse_scratch_unify(FuseScratch &f, const MapConst &c) {
 
 void launch_integrate(const DevMap &m, const sf_image &depth, const sf_image &rgb,
                       const sf_image *nmap, const sf_image *mask, int num_detection, const Cam *c,
-                      bool integrate, bool semantics, const int *run_flag, cudaStream_t s) {
+                      bool integrate, bool semantics, const int *run_flag, cudaStream_t s, int ctas_per_sm) {
   sf_image nm = nmap ? *nmap : sf_image{};
   sf_image mk = mask ? *mask : sf_image{};
   const bool sem = semantics && nmap && (num_detection <= 0 || mask);
-  k_integrate<<<sm_count() * 8, kIntThreads, 0, s>>>(m, depth, rgb, nm, mk, num_detection, c,
-                                                     integrate ? 1 : 0, sem ? 1 : 0, run_flag); note_launch();
+  k_integrate<<<sm_count() * ctas_per_sm, kIntThreads, 0, s>>>(m, depth, rgb, nm, mk, num_detection, c,
+                                                               integrate ? 1 : 0, sem ? 1 : 0, run_flag);
+  note_launch();
+}
+
+// The voxels of the visible blocks saved to / restored from scratch (the
+// autotuner's timing runs of the integration, which changes them).
+__global__ void k_save_visible(DevMap m, uint4 *scratch, unsigned nvis, int restore) {
+  for (unsigned b = blockIdx.x; b < nvis; b += gridDim.x) {
+    const int ptr = __ldcg(&m.visible[b].ptr);
+    if (ptr < 0) continue;
+    uint4 *v = (uint4 *)(m.voxels + ptr);
+    uint4 *w = scratch + (size_t)b * 512;
+    for (int i = threadIdx.x; i < 512; i += blockDim.x) {
+      if (restore) v[i] = w[i];
+      else w[i] = v[i];
+    }
+  }
+}
+
+void launch_save_visible(const DevMap &m, void *scratch, unsigned nvis, bool restore, cudaStream_t s) {
+  k_save_visible<<<sm_count() * 8, 256, 0, s>>>(m, (uint4 *)scratch, nvis, restore ? 1 : 0); note_launch();
 }
 
 }  // namespace sf

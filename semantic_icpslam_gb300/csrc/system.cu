@@ -235,8 +235,11 @@ struct sf_system {
   bool capturing = false;    // enqueue_device_frame is being captured
   bool stats_taken = false;  // this frame's enqueue took the stats early
   bool graph_early = false;  // the frame graph writes h_stats and h_ready
-  // raycast launch shape (sf_system_autotune)
+  // launch shapes (sf_system_autotune / sf_system_set_tune): the raycast's
+  // (an index into raycast_tune's candidates) and the integration's CTAs per SM
   RaycastTune rc_tune;
+  int rc_index = 0;
+  int int_ctas = 8;
   long long frames = 0;  // frames run (any form)
 };
 
@@ -457,7 +460,8 @@ int fuse_and_raytrace(sf_system *s, const Cam *cam, const int *run, int num_dete
     integrate = nvis > 0;
   }
   if (integrate) {
-    launch_integrate(m, depth, rgb, &nmap, &mask, num_detection, cam, true, num_detection > 0, run, st);
+    launch_integrate(m, depth, rgb, &nmap, &mask, num_detection, cam, true, num_detection > 0, run, st,
+                     s->int_ctas);
     if (num_detection > 0) launch_unify_neighbor(m, f, run, st);  // FuseMap.cu:1141-1160
   }
   if (first) mark(s, st, 5);
@@ -507,7 +511,7 @@ int enqueue_mapping(sf_system *s, const Cam *cam, const int *run, int num_detect
       const sf_image rd = img(s->d_rdepth, C, R, 4), rgb = img(s->d_rgb, C, R, 3), mask = img(s->d_mask, C, R, 1);
       launch_vmap_depth(img(s->d_mv[0], C, R, 16), rd, run, st);
       launch_visibility(m, f, cam, nullptr, nullptr, run, flags, st);
-      launch_integrate(m, rd, rgb, &mn0, &mask, num_detection, cam, false, true, run, st);
+      launch_integrate(m, rd, rgb, &mn0, &mask, num_detection, cam, false, true, run, st, s->int_ctas);
       launch_unify_neighbor(m, f, run, st);
     }
   }
@@ -966,7 +970,7 @@ int sf_system_set_mapping(sf_system *s, int enabled) {
 
 int sf_system_autotune(sf_system *s, int reps, sf_autotune_report *report) {
   if (!s || reps < 1 || reps > 1000) return SF_ERR_INVALID;
-  if (s->frames < 1) return SF_ERR_INVALID;  // needs one grabbed frame: the model maps' inputs
+  if (s->frames < 1) return SF_ERR_INVALID;  // needs one grabbed frame: the stages' inputs
   cudaStream_t st = ctx_stream(s->ctx);
   const int C = s->cfg.cols, R = s->cfg.rows;
   DevMap &m = map_dev(s->map);
@@ -974,50 +978,127 @@ int sf_system_autotune(sf_system *s, int reps, sf_autotune_report *report) {
   const sf_image mv = img(s->d_mv[0], C, R, 16), mn = img(s->d_mn[0], C, R, 16);
   const sf_image zmin = img(s->d_zmin, s->zc, s->zr, 4), zmax = img(s->d_zmax, s->zc, s->zr, 4);
   const sf_image fv = img(s->d_vmap[0], C, R, 16), fn = img(s->d_nmap[0], C, R, 16);
+  const sf_image depth = img(s->d_raw, C, R, 4), rgb = img(s->d_rgb, C, R, 3), mask = img(s->d_mask, C, R, 1);
   const Cam *cam = dev_field<Cam>(s->d_sys, offsetof(SysDev, cam));
   const int *run = dev_field<int>(s->d_sys, offsetof(SysDev, run));
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
-  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
-    if (e0) cudaEventDestroy(e0);
-    return SF_ERR_CUDA;
-  }
-  // The last frame's raycast again, with each shape: its inputs are
-  // unchanged, so it rewrites the same model maps and the loop's state is
-  // untouched.
+  static const int kIntCtas[4] = {2, 4, 8, 16};
   sf_autotune_report rep;
   memset(&rep, 0, sizeof(rep));
   rep.candidates = kRaycastTunes;
+  rep.integrate_chosen = -1;
+  // The last frame's integration and raycast run again as the frame ran
+  // them: the visible blocks' voxels are saved first and restored before
+  // every run, and L2 is flushed after the restore, so each timed launch
+  // starts from the frame's state; the raycast is timed right after an
+  // integration, as in the frame.  At the end the voxels are restored and
+  // the raycast rerun with the frame's shape, which rewrites the same model
+  // maps: the loop's state is unchanged.
+  unsigned nvis = 0;
+  cudaError_t e = cudaMemcpyAsync(&nvis, m.no_visible, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return SF_ERR_CUDA;
+  nvis = nvis < m.c.num_entries ? nvis : m.c.num_entries;
+  const bool fuse = s->mapping && nvis > 0;
+  const size_t flush_bytes = 256u << 20;
+  void *save = nullptr, *flush = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  if (e == cudaSuccess) e = cudaMalloc(&flush, flush_bytes);
+  if (e == cudaSuccess && fuse) e = cudaMalloc(&save, (size_t)nvis * 512 * sizeof(sf_voxel));
+  if (e == cudaSuccess && fuse) launch_save_visible(m, save, nvis, false, st);
+  auto prepare = [&]() {
+    if (fuse) launch_save_visible(m, save, nvis, true, st);
+    return cudaMemsetAsync(flush, 0, flush_bytes, st);
+  };
+  auto timed = [&](auto &&launch, float &ms_out) {
+    float total = 0.f;
+    for (int k = 0; k <= reps && e == cudaSuccess; ++k) {  // k = 0 warms up
+      e = launch(true);
+      if (e != cudaSuccess) break;
+      cudaEventRecord(e0, st);
+      launch(false);
+      cudaEventRecord(e1, st);
+      e = cudaEventSynchronize(e1);
+      float ms = 0.f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      if (k > 0) total += ms;
+    }
+    ms_out = total / (float)reps;
+  };
   int best = 0;
-  cudaError_t e = cudaSuccess;
   for (int i = 0; i < kRaycastTunes && e == cudaSuccess; ++i) {
     const RaycastTune t = raycast_tune(i);
-    launch_raycast(m, f, mv, mn, zmin, zmax, cam, f.counters + 3, &fv, &fn, run, st, t);  // warm-up
-    cudaEventRecord(e0, st);
-    for (int k = 0; k < reps; ++k)
+    timed([&](bool before) -> cudaError_t {
+      if (before) {
+        cudaError_t q = prepare();
+        if (fuse) launch_integrate(m, depth, rgb, &fn, &mask, 0, cam, true, false, run, st, s->int_ctas);
+        return q;
+      }
       launch_raycast(m, f, mv, mn, zmin, zmax, cam, f.counters + 3, &fv, &fn, run, st, t);
-    cudaEventRecord(e1, st);
-    e = cudaEventSynchronize(e1);
-    float ms = 0.f;
-    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-    rep.ms[i] = ms / (float)reps;
+      return cudaSuccess;
+    }, rep.ms[i]);
     rep.minb[i] = t.minb;
     rep.tile_x[i] = t.tx;
     rep.tile_y[i] = t.ty;
     if (rep.ms[i] < rep.ms[best]) best = i;
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  if (e != cudaSuccess) return SF_ERR_CUDA;
   rep.chosen = best;
-  const RaycastTune t = raycast_tune(best);
-  if (t.minb != s->rc_tune.minb || t.tx != s->rc_tune.tx || t.ty != s->rc_tune.ty) {
-    s->rc_tune = t;
-    if (s->gexec) {  // recaptured with the new shape on the next frame
-      cudaGraphExecDestroy(s->gexec);
-      s->gexec = nullptr;
+  int ibest = 2;
+  if (fuse) {
+    rep.integrate_candidates = 4;
+    for (int i = 0; i < 4 && e == cudaSuccess; ++i) {
+      timed([&](bool before) -> cudaError_t {
+        if (before) return prepare();
+        launch_integrate(m, depth, rgb, &fn, &mask, 0, cam, true, false, run, st, kIntCtas[i]);
+        return cudaSuccess;
+      }, rep.integrate_ms[i]);
+      rep.integrate_ctas[i] = kIntCtas[i];
+      if (rep.integrate_ms[i] < rep.integrate_ms[ibest]) ibest = i;
     }
+    rep.integrate_chosen = ibest;
   }
+  // the frame's state back
+  if (e == cudaSuccess && fuse) launch_save_visible(m, save, nvis, true, st);
+  if (e == cudaSuccess) launch_raycast(m, f, mv, mn, zmin, zmax, cam, f.counters + 3, &fv, &fn, run, st, s->rc_tune);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(save);
+  cudaFree(flush);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return SF_ERR_CUDA;
+  }
+  sf_frame_tune tune;
+  tune.raycast = best;
+  tune.integrate_ctas_per_sm = fuse ? kIntCtas[ibest] : s->int_ctas;
+  const int r = sf_system_set_tune(s, &tune);
   if (report) *report = rep;
+  return r;
+}
+
+int sf_system_get_tune(sf_system *s, sf_frame_tune *t) {
+  if (!s || !t) return SF_ERR_INVALID;
+  t->raycast = s->rc_index;
+  t->integrate_ctas_per_sm = s->int_ctas;
+  return SF_OK;
+}
+
+int sf_system_set_tune(sf_system *s, const sf_frame_tune *t) {
+  if (!s || !t || t->raycast < 0 || t->raycast >= kRaycastTunes || t->integrate_ctas_per_sm < 1 ||
+      t->integrate_ctas_per_sm > 64)
+    return SF_ERR_INVALID;
+  const RaycastTune rt = raycast_tune(t->raycast);
+  const bool changed = rt.minb != s->rc_tune.minb || rt.tx != s->rc_tune.tx || rt.ty != s->rc_tune.ty ||
+                       t->integrate_ctas_per_sm != s->int_ctas;
+  s->rc_tune = rt;
+  s->rc_index = t->raycast;
+  s->int_ctas = t->integrate_ctas_per_sm;
+  if (changed && s->gexec) {  // recaptured with the new shapes on the next frame
+    cudaGraphExecDestroy(s->gexec);
+    s->gexec = nullptr;
+  }
   return SF_OK;
 }
 

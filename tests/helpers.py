@@ -113,3 +113,18 @@ MAP_C3 = dict(voxel_size=0.003, trunc_dist=0.024, num_buckets=1 << 22, num_exces
               num_sdf_blocks=1 << 18)
 C3_ICP = dict(levels=4, iters=(10, 5, 4, 0), min_count=(2000, 1000, 100, 0))
 C3_SEQ = dict(scene=1, trajectory=2, dropout=0.02, noise=0.25)
+
+
+class _DevBuf:
+    """A device allocation made outside torch, seen through
+    __cuda_array_interface__ (bytes)."""
+
+    def __init__(self, ptr, nbytes):
+        self.__cuda_array_interface__ = {"shape": (nbytes,), "typestr": "|u1", "data": (int(ptr), False),
+                                         "version": 3, "strides": None}
+
+
+def dev_bytes(ptr, nbytes):
+    """A uint8 torch tensor viewing nbytes of device memory at ptr."""
+    import torch
+    return torch.as_tensor(_DevBuf(ptr, nbytes), device="cuda")

@@ -4,30 +4,36 @@ TSDF refinement it drives.
 * Its backward equals direct sf_RaycastAdjoint calls (pose exactly, TSDF up
   to the order of float atomics).
 * 50 Adam steps on the TSDF against 8 seeded keyframes with noisy depth
-  (the differentiable-raycast workload, at 320x240 and 10 mm) lower the
-  depth loss.
+  (the differentiable-raycast workload, at 320x240 / 10 mm and at
+  640x480 / 5 mm) lower the depth loss.
 """
 import ctypes as C
 
 import numpy as np
 import pytest
 
-from tests.helpers import C1, MAP_C1, cuda, sequence
+from tests.helpers import C1, C2, MAP_C1, MAP_C2, cuda, sequence
 from tests.test_gpu_fusion import _frame_inputs
 
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(scope="module")
-def fused(built):
+# c1: 320x240 / 10 mm; c4: the differentiable-raycast workload at 640x480
+# and 5 mm (50 Adam steps against 8 seeded keyframes with noisy depth)
+SCENES = {"c1": (C1, MAP_C1), "c4": (C2, MAP_C2)}
+
+
+@pytest.fixture(scope="module", params=sorted(SCENES))
+def fused(built, request):
     import torch
     import semantic_icpslam_gb300 as sf
     from semantic_icpslam_gb300 import autograd as ag
     assert torch.cuda.is_available()
     ctx = sf.Context()
-    K = C1["K"]
-    seq = sequence(C1["cols"], C1["rows"], K, 9, trajectory=0, dropout=0.02)
-    tmap = ag.TorchMap(ctx, **MAP_C1)
+    cfg, mapkw = SCENES[request.param]
+    K = cfg["K"]
+    seq = sequence(cfg["cols"], cfg["rows"], K, 9, trajectory=0, dropout=0.02)
+    tmap = ag.TorchMap(ctx, **mapkw)
     for d, rgb, mask, P in seq[:8]:
         f = _frame_inputs(sf, ctx, d, rgb, mask, K)
         R, RI, t = sf.pose_to_gpu(P)
@@ -35,7 +41,7 @@ def fused(built):
         sf.call("sf_FuseMapColor", ctx.h, tmap.h, sf.image(f["raw"]), sf.image(f["rgb"]), sf.image(f["nmap"]),
                 sf.image(f["mask"]), 0, R, RI, t, *K, 3.0, 0.1, C.byref(nvis))
     ctx.sync()
-    r = ag.Renderer(ctx, tmap, C1["cols"], C1["rows"], K)
+    r = ag.Renderer(ctx, tmap, cfg["cols"], cfg["rows"], K)
     yield sf, ag, ctx, tmap, r, seq
     tmap.close()
     ctx.close()

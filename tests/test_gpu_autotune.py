@@ -1,12 +1,16 @@
 """sf_system_autotune (the Autotune entry point, no counterpart in the
 reference): it times the last frame's raycast under each launch shape and
+the integration under each grid size, in the state the frame left, and
 keeps the fastest.  Every shape computes the same maps, so a system that
-autotunes mid-sequence must produce the same poses, statistics and model
-maps, bit for bit, as one that does not."""
+autotunes mid-sequence, or takes any shape by sf_system_set_tune, must
+produce the same poses, statistics, model maps and map, bit for bit, as one
+that does not; and the timing runs must leave the map and model maps as
+they were.  semantic_icpslam_gb300.tune caches the choice per
+configuration as JSON."""
 import numpy as np
 import pytest
 
-from tests.helpers import C1, MAP_C1, sequence
+from tests.helpers import C1, MAP_C1, map_to_host, sequence
 
 pytestmark = pytest.mark.gpu
 
@@ -50,12 +54,28 @@ def _compare(sf, ctx, seq, a, b):
     for d, rgb, _, _ in seq[:3]:
         a.grab(d, rgb)
         b.grab(d, rgb)
-    cands, chosen = b.autotune(reps=3)
-    assert len(cands) == 6 and 0 <= chosen < 6
+    import ctypes as C
+    rep = sf._lib.AutotuneReport()
+    sf.call("sf_system_autotune", b.h, 3, C.byref(rep))
+    cands = [(rep.minb[i], rep.tile_x[i], rep.tile_y[i], rep.ms[i]) for i in range(rep.candidates)]
+    assert len(cands) == 6 and 0 <= rep.chosen < 6
     assert all(ms > 0 for _, _, _, ms in cands)
     assert {(m, x, y) for m, x, y, _ in cands} == {(m, x, y) for m in (8, 6) for x, y in ((8, 16), (16, 8), (32, 4))}
+    assert rep.integrate_candidates == 4 and 0 <= rep.integrate_chosen < 4
+    assert [rep.integrate_ctas[i] for i in range(4)] == [2, 4, 8, 16] and min(rep.integrate_ms[:4]) > 0
+    t = sf._lib.FrameTune()
+    sf.call("sf_system_get_tune", b.h, C.byref(t))
+    assert t.raycast == rep.chosen and t.integrate_ctas_per_sm == rep.integrate_ctas[rep.integrate_chosen]
     for x, y in zip(_model(ctx, a), _model(ctx, b)):  # the timing runs left the model maps as they were
         np.testing.assert_array_equal(x, y)
+    ea, va, _ = map_to_host(ctx, a.map())  # and the voxels the integration runs touched
+    eb, vb, _ = map_to_host(ctx, b.map())
+    assert np.array_equal(va.view(np.uint8), vb.view(np.uint8))
+    # the least likely shapes: the results still do not change
+    far = sf._lib.FrameTune(5, 2)
+    sf.call("sf_system_set_tune", b.h, C.byref(far))
+    with pytest.raises(sf.SfError):
+        sf.call("sf_system_set_tune", b.h, C.byref(sf._lib.FrameTune(6, 8)))
     for d, rgb, _, _ in seq[3:]:
         sa = a.grab(d, rgb)
         sb = b.grab(d, rgb)
@@ -66,3 +86,25 @@ def _compare(sf, ctx, seq, a, b):
         np.testing.assert_array_equal(x, y)
     with pytest.raises(sf.SfError):
         b.autotune(reps=0)
+
+
+def test_tune_cache_per_configuration(lib, tmp_path):
+    """The first system of a configuration times and caches; the next takes
+    the cached shapes without timing."""
+    import ctypes as C
+    from semantic_icpslam_gb300 import tune as T
+    sf, ctx = lib
+    seq = sequence(C1["cols"], C1["rows"], C1["K"], 2, trajectory=1, dropout=0.02)
+    cfg = sf.system_config(cols=C1["cols"], rows=C1["rows"], K=C1["K"], use_graph=1, **MAP_C1)
+    path = str(tmp_path / "tune.json")
+    s1 = sf.System(ctx, cfg, init_pose=seq[0][3])
+    s1.grab(seq[0][0], seq[0][1])
+    e1, cached1 = T.tuned(s1, reps=2, path=path)
+    s2 = sf.System(ctx, cfg, init_pose=seq[0][3])
+    e2, cached2 = T.tuned(s2, reps=2, path=path)  # before any frame: only the cache can serve it
+    assert not cached1 and cached2 and e1 == e2
+    t = sf._lib.FrameTune()
+    sf.call("sf_system_get_tune", s2.h, C.byref(t))
+    assert (t.raycast, t.integrate_ctas_per_sm) == (e1["raycast"], e1["integrate_ctas_per_sm"])
+    s1.close()
+    s2.close()

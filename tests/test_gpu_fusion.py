@@ -87,17 +87,20 @@ def test_fuse_sequence_bit_exact(lib, cfg, mcfg, dropout, nframes):
     gmap.close()
 
 
-def test_label_fusion_bit_exact(lib):
-    """FuseMapColor with instance masks: label / count / label_2 / count_2."""
+@pytest.mark.parametrize("cfg,mcfg,nframes", [(C1, MAP_C1, 5), (C2, MAP_C2, 3)])
+def test_label_fusion_bit_exact(lib, cfg, mcfg, nframes):
+    """FuseMapColor with instance masks: label / count / label_2 / count_2.
+    The 640x480 case is the label-fusion workload: class ids 0-80, ten
+    projected primitives per frame, 5% random label flips."""
     from oracle import oracle as O
     import ctypes as C
     sf, ctx = lib
-    cfg = C1
     K = cfg["K"]
-    seq = sequence(cfg["cols"], cfg["rows"], K, 5, trajectory=0, label_flip=0.05, n_objects=10, seed=5)
-    gmap = sf.Map(**MAP_C1)
-    omap = O.Map(**MAP_C1)
-    for i in range(5):
+    seq = sequence(cfg["cols"], cfg["rows"], K, nframes, trajectory=0, label_flip=0.05, n_objects=10, seed=5)
+    gmap = sf.Map(**mcfg)
+    omap = O.Map(**mcfg)
+    labels = set()
+    for i in range(nframes):
         d, rgb, mask, P = seq[i]
         f = _frame_inputs(sf, ctx, d, rgb, mask, K)
         R, RI, t = sf.pose_to_gpu(P)
@@ -109,8 +112,10 @@ def test_label_fusion_bit_exact(lib):
         adopt_layout(omap, map_to_host(ctx, gmap)[0])
         omap.unify_neighbor()
         _compare_maps(ctx, gmap, omap)
+        labels |= set(np.unique(mask).tolist())
     e, v, _ = map_to_host(ctx, gmap)
     assert (v["count"] > 0).sum() > 1000 and (v["label"] > 0).sum() > 100
+    assert max(labels) <= 80 and len(labels) > 40  # flipped labels span the 0-80 ids
     gmap.close()
 
 

@@ -1,0 +1,141 @@
+"""Parity against the reference's own CUDA kernels on the GPU: the
+reference's Tracking/*.cu and Mapping/*.cu, built for sm_103a from copies
+with the 640x480 benchmark map's constants (oracle/_ref/gpu_c2, prepared by
+oracle/ref_shim/build_ref_gpu.py), run the first frame of the benchmark
+sequence in System::GrabImage's order, and so does this library's loop, on
+the same inputs and pose.
+
+Two builds of the reference take part:
+  * as the reference builds it (nvcc's default FMA contraction): the
+    integration's world-to-camera products fuse into FMAs, so TSDF values
+    differ in their last bits and a few voxels at pixel borders project to
+    the neighbouring pixel;
+  * with contraction off (-fmad=false), where every float operation rounds
+    once, as the reference's source states it and as this library computes
+    it: the voxels of every block both allocated are equal bit for bit.
+In both, the reference's bucket lock drops allocations under contention
+(Mapping/DeviceMap.cu:23-69: a thread that finds the bucket locked skips the
+block for this frame), so its allocated set is a subset of this library's,
+whose allocation is the serial semantics without drops.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+from tests.helpers import C2, dev_bytes, sequence
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+BUILDS = {"fma": os.path.join(ROOT, "oracle", "_ref", "gpu_c2", "librefgpu.so"),
+          "nofma": os.path.join(ROOT, "oracle", "_ref", "gpu_c2_nofma", "librefgpu.so")}
+MAP = dict(voxel_size=0.005, trunc_dist=0.04, num_buckets=1 << 20, num_excess=1 << 18, num_sdf_blocks=1 << 19)
+
+
+def _blocks(entries, voxels_dev, nbytes):
+    """{position key: 512 x 16 voxel bytes} of the allocated blocks."""
+    import torch
+    sel = entries[entries["ptr"] >= 0]
+    vox = dev_bytes(voxels_dev, nbytes).view(-1, 512 * 16)
+    blk = vox[torch.from_numpy((sel["ptr"] // 512).astype(np.int64)).cuda()].cpu().numpy()
+    keys = [(int(x), int(y), int(z)) for x, y, z in zip(sel["x"], sel["y"], sel["z"])]
+    return dict(zip(keys, blk))
+
+
+def _reference_frame(path, frame, K):
+    from oracle.oracle import ENTRY_DTYPE
+    import torch
+    L = C.CDLL(path)
+    L.refgpu_create.restype = C.c_void_p
+    L.refgpu_create.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_float), C.c_float, C.c_float, C.POINTER(C.c_double)]
+    L.refgpu_grab.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]
+    L.refgpu_destroy.argtypes = [C.c_void_p]
+    L.refgpu_map_arrays.argtypes = [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_longlong)]
+    d, rgb, _, P = frame
+    init = np.ascontiguousarray(P, np.float64)
+    h = L.refgpu_create(C2["cols"], C2["rows"], (C.c_float * 4)(*K), 1000.0, 3.0,
+                        init.ctypes.data_as(C.POINTER(C.c_double)))
+    assert h
+    pose = np.zeros(16, np.float64)
+    assert L.refgpu_grab(h, np.ascontiguousarray(d).ctypes.data, np.ascontiguousarray(rgb).ctypes.data,
+                         pose.ctypes.data_as(C.POINTER(C.c_double))) == 1
+    torch.cuda.synchronize()
+    ptrs = (C.c_void_p * 6)()
+    sizes = (C.c_longlong * 2)()
+    L.refgpu_map_arrays(h, ptrs, sizes)
+    ne, ns = int(sizes[0]), int(sizes[1])
+    ent = np.empty(ne, ENTRY_DTYPE)
+    ent[:] = dev_bytes(ptrs[0], ne * 32).cpu().numpy().view(ENTRY_DTYPE)
+    nvis = int(dev_bytes(ptrs[3], 4).cpu().numpy().view(np.uint32)[0])
+    vis = dev_bytes(ptrs[2], ne * 32).cpu().numpy().view(ENTRY_DTYPE)[:nvis]
+    blocks = _blocks(ent, ptrs[1], ns * 512 * 16)
+    L.refgpu_destroy(h)
+    return blocks, vis
+
+
+def _our_frame(frame, K):
+    from oracle.oracle import ENTRY_DTYPE
+    import semantic_icpslam_gb300 as sf
+    ctx = sf.Context()
+    try:
+        d, rgb, _, P = frame
+        cfg = sf.system_config(cols=C2["cols"], rows=C2["rows"], K=K, use_graph=2, **MAP)
+        s = sf.System(ctx, cfg, init_pose=P)
+        st = s.grab(d, rgb)
+        assert st.tracked == 1
+        m = s.map()
+        a = m.arrays()
+        ent = ctx.download(a.hash_entries, ENTRY_DTYPE, m.num_entries)
+        nvis = st.visible
+        vis = ctx.download(a.visible_entries, ENTRY_DTYPE, m.num_entries)[:nvis]
+        blocks = _blocks(ent, a.voxel_blocks, MAP["num_sdf_blocks"] * 512 * 16)
+        s.close()
+        return blocks, vis
+    finally:
+        ctx.close()
+
+
+@pytest.fixture(scope="module")
+def frames(built):
+    import torch
+    assert torch.cuda.is_available()
+    for p in BUILDS.values():
+        if not os.path.exists(p):
+            pytest.skip("the reference's CUDA build is not present")
+    seq = sequence(C2["cols"], C2["rows"], C2["K"], 1, trajectory=1, seed=2, dropout=0.02)
+    return seq[0], _our_frame(seq[0], C2["K"])
+
+
+def _keys(entries):
+    return {(int(x), int(y), int(z)) for x, y, z in zip(entries["x"], entries["y"], entries["z"])}
+
+
+@pytest.mark.parametrize("build", ["nofma", "fma"])
+def test_first_frame_matches_reference_cuda_build(frames, build):
+    frame, (ours, our_vis) = frames
+    ref, ref_vis = _reference_frame(BUILDS[build], frame, C2["K"])
+    a, b = set(ours), set(ref)
+    assert b <= a, "the reference allocated %d blocks this library did not" % len(b - a)
+    assert len(a - b) <= 0.05 * len(a)  # the reference's dropped allocations
+    # visible blocks: the reference's are this library's minus the dropped ones
+    rv, ov = _keys(ref_vis), _keys(our_vis)
+    assert rv <= ov and rv == ov & b
+    common = sorted(b)
+    g = np.stack([ours[k] for k in common]).view(np.uint8).reshape(-1, 16)
+    r = np.stack([ref[k] for k in common]).view(np.uint8).reshape(-1, 16)
+    w_g, w_r = g[:, 4], r[:, 4]
+    sdf_g, sdf_r = g[:, :4].copy().view(np.float32)[:, 0], r[:, :4].copy().view(np.float32)[:, 0]
+    seen = w_g > 0
+    assert seen.sum() > 1e6
+    if build == "nofma":
+        assert np.array_equal(g, r)  # every voxel of every common block, bit for bit
+    else:
+        same_w = (w_g == w_r).mean()
+        both = seen & (w_r > 0)
+        dt = np.abs(sdf_g[both] - sdf_r[both])
+        print("FMA-contracted reference: %d common blocks, weights equal on %.6f of voxels, TSDF max diff %.3g, "
+              "bit-equal TSDF on %.4f" % (len(common), same_w, dt.max(), (dt == 0).mean()))
+        assert same_w > 0.999
+        assert dt.max() < 1e-5
