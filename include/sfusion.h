@@ -137,6 +137,18 @@ int sf_map_create(const sf_map_config *cfg, sf_map **out);
 int sf_map_wrap(const sf_map_config *cfg, const sf_device_map *arrays, sf_map **out);
 int sf_map_destroy(sf_map *map);
 int sf_map_arrays(const sf_map *map, sf_device_map *out);
+/* Bounds-checked build (no counterpart in the reference, whose race
+ * analysis would need a memory checker): the library built with
+ * SF_BOUNDS_CHECK (semantic_icpslam_gb300/build.py, debug_bounds) checks
+ * every hash-chain link and every block pointer taken from the table or the
+ * block window before use; a bad one sets a bit in the map's status word
+ * (SF_BOUND_CHAIN 1: a chain link beyond the table; SF_BOUND_PTR 2: a block
+ * pointer outside the voxel array or not a multiple of 512) and the access
+ * is skipped.  sf_map_bounds_status reads the word (always 0 in the
+ * release build); sf_build_flags tells which build is loaded. */
+#define SF_BUILD_BOUNDS_CHECK 1u
+int sf_map_bounds_status(sf_context *ctx, const sf_map *map, uint32_t *out);
+int sf_build_flags(uint32_t *out);
 /* Rebuilds the allocated-entry index after the hash table was written
  * outside this library (e.g. a map loaded from disk). */
 int sf_map_rebuild_index(sf_context *ctx, sf_map *map);

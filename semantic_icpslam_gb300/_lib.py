@@ -8,7 +8,9 @@ import os
 import threading
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "libsfusion.so")
+# SF_LIBRARY selects another build of the library (the bounds-checked
+# libsfusion_checked.so); the default is the release build
+LIB_PATH = os.environ.get("SF_LIBRARY") or os.path.join(_HERE, "libsfusion.so")
 
 (SF_OK, SF_ERR_INVALID, SF_ERR_CUDA, SF_ERR_OVERFLOW, SF_ERR_TIMEOUT, SF_ERR_NO_DEVICE, SF_ERR_STATE,
  SF_ERR_TOO_LARGE, SF_ERR_IO) = range(9)
@@ -115,6 +117,8 @@ SIGNATURES = {
     "sf_map_wrap": [C.POINTER(MapConfig), C.POINTER(DeviceMap), pvp],
     "sf_map_destroy": [vp],
     "sf_map_arrays": [vp, C.POINTER(DeviceMap)],
+    "sf_map_bounds_status": [vp, vp, U32P],
+    "sf_build_flags": [U32P],
     "sf_map_rebuild_index": [vp, vp],
     "sf_map_counters": [vp, vp, I32P],
     "sf_map_write": [vp, vp, C.c_char_p],

@@ -47,23 +47,33 @@ def _stale(obj, src, headers):
     return os.path.getmtime(src) > t or any(os.path.getmtime(h) > t for h in headers)
 
 
-def build(force=False, verbose=False, jobs=None):
-    os.makedirs(BUILD, exist_ok=True)
+LIB_CHECKED = os.path.join(HERE, "libsfusion_checked.so")
+
+
+def build(force=False, verbose=False, jobs=None, debug_bounds=False):
+    """The release library, or with debug_bounds the bounds-checked one
+    (-DSF_BOUNDS_CHECK, libsfusion_checked.so, objects in _build/checked):
+    the same kernels with every hash-chain link and block pointer checked
+    before use, for tests against corrupted maps."""
+    bdir = os.path.join(BUILD, "checked") if debug_bounds else BUILD
+    lib = LIB_CHECKED if debug_bounds else LIB
+    extra = ["-DSF_BOUNDS_CHECK"] if debug_bounds else []
+    os.makedirs(bdir, exist_ok=True)
     cu, cpp = sources()
     headers = _headers()
     nvcc = _nvcc()
     cmds = []
     objs = []
     for f in cu:
-        src, obj = os.path.join(CSRC, f), os.path.join(BUILD, f + ".o")
+        src, obj = os.path.join(CSRC, f), os.path.join(bdir, f + ".o")
         objs.append(obj)
         if force or _stale(obj, src, headers):
-            cmds.append([nvcc] + NVCC_FLAGS + ["-c", src, "-o", obj])
+            cmds.append([nvcc] + NVCC_FLAGS + extra + ["-c", src, "-o", obj])
     for f in cpp:
-        src, obj = os.path.join(CSRC, f), os.path.join(BUILD, f + ".o")
+        src, obj = os.path.join(CSRC, f), os.path.join(bdir, f + ".o")
         objs.append(obj)
         if force or _stale(obj, src, headers):
-            cmds.append(["g++"] + CXX_FLAGS + ["-c", src, "-o", obj])
+            cmds.append(["g++"] + CXX_FLAGS + extra + ["-c", src, "-o", obj])
 
     def run(cmd):
         if verbose:
@@ -77,10 +87,10 @@ def build(force=False, verbose=False, jobs=None):
         for err in ex.map(run, cmds):
             if verbose and err.strip():
                 print(err)
-    if cmds or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
-        run([nvcc] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs)
-        os.replace(LIB + ".tmp", LIB)
-    return LIB
+    if cmds or not os.path.exists(lib) or any(os.path.getmtime(o) > os.path.getmtime(lib) for o in objs):
+        run([nvcc] + ARCH + ["-shared", "-o", lib + ".tmp"] + objs)
+        os.replace(lib + ".tmp", lib)
+    return lib
 
 
 # The libtorch C++ autograd function (torch_ext/raycast_autograd.cpp): a

@@ -210,6 +210,8 @@ static int map_alloc_index(sf_map *m) {
   SF_CHECK(cudaMalloc(&m->d.alloc_list, sizeof(int) * ne));
   SF_CHECK(cudaMalloc(&m->d.alloc_count, sizeof(int)));
   SF_CHECK(cudaMemset(m->d.alloc_count, 0, sizeof(int)));
+  SF_CHECK(cudaMalloc(&m->d.status, sizeof(uint32_t)));
+  SF_CHECK(cudaMemset(m->d.status, 0, sizeof(uint32_t)));
   return SF_OK;
 }
 
@@ -296,8 +298,26 @@ int sf_map_destroy(sf_map *m) {
   }
   cudaFree(m->d.alloc_list);
   cudaFree(m->d.alloc_count);
+  cudaFree(m->d.status);
   fuse_scratch_free(m->scratch);
   delete m;
+  return SF_OK;
+}
+
+int sf_map_bounds_status(sf_context *ctx, const sf_map *m, uint32_t *out) {
+  if (!ctx || !m || !out) return SF_ERR_INVALID;
+  SF_CHECK(cudaMemcpyAsync(out, m->d.status, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  SF_CHECK(cudaStreamSynchronize(ctx->stream));
+  return SF_OK;
+}
+
+int sf_build_flags(uint32_t *out) {
+  if (!out) return SF_ERR_INVALID;
+#ifdef SF_BOUNDS_CHECK
+  *out = SF_BUILD_BOUNDS_CHECK;
+#else
+  *out = 0;
+#endif
   return SF_OK;
 }
 

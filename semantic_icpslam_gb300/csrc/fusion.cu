@@ -296,7 +296,7 @@ __device__ __forceinline__ void create_entry(DevMap &m, i3 p, int offset, int4 &
   int old = atomicSub(m.heap_counter, 1);
   if (old >= 0) {
     int ptr = m.heap[old];
-    if (ptr != -1) {
+    if (ptr != -1 && bound_ok(m, (uint32_t)ptr < m.c.num_sdf_blocks, SF_BOUND_PTR)) {
       h0 = make_int4(p.x, p.y, p.z, ptr * 512);
       off_out = offset;
       return;
@@ -803,7 +803,7 @@ __global__ void k_unify_list(DevMap m, int *list, unsigned *count, const int *ru
   const unsigned n = min(*m.no_visible, m.c.num_entries);
   for (unsigned base = blockIdx.x * blockDim.x; base < n; base += grid_stride()) {
     const unsigned e = base + threadIdx.x;
-    const bool occ = e < n && __ldcg(&m.entries[e].ptr) >= 0;
+    const bool occ = e < n && checked_ptr(m, __ldcg(&m.entries[e].ptr)) >= 0;
     const unsigned slot = warp_append(count, occ);
     if (occ) list[slot] = (int)e;
   }
@@ -854,7 +854,8 @@ __global__ void __launch_bounds__(kIntThreads, SF_INT_MINB) k_integrate(DevMap m
   const float voxel = m.c.voxel_size;
   const int pal0 = 33554431, pal1 = 32767, pal2 = 2097151;  // 2^25-1, 2^15-1, 2^21-1 (FuseMap.cu:18)
   for (unsigned b = blockIdx.x; b < nvis; b += gridDim.x) {
-    const int4 h = __ldcg((const int4 *)(m.visible + b));
+    int4 h = __ldcg((const int4 *)(m.visible + b));
+    h.w = checked_ptr(m, h.w);
     if (h.w == -1) continue;
     for (int li = threadIdx.x; li < 512; li += kIntThreads) {
       const int lx = li & 7, ly = (li >> 3) & 7, lz = li >> 6;

@@ -159,7 +159,8 @@ __global__ void __launch_bounds__(kMeshThreads) k_mesh(DevMap m, float3 *vert, f
   const int cx[8] = {0, 1, 1, 0, 0, 1, 1, 0}, cy[8] = {0, 0, 1, 1, 0, 0, 1, 1}, cz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
   for (unsigned b = blockIdx.x; b < nblocks; b += gridDim.x) {
     if (__ldcg(count) >= max_tri) return;
-    const int4 h = entry_head(m.entries + __ldcg(m.alloc_list + b));
+    int4 h = entry_head(m.entries + __ldcg(m.alloc_list + b));
+    h.w = checked_ptr(m, h.w);
     if (h.w < 0) continue;
     MeshLookup look(m, mk_i3(h.x, h.y, h.z), h.w);
     for (int z = 0; z < 8; ++z) {

@@ -344,9 +344,7 @@ __device__ __forceinline__ RayCtx ray_ctx(const DevMap &m, const FuseScratch &f)
   r.voxels = m.voxels;
   r.cells = f.win_cells;
   for (int k = 0; k < 6; ++k) r.win[k] = f.win[k];
-  r.entries = m.entries;
-  r.num_buckets = m.c.num_buckets;
-  r.num_excess = m.c.num_excess;
+  ray_ctx_map(r, m);
   return r;
 }
 
@@ -476,9 +474,7 @@ __global__ void __launch_bounds__(128) k_raycast_adjoint(DevMap m, FuseScratch f
       r.voxels = m.voxels;
       r.cells = f.win_cells;
       for (int k = 0; k < 6; ++k) r.win[k] = f.win[k];
-      r.entries = m.entries;
-      r.num_buckets = m.c.num_buckets;
-      r.num_excess = m.c.num_excess;
+      ray_ctx_map(r, m);
       MarchState ms;
       march_ray(r, c, m.c.voxel_size_inv, x, y, zx, zy, ms);
       if (!ms.behind && ms.sdf <= 0.0f) {

@@ -38,9 +38,7 @@ __global__ void __launch_bounds__(kRelocThreads) k_reloc_score(DevMap m, sf_imag
   r.voxels = m.voxels;
   r.cells = nullptr;
   for (int i = 0; i < 6; ++i) r.win[i] = 0;  // empty window: every lookup hashes
-  r.entries = m.entries;
-  r.num_buckets = m.c.num_buckets;
-  r.num_excess = m.c.num_excess;
+  ray_ctx_map(r, m);
   const float vsi = m.c.voxel_size_inv;
   const int sc = (vmap.cols + stride - 1) / stride, sr = (vmap.rows + stride - 1) / stride;
   const int N = sc * sr;

@@ -97,8 +97,38 @@ struct DevMap {
   // index of allocated entries (ptr >= 0), in allocation order
   int *alloc_list;          // [num_entries]
   int *alloc_count;         // [1]
+  uint32_t *status;         // [1] SF_BOUND_* bits of the bounds-checked build (else stays 0)
   MapConst c;
 };
+
+// ------------------------------------------------- bounds-checked build
+// Built with -DSF_BOUNDS_CHECK (the debug library, build.py's
+// debug_bounds), every hash-chain link and every voxel index taken from a
+// hash entry or the block window is checked before use: an index outside
+// its array, or a block pointer that is not a multiple of 512, records its
+// SF_BOUND_* bit in the map's status word and the access is skipped (the
+// lookup finds no block).  This stands in for a memory checker against
+// corrupted maps and the reference's allocation races
+// (Mapping/DeviceMap.cu:23-69).  The release build compiles the checks out.
+enum : uint32_t {
+  SF_BOUND_CHAIN = 1u << 0,   // an excess-chain link beyond the table
+  SF_BOUND_PTR = 1u << 1,     // a block pointer outside the voxel array or not block-aligned
+  SF_BOUND_VISIBLE = 1u << 2, // a visible-list index beyond the table
+};
+#ifdef SF_BOUNDS_CHECK
+__device__ __forceinline__ bool bound_ok(const DevMap &m, bool ok, uint32_t bit) {
+  if (!ok) atomicOr(m.status, bit);
+  return ok;
+}
+#else
+__device__ __forceinline__ bool bound_ok(const DevMap &, bool, uint32_t) { return true; }
+#endif
+// A block pointer read from the table or the window: -1 stays -1; a
+// pointer the checked build rejects reads as -1 (no block).
+__device__ __forceinline__ int checked_ptr(const DevMap &m, int ptr) {
+  if (ptr < 0) return ptr;
+  return bound_ok(m, (ptr & 511) == 0 && (uint32_t)ptr < m.c.num_sdf_blocks * 512u, SF_BOUND_PTR) ? ptr : -1;
+}
 
 // DeviceMap::Hash (Mapping/DeviceMap.cu:3-10).  NumBuckets is unsigned, so
 // the signed product-xor is taken modulo NumBuckets as an unsigned value.
@@ -134,12 +164,13 @@ __device__ __forceinline__ int entry_offset(const sf_hash_entry *e) { return __l
 // The lookup given the head and offset of p's bucket entry, already loaded
 // (so that several lookups can have their first loads in flight at once).
 __device__ __forceinline__ int find_block_from(const DevMap &m, i3 p, int4 h, int off) {
-  if (h.w != -1 && h.x == p.x && h.y == p.y && h.z == p.z) return h.w;
+  if (h.w != -1 && h.x == p.x && h.y == p.y && h.z == p.z) return checked_ptr(m, h.w);
   int guard = 0;
   while (off > 0) {
+    if (!bound_ok(m, (uint32_t)off <= m.c.num_excess, SF_BOUND_CHAIN)) break;
     const sf_hash_entry *e = m.entries + (m.c.num_buckets + (uint32_t)off - 1u);
     h = entry_head(e);
-    if (h.x == p.x && h.y == p.y && h.z == p.z && h.w != -1) return h.w;
+    if (h.x == p.x && h.y == p.y && h.z == p.z && h.w != -1) return checked_ptr(m, h.w);
     off = entry_offset(e);
     if (++guard > (int)m.c.num_excess) break;  // corrupted chain: stop
   }

@@ -21,10 +21,38 @@ struct RayCtx {
   int win[6];
   const sf_hash_entry *entries;
   uint32_t num_buckets, num_excess;
+#ifdef SF_BOUNDS_CHECK
+  uint32_t *status;  // the map's bounds status word
+  uint32_t num_sdf_blocks;
+#endif
 };
+
+// The map fields a RayCtx carries besides the arrays.
+__device__ __forceinline__ void ray_ctx_map(RayCtx &r, const DevMap &m) {
+  r.entries = m.entries;
+  r.num_buckets = m.c.num_buckets;
+  r.num_excess = m.c.num_excess;
+#ifdef SF_BOUNDS_CHECK
+  r.status = m.status;
+  r.num_sdf_blocks = m.c.num_sdf_blocks;
+#endif
+}
 
 // Hash-table lookup (DeviceMap::FindEntry) for a block outside the window;
 // rare, so kept out of line to keep the inlined sample code small.
+#ifdef SF_BOUNDS_CHECK
+__device__ __noinline__ int block_ptr_hash(const RayCtx r, int bx, int by, int bz) {
+  DevMap m;
+  m.entries = const_cast<sf_hash_entry *>(r.entries);
+  m.c.num_buckets = r.num_buckets;
+  m.c.num_excess = r.num_excess;
+  m.c.num_sdf_blocks = r.num_sdf_blocks;
+  m.status = r.status;
+  i3 p;
+  p.x = bx; p.y = by; p.z = bz;
+  return find_block(m, p);
+}
+#else
 __device__ __noinline__ int block_ptr_hash(const sf_hash_entry *entries, uint32_t num_buckets,
                                            uint32_t num_excess, int bx, int by, int bz) {
   DevMap m;
@@ -35,13 +63,24 @@ __device__ __noinline__ int block_ptr_hash(const sf_hash_entry *entries, uint32_
   p.x = bx; p.y = by; p.z = bz;
   return find_block(m, p);
 }
+#endif
 
 // Voxel index of block (bx, by, bz), or -1.
 __device__ __forceinline__ int block_ptr(const RayCtx &r, int bx, int by, int bz) {
   const unsigned x = (unsigned)(bx - r.win[0]), y = (unsigned)(by - r.win[1]), z = (unsigned)(bz - r.win[2]);
+#ifdef SF_BOUNDS_CHECK
+  if (x < (unsigned)r.win[3] && y < (unsigned)r.win[4] && z < (unsigned)r.win[5]) {
+    const int v = __ldg(r.cells + (int)((z * (unsigned)r.win[4] + y) * (unsigned)r.win[3] + x));
+    if (v < 0 || ((v & 511) == 0 && (uint32_t)v < r.num_sdf_blocks * 512u)) return v;
+    atomicOr(r.status, SF_BOUND_PTR);
+    return -1;
+  }
+  return block_ptr_hash(r, bx, by, bz);
+#else
   if (x < (unsigned)r.win[3] && y < (unsigned)r.win[4] && z < (unsigned)r.win[5])
     return __ldg(r.cells + (int)((z * (unsigned)r.win[4] + y) * (unsigned)r.win[3] + x));
   return block_ptr_hash(r.entries, r.num_buckets, r.num_excess, bx, by, bz);
+#endif
 }
 
 struct VoxelRead {

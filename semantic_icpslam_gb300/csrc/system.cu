@@ -22,7 +22,18 @@
 #include <new>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "sf_kernels.cuh"
+
+namespace {
+// NVTX range over a host scope (a profiler shows which stage issued which
+// launches; without a tool attached the calls return at once).
+struct Range {
+  explicit Range(const char *name) { nvtxRangePushA(name); }
+  ~Range() { nvtxRangePop(); }
+};
+}  // namespace
 
 namespace sf {
 cudaStream_t ctx_stream(sf_context *c);
@@ -362,6 +373,7 @@ void rgb_levels(sf_system *s, RgbLevelArgs *rg) {
 // that the two run side by side (joined before this returns).
 void enqueue_depth_pyramid(sf_system *s, cudaStream_t st);
 void enqueue_pyramid(sf_system *s, cudaStream_t st) {
+  Range nvtx_range("sf pyramid");
   if (!s->cfg.rgb_term) {
     enqueue_depth_pyramid(s, st);
     return;
@@ -486,6 +498,7 @@ int fuse_and_raytrace(sf_system *s, const Cam *cam, const int *run, int num_dete
 // (vmap[0].z, Mapping.cc:99-123).
 int enqueue_mapping(sf_system *s, const Cam *cam, const int *run, int num_detection, bool plain,
                     cudaStream_t st) {
+  Range nvtx_range("sf mapping");
   const int C = s->cfg.cols, R = s->cfg.rows;
   DevMap &m = map_dev(s->map);
   FuseScratch &f = map_scratch(s->map);
@@ -525,6 +538,7 @@ int enqueue_mapping(sf_system *s, const Cam *cam, const int *run, int num_detect
 
 // Device-driven frame (eager and graph forms).
 cudaError_t enqueue_device_frame(sf_system *s, int num_detection, cudaStream_t st) {
+  Range nvtx_range("sf frame (device-driven)");
   IcpWorkspace &w = ctx_icp(s->ctx);
   mark(s, st, 0);
   enqueue_pyramid(s, st);
@@ -555,6 +569,7 @@ cudaError_t enqueue_device_frame(sf_system *s, int num_detection, cudaStream_t s
 
 // Host-driven frame (plain per-launch form).
 int run_plain_frame(sf_system *s, int num_detection) {
+  Range nvtx_range("sf frame (plain)");
   cudaStream_t st = ctx_stream(s->ctx);
   IcpWorkspace &w = ctx_icp(s->ctx);
   enqueue_pyramid(s, st);
@@ -670,6 +685,7 @@ void set_cam(Cam &c, const Cam &tmpl, const double *P) {
 // iterations and threshold refines it.  Accepted, the frame is tracked and
 // mapped like any other.
 int run_reloc_frame(sf_system *s, int num_detection) {
+  Range nvtx_range("sf frame (relocalise)");
   cudaStream_t st = ctx_stream(s->ctx);
   IcpWorkspace &w = ctx_icp(s->ctx);
   const int C = s->cfg.cols, R = s->cfg.rows, L = s->L;
@@ -827,6 +843,7 @@ int run_frame(sf_system *s, int num_detection) {
     s->graph_early = true;  // every captured frame writes h_stats and h_ready
     s->num_detection_captured = num_detection;
   }
+  Range nvtx_range("sf frame (graph replay)");
   if (cudaGraphLaunch(s->gexec, st) != cudaSuccess) return SF_ERR_CUDA;
   ++s->graph_seq;  // this replay's k_sys_stats writes this number to h_ready
   note_launch(s->graph_kernels);
@@ -969,6 +986,7 @@ int sf_system_set_mapping(sf_system *s, int enabled) {
 }
 
 int sf_system_autotune(sf_system *s, int reps, sf_autotune_report *report) {
+  Range nvtx_range("sf autotune");
   if (!s || reps < 1 || reps > 1000) return SF_ERR_INVALID;
   if (s->frames < 1) return SF_ERR_INVALID;  // needs one grabbed frame: the stages' inputs
   cudaStream_t st = ctx_stream(s->ctx);
