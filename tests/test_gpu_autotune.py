@@ -10,7 +10,7 @@ configuration as JSON."""
 import numpy as np
 import pytest
 
-from tests.helpers import C1, MAP_C1, map_to_host, sequence
+from tests.helpers import C1, MAP_C1, map_to_host, sequence, voxels_by_pos
 
 pytestmark = pytest.mark.gpu
 
@@ -68,9 +68,11 @@ def _compare(sf, ctx, seq, a, b):
     assert t.raycast == rep.chosen and t.integrate_ctas_per_sm == rep.integrate_ctas[rep.integrate_chosen]
     for x, y in zip(_model(ctx, a), _model(ctx, b)):  # the timing runs left the model maps as they were
         np.testing.assert_array_equal(x, y)
-    ea, va, _ = map_to_host(ctx, a.map())  # and the voxels the integration runs touched
-    eb, vb, _ = map_to_host(ctx, b.map())
-    assert np.array_equal(va.view(np.uint8), vb.view(np.uint8))
+    ea, va, _ = map_to_host(ctx, a.map())  # and the voxels the integration runs touched (per block
+    eb, vb, _ = map_to_host(ctx, b.map())  # position: which heap block a block takes varies between runs)
+    ka, xa = voxels_by_pos(ea, va)
+    kb, xb = voxels_by_pos(eb, vb)
+    assert ka == kb and np.array_equal(xa.view(np.uint8), xb.view(np.uint8))
     # the least likely shapes: the results still do not change
     far = sf._lib.FrameTune(5, 2)
     sf.call("sf_system_set_tune", b.h, C.byref(far))

@@ -55,7 +55,7 @@ if %(corrupt)r:
     m = s.map()
     a = m.arrays()
     ent = ctx.download(a.hash_entries, ENTRY_DTYPE, m.num_entries)
-    vis = ctx.download(a.visible_entries, ENTRY_DTYPE, m.num_entries)[:stats[-1][3]]
+    vis = ctx.download(a.visible_entries, ENTRY_DTYPE, m.num_entries)[:m.counters(ctx)[2]]
     pos = vis[len(vis) // 2]
     k = int(np.flatnonzero((ent["x"] == pos["x"]) & (ent["y"] == pos["y"]) & (ent["z"] == pos["z"]) &
                            (ent["ptr"] >= 0))[0])
