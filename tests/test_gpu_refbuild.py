@@ -9,7 +9,7 @@ Two builds of the reference take part:
   * as the reference builds it (nvcc's default FMA contraction): the
     integration's world-to-camera products fuse into FMAs, so TSDF values
     differ in their last bits and a few voxels at pixel borders project to
-    the neighbouring pixel;
+    the neighbouring pixel (their TSDF then comes from another depth);
   * with contraction off (-fmad=false), where every float operation rounds
     once, as the reference's source states it and as this library computes
     it: the voxels of every block both allocated are equal bit for bit.
@@ -137,5 +137,5 @@ def test_first_frame_matches_reference_cuda_build(frames, build):
         dt = np.abs(sdf_g[both] - sdf_r[both])
         print("FMA-contracted reference: %d common blocks, weights equal on %.6f of voxels, TSDF max diff %.3g, "
               "bit-equal TSDF on %.4f" % (len(common), same_w, dt.max(), (dt == 0).mean()))
-        assert same_w > 0.999
-        assert dt.max() < 1e-5
+        assert same_w > 0.9999
+        assert (dt <= 1e-5).mean() > 0.9999  # all but the voxels that took a neighbouring pixel
