@@ -138,4 +138,6 @@ def test_first_frame_matches_reference_cuda_build(frames, build):
         print("FMA-contracted reference: %d common blocks, weights equal on %.6f of voxels, TSDF max diff %.3g, "
               "bit-equal TSDF on %.4f" % (len(common), same_w, dt.max(), (dt == 0).mean()))
         assert same_w > 0.9999
-        assert (dt <= 1e-5).mean() > 0.9999  # all but the voxels that took a neighbouring pixel
+        # fused products change a voxel's camera depth by a few ulps of the
+        # world coordinates (~1e-6 m, ~3e-5 of the 4 cm truncation)
+        assert (dt <= 1e-4).mean() > 0.9999  # all but the voxels that took a neighbouring pixel
