@@ -479,6 +479,9 @@ def error_pass(sf, ctx, frames, steps, warmup):
     return {"frames": "timed frames %d..%d (pose, J^T J: %d compared); TSDF over frames 0..%d"
                       % (warmup, warmup + steps - 1, n_t, warmup + steps - 1),
             "pose_max": max(pose_err) if pose_err else None, "pose_mean": float(np.mean(pose_err)) if pose_err else None,
+            "pose_median": float(np.median(pose_err)) if pose_err else None,
+            "pose_frac_le_1e-5": float(np.mean(np.array(pose_err) <= 1e-5)) if pose_err else None,
+            "fp32_oracle_frac_le_1e-5": float(np.mean(np.array(ref32) <= 1e-5)) if ref32 else None,
             "pose_worst": worst,
             "pose_max_same_iterations": max(same_it) if same_it else None,
             "frames_same_iterations": len(same_it),
