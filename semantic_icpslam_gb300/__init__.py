@@ -57,6 +57,9 @@ class Context:
         self._systems = weakref.WeakSet()  # closed before the context
 
     def close(self):
+        if getattr(self, "log", None) is not None:
+            self.log.close()
+            self.log = None
         if getattr(self, "h", None):
             for s in list(getattr(self, "_systems", ())):
                 s.close()
@@ -139,9 +142,15 @@ class Map:
 class System:
     """sf_system: the whole per-frame loop (System::GrabImage)."""
 
-    def __init__(self, ctx, cfg, init_pose=None):
+    def __init__(self, ctx, cfg, init_pose=None, log=None):
+        """log: a metrics.FrameLog, or a path for one (one JSON line per
+        grabbed frame)."""
         self.ctx = ctx
         self.cfg = cfg
+        if isinstance(log, str):
+            from .metrics import FrameLog
+            log = FrameLog(log, cfg.map.num_sdf_blocks)
+        self.log = log
         h = C.c_void_p()
         P = np.eye(4) if init_pose is None else np.asarray(init_pose, np.float64)
         P = np.ascontiguousarray(P, np.float64)
@@ -150,6 +159,9 @@ class System:
         ctx._systems.add(self)
 
     def close(self):
+        if getattr(self, "log", None) is not None:
+            self.log.close()
+            self.log = None
         if getattr(self, "h", None):
             load().sf_system_destroy(self.h)
             self.h = None
@@ -163,6 +175,8 @@ class System:
         st = FrameStats()
         call("sf_system_grab", self.h, d.ctypes.data, c.ctypes.data, None if m is None else m.ctypes.data,
              num_detection, C.byref(st))
+        if self.log is not None:
+            self.log.write(st)
         return st
 
     def set_reloc_candidates(self, poses):

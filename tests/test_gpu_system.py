@@ -181,3 +181,22 @@ def test_graph_grab_after_grab_device(lib):
         else:
             g.grab_device(dev[i][0].data_ptr(), dev[i][1].data_ptr(), None, 0)
     g.close()
+
+
+def test_frame_log_lines_match_stats(lib, tmp_path):
+    """System(..., log=path) writes one JSON line per grabbed frame, equal to
+    the frame's stats."""
+    import json
+    sf, ctx = lib
+    seq = sequence(C1["cols"], C1["rows"], C1["K"], 4, trajectory=0)
+    cfg = sf.system_config(cols=C1["cols"], rows=C1["rows"], K=C1["K"], use_graph=1, **MAP_C1)
+    path = str(tmp_path / "frames.jsonl")
+    s = sf.System(ctx, cfg, init_pose=seq[0][3], log=path)
+    stats = [s.grab(d, rgb) for d, rgb, _, _ in seq]
+    s.close()
+    recs = [json.loads(x) for x in open(path)]
+    assert len(recs) == 4
+    for i, (r, st) in enumerate(zip(recs, stats)):
+        assert r["frame"] == i and r["tracked"] == st.tracked and r["iterations"] == st.iterations
+        assert r["visible_blocks"] == st.visible and r["t"] == [st.pose[3], st.pose[7], st.pose[11]]
+        assert 0 < r["visible_percent"] <= 1.0
