@@ -758,6 +758,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-errors", action="store_true", help="skip the accuracy pass against the FP64 oracle")
+    ap.add_argument("--no-modes", action="store_true",
+                    help="skip the RGB-D, semantic, mesh, ValidatePose and reloc-score measurements")
     ap.add_argument("--map-blocks", type=int, default=19,
                     help="log2 of the voxel-block heap (2^19 blocks = 4 GB of voxels)")
     ap.add_argument("--config", default="c2", choices=["c2", "c3"],
@@ -865,7 +867,7 @@ def main():
                   "h2d_bytes_per_step": COLS * ROWS * (2 + 3),
                   "d2h_bytes_per_step": C.sizeof(sf._lib.FrameStats),
                   "tracked_frames": int(tracked)}
-    if args.config == "c2":
+    if args.config == "c2" and not args.no_modes:
         # the reference's default tracking mode: ComputeSE3(icpOnly = false)
         r = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 1, barrier, rgb=1, flush=flush)
         re2e, rtracked = time_e2e(sf, ctx, frames, args.steps, args.warmup, 1, rgb=1, flush=flush)
@@ -891,7 +893,7 @@ def main():
         out["mesh"] = time_mesh(sf, ctx, frames, args.steps + args.warmup)
     if not args.no_errors:
         out["errors"] = error_pass(sf, ctx, frames, args.steps, args.warmup)
-    if args.config == "c2":
+    if args.config == "c2" and not args.no_modes:
         out["validate_pose"] = time_validate(sf, ctx, frames)
         out["reloc_score"] = time_reloc(sf, ctx, frames)
     if rank == 0 and not args.no_cpu:
