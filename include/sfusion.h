@@ -150,11 +150,7 @@ int sf_map_arrays(const sf_map *map, sf_device_map *out);
 int sf_map_bounds_status(sf_context *ctx, const sf_map *map, uint32_t *out);
 int sf_build_flags(uint32_t *out);
 /* Rebuilds the allocated-entry index after the hash table was written
- * outside this library (e.g. a map loaded from disk), and drops the
- * library's per-block summaries of the voxels (which blocks are all
- * observed and far in front of a surface, kept by the integration to let
- * the raycast skip their voxels).  A caller that writes voxels itself calls
- * it before the next raycast. */
+ * outside this library (e.g. a map loaded from disk). */
 int sf_map_rebuild_index(sf_context *ctx, sf_map *map);
 /* Host copies of the map's counters: heapCounter, entryPtr, visible count,
  * allocated (ptr >= 0) entry count. */

@@ -90,14 +90,6 @@ class TorchMap:
         """Integration weights (uint8 byte 4 of each voxel) as int32."""
         return self.voxels.view(torch.uint8).view(-1, 16)[:, 4].to(torch.int32)
 
-    def voxels_changed(self, ctx):
-        """After voxel values were written through the tensors (sdf()):
-        sf_map_rebuild_index drops the library's per-block summaries of
-        them (and rebuilds the allocated-entry index)."""
-        torch.cuda.synchronize()
-        call("sf_map_rebuild_index", ctx.h, self.h)
-        ctx.sync()
-
     def close(self):
         if self.h:
             call("sf_map_destroy", self.h)
@@ -225,5 +217,4 @@ def refine_tsdf(renderer, tmap, keyframes, steps=50, lr=0.01, betas=(0.9, 0.999)
         step = lr * (m / (1 - b1 ** it)) / ((v / (1 - b2 ** it)).sqrt() + eps)
         new = torch.where(observed, (sdf - step).clamp(-1.0, 1.0), sdf)
         sdf.copy_(new)
-        tmap.voxels_changed(renderer.ctx)
     return losses

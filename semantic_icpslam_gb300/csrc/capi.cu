@@ -212,8 +212,6 @@ static int map_alloc_index(sf_map *m) {
   SF_CHECK(cudaMemset(m->d.alloc_count, 0, sizeof(int)));
   SF_CHECK(cudaMalloc(&m->d.status, sizeof(uint32_t)));
   SF_CHECK(cudaMemset(m->d.status, 0, sizeof(uint32_t)));
-  SF_CHECK(cudaMalloc(&m->d.blk_class, m->d.c.num_sdf_blocks));
-  SF_CHECK(cudaMemset(m->d.blk_class, 0, m->d.c.num_sdf_blocks));
   return SF_OK;
 }
 
@@ -301,7 +299,6 @@ int sf_map_destroy(sf_map *m) {
   cudaFree(m->d.alloc_list);
   cudaFree(m->d.alloc_count);
   cudaFree(m->d.status);
-  cudaFree(m->d.blk_class);
   fuse_scratch_free(m->scratch);
   delete m;
   return SF_OK;
@@ -864,7 +861,7 @@ int sf_FuseMapColor(sf_context *ctx, sf_map *m, sf_image depth, sf_image color, 
   SF_CHECK(cudaMemcpyAsync(host_data, m->d.no_visible, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
   SF_CHECK(cudaStreamSynchronize(ctx->stream));
   if (host_data[0] == 0) return SF_OK;  // "no visible blocks found" early return
-  launch_integrate(m->d, m->scratch, depth, color, num_detection > 0 ? &nmap : nullptr,
+  launch_integrate(m->d, depth, color, num_detection > 0 ? &nmap : nullptr,
                    num_detection > 0 ? &mask : nullptr, num_detection, ctx->cam, true,
                    num_detection > 0, nullptr, ctx->stream);
   if (num_detection > 0) {  // FuseMap.cu:1141-1160
@@ -889,7 +886,7 @@ int sf_AnalyzeMapSemantics(sf_context *ctx, sf_map *m, sf_image depth, sf_image 
   if (st) return st;
   if ((st = ensure_scratch(m, depth.cols * depth.rows))) return st;
   launch_visibility(m->d, m->scratch, ctx->cam, nullptr, nullptr, nullptr, ctx->flags, ctx->stream);
-  launch_integrate(m->d, m->scratch, depth, color, &nmap, num_detection > 0 ? &mask : nullptr, num_detection,
+  launch_integrate(m->d, depth, color, &nmap, num_detection > 0 ? &mask : nullptr, num_detection,
                    ctx->cam, false, true, nullptr, ctx->stream);
   if ((st = fuse_scratch_unify(m->scratch, m->d.c))) return st;
   launch_unify_neighbor(m->d, m->scratch, nullptr, ctx->stream);

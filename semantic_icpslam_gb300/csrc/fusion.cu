@@ -93,10 +93,7 @@ __global__ void k_reset_voxels(DevMap m) {
     v.z = 0u;
     v.w &= 0xff000000u;
     *p = v;
-    if (i < m.c.num_sdf_blocks) {
-      m.heap[i] = (int)m.c.num_sdf_blocks - (int)i - 1;
-      m.blk_class[i] = 0;
-    }
+    if (i < m.c.num_sdf_blocks) m.heap[i] = (int)m.c.num_sdf_blocks - (int)i - 1;
   }
   if (grid_tid() == 0) {
     *m.heap_counter = (int)m.c.num_sdf_blocks - 1;
@@ -300,7 +297,6 @@ __device__ __forceinline__ void create_entry(DevMap &m, i3 p, int offset, int4 &
   if (old >= 0) {
     int ptr = m.heap[old];
     if (ptr != -1 && bound_ok(m, (uint32_t)ptr < m.c.num_sdf_blocks, SF_BOUND_PTR)) {
-      m.blk_class[ptr] = 0;  // a new block: its voxels are not (yet) far-positive
       h0 = make_int4(p.x, p.y, p.z, ptr * 512);
       off_out = offset;
       return;
@@ -432,10 +428,7 @@ __global__ void k_visibility(DevMap m, FuseScratch f, const Cam *cam, sf_image z
       vis = h0.w != -1 && block_visible(c, m.c.block_width, pos);
       // every allocated block inside the frustum box goes into the window
       const int cell = window_cell(win, pos);
-      if (cell >= 0) {
-        const int wp = checked_ptr(m, h0.w);
-        f.win_cells[cell] = wp < 0 ? wp : (wp | (int)m.blk_class[wp >> 9]);
-      }
+      if (cell >= 0) f.win_cells[cell] = h0.w;
     }
     unsigned slot = warp_append(m.no_visible, vis);
     if (vis) {
@@ -849,12 +842,6 @@ constexpr int kIntThreads = 256;
 #ifndef SF_INT_MINB
 #define SF_INT_MINB 8
 #endif
-//
-// With do_int, the kernel also keeps the blocks' far-positive summaries
-// (DevMap::blk_class): a block whose 512 voxels all have weight > 0 and
-// sdf > 0.1 after the update is marked kBlockFar, else unmarked (the
-// window cells take the marks in k_window_classes).  Voxels the update
-// skips are read (8 bytes) while the block is still a candidate.
 __global__ void __launch_bounds__(kIntThreads, SF_INT_MINB) k_integrate(DevMap m, sf_image depth, sf_image rgb,
                                                            sf_image nmap, sf_image mask,
                                                            int num_detection, const Cam *cam,
@@ -869,8 +856,7 @@ __global__ void __launch_bounds__(kIntThreads, SF_INT_MINB) k_integrate(DevMap m
   for (unsigned b = blockIdx.x; b < nvis; b += gridDim.x) {
     int4 h = __ldcg((const int4 *)(m.visible + b));
     h.w = checked_ptr(m, h.w);
-    if (h.w == -1) continue;  // uniform over the CTA
-    bool far = do_int != 0;
+    if (h.w == -1) continue;
     for (int li = threadIdx.x; li < 512; li += kIntThreads) {
       const int lx = li & 7, ly = (li >> 3) & 7, lz = li >> 6;
       f3 w3 = mk3((float)(h.x * 8 + lx) * voxel, (float)(h.y * 8 + ly) * voxel,
@@ -878,23 +864,11 @@ __global__ void __launch_bounds__(kIntThreads, SF_INT_MINB) k_integrate(DevMap m
       f3 pos = mul(c.Rinv, w3 - c.t);
       int u = (int)(c.fx * pos.x / pos.z + c.cx);
       int v = (int)(c.fy * pos.y / pos.z + c.cy);
-      bool pass = !(u < 0 || v < 0 || u >= c.cols || v >= c.rows);
-      float dp = 0.f, sdf = 0.f;
-      if (pass) {
-        dp = __ldg(row_ptr<const float>(depth, v) + u);
-        pass = !(isnan(dp) || dp > c.dmax || dp < c.dmin);
-      }
-      if (pass) {
-        sdf = dp - pos.z;
-        pass = sdf >= -thresh;
-      }
-      if (!pass) {
-        if (far) {  // the voxel keeps its value
-          const uint2 raw = __ldcg((const uint2 *)(m.voxels + h.w + li));
-          far = (raw.y & 0xffu) != 0u && __uint_as_float(raw.x) > 0.1f;
-        }
-        continue;
-      }
+      if (u < 0 || v < 0 || u >= c.cols || v >= c.rows) continue;
+      float dp = __ldg(row_ptr<const float>(depth, v) + u);
+      if (isnan(dp) || dp > c.dmax || dp < c.dmin) continue;
+      float sdf = dp - pos.z;
+      if (!(sdf >= -thresh)) continue;
       const uint8_t *px = row_ptr<const uint8_t>(rgb, v) + 3 * u;
       uint4 *vp = (uint4 *)(m.voxels + h.w) + li;
       VoxelU vx;
@@ -927,48 +901,8 @@ __global__ void __launch_bounds__(kIntThreads, SF_INT_MINB) k_integrate(DevMap m
           dirty = true;
         }
       }
-      if (far) far = vx.v.weight != 0 && vx.v.sdf > 0.1f;
       if (dirty) *vp = vx.u;
     }
-    if (do_int) {
-      const bool all_far = __syncthreads_and(far);
-      if (threadIdx.x == 0) m.blk_class[h.w >> 9] = all_far ? (uint8_t)kBlockFar : (uint8_t)0;
-    }
-  }
-}
-
-// The visible blocks' window cells take their summaries (after the
-// integration, which changed them; the visibility pass filled the cells
-// with the summaries as they stood).
-__global__ void k_window_classes(DevMap m, FuseScratch f, const int *run_flag) {
-  if (run_flag && *run_flag == 0) return;
-  const unsigned nvis = min(*m.no_visible, m.c.num_entries);
-  int win[6];
-  for (int k = 0; k < 6; ++k) win[k] = __ldcg(f.win + k);
-  for (unsigned b = grid_tid(); b < nvis; b += grid_stride()) {
-    const int4 h = __ldcg((const int4 *)(m.visible + b));
-    const int wp = checked_ptr(m, h.w);
-    if (wp < 0) continue;
-    i3 bp; bp.x = h.x; bp.y = h.y; bp.z = h.z;
-    const int cell = window_cell(win, bp);
-    if (cell >= 0) f.win_cells[cell] = wp | (int)m.blk_class[wp >> 9];
-  }
-}
-
-// The far-positive summaries of the visible blocks recomputed from their
-// voxels (after the autotuner restored them).
-__global__ void k_reclass_visible(DevMap m, unsigned nvis) {
-  for (unsigned b = blockIdx.x; b < nvis; b += gridDim.x) {
-    int4 h = __ldcg((const int4 *)(m.visible + b));
-    h.w = checked_ptr(m, h.w);
-    if (h.w == -1) continue;
-    bool far = true;
-    for (int li = threadIdx.x; li < 512; li += blockDim.x) {
-      const uint2 raw = __ldcg((const uint2 *)(m.voxels + h.w + li));
-      far = far && (raw.y & 0xffu) != 0u && __uint_as_float(raw.x) > 0.1f;
-    }
-    const bool all_far = __syncthreads_and(far);
-    if (threadIdx.x == 0) m.blk_class[h.w >> 9] = all_far ? (uint8_t)kBlockFar : (uint8_t)0;
   }
 }
 
@@ -1028,7 +962,6 @@ void launch_map_reset(const DevMap &m, cudaStream_t s) {
 
 void launch_rebuild_index(const DevMap &m, cudaStream_t s) {
   cudaMemsetAsync(m.alloc_count, 0, sizeof(int), s);
-  cudaMemsetAsync(m.blk_class, 0, m.c.num_sdf_blocks, s);  // voxels written from outside: no summary holds
   k_rebuild_index<<<sm_count() * 8, 256, 0, s>>>(m); note_launch();
 }
 
@@ -1085,7 +1018,7 @@ int fuse_scratch_unify(FuseScratch &f, const MapConst &c) {
   return cudaDeviceSynchronize() == cudaSuccess ? SF_OK : SF_ERR_CUDA;
 }
 
-void launch_integrate(const DevMap &m, const FuseScratch &f, const sf_image &depth, const sf_image &rgb,
+void launch_integrate(const DevMap &m, const sf_image &depth, const sf_image &rgb,
                       const sf_image *nmap, const sf_image *mask, int num_detection, const Cam *c,
                       bool integrate, bool semantics, const int *run_flag, cudaStream_t s, int ctas_per_sm) {
   sf_image nm = nmap ? *nmap : sf_image{};
@@ -1094,14 +1027,6 @@ void launch_integrate(const DevMap &m, const FuseScratch &f, const sf_image &dep
   k_integrate<<<sm_count() * ctas_per_sm, kIntThreads, 0, s>>>(m, depth, rgb, nm, mk, num_detection, c,
                                                                integrate ? 1 : 0, sem ? 1 : 0, run_flag);
   note_launch();
-  if (integrate) {
-    k_window_classes<<<sm_count() * 2, 256, 0, s>>>(m, f, run_flag); note_launch();
-  }
-}
-
-void launch_reclass_visible(const DevMap &m, const FuseScratch &f, unsigned nvis, cudaStream_t s) {
-  k_reclass_visible<<<sm_count() * 8, 256, 0, s>>>(m, nvis); note_launch();
-  k_window_classes<<<sm_count() * 2, 256, 0, s>>>(m, f, nullptr); note_launch();
 }
 
 // The voxels of the visible blocks saved to / restored from scratch (the

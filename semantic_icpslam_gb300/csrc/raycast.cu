@@ -269,7 +269,7 @@ __device__ __forceinline__ void march_ray(const RayCtx &r, const Cam &c, float v
   float s_sample = 0.f;
   f3 sample = block_s;
   BlockCache cache;
-  cache.bx = 0x7fffffff; cache.by = 0; cache.bz = 0; cache.cell = -1;
+  cache.bx = 0x7fffffff; cache.by = 0; cache.bz = 0; cache.ptr = -1;
   while (!done && dist_s < dist_e) {
     f3 pos[kSpec];
     float ds[kSpec];
@@ -606,8 +606,7 @@ __global__ void k_window_build_fill(DevMap m, FuseScratch f) {
     const int4 h = entry_head(m.entries + m.alloc_list[k]);
     i3 pos; pos.x = h.x; pos.y = h.y; pos.z = h.z;
     const int cell = window_cell(win, pos);
-    const int wp = checked_ptr(m, h.w);
-    if (cell >= 0 && wp >= 0) f.win_cells[cell] = wp | (int)m.blk_class[wp >> 9];
+    if (cell >= 0 && h.w >= 0) f.win_cells[cell] = h.w;
   }
 }
 

@@ -98,20 +98,8 @@ struct DevMap {
   int *alloc_list;          // [num_entries]
   int *alloc_count;         // [1]
   uint32_t *status;         // [1] SF_BOUND_* bits of the bounds-checked build (else stays 0)
-  // Per heap block: kBlockFar when every voxel of the block had weight > 0
-  // and sdf > 0.1 after the integration that last touched it, else 0.
-  // Cleared on reset, on allocation and whenever the map is rebuilt from
-  // outside (sf_map_rebuild_index, map.bin reads).
-  uint8_t *blk_class;       // [num_sdf_blocks]
   MapConst c;
 };
-
-// A block-window cell holds the block's voxel index (a multiple of 512, or
-// -1) with kBlockFar in its low bits when the block is all far-positive:
-// the raycast's march then needs no voxel of that block (every sample there
-// is valid with sdf > 0.1, which only its sign enters).
-constexpr int kBlockFar = 1;
-__device__ __forceinline__ int cell_ptr(int cell) { return cell < 0 ? cell : (cell & ~511); }
 
 // ------------------------------------------------- bounds-checked build
 // Built with -DSF_BOUNDS_CHECK (the debug library, build.py's

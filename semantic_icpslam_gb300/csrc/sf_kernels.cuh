@@ -201,12 +201,9 @@ int fuse_scratch_unify(FuseScratch &f, const MapConst &c);
 void launch_unify_neighbor(const DevMap &m, const FuseScratch &f, const int *run_flag, cudaStream_t s);
 // ctas_per_sm: the launch's CTAs per SM (grid-stride over the visible
 // blocks; every shape computes the same voxels).
-void launch_integrate(const DevMap &m, const FuseScratch &f, const sf_image &depth, const sf_image &rgb,
+void launch_integrate(const DevMap &m, const sf_image &depth, const sf_image &rgb,
                       const sf_image *nmap, const sf_image *mask, int num_detection, const Cam *c,
                       bool integrate, bool semantics, const int *run_flag, cudaStream_t s, int ctas_per_sm = 8);
-// The far-positive summaries (DevMap::blk_class and the window cells) of
-// visible blocks [0, nvis) recomputed from their voxels.
-void launch_reclass_visible(const DevMap &m, const FuseScratch &f, unsigned nvis, cudaStream_t s);
 // Copies the voxels of visible blocks [0, nvis) to scratch (nvis x 8 KiB),
 // or back with restore.
 void launch_save_visible(const DevMap &m, void *scratch, unsigned nvis, bool restore, cudaStream_t s);

@@ -65,16 +65,13 @@ __device__ __noinline__ int block_ptr_hash(const sf_hash_entry *entries, uint32_
 }
 #endif
 
-// Block (bx, by, bz) as a window cell holds it: its voxel index with the
-// kBlockFar summary in the low bits, or -1; blocks outside the window come
-// from the hash table, without a summary.
-__device__ __forceinline__ int block_cell(const RayCtx &r, int bx, int by, int bz) {
+// Voxel index of block (bx, by, bz), or -1.
+__device__ __forceinline__ int block_ptr(const RayCtx &r, int bx, int by, int bz) {
   const unsigned x = (unsigned)(bx - r.win[0]), y = (unsigned)(by - r.win[1]), z = (unsigned)(bz - r.win[2]);
 #ifdef SF_BOUNDS_CHECK
   if (x < (unsigned)r.win[3] && y < (unsigned)r.win[4] && z < (unsigned)r.win[5]) {
     const int v = __ldg(r.cells + (int)((z * (unsigned)r.win[4] + y) * (unsigned)r.win[3] + x));
-    const int p = cell_ptr(v);
-    if (p < 0 || (uint32_t)p < r.num_sdf_blocks * 512u) return v;
+    if (v < 0 || ((v & 511) == 0 && (uint32_t)v < r.num_sdf_blocks * 512u)) return v;
     atomicOr(r.status, SF_BOUND_PTR);
     return -1;
   }
@@ -84,11 +81,6 @@ __device__ __forceinline__ int block_cell(const RayCtx &r, int bx, int by, int b
     return __ldg(r.cells + (int)((z * (unsigned)r.win[4] + y) * (unsigned)r.win[3] + x));
   return block_ptr_hash(r.entries, r.num_buckets, r.num_excess, bx, by, bz);
 #endif
-}
-
-// Voxel index of block (bx, by, bz), or -1.
-__device__ __forceinline__ int block_ptr(const RayCtx &r, int bx, int by, int bz) {
-  return cell_ptr(block_cell(r, bx, by, bz));
 }
 
 struct VoxelRead {
@@ -124,22 +116,18 @@ __device__ __forceinline__ VoxelRead read_voxel(const RayCtx &r, f3 pt) {
 // A ray's last looked-up block (DeviceMap::FindVoxel's per-ray entry cache,
 // DeviceMap.cu:116-133): consecutive samples mostly fall in one block, and
 // a hit skips the lookup, so the voxel read is the sample's only dependent
-// load.  The cache changes no value (block_cell is exact for every block).
+// load.  The cache changes no value (block_ptr is exact for every block).
 struct BlockCache {
-  int bx, by, bz, cell;
+  int bx, by, bz, ptr;
 };
 
 // The voxels at n consecutive sample points, their block lookups issued
 // together: a sample in the cached block or in the previous sample's block
-// reuses that cell.  The cache then holds the last sample's block.  A
-// sample in a block marked kBlockFar reads no voxel: every voxel there is
-// observed with sdf > 0.1, so it reads as valid with sdf 1 (the march then
-// takes the same decisions: a 1-voxel step, no interpolation, and a
-// positive previous value for the next sample's crossing tests).
+// reuses that pointer.  The cache then holds the last sample's block.
 template <int N>
 __device__ __forceinline__ void read_voxels(const RayCtx &r, const f3 *pt, VoxelRead *v, BlockCache &cache) {
   i3 p[N];
-  int cell[N];
+  int ptr[N];
 #pragma unroll
   for (int i = 0; i < N; ++i) {
     p[i] = floor3(pt[i]);
@@ -147,26 +135,18 @@ __device__ __forceinline__ void read_voxels(const RayCtx &r, const f3 *pt, Voxel
     const bool same_prev =
         i > 0 && bx == (p[i - 1].x >> 3) && by == (p[i - 1].y >> 3) && bz == (p[i - 1].z >> 3);
     if (same_prev)
-      cell[i] = cell[i > 0 ? i - 1 : 0];
+      ptr[i] = ptr[i > 0 ? i - 1 : 0];
     else if (bx == cache.bx && by == cache.by && bz == cache.bz)
-      cell[i] = cache.cell;
+      ptr[i] = cache.ptr;
     else
-      cell[i] = block_cell(r, bx, by, bz);
+      ptr[i] = block_ptr(r, bx, by, bz);
   }
 #pragma unroll
-  for (int i = 0; i < N; ++i) {
-    if (cell[i] >= 0 && (cell[i] & kBlockFar)) {
-      v[i].sdf = 1.0f;
-      v[i].weight = 1u;
-      v[i].found = true;
-    } else {
-      v[i] = voxel_in(r, cell_ptr(cell[i]), p[i].x, p[i].y, p[i].z);
-    }
-  }
+  for (int i = 0; i < N; ++i) v[i] = voxel_in(r, ptr[i], p[i].x, p[i].y, p[i].z);
   cache.bx = p[N - 1].x >> 3;
   cache.by = p[N - 1].y >> 3;
   cache.bz = p[N - 1].z >> 3;
-  cache.cell = cell[N - 1];
+  cache.ptr = ptr[N - 1];
 }
 
 // Rendering::readSdfInterped (RenderScene.cu:310-343).  The corners are

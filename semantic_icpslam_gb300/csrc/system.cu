@@ -472,7 +472,7 @@ int fuse_and_raytrace(sf_system *s, const Cam *cam, const int *run, int num_dete
     integrate = nvis > 0;
   }
   if (integrate) {
-    launch_integrate(m, f, depth, rgb, &nmap, &mask, num_detection, cam, true, num_detection > 0, run, st,
+    launch_integrate(m, depth, rgb, &nmap, &mask, num_detection, cam, true, num_detection > 0, run, st,
                      s->int_ctas);
     if (num_detection > 0) launch_unify_neighbor(m, f, run, st);  // FuseMap.cu:1141-1160
   }
@@ -524,7 +524,7 @@ int enqueue_mapping(sf_system *s, const Cam *cam, const int *run, int num_detect
       const sf_image rd = img(s->d_rdepth, C, R, 4), rgb = img(s->d_rgb, C, R, 3), mask = img(s->d_mask, C, R, 1);
       launch_vmap_depth(img(s->d_mv[0], C, R, 16), rd, run, st);
       launch_visibility(m, f, cam, nullptr, nullptr, run, flags, st);
-      launch_integrate(m, f, rd, rgb, &mn0, &mask, num_detection, cam, false, true, run, st, s->int_ctas);
+      launch_integrate(m, rd, rgb, &mn0, &mask, num_detection, cam, false, true, run, st, s->int_ctas);
       launch_unify_neighbor(m, f, run, st);
     }
   }
@@ -1050,7 +1050,7 @@ int sf_system_autotune(sf_system *s, int reps, sf_autotune_report *report) {
     timed([&](bool before) -> cudaError_t {
       if (before) {
         cudaError_t q = prepare();
-        if (fuse) launch_integrate(m, f, depth, rgb, &fn, &mask, 0, cam, true, false, run, st, s->int_ctas);
+        if (fuse) launch_integrate(m, depth, rgb, &fn, &mask, 0, cam, true, false, run, st, s->int_ctas);
         return q;
       }
       launch_raycast(m, f, mv, mn, zmin, zmax, cam, f.counters + 3, &fv, &fn, run, st, t);
@@ -1068,7 +1068,7 @@ int sf_system_autotune(sf_system *s, int reps, sf_autotune_report *report) {
     for (int i = 0; i < 4 && e == cudaSuccess; ++i) {
       timed([&](bool before) -> cudaError_t {
         if (before) return prepare();
-        launch_integrate(m, f, depth, rgb, &fn, &mask, 0, cam, true, false, run, st, kIntCtas[i]);
+        launch_integrate(m, depth, rgb, &fn, &mask, 0, cam, true, false, run, st, kIntCtas[i]);
         return cudaSuccess;
       }, rep.integrate_ms[i]);
       rep.integrate_ctas[i] = kIntCtas[i];
@@ -1076,11 +1076,8 @@ int sf_system_autotune(sf_system *s, int reps, sf_autotune_report *report) {
     }
     rep.integrate_chosen = ibest;
   }
-  // the frame's state back: the voxels, their far-positive summaries
-  if (e == cudaSuccess && fuse) {
-    launch_save_visible(m, save, nvis, true, st);
-    launch_reclass_visible(m, f, nvis, st);
-  }
+  // the frame's state back
+  if (e == cudaSuccess && fuse) launch_save_visible(m, save, nvis, true, st);
   if (e == cudaSuccess) launch_raycast(m, f, mv, mn, zmin, zmax, cam, f.counters + 3, &fv, &fn, run, st, s->rc_tune);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e0) cudaEventDestroy(e0);
