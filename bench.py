@@ -648,8 +648,10 @@ def load_traffic(kernel, first, count):
     path = os.path.join(ROOT, "profiles", "roofline_traffic_640x480.json")
     try:
         with open(path) as f:
-            per = json.load(f)["kernels"][kernel]["per_frame_dram_bytes"]
-        vals = [per[str(i)] for i in range(first, first + count)]
+            per = json.load(f)["kernels"][kernel]["per_frame_dram_bytes"]  # entry i: frame i
+        if first + count > len(per):
+            return None
+        vals = per[first:first + count]
         return float(np.mean(vals))
     except (OSError, KeyError, ValueError, TypeError):
         return None
