@@ -558,17 +558,28 @@ typedef struct {
   int integrate_chosen;
   float integrate_ms[8];
   int integrate_ctas[8];
+  /* the allocation walk's pixel tile (256 threads: 32x8, 64x4, 16x16,
+   * 128x2), timed by rerunning the last frame's probe pass over its depth
+   * and pose after the frame allocated (it finds every block and requests
+   * none, so the map is unchanged); alloc_chosen = -1 when the last frame
+   * was not mapped */
+  int alloc_candidates;
+  int alloc_chosen;
+  float alloc_ms[8];
+  int alloc_tile_x[8], alloc_tile_y[8];
 } sf_autotune_report;
 int sf_system_autotune(sf_system *sys, int reps, sf_autotune_report *report);
 /* The frame's launch shapes: the raycast's (index of its candidate,
- * 0..5: registers for 8 or 6 CTAs per SM x tiles 8x16, 16x8, 32x4) and the
- * integration's CTAs per SM (1..64).  Every shape computes the same maps.
+ * 0..5: registers for 8 or 6 CTAs per SM x tiles 8x16, 16x8, 32x4), the
+ * integration's CTAs per SM (1..64) and the allocation walk's pixel tile
+ * (0..3: 32x8, 64x4, 16x16, 128x2).  Every shape computes the same maps.
  * sf_system_autotune picks them on the device at hand; a caller that cached
  * a choice for a configuration sets it back with sf_system_set_tune (the
  * frame graph is captured again on the next frame). */
 typedef struct {
   int raycast;
   int integrate_ctas_per_sm;
+  int alloc_tile;
 } sf_frame_tune;
 int sf_system_get_tune(sf_system *sys, sf_frame_tune *tune);
 int sf_system_set_tune(sf_system *sys, const sf_frame_tune *tune);

@@ -88,11 +88,13 @@ class RelocCandidate(C.Structure):
 class AutotuneReport(C.Structure):
     _fields_ = [("candidates", C.c_int), ("chosen", C.c_int), ("ms", C.c_float * 16), ("minb", C.c_int * 16),
                 ("tile_x", C.c_int * 16), ("tile_y", C.c_int * 16), ("integrate_candidates", C.c_int),
-                ("integrate_chosen", C.c_int), ("integrate_ms", C.c_float * 8), ("integrate_ctas", C.c_int * 8)]
+                ("integrate_chosen", C.c_int), ("integrate_ms", C.c_float * 8), ("integrate_ctas", C.c_int * 8),
+                ("alloc_candidates", C.c_int), ("alloc_chosen", C.c_int), ("alloc_ms", C.c_float * 8),
+                ("alloc_tile_x", C.c_int * 8), ("alloc_tile_y", C.c_int * 8)]
 
 
 class FrameTune(C.Structure):
-    _fields_ = [("raycast", C.c_int), ("integrate_ctas_per_sm", C.c_int)]
+    _fields_ = [("raycast", C.c_int), ("integrate_ctas_per_sm", C.c_int), ("alloc_tile", C.c_int)]
 
 
 vp = C.c_void_p

@@ -965,15 +965,29 @@ void launch_rebuild_index(const DevMap &m, cudaStream_t s) {
   k_rebuild_index<<<sm_count() * 8, 256, 0, s>>>(m); note_launch();
 }
 
+AllocTile alloc_tile(int tile) {
+  // 256 threads each (the probe's shared block lists are sized for that);
+  // a warp covers 32, 32, 16 x 2 or 32 pixels of a row
+  static const AllocTile kTiles[kAllocTileCount] = {{32, 8}, {64, 4}, {16, 16}, {128, 2}};
+  return kTiles[tile >= 0 && tile < kAllocTileCount ? tile : 0];
+}
+
+void launch_alloc_probe(const DevMap &m, const FuseScratch &f, const sf_image &depth, const Cam *c,
+                        const int *run_flag, uint32_t *flags, cudaStream_t s, int tile) {
+  const AllocTile t = alloc_tile(tile);
+  static_assert(kAllocThreads == 256, "alloc tiles hold 256 threads");
+  dim3 blk(t.x, t.y);
+  dim3 grd((depth.cols + t.x - 1) / t.x, (depth.rows + t.y - 1) / t.y);
+  k_alloc_probe<<<grd, blk, 0, s>>>(m, f, depth, c, run_flag, flags); note_launch();
+}
+
 void launch_alloc(const DevMap &m, const FuseScratch &f, const sf_image &depth, const Cam *c,
-                  const int *run_flag, uint32_t *flags, cudaStream_t s, bool begin) {
+                  const int *run_flag, uint32_t *flags, cudaStream_t s, bool begin, int tile) {
   if (begin) {
     k_alloc_begin<<<1, 1, 0, s>>>(f, run_flag);
     note_launch();
   }
-  dim3 blk(32, 8);
-  dim3 grd((depth.cols + 31) / 32, (depth.rows + 7) / 8);
-  k_alloc_probe<<<grd, blk, 0, s>>>(m, f, depth, c, run_flag, flags); note_launch();
+  launch_alloc_probe(m, f, depth, c, run_flag, flags, s, tile);
   k_alloc_insert<<<sm_count() * 2, 128, 0, s>>>(m, f, run_flag, flags); note_launch();
 }
 

@@ -181,8 +181,18 @@ void launch_rebuild_index(const DevMap &m, cudaStream_t s);
 // Fusion::CreateBlocks (FuseMap.cu:92-132) as probe + insert passes.  With
 // begin = false the caller has run alloc_frame_begin itself (in its own
 // single-thread kernel, gated by the same run flag).
+// tile: the probe's 256-thread pixel tile, kAllocTiles[tile] (every tile
+// allocates the same blocks; sf_system_autotune times them).
+constexpr int kAllocTileCount = 4;
+struct AllocTile {
+  int x, y;
+};
+AllocTile alloc_tile(int tile);
 void launch_alloc(const DevMap &m, const FuseScratch &f, const sf_image &depth, const Cam *c,
-                  const int *run_flag, uint32_t *flags, cudaStream_t s, bool begin = true);
+                  const int *run_flag, uint32_t *flags, cudaStream_t s, bool begin = true, int tile = 0);
+// The probe pass alone (no epoch start, no insert pass), for the autotuner.
+void launch_alloc_probe(const DevMap &m, const FuseScratch &f, const sf_image &depth, const Cam *c,
+                        const int *run_flag, uint32_t *flags, cudaStream_t s, int tile);
 // CheckFullVisibility (FuseMap.cu:134-168) over the allocated-entry index.
 // When zmin/zmax images are given, also lays down the z-range tiles of
 // Projection + fillBlocks (RenderScene.cu:54-190) for each visible block.

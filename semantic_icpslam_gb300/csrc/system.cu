@@ -251,6 +251,7 @@ struct sf_system {
   RaycastTune rc_tune;
   int rc_index = 0;
   int int_ctas = 8;
+  int alloc_tile = 0;           // the allocation walk's pixel tile (alloc_tile())
   long long frames = 0;  // frames run (any form)
 };
 
@@ -454,7 +455,7 @@ int fuse_and_raytrace(sf_system *s, const Cam *cam, const int *run, int num_dete
   sf_image zmin = img(s->d_zmin, s->zc, s->zr, 4), zmax = img(s->d_zmax, s->zc, s->zr, 4);
   // the first pass of a device-driven frame starts its allocation epoch in
   // k_sys_post
-  launch_alloc(m, f, depth, cam, run, flags, st, /*begin=*/!first || run == nullptr);
+  launch_alloc(m, f, depth, cam, run, flags, st, /*begin=*/!first || run == nullptr, s->alloc_tile);
   if (first) mark(s, st, 3);
   launch_visibility(m, f, cam, &zmin, &zmax, run, flags, st);
   if (first) {
@@ -1076,6 +1077,26 @@ int sf_system_autotune(sf_system *s, int reps, sf_autotune_report *report) {
     }
     rep.integrate_chosen = ibest;
   }
+  // the allocation walk's probe pass over the frame's depth and pose: the
+  // frame allocated every block it meets (and requested, in this epoch,
+  // any it could not), so the reruns request nothing and change nothing
+  int abest = s->alloc_tile;
+  rep.alloc_chosen = -1;
+  if (fuse) {
+    rep.alloc_candidates = kAllocTileCount;
+    abest = 0;
+    for (int i = 0; i < kAllocTileCount && e == cudaSuccess; ++i) {
+      timed([&](bool before) -> cudaError_t {
+        if (before) return cudaMemsetAsync(flush, 0, flush_bytes, st);
+        launch_alloc_probe(m, f, depth, cam, run, ctx_flags(s->ctx), st, i);
+        return cudaSuccess;
+      }, rep.alloc_ms[i]);
+      rep.alloc_tile_x[i] = alloc_tile(i).x;
+      rep.alloc_tile_y[i] = alloc_tile(i).y;
+      if (rep.alloc_ms[i] < rep.alloc_ms[abest]) abest = i;
+    }
+    rep.alloc_chosen = abest;
+  }
   // the frame's state back
   if (e == cudaSuccess && fuse) launch_save_visible(m, save, nvis, true, st);
   if (e == cudaSuccess) launch_raycast(m, f, mv, mn, zmin, zmax, cam, f.counters + 3, &fv, &fn, run, st, s->rc_tune);
@@ -1091,6 +1112,7 @@ int sf_system_autotune(sf_system *s, int reps, sf_autotune_report *report) {
   sf_frame_tune tune;
   tune.raycast = best;
   tune.integrate_ctas_per_sm = fuse ? kIntCtas[ibest] : s->int_ctas;
+  tune.alloc_tile = abest;
   const int r = sf_system_set_tune(s, &tune);
   if (report) *report = rep;
   return r;
@@ -1100,19 +1122,21 @@ int sf_system_get_tune(sf_system *s, sf_frame_tune *t) {
   if (!s || !t) return SF_ERR_INVALID;
   t->raycast = s->rc_index;
   t->integrate_ctas_per_sm = s->int_ctas;
+  t->alloc_tile = s->alloc_tile;
   return SF_OK;
 }
 
 int sf_system_set_tune(sf_system *s, const sf_frame_tune *t) {
   if (!s || !t || t->raycast < 0 || t->raycast >= kRaycastTunes || t->integrate_ctas_per_sm < 1 ||
-      t->integrate_ctas_per_sm > 64)
+      t->integrate_ctas_per_sm > 64 || t->alloc_tile < 0 || t->alloc_tile >= kAllocTileCount)
     return SF_ERR_INVALID;
   const RaycastTune rt = raycast_tune(t->raycast);
   const bool changed = rt.minb != s->rc_tune.minb || rt.tx != s->rc_tune.tx || rt.ty != s->rc_tune.ty ||
-                       t->integrate_ctas_per_sm != s->int_ctas;
+                       t->integrate_ctas_per_sm != s->int_ctas || t->alloc_tile != s->alloc_tile;
   s->rc_tune = rt;
   s->rc_index = t->raycast;
   s->int_ctas = t->integrate_ctas_per_sm;
+  s->alloc_tile = t->alloc_tile;
   if (changed && s->gexec) {  // recaptured with the new shapes on the next frame
     cudaGraphExecDestroy(s->gexec);
     s->gexec = nullptr;

@@ -1,7 +1,7 @@
 """Launch-shape tuning of the frame loop with a per-configuration cache.
 
-sf_system_autotune times the raycast's launch shapes and the integration's
-grid on the device at hand, in the state the frame left (every shape
+sf_system_autotune times the raycast's launch shapes, the integration's
+grid and the allocation walk's pixel tile on the device at hand, in the state the frame left (every shape
 computes the same maps), and keeps the fastest.  tuned() runs it once per
 configuration and device and keeps the choice in a JSON file, so later
 systems of the same configuration take it with sf_system_set_tune instead
@@ -68,18 +68,20 @@ def tuned(system, reps=10, path=None):
     data = _load(path)
     if key in data:
         e = data[key]
-        t = _lib.FrameTune(int(e["raycast"]), int(e["integrate_ctas_per_sm"]))
+        t = _lib.FrameTune(int(e["raycast"]), int(e["integrate_ctas_per_sm"]), int(e.get("alloc_tile", 0)))
         _lib.call("sf_system_set_tune", system.h, C.byref(t))
         return e, True
     rep = _lib.AutotuneReport()
     _lib.call("sf_system_autotune", system.h, int(reps), C.byref(rep))
     t = _lib.FrameTune()
     _lib.call("sf_system_get_tune", system.h, C.byref(t))
-    entry = {"raycast": t.raycast, "integrate_ctas_per_sm": t.integrate_ctas_per_sm,
+    entry = {"raycast": t.raycast, "integrate_ctas_per_sm": t.integrate_ctas_per_sm, "alloc_tile": t.alloc_tile,
              "raycast_ms": {"%dx%d/%d" % (rep.tile_x[i], rep.tile_y[i], rep.minb[i]): round(rep.ms[i], 5)
                             for i in range(rep.candidates)},
              "integrate_ms": {str(rep.integrate_ctas[i]): round(rep.integrate_ms[i], 5)
-                              for i in range(rep.integrate_candidates)}}
+                              for i in range(rep.integrate_candidates)},
+             "alloc_ms": {"%dx%d" % (rep.alloc_tile_x[i], rep.alloc_tile_y[i]): round(rep.alloc_ms[i], 5)
+                          for i in range(rep.alloc_candidates)}}
     data[key] = entry
     _store(path, data)
     return entry, False

@@ -1,7 +1,7 @@
 """sf_system_autotune (the Autotune entry point, no counterpart in the
-reference): it times the last frame's raycast under each launch shape and
-the integration under each grid size, in the state the frame left, and
-keeps the fastest.  Every shape computes the same maps, so a system that
+reference): it times the last frame's raycast under each launch shape, the
+integration under each grid size and the allocation walk's probe under each
+pixel tile, in the state the frame left, and keeps the fastest.  Every shape computes the same maps, so a system that
 autotunes mid-sequence, or takes any shape by sf_system_set_tune, must
 produce the same poses, statistics, model maps and map, bit for bit, as one
 that does not; and the timing runs must leave the map and model maps as
@@ -63,9 +63,12 @@ def _compare(sf, ctx, seq, a, b):
     assert {(m, x, y) for m, x, y, _ in cands} == {(m, x, y) for m in (8, 6) for x, y in ((8, 16), (16, 8), (32, 4))}
     assert rep.integrate_candidates == 4 and 0 <= rep.integrate_chosen < 4
     assert [rep.integrate_ctas[i] for i in range(4)] == [2, 4, 8, 16] and min(rep.integrate_ms[:4]) > 0
+    assert rep.alloc_candidates == 4 and 0 <= rep.alloc_chosen < 4 and min(rep.alloc_ms[:4]) > 0
+    assert [(rep.alloc_tile_x[i], rep.alloc_tile_y[i]) for i in range(4)] == [(32, 8), (64, 4), (16, 16), (128, 2)]
     t = sf._lib.FrameTune()
     sf.call("sf_system_get_tune", b.h, C.byref(t))
     assert t.raycast == rep.chosen and t.integrate_ctas_per_sm == rep.integrate_ctas[rep.integrate_chosen]
+    assert t.alloc_tile == rep.alloc_chosen
     for x, y in zip(_model(ctx, a), _model(ctx, b)):  # the timing runs left the model maps as they were
         np.testing.assert_array_equal(x, y)
     ea, va, _ = map_to_host(ctx, a.map())  # and the voxels the integration runs touched (per block
@@ -74,10 +77,12 @@ def _compare(sf, ctx, seq, a, b):
     kb, xb = voxels_by_pos(eb, vb)
     assert ka == kb and np.array_equal(xa.view(np.uint8), xb.view(np.uint8))
     # the least likely shapes: the results still do not change
-    far = sf._lib.FrameTune(5, 2)
+    far = sf._lib.FrameTune(5, 2, 2)
     sf.call("sf_system_set_tune", b.h, C.byref(far))
     with pytest.raises(sf.SfError):
-        sf.call("sf_system_set_tune", b.h, C.byref(sf._lib.FrameTune(6, 8)))
+        sf.call("sf_system_set_tune", b.h, C.byref(sf._lib.FrameTune(6, 8, 0)))
+    with pytest.raises(sf.SfError):
+        sf.call("sf_system_set_tune", b.h, C.byref(sf._lib.FrameTune(0, 8, 4)))
     for d, rgb, _, _ in seq[3:]:
         sa = a.grab(d, rgb)
         sb = b.grab(d, rgb)
@@ -107,6 +112,7 @@ def test_tune_cache_per_configuration(lib, tmp_path):
     assert not cached1 and cached2 and e1 == e2
     t = sf._lib.FrameTune()
     sf.call("sf_system_get_tune", s2.h, C.byref(t))
-    assert (t.raycast, t.integrate_ctas_per_sm) == (e1["raycast"], e1["integrate_ctas_per_sm"])
+    assert (t.raycast, t.integrate_ctas_per_sm, t.alloc_tile) == (e1["raycast"], e1["integrate_ctas_per_sm"],
+                                                                  e1["alloc_tile"])
     s1.close()
     s2.close()
