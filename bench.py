@@ -116,7 +116,28 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x):
+    """The largest x over the ranks of the default process group (x itself
+    when there is none, or one rank): the job's time is its slowest rank's."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_fps(ws, steps, elapsed):
+    """Whole-job frames/s: every rank runs `steps` frames of its own copy of
+    the sequence (weak scaling), the job takes the slowest rank's time."""
+    return ws * steps / elapsed
+
+
 def make_frames(n, rank=0):
+    """The sequence a rank runs: every replica runs the same frames (the
+    same work per GPU), independently."""
     from synth import Synth  # host-only generator library: loads none of the product's code
     syn = Synth(COLS, ROWS, K, **SEQ)
     return [syn.frame(i) for i in range(n)]
@@ -126,7 +147,7 @@ def bench_config():
     """The `config` of both arms' lines (the same dict, so the two arms'
     configurations compare equal)."""
     return {"workload": WORKLOAD, "global_batch": "1 frame per GPU per step",
-            "parallelism": "replicas (one independent sequence per GPU)",
+            "parallelism": "replicas (every GPU runs its own copy of the sequence; no data exchanged)",
             "l2": "flushed before every timed step (a %d MiB write on the timed stream, outside the timed "
                   "intervals); each step reads a new frame" % (FLUSH_BYTES >> 20)}
 
@@ -811,13 +832,8 @@ def main():
     AUTOTUNE = not args.no_autotune
     g = time_device_resident(sf, ctx, frames, args.steps, args.warmup, 1, barrier,
                              rgb=1 if (args.quick and args.rgbd) else 0, flush=flush)
-    elapsed = g["elapsed"]
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([elapsed], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
-    fps = ws * args.steps / elapsed
+    elapsed = max_over_ranks(g["elapsed"])
+    fps = job_fps(ws, args.steps, elapsed)
     out = {"metric": METRIC, "value": round(fps, 3), "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(1000.0 * elapsed / args.steps, 4), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 6x6 solve)",
@@ -844,6 +860,9 @@ def main():
                       "achieved_gbs": round(gbs, 1), "frac_of_%s_hbm" % peak_kind: round(gbs / peak, 4)}
     dom = max(sbytes, key=lambda k: st_ms[k])  # the frame's dominant kernel
     out["stages_ms"] = st_ms
+    out["frames"] = {"tracked": int(sum(st.tracked for st in tp["stats"])),
+                     "lost": int(sum(st.state == -1 for st in tp["stats"])), "timed": len(tp["stats"]),
+                     "note": "a lost frame (state -1, no relocalisation candidates) runs no ICP and no mapping"}
     out["kernels"] = kern
     out["visible_blocks_mean"] = round(float(V.mean()), 1)
     d = kern[dom]
