@@ -43,6 +43,32 @@
 
 namespace sf {
 
+// Compares and conversions run on the FP64 pipe at the cost of an FP64
+// operation; these integer forms take the exponent and mantissa bits
+// instead.  nonneg_below: x < y for x >= 0 and finite y >= 0, as the bit
+// patterns order those doubles (|x| < y for any x; NaN compares false).
+__device__ __forceinline__ bool nonneg_below(double x, double y) {
+  return (__double_as_longlong(x) & 0x7fffffffffffffffll) < __double_as_longlong(y);
+}
+// A non-negative double to float, truncating the mantissa (within one float
+// ulp of the rounded conversion); values below the float normal range give 0.
+__device__ __forceinline__ float nonneg_to_float_rz(double x) {
+  const int hi = __double2hiint(x), lo = __double2loint(x);
+  const int fe = ((hi >> 20) & 0x7ff) - 1023 + 127;
+  if (fe <= 0) return 0.0f;
+  if (fe >= 0xff) return __int_as_float(0x7f800000);
+  return __int_as_float((fe << 23) | ((hi & 0xfffff) << 3) | (int)((unsigned)lo >> 29));
+}
+// A float to double, exactly, for zero and normal floats (subnormal floats
+// give 0).
+__device__ __forceinline__ double float_to_double_exact(float f) {
+  const int b = __float_as_int(f);
+  const int e = (b >> 23) & 0xff;
+  if (e == 0) return 0.0;
+  const int hi = (b & (int)0x80000000) | ((e - 127 + 1023) << 20) | ((b & 0x7fffff) >> 3);
+  return __hiloint2double(hi, (b & 7) << 29);
+}
+
 struct IcpSolveSmem {
   double a[2][6][8];  // augmented [A | b], row stride 8, double-buffered
   int code, copy_cand;  // the stop decision of ctl_decide
@@ -193,22 +219,22 @@ __device__ bool ctl_step_fast(TrackCtl &c, const double *sums, int min_count, Ic
   const double u0 = x[0], u1 = x[1], u2 = x[2];
   const double w0 = x[3], w1 = x[4], w2 = x[5];
   const double th2 = fma(w2, w2, fma(w1, w1, w0 * w0));
-  const bool tiny = th2 < 1e-20;  // below 1e-10 rad Sophus's V is R
+  const bool tiny = nonneg_below(th2, 1e-20);  // below 1e-10 rad Sophus's V is R
   double ca = 0.0, c1, c2 = 0.0;
-  if (th2 < 0.01) {
+  if (nonneg_below(th2, 0.01)) {
     // sin t / t = 1 - x/6 + x^2/120 - ..., (1 - cos t)/t^2 = 1/2 - x/24 + ...,
     // (t - sin t)/t^3 = 1/6 - x/120 + ..., x = t^2
-    const float xf = (float)th2;
+    const float xf = nonneg_to_float_rz(th2);
     const float c1_tail = xf * (1.f / 720 + xf * (-1.f / 40320 + xf * (1.f / 3628800 + xf * (-1.f / 479001600))));
-    c1 = fma(th2, -1.0 / 24 + (double)c1_tail, 0.5);
+    c1 = fma(th2, -1.0 / 24 + float_to_double_exact(c1_tail), 0.5);
     if (!tw || tiny) {
       const float ca_tail = xf * (1.f / 120 + xf * (-1.f / 5040 + xf * (1.f / 362880 + xf * (-1.f / 39916800))));
-      ca = fma(th2, -1.0 / 6 + (double)ca_tail, 1.0);
+      ca = fma(th2, -1.0 / 6 + float_to_double_exact(ca_tail), 1.0);
     }
     if (tw && !tiny) {
       const float c2_tail =
           xf * (1.f / 5040 + xf * (-1.f / 362880 + xf * (1.f / 39916800 + xf * (-1.f / 6227020800.f))));
-      c2 = fma(th2, -1.0 / 120 + (double)c2_tail, 1.0 / 6);
+      c2 = fma(th2, -1.0 / 120 + float_to_double_exact(c2_tail), 1.0 / 6);
     }
   } else {
     const double th = sqrt(th2);

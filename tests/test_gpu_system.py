@@ -200,3 +200,24 @@ def test_frame_log_lines_match_stats(lib, tmp_path):
         assert r["frame"] == i and r["tracked"] == st.tracked and r["iterations"] == st.iterations
         assert r["visible_blocks"] == st.visible and r["t"] == [st.pose[3], st.pose[7], st.pose[11]]
         assert 0 < r["visible_percent"] <= 1.0
+
+
+def test_pinned_and_pageable_inputs_agree(lib):
+    """sf_system_grab from page-locked host buffers (copied straight from
+    the caller's memory) and from ordinary ones (through the staging buffer)
+    gives the same frames."""
+    import torch
+    sf, ctx = lib
+    seq = sequence(C1["cols"], C1["rows"], C1["K"], 5, trajectory=0)
+    cfg = sf.system_config(cols=C1["cols"], rows=C1["rows"], K=C1["K"], use_graph=1, **MAP_C1)
+    a = sf.System(ctx, cfg, init_pose=seq[0][3])
+    b = sf.System(ctx, cfg, init_pose=seq[0][3])
+    for d, rgb, _, _ in seq:
+        dp = torch.from_numpy(np.ascontiguousarray(d)).pin_memory()
+        cp = torch.from_numpy(np.ascontiguousarray(rgb)).pin_memory()
+        sa = a.grab(dp.numpy(), cp.numpy())
+        sb = b.grab(np.array(d), np.array(rgb))
+        assert np.array_equal(np.array(sa.pose[:]), np.array(sb.pose[:]))
+        assert (sa.tracked, sa.iterations, sa.visible) == (sb.tracked, sb.iterations, sb.visible)
+    a.close()
+    b.close()
