@@ -836,16 +836,19 @@ __global__ void k_unify_apply(DevMap m, const uint32_t *out, unsigned *list_coun
 
 constexpr int kIntThreads = 256;
 
-// Eight 256-thread CTAs per SM (32 registers, a few spilled bytes): the
-// kernel waits on its voxel loads, and full occupancy hides that best
-// (measured on GB300 against 3-6 CTAs per SM).
+// Eight 256-thread CTAs per SM (32 registers, a few spilled bytes) for the
+// TSDF pass: the kernel waits on its depth and voxel loads, and full
+// occupancy hides that best (measured on GB300 against 3-6 CTAs per SM);
+// the label passes, with more state per voxel, take six.
 #ifndef SF_INT_MINB
 #define SF_INT_MINB 8
 #endif
-__global__ void __launch_bounds__(kIntThreads, SF_INT_MINB) k_integrate(DevMap m, sf_image depth, sf_image rgb,
+// One instantiation per pass (TSDF only, labels only, both): the TSDF pass
+// carries none of the label update's registers.
+template <bool do_int, bool do_sem>
+__global__ void __launch_bounds__(kIntThreads, do_sem ? 6 : SF_INT_MINB) k_integrate(DevMap m, sf_image depth, sf_image rgb,
                                                            sf_image nmap, sf_image mask,
                                                            int num_detection, const Cam *cam,
-                                                           int do_int, int do_sem,
                                                            const int *run_flag) {
   if (run_flag && *run_flag == 0) return;
   const Cam c = *cam;
@@ -857,36 +860,57 @@ __global__ void __launch_bounds__(kIntThreads, SF_INT_MINB) k_integrate(DevMap m
     int4 h = __ldcg((const int4 *)(m.visible + b));
     h.w = checked_ptr(m, h.w);
     if (h.w == -1) continue;
-    for (int li = threadIdx.x; li < 512; li += kIntThreads) {
+    // Each thread's two voxels (li = tid, tid + 256) in phases, so that
+    // their dependent loads overlap: both projections and depth reads, then
+    // both voxel (and colour) reads, then both updates.
+    static_assert(kIntThreads * 2 == 512, "two voxels per thread");
+    f3 pos[2];
+    int u[2], v[2];
+    float dp[2];
+    bool ok[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const int li = threadIdx.x + k * kIntThreads;
       const int lx = li & 7, ly = (li >> 3) & 7, lz = li >> 6;
       f3 w3 = mk3((float)(h.x * 8 + lx) * voxel, (float)(h.y * 8 + ly) * voxel,
                   (float)(h.z * 8 + lz) * voxel);
-      f3 pos = mul(c.Rinv, w3 - c.t);
-      int u = (int)(c.fx * pos.x / pos.z + c.cx);
-      int v = (int)(c.fy * pos.y / pos.z + c.cy);
-      if (u < 0 || v < 0 || u >= c.cols || v >= c.rows) continue;
-      float dp = __ldg(row_ptr<const float>(depth, v) + u);
-      if (isnan(dp) || dp > c.dmax || dp < c.dmin) continue;
-      float sdf = dp - pos.z;
-      if (!(sdf >= -thresh)) continue;
-      const uint8_t *px = row_ptr<const uint8_t>(rgb, v) + 3 * u;
-      uint4 *vp = (uint4 *)(m.voxels + h.w) + li;
-      VoxelU vx;
-      vx.u = *vp;
+      pos[k] = mul(c.Rinv, w3 - c.t);
+      u[k] = (int)(c.fx * pos[k].x / pos[k].z + c.cx);
+      v[k] = (int)(c.fy * pos[k].y / pos[k].z + c.cy);
+      ok[k] = !(u[k] < 0 || v[k] < 0 || u[k] >= c.cols || v[k] >= c.rows);
+      dp[k] = ok[k] ? __ldg(row_ptr<const float>(depth, v[k]) + u[k]) : 0.0f;
+    }
+    VoxelU vx[2];
+    uint8_t px[2][3];
+    float sdf[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      ok[k] = ok[k] && !(isnan(dp[k]) || dp[k] > c.dmax || dp[k] < c.dmin);
+      sdf[k] = dp[k] - pos[k].z;
+      ok[k] = ok[k] && sdf[k] >= -thresh;
+      if (ok[k]) {
+        vx[k].u = *((const uint4 *)(m.voxels + h.w) + threadIdx.x + k * kIntThreads);
+        const uint8_t *p = row_ptr<const uint8_t>(rgb, v[k]) + 3 * u[k];
+        px[k][0] = p[0]; px[k][1] = p[1]; px[k][2] = p[2];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      if (!ok[k]) continue;
       bool dirty = false;
       if (do_int) {
-        f3 val = mk3((float)px[0], (float)px[1], (float)px[2]);
-        dirty = integrate_voxel(vx.v, fminf(1.0f, sdf / thresh), val);
+        f3 val = mk3((float)px[k][0], (float)px[k][1], (float)px[k][2]);
+        dirty = integrate_voxel(vx[k].v, fminf(1.0f, sdf[k] / thresh), val);
       }
       if (do_sem) {
-        float4 nl = __ldg(row_ptr<const float4>(nmap, v) + u);
+        float4 nl = __ldg(row_ptr<const float4>(nmap, v[k]) + u[k]);
         if (!isnan(nl.x)) {
           uint8_t label;
           f3 val;
           if (num_detection > 0) {
-            label = __ldg(row_ptr<const uint8_t>(mask, v) + u);
+            label = __ldg(row_ptr<const uint8_t>(mask, v[k]) + u[k]);
             if (label == 0) {
-              val = mk3((float)px[0], (float)px[1], (float)px[2]);
+              val = mk3((float)px[k][0], (float)px[k][1], (float)px[k][2]);
             } else {
               int p0 = (int)((unsigned)pal0 * (unsigned)label) % 255;
               int p1 = (int)((unsigned)pal1 * (unsigned)label) % 255;
@@ -895,13 +919,13 @@ __global__ void __launch_bounds__(kIntThreads, SF_INT_MINB) k_integrate(DevMap m
             }
           } else {
             label = 0;
-            val = mk3((float)px[0], (float)px[1], (float)px[2]);
+            val = mk3((float)px[k][0], (float)px[k][1], (float)px[k][2]);
           }
-          semantic_voxel(vx.v, label, val, nl, pos);
+          semantic_voxel(vx[k].v, label, val, nl, pos[k]);
           dirty = true;
         }
       }
-      if (dirty) *vp = vx.u;
+      if (dirty) *((uint4 *)(m.voxels + h.w) + threadIdx.x + k * kIntThreads) = vx[k].u;
     }
   }
 }
@@ -1038,8 +1062,15 @@ void launch_integrate(const DevMap &m, const sf_image &depth, const sf_image &rg
   sf_image nm = nmap ? *nmap : sf_image{};
   sf_image mk = mask ? *mask : sf_image{};
   const bool sem = semantics && nmap && (num_detection <= 0 || mask);
-  k_integrate<<<sm_count() * ctas_per_sm, kIntThreads, 0, s>>>(m, depth, rgb, nm, mk, num_detection, c,
-                                                               integrate ? 1 : 0, sem ? 1 : 0, run_flag);
+  const dim3 grid(sm_count() * ctas_per_sm);
+  if (integrate && sem)
+    k_integrate<true, true><<<grid, kIntThreads, 0, s>>>(m, depth, rgb, nm, mk, num_detection, c, run_flag);
+  else if (integrate)
+    k_integrate<true, false><<<grid, kIntThreads, 0, s>>>(m, depth, rgb, nm, mk, num_detection, c, run_flag);
+  else if (sem)
+    k_integrate<false, true><<<grid, kIntThreads, 0, s>>>(m, depth, rgb, nm, mk, num_detection, c, run_flag);
+  else
+    return;
   note_launch();
 }
 
