@@ -108,12 +108,15 @@ int sf_context_flags(sf_context *ctx, uint32_t *flags_out);
 /* Process-wide number of kernels this library has launched (a CUDA-graph
  * replay counts the kernel nodes it runs). */
 int sf_kernel_launches(uint64_t *out);
-/* Tracing of the persistent ICP kernel: when enabled, CTA 0 records SM
- * clocks at six phase boundaries of each iteration (start, pixels
- * accumulated, block total written, grid barrier passed, cross-block sum,
- * solve) into slots 0-5 of 64 x 16 slots, the global timer (ns) at the
- * iteration start into slot 6, and clocks inside the solve into slots
- * 8-13; out (may be NULL, else 64 * 16 values) receives them. */
+/* Tracing of the persistent ICP kernel: when enabled, the first pixel CTA
+ * records SM clocks at five phase boundaries of each iteration (round
+ * start, rows accumulated, block total written, grid barrier passed, sums
+ * and the solving CTA's pose in hand) into slots 0-4 of 64 x 16 slots, the
+ * global timer (ns) at the round start into slot 6, whether the rows came
+ * from a predicted pose into slot 7 and the start of the rows after the
+ * prediction into slot 14; the solving CTA records clocks inside the
+ * iteration's solve into slots 8-13; out (may be NULL, else 64 * 16
+ * values) receives them. */
 int sf_icp_profile(sf_context *ctx, int enable, uint64_t *out);
 /* Bounds of the persistent ICP kernel's grid barriers (a diagnostic hook
  * for testing failure detection; no counterpart in the reference).  Each
@@ -126,6 +129,19 @@ int sf_icp_profile(sf_context *ctx, int enable, uint64_t *out);
  * frame's stats.fail = 3); the context stays usable.  Takes effect for
  * later launches (a frame graph captured before keeps its bounds). */
 int sf_icp_barrier_limits(sf_context *ctx, uint32_t poll_limit, uint32_t extra_arrivals);
+/* Next-pose prediction of the persistent ICP kernel (a diagnostic switch;
+ * no counterpart in the reference; on by default).  One CTA runs each
+ * iteration's FP64 solve while the others predict the float pose it will
+ * give (FP32 / float-float arithmetic) and accumulate the next iteration's
+ * rows on the prediction; the rows are kept only when the prediction
+ * equals the float form of the solved FP64 pose in every bit, else they
+ * are accumulated again on that pose.  Poses, sums and decisions are the
+ * same with the prediction on or off; off, every iteration takes two grid
+ * rounds (the solve, then the rows).  Takes effect for later launches (a
+ * frame graph captured before keeps its setting).  Phase-clock slot 7 of
+ * sf_icp_profile records per iteration whether its rows came from a
+ * prediction. */
+int sf_icp_predict(sf_context *ctx, int enable);
 /* Copies `bytes` between any two host/device pointers (unified addressing)
  * on the context stream and waits for it. */
 int sf_memcpy(sf_context *ctx, void *dst, const void *src, size_t bytes);

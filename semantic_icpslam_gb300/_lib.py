@@ -115,6 +115,7 @@ SIGNATURES = {
     "sf_kernel_launches": [C.POINTER(C.c_uint64)],
     "sf_icp_profile": [vp, C.c_int, C.POINTER(C.c_uint64)],
     "sf_icp_barrier_limits": [vp, C.c_uint32, C.c_uint32],
+    "sf_icp_predict": [vp, C.c_int],
     "sf_map_create": [C.POINTER(MapConfig), pvp],
     "sf_map_wrap": [C.POINTER(MapConfig), C.POINTER(DeviceMap), pvp],
     "sf_map_destroy": [vp],

@@ -179,6 +179,12 @@ int sf_icp_barrier_limits(sf_context *ctx, uint32_t poll_limit, uint32_t extra_a
   return SF_OK;
 }
 
+int sf_icp_predict(sf_context *ctx, int enable) {
+  if (!ctx) return SF_ERR_INVALID;
+  ctx->icp.predict = enable ? 1 : 0;
+  return SF_OK;
+}
+
 int sf_icp_profile(sf_context *ctx, int enable, uint64_t *out) {
   if (!ctx) return SF_ERR_INVALID;
   ctx->icp.profile = enable ? 1 : 0;

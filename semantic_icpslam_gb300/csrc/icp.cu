@@ -25,6 +25,7 @@ __shared__ unsigned long long *s_solve_marks;
     if (threadIdx.x == 0 && s_solve_marks) s_solve_marks[k] = clock64(); \
   } while (0)
 #include "sf_icp_solve.cuh"
+#include "sf_icp_spec.cuh"
 
 namespace sf {
 
@@ -541,14 +542,27 @@ struct PersistentArgs {
   unsigned poll_limit;       // polls before a grid barrier gives up
   unsigned extra_arrivals;   // arrivals a barrier waits for beyond the grid (0; a test sets it to make
                              // every wait run out)
+  int predict;               // predict each iteration's pose and accumulate its rows during the solve
+  void *pub;                 // [3] IcpPub: the solving CTA's pose and decision per accumulator set
 };
 
-// Phase clock of CTA 0 (SM cycles): 0 iteration start, 1 pixels
-// accumulated, 2 block total sent, 3 barrier passed, 4 the 29 sums in
-// hand, 5 solve done.
+// Phase clocks of the first pixel CTA (SM cycles), per iteration (the
+// last round that accumulated its rows): 0 round start, 1 rows
+// accumulated, 2 block total sent, 3 barrier passed, 4 the 29 sums and the
+// solving CTA's pose in hand; 6 the global timer at 0; 7 whether the rows
+// came from a prediction; 14 the rows started (after the prediction).
+// Slots 8-13 take clocks of CTA 0 inside the iteration's solve.
+// SM clock read that the compiler keeps in place relative to barriers and
+// memory operations (clock64() alone may be moved ahead of a barrier).
+__device__ __forceinline__ unsigned long long prof_clock() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%clock64;" : "=l"(t)::"memory");
+  return t;
+}
+
 __device__ __forceinline__ void prof_mark(const PersistentArgs &a, int it, int k) {
-  if (a.prof && blockIdx.x == 0 && threadIdx.x == 0 && it < kProfIters) {
-    a.prof[it * kProfSlots + k] = clock64();
+  if (a.prof && blockIdx.x == 1 && threadIdx.x == 0 && it < kProfIters) {
+    a.prof[it * kProfSlots + k] = prof_clock();
     if (k == 0) {
       unsigned long long ns;
       asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(ns));
@@ -609,6 +623,51 @@ __device__ __forceinline__ void read_fix_set(const unsigned long long *fx,
   if (sync_after) __syncthreads();
 }
 
+// What the solving CTA publishes per accumulator set: the FP64 pose after
+// its solve (rows 0..2) and whether the iterations stop there.
+struct IcpPub {
+  double pose[12];
+  int stop;
+  int pad[7];
+};
+static_assert(sizeof(IcpPub) == 128, "one publication per 128 B");
+
+// The iteration after (l, j): its level in *nl and index in *nj (levels
+// without iterations skipped); false after the last one.
+__device__ __forceinline__ bool next_iteration(const PersistentArgs &a, int l, int j, int *nl, int *nj) {
+  if (j + 1 < a.lv[l].iters) {
+    *nl = l;
+    *nj = j + 1;
+    return true;
+  }
+  for (int m = l - 1; m >= 0; --m)
+    if (a.lv[m].iters > 0) {
+      *nl = m;
+      *nj = 0;
+      return true;
+    }
+  return false;
+}
+
+// Every level and iteration of ComputeSE3 in one cooperative launch.
+//
+// CTA 0 solves; CTAs 1.. take the pixels.  Each iteration's rows need the
+// pose the previous iteration's FP64 solve gives, so rather than wait for
+// it, the pixel CTAs predict that pose (its float form, from the same 29
+// sums and the previous FP64 pose, with FP32 / float-float arithmetic in
+// one warp: sf_icp_spec.cuh) and accumulate the iteration's rows on the
+// prediction while CTA 0 runs the FP64 solve.  CTA 0 publishes the FP64
+// pose (and the stop decision) before it arrives at the round's grid
+// barrier; after the barrier every CTA compares the float form of the
+// published pose with its prediction, bit for bit.  When they agree the
+// round's sums are the iteration's sums; when they do not (or no
+// prediction was made) the next round accumulates the rows again on the
+// published pose.  So sums, poses and decisions are those of the FP64
+// path whatever the prediction does.  Rounds rotate over three
+// accumulator sets; a round's barrier index is its number (twice its
+// number, and once more after the correspondence pass, with the
+// photometric term).
+//
 // RGB: each iteration also runs RGBStep (Tracking.cc:400-431): the
 // correspondence pass beside the ICP rows, a grid barrier for its count
 // and sum of diff^2 (sigma), the photometric rows, a second barrier, and
@@ -617,7 +676,11 @@ template <bool RGB>
 __global__ void __launch_bounds__(kPThreads, 1) k_icp_persistent(PersistentArgs a) {
   __shared__ TrackCtl ctl;
   __shared__ IcpSolveSmem ssolve;
-  __shared__ PoseF pose;
+  __shared__ PoseF pose;          // the float pose of this round's rows
+  __shared__ spec::f2f nff[12];   // the last solved FP64 pose (rows 0..2) as float-float
+  __shared__ float spred[12];     // this round's prediction (row-major 3 x 4)
+  __shared__ int made;            // a prediction was made this round
+  __shared__ int pub_stop, hit;
   __shared__ float2 bsum[29];
   __shared__ double sums[29];
   __shared__ double rsums[RGB ? 29 : 1];
@@ -626,93 +689,196 @@ __global__ void __launch_bounds__(kPThreads, 1) k_icp_persistent(PersistentArgs 
   __shared__ unsigned long long sfix[kFixGroups * 29][kFixSlots];
   __shared__ int abort_wait;  // a grid barrier gave up
   if (a.skip_flag && *a.skip_flag != 0) return;  // uniform across the grid
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const bool solver = blockIdx.x == 0;
   if (threadIdx.x == 0) {
     ctl_begin(ctl, a.last_pose);
     s_solve_marks = nullptr;
     abort_wait = 0;
+    made = 0;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    pose_to_float_warp(ctl.next_pose, ctl.last_pose, pose);
+    if (lane < 12) nff[lane] = spec::split(ctl.next_pose[lane]);
   }
   __syncthreads();
   const int nb = gridDim.x;
-  // Warp w of CTA b takes the 32-pixel runs w * nb + b (+ multiples of the
-  // grid): every CTA's work is spread over the whole image, which evens out
-  // the CTAs' arrival at the barrier; each warp's loads stay coalesced.
-  const int gtid = ((threadIdx.x >> 5) * nb + blockIdx.x) * 32 + (threadIdx.x & 31);
-  const int gstride = nb * blockDim.x;
-  int set = 0, it = 0;  // set = it % 3
-  for (int l = a.levels - 1; l >= 0; --l) {
-    const IcpLevelArgs &L = a.lv[l];
-    for (int j = 0; j < L.iters; ++j, ++it) {
-      prof_mark(a, it, 0);
-      if (threadIdx.x < 32) pose_to_float_warp(ctl.next_pose, ctl.last_pose, pose);
-      if (RGB && threadIdx.x < 2) s2[threadIdx.x] = 0u;
-      __syncthreads();
-      float acc[29];
-      icp_accumulate(L, pose, gtid, gstride, acc);
-      unsigned cnt = 0u, ssq = 0u;
-      if (RGB) rgb_residual_pass(L, a.rg[l], pose, gtid, gstride, cnt, ssq);
-      prof_mark(a, it, 1);
-      block_reduce29<kPWarps>(acc, wpart, bsum);
-      const int group = blockIdx.x % kFixGroups;
-      unsigned long long *fx = a.fix + (size_t)set * kFixSet;
-      if (threadIdx.x < 29) fix_add(fx + (group * 29 + threadIdx.x) * kFixSlots, bsum[threadIdx.x]);
-      unsigned *rres = a.rgb_res + (size_t)set * kFixGroups * 2;
-      if (RGB) {
-        block_sum2(cnt, ssq, s2);
-        if (threadIdx.x < 2) atomicAdd(rres + group * 2 + threadIdx.x, s2[threadIdx.x]);
-      }
-      prof_mark(a, it, 2);
-      grid_barrier(a, nb, RGB ? 2 * it : it, &abort_wait);
-      if (abort_wait) break;  // uniform: read after the barrier's __syncthreads
-      prof_mark(a, it, 3);
-      unsigned long long *fxr = a.fix_rgb + (size_t)set * kFixSet;
-      if (RGB) {
-        // sigma from the grid's count and sum of diff^2, then the rows
-        if (threadIdx.x < 32) {
-          const int lane = threadIdx.x;
-          const unsigned v = lane < kFixGroups * 2 ? __ldcg(rres + lane) : 0u;
-          const unsigned c2 = __reduce_add_sync(0xffffffffu, (lane & 1) ? 0u : v);
-          const unsigned q2 = __reduce_add_sync(0xffffffffu, (lane & 1) ? v : 0u);
-          if (lane == 0) { s2[0] = c2; s2[1] = q2; }
+  // Warp w of pixel CTA b takes the 32-pixel runs w * (nb - 1) + b - 1 (+
+  // multiples of the pixel CTAs' threads): every CTA's work is spread over
+  // the whole image, which evens out the CTAs' arrival at the barrier;
+  // each warp's loads stay coalesced.
+  const int gtid = (warp * (nb - 1) + (int)blockIdx.x - 1) * 32 + lane;
+  const int gstride = (nb - 1) * kPThreads;
+  IcpPub *const pubs = reinterpret_cast<IcpPub *>(a.pub);
+  int l = a.levels - 1;  // level of iteration it (-1: none left)
+  while (l >= 0 && a.lv[l].iters == 0) --l;
+  int j = 0, it = 0, round = 0, set = 0;  // set = round % 3
+  int sl = 0;             // level of the iteration whose sums are in `sums`
+  bool predict = false;   // this round's rows go on a prediction (the sums of iteration it - 1 are in hand)
+  for (;;) {
+    const bool have = l >= 0;
+    if (have) prof_mark(a, it, 0);
+    if (predict) {
+      if (solver) {
+        // the FP64 solve of iteration it - 1, and the same prediction as the
+        // pixel CTAs make (to check it after the barrier)
+        if (warp < 3) {
+          if (threadIdx.x == 0)
+            s_solve_marks = (a.prof && it - 1 < kProfIters) ? a.prof + (it - 1) * kProfSlots + 8 : nullptr;
+          __syncwarp();
+          ctl_step_fast(ctl, sums, a.lv[sl].min_count, ssolve, RGB ? rsums : nullptr);
+        } else if (warp == 3) {
+          const bool m = a.predict && have && spec::predict_pose_warp(sums, nff, spred);
+          if (lane == 0) made = m;
         }
         __syncthreads();
-        bool tiny;
-        const float sigma = rgb_sigma(s2[0], s2[1], tiny);
-        rgb_rows_pass(L, a.rg[l], sigma, tiny, gtid, gstride, acc);
-        block_reduce29<kPWarps>(acc, wpart, bsum);
-        if (threadIdx.x < 29) fix_add(fxr + (group * 29 + threadIdx.x) * kFixSlots, bsum[threadIdx.x]);
-        grid_barrier(a, nb, 2 * it + 1, &abort_wait);
-        if (abort_wait) break;
+        if (!have) break;  // the last iteration's solve: done
+        if (threadIdx.x < 12) __stcg(&pubs[set].pose[threadIdx.x], ctl.next_pose[threadIdx.x]);
+        if (threadIdx.x == 0) __stcg(&pubs[set].stop, ctl.stop);
+      } else {
+        if (!have) break;  // the solving CTA finishes alone
+        if (warp == 0) {
+          const bool m = a.predict && spec::predict_pose_warp(sums, nff, spred);
+          if (m && lane < 12) {  // the last pose's parts of pose stay as they are
+            const int i = lane >> 2, c = lane & 3;
+            if (c < 3) {
+              (&pose.Rc.rx.x)[i * 3 + c] = spred[lane];
+              (&pose.RcI.rx.x)[c * 3 + i] = spred[lane];
+            } else {
+              (&pose.tc.x)[i] = spred[lane];
+            }
+          }
+          if (lane == 0) made = m;
+        }
+        __syncthreads();
       }
-      read_fix_set(fx, sfix, sums, RGB);
+    }
+    const bool rows = !solver && (!predict || made);
+    if (a.prof && blockIdx.x == 1 && threadIdx.x == 0 && it < kProfIters) a.prof[it * kProfSlots + 14] = prof_clock();
+    float acc[29];
+    unsigned cnt = 0u, ssq = 0u;
+    if (rows) {
+      icp_accumulate(a.lv[l], pose, gtid, gstride, acc);
+      if (RGB) rgb_residual_pass(a.lv[l], a.rg[l], pose, gtid, gstride, cnt, ssq);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 29; ++k) acc[k] = 0.f;
+    }
+    if (RGB && threadIdx.x < 2) s2[threadIdx.x] = 0u;
+    prof_mark(a, it, 1);
+    const int group = blockIdx.x % kFixGroups;
+    unsigned long long *fx = a.fix + (size_t)set * kFixSet;
+    unsigned *rres = a.rgb_res + (size_t)set * kFixGroups * 2;
+    if (!solver) {  // uniform over the CTA (the solving CTA adds nothing)
+      block_reduce29<kPWarps>(acc, wpart, bsum);
+      if (rows && threadIdx.x < 29) fix_add(fx + (group * 29 + threadIdx.x) * kFixSlots, bsum[threadIdx.x]);
       if (RGB) {
-        read_fix_set(fxr, sfix, rsums, true);
-        // A = A_rgb w + A_icp, b = b_rgb w + b_icp (Tracking.cc:484-487)
-        if (threadIdx.x < 27) sums[threadIdx.x] = __dadd_rn(__dmul_rn(rsums[threadIdx.x], (double)1e-4f), sums[threadIdx.x]);
+        block_sum2(cnt, ssq, s2);
+        if (rows && threadIdx.x < 2) atomicAdd(rres + group * 2 + threadIdx.x, s2[threadIdx.x]);
       }
-      // Every CTA read the previous iteration's sets before it arrived here,
-      // so CTA 0 clears them for iteration it + 2; its clearing is released
-      // with its next arrival, before anyone can add into them.
-      const int prev = set == 0 ? 2 : set - 1;
-      if (blockIdx.x == 0) {
-        for (int k = threadIdx.x; k < kFixSet; k += blockDim.x) __stcg(a.fix + (size_t)prev * kFixSet + k, 0ull);
-        if (RGB) {
-          for (int k = threadIdx.x; k < kFixSet; k += blockDim.x) __stcg(a.fix_rgb + (size_t)prev * kFixSet + k, 0ull);
-          if (threadIdx.x < kFixGroups * 2) __stcg(a.rgb_res + (size_t)prev * kFixGroups * 2 + threadIdx.x, 0u);
+    }
+    prof_mark(a, it, 2);
+    grid_barrier(a, nb, RGB ? 2 * round : round, &abort_wait);
+    if (abort_wait) break;  // uniform: read after the barrier's __syncthreads
+    prof_mark(a, it, 3);
+    unsigned long long *fxr = a.fix_rgb + (size_t)set * kFixSet;
+    if (RGB) {
+      // sigma from the grid's count and sum of diff^2, then the rows
+      if (threadIdx.x < 32) {
+        const unsigned v = lane < kFixGroups * 2 ? __ldcg(rres + lane) : 0u;
+        const unsigned c2 = __reduce_add_sync(0xffffffffu, (lane & 1) ? 0u : v);
+        const unsigned q2 = __reduce_add_sync(0xffffffffu, (lane & 1) ? v : 0u);
+        if (lane == 0) { s2[0] = c2; s2[1] = q2; }
+      }
+      __syncthreads();
+      bool tiny;
+      const float sigma = rgb_sigma(s2[0], s2[1], tiny);
+      if (!solver) {
+        if (rows) {
+          rgb_rows_pass(a.lv[l], a.rg[l], sigma, tiny, gtid, gstride, acc);
+        } else {
+#pragma unroll
+          for (int k = 0; k < 29; ++k) acc[k] = 0.f;
+        }
+        block_reduce29<kPWarps>(acc, wpart, bsum);
+        if (rows && threadIdx.x < 29) fix_add(fxr + (group * 29 + threadIdx.x) * kFixSlots, bsum[threadIdx.x]);
+      }
+      grid_barrier(a, nb, 2 * round + 1, &abort_wait);
+      if (abort_wait) break;
+    }
+    // the solving CTA's pose, loaded beside the accumulator sets
+    double P = 0.0;
+    int P_stop = 0;
+    if (predict && warp == 0) {
+      if (lane < 12) P = __ldcg(&pubs[set].pose[lane]);
+      if (lane == 0) P_stop = __ldcg(&pubs[set].stop);
+    }
+    read_fix_set(fx, sfix, sums, RGB);
+    if (RGB) {
+      read_fix_set(fxr, sfix, rsums, true);
+      // A = A_rgb w + A_icp, b = b_rgb w + b_icp (Tracking.cc:484-487)
+      if (threadIdx.x < 27) sums[threadIdx.x] = __dadd_rn(__dmul_rn(rsums[threadIdx.x], (double)1e-4f), sums[threadIdx.x]);
+    }
+    // Every CTA read the previous round's sets before it arrived here, so
+    // CTA 0 clears them for round + 2; its clearing is released with its
+    // next arrival, before anyone can add into them.
+    const int prev = set == 0 ? 2 : set - 1;
+    if (solver) {
+      for (int k = threadIdx.x; k < kFixSet; k += blockDim.x) __stcg(a.fix + (size_t)prev * kFixSet + k, 0ull);
+      if (RGB) {
+        for (int k = threadIdx.x; k < kFixSet; k += blockDim.x) __stcg(a.fix_rgb + (size_t)prev * kFixSet + k, 0ull);
+        if (threadIdx.x < kFixGroups * 2) __stcg(a.rgb_res + (size_t)prev * kFixGroups * 2 + threadIdx.x, 0u);
+      }
+    }
+    if (predict && warp == 0) {
+      // the published FP64 pose: its float form against the prediction
+      const float f = (float)P;
+      const bool same = lane >= 12 || __float_as_uint(f) == __float_as_uint(spred[lane]);
+      const bool agree = __all_sync(0xffffffffu, same);
+      if (lane < 12) {
+        nff[lane] = spec::split(P);
+        if (!(made && agree)) {  // the next round accumulates on this pose
+          const int i = lane >> 2, c = lane & 3;
+          if (c < 3) {
+            (&pose.Rc.rx.x)[i * 3 + c] = f;
+            (&pose.RcI.rx.x)[c * 3 + i] = f;
+          } else {
+            (&pose.tc.x)[i] = f;
+          }
         }
       }
-      __syncthreads();
-      prof_mark(a, it, 4);
-      if (threadIdx.x == 0)
-        s_solve_marks = (a.prof && blockIdx.x == 0 && it < kProfIters) ? a.prof + it * kProfSlots + 8 : nullptr;
-      __syncwarp();
-      if (threadIdx.x < 96) ctl_step_fast(ctl, sums, L.min_count, ssolve, RGB ? rsums : nullptr);
-      __syncthreads();
-      prof_mark(a, it, 5);
-      set = set == 2 ? 0 : set + 1;
-      if (ctl.stop) break;
+      if (lane == 0) {
+        pub_stop = P_stop;
+        hit = made && agree;
+      }
     }
-    if (ctl.stop || abort_wait) break;
+    __syncthreads();
+    prof_mark(a, it, 4);
+    set = set == 2 ? 0 : set + 1;
+    ++round;
+    if (predict) {
+      if (pub_stop) break;  // the solve of iteration it - 1 ended the iterations
+      if (!hit) {           // the rows again, on the FP64 pose
+        if (a.prof && blockIdx.x == 1 && threadIdx.x == 0 && it < kProfIters) a.prof[it * kProfSlots + 7] = 0;
+        predict = false;
+        continue;
+      }
+    }
+    if (a.prof && blockIdx.x == 1 && threadIdx.x == 0 && it < kProfIters) a.prof[it * kProfSlots + 7] = predict;
+    // the sums of iteration it are in hand
+    predict = true;
+    sl = l;
+    int nl = 0, nj = 0;
+    if (next_iteration(a, l, j, &nl, &nj)) {
+      l = nl;
+      j = nj;
+    } else {
+      l = -1;
+    }
+    ++it;
   }
+  if (!solver) return;
   if (threadIdx.x == 0) {
     s_solve_marks = nullptr;
     if (abort_wait) {  // a barrier gave up: the tracking failed
@@ -724,7 +890,7 @@ __global__ void __launch_bounds__(kPThreads, 1) k_icp_persistent(PersistentArgs 
   __syncwarp();
   if (threadIdx.x < 32) ctl_finish_fast(ctl, a.thresh, ssolve);
   __syncthreads();
-  if (threadIdx.x == 0 && blockIdx.x == 0) *a.ctl = ctl;
+  if (threadIdx.x == 0) *a.ctl = ctl;
 }
 
 // Plain form, launch 1: per-CTA FP64 partials.
@@ -883,7 +1049,9 @@ __global__ void __launch_bounds__(32) k_vp_finish(TrackCtl *ctl_g, const int *sr
 // arrival count (256 B), ICP accumulator sets, photometric accumulator
 // sets, photometric count / sum of diff^2 sets
 constexpr size_t kFixBytes = sizeof(unsigned long long) * 3 * kFixSet;
-constexpr size_t kBarrierBytes = 256 + 2 * kFixBytes + sizeof(unsigned) * 3 * kFixGroups * 2;
+constexpr size_t kResBytes = sizeof(unsigned) * 3 * kFixGroups * 2;
+constexpr size_t kPubBytes = 3 * 128;  // IcpPub per accumulator set
+constexpr size_t kBarrierBytes = 256 + 2 * kFixBytes + kResBytes + kPubBytes;
 
 cudaError_t icp_persistent_reset(const IcpWorkspace &w, cudaStream_t s) {
   return cudaMemsetAsync(w.barrier, 0, kBarrierBytes, s);
@@ -912,6 +1080,7 @@ int icp_workspace_init(IcpWorkspace &w) {
   w.fix = reinterpret_cast<unsigned long long *>(base + 256);
   w.fix_rgb = reinterpret_cast<unsigned long long *>(base + 256 + kFixBytes);
   w.rgb_res = reinterpret_cast<unsigned *>(base + 256 + 2 * kFixBytes);
+  w.pub = base + 256 + 2 * kFixBytes + kResBytes;
   if (cudaMalloc(&w.ctl, sizeof(TrackCtl)) != cudaSuccess) return SF_ERR_CUDA;
   if (cudaMalloc(&w.prof, sizeof(unsigned long long) * kProfSlots * kProfIters) != cudaSuccess) return SF_ERR_CUDA;
   if (cudaMemset(w.prof, 0, sizeof(unsigned long long) * kProfSlots * kProfIters) != cudaSuccess) return SF_ERR_CUDA;
@@ -1016,6 +1185,9 @@ cudaError_t launch_icp_persistent(const IcpWorkspace &w, const IcpLevelArgs *lev
   a.prof = w.profile ? w.prof : nullptr;
   a.poll_limit = w.barrier_poll_limit;
   a.extra_arrivals = w.barrier_extra;
+  a.predict = w.predict;
+  a.pub = w.pub;
+  if ((rgb ? w.max_blocks_rgb : w.max_blocks) < 2) return cudaErrorInvalidConfiguration;  // a solving CTA and pixel CTAs
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(rgb ? w.max_blocks_rgb : w.max_blocks);
   cfg.blockDim = dim3(kPThreads);

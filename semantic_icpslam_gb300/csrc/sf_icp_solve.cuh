@@ -202,7 +202,7 @@ __device__ __forceinline__ int ctl_decide(TrackCtl &c, const double *sums, int m
 // sf::ctl_step; warp 0 returns whether to go on.  With the photometric
 // term, sums[0..26] already hold the combined system and rsums the RGB
 // sums (for its error and count).
-__device__ bool ctl_step_fast(TrackCtl &c, const double *sums, int min_count, IcpSolveSmem &s,
+__device__ __noinline__ bool ctl_step_fast(TrackCtl &c, const double *sums, int min_count, IcpSolveSmem &s,
                               const double *rsums = nullptr) {
   const int lane = threadIdx.x & 31;
   if (threadIdx.x >= 64) {  // warp 2
@@ -336,7 +336,7 @@ __device__ bool ctl_step_fast(TrackCtl &c, const double *sums, int min_count, Ic
 // the matrix entries instead of asin / atan2 / sin: sin b = r02,
 // |sin a| = |r12| / |(r12, r22)|, |sin c| = |r01| / |(r00, r01)|, the same
 // for both of Eigen's solution branches.
-__device__ void ctl_finish_fast(TrackCtl &c, float thresh, IcpSolveSmem &s) {
+__device__ __noinline__ void ctl_finish_fast(TrackCtl &c, float thresh, IcpSolveSmem &s) {
   const int lane = threadIdx.x & 31;
   if (c.stop == 1) {
     if (lane == 0) c.accepted = 0;

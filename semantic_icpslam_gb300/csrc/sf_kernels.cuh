@@ -73,6 +73,8 @@ struct IcpWorkspace {
   // grid barrier bounds of the persistent kernel (sf_icp_barrier_limits)
   unsigned barrier_poll_limit = 1u << 22;
   unsigned barrier_extra = 0;
+  int predict = 1;  // next-pose prediction of the persistent kernel (sf_icp_predict)
+  void *pub = nullptr;  // persistent kernel: the solving CTA's publications (inside barrier)
   // photometric scratch, grown on demand: correspondences of the largest
   // level, and candidate flags of every level for callers that pass none
   float4 *corr = nullptr;
