@@ -1013,7 +1013,9 @@ int sf_system_autotune(sf_system *s, int reps, sf_autotune_report *report) {
   // the raycast rerun with the frame's shape, which rewrites the same model
   // maps: the loop's state is unchanged.
   unsigned nvis = 0;
+  int win[6] = {0, 0, 0, 0, 0, 0};
   cudaError_t e = cudaMemcpyAsync(&nvis, m.no_visible, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(win, f.win, sizeof(win), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return SF_ERR_CUDA;
   nvis = nvis < m.c.num_entries ? nvis : m.c.num_entries;
@@ -1026,9 +1028,16 @@ int sf_system_autotune(sf_system *s, int reps, sf_autotune_report *report) {
   if (e == cudaSuccess) e = cudaMalloc(&flush, flush_bytes);
   if (e == cudaSuccess && fuse) e = cudaMalloc(&save, (size_t)nvis * 512 * sizeof(sf_voxel));
   if (e == cudaSuccess && fuse) launch_save_visible(m, save, nvis, false, st);
+  // the frame's visibility pass has just written the block-pointer window
+  // when its integration and raycast run: after the flush, the window is
+  // read back into L2 (copied into the flush buffer) to stand in for it
+  const size_t win_bytes = sizeof(int) * (size_t)win[3] * (size_t)win[4] * (size_t)win[5];
   auto prepare = [&]() {
     if (fuse) launch_save_visible(m, save, nvis, true, st);
-    return cudaMemsetAsync(flush, 0, flush_bytes, st);
+    cudaError_t q = cudaMemsetAsync(flush, 0, flush_bytes, st);
+    if (q == cudaSuccess && win_bytes > 0 && win_bytes <= flush_bytes)
+      q = cudaMemcpyAsync(flush, f.win_cells, win_bytes, cudaMemcpyDeviceToDevice, st);
+    return q;
   };
   auto timed = [&](auto &&launch, float &ms_out) {
     float total = 0.f;
