@@ -352,7 +352,40 @@ __device__ void create_block_serial(DevMap &m, i3 p, uint32_t bucket, uint32_t *
   }
 }
 
-__global__ void k_alloc_insert(DevMap m, FuseScratch f, const int *run_flag, uint32_t *flags) {
+// Start of the visibility pass: resets the visible count and the rendered
+// flag, sets the frame's block-pointer window (each CTA computes it for
+// itself; CTA 0 publishes it for the later passes), then clears the window
+// cells and (when given) the z-range images.  Run by every thread of the
+// grid; win is shared memory of the calling CTA.
+__device__ __forceinline__ void vis_start(const DevMap &m, const FuseScratch &f, const Cam *cam, unsigned *rendered,
+                                          const sf_image &zmin, const sf_image &zmax, int do_z, int *win) {
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 8; ++k) win[k] = 0;
+    window_setup(*cam, m.c.block_width, m.c.depth_min, m.c.depth_max, f.win_cap, win);
+    if (blockIdx.x == 0) {
+      *m.no_visible = 0u;
+      if (rendered) *rendered = 0u;
+      for (int k = 0; k < 6; ++k) f.win[k] = win[k];
+    }
+  }
+  __syncthreads();
+  const unsigned ncell = (unsigned)win[3] * (unsigned)win[4] * (unsigned)win[5];
+  const unsigned nz = do_z ? (unsigned)(zmin.cols * zmin.rows) : 0u;
+  const unsigned n = ncell > nz ? ncell : nz;
+  for (unsigned i = grid_tid(); i < n; i += grid_stride()) {
+    if (i < ncell) f.win_cells[i] = -1;
+    if (i < nz) {
+      const int y = (int)(i / (unsigned)zmin.cols), x = (int)(i % (unsigned)zmin.cols);
+      row_ptr<float>(zmin, y)[x] = 100.f;
+      row_ptr<float>(zmax, y)[x] = 0.f;
+    }
+  }
+}
+
+// With vs.on, the next visibility pass's start (vis_start) follows the
+// inserts in the same launch: it touches none of the entries, heap or
+// request set the inserts use.
+__global__ void k_alloc_insert(DevMap m, FuseScratch f, const int *run_flag, uint32_t *flags, VisStartArgs vs) {
   if (run_flag && *run_flag == 0) return;
   const unsigned ndirty = min(f.counters[1], f.pend_cap);
   for (unsigned d = grid_tid(); d < ndirty; d += grid_stride()) {
@@ -372,6 +405,10 @@ __global__ void k_alloc_insert(DevMap m, FuseScratch f, const int *run_flag, uin
   // now (the probe pass is over), so no entry of 65535 frames ago matches.
   if (f.counters[2] == 0xffffu)
     for (unsigned i = grid_tid(); i < f.req_cap; i += grid_stride()) f.req_set[i] = 0ull;
+  if (vs.on) {
+    __shared__ int win[8];
+    vis_start(m, f, vs.cam, vs.rendered, vs.zmin, vs.zmax, vs.do_z, win);
+  }
 }
 
 // Clears the per-frame counters and advances the request epoch.  The
@@ -460,36 +497,11 @@ __global__ void k_zrange_init(sf_image zmin, sf_image zmax) {
   row_ptr<float>(zmax, y)[x] = 0.f;
 }
 
-// Per-frame start of the visibility pass: counters and the window box.
-// Start of the visibility pass: resets the visible count and the rendered
-// flag, sets the frame's block-pointer window (each CTA computes it for
-// itself; CTA 0 publishes it for the later passes), then clears the window
-// cells and (when given) the z-range images.
 __global__ void k_vis_start(DevMap m, FuseScratch f, const Cam *cam, unsigned *rendered, sf_image zmin,
                             sf_image zmax, int do_z, const int *run_flag) {
   if (run_flag && *run_flag == 0) return;
   __shared__ int win[8];
-  if (threadIdx.x == 0) {
-    for (int k = 0; k < 8; ++k) win[k] = 0;
-    window_setup(*cam, m.c.block_width, m.c.depth_min, m.c.depth_max, f.win_cap, win);
-    if (blockIdx.x == 0) {
-      *m.no_visible = 0u;
-      if (rendered) *rendered = 0u;
-      for (int k = 0; k < 6; ++k) f.win[k] = win[k];
-    }
-  }
-  __syncthreads();
-  const unsigned ncell = (unsigned)win[3] * (unsigned)win[4] * (unsigned)win[5];
-  const unsigned nz = do_z ? (unsigned)(zmin.cols * zmin.rows) : 0u;
-  const unsigned n = ncell > nz ? ncell : nz;
-  for (unsigned i = grid_tid(); i < n; i += grid_stride()) {
-    if (i < ncell) f.win_cells[i] = -1;
-    if (i < nz) {
-      const int y = (int)(i / (unsigned)zmin.cols), x = (int)(i % (unsigned)zmin.cols);
-      row_ptr<float>(zmin, y)[x] = 100.f;
-      row_ptr<float>(zmax, y)[x] = 0.f;
-    }
-  }
+  vis_start(m, f, cam, rendered, zmin, zmax, do_z, win);
 }
 
 // UpdateVisibility + CreateRenderingBlocks' z-range for n candidate
@@ -1009,13 +1021,23 @@ void launch_alloc_probe(const DevMap &m, const FuseScratch &f, const sf_image &d
 }
 
 void launch_alloc(const DevMap &m, const FuseScratch &f, const sf_image &depth, const Cam *c,
-                  const int *run_flag, uint32_t *flags, cudaStream_t s, bool begin, int tile) {
+                  const int *run_flag, uint32_t *flags, cudaStream_t s, bool begin, int tile,
+                  const sf_image *vis_zmin, const sf_image *vis_zmax) {
   if (begin) {
     k_alloc_begin<<<1, 1, 0, s>>>(f, run_flag);
     note_launch();
   }
   launch_alloc_probe(m, f, depth, c, run_flag, flags, s, tile);
-  k_alloc_insert<<<sm_count() * 2, 128, 0, s>>>(m, f, run_flag, flags); note_launch();
+  VisStartArgs vs = {};
+  if (vis_zmin && vis_zmax) {
+    vs.on = 1;
+    vs.cam = c;
+    vs.rendered = f.counters + 3;
+    vs.zmin = *vis_zmin;
+    vs.zmax = *vis_zmax;
+    vs.do_z = 1;
+  }
+  k_alloc_insert<<<sm_count() * 2, 128, 0, s>>>(m, f, run_flag, flags, vs); note_launch();
 }
 
 void launch_zrange_init(const sf_image &zmin, const sf_image &zmax, cudaStream_t s) {
@@ -1026,11 +1048,14 @@ void launch_zrange_init(const sf_image &zmin, const sf_image &zmax, cudaStream_t
 
 void launch_visibility(const DevMap &m, const FuseScratch &f, const Cam *c, const sf_image *zmin,
                        const sf_image *zmax, const int *run_flag, uint32_t *flags,
-                       cudaStream_t s) {
+                       cudaStream_t s, bool started) {
   unsigned *rendered = f.counters + 3;
   const bool do_z = zmin && zmax;
   sf_image zn = do_z ? *zmin : sf_image{}, zx = do_z ? *zmax : sf_image{};
-  k_vis_start<<<sm_count() * 8, 256, 0, s>>>(m, f, c, rendered, zn, zx, do_z ? 1 : 0, run_flag); note_launch();
+  if (!started) {
+    k_vis_start<<<sm_count() * 8, 256, 0, s>>>(m, f, c, rendered, zn, zx, do_z ? 1 : 0, run_flag);
+    note_launch();
+  }
   k_visibility<<<sm_count() * 4, 256, 0, s>>>(m, f, c, zn, zx, do_z ? 1 : 0, rendered, run_flag,
                                               flags); note_launch();
 }

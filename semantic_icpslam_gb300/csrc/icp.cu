@@ -15,7 +15,7 @@
 // same pose without a second barrier.  Accumulators rotate over three sets.
 #include <mutex>
 
-#include "sf_kernels.cuh"
+#include "sf_frame.cuh"
 
 // Tracing slots of the solve phases (set per iteration in CTA 0 when
 // tracing is on, else null); read by SF_SOLVE_MARK inside the solve.
@@ -544,6 +544,7 @@ struct PersistentArgs {
                              // every wait run out)
   int predict;               // predict each iteration's pose and accumulate its rows during the solve
   void *pub;                 // [3] IcpPub: the solving CTA's pose and decision per accumulator set
+  FramePost post;            // the frame loop's state update at the end (post.sys null: none)
 };
 
 // Phase clocks of the first pixel CTA (SM cycles), per iteration (the
@@ -688,7 +689,10 @@ __global__ void __launch_bounds__(kPThreads, 1) k_icp_persistent(PersistentArgs 
   __shared__ ff wpart[kPWarps][33];
   __shared__ unsigned long long sfix[kFixGroups * 29][kFixSlots];
   __shared__ int abort_wait;  // a grid barrier gave up
-  if (a.skip_flag && *a.skip_flag != 0) return;  // uniform across the grid
+  if (a.skip_flag && *a.skip_flag != 0) {  // uniform across the grid
+    if (a.post.sys && blockIdx.x == 0 && threadIdx.x == 0) sys_post(a.post.sys, *a.ctl, a.post.tmpl, a.post.f);
+    return;
+  }
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const bool solver = blockIdx.x == 0;
   if (threadIdx.x == 0) {
@@ -890,7 +894,10 @@ __global__ void __launch_bounds__(kPThreads, 1) k_icp_persistent(PersistentArgs 
   __syncwarp();
   if (threadIdx.x < 32) ctl_finish_fast(ctl, a.thresh, ssolve);
   __syncthreads();
-  if (threadIdx.x == 0) *a.ctl = ctl;
+  if (threadIdx.x == 0) {
+    *a.ctl = ctl;
+    if (a.post.sys) sys_post(a.post.sys, ctl, a.post.tmpl, a.post.f);
+  }
 }
 
 // Plain form, launch 1: per-CTA FP64 partials.
@@ -1166,8 +1173,10 @@ void launch_icp_step(const IcpWorkspace &w, const IcpLevelArgs &L, const m3 &Rc,
 
 cudaError_t launch_icp_persistent(const IcpWorkspace &w, const IcpLevelArgs *levels, int nlevels,
                                   float thresh, const double *last_pose, const int *skip_flag,
-                                  uint32_t *flags, cudaStream_t s, const RgbLevelArgs *rgb) {
+                                  uint32_t *flags, cudaStream_t s, const RgbLevelArgs *rgb,
+                                  const FramePost *post) {
   PersistentArgs a = {};
+  if (post) a.post = *post;
   for (int l = 0; l < nlevels && l < kMaxLevels; ++l) {
     a.lv[l] = levels[l];
     if (rgb) a.rg[l] = rgb[l];

@@ -338,36 +338,67 @@ __global__ void k_nmap(sf_image vmap, sf_image nmap) {
 
 // ResizeMapKernel (Pyrdown.cu:318-346): 2x2 mean, any NaN -> NaN; normals
 // normalised as float4 (w included in the norm, VectorMath.h:328-346).
-// Guarded on the destination size (the reference guards on the source).
+__device__ __forceinline__ float4 resize_vertex(float4 a, float4 b, float4 c, float4 d) {
+  if (isnan(a.x) || isnan(b.x) || isnan(c.x) || isnan(d.x)) return nan4();
+  float4 out;
+  out.x = (((a.x + b.x) + c.x) + d.x) / 4.0f;
+  out.y = (((a.y + b.y) + c.y) + d.y) / 4.0f;
+  out.z = (((a.z + b.z) + c.z) + d.z) / 4.0f;
+  out.w = (((a.w + b.w) + c.w) + d.w) / 4.0f;
+  return out;
+}
+
+__device__ __forceinline__ float4 resize_normal(float4 a, float4 b, float4 c, float4 d) {
+  if (isnan(a.x) || isnan(b.x) || isnan(c.x) || isnan(d.x)) return nan4();
+  float s0 = (((a.x + b.x) + c.x) + d.x) / 4.0f;
+  float s1 = (((a.y + b.y) + c.y) + d.y) / 4.0f;
+  float s2 = (((a.z + b.z) + c.z) + d.z) / 4.0f;
+  float s3 = (((a.w + b.w) + c.w) + d.w) / 4.0f;
+  float len = sqrtf(s0 * s0 + s1 * s1 + s2 * s2 + s3 * s3);
+  return make_float4(s0 / len, s1 / len, s2 / len, s3 / len);
+}
+
+// One destination pixel.  Guarded on the destination size (the reference
+// guards on the source).
 __device__ __forceinline__ void resize_px(const sf_image &vsrc, const sf_image &nsrc, const sf_image &vdst,
                                           const sf_image &ndst, int x, int y) {
   const float4 *v0 = row_ptr<const float4>(vsrc, 2 * y) + 2 * x;
   const float4 *v1 = row_ptr<const float4>(vsrc, 2 * y + 1) + 2 * x;
   const float4 *n0 = row_ptr<const float4>(nsrc, 2 * y) + 2 * x;
   const float4 *n1 = row_ptr<const float4>(nsrc, 2 * y + 1) + 2 * x;
-  float4 a = v0[0], b = v0[1], c = v1[0], d = v1[1];
-  float4 out;
-  if (isnan(a.x) || isnan(b.x) || isnan(c.x) || isnan(d.x)) {
-    out = nan4();
-  } else {
-    out.x = (((a.x + b.x) + c.x) + d.x) / 4.0f;
-    out.y = (((a.y + b.y) + c.y) + d.y) / 4.0f;
-    out.z = (((a.z + b.z) + c.z) + d.z) / 4.0f;
-    out.w = (((a.w + b.w) + c.w) + d.w) / 4.0f;
+  row_ptr<float4>(vdst, y)[x] = resize_vertex(v0[0], v0[1], v1[0], v1[1]);
+  row_ptr<float4>(ndst, y)[x] = resize_normal(n0[0], n0[1], n1[0], n1[1]);
+}
+
+// Two ResizeMap levels in one launch (level 0 -> 1 -> 2): thread (x, y)
+// makes the level-1 pixels (2x + i, 2y + j) that exist and, from those four
+// values, level-2 pixel (x, y) when it exists; the same operations as two
+// k_resize launches, so the maps are bit-identical.  The grid covers level
+// 1 in 2x2 cells (an odd level-1 size leaves its last column or row to
+// threads without a level-2 pixel).
+__global__ void k_resize2(sf_image v0, sf_image n0, sf_image v1, sf_image n1, sf_image v2, sf_image n2) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (2 * x >= v1.cols || 2 * y >= v1.rows) return;
+  float4 pv[4], pn[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int px = 2 * x + (k & 1), py = 2 * y + (k >> 1);
+    if (px < v1.cols && py < v1.rows) {
+      const float4 *a = row_ptr<const float4>(v0, 2 * py) + 2 * px;
+      const float4 *b = row_ptr<const float4>(v0, 2 * py + 1) + 2 * px;
+      const float4 *c = row_ptr<const float4>(n0, 2 * py) + 2 * px;
+      const float4 *d = row_ptr<const float4>(n0, 2 * py + 1) + 2 * px;
+      pv[k] = resize_vertex(a[0], a[1], b[0], b[1]);
+      pn[k] = resize_normal(c[0], c[1], d[0], d[1]);
+      row_ptr<float4>(v1, py)[px] = pv[k];
+      row_ptr<float4>(n1, py)[px] = pn[k];
+    }
   }
-  row_ptr<float4>(vdst, y)[x] = out;
-  a = n0[0]; b = n0[1]; c = n1[0]; d = n1[1];
-  if (isnan(a.x) || isnan(b.x) || isnan(c.x) || isnan(d.x)) {
-    out = nan4();
-  } else {
-    float s0 = (((a.x + b.x) + c.x) + d.x) / 4.0f;
-    float s1 = (((a.y + b.y) + c.y) + d.y) / 4.0f;
-    float s2 = (((a.z + b.z) + c.z) + d.z) / 4.0f;
-    float s3 = (((a.w + b.w) + c.w) + d.w) / 4.0f;
-    float len = sqrtf(s0 * s0 + s1 * s1 + s2 * s2 + s3 * s3);
-    out = make_float4(s0 / len, s1 / len, s2 / len, s3 / len);
+  if (x < v2.cols && y < v2.rows) {
+    row_ptr<float4>(v2, y)[x] = resize_vertex(pv[0], pv[1], pv[2], pv[3]);
+    row_ptr<float4>(n2, y)[x] = resize_normal(pn[0], pn[1], pn[2], pn[3]);
   }
-  row_ptr<float4>(ndst, y)[x] = out;
 }
 
 __global__ void k_resize(sf_image vsrc, sf_image nsrc, sf_image vdst, sf_image ndst) {
@@ -485,6 +516,13 @@ void launch_resize(const sf_image &vsrc, const sf_image &nsrc, const sf_image &v
                    const sf_image &ndst, cudaStream_t s) {
   dim3 blk(32, 8);
   k_resize<<<grid2d(vdst.cols, vdst.rows, blk), blk, 0, s>>>(vsrc, nsrc, vdst, ndst); note_launch();
+}
+
+void launch_resize2(const sf_image &v0, const sf_image &n0, const sf_image &v1, const sf_image &n1,
+                    const sf_image &v2, const sf_image &n2, cudaStream_t s) {
+  const dim3 blk(16, 8);
+  k_resize2<<<grid2d((v1.cols + 1) / 2, (v1.rows + 1) / 2, blk), blk, 0, s>>>(v0, n0, v1, n1, v2, n2);
+  note_launch();
 }
 
 void launch_resize_batch(const sf_image &vsrc, const sf_image &nsrc, const sf_image &vdst, const sf_image &ndst,

@@ -11,7 +11,7 @@
 // reference's CAS-loop float min/max become single integer atomicMin/Max
 // on the bit patterns.  The raycast reads only the first 8 bytes of a
 // voxel (sdf, weight) per sample.
-#include "sf_kernels.cuh"
+#include "sf_frame.cuh"
 #include "sf_render.cuh"
 #include "sf_sample.cuh"
 
@@ -397,7 +397,10 @@ template <int MINB>
 __global__ void __launch_bounds__(128, MINB) k_raycast(DevMap m, FuseScratch f, sf_image vmap, sf_image nmap,
                                                        sf_image zmin, sf_image zmax, const Cam *cam,
                                                        const unsigned *rendered, sf_image fb_v,
-                                                       sf_image fb_n, const int *run_flag) {
+                                                       sf_image fb_n, const int *run_flag, FrameStatsArgs stats) {
+  // the frame's statistics are final when its last raycast starts
+  if (stats.sys && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0)
+    sys_stats(stats.sys, *stats.ctl, m, stats.flags, stats.out, stats.host_out, stats.host_ready, stats.seq);
   if (run_flag && *run_flag == 0) return;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -694,15 +697,17 @@ void launch_raycast(const DevMap &m, const FuseScratch &f, const sf_image &vmap,
                     const sf_image &zmin, const sf_image &zmax, const Cam *c,
                     const unsigned *rendered, const sf_image *fallback_v,
                     const sf_image *fallback_n, const int *run_flag, cudaStream_t s,
-                    const RaycastTune &tune) {
+                    const RaycastTune &tune, const FrameStatsArgs *stats) {
   const dim3 blk(tune.tx, tune.ty);
   const dim3 grd((vmap.cols + tune.tx - 1) / tune.tx, (vmap.rows + tune.ty - 1) / tune.ty);
   sf_image fv = fallback_v ? *fallback_v : sf_image{};
   sf_image fn = fallback_n ? *fallback_n : sf_image{};
+  FrameStatsArgs st = {};
+  if (stats) st = *stats;
   if (tune.minb == 6)
-    k_raycast<6><<<grd, blk, 0, s>>>(m, f, vmap, nmap, zmin, zmax, c, rendered, fv, fn, run_flag);
+    k_raycast<6><<<grd, blk, 0, s>>>(m, f, vmap, nmap, zmin, zmax, c, rendered, fv, fn, run_flag, st);
   else
-    k_raycast<8><<<grd, blk, 0, s>>>(m, f, vmap, nmap, zmin, zmax, c, rendered, fv, fn, run_flag);
+    k_raycast<8><<<grd, blk, 0, s>>>(m, f, vmap, nmap, zmin, zmax, c, rendered, fv, fn, run_flag, st);
   note_launch();
 }
 

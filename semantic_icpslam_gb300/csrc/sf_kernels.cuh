@@ -22,6 +22,10 @@ void launch_nmap(const sf_image &vmap, const sf_image &nmap, cudaStream_t s);
 void launch_vmap_depth(const sf_image &vmap, const sf_image &depth, const int *run_flag, cudaStream_t s);
 void launch_resize(const sf_image &vsrc, const sf_image &nsrc, const sf_image &vdst,
                    const sf_image &ndst, cudaStream_t s);
+// Two ResizeMap levels (0 -> 1 -> 2) in one launch, bit-identical to two
+// launch_resize calls.
+void launch_resize2(const sf_image &v0, const sf_image &n0, const sf_image &v1, const sf_image &n1,
+                    const sf_image &v2, const sf_image &n2, cudaStream_t s);
 
 // Levels 1..levels-1 of the pyramid from the filtered depths[0], and every
 // level's vertex and normal maps, in one launch (2 <= levels <= kMaxLevels;
@@ -121,14 +125,20 @@ void launch_rgb_cand(const sf_image &inext, const sf_image &dx, const sf_image &
 // enqueue it before each launch_icp_persistent.
 cudaError_t icp_persistent_reset(const IcpWorkspace &w, cudaStream_t s);
 
+struct FramePost;        // sf_frame.cuh
+struct FrameStatsArgs;   // sf_frame.cuh
+
 // Persistent form: every level and iteration of Tracker::ComputeSE3 in one
 // cooperative launch.  last_pose: device double[16]; result in *w.ctl.
 // skip_flag (device int, may be null): when nonzero the kernel does nothing.
 // rgb (may be null): per-level photometric inputs; then each iteration
-// adds RGBStep's rows (ComputeSE3 with icpOnly = false).
+// adds RGBStep's rows (ComputeSE3 with icpOnly = false).  post (may be
+// null): the frame loop's state update after ComputeSE3 (sys_post), run by
+// the kernel at its end, skipped or not.
 cudaError_t launch_icp_persistent(const IcpWorkspace &w, const IcpLevelArgs *levels, int nlevels,
                                   float thresh, const double *last_pose, const int *skip_flag,
-                                  uint32_t *flags, cudaStream_t s, const RgbLevelArgs *rgb = nullptr);
+                                  uint32_t *flags, cudaStream_t s, const RgbLevelArgs *rgb = nullptr,
+                                  const FramePost *post = nullptr);
 
 // -------------------------------------------------------------- fusion
 struct FuseScratch {
@@ -190,8 +200,19 @@ struct AllocTile {
   int x, y;
 };
 AllocTile alloc_tile(int tile);
+// The start of the next visibility pass run by the insert pass's launch
+// (k_alloc_insert): on when vis_zmin / vis_zmax are given; the visibility
+// pass is then launched with started = true.
+struct VisStartArgs {
+  int on;
+  const Cam *cam;
+  unsigned *rendered;
+  sf_image zmin, zmax;
+  int do_z;
+};
 void launch_alloc(const DevMap &m, const FuseScratch &f, const sf_image &depth, const Cam *c,
-                  const int *run_flag, uint32_t *flags, cudaStream_t s, bool begin = true, int tile = 0);
+                  const int *run_flag, uint32_t *flags, cudaStream_t s, bool begin = true, int tile = 0,
+                  const sf_image *vis_zmin = nullptr, const sf_image *vis_zmax = nullptr);
 // The probe pass alone (no epoch start, no insert pass), for the autotuner.
 void launch_alloc_probe(const DevMap &m, const FuseScratch &f, const sf_image &depth, const Cam *c,
                         const int *run_flag, uint32_t *flags, cudaStream_t s, int tile);
@@ -200,7 +221,7 @@ void launch_alloc_probe(const DevMap &m, const FuseScratch &f, const sf_image &d
 // Projection + fillBlocks (RenderScene.cu:54-190) for each visible block.
 void launch_visibility(const DevMap &m, const FuseScratch &f, const Cam *c, const sf_image *zmin,
                        const sf_image *zmax, const int *run_flag, uint32_t *flags,
-                       cudaStream_t s);
+                       cudaStream_t s, bool started = false);
 // createVoxels (+ analyzeSemantics when mask != null), FuseMap.cu:432-668.
 // MeshScene's marching cubes over the allocated blocks: up to max_tri
 // triangles (3 vertices, normals, colours each) appended at *count.
@@ -240,11 +261,13 @@ struct RaycastTune {
 };
 constexpr int kRaycastTunes = 6;
 RaycastTune raycast_tune(int i);  // candidate i < kRaycastTunes; 0 is the default
+// stats (may be null): the frame's statistics (sys_stats), written by the
+// kernel's first thread before anything else.
 void launch_raycast(const DevMap &m, const FuseScratch &f, const sf_image &vmap, const sf_image &nmap,
                     const sf_image &zmin, const sf_image &zmax, const Cam *c,
                     const unsigned *rendered, const sf_image *fallback_v,
                     const sf_image *fallback_n, const int *run_flag, cudaStream_t s,
-                    const RaycastTune &tune = RaycastTune());
+                    const RaycastTune &tune = RaycastTune(), const FrameStatsArgs *stats = nullptr);
 // RaycastAdjoint: gradients of launch_raycast's maps w.r.t. the pose (left
 // se(3) perturbation, 6 doubles into pose_out) and TSDF values (added into
 // grad_sdf, one float per voxel index; may be null).  pose_part holds

@@ -24,7 +24,7 @@
 
 #include <nvtx3/nvToolsExt.h>
 
-#include "sf_kernels.cuh"
+#include "sf_frame.cuh"
 
 namespace {
 // NVTX range over a host scope (a profiler shows which stage issued which
@@ -44,120 +44,14 @@ FuseScratch &map_scratch(sf_map *m);
 int map_ensure_scratch(sf_map *m, int pixels);
 const sf_map_config &map_cfg(sf_map *m);
 
-struct SysDev {
-  double last_pose[16];
-  int state;       // state of the next frame: 1 initialise, 0 track, -1 lost (relocalise); ICP runs only in 0
-  int run;         // this frame is tracked: mapping runs
-  int accepted;
-  int first;       // this frame was the initialisation frame
-  int prev_state;  // state this frame ran in (Tracker::lastState once the frame is done)
-  int missed;      // Tracker::noMissedFrames
-  int relocalised; // this frame was relocalised
-  int icp_ran;     // a ComputeSE3 ran this frame (its stats are reported)
-  Cam cam;         // camera of this frame's mapping pass
-};
-
-// Tracker::Track's state machine (Tracking.cc:65-119) after one frame's
-// attempt.  st: the state the frame ran in (1 initialise, 0 track, -1
-// relocalise); prev: the state the previous frame ran in; ok: the
-// attempt's result (ComputeSE3's acceptance in state 0, Relocalise's in
-// state -1).  Returns whether the frame is tracked (SwapFrame, then the
-// mapping stage), and sets the next frame's state and the missed-frame
-// count: ten misses in a row make the tracker lost, and the first frame
-// tracked after a relocalisation is not swapped (Track returns false).
-SF_HD int track_transition(int st, int prev, int ok, int &next, int &missed) {
-  if (st == 1) {
-    next = 0;
-    return 1;
-  }
-  if (st == 0) {
-    next = 0;
-    if (ok) {
-      missed = 0;
-      return prev != -1 ? 1 : 0;
-    }
-    if (++missed > 9) next = -1;
-    return 0;
-  }
-  next = ok ? 0 : -1;
-  return ok ? 1 : 0;
-}
-
 namespace {
 
-// Track() outcome (Tracking.cc:65-119) and the mapping camera
-// (Frame::GpuRotation / GpuInvRotation / GpuTranslation, Frame.cc:626-645);
-// when the frame is tracked, also the start of its allocation pass
-// (alloc_frame_begin), which would otherwise be a launch of its own.
-// A lost frame (state -1) relocalises only in the host-driven path of
-// sf_system_grab with candidates registered; here it stays lost.
-__global__ void k_sys_post(SysDev *s, const TrackCtl *ctl, Cam tmpl, FuseScratch f) {
-  const int st = s->state;
-  const int ok = st == 0 ? ctl->accepted : 0;
-  int next, missed = s->missed;
-  const int tracked = track_transition(st, s->prev_state, ok, next, missed);
-  s->first = st == 1 ? 1 : 0;
-  s->accepted = st == 1 ? 1 : ok;
-  if (st == 0 && tracked)
-    for (int k = 0; k < 16; ++k) s->last_pose[k] = ctl->next_pose[k];
-  s->prev_state = st;
-  s->state = next;
-  s->missed = missed;
-  s->relocalised = 0;
-  s->icp_ran = st == 0 ? 1 : 0;
-  s->run = tracked;
-  if (tracked) alloc_frame_begin(f);
-  const double *P = s->last_pose;
-  Cam c = tmpl;
-  c.R.rx = mk3((float)P[0], (float)P[1], (float)P[2]);
-  c.R.ry = mk3((float)P[4], (float)P[5], (float)P[6]);
-  c.R.rz = mk3((float)P[8], (float)P[9], (float)P[10]);
-  c.Rinv.rx = mk3((float)P[0], (float)P[4], (float)P[8]);
-  c.Rinv.ry = mk3((float)P[1], (float)P[5], (float)P[9]);
-  c.Rinv.rz = mk3((float)P[2], (float)P[6], (float)P[10]);
-  c.t = mk3((float)P[3], (float)P[7], (float)P[11]);
-  s->cam = c;
-}
+__global__ void k_sys_post(SysDev *s, const TrackCtl *ctl, Cam tmpl, FuseScratch f) { sys_post(s, *ctl, tmpl, f); }
 
-// `host_out` (pinned host memory, or null) receives a copy, and then
-// *host_ready the frame's sequence number, *seq + 1, which *seq keeps
-// (stores from the kernel cost the frame less than a copy node and an
-// event).  A reader waits for its own frame's number, so a flag left by an
-// earlier frame that nobody waited for cannot stand in for it.
 __global__ void k_sys_stats(const SysDev *s, const TrackCtl *ctl, DevMap m, const uint32_t *flags,
                             sf_frame_stats *out, sf_frame_stats *host_out, uint32_t *host_ready,
                             uint32_t *seq) {
-  sf_frame_stats st;
-  st.tracked = s->run;
-  st.accepted = s->accepted;
-  st.state = s->state;
-  st.missed = s->missed;
-  st.relocalised = s->relocalised;
-  if (!s->icp_ran) {  // no ComputeSE3 ran this frame
-    st.fail = 0; st.iterations = 0; st.icp_error = 0.f; st.icp_count = 0;
-    st.rgb_error = 0.f; st.rgb_count = 0;
-  } else {
-    st.fail = ctl->timeout ? 3 : ctl->stop;
-    st.iterations = ctl->iters_run;
-    st.icp_error = ctl->icpError;
-    st.icp_count = ctl->icpCount;
-    st.rgb_error = ctl->rgbError;
-    st.rgb_count = ctl->rgbCount;
-  }
-  st.visible = s->run ? *m.no_visible : 0u;
-  st.heap_counter = *m.heap_counter;
-  st.entry_ptr = *m.entry_ptr;
-  st.allocated = *m.alloc_count;
-  st.flags = *flags;
-  for (int k = 0; k < 16; ++k) st.pose[k] = s->last_pose[k];
-  *out = st;
-  if (host_out) {
-    const uint32_t q = *seq + 1u;
-    *seq = q;
-    *host_out = st;
-    __threadfence_system();  // the stats before the flag, as the host sees them
-    *(volatile uint32_t *)host_ready = q;
-  }
+  sys_stats(s, *ctl, m, flags, out, host_out, host_ready, seq);
 }
 
 template <class T>
@@ -455,9 +349,11 @@ int fuse_and_raytrace(sf_system *s, const Cam *cam, const int *run, int num_dete
   sf_image zmin = img(s->d_zmin, s->zc, s->zr, 4), zmax = img(s->d_zmax, s->zc, s->zr, 4);
   // the first pass of a device-driven frame starts its allocation epoch in
   // k_sys_post
-  launch_alloc(m, f, depth, cam, run, flags, st, /*begin=*/!first || run == nullptr, s->alloc_tile);
+  // the insert pass's launch also starts the visibility pass (counters,
+  // window box, cleared window cells and z-range)
+  launch_alloc(m, f, depth, cam, run, flags, st, /*begin=*/!first || run == nullptr, s->alloc_tile, &zmin, &zmax);
   if (first) mark(s, st, 3);
-  launch_visibility(m, f, cam, &zmin, &zmax, run, flags, st);
+  launch_visibility(m, f, cam, &zmin, &zmax, run, flags, st, /*started=*/true);
   if (first) {
     mark(s, st, 4);
     // the frame's colour and mask (already waited for by the intensity
@@ -478,13 +374,24 @@ int fuse_and_raytrace(sf_system *s, const Cam *cam, const int *run, int num_dete
     if (num_detection > 0) launch_unify_neighbor(m, f, run, st);  // FuseMap.cu:1141-1160
   }
   if (first) mark(s, st, 5);
-  if (last && !plain) {
-    if (enqueue_stats(s, st) != cudaSuccess) return SF_ERR_CUDA;
+  // a device-driven frame's stats, final here, are written by the first
+  // thread of its last raycast (k_sys_stats's work, without its launch)
+  FrameStatsArgs stats;
+  const bool with_stats = last && !plain;
+  if (with_stats) {
+    stats.sys = s->d_sys;
+    stats.ctl = ctx_icp(s->ctx).ctl;
+    stats.flags = ctx_flags(s->ctx);
+    stats.out = s->d_stats;
+    stats.host_out = s->capturing ? s->h_stats : nullptr;
+    stats.host_ready = s->h_ready;
+    stats.seq = s->d_seq;
     s->stats_taken = true;
   }
   sf_image fv = img(s->d_vmap[0], C, R, 16), fn = img(s->d_nmap[0], C, R, 16);
   launch_raycast(m, f, img(s->d_mv[0], C, R, 16), img(s->d_mn[0], C, R, 16), zmin, zmax, cam,
-                 f.counters + 3, &fv, &fn, run, st, s->rc_tune);
+                 f.counters + 3, &fv, &fn, run, st, s->rc_tune, with_stats ? &stats : nullptr);
+  if (with_stats && cudaGetLastError() != cudaSuccess) return SF_ERR_CUDA;
   if (first) mark(s, st, 6);
   return SF_OK;
 }
@@ -530,7 +437,14 @@ int enqueue_mapping(sf_system *s, const Cam *cam, const int *run, int num_detect
     }
   }
   if (e != SF_OK) return e;
-  for (int l = 1; l < s->L; ++l)
+  int l = 1;
+  if (s->L >= 3) {  // levels 1 and 2 in one launch
+    launch_resize2(img(s->d_mv[0], C, R, 16), img(s->d_mn[0], C, R, 16), img(s->d_mv[1], C >> 1, R >> 1, 16),
+                   img(s->d_mn[1], C >> 1, R >> 1, 16), img(s->d_mv[2], C >> 2, R >> 2, 16),
+                   img(s->d_mn[2], C >> 2, R >> 2, 16), st);
+    l = 3;
+  }
+  for (; l < s->L; ++l)
     launch_resize(img(s->d_mv[l - 1], C >> (l - 1), R >> (l - 1), 16),
                   img(s->d_mn[l - 1], C >> (l - 1), R >> (l - 1), 16),
                   img(s->d_mv[l], C >> l, R >> l, 16), img(s->d_mn[l], C >> l, R >> l, 16), st);
@@ -550,11 +464,16 @@ cudaError_t enqueue_device_frame(sf_system *s, int num_detection, cudaStream_t s
   if (e != cudaSuccess) return e;
   RgbLevelArgs rg[kMaxLevels];
   if (s->cfg.rgb_term) rgb_levels(s, rg);
+  // the tracker's state update after ComputeSE3 (Track) runs at the
+  // kernel's end
+  FramePost post;
+  post.sys = s->d_sys;
+  post.tmpl = s->tmpl;
+  post.f = map_scratch(s->map);
   e = launch_icp_persistent(w, lv, s->L, s->cfg.icp_thresh, dev_field<double>(s->d_sys, offsetof(SysDev, last_pose)),
                             dev_field<int>(s->d_sys, offsetof(SysDev, state)),
-                            ctx_flags(s->ctx), st, s->cfg.rgb_term ? rg : nullptr);
+                            ctx_flags(s->ctx), st, s->cfg.rgb_term ? rg : nullptr, &post);
   if (e != cudaSuccess) return e;
-  k_sys_post<<<1, 1, 0, st>>>(s->d_sys, w.ctl, s->tmpl, map_scratch(s->map)); note_launch();
   mark(s, st, 2);
   s->stats_taken = false;
   if (enqueue_mapping(s, dev_field<Cam>(s->d_sys, offsetof(SysDev, cam)),
