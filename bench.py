@@ -658,7 +658,8 @@ def time_reloc(sf, ctx, frames, n=256, reps=10, seed=5):
     return {"candidates": n, "pixels": int(COLS * ROWS), "ms_per_call": round(ms, 3),
             "candidate_pixels_per_s": round(n * COLS * ROWS / (ms * 1e-3), 1),
             "true_pose_rank": int((inl > inl[0]).sum()),
-            "note": "one launch per call; sigma 5 cm / 5 deg candidates around the tracked pose of frame %d" % k}
+            "note": "two launches per call (8 CTAs per candidate, then the fixed-order sum of their partials); "
+                    "sigma 5 cm / 5 deg candidates around the tracked pose of frame %d" % k}
 
 
 def load_traffic(kernel, first, count):

@@ -1836,9 +1836,11 @@ extern "C" unsigned sfo_mesh(sfo_map *m, unsigned max_tri, float *vert, float *n
 // RelocScoreBatch of the GB300 loop (no reference kernel; see
 // semantic_icpslam_gb300/csrc/reloc.cu): per candidate, every stride-th
 // vertex moved into the map by (R | t) and read with readSdfInterped
-// (RenderScene.cu:310-343).  The float sums follow the kernel's order:
-// 256 per-thread sums over samples i = t, t + 256, ..., a shuffle-down tree
-// per warp, then over the eight warp sums.  out: n records of
+// (RenderScene.cu:310-343).  The float sums follow the kernel's order: the
+// candidate's samples over 8 CTAs of 256 threads, thread t of CTA c
+// summing samples i = 256 c + t, + 2048, ...; a shuffle-down tree per warp,
+// then over the eight warp sums, gives CTA c's partial; the eight partials
+// are added with a shuffle-down tree (offsets 4, 2, 1).  out: n records of
 // {uint32 valid, uint32 inliers, float sum, float mean}.
 extern "C" void sfo_reloc_score(sfo_map *m, const float *vmap, int cols, int rows, int stride,
                                 const float *poses, int n, float inlier_sdf, void *out) {
@@ -1847,6 +1849,7 @@ extern "C" void sfo_reloc_score(sfo_map *m, const float *vmap, int cols, int row
   const int sc = (cols + stride - 1) / stride, sr = (rows + stride - 1) / stride;
   const int N = sc * sr;
   const float vsi = m->voxelSizeInv;
+  constexpr int kSplit = 8, kThreads = 256;
 #pragma omp parallel for schedule(dynamic, 1)
   for (int k = 0; k < n; ++k) {
     const float *P = poses + 12 * (size_t)k;
@@ -1855,54 +1858,67 @@ extern "C" void sfo_reloc_score(sfo_map *m, const float *vmap, int cols, int row
     R.ry = {P[3], P[4], P[5]};
     R.rz = {P[6], P[7], P[8]};
     const f3 t = {P[9], P[10], P[11]};
-    float tsum[256];
-    uint32_t tvalid[256], tinl[256];
-    for (int th = 0; th < 256; ++th) {
-      float sum = 0.f;
-      uint32_t valid = 0, inl = 0;
-      RayCache cache{{0, 0, 0}, -1, false};
-      for (int i = th; i < N; i += 256) {
-        const int y = (i / sc) * stride, x = (i % sc) * stride;
-        const float *v = vmap + 4 * ((size_t)y * cols + x);
-        if (std::isnan(v[0])) continue;
-        const f3 pt = (mul(R, f3{v[0], v[1], v[2]}) + t) * vsi;
-        bool ok;
-        const float sdf = read_sdf_interp(*m, pt, cache, ok);
-        if (!ok || std::isnan(sdf)) continue;
-        ++valid;
-        const float a = std::fabs(sdf);
-        if (a < inlier_sdf) ++inl;
-        sum += a;
-      }
-      tsum[th] = sum;
-      tvalid[th] = valid;
-      tinl[th] = inl;
-    }
-    float wsum[8];
-    uint32_t wvalid[8], winl[8];
-    for (int w = 0; w < 8; ++w) {
-      float *v = tsum + 32 * w;
-      uint32_t *a = tvalid + 32 * w, *b = tinl + 32 * w;
-      for (int off = 16; off > 0; off >>= 1)
-        for (int l = 0; l < off; ++l) {
-          v[l] = v[l] + v[l + off];
-          a[l] += a[l + off];
-          b[l] += b[l + off];
+    float psum[kSplit];
+    uint32_t pvalid[kSplit], pinl[kSplit];
+    for (int c = 0; c < kSplit; ++c) {
+      float tsum[kThreads];
+      uint32_t tvalid[kThreads], tinl[kThreads];
+      for (int th = 0; th < kThreads; ++th) {
+        float sum = 0.f;
+        uint32_t valid = 0, inl = 0;
+        RayCache cache{{0, 0, 0}, -1, false};
+        for (int i = c * kThreads + th; i < N; i += kThreads * kSplit) {
+          const int y = (i / sc) * stride, x = (i % sc) * stride;
+          const float *v = vmap + 4 * ((size_t)y * cols + x);
+          if (std::isnan(v[0])) continue;
+          const f3 pt = (mul(R, f3{v[0], v[1], v[2]}) + t) * vsi;
+          bool ok;
+          const float sdf = read_sdf_interp(*m, pt, cache, ok);
+          if (!ok || std::isnan(sdf)) continue;
+          ++valid;
+          const float a = std::fabs(sdf);
+          if (a < inlier_sdf) ++inl;
+          sum += a;
         }
-      wsum[w] = v[0];
-      wvalid[w] = a[0];
-      winl[w] = b[0];
-    }
-    for (int off = 4; off > 0; off >>= 1)
-      for (int l = 0; l < off; ++l) {
-        wsum[l] = wsum[l] + wsum[l + off];
-        wvalid[l] += wvalid[l + off];
-        winl[l] += winl[l + off];
+        tsum[th] = sum;
+        tvalid[th] = valid;
+        tinl[th] = inl;
       }
-    rec[k].valid = wvalid[0];
-    rec[k].inliers = winl[0];
-    rec[k].sum = wsum[0];
-    rec[k].mean = wvalid[0] ? wsum[0] / (float)wvalid[0] : std::numeric_limits<float>::quiet_NaN();
+      float wsum[8];
+      uint32_t wvalid[8], winl[8];
+      for (int w = 0; w < 8; ++w) {
+        float *v = tsum + 32 * w;
+        uint32_t *a = tvalid + 32 * w, *b = tinl + 32 * w;
+        for (int off = 16; off > 0; off >>= 1)
+          for (int l = 0; l < off; ++l) {
+            v[l] = v[l] + v[l + off];
+            a[l] += a[l + off];
+            b[l] += b[l + off];
+          }
+        wsum[w] = v[0];
+        wvalid[w] = a[0];
+        winl[w] = b[0];
+      }
+      for (int off = 4; off > 0; off >>= 1)
+        for (int l = 0; l < off; ++l) {
+          wsum[l] = wsum[l] + wsum[l + off];
+          wvalid[l] += wvalid[l + off];
+          winl[l] += winl[l + off];
+        }
+      psum[c] = wsum[0];
+      pvalid[c] = wvalid[0];
+      pinl[c] = winl[0];
+    }
+    for (int off = kSplit / 2; off > 0; off >>= 1)
+      for (int l = 0; l < off; ++l) {
+        psum[l] = psum[l] + psum[l + off];
+        pvalid[l] += pvalid[l + off];
+        pinl[l] += pinl[l + off];
+      }
+    rec[k].valid = pvalid[0];
+    rec[k].inliers = pinl[0];
+    rec[k].sum = psum[0];
+    rec[k].mean = pvalid[0] ? psum[0] / (float)pvalid[0] : std::numeric_limits<float>::quiet_NaN();
   }
 }
 

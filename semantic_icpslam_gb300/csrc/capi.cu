@@ -30,6 +30,7 @@ struct sf_context {
   TrackCtl *host_ctl = nullptr; // pinned
   float *reloc_poses = nullptr;           // device [reloc_cap][12]
   sf_reloc_score *reloc_scores = nullptr; // device [reloc_cap]
+  sf_reloc_score *reloc_part = nullptr;   // device [reloc_cap][reloc_score_parts()]
   int reloc_cap = 0;
   float *adj_part = nullptr;              // device [adj_cap][6] pose partials
   double *adj_pose = nullptr;             // device [6]
@@ -144,6 +145,7 @@ int sf_context_destroy(sf_context *ctx) {
   if (ctx->host_ctl) cudaFreeHost(ctx->host_ctl);
   cudaFree(ctx->reloc_poses);
   cudaFree(ctx->reloc_scores);
+  cudaFree(ctx->reloc_part);
   cudaFree(ctx->adj_part);
   cudaFree(ctx->adj_pose);
   cudaFree(ctx->rdepth);
@@ -809,11 +811,14 @@ int sf_RelocScoreBatch(sf_context *ctx, sf_map *m, sf_image vmap, int stride, co
     SF_CHECK(cudaStreamSynchronize(ctx->stream));
     cudaFree(ctx->reloc_poses);
     cudaFree(ctx->reloc_scores);
+    cudaFree(ctx->reloc_part);
     ctx->reloc_poses = nullptr;
     ctx->reloc_scores = nullptr;
+    ctx->reloc_part = nullptr;
     ctx->reloc_cap = 0;
     SF_CHECK(cudaMalloc(&ctx->reloc_poses, sizeof(float) * 12 * (size_t)n));
     SF_CHECK(cudaMalloc(&ctx->reloc_scores, sizeof(sf_reloc_score) * (size_t)n));
+    SF_CHECK(cudaMalloc(&ctx->reloc_part, sizeof(sf_reloc_score) * (size_t)n * reloc_score_parts()));
     ctx->reloc_cap = n;
   }
   // Frame::GpuRotation / GpuTranslation (Core/Frame.cc:626-645) per candidate
@@ -826,7 +831,8 @@ int sf_RelocScoreBatch(sf_context *ctx, sf_map *m, sf_image vmap, int stride, co
   }
   SF_CHECK(cudaMemcpyAsync(ctx->reloc_poses, hp.data(), sizeof(float) * hp.size(), cudaMemcpyHostToDevice,
                            ctx->stream));
-  launch_reloc_score(m->d, vmap, stride, ctx->reloc_poses, n, inlier_sdf, ctx->reloc_scores, ctx->stream);
+  launch_reloc_score(m->d, vmap, stride, ctx->reloc_poses, n, inlier_sdf, ctx->reloc_part, ctx->reloc_scores,
+                     ctx->stream);
   SF_CHECK(cudaGetLastError());
   SF_CHECK(cudaMemcpyAsync(scores_out, ctx->reloc_scores, sizeof(sf_reloc_score) * (size_t)n,
                            cudaMemcpyDeviceToHost, ctx->stream));

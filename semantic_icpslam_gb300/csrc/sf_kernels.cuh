@@ -281,9 +281,12 @@ void launch_raycast_adjoint(const DevMap &m, const FuseScratch &f, const sf_imag
 void launch_window_build(const DevMap &m, const FuseScratch &f, const Cam *c, cudaStream_t s);
 
 // ------------------------------------------------------ relocalisation
-// n candidate poses (float rows R | t, 12 per pose) scored in one launch.
+// n candidate poses (float rows R | t, 12 per pose) scored, each candidate
+// over reloc_score_parts() CTAs whose partials go to part
+// [n][reloc_score_parts()], then added in a fixed order into out.
+int reloc_score_parts();
 void launch_reloc_score(const DevMap &m, const sf_image &vmap, int stride, const float *poses, int n,
-                        float inlier_sdf, sf_reloc_score *out, cudaStream_t s);
+                        float inlier_sdf, sf_reloc_score *part, sf_reloc_score *out, cudaStream_t s);
 
 // Tracker::ValidatePose (Tracking.cc:750-790) batched over n candidate
 // poses (csrc/validate.cu).  The candidates' model maps and z-range images
