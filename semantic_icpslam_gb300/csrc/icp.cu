@@ -10,9 +10,11 @@
 // iteration.  Per iteration each CTA reduces its pixels' 29 products
 // (FP32 per pixel, compensated FP32 warp and block trees), adds the block
 // totals into exact fixed-point accumulators with fire-and-forget atomics
-// and crosses a bounded grid barrier; then every CTA reads the same 29
-// totals and runs the same 6x6 solve and SE(3) update, so all CTAs hold the
-// same pose without a second barrier.  Accumulators rotate over three sets.
+// and crosses a bounded grid barrier.  One CTA runs the FP64 6x6 solve and
+// SE(3) update and publishes the pose before the next barrier, while the
+// pixel CTAs accumulate the next iteration's rows on a float prediction of
+// that pose and keep them only when it matches the published pose bit for
+// bit (k_icp_persistent below).  Accumulators rotate over three sets.
 #include <mutex>
 
 #include "sf_frame.cuh"
