@@ -95,6 +95,35 @@ def _compare(sf, ctx, seq, a, b):
         b.autotune(reps=0)
 
 
+def test_every_raycast_shape_same_maps(lib):
+    """Each raycast launch shape gives the default shape's poses,
+    statistics and model maps, bit for bit."""
+    sf, ctx = lib
+    seq = sequence(C1["cols"], C1["rows"], C1["K"], 4, trajectory=1, dropout=0.02)
+    cfg = sf.system_config(cols=C1["cols"], rows=C1["rows"], K=C1["K"], use_graph=1, **MAP_C1)
+    import ctypes as C
+
+    def run(shape):
+        s = sf.System(ctx, cfg, init_pose=seq[0][3])
+        try:
+            if shape is not None:
+                sf.call("sf_system_set_tune", s.h, C.byref(sf._lib.FrameTune(shape, 8, 0)))
+            out = []
+            for d, rgb, _, _ in seq:
+                st = s.grab(d, rgb)
+                out.append((np.array(st.pose[:]), st.iterations, st.icp_count, st.visible, _model(ctx, s)))
+            return out
+        finally:
+            s.close()
+
+    ref = run(None)
+    for shape in range(6):
+        for i, (x, y) in enumerate(zip(ref, run(shape))):
+            assert np.array_equal(x[0], y[0]) and x[1:4] == y[1:4], (shape, i)
+            for u, v in zip(x[4], y[4]):
+                np.testing.assert_array_equal(u, v, err_msg="shape %d frame %d" % (shape, i))
+
+
 def test_tune_cache_per_configuration(lib, tmp_path):
     """The first system of a configuration times and caches; the next takes
     the cached shapes without timing."""
