@@ -42,7 +42,7 @@ namespace {
 constexpr int kThreads = 512;               // plain-form kernels
 constexpr int kPThreads = SF_ICP_PTHREADS;  // persistent kernel
 constexpr int kProfIters = 64;
-constexpr int kProfSlots = 16;  // per iteration: 0-5 phases, 6 globaltimer, 8-13 solve steps
+constexpr int kProfSlots = 16;  // per iteration (prof_mark): phases, global timer, prediction, solve steps
 constexpr int kWarps = kThreads / 32;
 constexpr int kPWarps = kPThreads / 32;
 

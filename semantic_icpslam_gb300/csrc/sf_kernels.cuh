@@ -72,7 +72,7 @@ struct IcpWorkspace {
   int max_blocks = 0;          // co-resident CTAs of the persistent kernel
   int max_blocks_rgb = 0;      // the same for the photometric form
   int threads = 0;
-  unsigned long long *prof = nullptr;  // [64][8] phase clocks of CTA 0
+  unsigned long long *prof = nullptr;  // [64][16] per-iteration phase clocks (sf_icp_profile)
   int profile = 0;                     // record phase clocks when set
   // grid barrier bounds of the persistent kernel (sf_icp_barrier_limits)
   unsigned barrier_poll_limit = 1u << 22;
