@@ -2,12 +2,12 @@
 //
 // Every ICP iteration ends in the FP64 6x6 solve and SE(3) update
 // (sf_icp_solve.cuh), a dependent chain of FP64 instructions of about
-// 3.5 us on GB300 during which the pixel warps would idle: the next
+// 3.3 us on GB300 during which the pixel warps would idle: the next
 // iteration's rows need the pose the solve produces, in float (the
 // reference's GpuRotation / GpuTranslation, Core/Frame.cc:626-645).
 // This warp predicts that float pose from the same 29 sums with FP32 and
-// float-float (hi + lo) arithmetic only, off the FP64 pipe, in well under
-// a microsecond, so that the pixel warps can accumulate the next
+// float-float (hi + lo) arithmetic only, off the FP64 pipe, in about a
+// third of the solve's time, so that the pixel warps can accumulate the next
 // iteration's rows while the FP64 solve runs.  The FP64 result stays the
 // only result: once it is known, the prediction is compared with it bit
 // for bit (all twelve floats), and a prediction that differs in any bit,
@@ -118,8 +118,7 @@ __device__ __forceinline__ int sum_index(int i, int j) { return 7 * i - i * (i -
 // and the solution x of A x = b.  Run by one whole warp; returns
 // (warp-uniform) whether a prediction was made, and writes out (lanes
 // 0..11) only then.  Every step is spread over the lanes so that the
-// warp's dependent chain stays short (about a microsecond's fraction of
-// the FP64 solve it races):
+// warp's dependent chain stays short against the FP64 solve it races:
 //  - elimination without pivoting (J^T J is symmetric positive definite;
 //    a pivot that is not positive gives no prediction), lane c < 13 holding
 //    column c of [A | b | I], the six steps unrolled, each one shuffle of
